@@ -1,0 +1,319 @@
+"""Benchmark of the fit path on the composite 1-D workload (2,000,000 events).
+
+Workload: AddPdf(fsig; ConvolutionPdf(ExpPdf(alpha), GaussianPdf(mu, sigma)), flat PolynomialPdf) on
+x in [-5, 10], tau = 1.5, mu = 0, sigma = 0.3, background fraction 0.3, 10,000-bin numeric
+normalisation, 2e6 seeded synthetic events (accept-reject on the model density).
+
+A step is one FCN call of MIGRAD on the whole dataset: the NLL and its analytic gradient with
+respect to the four floated parameters, i.e. 2e6 event-NLL evaluations.  `value` is event-NLL
+evaluations per second with the events resident in HBM; the L2 cache (129 MB) is flushed with a
+256 MB write before every timed step because the event columns (16 MB) would otherwise stay in L2.
+`e2e` repeats the step through the C ABI with host buffers: the FP64 events are copied from pinned
+host memory and converted on the device every step, and the NLL/gradient are read back.
+
+--impl reference times the reference algorithm on the host cores instead: the FP64 restatement of
+GooFit's OMP path (brute-force convolution per event, numeric normalisation), on a bounded sample.
+
+--gpus N (under torchrun) runs N independent replicas (the fit path does not shard in this
+configuration); value is the sum over ranks of events / max step time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "MIGRAD fit wall-time & event-NLL evals/s: mixed-prec vs FP64 on GB300 at 1e-6 rel NLL"
+N_EVENTS = 2_000_000
+WORKLOAD = "c2: AddPdf(0.7 Conv(Exp tau=1.5, Gauss mu=0 sigma=0.3) + 0.3 flat Poly), x in [-5,10], 2e6 events"
+
+
+def load_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def barrier_max(value: float, world: int, device: str | None) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device or "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args) -> dict:
+    """The reference algorithm (oracle port, brute-force convolution) on all host cores."""
+    import numpy as np
+
+    from goofit_gb300 import workloads as W
+    from oracle import oracle as O
+
+    sample = args.ref_sample
+    wl = W.make_c2(sample, seed=2)
+    nodes, params, obs = wl.pdf._flatten()
+    olist = [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs]
+    pv = np.array([v.value for v in params])
+    data = wl.data.to_numpy()
+    for _ in range(args.warmup):
+        O.nll(nodes, olist, pv, data, brute_force=True)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.nll(nodes, olist, pv, data, brute_force=True)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    value = sample / (ms / 1e3)
+    cores = O.num_threads()
+    return {
+        "metric": METRIC, "value": value, "unit": "event-NLL evals/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_events": sample, "l2": "n/a (host)"},
+        "cpu_baseline": {"value": value, "unit": "event-NLL evals/s", "cores": cores, "kind": "port",
+                         "sample": f"{sample} events of the 2e6-event workload, one NLL per step "
+                                   "(FP64 restatement of the reference OMP path, brute-force convolution)"},
+        "e2e": {"value": value, "unit": "event-NLL evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def cpu_baseline(sample: int, reps: int = 2) -> dict:
+    import numpy as np
+
+    from goofit_gb300 import workloads as W
+    from oracle import oracle as O
+    wl = W.make_c2(sample, seed=2)
+    nodes, params, obs = wl.pdf._flatten()
+    olist = [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs]
+    pv = np.array([v.value for v in params])
+    data = wl.data.to_numpy()
+    O.nll(nodes, olist, pv, data, brute_force=True)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.nll(nodes, olist, pv, data, brute_force=True)
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": sample / dt, "unit": "event-NLL evals/s", "cores": O.num_threads(), "kind": "port",
+            "sample": f"{sample} events, {reps} NLL evaluations (FP64 restatement of the reference OMP path, "
+                      "brute-force convolution per event)"}
+
+
+def run_engine(args) -> dict | None:
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import goofit_gb300 as gf
+    from goofit_gb300 import _abi as A
+    from goofit_gb300 import workloads as W
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(dev))
+
+    wl = W.make_c2(N_EVENTS, seed=2 + rank)
+    nodes, params, obs = wl.pdf._flatten()
+    olist = [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs]
+    mask = [0 if v.fixed else 1 for v in params]
+    pv = np.array([v.value for v in params])
+    eng = gf.Engine(args.precision, device=local)
+    eng.set_tree(nodes, olist, len(params), mask)
+    host = torch.empty((1, N_EVENTS), dtype=torch.float64, pin_memory=True)
+    host.numpy()[:] = wl.data.to_numpy()
+    hp = C.cast(host.data_ptr(), C.POINTER(C.c_double))
+    L = A.lib()
+    A.check(L.gf_upload_events(eng._h, 0, hp, N_EVENTS), eng._h)
+    eng._n_events[0] = N_EVENTS
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        return eng.nll_grad(pv)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    dev_ms, evt_ms = [], []
+    with ClockSampler(local) as clk:
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            step()
+            a, b = eng.last_timing()
+            dev_ms.append(a)
+            evt_ms.append(b)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    ms = float(np.mean(dev_ms))
+    ms = barrier_max(ms, world, dev)
+    value = world * N_EVENTS / (ms / 1e3)
+
+    # end to end through the C ABI with host buffers
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        A.check(L.gf_upload_events(eng._h, 0, hp, N_EVENTS), eng._h)
+        eng.nll_grad(pv)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2e_ms.append(1e3 * dt)
+    e2e = barrier_max(float(np.mean(e2e_ms)), world, dev)
+
+    # roofline of the event kernel: algorithmic bytes = the int32 bin offset of every event
+    # (the flat polynomial needs no x; the convolution needs x only through its bin offset)
+    bytes_per_event = 4
+    evt = float(np.mean(evt_ms))
+    peaks = load_peaks()
+    achieved = N_EVENTS * bytes_per_event / (evt / 1e3) / 1e9
+
+    # MIGRAD fits on the same data: mixed + analytic gradient vs FP64 + numerical gradient
+    fits = {}
+    if rank == 0 and not args.no_fit:
+        for label, prec, grad in (("mixed_analytic", "mixed", "analytic"), ("fp64_numerical", "fp64", "numerical")):
+            wl.reset()
+            fm = gf.FitManager(wl.pdf, precision=prec, gradient=grad, tolerance=0.1)
+            fm.verbosity = 0
+            r = fm.fit()
+            fits[label] = {"wall_s": fm.wall_seconds, "nfcn": r.nfcn, "valid": r.valid, "fmin": r.fmin,
+                           "values": {v.name: v.value for v in params if not v.fixed},
+                           "errors": {v.name: v.error for v in params if not v.fixed}}
+        fits["speedup_wall"] = fits["fp64_numerical"]["wall_s"] / fits["mixed_analytic"]["wall_s"]
+        dn = fits["mixed_analytic"]["fmin"] - fits["fp64_numerical"]["fmin"]
+        fits["rel_dnll"] = abs(dn) / abs(fits["fp64_numerical"]["fmin"])
+
+    if rank != 0:
+        return None
+    cpu = cpu_baseline(args.cpu_sample) if not args.no_cpu else None
+    launches = eng.launches_per_eval(True)
+    line = {
+        "metric": METRIC, "value": value, "unit": "event-NLL evals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-events/f64-reductions" if args.precision == "mixed" else "f64",
+        "data": "synthetic (seeded accept-reject on the model density)",
+        "config": {"workload": WORKLOAD, "events": N_EVENTS, "precision": args.precision,
+                   "step": "one FCN call: NLL + analytic gradient (4 floated parameters)",
+                   "l2": "flushed (256 MB write) before every timed step",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": world * N_EVENTS / (e2e / 1e3), "unit": "event-NLL evals/s",
+                "h2d_bytes_per_step": N_EVENTS * 8 + len(params) * 8, "d2h_bytes_per_step": (2 + eng.n_grad) * 8,
+                "ms_per_step": e2e},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": "gf_evt_g",
+                     "kernel_ms": evt, "bytes_per_event": bytes_per_event, "peak_source": peaks["src"]},
+        "cpu_baseline": cpu,
+        "gpu_launches": launches * args.steps,
+        "clocks": clk.summary(),
+        "wall_ms_per_step": 1e3 * wall / args.steps,
+        "fit": fits,
+    }
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cpu-sample", type=int, default=200_000)
+    ap.add_argument("--ref-sample", type=int, default=100_000)
+    ap.add_argument("--no-fit", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args)))
+        return
+    line = run_engine(args)
+    if line is not None:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,827 @@
+"""GooFit-compatible host API over the GB300 engine.
+
+Mirrors the reference's operator surface (include/goofit/Variable.h,
+DataSet.h, UnbinnedDataSet.h, PdfBase.h, PDFs/GooPdf.h, PDFs/basic/*.h,
+PDFs/combine/*.h, fitting/FitManagerMinuit2.h) and its Python bindings
+(python/goofit/*.cpp): same class names, constructor argument orders and
+method names.  A PDF object describes one node; the tree under a root PDF is
+flattened depth-first (as PdfBase::populateArrays does,
+src/PDFs/PdfBase.cu:268-311) into the engine's node list, and every
+evaluation runs on the GPU through libgfengine.so.
+"""
+from __future__ import annotations
+
+import enum
+import math
+import time
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import _abi as A
+from .engine import Engine, FitResult
+
+_DEFAULT_PRECISION = "mixed"
+
+
+def set_precision(p: str) -> None:
+    """Arithmetic of new engines: 'mixed' (FP32 events, FP64 reductions) or 'fp64'."""
+    global _DEFAULT_PRECISION
+    if p not in ("mixed", "fp64"):
+        raise ValueError(p)
+    _DEFAULT_PRECISION = p
+
+
+def get_precision() -> str:
+    return _DEFAULT_PRECISION
+
+
+class GeneralError(RuntimeError):
+    """GooFit::GeneralError (include/goofit/Error.h:9-19)."""
+
+
+class OutOfRange(GeneralError):
+    """GooFit::OutOfRange raised by DataSet::checkAllVars (src/goofit/DataSet.cpp:72-77)."""
+
+    def __init__(self, name, value, lo, hi):
+        super().__init__(f"{name} value {value} outside of range {lo} to {hi}")
+
+
+class EvalFunc(enum.IntEnum):
+    """include/goofit/FitControl.h:11"""
+    Eval = 0
+    NLL = 1
+    Prob = 2
+    BinAvg = 3
+    BinWithError = 4
+    Chisq = 5
+
+
+# ---------------------------------------------------------------- variables
+class Indexable:
+    """Named quantity with value and limits (include/goofit/Variable.h:22-106).
+
+    Python objects are references, so copies alias as the reference's
+    shared_ptr members do."""
+
+    def __init__(self, name: str, value: float = 0.0, lowerlimit: float = 0.0, upperlimit: float = 0.0):
+        self.name = name
+        self._value = float(value)
+        self.lowerlimit = float(lowerlimit)
+        self.upperlimit = float(upperlimit)
+        self.index = -1
+
+    @property
+    def value(self) -> float:
+        return self._value
+
+    @value.setter
+    def value(self, v: float) -> None:
+        self._value = float(v)
+
+    def getName(self) -> str:
+        return self.name
+
+    def getValue(self) -> float:
+        return self._value
+
+    def setValue(self, v: float) -> None:
+        self._value = float(v)
+
+    def getLowerLimit(self) -> float:
+        return self.lowerlimit
+
+    def getUpperLimit(self) -> float:
+        return self.upperlimit
+
+    def setLowerLimit(self, v: float) -> None:
+        self.lowerlimit = float(v)
+
+    def setUpperLimit(self, v: float) -> None:
+        self.upperlimit = float(v)
+
+    def getIndex(self) -> int:
+        return self.index
+
+    def setIndex(self, i: int) -> None:
+        self.index = i
+
+    def __float__(self) -> float:
+        return self._value
+
+    def __bool__(self) -> bool:
+        # in range check (Variable.h:101-104)
+        return self.upperlimit == self.lowerlimit or (self.lowerlimit <= self._value <= self.upperlimit)
+
+    def __repr__(self) -> str:
+        return f"{type(self).__name__}({self.name!r}, {self._value})"
+
+
+class Observable(Indexable):
+    """include/goofit/Variable.h:109-140 (numbins defaults to 100)."""
+
+    def __init__(self, name: str, lowerlimit: float, upperlimit: float):
+        super().__init__(name, 0.0, lowerlimit, upperlimit)
+        self.numbins = 100
+        self.is_event_number = False
+
+    def setNumBins(self, n: int) -> None:
+        self.numbins = int(n)
+
+    def getNumBins(self) -> int:
+        return self.numbins
+
+    def getBinSize(self) -> float:
+        return (self.upperlimit - self.lowerlimit) / self.numbins
+
+    def isEventNumber(self) -> bool:
+        return self.is_event_number
+
+
+class EventNumber(Observable):
+    """include/goofit/Variable.h:246-263."""
+    maxint = float(1 << 53)
+
+    def __init__(self, name: str, lowerlimit: float = 0.0, upperlimit: float = maxint):
+        super().__init__(name, lowerlimit, upperlimit)
+        self.is_event_number = True
+
+
+class Variable(Indexable):
+    """include/goofit/Variable.h:143-241; the constructors keep the reference's meanings:
+
+    Variable(n, v)                 constant (fixed)
+    Variable(n, v, err)            fixed, no limits (the reference marks it fixed)
+    Variable(n, v, lo, hi)         free, limited, error 0.1 (hi - lo)
+    Variable(n, v, err, lo, hi[, fixed])
+    """
+
+    def __init__(self, name: str, value: float, *args):
+        if len(args) == 0:
+            super().__init__(name, value, value + 0.01, value - 0.01)
+            self.error, self.fixed = 0.002, True
+        elif len(args) == 1:
+            super().__init__(name, value, 0.0, 0.0)
+            self.error, self.fixed = float(args[0]), True
+        elif len(args) == 2:
+            super().__init__(name, value, args[0], args[1])
+            self.error, self.fixed = 0.1 * (args[1] - args[0]), False
+        elif len(args) in (3, 4):
+            super().__init__(name, value, args[1], args[2])
+            self.error = float(args[0])
+            self.fixed = bool(args[3]) if len(args) == 4 else False
+        else:
+            raise TypeError("Variable(name, value[, err][, lo, hi][, fixed])")
+        self._blind = 0.0
+        self.fitter_index = -1
+        self.changed = True
+
+    def getError(self) -> float:
+        return self.error
+
+    def setError(self, e: float) -> None:
+        self.error = float(e)
+
+    def IsFixed(self) -> bool:
+        return self.fixed
+
+    def setFixed(self, f: bool) -> None:
+        self.fixed = bool(f)
+
+    def setBlind(self, b: float) -> None:
+        self._blind = float(b)
+
+    def getFitterIndex(self) -> int:
+        return self.fitter_index
+
+    def __repr__(self) -> str:
+        s = f"{self.name}: {self._value} +/- {self.error}"
+        if not self.fixed:
+            s += f" [{self.lowerlimit}, {self.upperlimit}]"
+        return s
+
+
+# ---------------------------------------------------------------- datasets
+class DataSet:
+    """include/goofit/DataSet.h"""
+
+    def __init__(self, observables, name: str = ""):
+        if isinstance(observables, Observable):
+            observables = [observables]
+        self.observables: list[Observable] = list(observables)
+        self.name = name or ", ".join(o.name for o in self.observables)
+        self.numEventsAdded = 0
+
+    def getObservables(self) -> list[Observable]:
+        return self.observables
+
+    def numVariables(self) -> int:
+        return len(self.observables)
+
+    def getNumEvents(self) -> int:
+        return self.numEventsAdded
+
+    def getName(self) -> str:
+        return self.name
+
+    def indexOfVariable(self, var: Observable) -> int:
+        for i, o in enumerate(self.observables):
+            if o is var:
+                return i
+        raise GeneralError("Invalid variable access into dataset!")
+
+    def checkAllVars(self) -> None:
+        for o in self.observables:
+            if not o:
+                raise OutOfRange(o.name, o.value, o.lowerlimit, o.upperlimit)
+
+
+class UnbinnedDataSet(DataSet):
+    """include/goofit/UnbinnedDataSet.h; columns kept as float64 arrays."""
+
+    def __init__(self, observables, name: str = ""):
+        super().__init__(observables, name)
+        self._chunks: list[np.ndarray] = []
+        self._pending: list[list[float]] = []
+        self._cache: np.ndarray | None = None
+        self.version = 0
+
+    def _touch(self) -> None:
+        self._cache = None
+        self.version += 1
+
+    def addEvent(self, *values) -> None:
+        if values:
+            if len(values) != len(self.observables):
+                raise GeneralError(f"You must pass the correct number of values ({len(self.observables)}) to addEvent")
+            for o, v in zip(self.observables, values):
+                o.value = v
+        self.checkAllVars()
+        self._pending.append([o.value for o in self.observables])
+        self.numEventsAdded += 1
+        self._touch()
+
+    def _flush(self) -> None:
+        if self._pending:
+            self._chunks.append(np.asarray(self._pending, dtype=np.float64).T.reshape(len(self.observables), -1))
+            self._pending = []
+
+    def to_numpy(self) -> np.ndarray:
+        """(n_observables, n_events) array."""
+        if self._cache is None:
+            self._flush()
+            if self._chunks:
+                self._cache = np.concatenate(self._chunks, axis=1) if len(self._chunks) > 1 else self._chunks[0]
+                self._chunks = [self._cache]
+            else:
+                self._cache = np.zeros((len(self.observables), 0))
+        return self._cache
+
+    to_matrix = to_numpy
+
+    def from_numpy(self, mat, filter: bool = False) -> None:
+        """UnbinnedDataSet::from_matrix (include/goofit/UnbinnedDataSet.h:50-71)."""
+        m = np.asarray(mat, dtype=np.float64)
+        if m.ndim == 1:
+            m = m.reshape(1, -1)
+        nobs = len(self.observables)
+        if m.shape[0] not in (nobs, nobs - 1):
+            raise GeneralError(f"The wrong number of rows, expected {nobs}, but matrix had {m.shape[0]}")
+        if m.shape[0] == nobs - 1:
+            idx = np.arange(self.numEventsAdded, self.numEventsAdded + m.shape[1], dtype=np.float64)
+            m = np.vstack([m, idx])
+        ok = np.ones(m.shape[1], dtype=bool)
+        for i, o in enumerate(self.observables):
+            if o.upperlimit != o.lowerlimit:
+                ok &= (m[i] >= o.lowerlimit) & (m[i] <= o.upperlimit)
+        if filter:
+            m = m[:, ok]
+        elif not ok.all():
+            bad = int(np.argmin(ok))
+            o = next(o for i, o in enumerate(self.observables)
+                     if o.upperlimit != o.lowerlimit and not (o.lowerlimit <= m[i, bad] <= o.upperlimit))
+            raise OutOfRange(o.name, float(m[self.observables.index(o), bad]), o.lowerlimit, o.upperlimit)
+        self._flush()
+        self._chunks.append(np.ascontiguousarray(m))
+        self.numEventsAdded += m.shape[1]
+        self._touch()
+
+    from_matrix = from_numpy
+
+    def getValue(self, var: Observable, idx: int) -> float:
+        if idx >= self.getNumEvents():
+            raise GeneralError(f"UnbinnedDataSet: Attempted to find {var.name} in event {idx} when only "
+                               f"{self.getNumEvents()} events exits")
+        return float(self.to_numpy()[self.indexOfVariable(var), idx])
+
+    def __getitem__(self, key):
+        return self.to_numpy()[key]
+
+    def loadEvent(self, idx: int) -> None:
+        col = self.to_numpy()[:, idx]
+        for o, v in zip(self.observables, col):
+            o.value = v
+
+    def clear(self) -> None:
+        self._chunks, self._pending, self.numEventsAdded = [], [], 0
+        self._touch()
+
+    def column(self, var: Observable) -> np.ndarray:
+        return self.to_numpy()[self.indexOfVariable(var)]
+
+    def fillWithGrid(self) -> None:
+        """UnbinnedDataSet::fillWithGrid (src/goofit/UnbinnedDataSet.cpp:67-105): first observable fastest."""
+        if self.getNumEvents():
+            raise GeneralError("The dataset must be empty to fill with grid!")
+        axes = []
+        for o in self.observables:
+            if o.is_event_number:
+                axes.append(None)
+            else:
+                step = (o.upperlimit - o.lowerlimit) / o.numbins
+                axes.append(o.lowerlimit + (np.arange(o.numbins) + 0.5) * step)
+        sizes = [len(a) for a in axes if a is not None]
+        total = int(np.prod(sizes)) if sizes else 1
+        cols = []
+        stride = 1
+        for a in axes:
+            if a is None:
+                cols.append(None)
+                continue
+            cols.append(np.tile(np.repeat(a, stride), total // (stride * len(a))))
+            stride *= len(a)
+        m = np.zeros((len(self.observables), total))
+        for i, (o, c) in enumerate(zip(self.observables, cols)):
+            m[i] = np.arange(total, dtype=np.float64) + o.value if c is None else c
+        self._flush()
+        self._chunks.append(m)
+        self.numEventsAdded += total
+        self._touch()
+
+
+# ---------------------------------------------------------------- PDFs
+def _unique(seq: Iterable) -> list:
+    out, seen = [], set()
+    for x in seq:
+        if id(x) not in seen:
+            seen.add(id(x))
+            out.append(x)
+    return out
+
+
+class PdfBase:
+    """include/goofit/PdfBase.h: registration lists, data, normalisation, fit."""
+
+    op: int = 0
+
+    def __init__(self, pdf_name: str, name: str, *registered):
+        self.pdf_name = pdf_name
+        self.name = name
+        self.parametersList: list[Variable] = []
+        self.constantsList: list[float] = []
+        self.observablesList: list[Observable] = []
+        self.components: list[PdfBase] = []
+        self.integrationBins = 0
+        self.flags = 0
+        self.data = None
+        self._engines: dict = {}
+        for r in registered:
+            if isinstance(r, Observable):
+                self.registerObservable(r)
+            elif isinstance(r, Variable):
+                self.registerParameter(r)
+            else:
+                raise TypeError(r)
+
+    # registration (src/goofit/PdfBase.cpp)
+    def registerParameter(self, v: Variable) -> None:
+        self.parametersList.append(v)
+
+    def registerConstant(self, c: float) -> None:
+        self.constantsList.append(float(c))
+
+    def registerObservable(self, o: Observable) -> None:
+        if all(o is not q for q in self.observablesList):
+            self.observablesList.append(o)
+
+    def getName(self) -> str:
+        return self.name
+
+    def getPdfName(self) -> str:
+        return self.pdf_name
+
+    def getParameters(self) -> list[Variable]:
+        ret = list(self.parametersList)
+        for c in self.components:
+            ret += c.getParameters()
+        return _unique(ret)
+
+    def getObservables(self) -> list[Observable]:
+        ret = list(self.observablesList)
+        for c in self.components:
+            ret += c.getObservables()
+        return _unique(ret)
+
+    def getComponents(self) -> list["PdfBase"]:
+        return self.components
+
+    def getParameterByName(self, n: str):
+        for p in self.getParameters():
+            if p.name == n:
+                return p
+        return None
+
+    def setIntegrationFineness(self, i: int) -> None:
+        self.integrationBins = int(i)
+
+    def setCommonNorm(self, v: bool = True) -> None:
+        self.flags = (self.flags | A.GF_FLAG_COMMON_NORM) if v else (self.flags & ~A.GF_FLAG_COMMON_NORM)
+
+    def setSeparateNorm(self, v: bool = True) -> None:
+        self.flags = (self.flags | A.GF_FLAG_SEPARATE_NORM) if v else (self.flags & ~A.GF_FLAG_SEPARATE_NORM)
+
+    def getCommonNorm(self) -> bool:
+        return bool(self.flags & A.GF_FLAG_COMMON_NORM)
+
+    def getSeparateNorm(self) -> bool:
+        return bool(self.flags & A.GF_FLAG_SEPARATE_NORM)
+
+    def setData(self, data) -> None:
+        self.data = data
+
+    def getData(self):
+        return self.data
+
+    def copyParams(self) -> None:
+        """Parameters are read from the Variables at every evaluation."""
+
+    def _node_consts(self) -> list[float]:
+        return self.constantsList
+
+    # ---- flattening ----
+    def _flatten(self):
+        params = self.getParameters()
+        pidx = {id(v): i for i, v in enumerate(params)}
+        obs = self.getObservables()
+        oidx = {id(o): i for i, o in enumerate(obs)}
+        nodes: list = []
+
+        def visit(p: "PdfBase") -> int:
+            i = len(nodes)
+            nodes.append(None)
+            kids = [visit(c) for c in p.components]
+            nodes[i] = dict(op=p.op, flags=p.flags, params=[pidx[id(v)] for v in p.parametersList],
+                            consts=list(p._node_consts()), obs=[oidx[id(o)] for o in p.observablesList],
+                            children=kids, integration_bins=p.integrationBins)
+            return i
+
+        visit(self)
+        return nodes, params, obs
+
+    def _engine_for(self, data, precision: str | None = None):
+        """Engine with this PDF as root and `data` uploaded; cached per (precision, data)."""
+        precision = precision or _DEFAULT_PRECISION
+        nodes, params, obs = self._flatten()
+        mask = [0 if v.fixed else 1 for v in params]
+        olist = [(o.lowerlimit, o.upperlimit, o.numbins, 1 if o.is_event_number else 0) for o in obs]
+        key = repr((nodes, olist, mask))
+        ent = self._engines.get(precision)
+        if ent is None or ent["key"] != key:
+            eng = ent["engine"] if ent else Engine(precision)
+            eng.set_tree(nodes, olist, len(params), mask)
+            ent = dict(engine=eng, key=key, data=None, version=-1)
+            self._engines[precision] = ent
+        eng = ent["engine"]
+        if data is not None and (ent["data"] is not data or ent["version"] != getattr(data, "version", 0)):
+            cols = np.vstack([data.column(o) for o in obs]) if data.getNumEvents() else np.zeros((len(obs), 0))
+            eng.upload(cols)
+            ent["data"], ent["version"] = data, getattr(data, "version", 0)
+        return eng, params
+
+    @staticmethod
+    def _param_values(params: Sequence[Variable]) -> np.ndarray:
+        return np.array([v.value - v._blind for v in params], dtype=np.float64)
+
+    def normalize(self) -> float:
+        """Integral of this PDF as GooPdf::normalize returns it (src/PDFs/GooPdf.cu:340-396)."""
+        data = self.data if self.data is not None else self._point_dataset()
+        eng, params = self._engine_for(data)
+        eng.set_params(self._param_values(params))
+        I, N = eng.normalize()
+        return float(I[0])
+
+    def calculateNLL(self) -> float:
+        if self.data is None:
+            raise GeneralError("no data set")
+        eng, params = self._engine_for(self.data)
+        return eng.nll(self._param_values(params))
+
+    def _point_dataset(self) -> UnbinnedDataSet:
+        ds = UnbinnedDataSet(self.getObservables())
+        ds.addEvent()
+        return ds
+
+    def fitTo(self, data, verbosity: int = 3) -> FitResult:
+        old = self.data
+        self.setData(data)
+        try:
+            return self.fit(verbosity)
+        finally:
+            self.setData(old)
+
+    def fit(self, verbosity: int = 3) -> FitResult:
+        fm = FitManager(self)
+        fm.verbosity = verbosity
+        return fm.fit()
+
+
+class GooPdf(PdfBase):
+    """include/goofit/PDFs/GooPdf.h"""
+
+    def integrate(self, lo: float, hi: float) -> float:
+        return 0.0
+
+    def hasAnalyticIntegral(self) -> bool:
+        return False
+
+    def makeGrid(self) -> UnbinnedDataSet:
+        grid = UnbinnedDataSet(self.getObservables())
+        grid.fillWithGrid()
+        return grid
+
+    def _probs(self, data, metric=A.GF_METRIC_PROB) -> np.ndarray:
+        eng, params = self._engine_for(data)
+        eng.set_params(self._param_values(params))
+        return eng.eval_events(metric)
+
+    def getValue(self, evalfunc: EvalFunc = EvalFunc.Eval) -> float:
+        """GooPdf::getValue (src/PDFs/GooPdf.cu:214-248) at the observables' current values."""
+        metric = {EvalFunc.Prob: A.GF_METRIC_PROB, EvalFunc.Eval: A.GF_METRIC_EVAL,
+                  EvalFunc.NLL: A.GF_METRIC_NLL}.get(evalfunc)
+        if metric is None:
+            raise GeneralError("That EvalFunc is not supported")
+        return float(self._probs(self._point_dataset(), metric)[0])
+
+    def evaluateAtPoints(self, var: Observable) -> list[float]:
+        """GooPdf::evaluateAtPoints (src/PDFs/GooPdf.cu:187-212): normalised values at var's bin centres."""
+        ds = UnbinnedDataSet(self.getObservables())
+        step = var.getBinSize()
+        saved = var.value
+        for i in range(var.getNumBins()):
+            var.value = var.lowerlimit + (i + 0.5) * step
+            ds.addEvent()
+        var.value = saved
+        return list(self._probs(ds, A.GF_METRIC_PROB))
+
+    def getCompProbsAtDataPoints(self) -> list[list[float]]:
+        """GooPdf::getCompProbsAtDataPoints (src/PDFs/GooPdf.cu:402-435)."""
+        if self.data is None:
+            raise GeneralError("no data set")
+        out = [list(self._probs(self.data))]
+        for c in self.components:
+            sub = UnbinnedDataSet(c.getObservables())
+            sub.from_numpy(np.vstack([self.data.column(o) for o in c.getObservables()]))
+            out.append(list(c._probs(sub)))
+        return out
+
+    def scan(self, var: Variable, values: list | None = None) -> list[float]:
+        """GooPdf::scan (src/PDFs/GooPdf.cpp:69-82): NLL at bin centres of a parameter."""
+        res = []
+        step = (var.upperlimit - var.lowerlimit) / 100
+        v = var.lowerlimit + 0.5 * step
+        saved = var.value
+        while v < var.upperlimit:
+            var.value = v
+            res.append(self.calculateNLL())
+            v += step
+        var.value = saved
+        if values is not None:
+            values[:] = res
+        return res
+
+    def fillMCDataSimple(self, events: int, seed: int = 0) -> None:
+        """PdfBase::fillMCDataSimple (src/goofit/PdfBase.cpp:154-203): inverse-CDF fill of the data set."""
+        obs = self.getObservables()
+        if len(obs) != 1:
+            raise GeneralError("You can only fill MC on a 1D dataset with a simple fill")
+        var = obs[0]
+        origdata = self.data
+        if origdata is None:
+            raise GeneralError("Can't run on a PDF with no DataSet to fill!")
+        grid = UnbinnedDataSet(var)
+        grid.fillWithGrid()
+        pdfValues = np.asarray(self._probs(grid))
+        rng = np.random.default_rng(seed if seed else None)
+        integral = np.cumsum(pdfValues)
+        integral /= integral[-1]
+        r = rng.random(events)
+        j = np.searchsorted(integral, r, side="left")
+        x = grid.column(var)[j] + var.getBinSize() * (rng.random(events) - 0.5)
+        x = np.clip(x, var.lowerlimit, var.upperlimit)
+        origdata.from_numpy(x.reshape(1, -1))
+
+
+class CombinePdf(GooPdf):
+    """include/goofit/PDFs/CombinePdf.h"""
+
+
+class ExpPdf(GooPdf):
+    """include/goofit/PDFs/basic/ExpPdf.h, src/PDFs/basic/ExpPdf.cu"""
+
+    def __init__(self, name: str, x: Observable, alpha, offset: Variable | None = None):
+        if isinstance(alpha, (list, tuple)):
+            if not alpha:
+                raise GeneralError("Weights are empty!")
+            if offset is None:
+                super().__init__("ExpPdf", name, x)
+                self.op = A.GF_OP_EXP_POLY
+            else:
+                super().__init__("ExpPdf", name, x, offset)
+                self.op = A.GF_OP_EXP_POLY_OFFSET
+            for w in alpha:
+                self.registerParameter(w)
+        elif offset is None:
+            super().__init__("ExpPdf", name, x, alpha)
+            self.op = A.GF_OP_EXP
+        else:
+            super().__init__("ExpPdf", name, x, offset, alpha)
+            self.op = A.GF_OP_EXP_OFFSET
+
+    def hasAnalyticIntegral(self) -> bool:
+        return len(self.parametersList) == 1
+
+    def integrate(self, lo: float, hi: float) -> float:
+        alpha = self.parametersList[0].value
+        if alpha == 0:
+            return hi - lo
+        return (math.exp(alpha * hi) - math.exp(alpha * lo)) / alpha
+
+
+class GaussianPdf(GooPdf):
+    """include/goofit/PDFs/basic/GaussianPdf.h"""
+    op = A.GF_OP_GAUSSIAN
+
+    def __init__(self, name: str, x: Observable, mean: Variable, sigma: Variable):
+        super().__init__("GaussianPdf", name, x, mean, sigma)
+
+    def hasAnalyticIntegral(self) -> bool:
+        return True
+
+    def integrate(self, lo: float, hi: float) -> float:
+        return self.parametersList[1].value * math.sqrt(2.0) * math.sqrt(math.atan2(0.0, -1.0))
+
+
+class PolynomialPdf(GooPdf):
+    """include/goofit/PDFs/basic/PolynomialPdf.h (one-observable forms)."""
+
+    def __init__(self, name: str, x: Observable, weights: Sequence[Variable], *args):
+        super().__init__("PolynomialPdf", name, x)
+        x0 = None
+        lowest = 0
+        if args and isinstance(args[0], Variable):
+            x0 = args[0]
+            lowest = int(args[1]) if len(args) > 1 else 0
+        elif args:
+            lowest = int(args[0])
+        self.registerConstant(lowest)
+        for w in weights:
+            self.registerParameter(w)
+        if x0 is not None:
+            self.registerParameter(x0)
+            self.op = A.GF_OP_POLYNOMIAL_OFFSET
+        else:
+            self.op = A.GF_OP_POLYNOMIAL
+
+
+class AddPdf(CombinePdf):
+    """include/goofit/PDFs/combine/AddPdf.h: AddPdf(name, weights, comps) / AddPdf(name, frac, pdf1, pdf2)."""
+
+    def __init__(self, name: str, weights, comps, third=None):
+        super().__init__("AddPdf", name)
+        if isinstance(weights, Variable):
+            comps_l = [comps, third]
+            ws = [weights]
+            self.extended = False
+        else:
+            ws, comps_l = list(weights), list(comps)
+            if len(ws) != len(comps_l) and len(ws) + 1 != len(comps_l):
+                raise GeneralError(f"Size of weights {len(ws)} (+1) != comps {len(comps_l)}")
+            self.extended = len(ws) == len(comps_l)
+        for c in comps_l:
+            if c is None:
+                raise GeneralError("Invalid component")
+            self.components.append(c)
+        self.observablesList = self.getObservables()
+        for w in ws:
+            self.registerParameter(w)
+        self.op = A.GF_OP_ADD_EXT if self.extended else A.GF_OP_ADD
+
+
+class ProdPdf(CombinePdf):
+    """include/goofit/PDFs/combine/ProdPdf.h"""
+    op = A.GF_OP_PROD
+
+    def __init__(self, name: str, comps: Sequence[PdfBase]):
+        super().__init__("ProdPdf", name)
+        self.components = list(comps)
+        self.observablesList = self.getObservables()
+        self.registerConstant(len(self.components))
+
+
+class ConvolutionPdf(CombinePdf):
+    """include/goofit/PDFs/combine/ConvolutionPdf.h; integration constants default to (-10, 10, 0.01)."""
+    op = A.GF_OP_CONVOLUTION
+    _count = 0
+
+    def __init__(self, name: str, x: Observable, model: GooPdf, resolution: GooPdf, numOthers: int | None = None):
+        super().__init__("ConvolutionPdf", name, x)
+        self.model, self.resolution = model, resolution
+        self.components = [model, resolution]
+        self.observablesList = self.getObservables()
+        self.workSpaceIndex = ConvolutionPdf._count
+        ConvolutionPdf._count += 1
+        self.constantsList = [-10.0, 10.0, 0.01, float(self.workSpaceIndex)]
+
+    def setIntegrationConstants(self, lo: float, hi: float, step: float) -> None:
+        self.constantsList[0:3] = [float(lo), float(hi), float(step)]
+
+
+# ---------------------------------------------------------------- fitting
+class FitManager:
+    """FitManagerMinuit2 surface (include/goofit/fitting/FitManagerMinuit2.h) on the project MIGRAD.
+
+    Extra keywords: precision ('mixed'/'fp64'), gradient ('analytic' or
+    'numerical', the latter is MINUIT's 2-point scheme like the reference's
+    Minuit2 default) and tolerance (MnMigrad tolerance; EDM < 0.002 tol up)."""
+
+    Valid, NotRun, InValid = 0, 50, 51
+
+    def __init__(self, pdf: PdfBase, precision: str | None = None, gradient: str = "analytic",
+                 tolerance: float = 0.1):
+        self.pdf = pdf
+        self.precision = precision
+        self.gradient = gradient
+        self.tolerance = tolerance
+        self.verbosity = 3
+        self.max_calls = 0
+        self.strategy = 1
+        self.retval = FitManager.NotRun
+        self.minos = False
+        self.result: FitResult | None = None
+        self.wall_seconds = 0.0
+
+    def setMaxCalls(self, n: int = 0) -> None:
+        self.max_calls = int(n)
+
+    def setVerbosity(self, v: int) -> None:
+        self.verbosity = v
+
+    def getVerbosity(self) -> int:
+        return self.verbosity
+
+    def setStrategy(self, s: int) -> None:
+        self.strategy = int(s)
+
+    def setMinos(self, flag: bool = True) -> None:
+        if flag:
+            raise NotImplementedError("MINOS errors are not provided by this engine")
+
+    def fit(self) -> FitResult:
+        pdf = self.pdf
+        if pdf.data is None:
+            raise GeneralError("no data set")
+        eng, params = pdf._engine_for(pdf.data, self.precision)
+        n = len(params)
+        blind = np.array([v._blind for v in params])
+        x0 = np.array([v.value for v in params]) - blind
+        err = np.array([v.error for v in params])
+        lo = np.array([v.lowerlimit for v in params]) - blind
+        hi = np.array([v.upperlimit for v in params]) - blind
+        fixed = np.array([1 if v.fixed else 0 for v in params], dtype=np.int32)
+        limited = np.array([0 if (v.fixed or v.lowerlimit == v.upperlimit) else 1 for v in params], dtype=np.int32)
+        for i, v in enumerate(params):
+            v.fitter_index = i
+        t0 = time.perf_counter()
+        res = eng.fit(x0, err, lo, hi, limited, fixed, tolerance=self.tolerance, strategy=self.strategy,
+                      maxfcn=self.max_calls, use_grad=(self.gradient == "analytic"))
+        self.wall_seconds = time.perf_counter() - t0
+        for i, v in enumerate(params):
+            v.value = res.values[i] + blind[i]
+            v.error = res.errors[i]
+        self.result = res
+        self.retval = FitManager.Valid if res.valid else FitManager.InValid
+        if self.verbosity > 0:
+            print(f"MIGRAD {'valid' if res.valid else 'INVALID'}: fmin={res.fmin:.10g} edm={res.edm:.3g} "
+                  f"nfcn={res.nfcn} ({self.wall_seconds:.4f} s)")
+            for v in params:
+                print("  ", v)
+        return res
+
+    def __bool__(self) -> bool:
+        return self.retval == FitManager.Valid
+
+    def __int__(self) -> int:
+        return self.retval
+
+
+FitManagerMinuit2 = FitManager

@@ -1,0 +1,921 @@
+// Likelihood engine runtime: the C ABI of include/gfengine.h.
+//
+// Replaces the reference's process-global device state (d_parameters,
+// d_constants, d_observables, d_normalizations, d_function_table,
+// dev_event_array: src/PDFs/detail/Globals.cu:9-26, src/goofit/Globals.cpp:11)
+// with per-handle buffers: per-toy SoA event columns in HBM, a pinned
+// parameter/result exchange area, and one captured CUDA graph per
+// evaluation kind that runs   H2D(params) -> conv tables -> grid sums ->
+// event pass -> D2H(result)   in a single graph launch.
+#include "engine.h"
+#include "rtc.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+namespace {
+
+thread_local std::string g_create_err;
+
+struct ConvertArgs {
+    const double *soa;
+    long long n, npad;
+    int n_obs, n_conv;
+    void *cols[16];
+    int *kcols[8];
+    int conv_obs[8];
+    double conv_lo[8], conv_step[8];
+    int conv_kmin[8], conv_kmax[8];
+    double pad_val[16];
+    int *err;
+};
+
+// FP64 SoA -> engine columns (FP32 or FP64) plus the ConvolutionPdf bin
+// offset of every event (src/PDFs/combine/ConvolutionPdf.cu:40-43, FP64),
+// which is all the convolution needs of x.
+template <typename R>
+__global__ void gf_convert_events(const ConvertArgs a) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if(i >= a.npad)
+        return;
+    for(int o = 0; o < a.n_obs; ++o) {
+        double x = i < a.n ? a.soa[(long long)o * a.n + i] : a.pad_val[o];
+        reinterpret_cast<R *>(a.cols[o])[i] = (R)x;
+    }
+    for(int c = 0; c < a.n_conv; ++c) {
+        int k;
+        if(i < a.n) {
+            double x0  = a.soa[(long long)a.conv_obs[c] * a.n + i];
+            double lbo = a.conv_lo[c] / a.conv_step[c];
+            lbo -= floor(lbo);
+            k = (int)floor(x0 / a.conv_step[c] - lbo);
+            if(k < a.conv_kmin[c] || k > a.conv_kmax[c]) {
+                atomicOr(a.err, 1);
+                k = a.conv_kmin[c];
+            }
+        } else
+            k = a.conv_kmin[c];
+        a.kcols[c][i] = k;
+    }
+}
+
+size_t rsize(const gf_engine *e) { return e->precision == GF_MIXED ? 4 : 8; }
+
+void freeToy(GfToy &t) {
+    for(int o = 0; o < 16; ++o)
+        if(t.cols[o]) {
+            if(o == 0)
+                cudaFree(t.cols[0]);
+            t.cols[o] = nullptr;
+        }
+    for(int c = 0; c < 8; ++c)
+        t.kcols[c] = nullptr;
+    t.loaded = false;
+    t.n = t.npad = 0;
+}
+
+template <typename T>
+void dfree(T *&p) {
+    if(p)
+        cudaFree((void *)p);
+    p = nullptr;
+}
+template <typename T>
+void hfree(T *&p) {
+    if(p)
+        cudaFreeHost((void *)p);
+    p = nullptr;
+}
+
+void dropGraphs(gf_engine *e) {
+    for(auto &g : e->graph)
+        if(g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
+void freeLayout(gf_engine *e) {
+    dropGraphs(e);
+    dfree(e->d_P);
+    dfree(e->d_active);
+    dfree(e->d_cols);
+    dfree(e->d_kcols);
+    dfree(e->d_ctab);
+    dfree(e->d_kgrid);
+    dfree(e->d_gsum);
+    dfree(e->d_gpartial);
+    dfree(e->d_gcounter);
+    dfree(e->d_partial);
+    dfree(e->d_counter);
+    dfree(e->d_out);
+    dfree(e->d_chunks);
+    dfree(e->d_toy_chunk0);
+    dfree(e->d_toy_nchunks);
+    dfree(e->d_toy_nevents);
+    hfree(e->h_P);
+    hfree(e->h_active);
+    hfree(e->h_out);
+    e->layout_ready = false;
+}
+
+void freeModule(gf_engine *e) {
+    if(e->mod.lib)
+        cudaLibraryUnload(e->mod.lib);
+    e->mod = GfModule();
+}
+
+int nGradOf(const gf_engine *e) { return e->tree.NG; }
+
+template <typename T>
+int dalloc(gf_engine *e, T *&p, size_t count, bool zero = true) {
+    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    cudaError_t r = cudaMalloc((void **)&p, bytes);
+    if(r != cudaSuccess)
+        return gf_fail(e, GF_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(r));
+    if(zero)
+        cudaMemset((void *)p, 0, bytes);
+    return GF_OK;
+}
+
+int buildLayout(gf_engine *e) {
+    if(e->layout_ready)
+        return GF_OK;
+    freeLayout(e);
+    const gf::Tree &T = e->tree;
+    const int NT = e->n_toys, NO = (int)T.obs.size(), NC = (int)T.convs.size(), NQ = (int)T.nums.size();
+    const int NGp = 1 + T.NG;
+    for(int t = 0; t < NT; ++t)
+        if(!e->toys[t].loaded)
+            return gf_fail(e, GF_ERR_STATE, "toy " + std::to_string(t) + " has no events");
+    std::vector<long long> chunks;
+    std::vector<int> c0(NT), nc(NT);
+    std::vector<long long> ne(NT);
+    for(int t = 0; t < NT; ++t) {
+        int64_t n = e->toys[t].n;
+        int k     = std::max<int64_t>(1, (n + e->chunk - 1) / e->chunk);
+        c0[t]     = (int)(chunks.size() / 3);
+        nc[t]     = k;
+        ne[t]     = n;
+        for(int c = 0; c < k; ++c) {
+            chunks.push_back(t);
+            chunks.push_back((long long)c * e->chunk);
+            chunks.push_back(std::min<long long>((long long)(c + 1) * e->chunk, n));
+        }
+    }
+    e->n_chunks = (int)(chunks.size() / 3);
+    int rc      = GF_OK;
+    auto chk    = [&](int r) {
+        if(r != GF_OK && rc == GF_OK)
+            rc = r;
+    };
+    chk(dalloc(e, e->d_P, (size_t)NT * std::max(1, T.n_params)));
+    chk(dalloc(e, e->d_active, NT));
+    chk(dalloc(e, e->d_cols, (size_t)NT * NO));
+    chk(dalloc(e, e->d_kcols, (size_t)NT * std::max(1, NC)));
+    int64_t ctab = std::max(e->plan.ctab_per_toy_grad, e->plan.ctab_per_toy_nograd);
+    {
+        void *p = nullptr;
+        size_t bytes = (size_t)std::max<int64_t>(1, NT * ctab) * rsize(e);
+        if(cudaMalloc(&p, bytes) != cudaSuccess)
+            chk(gf_fail(e, GF_ERR_OOM, "cudaMalloc conv tables"));
+        else
+            cudaMemset(p, 0, bytes);
+        e->d_ctab = p;
+    }
+    chk(dalloc(e, e->d_kgrid, std::max<size_t>(1, T.kgrid.size())));
+    chk(dalloc(e, e->d_gsum, (size_t)NT * std::max(1, NQ) * NGp));
+    chk(dalloc(e, e->d_gpartial, (size_t)NT * std::max(1, NQ) * std::max(1, e->plan.max_grid_blocks) * NGp));
+    chk(dalloc(e, e->d_gcounter, (size_t)NT * std::max(1, NQ)));
+    chk(dalloc(e, e->d_partial, (size_t)e->n_chunks * NGp));
+    chk(dalloc(e, e->d_counter, NT));
+    chk(dalloc(e, e->d_out, (size_t)NT * (NGp + 1)));
+    chk(dalloc(e, e->d_chunks, chunks.size()));
+    chk(dalloc(e, e->d_toy_chunk0, NT));
+    chk(dalloc(e, e->d_toy_nchunks, NT));
+    chk(dalloc(e, e->d_toy_nevents, NT));
+    if(rc != GF_OK)
+        return rc;
+    if(cudaMallocHost((void **)&e->h_P, sizeof(double) * (size_t)NT * std::max(1, T.n_params)) != cudaSuccess ||
+       cudaMallocHost((void **)&e->h_active, sizeof(int) * NT) != cudaSuccess ||
+       cudaMallocHost((void **)&e->h_out, sizeof(double) * (size_t)NT * (NGp + 1)) != cudaSuccess)
+        return gf_fail(e, GF_ERR_OOM, "cudaMallocHost");
+    std::memset(e->h_P, 0, sizeof(double) * (size_t)NT * std::max(1, T.n_params));
+    for(int t = 0; t < NT; ++t)
+        e->h_active[t] = 1;
+    std::vector<void *> cols((size_t)NT * NO, nullptr);
+    std::vector<int *> kcols((size_t)NT * std::max(1, NC), nullptr);
+    for(int t = 0; t < NT; ++t) {
+        for(int o = 0; o < NO; ++o)
+            cols[(size_t)t * NO + o] = e->toys[t].cols[o];
+        for(int c = 0; c < NC; ++c)
+            kcols[(size_t)t * NC + c] = e->toys[t].kcols[c];
+    }
+    cudaMemcpy(e->d_cols, cols.data(), sizeof(void *) * cols.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(e->d_kcols, kcols.data(), sizeof(int *) * kcols.size(), cudaMemcpyHostToDevice);
+    if(!T.kgrid.empty())
+        cudaMemcpy(e->d_kgrid, T.kgrid.data(), sizeof(int) * T.kgrid.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(e->d_chunks, chunks.data(), sizeof(long long) * chunks.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(e->d_toy_chunk0, c0.data(), sizeof(int) * NT, cudaMemcpyHostToDevice);
+    cudaMemcpy(e->d_toy_nchunks, nc.data(), sizeof(int) * NT, cudaMemcpyHostToDevice);
+    cudaMemcpy(e->d_toy_nevents, ne.data(), sizeof(long long) * NT, cudaMemcpyHostToDevice);
+    cudaError_t r = cudaDeviceSynchronize();
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "layout upload");
+    e->layout_ready = true;
+    return GF_OK;
+}
+
+GfArgs makeArgs(gf_engine *e) {
+    GfArgs a{};
+    a.P           = e->d_P;
+    a.active      = e->d_active;
+    a.col         = (const void *const *)e->d_cols;
+    a.kcol        = (const int *const *)e->d_kcols;
+    a.ctab        = e->d_ctab;
+    a.kgrid       = e->d_kgrid;
+    a.gsum        = e->d_gsum;
+    a.gpartial    = e->d_gpartial;
+    a.gcounter    = e->d_gcounter;
+    a.partial     = e->d_partial;
+    a.counter     = e->d_counter;
+    a.out         = e->d_out;
+    a.chunks      = e->d_chunks;
+    a.toy_chunk0  = e->d_toy_chunk0;
+    a.toy_nchunks = e->d_toy_nchunks;
+    a.toy_nevents = e->d_toy_nevents;
+    a.vals        = e->d_vals;
+    a.n_chunks    = e->n_chunks;
+    a.n_toys      = e->n_toys;
+    a.metric      = 1;
+    return a;
+}
+
+cudaError_t launch(cudaKernel_t k, dim3 g, dim3 b, size_t smem, cudaStream_t s, GfArgs &a) {
+    void *args[] = {&a};
+    return cudaLaunchKernel((const void *)k, g, b, args, smem, s);
+}
+
+// Enqueues the prep kernels (conv tables, grid sums) for one variant.
+cudaError_t enqueuePrep(gf_engine *e, bool grad, GfArgs &a) {
+    const gf::Tree &T = e->tree;
+    cudaError_t r     = cudaSuccess;
+    if(!T.convs.empty()) {
+        dim3 g(e->plan.conv_blocks, e->n_toys, (unsigned)T.convs.size());
+        r = launch(grad ? e->mod.conv_g : e->mod.conv_n, g, dim3(e->block),
+                   grad ? e->plan.conv_smem_grad : e->plan.conv_smem_nograd, e->stream, a);
+        if(r != cudaSuccess)
+            return r;
+    }
+    if(!T.nums.empty()) {
+        dim3 g(e->plan.max_grid_blocks, e->n_toys, (unsigned)T.nums.size());
+        r = launch(grad ? e->mod.grid_g : e->mod.grid_n, g, dim3(e->block), 0, e->stream, a);
+    }
+    return r;
+}
+
+int evtGrid(const gf_engine *e) { return std::max(1, std::min(e->n_chunks, e->sm_count * e->evt_ctas_per_sm)); }
+
+cudaError_t enqueueEval(gf_engine *e, bool grad) {
+    const gf::Tree &T = e->tree;
+    const int NT = e->n_toys, NGp = 1 + T.NG;
+    GfArgs a         = makeArgs(e);
+    cudaError_t r    = cudaEventRecord(e->ev[0], e->stream);
+    if(r == cudaSuccess)
+        r = cudaMemcpyAsync(e->d_P, e->h_P, sizeof(double) * (size_t)NT * std::max(1, T.n_params),
+                            cudaMemcpyHostToDevice, e->stream);
+    if(r == cudaSuccess)
+        r = cudaMemcpyAsync(e->d_active, e->h_active, sizeof(int) * NT, cudaMemcpyHostToDevice, e->stream);
+    if(r == cudaSuccess)
+        r = enqueuePrep(e, grad, a);
+    if(r == cudaSuccess)
+        r = cudaEventRecord(e->ev[1], e->stream);
+    if(r == cudaSuccess)
+        r = launch(grad ? e->mod.evt_g : e->mod.evt_n, dim3(evtGrid(e)), dim3(e->block),
+                   grad ? e->plan.evt_smem_grad : e->plan.evt_smem_nograd, e->stream, a);
+    if(r == cudaSuccess)
+        r = cudaEventRecord(e->ev[2], e->stream);
+    if(r == cudaSuccess)
+        r = cudaMemcpyAsync(e->h_out, e->d_out, sizeof(double) * (size_t)NT * (NGp + 1), cudaMemcpyDeviceToHost,
+                            e->stream);
+    if(r == cudaSuccess)
+        r = cudaEventRecord(e->ev[3], e->stream);
+    return r;
+}
+
+int statusOf(double st) {
+    int s = (int)st;
+    if(s & 1)
+        return GF_ERR_NAN_NORM;
+    if(s & 2)
+        return GF_ERR_NONPOS_NORM;
+    if(s & 4)
+        return GF_ERR_ZERO_NLL;
+    return GF_OK;
+}
+
+int loadModule(gf_engine *e) {
+    std::vector<char> cubin;
+    std::string log;
+    std::string arch = "sm_103a";
+    if(const char *a = std::getenv("GF_ARCH"))
+        arch = a;
+    if(!gf::rtc_compile(e->plan.source, arch, cubin, log))
+        return gf_fail(e, GF_ERR_COMPILE, log);
+    freeModule(e);
+    cudaError_t r = cudaLibraryLoadData(&e->mod.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "cudaLibraryLoadData");
+    auto get = [&](cudaKernel_t &k, const char *name, bool need) -> int {
+        cudaError_t rr = cudaLibraryGetKernel(&k, e->mod.lib, name);
+        if(rr != cudaSuccess) {
+            k = nullptr;
+            cudaGetLastError();
+            if(need)
+                return gf_cuda_check(e, rr, name);
+        }
+        return GF_OK;
+    };
+    bool hasConv = !e->tree.convs.empty(), hasGrid = !e->tree.nums.empty();
+    int rc = GF_OK;
+    if((rc = get(e->mod.conv_g, "gf_conv_g", hasConv)) || (rc = get(e->mod.conv_n, "gf_conv_n", hasConv)) ||
+       (rc = get(e->mod.grid_g, "gf_grid_g", hasGrid)) || (rc = get(e->mod.grid_n, "gf_grid_n", hasGrid)) ||
+       (rc = get(e->mod.evt_g, "gf_evt_g", true)) || (rc = get(e->mod.evt_n, "gf_evt_n", true)) ||
+       (rc = get(e->mod.val_n, "gf_val_n", true)))
+        return rc;
+    auto smem = [&](cudaKernel_t k, size_t bytes) -> int {
+        if(!k || bytes <= 48 * 1024)
+            return GF_OK;
+        return gf_cuda_check(e,
+                             cudaKernelSetAttributeForDevice(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                             (int)bytes, e->device),
+                             "dynamic shared memory attribute");
+    };
+    if((rc = smem(e->mod.conv_g, e->plan.conv_smem_grad)) || (rc = smem(e->mod.conv_n, e->plan.conv_smem_nograd)) ||
+       (rc = smem(e->mod.evt_g, e->plan.evt_smem_grad)) || (rc = smem(e->mod.evt_n, e->plan.evt_smem_nograd)) ||
+       (rc = smem(e->mod.val_n, e->plan.evt_smem_nograd)))
+        return rc;
+    const size_t maxSmem = 227 * 1024;
+    if(e->plan.conv_smem_grad > maxSmem || e->plan.evt_smem_grad > maxSmem)
+        return gf_fail(e, GF_ERR_BAD_TREE, "convolution workspaces exceed shared memory");
+    return GF_OK;
+}
+
+} // namespace
+
+int gf_fail(gf_engine *e, int code, const std::string &msg) {
+    if(e)
+        e->err = msg;
+    else
+        g_create_err = msg;
+    return code;
+}
+
+int gf_cuda_check(gf_engine *e, cudaError_t r, const char *what) {
+    if(r == cudaSuccess)
+        return GF_OK;
+    return gf_fail(e, r == cudaErrorMemoryAllocation ? GF_ERR_OOM : GF_ERR_CUDA,
+                   std::string(what) + ": " + cudaGetErrorString(r));
+}
+
+// Runs one evaluation of every active toy.  Results land in e->h_out.
+int gf_run(gf_engine *e, bool grad, int, int) {
+    int rc = buildLayout(e);
+    if(rc)
+        return rc;
+    cudaError_t r;
+    if(e->use_graph) {
+        cudaGraphExec_t &ge = e->graph[grad ? 1 : 0];
+        if(!ge) {
+            cudaGraph_t g = nullptr;
+            r             = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+            if(r != cudaSuccess)
+                return gf_cuda_check(e, r, "cudaStreamBeginCapture");
+            cudaError_t r1 = enqueueEval(e, grad);
+            r              = cudaStreamEndCapture(e->stream, &g);
+            if(r1 != cudaSuccess) {
+                if(g)
+                    cudaGraphDestroy(g);
+                return gf_cuda_check(e, r1, "capturing the evaluation graph");
+            }
+            if(r != cudaSuccess)
+                return gf_cuda_check(e, r, "cudaStreamEndCapture");
+            r = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            if(r != cudaSuccess) {
+                ge = nullptr;
+                return gf_cuda_check(e, r, "cudaGraphInstantiate");
+            }
+        }
+        r = cudaGraphLaunch(ge, e->stream);
+        if(r != cudaSuccess)
+            return gf_cuda_check(e, r, "cudaGraphLaunch");
+    } else {
+        r = enqueueEval(e, grad);
+        if(r != cudaSuccess)
+            return gf_cuda_check(e, r, "launch");
+    }
+    r = cudaStreamSynchronize(e->stream);
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "evaluation");
+    float ms = 0;
+    if(cudaEventElapsedTime(&ms, e->ev[0], e->ev[3]) == cudaSuccess)
+        e->last_ms_total = ms;
+    if(cudaEventElapsedTime(&ms, e->ev[1], e->ev[2]) == cudaSuccess)
+        e->last_ms_evt = ms;
+    return GF_OK;
+}
+
+extern "C" {
+
+const char *gf_version(void) {
+    static std::string v = "gfengine 0.1 (sm_103a, nvrtc " + gf::rtc_version() + ")";
+    return v.c_str();
+}
+
+const char *gf_last_error(const gf_engine *eng) { return eng ? eng->err.c_str() : g_create_err.c_str(); }
+
+int gf_engine_create(gf_engine **out, int device, int precision) {
+    if(!out)
+        return gf_fail(nullptr, GF_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    if(precision != GF_FP64 && precision != GF_MIXED)
+        return gf_fail(nullptr, GF_ERR_INVALID, "precision must be GF_FP64 or GF_MIXED");
+    int count      = 0;
+    cudaError_t r  = cudaGetDeviceCount(&count);
+    if(r != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return gf_fail(nullptr, GF_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(r));
+    }
+    if(device < 0 || device >= count)
+        return gf_fail(nullptr, GF_ERR_INVALID, "device index out of range");
+    gf_engine *e = new(std::nothrow) gf_engine();
+    if(!e)
+        return gf_fail(nullptr, GF_ERR_OOM, "out of host memory");
+    e->device    = device;
+    e->precision = precision;
+    if((r = cudaSetDevice(device)) != cudaSuccess || (r = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        g_create_err = std::string("CUDA init: ") + cudaGetErrorString(r);
+        delete e;
+        return GF_ERR_CUDA;
+    }
+    for(auto &ev : e->ev)
+        cudaEventCreate(&ev);
+    cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if(const char *g = std::getenv("GF_NO_GRAPH"))
+        e->use_graph = !(g[0] == '1');
+    if(const char *c = std::getenv("GF_CHUNK"))
+        e->chunk = std::max(1024, (atoi(c) / 1024) * 1024);
+    if(const char *c = std::getenv("GF_EVT_CTAS_PER_SM"))
+        e->evt_ctas_per_sm = std::max(1, atoi(c));
+    e->toys.assign(1, GfToy());
+    *out = e;
+    return GF_OK;
+}
+
+int gf_engine_destroy(gf_engine *e) {
+    if(!e)
+        return GF_OK;
+    cudaSetDevice(e->device);
+    cudaStreamSynchronize(e->stream);
+    freeLayout(e);
+    for(auto &t : e->toys)
+        freeToy(t);
+    dfree(e->d_vals);
+    dfree(e->d_stage);
+    dfree(e->d_uperr);
+    hfree(e->h_uperr);
+    freeModule(e);
+    for(auto &ev : e->ev)
+        if(ev)
+            cudaEventDestroy(ev);
+    if(e->stream)
+        cudaStreamDestroy(e->stream);
+    delete e;
+    return GF_OK;
+}
+
+int gf_set_tree(gf_engine *e, const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
+                const int32_t *grad_mask) {
+    if(!e)
+        return gf_fail(nullptr, GF_ERR_INVALID, "null engine");
+    cudaSetDevice(e->device);
+    gf::Tree t;
+    std::string why = t.build(nodes, n_nodes, obs, n_obs, n_params, grad_mask);
+    if(!why.empty())
+        return gf_fail(e, GF_ERR_BAD_TREE, why);
+    freeLayout(e);
+    for(auto &ty : e->toys)
+        freeToy(ty);
+    e->tree     = t;
+    e->has_tree = false;
+    try {
+        e->plan = gf::generate_kernels(e->tree, e->precision == GF_MIXED, e->block, e->chunk);
+    } catch(std::exception &ex) {
+        return gf_fail(e, GF_ERR_BAD_TREE, ex.what());
+    }
+    int rc = loadModule(e);
+    if(rc)
+        return rc;
+    e->has_tree = true;
+    return GF_OK;
+}
+
+int gf_set_num_toys(gf_engine *e, int n) {
+    if(!e || n < 1)
+        return gf_fail(e, GF_ERR_INVALID, "toy count must be >= 1");
+    cudaSetDevice(e->device);
+    freeLayout(e);
+    for(auto &t : e->toys)
+        freeToy(t);
+    e->n_toys = n;
+    e->toys.assign(n, GfToy());
+    return GF_OK;
+}
+
+int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
+    if(!e)
+        return gf_fail(nullptr, GF_ERR_INVALID, "null engine");
+    if(!e->has_tree)
+        return gf_fail(e, GF_ERR_STATE, "gf_set_tree must come before gf_upload_events");
+    if(toy < 0 || toy >= e->n_toys)
+        return gf_fail(e, GF_ERR_INVALID, "toy index out of range");
+    if(n < 0 || (n > 0 && !soa))
+        return gf_fail(e, GF_ERR_INVALID, "bad event array");
+    cudaSetDevice(e->device);
+    const gf::Tree &T = e->tree;
+    const int NO = (int)T.obs.size(), NC = (int)T.convs.size();
+    GfToy &ty    = e->toys[toy];
+    int64_t npad = std::max<int64_t>(4, (n + 3) / 4 * 4);
+    size_t rs    = rsize(e);
+    cudaError_t r;
+    // a re-upload of the same size keeps the buffers, the chunk layout and the captured graphs
+    const bool reuse = ty.loaded && ty.n == n && ty.npad == npad;
+    if(!reuse) {
+        freeToy(ty);
+        e->layout_ready = false;
+        dropGraphs(e);
+        size_t colBytes = (size_t)npad * rs, kBytes = (size_t)npad * sizeof(int);
+        void *base      = nullptr;
+        r = cudaMalloc(&base, colBytes * NO + kBytes * std::max(NC, 0) + 256);
+        if(r != cudaSuccess)
+            return gf_cuda_check(e, r, "cudaMalloc events");
+        for(int o = 0; o < NO; ++o)
+            ty.cols[o] = (char *)base + colBytes * o;
+        for(int c = 0; c < NC; ++c)
+            ty.kcols[c] = (int *)((char *)base + colBytes * NO + kBytes * c);
+    }
+    const int64_t need = std::max<int64_t>(1, n) * NO;
+    if(e->stage_cap < need) {
+        dfree(e->d_stage);
+        r = cudaMalloc((void **)&e->d_stage, sizeof(double) * need);
+        if(r != cudaSuccess) {
+            e->stage_cap = 0;
+            return gf_cuda_check(e, r, "cudaMalloc staging");
+        }
+        e->stage_cap = need;
+    }
+    if(!e->d_uperr) {
+        if((r = cudaMalloc((void **)&e->d_uperr, sizeof(int))) != cudaSuccess ||
+           (r = cudaMallocHost((void **)&e->h_uperr, sizeof(int))) != cudaSuccess)
+            return gf_cuda_check(e, r, "cudaMalloc flag");
+    }
+    double *stage = e->d_stage;
+    int *derr     = e->d_uperr;
+    cudaMemsetAsync(derr, 0, sizeof(int), e->stream);
+    if(n > 0)
+        cudaMemcpyAsync(stage, soa, sizeof(double) * n * NO, cudaMemcpyHostToDevice, e->stream);
+    ConvertArgs a{};
+    a.soa    = stage;
+    a.n      = n;
+    a.npad   = npad;
+    a.n_obs  = NO;
+    a.n_conv = NC;
+    for(int o = 0; o < NO; ++o) {
+        a.cols[o]    = ty.cols[o];
+        a.pad_val[o] = 0.5 * (T.obs[o].lo + T.obs[o].hi);
+    }
+    for(int c = 0; c < NC; ++c) {
+        a.kcols[c]     = ty.kcols[c];
+        a.conv_obs[c]  = T.convs[c].obs;
+        a.conv_lo[c]   = T.convs[c].lo;
+        a.conv_step[c] = T.convs[c].step;
+        a.conv_kmin[c] = T.convs[c].kmin;
+        a.conv_kmax[c] = T.convs[c].kmax;
+    }
+    a.err = derr;
+    unsigned blocks = (unsigned)((npad + 255) / 256);
+    if(e->precision == GF_MIXED)
+        gf_convert_events<float><<<blocks, 256, 0, e->stream>>>(a);
+    else
+        gf_convert_events<double><<<blocks, 256, 0, e->stream>>>(a);
+    cudaMemcpyAsync(e->h_uperr, derr, sizeof(int), cudaMemcpyDeviceToHost, e->stream);
+    r        = cudaStreamSynchronize(e->stream);
+    int herr = *e->h_uperr;
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "event conversion");
+    ty.n      = n;
+    ty.npad   = npad;
+    ty.loaded = true;
+    if(herr)
+        return gf_fail(e, GF_ERR_INVALID, "event outside the observable range of a ConvolutionPdf");
+    return GF_OK;
+}
+
+int gf_set_params(gf_engine *e, int toy, const double *p, int n) {
+    if(!e || !e->has_tree)
+        return gf_fail(e, GF_ERR_STATE, "no tree");
+    if(toy < 0 || toy >= e->n_toys || n != e->tree.n_params || (n > 0 && !p))
+        return gf_fail(e, GF_ERR_INVALID, "bad toy index or parameter count");
+    cudaSetDevice(e->device);
+    int rc = buildLayout(e);
+    if(rc)
+        return rc;
+    std::memcpy(e->h_P + (size_t)toy * n, p, sizeof(double) * n);
+    return GF_OK;
+}
+
+static int evalOne(gf_engine *e, int toy, bool grad, double *nll, double *g) {
+    if(!e || !e->has_tree)
+        return gf_fail(e, GF_ERR_STATE, "no tree");
+    if(toy < 0 || toy >= e->n_toys)
+        return gf_fail(e, GF_ERR_INVALID, "toy index out of range");
+    cudaSetDevice(e->device);
+    int rc = buildLayout(e);
+    if(rc)
+        return rc;
+    for(int t = 0; t < e->n_toys; ++t)
+        e->h_active[t] = (t == toy);
+    rc = gf_run(e, grad, -1, 1);
+    if(rc)
+        return rc;
+    const int NGp = 1 + e->tree.NG;
+    const double *o = e->h_out + (size_t)toy * (NGp + 1);
+    if(nll)
+        *nll = o[0];
+    if(grad && g)
+        for(int s = 0; s < e->tree.NG; ++s)
+            g[s] = o[2 + s];
+    int st = statusOf(o[1]);
+    if(st == GF_ERR_NAN_NORM)
+        return gf_fail(e, st, "NaN in normalization");
+    if(st == GF_ERR_NONPOS_NORM)
+        return gf_fail(e, st, "non-positive normalization");
+    if(st == GF_ERR_ZERO_NLL)
+        return gf_fail(e, st, "zero NLL");
+    return GF_OK;
+}
+
+int gf_nll(gf_engine *e, int toy, double *nll) { return evalOne(e, toy, false, nll, nullptr); }
+
+int gf_nll_grad(gf_engine *e, int toy, double *nll, double *grad) { return evalOne(e, toy, true, nll, grad); }
+
+int gf_num_grad(const gf_engine *e) { return e && e->has_tree ? e->tree.NG : 0; }
+int gf_num_params(const gf_engine *e) { return e && e->has_tree ? e->tree.n_params : 0; }
+int gf_num_toys(const gf_engine *e) { return e ? e->n_toys : 0; }
+int gf_grad_params(const gf_engine *e, int32_t *out, int cap) {
+    if(!e || !e->has_tree)
+        return 0;
+    int n = (int)e->tree.gparam.size();
+    for(int s = 0; s < n && s < cap; ++s)
+        out[s] = e->tree.gparam[s];
+    return n;
+}
+
+int gf_nll_batch(gf_engine *e, int n_toys, const double *P, const int32_t *active, double *nll, double *grad) {
+    if(!e || !e->has_tree)
+        return gf_fail(e, GF_ERR_STATE, "no tree");
+    if(n_toys != e->n_toys || !P || !nll)
+        return gf_fail(e, GF_ERR_INVALID, "n_toys must equal the engine's toy count");
+    cudaSetDevice(e->device);
+    int rc = buildLayout(e);
+    if(rc)
+        return rc;
+    const int np = e->tree.n_params, NGp = 1 + e->tree.NG;
+    std::memcpy(e->h_P, P, sizeof(double) * (size_t)n_toys * np);
+    for(int t = 0; t < n_toys; ++t)
+        e->h_active[t] = active ? (active[t] != 0) : 1;
+    rc = gf_run(e, grad != nullptr, -1, 1);
+    if(rc)
+        return rc;
+    int worst = GF_OK;
+    for(int t = 0; t < n_toys; ++t) {
+        if(!e->h_active[t])
+            continue;
+        const double *o = e->h_out + (size_t)t * (NGp + 1);
+        nll[t]          = o[0];
+        if(grad)
+            for(int s = 0; s < e->tree.NG; ++s)
+                grad[(size_t)t * e->tree.NG + s] = o[2 + s];
+        int st = statusOf(o[1]);
+        if(st != GF_OK) {
+            nll[t] = NAN;
+            if(worst == GF_OK)
+                worst = st;
+        }
+    }
+    if(worst != GF_OK)
+        return gf_fail(e, worst, "a toy had an invalid normalisation or zero NLL (its nll is NaN)");
+    return GF_OK;
+}
+
+int gf_normalize(gf_engine *e, int toy, double *integral, double *norm) {
+    if(!e || !e->has_tree)
+        return gf_fail(e, GF_ERR_STATE, "no tree");
+    if(toy < 0 || toy >= e->n_toys)
+        return gf_fail(e, GF_ERR_INVALID, "toy index out of range");
+    cudaSetDevice(e->device);
+    int rc = buildLayout(e);
+    if(rc)
+        return rc;
+    const gf::Tree &T = e->tree;
+    const int NT = e->n_toys, NQ = (int)T.nums.size(), np = T.n_params;
+    for(int t = 0; t < NT; ++t)
+        e->h_active[t] = (t == toy);
+    GfArgs a = makeArgs(e);
+    cudaMemcpyAsync(e->d_P, e->h_P, sizeof(double) * (size_t)NT * std::max(1, np), cudaMemcpyHostToDevice, e->stream);
+    cudaMemcpyAsync(e->d_active, e->h_active, sizeof(int) * NT, cudaMemcpyHostToDevice, e->stream);
+    cudaError_t r = enqueuePrep(e, false, a);
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "normalisation kernels");
+    const int NGs = 1 + T.NG;
+    std::vector<double> gsum((size_t)NT * std::max(1, NQ) * NGs);
+    if(NQ > 0)
+        cudaMemcpyAsync(gsum.data(), e->d_gsum, sizeof(double) * (size_t)NT * NQ * NGs, cudaMemcpyDeviceToHost,
+                        e->stream);
+    r = cudaStreamSynchronize(e->stream);
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "normalisation");
+    const double *P = e->h_P + (size_t)toy * np;
+    const int n     = (int)T.nodes.size();
+    std::vector<double> I(n, 1.0), N(n, 1.0);
+    // forced nodes keep 1; evaluate children before parents
+    std::vector<char> forced(n, 0);
+    for(int i = 0; i < n; ++i) {
+        const gf::TNode &nd = T.nodes[i];
+        bool f = forced[i] || (nd.op == GF_OP_CONVOLUTION) || (nd.op == GF_OP_PROD && T.nk[i] == gf::NK_NUMERIC);
+        for(int c : nd.children)
+            forced[c] = forced[c] || f;
+    }
+    for(int i = n - 1; i >= 0; --i) {
+        const gf::TNode &nd = T.nodes[i];
+        switch(T.nk[i]) {
+        case gf::NK_EXP: {
+            const gf_observable &o = T.obs[nd.obs[0]];
+            double al = P[nd.params[0]];
+            I[i]      = al == 0 ? o.hi - o.lo : (std::exp(al * o.hi) - std::exp(al * o.lo)) / al;
+            N[i]      = 1.0 / I[i];
+            break;
+        }
+        case gf::NK_GAUSS: {
+            double s = P[nd.params[1]];
+            s *= std::sqrt(2.0) * std::sqrt(std::atan2(0.0, -1.0));
+            I[i] = s;
+            N[i] = 1.0 / s;
+            break;
+        }
+        case gf::NK_NUMERIC: {
+            const gf::NumInfo &g = T.nums[T.num_of[i]];
+            double v = 1;
+            v *= g.volume;
+            v /= (double)g.total;
+            v *= gsum[((size_t)toy * NQ + T.num_of[i]) * NGs];
+            I[i] = v;
+            N[i] = 1.0 / v;
+            break;
+        }
+        default:
+            N[i] = 1.0;
+            if(forced[i])
+                I[i] = 1.0;
+            else if(nd.op == GF_OP_ADD || nd.op == GF_OP_ADD_EXT) {
+                double ret = 0, tw = 0;
+                size_t nc  = nd.children.size();
+                for(size_t c = 0; c + 1 < nc; ++c) {
+                    double w = P[nd.params[c]];
+                    tw += w;
+                    ret += I[nd.children[c]] * w;
+                }
+                double last = I[nd.children[nc - 1]];
+                if(nd.op == GF_OP_ADD_EXT) {
+                    double lw = P[nd.params[nc - 1]];
+                    tw += lw;
+                    ret += last * lw;
+                    ret /= tw;
+                } else
+                    ret += (1 - tw) * last;
+                I[i] = ret;
+            } else
+                I[i] = 1.0;
+        }
+    }
+    for(int i = 0; i < n; ++i) {
+        if(integral)
+            integral[i] = I[i];
+        if(norm)
+            norm[i] = N[i];
+    }
+    return GF_OK;
+}
+
+int gf_eval_events(gf_engine *e, int toy, int node, int metric, double *out, int64_t n_out) {
+    if(!e || !e->has_tree)
+        return gf_fail(e, GF_ERR_STATE, "no tree");
+    if(node != 0)
+        return gf_fail(e, GF_ERR_INVALID, "per-event evaluation is defined for the root node; build a tree for a component");
+    if(toy < 0 || toy >= e->n_toys || !out)
+        return gf_fail(e, GF_ERR_INVALID, "bad arguments");
+    cudaSetDevice(e->device);
+    int rc = buildLayout(e);
+    if(rc)
+        return rc;
+    GfToy &ty = e->toys[toy];
+    if(n_out < ty.n)
+        return gf_fail(e, GF_ERR_INVALID, "output array too small");
+    if(e->vals_cap < ty.npad) {
+        dfree(e->d_vals);
+        if(dalloc(e, e->d_vals, (size_t)ty.npad, false))
+            return GF_ERR_OOM;
+        e->vals_cap = ty.npad;
+    }
+    const int NT = e->n_toys, np = e->tree.n_params;
+    for(int t = 0; t < NT; ++t)
+        e->h_active[t] = (t == toy);
+    GfArgs a  = makeArgs(e);
+    a.metric  = metric;
+    cudaMemcpyAsync(e->d_P, e->h_P, sizeof(double) * (size_t)NT * std::max(1, np), cudaMemcpyHostToDevice, e->stream);
+    cudaMemcpyAsync(e->d_active, e->h_active, sizeof(int) * NT, cudaMemcpyHostToDevice, e->stream);
+    cudaError_t r = enqueuePrep(e, false, a);
+    if(r == cudaSuccess)
+        r = launch(e->mod.val_n, dim3(evtGrid(e)), dim3(e->block), e->plan.evt_smem_nograd, e->stream, a);
+    if(r == cudaSuccess && ty.n > 0)
+        r = cudaMemcpyAsync(out, e->d_vals, sizeof(double) * ty.n, cudaMemcpyDeviceToHost, e->stream);
+    if(r == cudaSuccess)
+        r = cudaStreamSynchronize(e->stream);
+    return gf_cuda_check(e, r, "per-event evaluation");
+}
+
+int gf_last_timing(const gf_engine *e, double *ms_total, double *ms_evt) {
+    if(!e)
+        return GF_ERR_INVALID;
+    if(ms_total)
+        *ms_total = e->last_ms_total;
+    if(ms_evt)
+        *ms_evt = e->last_ms_evt;
+    return GF_OK;
+}
+
+int gf_launches_per_eval(const gf_engine *e, int) {
+    if(!e || !e->has_tree)
+        return 0;
+    return 1 + (e->tree.convs.empty() ? 0 : 1) + (e->tree.nums.empty() ? 0 : 1);
+}
+
+int gf_generated_source(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
+                        const int32_t *grad_mask, int precision, char *buf, int64_t cap, int64_t *len) {
+    gf::Tree t;
+    std::string why = t.build(nodes, n_nodes, obs, n_obs, n_params, grad_mask);
+    if(!why.empty())
+        return gf_fail(nullptr, GF_ERR_BAD_TREE, why);
+    gf::KernelPlan p;
+    try {
+        p = gf::generate_kernels(t, precision == GF_MIXED, 256, 8192);
+    } catch(std::exception &ex) {
+        return gf_fail(nullptr, GF_ERR_BAD_TREE, ex.what());
+    }
+    if(len)
+        *len = (int64_t)p.source.size();
+    if(buf && cap > 0) {
+        int64_t m = std::min<int64_t>(cap - 1, (int64_t)p.source.size());
+        std::memcpy(buf, p.source.data(), (size_t)m);
+        buf[m] = 0;
+    }
+    return GF_OK;
+}
+
+int gf_compile_tree(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
+                    const int32_t *grad_mask, int precision, int64_t *cubin_bytes) {
+    gf::Tree t;
+    std::string why = t.build(nodes, n_nodes, obs, n_obs, n_params, grad_mask);
+    if(!why.empty())
+        return gf_fail(nullptr, GF_ERR_BAD_TREE, why);
+    gf::KernelPlan p;
+    try {
+        p = gf::generate_kernels(t, precision == GF_MIXED, 256, 8192);
+    } catch(std::exception &ex) {
+        return gf_fail(nullptr, GF_ERR_BAD_TREE, ex.what());
+    }
+    std::vector<char> cubin;
+    std::string log;
+    if(!gf::rtc_compile(p.source, "sm_103a", cubin, log))
+        return gf_fail(nullptr, GF_ERR_COMPILE, log);
+    if(cubin_bytes)
+        *cubin_bytes = (int64_t)cubin.size();
+    return GF_OK;
+}
+
+} // extern "C"

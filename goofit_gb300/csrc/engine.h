@@ -1,0 +1,105 @@
+// Internal state of a likelihood engine handle.
+#pragma once
+
+#include "../../include/gfengine.h"
+#include "tree.h"
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+struct GfArgs {
+    const double *P;
+    const int *active;
+    const void *const *col;
+    const int *const *kcol;
+    void *ctab;
+    const int *kgrid;
+    double *gsum;
+    double *gpartial;
+    unsigned *gcounter;
+    double *partial;
+    unsigned *counter;
+    double *out;
+    const long long *chunks;
+    const int *toy_chunk0;
+    const int *toy_nchunks;
+    const long long *toy_nevents;
+    double *vals;
+    int n_chunks;
+    int n_toys;
+    int metric;
+    int pad;
+};
+
+struct GfToy {
+    int64_t n    = 0;
+    int64_t npad = 0;
+    void *cols[16] = {nullptr};
+    int *kcols[8]  = {nullptr};
+    bool loaded    = false;
+};
+
+struct GfModule {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t conv_g = nullptr, conv_n = nullptr, grid_g = nullptr, grid_n = nullptr;
+    cudaKernel_t evt_g = nullptr, evt_n = nullptr, val_n = nullptr;
+};
+
+struct gf_engine {
+    int device    = 0;
+    int precision = GF_MIXED;
+    int sm_count  = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    bool has_tree = false;
+    gf::Tree tree;
+    gf::KernelPlan plan;
+    GfModule mod;
+    int block = 256;
+    int chunk = 8192;
+    int evt_ctas_per_sm = 4;
+
+    int n_toys = 1;
+    std::vector<GfToy> toys;
+
+    // device buffers
+    double *d_P = nullptr;
+    int *d_active = nullptr;
+    void **d_cols = nullptr;
+    int **d_kcols = nullptr;
+    void *d_ctab = nullptr;
+    int *d_kgrid = nullptr;
+    double *d_gsum = nullptr, *d_gpartial = nullptr;
+    unsigned *d_gcounter = nullptr;
+    double *d_partial = nullptr;
+    unsigned *d_counter = nullptr;
+    double *d_out = nullptr;
+    long long *d_chunks = nullptr;
+    int *d_toy_chunk0 = nullptr, *d_toy_nchunks = nullptr;
+    long long *d_toy_nevents = nullptr;
+    double *d_vals = nullptr;
+    int64_t vals_cap = 0;
+    double *d_stage = nullptr; // FP64 staging of uploads (grow-only)
+    int64_t stage_cap = 0;
+    int *d_uperr = nullptr;
+    int *h_uperr = nullptr;
+    // pinned host mirrors
+    double *h_P = nullptr;
+    int *h_active = nullptr;
+    double *h_out = nullptr;
+
+    int n_chunks = 0;
+    bool layout_ready = false;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double last_ms_total = 0, last_ms_evt = 0;
+    bool use_graph = true;
+};
+
+// helpers shared between translation units
+int gf_fail(gf_engine *e, int code, const std::string &msg);
+int gf_cuda_check(gf_engine *e, cudaError_t r, const char *what);
+int gf_run(gf_engine *e, bool grad, int metric_values_toy, int metric);

@@ -1,0 +1,320 @@
+// Tree analysis: mirrors the normalisation recursion of the reference
+// (GooPdf::normalize src/PDFs/GooPdf.cu:340-396, AddPdf::normalize
+// src/PDFs/combine/AddPdf.cu:143-185, ProdPdf::normalize
+// src/PDFs/combine/ProdPdf.cu:75-99, ConvolutionPdf::normalize
+// src/PDFs/combine/ConvolutionPdf.cu:313-358) as a static plan, so that every
+// FCN call runs a fixed kernel sequence.
+#include "tree.h"
+
+#include <algorithm>
+#include <set>
+#include <sstream>
+
+namespace gf {
+
+namespace {
+
+std::vector<int> merge(const std::vector<int> &a, const std::vector<int> &b) {
+    std::vector<int> r;
+    std::set_union(a.begin(), a.end(), b.begin(), b.end(), std::back_inserter(r));
+    return r;
+}
+
+bool isExpOp(int op) {
+    return op == GF_OP_EXP || op == GF_OP_EXP_OFFSET || op == GF_OP_EXP_POLY || op == GF_OP_EXP_POLY_OFFSET;
+}
+
+} // namespace
+
+std::vector<int> Tree::subtreeObs(int i) const {
+    std::vector<int> r = nodes[i].obs;
+    for(int c : nodes[i].children)
+        for(int o : subtreeObs(c))
+            if(std::find(r.begin(), r.end(), o) == r.end())
+                r.push_back(o);
+    return r;
+}
+
+bool Tree::inSubtree(int root, int i) const {
+    if(root == i)
+        return true;
+    for(int c : nodes[root].children)
+        if(inSubtree(c, i))
+            return true;
+    return false;
+}
+
+// ProdPdf::ProdPdf overlap detection (src/PDFs/combine/ProdPdf.cu:28-68): each
+// component is compared with the previous one; separateNorm cancels it.
+bool Tree::prodOverlaps(int i) const {
+    bool over = false;
+    std::vector<int> check;
+    for(int c : nodes[i].children) {
+        if(over)
+            continue;
+        std::vector<int> cur = subtreeObs(c);
+        for(int o : cur)
+            if(std::find(check.begin(), check.end(), o) != check.end()) {
+                over = true;
+                break;
+            }
+        check = cur;
+    }
+    if(over)
+        for(int c : nodes[i].children)
+            if(nodes[c].flags & GF_FLAG_SEPARATE_NORM)
+                over = false;
+    return over;
+}
+
+std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob, int n_obs, int np,
+                        const int32_t *grad_mask) {
+    std::ostringstream err;
+    if(n_nodes <= 0 || !in)
+        return "empty tree";
+    if(n_obs <= 0 || n_obs > 16 || !ob)
+        return "observable count must be 1..16";
+    if(np < 0)
+        return "negative parameter count";
+    nodes.assign(n_nodes, TNode());
+    obs.assign(ob, ob + n_obs);
+    n_params = np;
+    for(int o = 0; o < n_obs; ++o)
+        if(!(obs[o].hi > obs[o].lo) || obs[o].nbins <= 0)
+            return "observable " + std::to_string(o) + " needs lo < hi and nbins > 0";
+    for(int i = 0; i < n_nodes; ++i) {
+        const gf_node &g = in[i];
+        TNode &n         = nodes[i];
+        if(g.n_params < 0 || g.n_consts < 0 || g.n_obs < 0 || g.n_children < 0)
+            return "node " + std::to_string(i) + ": negative count";
+        n.op    = g.op;
+        n.flags = g.flags;
+        n.params.assign(g.params, g.params + g.n_params);
+        n.consts.assign(g.consts, g.consts + g.n_consts);
+        n.obs.assign(g.obs, g.obs + g.n_obs);
+        n.children.assign(g.children, g.children + g.n_children);
+        n.ibins = g.integration_bins;
+        for(int p : n.params)
+            if(p < 0 || p >= np)
+                return "node " + std::to_string(i) + ": parameter index out of range";
+        for(int o : n.obs)
+            if(o < 0 || o >= n_obs)
+                return "node " + std::to_string(i) + ": observable index out of range";
+        for(int c : n.children)
+            if(c <= i || c >= n_nodes)
+                return "node " + std::to_string(i) + ": children must follow their parent";
+    }
+    // per-op arity
+    for(int i = 0; i < n_nodes; ++i) {
+        const TNode &n = nodes[i];
+        size_t P = n.params.size(), C = n.children.size();
+        bool ok  = true;
+        switch(n.op) {
+        case GF_OP_EXP: ok = P == 1 && n.obs.size() == 1 && C == 0; break;
+        case GF_OP_EXP_OFFSET: ok = P == 2 && n.obs.size() == 1 && C == 0; break;
+        case GF_OP_EXP_POLY: ok = P >= 1 && n.obs.size() == 1 && C == 0; break;
+        case GF_OP_EXP_POLY_OFFSET: ok = P >= 2 && n.obs.size() == 1 && C == 0; break;
+        case GF_OP_GAUSSIAN: ok = P == 2 && n.obs.size() == 1 && C == 0; break;
+        case GF_OP_POLYNOMIAL:
+        case GF_OP_POLYNOMIAL_OFFSET: ok = P >= 1 && n.consts.size() >= 1 && n.obs.size() == 1 && C == 0; break;
+        case GF_OP_ADD: ok = C >= 2 && P + 1 == C; break;
+        case GF_OP_ADD_EXT: ok = C >= 1 && P == C; break;
+        case GF_OP_PROD: ok = C >= 1; break;
+        case GF_OP_CONVOLUTION: ok = C == 2 && n.consts.size() >= 3 && n.obs.size() >= 1 && n.consts[2] > 0; break;
+        default: return "node " + std::to_string(i) + ": operator " + std::to_string(n.op) + " not supported";
+        }
+        if(!ok)
+            return "node " + std::to_string(i) + ": wrong arity for operator " + std::to_string(n.op);
+        if(n.flags & GF_FLAG_COMMON_NORM)
+            return "node " + std::to_string(i) + ": setCommonNorm is not supported by the engine";
+    }
+    // every node reachable exactly once from the root
+    {
+        std::vector<int> seen(n_nodes, 0);
+        std::vector<int> stack{0};
+        while(!stack.empty()) {
+            int i = stack.back();
+            stack.pop_back();
+            if(seen[i]++)
+                return "node " + std::to_string(i) + " is shared; each PdfBase object may appear once";
+            for(int c : nodes[i].children)
+                stack.push_back(c);
+        }
+        for(int i = 0; i < n_nodes; ++i)
+            if(!seen[i])
+                return "node " + std::to_string(i) + " is not reachable from the root";
+    }
+    extended_root = nodes[0].op == GF_OP_ADD_EXT;
+
+    // gradient slots
+    gslot.assign(np, -1);
+    gparam.clear();
+    for(int p = 0; p < np; ++p)
+        if(grad_mask && grad_mask[p]) {
+            gslot[p] = (int)gparam.size();
+            gparam.push_back(p);
+        }
+    NG = (int)gparam.size();
+
+    // normalisation plan
+    nk.assign(n_nodes, NK_ONE);
+    std::vector<std::pair<int, bool>> st{{0, false}};
+    while(!st.empty()) {
+        auto [i, forced] = st.back();
+        st.pop_back();
+        const TNode &n = nodes[i];
+        bool childForced = forced;
+        if(forced) {
+            nk[i] = NK_ONE;
+        } else if(n.op == GF_OP_ADD || n.op == GF_OP_ADD_EXT) {
+            nk[i] = NK_ONE;
+        } else if(n.op == GF_OP_PROD) {
+            if(prodOverlaps(i)) {
+                nk[i]       = NK_NUMERIC;
+                childForced = true;
+            } else
+                nk[i] = NK_ONE;
+        } else if(n.op == GF_OP_CONVOLUTION) {
+            nk[i]       = NK_NUMERIC;
+            childForced = true;
+        } else if(isExpOp(n.op) && n.params.size() == 1) {
+            nk[i] = NK_EXP;
+        } else if(n.op == GF_OP_GAUSSIAN) {
+            nk[i] = NK_GAUSS;
+        } else {
+            nk[i] = NK_NUMERIC;
+        }
+        for(int c : n.children)
+            st.push_back({c, childForced});
+    }
+
+    // gradient dependencies (children have larger indices: iterate backwards)
+    dep_val.assign(n_nodes, {});
+    dep_norm.assign(n_nodes, {});
+    for(int i = n_nodes - 1; i >= 0; --i) {
+        const TNode &n = nodes[i];
+        std::vector<int> own;
+        for(int p : n.params)
+            if(gslot[p] >= 0)
+                own.push_back(gslot[p]);
+        std::sort(own.begin(), own.end());
+        own.erase(std::unique(own.begin(), own.end()), own.end());
+        std::vector<int> v = own;
+        for(int c : n.children)
+            v = merge(v, merge(dep_val[c], dep_norm[c]));
+        if(n.op == GF_OP_POLYNOMIAL_OFFSET) {
+            // device_OffsetPolynomial reads parameters 2..nP-1 only
+            std::vector<int> used;
+            for(size_t k = 2; k < n.params.size(); ++k)
+                if(gslot[n.params[k]] >= 0)
+                    used.push_back(gslot[n.params[k]]);
+            std::sort(used.begin(), used.end());
+            used.erase(std::unique(used.begin(), used.end()), used.end());
+            v = used;
+        }
+        dep_val[i] = v;
+        if(nk[i] == NK_EXP) {
+            int s = gslot[n.params[0]];
+            if(s >= 0)
+                dep_norm[i] = {s};
+        } else if(nk[i] == NK_GAUSS) {
+            int s = gslot[n.params[1]];
+            if(s >= 0)
+                dep_norm[i] = {s};
+        } else if(nk[i] == NK_NUMERIC) {
+            dep_norm[i] = v;
+        }
+    }
+
+    // convolutions
+    conv_of.assign(n_nodes, -1);
+    convs.clear();
+    for(int i = 0; i < n_nodes; ++i) {
+        const TNode &n = nodes[i];
+        if(n.op != GF_OP_CONVOLUTION)
+            continue;
+        ConvInfo c;
+        c.node  = i;
+        c.model = n.children[0];
+        c.resol = n.children[1];
+        c.obs   = n.obs[0];
+        c.lo    = n.consts[0];
+        c.hi    = n.consts[1];
+        c.step  = n.consts[2];
+        const gf_observable &dep = obs[c.obs];
+        c.nM    = (int)std::floor((c.hi - c.lo) / c.step + 0.5);
+        c.ic[0] = c.lo;
+        c.ic[1] = c.hi;
+        c.ic[2] = c.nM;
+        c.ic[3] = c.lo - dep.hi;
+        c.ic[4] = c.hi - dep.lo;
+        c.nR    = (int)std::floor((c.ic[4] - c.ic[3]) / c.step + 0.5);
+        c.ic[5] = c.nR;
+        c.offset = (int)(dep.hi / c.step);
+        c.kmin   = conv_offset_in_bins(dep.lo, c.lo, c.step);
+        c.kmax   = conv_offset_in_bins(dep.hi, c.lo, c.step);
+        c.nK     = c.kmax - c.kmin + 1;
+        if(c.nM <= 0 || c.nR <= 0 || c.nK <= 0)
+            return "convolution node " + std::to_string(i) + ": empty workspace";
+        if(c.offset - c.kmax < 0 || c.nM - 1 + c.offset - c.kmin >= c.nR)
+            return "convolution node " + std::to_string(i) + ": resolution workspace index leaves its range";
+        for(int sub : {c.model, c.resol}) {
+            std::vector<int> so = subtreeObs(sub);
+            if(so.size() != 1)
+                return "convolution node " + std::to_string(i) + ": model and resolution must use one observable";
+            for(int j = sub; j < n_nodes; ++j)
+                if(inSubtree(sub, j) && nodes[j].op == GF_OP_CONVOLUTION)
+                    return "nested ConvolutionPdf is not supported";
+        }
+        c.dep = merge(dep_val[c.model], dep_val[c.resol]);
+        conv_of[i] = (int)convs.size();
+        convs.push_back(c);
+    }
+    if(convs.size() > 8)
+        return "at most 8 ConvolutionPdf nodes per tree";
+
+    // numeric grids
+    num_of.assign(n_nodes, -1);
+    nums.clear();
+    kgrid.clear();
+    for(int i = 0; i < n_nodes; ++i) {
+        if(nk[i] != NK_NUMERIC)
+            continue;
+        NumInfo g;
+        g.node = i;
+        g.obs  = nodes[i].obs;
+        if(g.obs.empty())
+            return "numerically normalised node " + std::to_string(i) + " has no observables";
+        for(int o : g.obs) {
+            int nb = nodes[i].ibins > 0 ? nodes[i].ibins : obs[o].nbins;
+            g.nbins.push_back(nb);
+            g.total *= nb;
+            g.volume *= obs[o].hi - obs[o].lo;
+        }
+        if(g.total > (int64_t)1 << 31)
+            return "numeric grid too large";
+        for(size_t c = 0; c < convs.size(); ++c) {
+            if(!inSubtree(i, convs[c].node))
+                continue;
+            int axis = -1;
+            for(size_t a = 0; a < g.obs.size(); ++a)
+                if(g.obs[a] == convs[c].obs)
+                    axis = (int)a;
+            if(axis < 0)
+                return "convolution observable missing from the grid of node " + std::to_string(i);
+            g.convs.push_back((int)c);
+            g.conv_axis.push_back(axis);
+            g.kgrid_off.push_back((int64_t)kgrid.size());
+            const gf_observable &o = obs[g.obs[axis]];
+            for(int b = 0; b < g.nbins[axis]; ++b) {
+                double x = bin_centre(o.lo, o.hi, g.nbins[axis], b);
+                kgrid.push_back(conv_offset_in_bins(x, convs[c].lo, convs[c].step));
+            }
+        }
+        num_of[i] = (int)nums.size();
+        nums.push_back(g);
+    }
+    return "";
+}
+
+} // namespace gf

@@ -1,0 +1,114 @@
+// Tree analysis for the likelihood engine: normalisation plan, gradient
+// dependencies, convolution geometry and numeric-grid layout of one PDF tree.
+#pragma once
+
+#include "../../include/gfengine.h"
+
+#include <cmath>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace gf {
+
+// How a node's normalisation factor is obtained on every FCN call.
+enum NormKind {
+    NK_ONE     = 0, // combine nodes (AddPdf/ProdPdf) and subtrees forced to 1 by
+                    // recursiveSetNormalization (src/goofit/PdfBase.cpp:29-38)
+    NK_EXP     = 1, // ExpPdf::integrate        (src/PDFs/basic/ExpPdf.cu:121-132)
+    NK_GAUSS   = 2, // GaussianPdf::integrate   (src/PDFs/basic/GaussianPdf.cu:28-35)
+    NK_NUMERIC = 3  // grid sum                 (src/PDFs/GooPdf.cu:366-395)
+};
+
+struct TNode {
+    int op = 0, flags = 0;
+    std::vector<int> params;
+    std::vector<double> consts;
+    std::vector<int> obs;
+    std::vector<int> children;
+    int ibins = 0;
+};
+
+// Geometry of one ConvolutionPdf (src/PDFs/combine/ConvolutionPdf.cu:228-282).
+struct ConvInfo {
+    int node = -1, model = -1, resol = -1, obs = -1;
+    double lo = 0, hi = 0, step = 0;
+    double ic[6]  = {0, 0, 0, 0, 0, 0}; // host_iConsts
+    int nM = 0, nR = 0, offset = 0;
+    int kmin = 0, kmax = 0, nK = 0; // bin-offset range of x in [obs.lo, obs.hi]
+    std::vector<int> dep;           // gradient slots the table depends on
+};
+
+// One numerically normalised node: grid over its observables.
+struct NumInfo {
+    int node = -1;
+    std::vector<int> obs;
+    std::vector<int> nbins;
+    int64_t total  = 1;
+    double volume  = 1;
+    std::vector<int> convs;       // conv nodes inside the subtree
+    std::vector<int> conv_axis;   // axis of each conv's observable in this grid
+    std::vector<int64_t> kgrid_off; // offset of each conv's per-axis-bin k table in the kgrid buffer
+};
+
+struct Tree {
+    std::vector<TNode> nodes;
+    std::vector<gf_observable> obs;
+    int n_params = 0;
+    std::vector<int> gslot; // parameter -> gradient slot or -1
+    std::vector<int> gparam; // gradient slot -> parameter
+    int NG = 0;
+
+    std::vector<int> nk;
+    std::vector<std::vector<int>> dep_val, dep_norm; // sorted gradient slots
+    std::vector<ConvInfo> convs;
+    std::vector<int> conv_of; // node -> index in convs or -1
+    std::vector<NumInfo> nums;
+    std::vector<int> num_of; // node -> index in nums or -1
+    std::vector<int> kgrid;  // host copy of all grid k tables
+    bool extended_root = false;
+
+    // Returns "" on success, else the reason the tree is rejected.
+    std::string build(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
+                      const int32_t *grad_mask);
+
+    std::vector<int> subtreeObs(int i) const;
+    bool inSubtree(int root, int i) const;
+    bool prodOverlaps(int i) const;
+};
+
+// ConvolutionPdf bin offset of x (src/PDFs/combine/ConvolutionPdf.cu:40-43), in FP64.
+inline int conv_offset_in_bins(double x0, double loBound, double step) {
+    double lowerBoundOffset = loBound / step;
+    lowerBoundOffset -= std::floor(lowerBoundOffset);
+    return (int)std::floor(x0 / step - lowerBoundOffset);
+}
+
+// Bin centre of the binned MetricTaker (src/PDFs/MetricTaker.cu:76-82), in FP64.
+inline double bin_centre(double lo, double hi, int nbins, int b) {
+    double x = hi - lo;
+    x /= nbins;
+    x *= (b + 0.5);
+    x += lo;
+    return x;
+}
+
+// Generates the CUDA source of the fused kernel set for a tree.
+struct KernelPlan {
+    std::string source;
+    size_t evt_smem_grad = 0, evt_smem_nograd = 0; // dynamic shared memory of the event kernels
+    size_t conv_smem_grad = 0, conv_smem_nograd = 0;
+    int conv_tk = 64;      // table entries per conv CTA
+    int conv_blocks = 0;   // CTAs per (toy, conv) of the table kernel
+    int grid_bins_per_block = 1024;
+    std::vector<int> grid_blocks; // per numeric node
+    int max_grid_blocks = 0;
+    int64_t ctab_per_toy_grad = 0, ctab_per_toy_nograd = 0; // table elements per toy
+    std::vector<int64_t> ctab_off_grad, ctab_off_nograd;    // per conv
+    std::vector<int> ctab_comps_grad;                       // per conv
+    std::vector<int> obs_used_evt;                          // observables the event kernel loads
+};
+
+KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, int chunk);
+
+} // namespace gf

@@ -1,0 +1,275 @@
+"""Object wrapper over the engine C ABI (include/gfengine.h).
+
+`Engine` owns one gf_engine handle: a PDF tree (node list), its datasets
+("toys") resident in HBM and the generated kernels.  `Minimizer` exposes the
+ask/tell minimiser.  Everything here calls libgfengine.so; there is no CPU
+path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi as A
+
+PRECISIONS = {"fp64": A.GF_FP64, "mixed": A.GF_MIXED}
+
+
+@dataclass
+class FitResult:
+    """Outcome of one MIGRAD fit (the FunctionMinimum fields the reference reads)."""
+    values: np.ndarray
+    errors: np.ndarray
+    fmin: float
+    edm: float
+    nfcn: int
+    ngrad: int
+    valid: bool
+    above_max_edm: bool
+    call_limit: bool
+    has_covariance: bool
+    hesse_failed: bool
+    made_posdef: bool
+    n_iter: int
+
+    @staticmethod
+    def from_c(r: A.gf_fit_result, x, e) -> "FitResult":
+        return FitResult(np.array(x, dtype=float), np.array(e, dtype=float), r.fmin, r.edm, r.nfcn, r.ngrad,
+                         bool(r.valid), bool(r.above_max_edm), bool(r.call_limit), bool(r.has_covariance),
+                         bool(r.hesse_failed), bool(r.made_posdef), r.n_iter)
+
+    # Minuit2::FunctionMinimum spellings used by GooFit users
+    def IsValid(self) -> bool:
+        return self.valid
+
+    def Fval(self) -> float:
+        return self.fmin
+
+    def Edm(self) -> float:
+        return self.edm
+
+    def NFcn(self) -> int:
+        return self.nfcn
+
+
+def _fit_options(n, err, lo, hi, limited, fixed, up, tolerance, strategy, maxfcn, use_grad):
+    keep = []
+
+    def f(a):
+        arr, p = A.f64(a)
+        keep.append(arr)
+        return p
+
+    def i(a):
+        arr, p = A.i32(a)
+        keep.append(arr)
+        return p
+
+    o = A.gf_fit_options()
+    o.err = f(err)
+    o.lo = f(lo)
+    o.hi = f(hi)
+    o.limited = i(limited)
+    o.fixed = i(fixed)
+    o.up = up
+    o.tolerance = tolerance
+    o.strategy = strategy
+    o.maxfcn = maxfcn
+    o.use_grad = 1 if use_grad else 0
+    return o, keep
+
+
+class Engine:
+    """One likelihood engine on one GPU."""
+
+    def __init__(self, precision: str = "mixed", device: int = 0):
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {list(PRECISIONS)}")
+        self.precision = precision
+        self._h = C.c_void_p()
+        self._L = A.lib()
+        A.check(self._L.gf_engine_create(C.byref(self._h), device, PRECISIONS[precision]))
+        self.n_params = 0
+        self.n_grad = 0
+        self.grad_params: list[int] = []
+        self.n_obs = 0
+        self.n_toys = 1
+        self._n_events: dict[int, int] = {}
+
+    def close(self) -> None:
+        if self._h:
+            self._L.gf_engine_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int) -> None:
+        A.check(rc, self._h)
+
+    # ---- tree / data ----
+    def set_tree(self, nodes: list[dict], observables: list[tuple], n_params: int, grad_mask=None) -> None:
+        self._nodes = A.NodeList(nodes)
+        self._obs = A.observables_array(observables)
+        mask = np.zeros(max(n_params, 1), dtype=np.int32) if grad_mask is None else np.asarray(grad_mask, np.int32)
+        marr, mp = A.i32(mask)
+        self._check(self._L.gf_set_tree(self._h, self._nodes.arr, self._nodes.n, self._obs, len(observables),
+                                        n_params, mp))
+        self.n_params = n_params
+        self.n_obs = len(observables)
+        self.n_grad = self._L.gf_num_grad(self._h)
+        buf = (C.c_int32 * max(1, self.n_grad))()
+        self._L.gf_grad_params(self._h, buf, self.n_grad)
+        self.grad_params = [buf[i] for i in range(self.n_grad)]
+        self.n_toys = 1
+        self._n_events = {}
+
+    def set_num_toys(self, n: int) -> None:
+        self._check(self._L.gf_set_num_toys(self._h, n))
+        self.n_toys = n
+        self._n_events = {}
+
+    def upload(self, soa: np.ndarray, toy: int = 0) -> None:
+        """soa: (n_obs, n_events) float64 array (or 1-D for one observable)."""
+        a = np.asarray(soa, dtype=np.float64)
+        if a.ndim == 1:
+            a = a.reshape(1, -1)
+        if a.shape[0] != self.n_obs:
+            raise ValueError(f"expected {self.n_obs} observable rows, got {a.shape[0]}")
+        arr, p = A.f64(a)
+        self._check(self._L.gf_upload_events(self._h, toy, p, a.shape[1]))
+        self._n_events[toy] = a.shape[1]
+
+    # ---- evaluation ----
+    def set_params(self, params, toy: int = 0) -> None:
+        arr, p = A.f64(params)
+        self._check(self._L.gf_set_params(self._h, toy, p, len(arr)))
+
+    def nll(self, params=None, toy: int = 0) -> float:
+        if params is not None:
+            self.set_params(params, toy)
+        out = C.c_double()
+        self._check(self._L.gf_nll(self._h, toy, C.byref(out)))
+        return out.value
+
+    def nll_grad(self, params=None, toy: int = 0) -> tuple[float, np.ndarray]:
+        if params is not None:
+            self.set_params(params, toy)
+        out = C.c_double()
+        g = np.zeros(max(1, self.n_grad))
+        self._check(self._L.gf_nll_grad(self._h, toy, C.byref(out), g.ctypes.data_as(A._f64p)))
+        return out.value, g[: self.n_grad]
+
+    def nll_batch(self, P: np.ndarray, active=None, grad: bool = False):
+        P = np.ascontiguousarray(P, dtype=np.float64).reshape(self.n_toys, self.n_params)
+        nll = np.zeros(self.n_toys)
+        G = np.zeros((self.n_toys, max(1, self.n_grad))) if grad else None
+        act = None if active is None else np.ascontiguousarray(active, dtype=np.int32)
+        rc = self._L.gf_nll_batch(self._h, self.n_toys, P.ctypes.data_as(A._f64p),
+                                  None if act is None else act.ctypes.data_as(A._i32p),
+                                  nll.ctypes.data_as(A._f64p), None if G is None else G.ctypes.data_as(A._f64p))
+        self._check(rc)
+        return (nll, G[:, : self.n_grad]) if grad else nll
+
+    def normalize(self, toy: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        n = self._nodes.n
+        I = np.zeros(n)
+        N = np.zeros(n)
+        self._check(self._L.gf_normalize(self._h, toy, I.ctypes.data_as(A._f64p), N.ctypes.data_as(A._f64p)))
+        return I, N
+
+    def eval_events(self, metric: int = A.GF_METRIC_PROB, toy: int = 0) -> np.ndarray:
+        n = self._n_events.get(toy, 0)
+        out = np.zeros(max(1, n))
+        self._check(self._L.gf_eval_events(self._h, toy, 0, metric, out.ctypes.data_as(A._f64p), n))
+        return out[:n]
+
+    def last_timing(self) -> tuple[float, float]:
+        a, b = C.c_double(), C.c_double()
+        self._L.gf_last_timing(self._h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def launches_per_eval(self, grad: bool = True) -> int:
+        return self._L.gf_launches_per_eval(self._h, 1 if grad else 0)
+
+    # ---- fits ----
+    def fit(self, x0, err, lo, hi, limited, fixed, *, up=0.5, tolerance=0.1, strategy=1, maxfcn=0,
+            use_grad=True, toy: int = 0) -> FitResult:
+        n = self.n_params
+        o, keep = _fit_options(n, err, lo, hi, limited, fixed, up, tolerance, strategy, maxfcn, use_grad)
+        xa, xp = A.f64(x0)
+        x = np.zeros(n)
+        e = np.zeros(n)
+        r = A.gf_fit_result()
+        self._check(self._L.gf_fit(self._h, toy, C.byref(o), xp, x.ctypes.data_as(A._f64p),
+                                   e.ctypes.data_as(A._f64p), C.byref(r)))
+        return FitResult.from_c(r, x, e)
+
+    def fit_batch(self, X0, err, lo, hi, limited, fixed, *, up=0.5, tolerance=0.1, strategy=1, maxfcn=0,
+                  use_grad=True) -> list[FitResult]:
+        n = self.n_params
+        T = self.n_toys
+        o, keep = _fit_options(n, err, lo, hi, limited, fixed, up, tolerance, strategy, maxfcn, use_grad)
+        X0 = np.ascontiguousarray(X0, dtype=np.float64).reshape(T, n)
+        X = np.zeros((T, n))
+        E = np.zeros((T, n))
+        R = (A.gf_fit_result * T)()
+        self._check(self._L.gf_fit_batch(self._h, T, C.byref(o), X0.ctypes.data_as(A._f64p),
+                                         X.ctypes.data_as(A._f64p), E.ctypes.data_as(A._f64p), R))
+        return [FitResult.from_c(R[t], X[t], E[t]) for t in range(T)]
+
+
+class Minimizer:
+    """Ask/tell MIGRAD (same code the native fit loop uses)."""
+
+    def __init__(self, x0, err, lo=None, hi=None, limited=None, fixed=None, *, up=0.5, strategy=1, tolerance=0.1,
+                 maxfcn=0, use_grad=False):
+        n = len(x0)
+        self.n = n
+        self._L = A.lib()
+        self._h = C.c_void_p()
+        z = np.zeros(n)
+        arrs = [A.f64(x0), A.f64(err), A.f64(z if lo is None else lo), A.f64(z if hi is None else hi),
+                A.i32(np.zeros(n, np.int32) if limited is None else limited),
+                A.i32(np.zeros(n, np.int32) if fixed is None else fixed)]
+        self._keep = [a for a, _ in arrs]
+        A.check(self._L.gf_minimizer_create(C.byref(self._h), n, *[p for _, p in arrs], up, strategy, tolerance,
+                                            maxfcn, 1 if use_grad else 0))
+
+    def minimize(self, fcn, grad=None) -> FitResult:
+        """fcn(x) -> float; grad(x) -> array (needed if use_grad)."""
+        x = np.zeros(self.n)
+        need = C.c_int32()
+        while self._L.gf_minimizer_ask(self._h, x.ctypes.data_as(A._f64p), C.byref(need)) == 1:
+            f = float(fcn(x.copy()))
+            if need.value:
+                g = np.ascontiguousarray(grad(x.copy()), dtype=np.float64)
+                self._L.gf_minimizer_tell(self._h, f, g.ctypes.data_as(A._f64p))
+            else:
+                self._L.gf_minimizer_tell(self._h, f, None)
+        return self.result()
+
+    def result(self) -> FitResult:
+        r = A.gf_fit_result()
+        x = np.zeros(self.n)
+        e = np.zeros(self.n)
+        self._L.gf_minimizer_result(self._h, C.byref(r), x.ctypes.data_as(A._f64p), e.ctypes.data_as(A._f64p), None)
+        return FitResult.from_c(r, x, e)
+
+    def covariance(self) -> np.ndarray:
+        r = A.gf_fit_result()
+        cov = np.zeros((self.n, self.n))
+        self._L.gf_minimizer_result(self._h, C.byref(r), None, None, cov.ctypes.data_as(A._f64p))
+        return cov
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._L.gf_minimizer_destroy(self._h)
+        except Exception:
+            pass

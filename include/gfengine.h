@@ -1,0 +1,235 @@
+/*
+ * gfengine.h — C ABI of the GB300 likelihood engine (libgfengine.so).
+ *
+ * This is the drop-in boundary for GooFit's fit path.  In the reference every
+ * PDF registers a device function pointer (`device_function_ptr`,
+ * include/goofit/PDFs/detail/Globals.h:12) into a process-global table that a
+ * Thrust functor (MetricTaker, src/PDFs/MetricTaker.cu:17-44) calls per event,
+ * and the host drives it through PdfBase/GooPdf (`setData`
+ * src/PDFs/PdfBase.cu:329-438, `normalize` src/PDFs/GooPdf.cu:340-396,
+ * `calculateNLL` src/PDFs/GooPdf.cu:254-273) and Minuit2 (`FCN::operator()`
+ * src/goofit/FCN.cpp:18-28).
+ *
+ * Here a PDF tree is handed over once as a flat node list (`gf_node`, one
+ * entry per PdfBase object in the same depth-first order that
+ * PdfBase::populateArrays flattens it, src/PDFs/PdfBase.cu:268-311).  The
+ * engine generates one fused kernel set for that tree, keeps events resident
+ * in HBM as structure-of-arrays columns, and answers NLL / gradient queries.
+ *
+ * Conventions: every function returns GF_OK (0) or a gf_status code and never
+ * throws or aborts; gf_last_error() gives the message.  Host arrays are
+ * caller-owned and copied.  Sizes are element counts.
+ */
+#ifndef GFENGINE_H
+#define GFENGINE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (GooFit::abort sites: src/PDFs/GooPdf.cu:260-271,381-391) ---- */
+enum gf_status {
+    GF_OK              = 0,
+    GF_ERR_INVALID     = 1,  /* bad argument / size / index */
+    GF_ERR_CUDA        = 2,  /* CUDA runtime error */
+    GF_ERR_COMPILE     = 3,  /* runtime code generation failed */
+    GF_ERR_NAN_NORM    = 4,  /* "NaN in normalization" */
+    GF_ERR_NONPOS_NORM = 5,  /* "non-positive normalization" */
+    GF_ERR_ZERO_NLL    = 6,  /* "zero NLL" */
+    GF_ERR_OOM         = 7,
+    GF_ERR_TIMEOUT     = 8,
+    GF_ERR_BAD_TREE    = 9,
+    GF_ERR_STATE       = 10, /* call order (no tree / no data) */
+    GF_ERR_NO_DEVICE   = 11
+};
+
+/* ---- arithmetic of the per-event path ---- */
+enum gf_precision {
+    GF_FP64  = 0, /* every event, workspace and reduction in FP64 (the plain path) */
+    GF_MIXED = 1  /* FP32 events and per-event PDF math, FP64 reductions and normalisations */
+};
+
+/* ---- node operators: one per reference device function ---- */
+enum gf_op {
+    GF_OP_EXP               = 1,  /* device_Exp            src/PDFs/basic/ExpPdf.cu:7-17      params [alpha] */
+    GF_OP_EXP_OFFSET        = 2,  /* device_ExpOffset      src/PDFs/basic/ExpPdf.cu:19-30     params [x0, alpha] */
+    GF_OP_EXP_POLY          = 3,  /* device_ExpPoly        src/PDFs/basic/ExpPdf.cu:32-46     params [w0..wn] */
+    GF_OP_EXP_POLY_OFFSET   = 4,  /* device_ExpPolyOffset  src/PDFs/basic/ExpPdf.cu:48-63     params [x0, w..] */
+    GF_OP_GAUSSIAN          = 5,  /* device_Gaussian       src/PDFs/basic/GaussianPdf.cu:7-17 params [mean, sigma] */
+    GF_OP_POLYNOMIAL        = 6,  /* device_Polynomial     src/PDFs/basic/PolynomialPdf.cu:8-26  consts [lowestDegree] params [c..] */
+    GF_OP_POLYNOMIAL_OFFSET = 7,  /* device_OffsetPolynomial src/PDFs/basic/PolynomialPdf.cu:28-44 consts [lowestDegree] params [c.., x0] */
+    GF_OP_ADD               = 8,  /* device_AddPdfs        src/PDFs/combine/AddPdf.cu:16-51   params [f1..f(n-1)] children n */
+    GF_OP_ADD_EXT           = 9,  /* device_AddPdfsExt     src/PDFs/combine/AddPdf.cu:53-80   params [N1..Nn] children n */
+    GF_OP_PROD              = 10, /* device_ProdPdfs       src/PDFs/combine/ProdPdf.cu:9-26   consts [nComps] children n */
+    GF_OP_CONVOLUTION       = 11, /* device_ConvolvePdfs   src/PDFs/combine/ConvolutionPdf.cu:27-75 consts [lo, hi, step] children [model, resolution] */
+    GF_OP_AMP3BODY          = 12, /* device_DalitzPlot     src/PDFs/physics/Amp3Body.cu:60-122 (see gfengine_amp.h) */
+    GF_OP_AMP4BODY          = 13  /* device_DP             src/PDFs/physics/Amp4Body.cu:53-90  (see gfengine_amp.h) */
+};
+
+/* node flags */
+#define GF_FLAG_COMMON_NORM   1 /* PdfBase::setCommonNorm   include/goofit/PdfBase.h:228 */
+#define GF_FLAG_SEPARATE_NORM 2 /* PdfBase::setSeparateNorm include/goofit/PdfBase.h:229 */
+
+/* One PdfBase object.  `params` index the engine parameter vector (one slot
+ * per distinct Variable), `obs` index the observable columns, `children`
+ * index this node list (children always come after their parent). */
+typedef struct gf_node {
+    int32_t op;
+    int32_t flags;
+    int32_t n_params;
+    int32_t n_consts;
+    int32_t n_obs;
+    int32_t n_children;
+    const int32_t *params;
+    const double *consts;
+    const int32_t *obs;
+    const int32_t *children;
+    int32_t integration_bins; /* PdfBase::setIntegrationFineness, 0 = observable bins */
+    int32_t reserved;
+} gf_node;
+
+/* One Observable (include/goofit/Variable.h:109-140). */
+typedef struct gf_observable {
+    double lo;
+    double hi;
+    int32_t nbins;
+    int32_t is_event_number;
+} gf_observable;
+
+/* What a per-event evaluation returns (include/goofit/FitControl.h:11). */
+enum gf_metric { GF_METRIC_EVAL = 0, GF_METRIC_NLL = 1, GF_METRIC_PROB = 2 };
+
+typedef struct gf_engine gf_engine;
+
+/* ---- engine lifetime ---- */
+int gf_engine_create(gf_engine **out, int device, int precision);
+int gf_engine_destroy(gf_engine *eng);
+const char *gf_last_error(const gf_engine *eng);
+const char *gf_version(void);
+
+/* ---- tree and data (PdfBase::setIndices / setData, src/PDFs/PdfBase.cu:313-438) ---- */
+/* n_params: length of the parameter vector.  grad_mask[n_params] (may be NULL)
+ * marks the parameters that get an analytic derivative. */
+int gf_set_tree(gf_engine *eng,
+                const gf_node *nodes,
+                int n_nodes,
+                const gf_observable *obs,
+                int n_obs,
+                int n_params,
+                const int32_t *grad_mask);
+
+/* Number of independent datasets ("toys"), each with its own parameter vector. */
+int gf_set_num_toys(gf_engine *eng, int n_toys);
+
+/* Events of one toy as SoA FP64 columns: soa[o * n_events + e]. */
+int gf_upload_events(gf_engine *eng, int toy, const double *soa, int64_t n_events);
+
+/* ---- evaluation: FCN::operator() + GooPdf::calculateNLL ---- */
+int gf_set_params(gf_engine *eng, int toy, const double *params, int n_params);
+int gf_nll(gf_engine *eng, int toy, double *nll);
+/* grad has one entry per parameter whose grad_mask is set, in parameter order */
+int gf_nll_grad(gf_engine *eng, int toy, double *nll, double *grad);
+/* All toys in one launch sequence: P[n_toys][n_params] -> nll[n_toys], grad[n_toys][n_grad] (grad may be NULL).
+ * active[n_toys] (may be NULL) skips toys whose entry is 0. */
+int gf_nll_batch(gf_engine *eng, int n_toys, const double *P, const int32_t *active, double *nll, double *grad);
+int gf_num_grad(const gf_engine *eng);
+int gf_num_params(const gf_engine *eng);
+int gf_num_toys(const gf_engine *eng);
+/* Parameter index of every gradient slot: out[0..gf_num_grad-1]; returns the count. */
+int gf_grad_params(const gf_engine *eng, int32_t *out, int cap);
+
+/* Normalisation of every node (GooPdf::normalize, src/PDFs/GooPdf.cu:340-396):
+ * integral[n] is the value normalize() returns, norm[n] the factor applied
+ * (1/integral, or 1 for forced/combine nodes). */
+int gf_normalize(gf_engine *eng, int toy, double *integral, double *norm);
+
+/* Per-event values of node `node` treated as the root (GooPdf::evaluate_with_metric,
+ * src/PDFs/GooPdf.cu:112-173): out[e] for the toy's events. */
+int gf_eval_events(gf_engine *eng, int toy, int node, int metric, double *out, int64_t n_out);
+
+/* Device time of the last evaluation's kernels in milliseconds (CUDA events). */
+int gf_last_timing(const gf_engine *eng, double *ms_total, double *ms_event_kernel);
+/* Number of kernel launches issued by one gf_nll_grad / gf_nll_batch call. */
+int gf_launches_per_eval(const gf_engine *eng, int with_grad);
+
+/* ---- minimiser (Minuit2 MnMigrad surface, src/goofit/FitManagerMinuit2.cpp:31-119) ---- */
+typedef struct gf_minimizer gf_minimizer;
+
+/* limited[i]: 0 none, 1 both bounds, 2 lower only, 3 upper only.  fixed[i] != 0 keeps x0[i].
+ * use_grad != 0: the caller supplies gradients (FCNGradientBase); else numerical (2-point, strategy cycles). */
+int gf_minimizer_create(gf_minimizer **out,
+                        int n,
+                        const double *x0,
+                        const double *err,
+                        const double *lo,
+                        const double *hi,
+                        const int32_t *limited,
+                        const int32_t *fixed,
+                        double up,
+                        int strategy,
+                        double tolerance,
+                        int maxfcn,
+                        int use_grad);
+/* Returns 1 and fills x[n] (external values) when a function value is needed;
+ * *need_grad says whether the gradient is wanted too.  Returns 0 when finished. */
+int gf_minimizer_ask(gf_minimizer *m, double *x, int32_t *need_grad);
+/* grad[n] over all parameters (entries of fixed ones are ignored); NULL if not asked. */
+int gf_minimizer_tell(gf_minimizer *m, double f, const double *grad);
+
+typedef struct gf_fit_result {
+    double fmin;
+    double edm;
+    int32_t nfcn;
+    int32_t ngrad;
+    int32_t valid;          /* IsValid && HasCovariance && !IsAboveMaxEdm && !HasReachedCallLimit */
+    int32_t above_max_edm;
+    int32_t call_limit;
+    int32_t has_covariance;
+    int32_t hesse_failed;
+    int32_t made_posdef;
+    int32_t n_iter;
+    int32_t reserved;
+} gf_fit_result;
+
+/* x[n], err[n] external; cov[n*n] external covariance (may be NULL). */
+int gf_minimizer_result(const gf_minimizer *m, gf_fit_result *res, double *x, double *err, double *cov);
+int gf_minimizer_destroy(gf_minimizer *m);
+
+/* ---- native fit loop: MIGRAD against the engine without leaving C++ ---- */
+typedef struct gf_fit_options {
+    const double *err;       /* [n_params] initial step / error */
+    const double *lo;        /* [n_params] */
+    const double *hi;        /* [n_params] */
+    const int32_t *limited;  /* [n_params] */
+    const int32_t *fixed;    /* [n_params] */
+    double up;               /* 0.5 for NLL (include/goofit/fitting/FCN.h:26) */
+    double tolerance;        /* MnMigrad tolerance, EDM < 0.002 * tolerance * up */
+    int32_t strategy;        /* MnStrategy(1) by default */
+    int32_t maxfcn;
+    int32_t use_grad;        /* analytic gradient from the adjoint path */
+    int32_t reserved;
+} gf_fit_options;
+
+/* Fits toy `toy` starting from x0[n_params]; x/err receive the result. */
+int gf_fit(gf_engine *eng, int toy, const gf_fit_options *opt, const double *x0, double *x, double *err,
+           gf_fit_result *res);
+/* Fits toys 0..n_toys-1 in lockstep (one batched launch sequence per round).
+ * X0/X/ERR are [n_toys][n_params]; res[n_toys]. */
+int gf_fit_batch(gf_engine *eng, int n_toys, const gf_fit_options *opt, const double *X0, double *X, double *ERR,
+                 gf_fit_result *res);
+
+/* ---- diagnostics: code generation without a device ---- */
+/* Generated CUDA source for a tree (precision as in gf_engine_create); *len gets the full length. */
+int gf_generated_source(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
+                        const int32_t *grad_mask, int precision, char *buf, int64_t cap, int64_t *len);
+/* Compiles a tree's kernels for sm_103a without loading them; *cubin_bytes gets the image size. */
+int gf_compile_tree(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
+                    const int32_t *grad_mask, int precision, int64_t *cubin_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GFENGINE_H */

@@ -1,0 +1,600 @@
+// FP64 CPU oracle for the GooFit fit path.  TEST INFRASTRUCTURE ONLY: the
+// engine never links, loads or calls this file; tests/, bench.py's CPU
+// baseline leg and __graft_entry__.smoke() use it as the checker.
+//
+// It restates the reference's per-event device functions, normalisation
+// recursion and NLL metric in plain FP64 C++ (OpenMP over events), walking the
+// same node list the engine receives (include/gfengine.h).  Each function
+// cites the reference file:line it follows.  Parity is pinned against the
+// reference's own known-answer tests (tests/simple/NormalizeTest.cpp,
+// tests/simple/AddNormTest.cpp, python/tests/test_min_conv.py) in
+// tests/test_oracle_golden.py.
+//
+// Deliberate deviation: for multi-dimensional numeric grids the reference's
+// binned MetricTaker writes every bin centre into the slot of the node's first
+// observable (src/PDFs/MetricTaker.cu:74-88) and leaves the other slots
+// uninitialised; the oracle evaluates the proper N-D grid.  1-D grids (all
+// configs) are identical.
+#include "../include/gfengine.h"
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+struct Node {
+    int op, flags;
+    std::vector<int> params;
+    std::vector<double> consts;
+    std::vector<int> obs;
+    std::vector<int> children;
+    int integration_bins;
+};
+
+struct ConvWork {
+    // host_iConsts of ConvolutionPdf::setIntegrationConstants (src/PDFs/combine/ConvolutionPdf.cu:228-282)
+    double ic[6];
+    int model_offset;
+    std::vector<double> model, resol;
+    // memo of sum_i M[i] R[i+off-k] keyed by k (same summation order as the per-event loop)
+    std::vector<double> table;
+    int kmin = 0, kmax = -1;
+};
+
+struct Oracle {
+    std::vector<Node> nodes;
+    std::vector<gf_observable> obs;
+    std::vector<double> P;
+    std::vector<double> norm;     // host_normalizations[normalIdx + 1]
+    std::vector<double> integral; // value returned by normalize()
+    std::map<int, ConvWork> conv;
+    bool brute_force = false;
+    std::string err;
+
+    const Node &N(int i) const { return nodes.at(i); }
+    double par(int node, int i) const { return P.at(nodes[node].params.at(i)); }
+
+    // PdfBase::recursiveSetNormalization (src/goofit/PdfBase.cpp:29-38)
+    void recursiveSetNormalization(int i, double v) {
+        norm[i] = v;
+        for(int c : nodes[i].children)
+            recursiveSetNormalization(c, v);
+    }
+
+    // Observables of a subtree in first-appearance order (PdfBase::getObservables, src/goofit/PdfBase.cpp:90-101)
+    std::vector<int> subtreeObs(int i) const {
+        std::vector<int> r = nodes[i].obs;
+        for(int c : nodes[i].children)
+            for(int o : subtreeObs(c)) {
+                bool f = false;
+                for(int q : r)
+                    f |= (q == o);
+                if(!f)
+                    r.push_back(o);
+            }
+        return r;
+    }
+
+    // ProdPdf::ProdPdf overlap detection (src/PDFs/combine/ProdPdf.cu:28-68): each component is
+    // compared with the previous one only; a component with separateNorm cancels it.
+    bool prodOverlaps(int i) const {
+        const Node &n = nodes[i];
+        bool over = false;
+        std::vector<int> check;
+        for(int c : n.children) {
+            if(over)
+                continue;
+            std::vector<int> cur = subtreeObs(c);
+            for(int o : cur) {
+                bool f = false;
+                for(int q : check)
+                    f |= (q == o);
+                if(f) {
+                    over = true;
+                    break;
+                }
+            }
+            check = cur;
+        }
+        if(over)
+            for(int c : n.children)
+                if(nodes[c].flags & GF_FLAG_SEPARATE_NORM)
+                    over = false;
+        return over;
+    }
+
+    bool hasAnalyticIntegral(int i) const {
+        const Node &n = nodes[i];
+        switch(n.op) {
+        case GF_OP_EXP:
+        case GF_OP_EXP_OFFSET:
+        case GF_OP_EXP_POLY:
+        case GF_OP_EXP_POLY_OFFSET:
+            // ExpPdf::hasAnalyticIntegral: 1 == nParams (include/goofit/PDFs/basic/ExpPdf.h:35)
+            return n.params.size() == 1;
+        case GF_OP_GAUSSIAN:
+            return true; // include/goofit/PDFs/basic/GaussianPdf.h:24
+        default:
+            return false;
+        }
+    }
+
+    // ExpPdf::integrate (src/PDFs/basic/ExpPdf.cu:121-132), GaussianPdf::integrate (src/PDFs/basic/GaussianPdf.cu:28-35)
+    double integrate(int i, double lo, double hi) const {
+        const Node &n = nodes[i];
+        if(n.op == GF_OP_GAUSSIAN) {
+            static const double rootPi = std::sqrt(std::atan2(0.0, -1.0));
+            double sigma               = par(i, 1);
+            sigma *= std::sqrt(2.0) * rootPi;
+            return sigma;
+        }
+        double alpha = par(i, 0); // host_parameters[parametersIdx + 1]
+        if(0 == alpha)
+            return hi - lo;
+        double ret = std::exp(alpha * hi) - std::exp(alpha * lo);
+        ret /= alpha;
+        return ret;
+    }
+
+    // GooPdf::normalize (src/PDFs/GooPdf.cu:340-396) with the per-class overrides
+    double normalize(int i) {
+        const Node &n = nodes[i];
+        if(n.op == GF_OP_ADD || n.op == GF_OP_ADD_EXT) {
+            // AddPdf::normalize (src/PDFs/combine/AddPdf.cu:143-185)
+            bool extended = n.op == GF_OP_ADD_EXT;
+            double ret = 0, totalWeight = 0;
+            size_t nc = n.children.size();
+            for(size_t c = 0; c + 1 < nc; ++c) {
+                double weight = par(i, (int)c);
+                totalWeight += weight;
+                double curr = normalize(n.children[c]);
+                ret += curr * weight;
+            }
+            double last = normalize(n.children[nc - 1]);
+            if(extended) {
+                double lastWeight = par(i, (int)nc - 1);
+                totalWeight += lastWeight;
+                ret += last * lastWeight;
+                ret /= totalWeight;
+            } else {
+                ret += (1 - totalWeight) * last;
+            }
+            norm[i]     = 1.0;
+            integral[i] = ret;
+            if(n.flags & GF_FLAG_COMMON_NORM)
+                for(int c : n.children)
+                    norm[c] = 1.0 / ret;
+            return ret;
+        }
+        if(n.op == GF_OP_PROD) {
+            // ProdPdf::normalize (src/PDFs/combine/ProdPdf.cu:75-99)
+            if(prodOverlaps(i)) {
+                recursiveSetNormalization(i, 1.0);
+                return numericNormalize(i);
+            }
+            for(int c : n.children)
+                normalize(c);
+            norm[i]     = 1.0;
+            integral[i] = 1.0;
+            return 1.0;
+        }
+        if(n.op == GF_OP_CONVOLUTION) {
+            // ConvolutionPdf::normalize (src/PDFs/combine/ConvolutionPdf.cu:313-358)
+            recursiveSetNormalization(i, 1.0);
+            fillWorkspaces(i);
+            return numericNormalize(i);
+        }
+        if(hasAnalyticIntegral(i)) {
+            double ret = 1;
+            for(int o : n.obs)
+                ret *= integrate(i, obs[o].lo, obs[o].hi);
+            norm[i]     = 1.0 / ret;
+            integral[i] = ret;
+            return ret;
+        }
+        return numericNormalize(i);
+    }
+
+    int gridBins(int i, int o) const {
+        return nodes[i].integration_bins > 0 ? nodes[i].integration_bins : obs[o].nbins;
+    }
+
+    // Numeric branch of GooPdf::normalize + GooPdf::reduce_with_bins + binned MetricTaker
+    // (src/PDFs/GooPdf.cu:83-108,366-395; src/PDFs/MetricTaker.cu:48-96; src/PDFs/GooPdf.cpp:32-50)
+    double numericNormalize(int i) {
+        const Node &n = nodes[i];
+        size_t totalBins = 1;
+        for(int o : n.obs)
+            totalBins *= (size_t)gridBins(i, o);
+        double ret = 1;
+        double vol = 1.0;
+        for(int o : n.obs)
+            vol *= obs[o].hi - obs[o].lo;
+        ret *= vol;
+        ret /= totalBins;
+        double sum = 0;
+#pragma omp parallel for reduction(+ : sum) schedule(static)
+        for(int64_t b = 0; b < (int64_t)totalBins; ++b) {
+            std::vector<double> evt(obs.size(), 0.0);
+            int64_t bin = b;
+            for(int o : n.obs) {
+                int nb       = gridBins(i, o);
+                int localBin = (int)(bin % nb);
+                double x     = obs[o].hi - obs[o].lo;
+                x /= nb;
+                x *= (localBin + 0.5);
+                x += obs[o].lo;
+                evt[o] = x;
+                bin /= nb;
+            }
+            sum += eval(i, evt.data());
+        }
+        if(std::isnan(sum))
+            throw std::runtime_error("NaN in normalization");
+        if(0 >= sum)
+            throw std::runtime_error("Non-positive normalization");
+        ret *= sum;
+        if(0 == ret)
+            throw std::runtime_error("Zero integral");
+        norm[i]     = 1.0 / ret;
+        integral[i] = ret;
+        return ret;
+    }
+
+    // ConvolutionPdf::setIntegrationConstants (src/PDFs/combine/ConvolutionPdf.cu:228-282) and the
+    // workspace fills of ConvolutionPdf::normalize (src/PDFs/combine/ConvolutionPdf.cu:325-353)
+    void fillWorkspaces(int i) {
+        const Node &n = nodes[i];
+        ConvWork &w   = conv[i];
+        double lo = n.consts.at(0), hi = n.consts.at(1), step = n.consts.at(2);
+        const gf_observable &dep = obs.at(n.obs.at(0));
+        int nM  = (int)std::floor((hi - lo) / step + 0.5);
+        w.ic[0] = lo;
+        w.ic[1] = hi;
+        w.ic[2] = nM;
+        w.ic[3] = lo - dep.hi;
+        w.ic[4] = hi - dep.lo;
+        int nR  = (int)std::floor((w.ic[4] - w.ic[3]) / step + 0.5);
+        w.ic[5] = nR;
+        w.model_offset = (int)(dep.hi / step);
+        int model = n.children.at(0), resol = n.children.at(1);
+        w.model.assign(nM, 0.0);
+        w.resol.assign(nR, 0.0);
+        binnedEval(model, w.ic + 0, w.model);
+        binnedEval(resol, w.ic + 3, w.resol);
+        w.table.clear();
+        w.kmax = w.kmin - 1;
+    }
+
+    // binned MetricTaker over one range triple (lo, hi, nbins) with the Eval metric
+    void binnedEval(int node, const double *range, std::vector<double> &out) {
+        int id      = nodes[node].obs.at(0);
+        int numBins = (int)std::floor(range[2] + 0.5);
+        for(int b = 0; b < (int)out.size(); ++b) {
+            std::vector<double> evt(obs.size(), 0.0);
+            int localBin = b % numBins;
+            double x     = range[1] - range[0];
+            x /= numBins;
+            x *= (localBin + 0.5);
+            x += range[0];
+            evt[id] = x;
+            out[b]  = eval(node, evt.data());
+        }
+    }
+
+    static int offsetInBins(double x0, double loBound, double step) {
+        double lowerBoundOffset = loBound / step;
+        lowerBoundOffset -= std::floor(lowerBoundOffset);
+        return (int)std::floor(x0 / step - lowerBoundOffset);
+    }
+
+    double convSum(int i, int k) const {
+        const Node &n     = nodes[i];
+        const ConvWork &w = conv.at(i);
+        double loBound = n.consts[0], hiBound = n.consts[1], step = n.consts[2];
+        int numbins = (int)std::floor((hiBound - loBound) / step + 0.5);
+        double ret  = 0;
+        for(int m = 0; m < numbins; ++m) {
+            int r = m + w.model_offset - k;
+            if(r < 0 || r >= (int)w.resol.size())
+                throw std::runtime_error("convolution resolution index out of range");
+            ret += w.model[m] * w.resol[r];
+        }
+        return ret;
+    }
+
+    // Fills the per-k memo over [kmin, kmax]; identical values to convSum(i, k).
+    void buildConvTable(int i, int kmin, int kmax) {
+        ConvWork &w = conv.at(i);
+        w.kmin      = kmin;
+        w.kmax      = kmax;
+        w.table.assign(kmax - kmin + 1, 0.0);
+#pragma omp parallel for schedule(static)
+        for(int k = kmin; k <= kmax; ++k)
+            w.table[k - kmin] = convSum(i, k);
+    }
+
+    // Per-event device functions (src/PDFs/basic/*.cu, src/PDFs/combine/*.cu)
+    double eval(int i, const double *evt) const {
+        const Node &n = nodes[i];
+        switch(n.op) {
+        case GF_OP_EXP: { // src/PDFs/basic/ExpPdf.cu:7-17
+            double x = evt[n.obs[0]];
+            return std::exp(par(i, 0) * x);
+        }
+        case GF_OP_EXP_OFFSET: { // src/PDFs/basic/ExpPdf.cu:19-30
+            double x = evt[n.obs[0]];
+            x -= par(i, 0);
+            return std::exp(par(i, 1) * x);
+        }
+        case GF_OP_EXP_POLY: { // src/PDFs/basic/ExpPdf.cu:32-46
+            double x = evt[n.obs[0]], exparg = 0;
+            for(size_t k = 0; k < n.params.size(); ++k)
+                exparg += std::pow(x, (double)k) * par(i, (int)k);
+            return std::exp(exparg);
+        }
+        case GF_OP_EXP_POLY_OFFSET: { // src/PDFs/basic/ExpPdf.cu:48-63
+            double x = evt[n.obs[0]];
+            x -= par(i, 0);
+            double exparg = 0;
+            for(size_t k = 1; k < n.params.size(); ++k)
+                exparg += std::pow(x, (double)k) * par(i, (int)k);
+            return std::exp(exparg);
+        }
+        case GF_OP_GAUSSIAN: { // src/PDFs/basic/GaussianPdf.cu:7-17
+            double x = evt[n.obs[0]], mean = par(i, 0), sigma = par(i, 1);
+            return std::exp(-0.5 * (x - mean) * (x - mean) / (sigma * sigma));
+        }
+        case GF_OP_POLYNOMIAL: { // src/PDFs/basic/PolynomialPdf.cu:8-26
+            int lowestDegree = (int)n.consts.at(0);
+            double x = evt[n.obs[0]], ret = 0;
+            for(size_t k = 0; k < n.params.size(); ++k)
+                ret += par(i, (int)k) * std::pow(x, (double)(lowestDegree + (int)k));
+            return ret;
+        }
+        case GF_OP_POLYNOMIAL_OFFSET: { // src/PDFs/basic/PolynomialPdf.cu:28-44
+            int lowestDegree = (int)n.consts.at(0);
+            double x = evt[n.obs[0]], ret = 0;
+            for(size_t k = 2; k < n.params.size(); ++k)
+                ret += par(i, (int)k) * std::pow(x, (double)(lowestDegree + (int)k - 2));
+            return ret;
+        }
+        case GF_OP_ADD: { // src/PDFs/combine/AddPdf.cu:16-51
+            double ret = 0, totalWeight = 0;
+            size_t np = n.params.size();
+            for(size_t k = 0; k < np; ++k) {
+                double weight = par(i, (int)k);
+                totalWeight += weight;
+                int c       = n.children[k];
+                double curr = eval(c, evt);
+                ret += weight * curr * norm[c];
+            }
+            int c       = n.children[np];
+            double last = eval(c, evt);
+            ret += (1 - totalWeight) * last * norm[c];
+            return ret;
+        }
+        case GF_OP_ADD_EXT: { // src/PDFs/combine/AddPdf.cu:53-80
+            double ret = 0, totalWeight = 0;
+            for(size_t k = 0; k < n.params.size(); ++k) {
+                double weight = par(i, (int)k);
+                int c         = n.children[k];
+                double curr   = eval(c, evt);
+                ret += weight * curr * norm[c];
+                totalWeight += weight;
+            }
+            ret /= totalWeight;
+            return ret;
+        }
+        case GF_OP_PROD: { // src/PDFs/combine/ProdPdf.cu:9-26
+            double ret = 1;
+            for(int c : n.children) {
+                double curr = eval(c, evt);
+                curr *= norm[c];
+                ret *= curr;
+            }
+            return ret;
+        }
+        case GF_OP_CONVOLUTION: { // src/PDFs/combine/ConvolutionPdf.cu:27-75
+            double x0 = evt[n.obs[0]];
+            int k     = offsetInBins(x0, n.consts[0], n.consts[2]);
+            const ConvWork &w = conv.at(i);
+            double ret;
+            if(!brute_force && k >= w.kmin && k <= w.kmax)
+                ret = w.table[k - w.kmin];
+            else
+                ret = convSum(i, k);
+            ret *= norm[n.children[0]];
+            ret *= norm[n.children[1]];
+            return ret;
+        }
+        default:
+            throw std::runtime_error("oracle: unsupported op " + std::to_string(n.op));
+        }
+    }
+
+    // Pre-builds conv memo tables over the k range of the given events (no effect on values).
+    void prepareConvTables(const double *soa, int64_t n_events) {
+        if(brute_force)
+            return;
+        for(auto &kv : conv) {
+            int i         = kv.first;
+            const Node &n = nodes[i];
+            int o         = n.obs[0];
+            int kmin = offsetInBins(obs[o].lo, n.consts[0], n.consts[2]);
+            int kmax = offsetInBins(obs[o].hi, n.consts[0], n.consts[2]);
+            for(int64_t e = 0; e < n_events; ++e) {
+                int k = offsetInBins(soa[o * n_events + e], n.consts[0], n.consts[2]);
+                kmin  = k < kmin ? k : kmin;
+                kmax  = k > kmax ? k : kmax;
+            }
+            buildConvTable(i, kmin, kmax);
+        }
+    }
+};
+
+bool load(Oracle &O,
+          const gf_node *nodes,
+          int n_nodes,
+          const gf_observable *obs,
+          int n_obs,
+          const double *params,
+          int n_params,
+          int brute_force) {
+    O.nodes.clear();
+    for(int i = 0; i < n_nodes; ++i) {
+        const gf_node &g = nodes[i];
+        Node n;
+        n.op    = g.op;
+        n.flags = g.flags;
+        n.params.assign(g.params, g.params + g.n_params);
+        n.consts.assign(g.consts, g.consts + g.n_consts);
+        n.obs.assign(g.obs, g.obs + g.n_obs);
+        n.children.assign(g.children, g.children + g.n_children);
+        n.integration_bins = g.integration_bins;
+        O.nodes.push_back(n);
+    }
+    O.obs.assign(obs, obs + n_obs);
+    O.P.assign(params, params + n_params);
+    O.norm.assign(n_nodes, 1.0);
+    O.integral.assign(n_nodes, 1.0);
+    O.brute_force = brute_force != 0;
+    return true;
+}
+
+thread_local std::string g_err;
+
+} // namespace
+
+extern "C" {
+
+const char *oracle_last_error() { return g_err.c_str(); }
+
+// Normalises the tree rooted at `root` and evaluates `metric` for every event
+// (GooPdf::evaluate_with_metric, src/PDFs/GooPdf.cu:112-173).  integrals/norms
+// (may be NULL) receive every node's normalize() value and factor.
+int oracle_evaluate(const gf_node *nodes,
+                    int n_nodes,
+                    const gf_observable *obs,
+                    int n_obs,
+                    const double *params,
+                    int n_params,
+                    const double *soa,
+                    int64_t n_events,
+                    int root,
+                    int metric,
+                    int brute_force,
+                    double *out,
+                    double *integrals,
+                    double *norms) {
+    try {
+        Oracle O;
+        load(O, nodes, n_nodes, obs, n_obs, params, n_params, brute_force);
+        O.normalize(root);
+        O.prepareConvTables(soa, n_events);
+        double rootNorm = O.norm[root];
+        std::vector<double> tmp;
+#pragma omp parallel for schedule(static) private(tmp)
+        for(int64_t e = 0; e < n_events; ++e) {
+            tmp.resize(n_obs);
+            for(int o = 0; o < n_obs; ++o)
+                tmp[o] = soa[o * n_events + e];
+            double raw = O.eval(root, tmp.data());
+            double v;
+            if(metric == GF_METRIC_EVAL)
+                v = raw; // calculateEval, src/PDFs/MetricPointer.cu:8-11
+            else if(metric == GF_METRIC_PROB)
+                v = raw * rootNorm; // calculateProb, src/PDFs/MetricPointer.cu:18-21
+            else {
+                raw *= rootNorm; // calculateNLL, src/PDFs/MetricPointer.cu:13-16
+                v = raw > 0.0 ? -std::log(raw) : 0.0;
+            }
+            out[e] = v;
+        }
+        if(integrals)
+            for(int i = 0; i < n_nodes; ++i)
+                integrals[i] = O.integral[i];
+        if(norms)
+            for(int i = 0; i < n_nodes; ++i)
+                norms[i] = O.norm[i];
+        return 0;
+    } catch(std::exception &ex) {
+        g_err = ex.what();
+        return 1;
+    }
+}
+
+// GooPdf::calculateNLL (src/PDFs/GooPdf.cu:254-273) + AddPdf::calculateNLL extended term
+// (src/PDFs/combine/AddPdf.cu:187-204).  Root is node 0.
+int oracle_nll(const gf_node *nodes,
+               int n_nodes,
+               const gf_observable *obs,
+               int n_obs,
+               const double *params,
+               int n_params,
+               const double *soa,
+               int64_t n_events,
+               int brute_force,
+               double *nll) {
+    try {
+        Oracle O;
+        load(O, nodes, n_nodes, obs, n_obs, params, n_params, brute_force);
+        O.normalize(0);
+        if(O.norm[0] <= 0)
+            throw std::runtime_error("non-positive normalization");
+        O.prepareConvTables(soa, n_events);
+        double rootNorm = O.norm[0];
+        double ret      = 0;
+#pragma omp parallel for reduction(+ : ret) schedule(static)
+        for(int64_t e = 0; e < n_events; ++e) {
+            double evt[16];
+            for(int o = 0; o < n_obs; ++o)
+                evt[o] = soa[o * n_events + e];
+            double raw = O.eval(0, evt) * rootNorm;
+            ret += raw > 0.0 ? -std::log(raw) : 0.0;
+        }
+        if(0.0 == ret)
+            throw std::runtime_error("zero NLL");
+        if(O.nodes[0].op == GF_OP_ADD_EXT) {
+            double expEvents = 0;
+            for(size_t k = 0; k < O.nodes[0].params.size(); ++k)
+                expEvents += O.par(0, (int)k);
+            ret += (expEvents - (double)n_events * std::log(expEvents));
+        }
+        *nll = ret;
+        return 0;
+    } catch(std::exception &ex) {
+        g_err = ex.what();
+        return 1;
+    }
+}
+
+// std::mt19937(seed) + std::exponential_distribution<>(lambda), the generator of the
+// reference's tests (tests/simple/NormalizeTest.cpp:16-30, tests/convert/GaussianTest.cpp).
+void oracle_mt19937_exponential(uint32_t seed, double lambda, int64_t n, double *out) {
+    std::mt19937 gen(seed);
+    std::exponential_distribution<> d(lambda);
+    for(int64_t i = 0; i < n; ++i)
+        out[i] = d(gen);
+}
+
+int oracle_num_threads() {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+} // extern "C"

@@ -1,0 +1,110 @@
+"""ctypes wrapper of the FP64 CPU oracle (oracle/oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by bench.py's CPU-baseline leg
+and by __graft_entry__.smoke() as the checker; the engine never uses it.
+The library is built by `make -C oracle` into oracle/_build/.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+from goofit_gb300 import _abi as A
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+_lib = None
+
+
+def build() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists() or LIB.stat().st_mtime < (HERE / "oracle.cpp").stat().st_mtime:
+            build()
+        L = C.CDLL(str(LIB))
+        f64p, i32p = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+        L.oracle_evaluate.argtypes = [C.POINTER(A.gf_node), C.c_int, C.POINTER(A.gf_observable), C.c_int, f64p,
+                                      C.c_int, f64p, C.c_int64, C.c_int, C.c_int, C.c_int, f64p, f64p, f64p]
+        L.oracle_evaluate.restype = C.c_int
+        L.oracle_nll.argtypes = [C.POINTER(A.gf_node), C.c_int, C.POINTER(A.gf_observable), C.c_int, f64p, C.c_int,
+                                 f64p, C.c_int64, C.c_int, f64p]
+        L.oracle_nll.restype = C.c_int
+        L.oracle_last_error.restype = C.c_char_p
+        L.oracle_mt19937_exponential.argtypes = [C.c_uint32, C.c_double, C.c_int64, f64p]
+        L.oracle_num_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def _prep(nodes, observables, params, soa):
+    nl = A.NodeList(nodes)
+    obs = A.observables_array(observables)
+    p, pp = A.f64(params)
+    s = np.ascontiguousarray(np.asarray(soa, dtype=np.float64).reshape(len(observables), -1))
+    return nl, obs, p, pp, s
+
+
+def nll(nodes, observables, params, soa, brute_force: bool = False) -> float:
+    """GooPdf::calculateNLL restated in FP64 (root = node 0)."""
+    L = lib()
+    nl, obs, p, pp, s = _prep(nodes, observables, params, soa)
+    out = C.c_double()
+    rc = L.oracle_nll(nl.arr, nl.n, obs, len(observables), pp, len(p), s.ctypes.data_as(C.POINTER(C.c_double)),
+                      s.shape[1], 1 if brute_force else 0, C.byref(out))
+    if rc:
+        raise OracleError(L.oracle_last_error().decode())
+    return out.value
+
+
+def evaluate(nodes, observables, params, soa, metric: int = A.GF_METRIC_PROB, root: int = 0,
+             brute_force: bool = False):
+    """Per-event metric values plus every node's normalize() integral and factor."""
+    L = lib()
+    nl, obs, p, pp, s = _prep(nodes, observables, params, soa)
+    n = s.shape[1]
+    out = np.zeros(max(n, 1))
+    I = np.zeros(nl.n)
+    N = np.zeros(nl.n)
+    f64p = C.POINTER(C.c_double)
+    rc = L.oracle_evaluate(nl.arr, nl.n, obs, len(observables), pp, len(p), s.ctypes.data_as(f64p), n, root,
+                           metric, 1 if brute_force else 0, out.ctypes.data_as(f64p), I.ctypes.data_as(f64p),
+                           N.ctypes.data_as(f64p))
+    if rc:
+        raise OracleError(L.oracle_last_error().decode())
+    return out[:n], I, N
+
+
+def fd_grad(nodes, observables, params, soa, indices, h: float = 1e-5) -> np.ndarray:
+    """Central finite differences of the oracle NLL (step h relative to max(1, |p|))."""
+    p0 = np.asarray(params, dtype=np.float64)
+    g = np.zeros(len(indices))
+    for j, i in enumerate(indices):
+        step = h * max(1.0, abs(p0[i]))
+        pp, pm = p0.copy(), p0.copy()
+        pp[i] += step
+        pm[i] -= step
+        g[j] = (nll(nodes, observables, pp, soa) - nll(nodes, observables, pm, soa)) / (2 * step)
+    return g
+
+
+def mt19937_exponential(seed: int, lam: float, n: int) -> np.ndarray:
+    """std::mt19937(seed) + std::exponential_distribution<>(lam) draws."""
+    out = np.zeros(n)
+    lib().oracle_mt19937_exponential(seed, lam, n, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def num_threads() -> int:
+    return lib().oracle_num_threads()
