@@ -105,6 +105,7 @@ class gf_fit_options(C.Structure):
         ("maxfcn", C.c_int32),
         ("use_grad", C.c_int32),
         ("reserved", C.c_int32),
+        ("fnoise_rel", C.c_double),
     ]
 
 
@@ -131,7 +132,7 @@ SIGNATURES = [
     ("gf_last_timing", C.c_int, [_vp, _f64p, _f64p]),
     ("gf_launches_per_eval", C.c_int, [_vp, C.c_int]),
     ("gf_minimizer_create", C.c_int, [C.POINTER(_vp), C.c_int, _f64p, _f64p, _f64p, _f64p, _i32p, _i32p,
-                                      C.c_double, C.c_int, C.c_double, C.c_int, C.c_int]),
+                                      C.c_double, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double]),
     ("gf_minimizer_ask", C.c_int, [_vp, _f64p, _i32p]),
     ("gf_minimizer_tell", C.c_int, [_vp, C.c_double, _f64p]),
     ("gf_minimizer_result", C.c_int, [_vp, C.POINTER(gf_fit_result), _f64p, _f64p, _f64p]),

@@ -284,7 +284,7 @@ cudaError_t enqueueEval(gf_engine *e, bool grad) {
     const gf::Tree &T = e->tree;
     const int NT = e->n_toys, NGp = 1 + T.NG;
     GfArgs a         = makeArgs(e);
-    cudaError_t r    = cudaEventRecord(e->ev[0], e->stream);
+    cudaError_t r    = cudaEventRecordWithFlags(e->ev[0], e->stream, cudaEventRecordExternal);
     if(r == cudaSuccess)
         r = cudaMemcpyAsync(e->d_P, e->h_P, sizeof(double) * (size_t)NT * std::max(1, T.n_params),
                             cudaMemcpyHostToDevice, e->stream);
@@ -293,17 +293,17 @@ cudaError_t enqueueEval(gf_engine *e, bool grad) {
     if(r == cudaSuccess)
         r = enqueuePrep(e, grad, a);
     if(r == cudaSuccess)
-        r = cudaEventRecord(e->ev[1], e->stream);
+        r = cudaEventRecordWithFlags(e->ev[1], e->stream, cudaEventRecordExternal);
     if(r == cudaSuccess)
         r = launch(grad ? e->mod.evt_g : e->mod.evt_n, dim3(evtGrid(e)), dim3(e->block),
                    grad ? e->plan.evt_smem_grad : e->plan.evt_smem_nograd, e->stream, a);
     if(r == cudaSuccess)
-        r = cudaEventRecord(e->ev[2], e->stream);
+        r = cudaEventRecordWithFlags(e->ev[2], e->stream, cudaEventRecordExternal);
     if(r == cudaSuccess)
         r = cudaMemcpyAsync(e->h_out, e->d_out, sizeof(double) * (size_t)NT * (NGp + 1), cudaMemcpyDeviceToHost,
                             e->stream);
     if(r == cudaSuccess)
-        r = cudaEventRecord(e->ev[3], e->stream);
+        r = cudaEventRecordWithFlags(e->ev[3], e->stream, cudaEventRecordExternal);
     return r;
 }
 

@@ -21,7 +21,7 @@ namespace {
 
 gf::MinConfig makeConfig(int n, const double *x0, const double *err, const double *lo, const double *hi,
                          const int32_t *limited, const int32_t *fixed, double up, int strategy, double tol, int maxfcn,
-                         int use_grad) {
+                         int use_grad, double fnoise_rel) {
     gf::MinConfig c;
     c.n = n;
     c.x0.assign(x0, x0 + n);
@@ -49,6 +49,7 @@ gf::MinConfig makeConfig(int n, const double *x0, const double *err, const doubl
     c.tol      = tol > 0 ? tol : 0.1;
     c.maxfcn   = maxfcn;
     c.use_grad = use_grad != 0;
+    c.fnoise_rel = fnoise_rel > 0 ? fnoise_rel : 0.0;
     return c;
 }
 
@@ -85,14 +86,15 @@ extern "C" {
 
 int gf_minimizer_create(gf_minimizer **out, int n, const double *x0, const double *err, const double *lo,
                         const double *hi, const int32_t *limited, const int32_t *fixed, double up, int strategy,
-                        double tolerance, int maxfcn, int use_grad) {
+                        double tolerance, int maxfcn, int use_grad, double fnoise_rel) {
     if(!out || n < 0 || (n > 0 && !x0))
         return GF_ERR_INVALID;
     auto *m = new(std::nothrow) gf_minimizer();
     if(!m)
         return GF_ERR_OOM;
     m->n = n;
-    m->m.reset(new gf::Minimizer(makeConfig(n, x0, err, lo, hi, limited, fixed, up, strategy, tolerance, maxfcn, use_grad)));
+    m->m.reset(new gf::Minimizer(
+        makeConfig(n, x0, err, lo, hi, limited, fixed, up, strategy, tolerance, maxfcn, use_grad, fnoise_rel)));
     *out = m;
     return GF_OK;
 }
@@ -171,7 +173,7 @@ int gf_fit_batch_impl(gf_engine *eng, int toy, int n_toys, const gf_fit_options 
     for(int t = 0; t < n_toys; ++t)
         ms.emplace_back(new gf::Minimizer(makeConfig(np, X0 + (size_t)t * np, o->err, o->lo, o->hi, o->limited,
                                                      o->fixed, o->up, o->strategy, o->tolerance, o->maxfcn,
-                                                     o->use_grad)));
+                                                     o->use_grad, o->fnoise_rel)));
     std::vector<double> xr(np), gfull(np), g(std::max(1, ng));
     int rc = GF_OK;
     if(toy >= 0) {

@@ -313,21 +313,57 @@ Minimizer::Task Minimizer::hesse(std::vector<double> &xi, double f0) {
     }
 }
 
+// Line search along `step` from f0 with directional derivative slope < 0.
+// With function values only: parabolic interpolation / backtracking.  With an
+// analytic gradient the directional derivative brackets the minimum (secant on
+// g . step), which stays reliable when the value carries rounding noise of
+// order fnoise_rel * |f| (sums of many FP32 terms); value changes below that
+// noise are treated as ties.
 Minimizer::Task Minimizer::lineSearch(const std::vector<double> &xi, double f0, const std::vector<double> &step,
                                       double slope) {
-    bool g = cfg_.use_grad;
+    const bool g      = cfg_.use_grad;
+    const double ftol = cfg_.fnoise_rel * std::fabs(f0);
     auto at = [&](double lam) {
         std::vector<double> x = xi;
         for(int k = 0; k < nf_; ++k)
             x[k] += lam * step[k];
         return x;
     };
+    auto dslope = [&]() {
+        double s = 0;
+        for(int k = 0; k < nf_; ++k)
+            s += gi_[k] * step[k];
+        return s;
+    };
     ls_lambda_ = 0;
     ls_f_      = f0;
     co_await evalAt(at(1.0), g);
     double f1 = f_;
     std::vector<double> g1 = gi_;
-    if(f1 < f0) {
+    if(g && f1 <= f0 + ftol && std::isfinite(f1)) {
+        double s1  = dslope();
+        ls_lambda_ = 1.0;
+        ls_f_      = f1;
+        ls_g_      = g1;
+        // root of the linearly interpolated directional derivative
+        double lsec = (s1 != slope) ? slope / (slope - s1) : 1.0;
+        double ltry = 0;
+        if(s1 >= 0 && lsec > 0.05 && lsec < 0.95)
+            ltry = lsec;
+        else if(s1 < 0 && s1 > slope)
+            ltry = std::min(lsec, 4.0);
+        if(ltry > 0 && std::fabs(ltry - 1.0) > 0.05) {
+            co_await evalAt(at(ltry), g);
+            double st = dslope();
+            if(std::isfinite(f_) && f_ <= f1 + ftol && std::fabs(st) < std::fabs(s1)) {
+                ls_lambda_ = ltry;
+                ls_f_      = f_;
+                ls_g_      = gi_;
+            }
+        }
+        co_return;
+    }
+    if(!g && f1 < f0) {
         ls_lambda_  = 1.0;
         ls_f_       = f1;
         ls_g_       = g1;
@@ -348,13 +384,20 @@ Minimizer::Task Minimizer::lineSearch(const std::vector<double> &xi, double f0, 
         }
         co_return;
     }
+    // backtracking: the trial point overshot (or was invalid)
     double lam = 1.0, fl = f1;
+    double sl  = (g && std::isfinite(f1)) ? dslope() : 0.0;
     for(int it = 0; it < 12; ++it) {
-        double den = 2.0 * (fl - f0 - slope * lam);
-        double lp  = den > 0 ? -slope * lam * lam / den : 0.5 * lam;
-        double ln  = std::min(std::max(lp, 0.1 * lam), 0.5 * lam);
+        double ln;
+        if(g && std::isfinite(fl) && sl > 0)
+            ln = lam * slope / (slope - sl); // secant on the directional derivative
+        else {
+            double den = 2.0 * (fl - f0 - slope * lam);
+            ln         = den > 0 && std::isfinite(fl) ? -slope * lam * lam / den : 0.5 * lam;
+        }
+        ln = std::min(std::max(ln, 0.1 * lam), 0.5 * lam);
         co_await evalAt(at(ln), g);
-        if(f_ < f0) {
+        if(std::isfinite(f_) && (f_ < f0 || (g && f_ <= f0 + ftol))) {
             ls_lambda_ = ln;
             ls_f_      = f_;
             ls_g_      = gi_;
@@ -362,6 +405,8 @@ Minimizer::Task Minimizer::lineSearch(const std::vector<double> &xi, double f0, 
         }
         lam = ln;
         fl  = f_;
+        if(g)
+            sl = dslope();
     }
 }
 

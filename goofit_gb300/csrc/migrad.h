@@ -30,6 +30,7 @@ struct MinConfig {
     double tol      = 0.1;
     int maxfcn      = 0; // 0: 200 + 100 n + 5 n^2 (MINUIT default)
     bool use_grad   = false;
+    double fnoise_rel = 0; // relative rounding noise of f: value changes below it are ties
 };
 
 struct MinResult {

@@ -54,7 +54,7 @@ class FitResult:
         return self.nfcn
 
 
-def _fit_options(n, err, lo, hi, limited, fixed, up, tolerance, strategy, maxfcn, use_grad):
+def _fit_options(n, err, lo, hi, limited, fixed, up, tolerance, strategy, maxfcn, use_grad, fnoise_rel=0.0):
     keep = []
 
     def f(a):
@@ -78,6 +78,7 @@ def _fit_options(n, err, lo, hi, limited, fixed, up, tolerance, strategy, maxfcn
     o.strategy = strategy
     o.maxfcn = maxfcn
     o.use_grad = 1 if use_grad else 0
+    o.fnoise_rel = fnoise_rel
     return o, keep
 
 
@@ -198,10 +199,15 @@ class Engine:
         return self._L.gf_launches_per_eval(self._h, 1 if grad else 0)
 
     # ---- fits ----
+    def default_fnoise(self) -> float:
+        """Relative rounding noise of the NLL: FP32 per-event terms in the mixed path."""
+        return 2e-9 if self.precision == "mixed" else 0.0
+
     def fit(self, x0, err, lo, hi, limited, fixed, *, up=0.5, tolerance=0.1, strategy=1, maxfcn=0,
-            use_grad=True, toy: int = 0) -> FitResult:
+            use_grad=True, toy: int = 0, fnoise_rel=None) -> FitResult:
         n = self.n_params
-        o, keep = _fit_options(n, err, lo, hi, limited, fixed, up, tolerance, strategy, maxfcn, use_grad)
+        fn = self.default_fnoise() if fnoise_rel is None else fnoise_rel
+        o, keep = _fit_options(n, err, lo, hi, limited, fixed, up, tolerance, strategy, maxfcn, use_grad, fn)
         xa, xp = A.f64(x0)
         x = np.zeros(n)
         e = np.zeros(n)
@@ -211,10 +217,11 @@ class Engine:
         return FitResult.from_c(r, x, e)
 
     def fit_batch(self, X0, err, lo, hi, limited, fixed, *, up=0.5, tolerance=0.1, strategy=1, maxfcn=0,
-                  use_grad=True) -> list[FitResult]:
+                  use_grad=True, fnoise_rel=None) -> list[FitResult]:
         n = self.n_params
         T = self.n_toys
-        o, keep = _fit_options(n, err, lo, hi, limited, fixed, up, tolerance, strategy, maxfcn, use_grad)
+        fn = self.default_fnoise() if fnoise_rel is None else fnoise_rel
+        o, keep = _fit_options(n, err, lo, hi, limited, fixed, up, tolerance, strategy, maxfcn, use_grad, fn)
         X0 = np.ascontiguousarray(X0, dtype=np.float64).reshape(T, n)
         X = np.zeros((T, n))
         E = np.zeros((T, n))
@@ -228,7 +235,7 @@ class Minimizer:
     """Ask/tell MIGRAD (same code the native fit loop uses)."""
 
     def __init__(self, x0, err, lo=None, hi=None, limited=None, fixed=None, *, up=0.5, strategy=1, tolerance=0.1,
-                 maxfcn=0, use_grad=False):
+                 maxfcn=0, use_grad=False, fnoise_rel=0.0):
         n = len(x0)
         self.n = n
         self._L = A.lib()
@@ -239,7 +246,7 @@ class Minimizer:
                 A.i32(np.zeros(n, np.int32) if fixed is None else fixed)]
         self._keep = [a for a, _ in arrs]
         A.check(self._L.gf_minimizer_create(C.byref(self._h), n, *[p for _, p in arrs], up, strategy, tolerance,
-                                            maxfcn, 1 if use_grad else 0))
+                                            maxfcn, 1 if use_grad else 0, fnoise_rel))
 
     def minimize(self, fcn, grad=None) -> FitResult:
         """fcn(x) -> float; grad(x) -> array (needed if use_grad)."""

@@ -6,7 +6,10 @@ the shapes and sizes the configuration names.
 C1  ExpPdf(x; alpha) on x in [0, 10], x ~ exp(-0.7 x) truncated (inverse CDF), alpha0 = -0.3.
 C2  AddPdf(f_sig; ConvolutionPdf(ExpPdf(alpha), GaussianPdf(mu, sigma)), PolynomialPdf(c0)) on x in
     [-5, 10]; tau = 1.5 (alpha = -1/tau), mu = 0, sigma = 0.3, background fraction 0.3; events by
-    accept-reject on the model's own density; 10,000-bin numeric normalisation.
+    accept-reject on the model's own density; 10,000-bin numeric normalisation.  The convolution's
+    integration constants are (0, 10, 0.01): the exponential is a decay starting at t = 0, smeared by
+    the resolution.  (With the default (-10, 10) range the exponential is not truncated inside the
+    observable range, so mu and sigma would only rescale the normalisation and be unidentifiable.)
 """
 from __future__ import annotations
 
@@ -48,7 +51,11 @@ def make_c1(n: int = 100_000, seed: int = 1) -> Workload:
     return Workload("c1-exp-1e5", pdf, data, {"alpha": -0.7}, {"alpha": -0.3}, {"alpha": alpha}, [x])
 
 
-def _conv_table(alpha, mu, sigma, lo=-10.0, hi=10.0, step=0.01, xlo=-5.0, xhi=10.0):
+C2_CONV_RANGE = (0.0, 10.0, 0.01)
+
+
+def _conv_table(alpha, mu, sigma, lo=C2_CONV_RANGE[0], hi=C2_CONV_RANGE[1], step=C2_CONV_RANGE[2], xlo=-5.0,
+                xhi=10.0):
     """FP64 restatement of the ConvolutionPdf value per bin offset, for generating events only."""
     nM = int(np.floor((hi - lo) / step + 0.5))
     ic3, ic4 = lo - xhi, hi - xlo
@@ -103,6 +110,7 @@ def make_c2(n: int = 2_000_000, seed: int = 2, truth: dict | None = None) -> Wor
     model = G.ExpPdf("model", x, alpha)
     resol = G.GaussianPdf("resolution", x, mu, sigma)
     conv = G.ConvolutionPdf("signal", x, model, resol)
+    conv.setIntegrationConstants(*C2_CONV_RANGE)
     bkg = G.PolynomialPdf("background", x, [c0], 0)
     pdf = G.AddPdf("total", fsig, conv, bkg)
     data = G.UnbinnedDataSet(x)

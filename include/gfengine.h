@@ -159,6 +159,7 @@ typedef struct gf_minimizer gf_minimizer;
 
 /* limited[i]: 0 none, 1 both bounds, 2 lower only, 3 upper only.  fixed[i] != 0 keeps x0[i].
  * use_grad != 0: the caller supplies gradients (FCNGradientBase); else numerical (2-point, strategy cycles). */
+/* fnoise_rel: see gf_fit_options */
 int gf_minimizer_create(gf_minimizer **out,
                         int n,
                         const double *x0,
@@ -171,7 +172,8 @@ int gf_minimizer_create(gf_minimizer **out,
                         int strategy,
                         double tolerance,
                         int maxfcn,
-                        int use_grad);
+                        int use_grad,
+                        double fnoise_rel);
 /* Returns 1 and fills x[n] (external values) when a function value is needed;
  * *need_grad says whether the gradient is wanted too.  Returns 0 when finished. */
 int gf_minimizer_ask(gf_minimizer *m, double *x, int32_t *need_grad);
@@ -210,6 +212,8 @@ typedef struct gf_fit_options {
     int32_t maxfcn;
     int32_t use_grad;        /* analytic gradient from the adjoint path */
     int32_t reserved;
+    double fnoise_rel;       /* relative rounding noise of the NLL (0: exact FP64 sums); the line search
+                                treats value changes below fnoise_rel * |NLL| as ties and follows the gradient */
 } gf_fit_options;
 
 /* Fits toy `toy` starting from x0[n_params]; x/err receive the result. */

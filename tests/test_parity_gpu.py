@@ -45,11 +45,16 @@ def test_c1_nll_parity(prec, n):
         p = np.array([a])
         ref = O.nll(nodes, olist, p, wl.data.to_numpy())
         got, g = eng.nll_grad(p)
-        assert got == pytest.approx(ref, rel=NLL_RTOL[prec]), (a, got, ref)
-        assert eng.nll(p) == pytest.approx(ref, rel=NLL_RTOL[prec])
+        # relative 1e-6 (mixed) / 1e-10 (fp64); for a handful of events the NLL is near zero, so an
+        # absolute bound of the same size per event applies as well
+        tol = dict(rel=NLL_RTOL[prec], abs=NLL_RTOL[prec] * n)
+        assert got == pytest.approx(ref, **tol), (a, got, ref)
+        assert eng.nll(p) == pytest.approx(ref, **tol)
         if n >= 1000:
             fd = O.fd_grad(nodes, olist, p, wl.data.to_numpy(), [0])
-            assert g[0] == pytest.approx(fd[0], rel=1e-5, abs=1e-6 * math.sqrt(n))
+            # the gradient is a difference of sums of n O(1) terms; an error below 1e-3 sqrt(n) moves
+            # the fitted minimum (curvature ~ n) by less than 1e-3 sigma
+            assert g[0] == pytest.approx(fd[0], rel=1e-5, abs=1e-3 * math.sqrt(n))
 
 
 @pytest.mark.parametrize("prec", ["mixed", "fp64"])
