@@ -140,6 +140,9 @@ SIGNATURES = [
     ("gf_fit", C.c_int, [_vp, C.c_int, C.POINTER(gf_fit_options), _f64p, _f64p, _f64p, C.POINTER(gf_fit_result)]),
     ("gf_fit_batch", C.c_int, [_vp, C.c_int, C.POINTER(gf_fit_options), _f64p, _f64p, _f64p,
                                C.POINTER(gf_fit_result)]),
+    ("gf_nll_exp_noalloc", C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_void_p,
+                                     C.c_void_p]),
+    ("gf_noalloc_last_error", C.c_char_p, []),
     ("gf_generated_source", C.c_int, [C.POINTER(gf_node), C.c_int, C.POINTER(gf_observable), C.c_int, C.c_int,
                                       _i32p, C.c_int, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
     ("gf_compile_tree", C.c_int, [C.POINTER(gf_node), C.c_int, C.POINTER(gf_observable), C.c_int, C.c_int,

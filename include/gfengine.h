@@ -224,6 +224,26 @@ int gf_fit(gf_engine *eng, int toy, const gf_fit_options *opt, const double *x0,
 int gf_fit_batch(gf_engine *eng, int n_toys, const gf_fit_options *opt, const double *X0, double *X, double *ERR,
                  gf_fit_result *res);
 
+/* ---- NLL without device allocation ----
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they evaluate the likelihood (a host whose device memory is owned
+ * by another allocator or a fixed budget; latency-critical code where
+ * cudaMalloc/cudaFree may synchronise the device).  Computes, on `stream`
+ * (a cudaStream_t, NULL = default stream), the NLL of ExpPdf(x; alpha) with its
+ * analytic normalisation over [lo, hi] for n_events FP32 values x (device
+ * memory), writing out[0] = NLL and out[1] = dNLL/dalpha (device memory, two
+ * doubles).  Allocates nothing: its reduction scratch is a fixed device array
+ * inside the library (16 KB per device, kept until exit) that limits a call to
+ * 8,388,608 events; larger counts return GF_ERR_INVALID.  The first call on a
+ * device looks up that array's device address (make that first call before any
+ * stream capture).  All calls share the array, so calls that overlap on the
+ * GPU (other streams, other host threads) race: order them on one stream.
+ * Asynchronous: errors that only the device can see (NaN) show in out[].
+ * gf_noalloc_last_error() describes the last failure of this entry point. */
+int gf_nll_exp_noalloc(const float *x, int64_t n_events, double alpha, double lo, double hi, double *out,
+                       void *stream);
+const char *gf_noalloc_last_error(void);
+
 /* ---- diagnostics: code generation without a device ---- */
 /* Generated CUDA source for a tree (precision as in gf_engine_create); *len gets the full length. */
 int gf_generated_source(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
