@@ -131,6 +131,7 @@ SIGNATURES = [
     ("gf_eval_events", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _f64p, C.c_int64]),
     ("gf_last_timing", C.c_int, [_vp, _f64p, _f64p]),
     ("gf_launches_per_eval", C.c_int, [_vp, C.c_int]),
+    ("gf_time_kernels", C.c_int, [_vp, C.c_int, C.c_int, _f64p, _f64p, _f64p]),
     ("gf_minimizer_create", C.c_int, [C.POINTER(_vp), C.c_int, _f64p, _f64p, _f64p, _f64p, _i32p, _i32p,
                                       C.c_double, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double]),
     ("gf_minimizer_ask", C.c_int, [_vp, _f64p, _i32p]),

@@ -342,6 +342,9 @@ struct GfArgs {
     const int *toy_nchunks;
     const i64 *toy_nevents;
     double *vals;
+    const void *Pr;  /* [toy][npr] R: parameters, then host-computed analytic factors */
+    void *Nq;        /* [toy][nq] R: numeric factors from the grid kernel */
+    int *qflag;      /* [toy] bit 1 NaN, bit 2 non-positive numeric integral */
     int n_chunks;
     int n_toys;
     int metric;
@@ -354,66 +357,146 @@ __device__ __forceinline__ double gf_warp_sum(double v) {
         v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
 }
+
+// Programmatic dependent launch: let the next kernel of the evaluation start its independent prologue,
+// and wait for the previous kernel's results (both are no-ops without a programmatic dependency).
+__device__ __forceinline__ void gf_pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void gf_pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Bin centre lo + w (b + 1/2) with w = (hi - lo) / n from the host: the binned MetricTaker's
+// arithmetic (src/PDFs/MetricTaker.cu:76-82) with its two roundings kept separate.
+__device__ __forceinline__ double gf_centre(double lo, double w, int b) {
+    return __dadd_rn(__dmul_rn(w, (double)b + 0.5), lo);
+}
 )CUDA";
 
-// Emits parameter loads (FP64 and R copies).
-void emitParams(std::ostream &os, const Tree &T) {
-    os << "    const double *Pt = a.P + (i64)toy * " << T.n_params << ";\n";
-    for(int j = 0; j < T.n_params; ++j)
-        os << "    const double pd" << j << " = Pt[" << j << "]; const R p" << j << " = (R)pd" << j << ";\n";
+// FP32 lane reductions with a two-sum compensation term (error of the sum ~ one rounding of the total).
+const char *kPreludeF32 = R"CUDA(
+__device__ __forceinline__ void gf_two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ float gf_group_sum(float v, int width) {
+    float hi = v, lo = 0.f;
+    for(int o = width >> 1; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(0xffffffffu, hi, o, width);
+        const float l2 = __shfl_down_sync(0xffffffffu, lo, o, width);
+        float s, e;
+        gf_two_sum(hi, h2, s, e);
+        hi = s;
+        lo += l2 + e;
+    }
+    return hi + lo;
+}
+// Partial sums as an unevaluated pair hi + lo of FP32 values (about 48 significant bits).
+typedef float2 ACC;
+__device__ __forceinline__ ACC acc_zero() { return make_float2(0.f, 0.f); }
+__device__ __forceinline__ ACC acc_of(float v) { return make_float2(v, 0.f); }
+__device__ __forceinline__ ACC acc_add(ACC a, ACC b) {
+    float s, e;
+    gf_two_sum(a.x, b.x, s, e);
+    e += a.y + b.y;
+    const float hi = s + e;
+    const float lo = e - (hi - s);
+    return make_float2(hi, lo);
+}
+__device__ __forceinline__ ACC warp_acc(float v) {
+    ACC a = acc_of(v);
+#pragma unroll
+    for(int o = 16; o > 0; o >>= 1) {
+        ACC b;
+        b.x = __shfl_down_sync(0xffffffffu, a.x, o);
+        b.y = __shfl_down_sync(0xffffffffu, a.y, o);
+        a   = acc_add(a, b);
+    }
+    return a;
+}
+__device__ __forceinline__ ACC warp_acc2(ACC a) {
+#pragma unroll
+    for(int o = 16; o > 0; o >>= 1) {
+        ACC b;
+        b.x = __shfl_down_sync(0xffffffffu, a.x, o);
+        b.y = __shfl_down_sync(0xffffffffu, a.y, o);
+        a   = acc_add(a, b);
+    }
+    return a;
+}
+__device__ __forceinline__ double acc_value(ACC a) { return (double)a.x + (double)a.y; }
+__device__ __forceinline__ float acc_r(ACC a) { return a.x + a.y; }
+#define GF_CENTRE(lo, w, b) ((float)(lo) + (float)(w) * ((float)(b) + 0.5f))
+)CUDA";
+
+const char *kPreludeF64 = R"CUDA(
+__device__ __forceinline__ double gf_group_sum(double v, int width) {
+    for(int o = width >> 1; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o, width);
+    return v;
+}
+typedef double ACC;
+__device__ __forceinline__ ACC acc_zero() { return 0.0; }
+__device__ __forceinline__ ACC acc_of(double v) { return v; }
+__device__ __forceinline__ ACC acc_add(ACC a, ACC b) { return a + b; }
+__device__ __forceinline__ ACC warp_acc(double v) { return gf_warp_sum(v); }
+__device__ __forceinline__ ACC warp_acc2(ACC a) { return gf_warp_sum(a); }
+__device__ __forceinline__ double acc_value(ACC a) { return a; }
+__device__ __forceinline__ double acc_r(ACC a) { return a; }
+#define GF_CENTRE(lo, w, b) gf_centre(lo, w, b)
+)CUDA";
+
+// Where every normalisation factor is kept (see NormLayout in tree.h).
+NormLayout computeNormLayout(const Tree &T) {
+    NormLayout nl;
+    nl.npr = T.n_params;
+    for(size_t i = 0; i < T.nodes.size(); ++i) {
+        if(T.nk[i] != NK_EXP && T.nk[i] != NK_GAUSS)
+            continue;
+        NormLayout::Analytic a;
+        a.node  = (int)i;
+        a.kind  = T.nk[i];
+        a.slotN = nl.npr++;
+        for(int s : T.dep_norm[i])
+            a.dN.push_back({s, nl.npr++});
+        nl.analytic.push_back(a);
+    }
+    nl.qN.assign(T.nums.size(), -1);
+    nl.qdN.assign(T.nums.size(), {});
+    for(size_t q = 0; q < T.nums.size(); ++q) {
+        int i    = T.nums[q].node;
+        nl.qN[q] = nl.nq++;
+        for(int s : T.dep_norm[i])
+            nl.qdN[q].push_back({s, nl.nq++});
+    }
+    return nl;
 }
 
-// Emits normalisation factors of every non-forced node for one toy, in FP64,
-// and their R copies; sets `nflag` bits for NaN / non-positive sums.
-void emitNorms(std::ostream &os, const Tree &T, bool grad) {
-    const int NQ  = (int)T.nums.size();
-    const int NGs = 1 + T.NG; // buffer stride, identical for both variants
-    os << "    int nflag = 0; (void)nflag;\n";
-    for(size_t i = 0; i < T.nodes.size(); ++i) {
-        int kind = T.nk[i];
-        if(kind == NK_ONE)
-            continue;
-        const TNode &n = T.nodes[i];
-        std::string I = "I" + std::to_string(i), N = "Nd" + std::to_string(i);
-        std::vector<std::string> dI; // per dep_norm slot, FP64 expression of dI/dslot
-        if(kind == NK_EXP) {
-            const gf_observable &o = T.obs[n.obs[0]];
-            os << "    double " << I << ", dI" << i << ";\n";
-            os << "    { const double al = pd" << n.params[0] << ", hi = " << lit(o.hi) << ", lo = " << lit(o.lo)
-               << ";\n"
-               << "      if(0 == al) { " << I << " = hi - lo; dI" << i << " = 0.5 * (hi * hi - lo * lo); }\n"
-               << "      else { const double eh = exp(al * hi), el = exp(al * lo); " << I << " = (eh - el) / al; dI"
-               << i << " = (hi * eh - lo * el) / al - " << I << " / al; } }\n";
-        } else if(kind == NK_GAUSS) {
-            double rootPi = std::sqrt(std::atan2(0.0, -1.0));
-            double root2  = std::sqrt(2.0);
-            os << "    const double " << I << " = pd" << n.params[1] << " * " << lit(root2 * rootPi) << ";\n";
-            os << "    const double dI" << i << " = " << lit(root2 * rootPi) << ";\n";
-        } else { // numeric
-            int q = T.num_of[i];
-            const NumInfo &g = T.nums[q];
-            os << "    const double *gs" << i << " = a.gsum + ((i64)toy * " << NQ << " + " << q << ") * " << NGs
-               << ";\n";
-            os << "    double " << I << " = 1.0; " << I << " *= " << lit(g.volume) << "; " << I << " /= "
-               << lit((double)g.total) << "; " << I << " *= gs" << i << "[0];\n";
-            os << "    if(isnan(gs" << i << "[0])) nflag |= 1; else if(!(gs" << i << "[0] > 0.0)) nflag |= 2;\n";
-        }
-        os << "    const double " << N << " = 1.0 / " << I << ";\n";
-        os << "    const R N" << i << " = (R)" << N << ";\n";
+// Parameters (type R) of the toy from its record.
+void emitParamsR(std::ostream &os, const Tree &T, const NormLayout &nl, const char *ind) {
+    os << ind << "const R *Pr = reinterpret_cast<const R *>(a.Pr) + (i64)toy * " << nl.npr << "; (void)Pr;\n";
+    for(int j = 0; j < T.n_params; ++j)
+        os << ind << "const R p" << j << " = Pr[" << j << "]; (void)p" << j << ";\n";
+}
+
+// Normalisation factors used by the event pass: analytic ones from the record, numeric ones from Nq.
+void emitNormReads(std::ostream &os, const Tree &T, bool grad, const NormLayout &nl, const char *ind) {
+    if(nl.nq > 0)
+        os << ind << "const R *Nq = reinterpret_cast<const R *>(a.Nq) + (i64)toy * " << nl.nq << ";\n";
+    for(auto &an : nl.analytic) {
+        os << ind << "const R N" << an.node << " = Pr[" << an.slotN << "];\n";
         if(grad)
-            for(int s : T.dep_norm[i]) {
-                std::string dexpr;
-                if(kind == NK_NUMERIC) {
-                    const NumInfo &g = T.nums[T.num_of[i]];
-                    dexpr = "-" + N + " * " + N + " * (" + lit(g.volume) + " / " + lit((double)g.total) + ") * gs" +
-                            std::to_string(i) + "[" + std::to_string(1 + s) + "]";
-                } else {
-                    dexpr = "-" + N + " * " + N + " * dI" + std::to_string(i);
-                }
-                os << "    const R dN" << i << "_" << s << " = (R)(" << dexpr << ");\n";
-            }
+            for(auto &d : an.dN)
+                os << ind << "const R dN" << an.node << "_" << d.first << " = Pr[" << d.second << "];\n";
+    }
+    for(size_t q = 0; q < T.nums.size(); ++q) {
+        int i = T.nums[q].node;
+        os << ind << "const R N" << i << " = Nq[" << nl.qN[q] << "];\n";
+        if(grad)
+            for(auto &d : nl.qdN[q])
+                os << ind << "const R dN" << i << "_" << d.first << " = Nq[" << d.second << "];\n";
     }
 }
+
+int padComps(int c) { return c <= 1 ? 1 : c <= 2 ? 2 : (c + 3) / 4 * 4; }
 
 struct Gen {
     const Tree &T;
@@ -424,42 +507,57 @@ struct Gen {
 
     int convComps(int ci, bool grad) const { return 1 + (grad ? (int)T.convs[ci].dep.size() : 0); }
 
+    // Table layout per toy: for each conv, AoS [k][cp] with cp = padded component count (16-byte rows).
+    void tableLayout(bool grad) {
+        auto &off = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
+        auto &cps = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
+        off.clear();
+        cps.clear();
+        int64_t total = 0;
+        for(size_t ci = 0; ci < T.convs.size(); ++ci) {
+            int cp = padComps(convComps((int)ci, grad));
+            total  = (total + 3) / 4 * 4;
+            off.push_back(total);
+            cps.push_back(cp);
+            total += (int64_t)cp * T.convs[ci].nK;
+        }
+        total = (total + 3) / 4 * 4;
+        (grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd) = total;
+    }
+
     // ---------------- convolution tables ----------------
+    // T_c[k] = sum_m A_c[m] B_c[m + off - k] for k in [kmin, kmax].  One CTA covers KB consecutive k; a
+    // thread owns KT consecutive k of one component over a contiguous slice of m (MS slices per k-tile),
+    // keeping a sliding window of the resolution values in registers (KT FMAs per two shared loads).
+    // The MS lane partials are combined with a compensated (two-sum) shuffle reduction.
     void convKernel(bool grad) {
         const char *sfx = grad ? "g" : "n";
-        int NC          = (int)T.convs.size();
+        const int NC    = (int)T.convs.size();
         if(NC == 0)
             return;
-        const int MS = 8; // lanes sharing one (k, component) sum
-        auto &off    = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
-        int64_t total = 0;
-        off.clear();
-        size_t smem = 0;
+        const int MS = 8, KT = 8;
+        const int items = block / MS;
+        auto &off       = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
+        auto &cps       = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
+        const int64_t total = grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd;
+        size_t smem   = 0;
         int maxBlocks = 0;
-        std::vector<int> tks;
+        std::vector<int> KBs;
         for(int ci = 0; ci < NC; ++ci) {
-            off.push_back(total);
-            total += (int64_t)convComps(ci, grad) * T.convs[ci].nK;
-            int comps = convComps(ci, grad);
-            int tk    = std::max(1, block / (comps * MS));
-            tks.push_back(tk);
             const ConvInfo &cv = T.convs[ci];
+            int comps          = convComps(ci, grad);
+            if(comps > items)
+                throw std::runtime_error("codegen: too many convolution derivative components");
+            int ktiles = items / comps;
+            int KB     = KT * ktiles;
+            KBs.push_back(KB);
             int mcomp = 1 + (grad ? (int)T.dep_val[cv.model].size() : 0);
             int rcomp = 1 + (grad ? (int)T.dep_val[cv.resol].size() : 0);
-            size_t sm = (size_t)(mcomp * cv.nM + rcomp * (cv.nM + tk - 1)) * (mixed ? 4 : 8);
+            size_t sm = (size_t)(mcomp * cv.nM + rcomp * (cv.nM + KB)) * (mixed ? 4 : 8);
             smem      = std::max(smem, sm);
-            maxBlocks = std::max(maxBlocks, (cv.nK + tk - 1) / tk);
+            maxBlocks = std::max(maxBlocks, (cv.nK + KB - 1) / KB);
         }
-        if(grad) {
-            plan.ctab_per_toy_grad = total;
-            plan.conv_smem_grad    = smem;
-            plan.ctab_comps_grad.clear();
-            for(int ci = 0; ci < NC; ++ci)
-                plan.ctab_comps_grad.push_back(convComps(ci, true));
-        } else {
-            plan.ctab_per_toy_nograd = total;
-            plan.conv_smem_nograd    = smem;
-        }
+        (grad ? plan.conv_smem_grad : plan.conv_smem_nograd) = smem;
         plan.conv_blocks = std::max(plan.conv_blocks, maxBlocks);
 
         os << "extern \"C\" __global__ void __launch_bounds__(" << block << ") gf_conv_" << sfx
@@ -467,126 +565,124 @@ struct Gen {
         os << "  extern __shared__ __align__(16) unsigned char smraw[];\n";
         os << "  R *sm = reinterpret_cast<R *>(smraw);\n";
         os << "  const int toy = blockIdx.y; const int ci = blockIdx.z; const int tid = threadIdx.x;\n";
+        os << "  gf_pdl_trigger();\n";
         os << "  if(a.active && !a.active[toy]) return;\n";
-        emitParams(os, T);
+        emitParamsR(os, T, plan.nl, "  ");
         os << "  R *ctab = reinterpret_cast<R *>(a.ctab) + (i64)toy * " << total << ";\n";
         os << "  switch(ci) {\n";
         for(int ci = 0; ci < NC; ++ci) {
             const ConvInfo &cv = T.convs[ci];
-            int comps = convComps(ci, grad), tk = tks[ci];
+            const int comps = convComps(ci, grad), KB = KBs[ci], ktiles = items / comps, cp = cps[ci];
             const auto &dm = T.dep_val[cv.model];
             const auto &dr = T.dep_val[cv.resol];
-            int mcomp = 1 + (grad ? (int)dm.size() : 0);
-            int rcomp = 1 + (grad ? (int)dr.size() : 0);
-            int win   = cv.nM + tk - 1;
+            const int mcomp = 1 + (grad ? (int)dm.size() : 0);
+            const int W1    = cv.nM + KB; // window entries (one spare for the last shift)
             os << "  case " << ci << ": {\n";
-            os << "    const int k0 = " << cv.kmin << " + (int)blockIdx.x * " << tk << ";\n";
+            os << "    const int k0 = " << cv.kmin << " + (int)blockIdx.x * " << KB << ";\n";
             os << "    if(k0 > " << cv.kmax << ") return;\n";
             os << "    R *sM = sm; R *sR = sm + " << mcomp * cv.nM << ";\n";
-            os << "    const int rbase = " << cv.offset << " - (k0 + " << tk - 1 << ");\n";
-            // model workspace
-            os << "    for(int m = tid; m < " << cv.nM << "; m += " << block << ") {\n";
-            os << "      const R wx = (R)gf_centre(" << lit(cv.ic[0]) << ", " << lit(cv.ic[1]) << ", " << cv.nM
-               << ", m);\n";
-            {
+            os << "    const int rbase = " << cv.offset << " - (k0 + " << KB - 1 << ");\n";
+            const double wM = (cv.ic[1] - cv.ic[0]) / cv.nM, wR = (cv.ic[4] - cv.ic[3]) / cv.nR;
+            for(int pass = 0; pass < 2; ++pass) {
+                bool model = pass == 0;
+                int sub    = model ? cv.model : cv.resol;
+                const auto &dd = model ? dm : dr;
+                int len        = model ? cv.nM : W1;
+                if(model)
+                    os << "    for(int m = tid; m < " << cv.nM << "; m += " << block << ") {\n"
+                       << "      const R wx = (R)GF_CENTRE(" << lit(cv.ic[0]) << ", " << lit(wM) << ", m);\n";
+                else
+                    os << "    for(int w = tid; w < " << W1 << "; w += " << block << ") {\n"
+                       << "      const int r = rbase + w;\n"
+                       << "      if(r < 0 || r >= " << cv.nR << ") {\n"
+                       << "        for(int c = 0; c < " << 1 + (grad ? (int)dr.size() : 0) << "; ++c) sR[c * " << W1
+                       << " + w] = R(0);\n"
+                       << "        continue;\n      }\n"
+                       << "      const R wx = (R)GF_CENTRE(" << lit(cv.ic[3]) << ", " << lit(wR) << ", r);\n";
                 std::ostringstream body;
                 Ctx c{body, T, grad, false, nullptr, nullptr, nullptr, nullptr};
-                c.x = [&](int) { return std::string("wx"); };
-                c.k = [&](int) -> std::string { throw std::runtime_error("codegen: conv in workspace"); };
+                c.x   = [&](int) { return std::string("wx"); };
+                c.k   = [&](int) -> std::string { throw std::runtime_error("codegen: conv in workspace"); };
                 c.tab = [&](int, int) -> std::string { throw std::runtime_error("codegen: conv in workspace"); };
-                c.uid = 0;
-                Val v = emit(c, cv.model);
+                c.uid = model ? 0 : 1000;
+                Val v = emit(c, sub);
+                std::string idx = model ? "m" : "w";
                 os << "      {\n" << body.str();
-                os << "      sM[m] = " << v.v << ";\n";
+                os << "      " << (model ? "sM" : "sR") << "[" << idx << "] = " << v.v << ";\n";
                 if(grad)
-                    for(size_t j = 0; j < dm.size(); ++j) {
-                        auto it = v.g.find(dm[j]);
-                        os << "      sM[" << (1 + j) * cv.nM << " + m] = "
+                    for(size_t j = 0; j < dd.size(); ++j) {
+                        auto it = v.g.find(dd[j]);
+                        os << "      " << (model ? "sM" : "sR") << "[" << (1 + j) * len << " + " << idx << "] = "
                            << (it == v.g.end() ? std::string("R(0)") : it->second) << ";\n";
                     }
-                os << "      }\n";
+                os << "      }\n    }\n";
             }
-            os << "    }\n";
-            // resolution window
-            os << "    for(int w = tid; w < " << win << "; w += " << block << ") {\n";
-            os << "      const int r = rbase + w;\n";
-            os << "      if(r < 0 || r >= " << cv.nR << ") continue;\n";
-            os << "      const R wx = (R)gf_centre(" << lit(cv.ic[3]) << ", " << lit(cv.ic[4]) << ", " << cv.nR
-               << ", r);\n";
-            {
-                std::ostringstream body;
-                Ctx c{body, T, grad, false, nullptr, nullptr, nullptr, nullptr};
-                c.x = [&](int) { return std::string("wx"); };
-                c.k = [&](int) -> std::string { throw std::runtime_error("codegen: conv in workspace"); };
-                c.tab = [&](int, int) -> std::string { throw std::runtime_error("codegen: conv in workspace"); };
-                c.uid = 1000;
-                Val v = emit(c, cv.resol);
-                os << "      {\n" << body.str();
-                os << "      sR[w] = " << v.v << ";\n";
-                if(grad)
-                    for(size_t j = 0; j < dr.size(); ++j) {
-                        auto it = v.g.find(dr[j]);
-                        os << "      sR[" << (1 + j) * win << " + w] = "
-                           << (it == v.g.end() ? std::string("R(0)") : it->second) << ";\n";
-                    }
-                os << "      }\n";
-            }
-            os << "    }\n";
             os << "    __syncthreads();\n";
-            // table entries: lanes (kk, comp, ms)
-            os << "    const int ms = tid % " << MS << "; const int comp = (tid / " << MS << ") % " << comps
-               << "; const int kk = tid / " << MS * comps << ";\n";
-            os << "    const int k = k0 + kk;\n";
-            os << "    const bool live = kk < " << tk << " && k <= " << cv.kmax << ";\n";
-            os << "    ACC acc = 0;\n";
+            os << "    const int ms = tid % " << MS << ", item = tid / " << MS << ", comp = item % " << comps
+               << ", kt = item / " << comps << ";\n";
+            os << "    const bool live = kt < " << ktiles << ";\n";
+            os << "    const int kt0 = k0 + kt * " << KT << ";\n";
+            os << "    const int c0 = " << KB - 1 << " - kt * " << KT << ";\n";
+            os << "    const int mlo = (" << cv.nM << " * ms) / " << MS << ", mhi = (" << cv.nM << " * (ms + 1)) / " << MS
+               << ";\n";
+            os << "    R acc[" << KT << "];\n#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) acc[j] = R(0);\n";
             os << "    if(live) {\n";
-            os << "      const int rb = " << cv.offset << " - k - rbase;\n"; // window index of r for m = 0
-            os << "      const R *mA; const R *rA; const R *mB = nullptr; const R *rB = nullptr;\n";
+            os << "      const R *mA[2] = {nullptr, nullptr}; const R *rA[2] = {nullptr, nullptr};\n";
             os << "      switch(comp) {\n";
-            os << "      case 0: mA = sM; rA = sR; break;\n";
+            os << "      case 0: mA[0] = sM; rA[0] = sR; break;\n";
             if(grad)
                 for(size_t j = 0; j < cv.dep.size(); ++j) {
-                    int s = cv.dep[j];
-                    auto im = std::find(dm.begin(), dm.end(), s);
-                    auto ir = std::find(dr.begin(), dr.end(), s);
+                    int sl  = cv.dep[j];
+                    auto im = std::find(dm.begin(), dm.end(), sl);
+                    auto ir = std::find(dr.begin(), dr.end(), sl);
                     os << "      case " << 1 + j << ": ";
-                    bool first = true;
+                    int t = 0;
                     if(im != dm.end()) {
-                        os << "mA = sM + " << (1 + (im - dm.begin())) * cv.nM << "; rA = sR; ";
-                        first = false;
+                        os << "mA[" << t << "] = sM + " << (1 + (im - dm.begin())) * cv.nM << "; rA[" << t << "] = sR; ";
+                        ++t;
                     }
                     if(ir != dr.end()) {
-                        if(first)
-                            os << "mA = sM; rA = sR + " << (1 + (ir - dr.begin())) * win << "; ";
-                        else
-                            os << "mB = sM; rB = sR + " << (1 + (ir - dr.begin())) * win << "; ";
+                        os << "mA[" << t << "] = sM; rA[" << t << "] = sR + " << (1 + (ir - dr.begin())) * W1 << "; ";
+                        ++t;
                     }
                     os << "break;\n";
                 }
-            os << "      default: mA = sM; rA = sR; break;\n";
-            os << "      }\n";
-            os << "      R s0 = R(0), s1 = R(0);\n";
-            os << "      for(int m = ms; m < " << cv.nM << "; m += " << MS << ") { s0 = fma(mA[m], rA[m + rb], s0); }\n";
-            os << "      if(mB) for(int m = ms; m < " << cv.nM << "; m += " << MS << ") { s1 = fma(mB[m], rB[m + rb], s1); }\n";
-            os << "      acc = (ACC)s0 + (ACC)s1;\n";
+            os << "      default: break;\n      }\n";
+            os << "      for(int t = 0; t < 2; ++t) {\n";
+            os << "        if(!mA[t]) break;\n";
+            os << "        const R *M = mA[t]; const R *Rw = rA[t] + c0;\n";
+            os << "        R rv[" << KT << "];\n#pragma unroll\n        for(int j = 0; j < " << KT
+               << "; ++j) rv[j] = Rw[mlo - j];\n";
+            os << "        for(int m = mlo; m < mhi; ++m) {\n";
+            os << "          const R mv = M[m];\n";
+            os << "#pragma unroll\n          for(int j = 0; j < " << KT << "; ++j) acc[j] = fma(mv, rv[j], acc[j]);\n";
+            os << "#pragma unroll\n          for(int j = " << KT - 1 << "; j > 0; --j) rv[j] = rv[j - 1];\n";
+            os << "          rv[0] = Rw[m + 1];\n";
+            os << "        }\n      }\n    }\n";
+            os << "#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) {\n";
+            os << "      const R t = gf_group_sum(acc[j], " << MS << ");\n";
+            os << "      const int k = kt0 + j;\n";
+            os << "      if(live && ms == 0 && k <= " << cv.kmax << ") ctab[" << off[ci] << " + (k - " << cv.kmin << ") * "
+               << cp << " + comp] = t;\n";
             os << "    }\n";
-            os << "#pragma unroll\n    for(int o = " << MS / 2 << "; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, " << MS << ");\n";
-            os << "    if(live && ms == 0) ctab[" << off[ci] << " + comp * " << cv.nK << " + (k - " << cv.kmin
-               << ")] = (R)acc;\n";
             os << "    break; }\n";
         }
         os << "  }\n}\n\n";
     }
 
     // ---------------- numeric grids ----------------
+    // One CTA row per numeric node; the finishing CTA of a (toy, node) turns the grid sum into the node's
+    // normalisation factor and its derivatives (GooPdf::normalize numeric branch,
+    // src/PDFs/GooPdf.cu:366-395) and stores them for the event pass.
     void gridKernel(bool grad) {
         const char *sfx = grad ? "g" : "n";
-        int NQ          = (int)T.nums.size();
+        const int NQ    = (int)T.nums.size();
         if(NQ == 0)
             return;
-        int NGp = 1 + (grad ? T.NG : 0); // components reduced
-        int NGs = 1 + T.NG;              // buffer stride
-        int BPB = plan.grid_bins_per_block;
+        const int NGp = 1 + (grad ? T.NG : 0); // components reduced
+        const int NGs = 1 + T.NG;              // buffer stride
+        const int BPB = plan.grid_bins_per_block;
+        const int NW  = block / 32;
         plan.grid_blocks.clear();
         plan.max_grid_blocks = 0;
         for(auto &g : T.nums) {
@@ -594,34 +690,40 @@ struct Gen {
             plan.grid_blocks.push_back(nb);
             plan.max_grid_blocks = std::max(plan.max_grid_blocks, nb);
         }
-        int64_t ctabTotal = grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd;
-        auto &off         = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
+        const int64_t ctabTotal = grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd;
+        auto &off               = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
+        auto &cps               = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
+        const NormLayout &nl    = plan.nl;
         os << "extern \"C\" __global__ void __launch_bounds__(" << block << ") gf_grid_" << sfx
            << "(const GfArgs a) {\n";
         os << "  const int toy = blockIdx.y; const int q = blockIdx.z; const int tid = threadIdx.x;\n";
+        os << "  const int lane = tid & 31, wid = tid >> 5;\n";
+        os << "  gf_pdl_trigger();\n";
+        os << "  gf_pdl_wait();\n";
         os << "  if(a.active && !a.active[toy]) return;\n";
-        emitParams(os, T);
+        emitParamsR(os, T, nl, "  ");
         os << "  const R *ctab = reinterpret_cast<const R *>(a.ctab) + (i64)toy * " << ctabTotal << ";\n";
         os << "  (void)ctab;\n";
         os << "  R av = R(0);\n";
-        for(int s = 0; s < (grad ? T.NG : 0); ++s)
+        for(int s = 0; s < NGp - 1; ++s)
             os << "  R ag" << s << " = R(0);\n";
-        os << "  i64 total = 0; int nblk = 0;\n";
+        os << "  int nblk = 0;\n";
         os << "  switch(q) {\n";
         for(int q = 0; q < NQ; ++q) {
             const NumInfo &g = T.nums[q];
             os << "  case " << q << ": {\n";
-            os << "    total = " << g.total << "LL; nblk = " << plan.grid_blocks[q] << ";\n";
+            os << "    nblk = " << plan.grid_blocks[q] << ";\n";
             os << "    if((int)blockIdx.x >= nblk) return;\n";
-            os << "    const i64 bend = min(total, (i64)(blockIdx.x + 1) * " << BPB << ");\n";
+            os << "    const i64 bend = min((i64)" << g.total << "LL, (i64)(blockIdx.x + 1) * " << BPB << ");\n";
             os << "    for(i64 b = (i64)blockIdx.x * " << BPB << " + tid; b < bend; b += " << block << ") {\n";
             os << "      i64 bb = b;\n";
             for(size_t ax = 0; ax < g.obs.size(); ++ax) {
                 const gf_observable &o = T.obs[g.obs[ax]];
+                double w               = (o.hi - o.lo) / g.nbins[ax];
                 os << "      const int lb" << ax << " = (int)(bb % " << g.nbins[ax] << "); bb /= " << g.nbins[ax]
                    << ";\n";
-                os << "      const R gx" << g.obs[ax] << " = (R)gf_centre(" << lit(o.lo) << ", " << lit(o.hi) << ", "
-                   << g.nbins[ax] << ", lb" << ax << ");\n";
+                os << "      const R gx" << g.obs[ax] << " = (R)GF_CENTRE(" << lit(o.lo) << ", " << lit(w) << ", lb"
+                   << ax << ");\n";
             }
             std::ostringstream body;
             Ctx c{body, T, grad, false, nullptr, nullptr, nullptr, nullptr};
@@ -629,14 +731,14 @@ struct Gen {
             c.k = [&](int ci) -> std::string {
                 for(size_t j = 0; j < g.convs.size(); ++j)
                     if(g.convs[j] == ci)
-                        return "a.kgrid[" + std::to_string(g.kgrid_off[j]) + " + lb" +
-                               std::to_string(g.conv_axis[j]) + "]";
+                        return "a.kgrid[" + std::to_string(g.kgrid_off[j]) + " + lb" + std::to_string(g.conv_axis[j]) +
+                               "]";
                 throw std::runtime_error("codegen: conv without grid k");
             };
             c.tab = [&](int ci, int comp) {
                 const ConvInfo &cv = T.convs[ci];
-                return "ctab[" + std::to_string(off[ci]) + " + " + std::to_string(comp * cv.nK) + " + (" + c.k(ci) +
-                       " - " + std::to_string(cv.kmin) + ")]";
+                return "ctab[" + std::to_string(off[ci]) + " + (" + c.k(ci) + " - " + std::to_string(cv.kmin) + ") * " +
+                       std::to_string(cps[ci]) + " + " + std::to_string(comp) + "]";
             };
             Val v = emit(c, g.node);
             os << "      {\n" << body.str();
@@ -649,51 +751,83 @@ struct Gen {
             os << "    break; }\n";
         }
         os << "  default: return;\n  }\n";
-        // block reduction of NGp doubles
-        os << "  __shared__ double red[" << block / 32 << "][" << NGp << "];\n";
+        os << "  __shared__ ACC red[" << NW << "][" << NGp << "];\n";
+        os << "  __shared__ ACC tot[" << NGp << "];\n";
         os << "  __shared__ int last;\n";
-        os << "  const int lane = tid & 31, wid = tid >> 5;\n";
-        os << "  { double t = gf_warp_sum((double)av); if(lane == 0) red[wid][0] = t; }\n";
+        os << "  { const ACC t = warp_acc(av); if(lane == 0) red[wid][0] = t; }\n";
         for(int s = 0; s < NGp - 1; ++s)
-            os << "  { double t = gf_warp_sum((double)ag" << s << "); if(lane == 0) red[wid][" << 1 + s
-               << "] = t; }\n";
+            os << "  { const ACC t = warp_acc(ag" << s << "); if(lane == 0) red[wid][" << 1 + s << "] = t; }\n";
         os << "  __syncthreads();\n";
-        os << "  double *gp = a.gpartial + (((i64)toy * " << NQ << " + q) * " << plan.max_grid_blocks
+        os << "  ACC *gp = reinterpret_cast<ACC *>(a.gpartial) + (((i64)toy * " << NQ << " + q) * " << plan.max_grid_blocks
            << " + blockIdx.x) * " << NGs << ";\n";
-        os << "  if(tid < " << NGp << ") { double t = 0; for(int w = 0; w < " << block / 32
-           << "; ++w) t += red[w][tid]; gp[tid] = t; }\n";
+        os << "  if(tid < " << NGp << ") { ACC t = acc_zero(); for(int w = 0; w < " << NW
+           << "; ++w) t = acc_add(t, red[w][tid]); gp[tid] = t; }\n";
         os << "  __threadfence();\n  __syncthreads();\n";
         os << "  if(tid == 0) { unsigned prev = atomicAdd(&a.gcounter[toy * " << NQ
            << " + q], 1u); last = (prev == (unsigned)(nblk - 1)); }\n";
         os << "  __syncthreads();\n";
-        os << "  if(last) {\n";
-        os << "    __threadfence();\n";
-        os << "    const double *g0 = a.gpartial + ((i64)toy * " << NQ << " + q) * " << plan.max_grid_blocks << " * "
-           << NGs << ";\n";
-        os << "    if(tid < " << NGp << ") { double t = 0; for(int bi = 0; bi < nblk; ++bi) t += g0[bi * " << NGs
-           << " + tid]; a.gsum[((i64)toy * " << NQ << " + q) * " << NGs << " + tid] = t; }\n";
-        os << "    if(tid == 0) a.gcounter[toy * " << NQ << " + q] = 0u;\n";
-        os << "  }\n}\n\n";
+        os << "  if(!last) return;\n";
+        os << "  __threadfence();\n";
+        os << "  const ACC *g0 = reinterpret_cast<const ACC *>(a.gpartial) + ((i64)toy * " << NQ << " + q) * "
+           << plan.max_grid_blocks << " * " << NGs << ";\n";
+        os << "  {\n";
+        os << "    ACC s[" << NGp << "];\n";
+        os << "#pragma unroll\n    for(int comp = 0; comp < " << NGp << "; ++comp) s[comp] = acc_zero();\n";
+        os << "    for(int bi = tid; bi < nblk; bi += " << block << ") {\n";
+        os << "#pragma unroll\n      for(int comp = 0; comp < " << NGp << "; ++comp) s[comp] = acc_add(s[comp], g0[bi * " << NGs << " + comp]);\n";
+        os << "    }\n";
+        os << "#pragma unroll\n    for(int comp = 0; comp < " << NGp << "; ++comp) { const ACC t = warp_acc2(s[comp]); if(lane == 0) red[wid][comp] = t; }\n";
+        os << "  }\n";
+        os << "  __syncthreads();\n";
+        os << "  if(tid < " << NGp << ") { ACC t = acc_zero(); for(int w = 0; w < " << NW << "; ++w) t = acc_add(t, red[w][tid]); tot[tid] = t; }\n";
+        os << "  __syncthreads();\n";
+        os << "  if(tid == 0) {\n";
+        os << "    a.gcounter[toy * " << NQ << " + q] = 0u;\n";
+        os << "    R *Nq = reinterpret_cast<R *>(a.Nq) + (i64)toy * " << nl.nq << ";\n";
+        os << "    const double S = acc_value(tot[0]);\n";
+        os << "    a.gsum[(i64)toy * " << NQ << " + q] = S;\n";
+        os << "    if(isnan(S)) atomicOr(&a.qflag[toy], 1); else if(!(S > 0.0)) atomicOr(&a.qflag[toy], 2);\n";
+        os << "    switch(q) {\n";
+        for(int q = 0; q < NQ; ++q) {
+            const NumInfo &g = T.nums[q];
+            // ((1 * volume) / bins), the reference's order of operations, evaluated on the host
+            double c = 1.0;
+            c *= g.volume;
+            c /= (double)g.total;
+            os << "    case " << q << ": {\n";
+            os << "      const double I = " << lit(c) << " * S;\n";
+            if(mixed)
+                os << "      const R N = 1.0f / (float)I;\n";
+            else
+                os << "      const R N = 1.0 / I;\n";
+            os << "      Nq[" << nl.qN[q] << "] = N;\n";
+            if(grad)
+                for(auto &d : nl.qdN[q])
+                    os << "      Nq[" << d.second << "] = -N * N * (R)" << lit(c) << " * (R)acc_r(tot[" << 1 + d.first
+                       << "]);\n";
+            os << "      break; }\n";
+        }
+        os << "    }\n  }\n}\n\n";
     }
 
     // ---------------- event pass ----------------
+    // Persistent CTAs take contiguous ranges of the chunk list and stage a toy's conv tables once; each
+    // thread streams 8 events per iteration with 16-byte loads.  Partial sums: FP32 per thread, then
+    // compensated FP32 pairs across the warp, the CTA, the chunks of a toy; FP64 for the final value.
     void eventKernel(bool grad, bool values) {
-        std::string name = values ? "gf_val_n" : (grad ? "gf_evt_g" : "gf_evt_n");
-        int NGp          = 1 + (grad ? T.NG : 0); // components reduced
-        int NGs          = 1 + T.NG;              // buffer stride
-        int NC           = (int)T.convs.size();
-        int NO           = (int)T.obs.size();
-        auto &off        = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
-        int64_t ctabTotal = grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd;
-        // shared-memory staging of the toy's conv tables
-        size_t smemElems = (size_t)ctabTotal;
-        if(!values) {
-            if(grad)
-                plan.evt_smem_grad = smemElems * (mixed ? 4 : 8);
-            else
-                plan.evt_smem_nograd = smemElems * (mixed ? 4 : 8);
-        }
-        // body: tree code for one event, into a string so that used columns are known
+        const std::string name = values ? "gf_val_n" : (grad ? "gf_evt_g" : "gf_evt_n");
+        const int NGp = 1 + (grad ? T.NG : 0);
+        const int NGs = 1 + T.NG;
+        const int NC  = (int)T.convs.size();
+        const int NO  = (int)T.obs.size();
+        const int NW  = block / 32;
+        const int VEC = 8;
+        auto &off     = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
+        auto &cps     = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
+        const int64_t ctabTotal = grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd;
+        if(!values)
+            (grad ? plan.evt_smem_grad : plan.evt_smem_nograd) = (size_t)ctabTotal * (mixed ? 4 : 8);
+
         std::vector<int> xused(NO, 0);
         std::ostringstream body;
         Ctx c{body, T, grad, true, nullptr, nullptr, nullptr, &xused};
@@ -701,11 +835,17 @@ struct Gen {
             xused[o] = 1;
             return "ex" + std::to_string(o);
         };
-        c.k = [&](int ci) { return "ek" + std::to_string(ci); };
-        c.tab = [&](int ci, int comp) {
-            const ConvInfo &cv = T.convs[ci];
-            return "stab[" + std::to_string(off[ci] + (int64_t)comp * cv.nK) + " + (ek" + std::to_string(ci) + " - " +
-                   std::to_string(cv.kmin) + ")]";
+        c.k   = [&](int ci) { return "ek" + std::to_string(ci); };
+        c.tab = [&](int ci, int comp) -> std::string {
+            int cp = cps[ci];
+            if(!mixed)
+                return "tp" + std::to_string(ci) + "[" + std::to_string(comp) + "]";
+            if(cp == 1)
+                return "tq" + std::to_string(ci);
+            const char *fld[] = {".x", ".y", ".z", ".w"};
+            if(cp == 2)
+                return "tq" + std::to_string(ci) + fld[comp];
+            return "tq" + std::to_string(ci) + "_" + std::to_string(comp / 4) + fld[comp % 4];
         };
         Val root = emit(c, 0);
         if(!values && !grad) {
@@ -714,33 +854,62 @@ struct Gen {
                 if(xused[o])
                     plan.obs_used_evt.push_back(o);
         }
-        std::string rootN = T.nk[0] == NK_ONE ? "" : "N0";
+        const std::string rootN = T.nk[0] == NK_ONE ? "" : "N0";
 
         os << "extern \"C\" __global__ void __launch_bounds__(" << block << ") " << name << "(const GfArgs a) {\n";
         os << "  extern __shared__ __align__(16) unsigned char smraw[];\n";
         os << "  R *stab = reinterpret_cast<R *>(smraw); (void)stab;\n";
-        os << "  __shared__ double red[" << block / 32 << "][" << NGp << "];\n";
-        os << "  __shared__ int last;\n";
-        os << "  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;\n";
-        os << "  for(int ch = blockIdx.x; ch < a.n_chunks; ch += gridDim.x) {\n";
+        os << "  __shared__ int s_toy, last;\n";
+        if(!values)
+            os << "  __shared__ ACC red[" << NW << "][" << NGp << "];\n";
+        os << "  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5; (void)lane; (void)wid;\n";
+        os << "  const int cb = (int)(((i64)a.n_chunks * blockIdx.x) / gridDim.x);\n";
+        os << "  const int ce = (int)(((i64)a.n_chunks * (blockIdx.x + 1)) / gridDim.x);\n";
+        os << "  if(tid == 0) s_toy = -1;\n";
+        os << "  gf_pdl_trigger();\n";
+        // event columns do not depend on the preceding kernels: pull the first chunk towards L2 meanwhile
+        os << "  if(cb < ce) {\n";
+        os << "    const i64 *cd = a.chunks + 3 * (i64)cb;\n";
+        os << "    const int toy = (int)cd[0]; const i64 b0 = cd[1], e0 = cd[2];\n";
+        os << "    if(!a.active || a.active[toy]) {\n";
+        os << "      for(i64 i0 = b0 + " << VEC << " * (i64)tid; i0 < e0; i0 += " << VEC << " * " << block << ") {\n";
+        for(int o = 0; o < NO; ++o)
+            if(xused[o])
+                os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(reinterpret_cast<const R *>(a.col[(i64)toy * "
+                   << NO << " + " << o << "]) + i0));\n";
+        for(int ci = 0; ci < NC; ++ci)
+            os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(a.kcol[(i64)toy * " << NC << " + " << ci
+               << "] + i0));\n";
+        os << "      }\n    }\n  }\n";
+        os << "  gf_pdl_wait();\n";
+        os << "  __syncthreads();\n";
+        os << "  for(int ch = cb; ch < ce; ++ch) {\n";
         os << "    const i64 *cd = a.chunks + 3 * (i64)ch;\n";
         os << "    const int toy = (int)cd[0]; const i64 b0 = cd[1], e0 = cd[2];\n";
         os << "    if(a.active && !a.active[toy]) continue;\n";
-        {
-            std::ostringstream pr;
-            emitParams(pr, T);
-            emitNorms(pr, T, grad);
-            os << pr.str();
-        }
         if(NC > 0) {
-            os << "    { const R *src = reinterpret_cast<const R *>(a.ctab) + (i64)toy * " << ctabTotal << ";\n";
-            os << "      for(int i = tid; i < " << ctabTotal << "; i += " << block << ") stab[i] = src[i]; }\n";
+            os << "    if(toy != s_toy) {\n";
+            os << "      __syncthreads();\n";
+            if(mixed)
+                os << "      { const float4 *src = reinterpret_cast<const float4 *>(reinterpret_cast<const R *>(a.ctab) + "
+                      "(i64)toy * "
+                   << ctabTotal << "); float4 *dst = reinterpret_cast<float4 *>(stab);\n"
+                   << "        for(int i = tid; i < " << ctabTotal / 4 << "; i += " << block << ") dst[i] = src[i]; }\n";
+            else
+                os << "      { const double2 *src = reinterpret_cast<const double2 *>(reinterpret_cast<const R *>(a.ctab) "
+                      "+ (i64)toy * "
+                   << ctabTotal << "); double2 *dst = reinterpret_cast<double2 *>(stab);\n"
+                   << "        for(int i = tid; i < " << ctabTotal / 2 << "; i += " << block << ") dst[i] = src[i]; }\n";
+            os << "      if(tid == 0) s_toy = toy;\n";
+            os << "      __syncthreads();\n";
+            os << "    }\n";
         }
-        os << "    __syncthreads();\n";
+        emitParamsR(os, T, plan.nl, "    ");
+        emitNormReads(os, T, grad, plan.nl, "    ");
         for(int o = 0; o < NO; ++o)
             if(xused[o])
-                os << "    const R *col" << o << " = reinterpret_cast<const R *>(a.col[(i64)toy * " << NO << " + "
-                   << o << "]);\n";
+                os << "    const R *col" << o << " = reinterpret_cast<const R *>(a.col[(i64)toy * " << NO << " + " << o
+                   << "]);\n";
         for(int ci = 0; ci < NC; ++ci)
             os << "    const int *kc" << ci << " = a.kcol[(i64)toy * " << NC << " + " << ci << "];\n";
         if(!values) {
@@ -748,30 +917,47 @@ struct Gen {
             for(int s = 0; s < NGp - 1; ++s)
                 os << "    R ag" << s << " = R(0);\n";
         }
-        os << "    for(i64 i0 = b0 + 4 * (i64)tid; i0 < e0; i0 += 4 * " << block << ") {\n";
+        os << "    for(i64 i0 = b0 + " << VEC << " * (i64)tid; i0 < e0; i0 += " << VEC << " * " << block << ") {\n";
         for(int o = 0; o < NO; ++o)
             if(xused[o]) {
                 if(mixed)
-                    os << "      const float4 xv" << o << " = *reinterpret_cast<const float4 *>(col" << o
-                       << " + i0);\n"
-                       << "      const R xa" << o << "[4] = {xv" << o << ".x, xv" << o << ".y, xv" << o << ".z, xv"
-                       << o << ".w};\n";
-                else
-                    os << "      const double2 xv" << o << "a = *reinterpret_cast<const double2 *>(col" << o
-                       << " + i0), xv" << o << "b = *reinterpret_cast<const double2 *>(col" << o << " + i0 + 2);\n"
-                       << "      const R xa" << o << "[4] = {xv" << o << "a.x, xv" << o << "a.y, xv" << o << "b.x, xv"
-                       << o << "b.y};\n";
+                    os << "      const float4 xv" << o << "a = *reinterpret_cast<const float4 *>(col" << o
+                       << " + i0), xv" << o << "b = *reinterpret_cast<const float4 *>(col" << o << " + i0 + 4);\n"
+                       << "      const R xa" << o << "[8] = {xv" << o << "a.x, xv" << o << "a.y, xv" << o << "a.z, xv" << o
+                       << "a.w, xv" << o << "b.x, xv" << o << "b.y, xv" << o << "b.z, xv" << o << "b.w};\n";
+                else {
+                    os << "      R xa" << o << "[8];\n";
+                    os << "#pragma unroll\n      for(int h = 0; h < 4; ++h) { const double2 t = "
+                          "*reinterpret_cast<const double2 *>(col"
+                       << o << " + i0 + 2 * h); xa" << o << "[2 * h] = t.x; xa" << o << "[2 * h + 1] = t.y; }\n";
+                }
             }
         for(int ci = 0; ci < NC; ++ci)
-            os << "      const int4 kv" << ci << " = *reinterpret_cast<const int4 *>(kc" << ci << " + i0);\n"
-               << "      const int ka" << ci << "[4] = {kv" << ci << ".x, kv" << ci << ".y, kv" << ci << ".z, kv"
-               << ci << ".w};\n";
-        os << "#pragma unroll\n      for(int j = 0; j < 4; ++j) {\n";
+            os << "      const int4 kv" << ci << "a = *reinterpret_cast<const int4 *>(kc" << ci << " + i0), kv" << ci
+               << "b = *reinterpret_cast<const int4 *>(kc" << ci << " + i0 + 4);\n"
+               << "      const int ka" << ci << "[8] = {kv" << ci << "a.x, kv" << ci << "a.y, kv" << ci << "a.z, kv" << ci
+               << "a.w, kv" << ci << "b.x, kv" << ci << "b.y, kv" << ci << "b.z, kv" << ci << "b.w};\n";
+        os << "#pragma unroll\n      for(int j = 0; j < " << VEC << "; ++j) {\n";
         for(int o = 0; o < NO; ++o)
             if(xused[o])
                 os << "        const R ex" << o << " = xa" << o << "[j];\n";
-        for(int ci = 0; ci < NC; ++ci)
+        for(int ci = 0; ci < NC; ++ci) {
+            const ConvInfo &cv = T.convs[ci];
+            int cp             = cps[ci];
             os << "        const int ek" << ci << " = ka" << ci << "[j];\n";
+            os << "        const R *tp" << ci << " = stab + " << off[ci] << " + (ek" << ci << " - " << cv.kmin << ") * "
+               << cp << "; (void)tp" << ci << ";\n";
+            if(mixed) {
+                if(cp == 1)
+                    os << "        const float tq" << ci << " = tp" << ci << "[0];\n";
+                else if(cp == 2)
+                    os << "        const float2 tq" << ci << " = *reinterpret_cast<const float2 *>(tp" << ci << ");\n";
+                else
+                    for(int g4 = 0; g4 < cp / 4; ++g4)
+                        os << "        const float4 tq" << ci << "_" << g4 << " = *reinterpret_cast<const float4 *>(tp"
+                           << ci << " + " << 4 * g4 << ");\n";
+            }
+        }
         os << "        {\n" << body.str();
         os << "        const R pv = " << root.v << (rootN.empty() ? "" : " * " + rootN) << ";\n";
         if(values) {
@@ -802,56 +988,39 @@ struct Gen {
         }
         os << "        }\n      }\n    }\n";
         if(values) {
-            os << "    __syncthreads();\n  }\n}\n\n";
+            os << "  }\n}\n\n";
             return;
         }
-        // block reduction
-        os << "    { double t = gf_warp_sum((double)av); if(lane == 0) red[wid][0] = t; }\n";
+        os << "    { const ACC t = warp_acc(av); if(lane == 0) red[wid][0] = t; }\n";
         for(int s = 0; s < NGp - 1; ++s)
-            os << "    { double t = gf_warp_sum((double)ag" << s << "); if(lane == 0) red[wid][" << 1 + s
-               << "] = t; }\n";
+            os << "    { const ACC t = warp_acc(ag" << s << "); if(lane == 0) red[wid][" << 1 + s << "] = t; }\n";
         os << "    __syncthreads();\n";
-        os << "    if(tid < " << NGp << ") { double t = 0; for(int w = 0; w < " << block / 32
-           << "; ++w) t += red[w][tid]; a.partial[(i64)ch * " << NGs << " + tid] = t; }\n";
+        os << "    ACC *part = reinterpret_cast<ACC *>(a.partial);\n";
+        os << "    if(tid < " << NGp << ") { ACC t = acc_zero(); for(int w = 0; w < " << NW
+           << "; ++w) t = acc_add(t, red[w][tid]); part[(i64)ch * " << NGs << " + tid] = t; }\n";
         os << "    __threadfence();\n    __syncthreads();\n";
-        os << "    if(tid == 0) { unsigned prev = atomicAdd(&a.counter[toy], 1u); last = (prev == (unsigned)(a.toy_nchunks[toy] - 1)); }\n";
+        os << "    if(tid == 0) { unsigned prev = atomicAdd(&a.counter[toy], 1u); last = (prev == "
+              "(unsigned)(a.toy_nchunks[toy] - 1)); }\n";
         os << "    __syncthreads();\n";
+        // finishing CTA of the toy: every thread loads a strided share of the chunk partials (independent
+        // loads), then a warp and a CTA reduction of the compensated pairs
         os << "    if(last) {\n";
         os << "      __threadfence();\n";
         os << "      const int c0 = a.toy_chunk0[toy], nc = a.toy_nchunks[toy];\n";
-        // deterministic: thread t sums chunks t, t+B, ... per component, then fixed-order tree
-        os << "      for(int comp = 0; comp < " << NGp << "; ++comp) {\n";
-        os << "        double t = 0; for(int c = tid; c < nc; c += " << block << ") t += a.partial[(i64)(c0 + c) * " << NGs
-           << " + comp];\n";
-        os << "        t = gf_warp_sum(t); if(lane == 0) red[wid][comp] = t;\n";
+        os << "      ACC s[" << NGp << "];\n";
+        os << "#pragma unroll\n      for(int comp = 0; comp < " << NGp << "; ++comp) s[comp] = acc_zero();\n";
+        os << "#pragma unroll 4\n      for(int c = tid; c < nc; c += " << block << ") {\n";
+        os << "        const ACC *pc = part + (i64)(c0 + c) * " << NGs << ";\n";
+        os << "#pragma unroll\n        for(int comp = 0; comp < " << NGp << "; ++comp) s[comp] = acc_add(s[comp], pc[comp]);\n";
         os << "      }\n";
+        os << "#pragma unroll\n      for(int comp = 0; comp < " << NGp << "; ++comp) { const ACC t = warp_acc2(s[comp]); if(lane == 0) red[wid][comp] = t; }\n";
         os << "      __syncthreads();\n";
-        os << "      if(tid == 0) {\n";
+        os << "      if(tid < " << NGp << ") {\n";
+        os << "        ACC t = acc_zero(); for(int w = 0; w < " << NW << "; ++w) t = acc_add(t, red[w][tid]);\n";
         os << "        double *o = a.out + (i64)toy * " << NGs + 1 << ";\n";
-        os << "        double s[" << NGp << "];\n";
-        os << "        for(int comp = 0; comp < " << NGp << "; ++comp) { double t = 0; for(int w = 0; w < "
-           << block / 32 << "; ++w) t += red[w][comp]; s[comp] = t; }\n";
-        if(T.extended_root) {
-            // AddPdf::calculateNLL extended term (src/PDFs/combine/AddPdf.cu:187-204)
-            os << "        { double ex = 0; ";
-            for(int p : T.nodes[0].params)
-                os << "ex += pd" << p << "; ";
-            os << "const double ne = (double)a.toy_nevents[toy]; s[0] += (ex - ne * log(ex));\n";
-            if(grad)
-                for(int p : T.nodes[0].params)
-                    if(T.gslot[p] >= 0)
-                        os << "          s[" << 1 + T.gslot[p] << "] += 1.0 - ne / ex;\n";
-            os << "        }\n";
-        }
-        os << "        int st = nflag;\n";
-        if(rootN.empty())
-            os << "        (void)0;\n";
-        else
-            os << "        if(!(Nd0 > 0.0)) st |= 2;\n";
-        os << "        if(s[0] == 0.0) st |= 4;\n";
-        os << "        o[0] = s[0]; o[1] = (double)st;\n";
-        os << "        for(int comp = 1; comp < " << NGp << "; ++comp) o[1 + comp] = s[comp];\n";
-        os << "        a.counter[toy] = 0u;\n";
+        os << "        const double v = acc_value(t);\n";
+        os << "        o[tid == 0 ? 0 : 1 + tid] = v;\n";
+        os << "        if(tid == 0) { int st = a.qflag[toy]; if(v == 0.0) st |= 4; o[1] = (double)st; a.counter[toy] = 0u; }\n";
         os << "      }\n";
         os << "    }\n";
         os << "    __syncthreads();\n";
@@ -861,17 +1030,24 @@ struct Gen {
 
 } // namespace
 
+NormLayout norm_layout(const Tree &t) { return computeNormLayout(t); }
+
 KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, int chunk) {
     KernelPlan plan;
+    plan.nl = norm_layout(t);
     Gen g{t, mixed, evt_block, chunk, plan, {}};
     g.os << "// generated likelihood kernels\n";
     if(mixed)
-        g.os << "typedef float R;\ntypedef double ACC;\n#define GF_EXP(x) expf(x)\n#define GF_LOG(x) logf(x)\n";
+        g.os << "typedef float R;\n#define GF_EXP(x) expf(x)\n#define GF_LOG(x) logf(x)\n";
     else
-        g.os << "typedef double R;\ntypedef double ACC;\n#define GF_EXP(x) exp(x)\n#define GF_LOG(x) log(x)\n";
+        g.os << "typedef double R;\n#define GF_EXP(x) exp(x)\n#define GF_LOG(x) log(x)\n";
     g.os << kPrelude;
-    g.os << "__device__ __forceinline__ double gf_centre(double lo, double hi, int n, int b) { double x = hi - lo; x /= n; "
-            "x *= (b + 0.5); x += lo; return x; }\n\n";
+    if(mixed)
+        g.os << kPreludeF32;
+    else
+        g.os << kPreludeF64;
+    g.tableLayout(true);
+    g.tableLayout(false);
     g.convKernel(true);
     g.convKernel(false);
     g.gridKernel(true);

@@ -28,7 +28,8 @@ struct ConvertArgs {
     void *cols[16];
     int *kcols[8];
     int conv_obs[8];
-    double conv_lo[8], conv_step[8];
+    double conv_lo[8], conv_step[8], conv_lbo[8];
+    float conv_inv_step[8], conv_lbo_f[8];
     int conv_kmin[8], conv_kmax[8];
     double pad_val[16];
     int *err;
@@ -49,10 +50,17 @@ __global__ void gf_convert_events(const ConvertArgs a) {
     for(int c = 0; c < a.n_conv; ++c) {
         int k;
         if(i < a.n) {
-            double x0  = a.soa[(long long)a.conv_obs[c] * a.n + i];
-            double lbo = a.conv_lo[c] / a.conv_step[c];
-            lbo -= floor(lbo);
-            k = (int)floor(x0 / a.conv_step[c] - lbo);
+            const double x0 = a.soa[(long long)a.conv_obs[c] * a.n + i];
+            // FP32 estimate of x0/step - frac(lo/step); its error is below 3e-7 (|q| + 1), so away from
+            // a bin edge its floor is the FP64 result, and near an edge the FP64 division decides
+            const float qf = fmaf((float)x0, a.conv_inv_step[c], -a.conv_lbo_f[c]);
+            const float kf = floorf(qf);
+            const float d  = qf - kf;
+            const float th = 4e-7f * (fabsf(qf) + 1.0f);
+            if(d > th && d < 1.0f - th)
+                k = (int)kf;
+            else
+                k = (int)floor(x0 / a.conv_step[c] - a.conv_lbo[c]);
             if(k < a.conv_kmin[c] || k > a.conv_kmax[c]) {
                 atomicOr(a.err, 1);
                 k = a.conv_kmin[c];
@@ -117,6 +125,8 @@ void freeLayout(gf_engine *e) {
     dfree(e->d_toy_chunk0);
     dfree(e->d_toy_nchunks);
     dfree(e->d_toy_nevents);
+    dfree(e->d_Nq);
+    dfree(e->d_qflag);
     hfree(e->h_P);
     hfree(e->h_active);
     hfree(e->h_out);
@@ -152,6 +162,16 @@ int buildLayout(gf_engine *e) {
     for(int t = 0; t < NT; ++t)
         if(!e->toys[t].loaded)
             return gf_fail(e, GF_ERR_STATE, "toy " + std::to_string(t) + " has no events");
+    // chunk size: about one chunk per resident event CTA, a multiple of 8 events x 256 threads
+    if(!e->chunk_fixed) {
+        int64_t total = 0;
+        for(int t = 0; t < NT; ++t)
+            total += e->toys[t].n;
+        const int64_t target = (int64_t)std::max(1, e->sm_count) * e->evt_ctas_per_sm;
+        int64_t ch           = (total + target - 1) / target;
+        ch                   = (ch + 2047) / 2048 * 2048;
+        e->chunk             = (int)std::min<int64_t>(std::max<int64_t>(ch, 2048), 1 << 20);
+    }
     std::vector<long long> chunks;
     std::vector<int> c0(NT), nc(NT);
     std::vector<long long> ne(NT);
@@ -173,7 +193,17 @@ int buildLayout(gf_engine *e) {
         if(r != GF_OK && rc == GF_OK)
             rc = r;
     };
-    chk(dalloc(e, e->d_P, (size_t)NT * std::max(1, T.n_params)));
+    const gf::NormLayout &nl = e->plan.nl;
+    e->pblock_bytes = sizeof(double) * (size_t)NT * std::max(1, T.n_params) + rsize(e) * (size_t)NT * std::max(1, nl.npr);
+    e->pblock_bytes = (e->pblock_bytes + 15) / 16 * 16;
+    chk(dalloc(e, e->d_P, e->pblock_bytes / sizeof(double)));
+    {
+        void *p = nullptr;
+        if(cudaMalloc(&p, rsize(e) * (size_t)NT * std::max(1, nl.nq)) != cudaSuccess)
+            chk(gf_fail(e, GF_ERR_OOM, "cudaMalloc numeric factors"));
+        e->d_Nq = p;
+    }
+    chk(dalloc(e, e->d_qflag, NT));
     chk(dalloc(e, e->d_active, NT));
     chk(dalloc(e, e->d_cols, (size_t)NT * NO));
     chk(dalloc(e, e->d_kcols, (size_t)NT * std::max(1, NC)));
@@ -188,7 +218,7 @@ int buildLayout(gf_engine *e) {
         e->d_ctab = p;
     }
     chk(dalloc(e, e->d_kgrid, std::max<size_t>(1, T.kgrid.size())));
-    chk(dalloc(e, e->d_gsum, (size_t)NT * std::max(1, NQ) * NGp));
+    chk(dalloc(e, e->d_gsum, (size_t)NT * std::max(1, NQ)));
     chk(dalloc(e, e->d_gpartial, (size_t)NT * std::max(1, NQ) * std::max(1, e->plan.max_grid_blocks) * NGp));
     chk(dalloc(e, e->d_gcounter, (size_t)NT * std::max(1, NQ)));
     chk(dalloc(e, e->d_partial, (size_t)e->n_chunks * NGp));
@@ -200,11 +230,12 @@ int buildLayout(gf_engine *e) {
     chk(dalloc(e, e->d_toy_nevents, NT));
     if(rc != GF_OK)
         return rc;
-    if(cudaMallocHost((void **)&e->h_P, sizeof(double) * (size_t)NT * std::max(1, T.n_params)) != cudaSuccess ||
+    if(cudaMallocHost((void **)&e->h_P, e->pblock_bytes) != cudaSuccess ||
        cudaMallocHost((void **)&e->h_active, sizeof(int) * NT) != cudaSuccess ||
        cudaMallocHost((void **)&e->h_out, sizeof(double) * (size_t)NT * (NGp + 1)) != cudaSuccess)
         return gf_fail(e, GF_ERR_OOM, "cudaMallocHost");
-    std::memset(e->h_P, 0, sizeof(double) * (size_t)NT * std::max(1, T.n_params));
+    std::memset(e->h_P, 0, e->pblock_bytes);
+    e->host_flag.assign(NT, 0);
     for(int t = 0; t < NT; ++t)
         e->h_active[t] = 1;
     std::vector<void *> cols((size_t)NT * NO, nullptr);
@@ -249,32 +280,56 @@ GfArgs makeArgs(gf_engine *e) {
     a.toy_nchunks = e->d_toy_nchunks;
     a.toy_nevents = e->d_toy_nevents;
     a.vals        = e->d_vals;
+    a.Pr          = (const char *)e->d_P + sizeof(double) * (size_t)e->n_toys * std::max(1, e->tree.n_params);
+    a.Nq          = e->d_Nq;
+    a.qflag       = e->d_qflag;
     a.n_chunks    = e->n_chunks;
     a.n_toys      = e->n_toys;
     a.metric      = 1;
     return a;
 }
 
-cudaError_t launch(cudaKernel_t k, dim3 g, dim3 b, size_t smem, cudaStream_t s, GfArgs &a) {
+cudaError_t launch(cudaKernel_t k, dim3 g, dim3 b, size_t smem, cudaStream_t s, GfArgs &a, bool pdl = false) {
     void *args[] = {&a};
-    return cudaLaunchKernel((const void *)k, g, b, args, smem, s);
+    if(!pdl)
+        return cudaLaunchKernel((const void *)k, g, b, args, smem, s);
+    // programmatic dependent launch: the kernel may start while the previous kernel of the stream is
+    // finishing; it waits (griddepcontrol.wait) before it reads that kernel's results
+    cudaLaunchAttribute attr[1];
+    attr[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim          = g;
+    cfg.blockDim         = b;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream           = s;
+    cfg.attrs            = attr;
+    cfg.numAttrs         = 1;
+    return cudaLaunchKernelExC(&cfg, (const void *)k, args);
 }
 
 // Enqueues the prep kernels (conv tables, grid sums) for one variant.
-cudaError_t enqueuePrep(gf_engine *e, bool grad, GfArgs &a) {
+// Enqueues the prep kernels (conv tables, grid sums) for one variant; returns whether a kernel was the last
+// operation, so that the next kernel can be chained programmatically.
+cudaError_t enqueuePrep(gf_engine *e, bool grad, GfArgs &a, bool *kernelLast = nullptr) {
     const gf::Tree &T = e->tree;
     cudaError_t r     = cudaSuccess;
+    bool prevKernel   = false;
     if(!T.convs.empty()) {
         dim3 g(e->plan.conv_blocks, e->n_toys, (unsigned)T.convs.size());
         r = launch(grad ? e->mod.conv_g : e->mod.conv_n, g, dim3(e->block),
                    grad ? e->plan.conv_smem_grad : e->plan.conv_smem_nograd, e->stream, a);
         if(r != cudaSuccess)
             return r;
+        prevKernel = true;
     }
     if(!T.nums.empty()) {
         dim3 g(e->plan.max_grid_blocks, e->n_toys, (unsigned)T.nums.size());
-        r = launch(grad ? e->mod.grid_g : e->mod.grid_n, g, dim3(e->block), 0, e->stream, a);
+        r = launch(grad ? e->mod.grid_g : e->mod.grid_n, g, dim3(e->block), 0, e->stream, a, prevKernel && e->use_pdl);
+        prevKernel = true;
     }
+    if(kernelLast)
+        *kernelLast = prevKernel;
     return r;
 }
 
@@ -286,19 +341,17 @@ cudaError_t enqueueEval(gf_engine *e, bool grad) {
     GfArgs a         = makeArgs(e);
     cudaError_t r    = cudaEventRecordWithFlags(e->ev[0], e->stream, cudaEventRecordExternal);
     if(r == cudaSuccess)
-        r = cudaMemcpyAsync(e->d_P, e->h_P, sizeof(double) * (size_t)NT * std::max(1, T.n_params),
-                            cudaMemcpyHostToDevice, e->stream);
+        r = cudaMemsetAsync(e->d_qflag, 0, sizeof(int) * NT, e->stream);
+    if(r == cudaSuccess)
+        r = cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
     if(r == cudaSuccess)
         r = cudaMemcpyAsync(e->d_active, e->h_active, sizeof(int) * NT, cudaMemcpyHostToDevice, e->stream);
+    bool kernelLast = false;
     if(r == cudaSuccess)
-        r = enqueuePrep(e, grad, a);
-    if(r == cudaSuccess)
-        r = cudaEventRecordWithFlags(e->ev[1], e->stream, cudaEventRecordExternal);
+        r = enqueuePrep(e, grad, a, &kernelLast);
     if(r == cudaSuccess)
         r = launch(grad ? e->mod.evt_g : e->mod.evt_n, dim3(evtGrid(e)), dim3(e->block),
-                   grad ? e->plan.evt_smem_grad : e->plan.evt_smem_nograd, e->stream, a);
-    if(r == cudaSuccess)
-        r = cudaEventRecordWithFlags(e->ev[2], e->stream, cudaEventRecordExternal);
+                   grad ? e->plan.evt_smem_grad : e->plan.evt_smem_nograd, e->stream, a, kernelLast && e->use_pdl);
     if(r == cudaSuccess)
         r = cudaMemcpyAsync(e->h_out, e->d_out, sizeof(double) * (size_t)NT * (NGp + 1), cudaMemcpyDeviceToHost,
                             e->stream);
@@ -365,6 +418,86 @@ int loadModule(gf_engine *e) {
     return GF_OK;
 }
 
+// Host part of every evaluation: the per-toy records the kernels read (parameters as R, then the
+// analytic normalisation factors, computed here from the FP64 parameters exactly as ExpPdf::integrate
+// and GaussianPdf::integrate do on the host in the reference).
+template <typename R>
+void fillRecordsT(gf_engine *e) {
+    const gf::Tree &T        = e->tree;
+    const gf::NormLayout &nl = e->plan.nl;
+    const int NT = e->n_toys, np = T.n_params;
+    R *rec = reinterpret_cast<R *>(reinterpret_cast<char *>(e->h_P) + sizeof(double) * (size_t)NT * std::max(1, np));
+    static const double rootPi = std::sqrt(std::atan2(0.0, -1.0)), root2 = std::sqrt(2.0);
+    for(int t = 0; t < NT; ++t) {
+        e->host_flag[t] = 0;
+        if(!e->h_active[t])
+            continue;
+        const double *P = e->h_P + (size_t)t * np;
+        R *r            = rec + (size_t)t * nl.npr;
+        for(int j = 0; j < np; ++j)
+            r[j] = (R)P[j];
+        for(auto &an : nl.analytic) {
+            const gf::TNode &nd = T.nodes[an.node];
+            double I = 1, dI;
+            if(an.kind == gf::NK_EXP) {
+                const gf_observable &o = T.obs[nd.obs[0]];
+                const double al        = P[nd.params[0]];
+                if(0 == al) {
+                    I *= o.hi - o.lo;
+                    dI = 0.5 * (o.hi * o.hi - o.lo * o.lo);
+                } else {
+                    const double eh = std::exp(al * o.hi), el = std::exp(al * o.lo);
+                    double v        = eh - el;
+                    v /= al;
+                    I *= v;
+                    dI = (o.hi * eh - o.lo * el) / al - I / al;
+                }
+            } else {
+                double sg = P[nd.params[1]];
+                sg *= root2 * rootPi;
+                I *= sg;
+                dI = root2 * rootPi;
+            }
+            const double N = 1.0 / I;
+            r[an.slotN]    = (R)N;
+            for(auto &d : an.dN)
+                r[d.second] = (R)(-N * N * dI);
+            if(an.node == 0) {
+                if(std::isnan(I))
+                    e->host_flag[t] |= 1;
+                else if(!(N > 0))
+                    e->host_flag[t] |= 2;
+            }
+        }
+    }
+}
+
+void fillRecords(gf_engine *e) {
+    if(e->precision == GF_MIXED)
+        fillRecordsT<float>(e);
+    else
+        fillRecordsT<double>(e);
+}
+
+// Host completion of one toy's result o = [nll, status, grad...]: status bits of host-computed factors and
+// the extended AddPdf term (AddPdf::calculateNLL, src/PDFs/combine/AddPdf.cu:187-204).
+void postToy(gf_engine *e, int t, double *o) {
+    const gf::Tree &T = e->tree;
+    int st            = (int)o[1] | e->host_flag[t];
+    if(T.extended_root && !(st & 4)) {
+        const double *P = e->h_P + (size_t)t * T.n_params;
+        double ex       = 0;
+        for(int p : T.nodes[0].params)
+            ex += P[p];
+        const double ne = (double)e->toys[t].n;
+        o[0] += (ex - ne * std::log(ex));
+        for(int p : T.nodes[0].params)
+            if(T.gslot[p] >= 0)
+                o[2 + T.gslot[p]] += 1.0 - ne / ex;
+    }
+    o[1] = (double)st;
+}
+
 } // namespace
 
 int gf_fail(gf_engine *e, int code, const std::string &msg) {
@@ -387,6 +520,7 @@ int gf_run(gf_engine *e, bool grad, int, int) {
     int rc = buildLayout(e);
     if(rc)
         return rc;
+    fillRecords(e);
     cudaError_t r;
     if(e->use_graph) {
         cudaGraphExec_t &ge = e->graph[grad ? 1 : 0];
@@ -425,8 +559,6 @@ int gf_run(gf_engine *e, bool grad, int, int) {
     float ms = 0;
     if(cudaEventElapsedTime(&ms, e->ev[0], e->ev[3]) == cudaSuccess)
         e->last_ms_total = ms;
-    if(cudaEventElapsedTime(&ms, e->ev[1], e->ev[2]) == cudaSuccess)
-        e->last_ms_evt = ms;
     return GF_OK;
 }
 
@@ -468,8 +600,12 @@ int gf_engine_create(gf_engine **out, int device, int precision) {
     cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device);
     if(const char *g = std::getenv("GF_NO_GRAPH"))
         e->use_graph = !(g[0] == '1');
-    if(const char *c = std::getenv("GF_CHUNK"))
-        e->chunk = std::max(1024, (atoi(c) / 1024) * 1024);
+    if(const char *c = std::getenv("GF_CHUNK")) {
+        e->chunk       = std::max(2048, (atoi(c) / 2048) * 2048);
+        e->chunk_fixed = true;
+    }
+    if(const char *p = std::getenv("GF_NO_PDL"))
+        e->use_pdl = !(p[0] == '1');
     if(const char *c = std::getenv("GF_EVT_CTAS_PER_SM"))
         e->evt_ctas_per_sm = std::max(1, atoi(c));
     e->toys.assign(1, GfToy());
@@ -550,7 +686,7 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
     const gf::Tree &T = e->tree;
     const int NO = (int)T.obs.size(), NC = (int)T.convs.size();
     GfToy &ty    = e->toys[toy];
-    int64_t npad = std::max<int64_t>(4, (n + 3) / 4 * 4);
+    int64_t npad = std::max<int64_t>(8, (n + 7) / 8 * 8);
     size_t rs    = rsize(e);
     cudaError_t r;
     // a re-upload of the same size keeps the buffers, the chunk layout and the captured graphs
@@ -604,6 +740,13 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
         a.conv_obs[c]  = T.convs[c].obs;
         a.conv_lo[c]   = T.convs[c].lo;
         a.conv_step[c] = T.convs[c].step;
+        {
+            double lbo = T.convs[c].lo / T.convs[c].step;
+            lbo -= std::floor(lbo);
+            a.conv_lbo[c]      = lbo;
+            a.conv_lbo_f[c]    = (float)lbo;
+            a.conv_inv_step[c] = (float)(1.0 / T.convs[c].step);
+        }
         a.conv_kmin[c] = T.convs[c].kmin;
         a.conv_kmax[c] = T.convs[c].kmax;
     }
@@ -654,7 +797,8 @@ static int evalOne(gf_engine *e, int toy, bool grad, double *nll, double *g) {
     if(rc)
         return rc;
     const int NGp = 1 + e->tree.NG;
-    const double *o = e->h_out + (size_t)toy * (NGp + 1);
+    double *o     = e->h_out + (size_t)toy * (NGp + 1);
+    postToy(e, toy, o);
     if(nll)
         *nll = o[0];
     if(grad && g)
@@ -706,8 +850,9 @@ int gf_nll_batch(gf_engine *e, int n_toys, const double *P, const int32_t *activ
     for(int t = 0; t < n_toys; ++t) {
         if(!e->h_active[t])
             continue;
-        const double *o = e->h_out + (size_t)t * (NGp + 1);
-        nll[t]          = o[0];
+        double *o = e->h_out + (size_t)t * (NGp + 1);
+        postToy(e, t, o);
+        nll[t] = o[0];
         if(grad)
             for(int s = 0; s < e->tree.NG; ++s)
                 grad[(size_t)t * e->tree.NG + s] = o[2 + s];
@@ -736,17 +881,16 @@ int gf_normalize(gf_engine *e, int toy, double *integral, double *norm) {
     const int NT = e->n_toys, NQ = (int)T.nums.size(), np = T.n_params;
     for(int t = 0; t < NT; ++t)
         e->h_active[t] = (t == toy);
+    fillRecords(e);
     GfArgs a = makeArgs(e);
-    cudaMemcpyAsync(e->d_P, e->h_P, sizeof(double) * (size_t)NT * std::max(1, np), cudaMemcpyHostToDevice, e->stream);
+    cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
     cudaMemcpyAsync(e->d_active, e->h_active, sizeof(int) * NT, cudaMemcpyHostToDevice, e->stream);
     cudaError_t r = enqueuePrep(e, false, a);
     if(r != cudaSuccess)
         return gf_cuda_check(e, r, "normalisation kernels");
-    const int NGs = 1 + T.NG;
-    std::vector<double> gsum((size_t)NT * std::max(1, NQ) * NGs);
+    std::vector<double> gsum((size_t)NT * std::max(1, NQ));
     if(NQ > 0)
-        cudaMemcpyAsync(gsum.data(), e->d_gsum, sizeof(double) * (size_t)NT * NQ * NGs, cudaMemcpyDeviceToHost,
-                        e->stream);
+        cudaMemcpyAsync(gsum.data(), e->d_gsum, sizeof(double) * (size_t)NT * NQ, cudaMemcpyDeviceToHost, e->stream);
     r = cudaStreamSynchronize(e->stream);
     if(r != cudaSuccess)
         return gf_cuda_check(e, r, "normalisation");
@@ -783,7 +927,7 @@ int gf_normalize(gf_engine *e, int toy, double *integral, double *norm) {
             double v = 1;
             v *= g.volume;
             v /= (double)g.total;
-            v *= gsum[((size_t)toy * NQ + T.num_of[i]) * NGs];
+            v *= gsum[(size_t)toy * NQ + T.num_of[i]];
             I[i] = v;
             N[i] = 1.0 / v;
             break;
@@ -845,9 +989,10 @@ int gf_eval_events(gf_engine *e, int toy, int node, int metric, double *out, int
     const int NT = e->n_toys, np = e->tree.n_params;
     for(int t = 0; t < NT; ++t)
         e->h_active[t] = (t == toy);
+    fillRecords(e);
     GfArgs a  = makeArgs(e);
     a.metric  = metric;
-    cudaMemcpyAsync(e->d_P, e->h_P, sizeof(double) * (size_t)NT * std::max(1, np), cudaMemcpyHostToDevice, e->stream);
+    cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
     cudaMemcpyAsync(e->d_active, e->h_active, sizeof(int) * NT, cudaMemcpyHostToDevice, e->stream);
     cudaError_t r = enqueuePrep(e, false, a);
     if(r == cudaSuccess)
@@ -866,6 +1011,58 @@ int gf_last_timing(const gf_engine *e, double *ms_total, double *ms_evt) {
         *ms_total = e->last_ms_total;
     if(ms_evt)
         *ms_evt = e->last_ms_evt;
+    return GF_OK;
+}
+
+int gf_time_kernels(gf_engine *e, int toy, int with_grad, double *ms_conv, double *ms_grid, double *ms_event) {
+    if(!e || !e->has_tree)
+        return gf_fail(e, GF_ERR_STATE, "no tree");
+    if(toy < 0 || toy >= e->n_toys)
+        return gf_fail(e, GF_ERR_INVALID, "toy index out of range");
+    cudaSetDevice(e->device);
+    int rc = buildLayout(e);
+    if(rc)
+        return rc;
+    const bool grad = with_grad != 0;
+    const gf::Tree &T = e->tree;
+    for(int t = 0; t < e->n_toys; ++t)
+        e->h_active[t] = (t == toy);
+    fillRecords(e);
+    GfArgs a = makeArgs(e);
+    cudaError_t r = cudaMemsetAsync(e->d_qflag, 0, sizeof(int) * e->n_toys, e->stream);
+    if(r == cudaSuccess)
+        r = cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
+    if(r == cudaSuccess)
+        r = cudaMemcpyAsync(e->d_active, e->h_active, sizeof(int) * e->n_toys, cudaMemcpyHostToDevice, e->stream);
+    cudaEvent_t t0 = e->ev[0], t1 = e->ev[1], t2 = e->ev[2], t3 = e->ev[3];
+    if(r == cudaSuccess)
+        r = cudaEventRecord(t0, e->stream);
+    if(r == cudaSuccess && !T.convs.empty())
+        r = launch(grad ? e->mod.conv_g : e->mod.conv_n, dim3(e->plan.conv_blocks, e->n_toys, (unsigned)T.convs.size()),
+                   dim3(e->block), grad ? e->plan.conv_smem_grad : e->plan.conv_smem_nograd, e->stream, a);
+    if(r == cudaSuccess)
+        r = cudaEventRecord(t1, e->stream);
+    if(r == cudaSuccess && !T.nums.empty())
+        r = launch(grad ? e->mod.grid_g : e->mod.grid_n, dim3(e->plan.max_grid_blocks, e->n_toys, (unsigned)T.nums.size()),
+                   dim3(e->block), 0, e->stream, a);
+    if(r == cudaSuccess)
+        r = cudaEventRecord(t2, e->stream);
+    if(r == cudaSuccess)
+        r = launch(grad ? e->mod.evt_g : e->mod.evt_n, dim3(evtGrid(e)), dim3(e->block),
+                   grad ? e->plan.evt_smem_grad : e->plan.evt_smem_nograd, e->stream, a);
+    if(r == cudaSuccess)
+        r = cudaEventRecord(t3, e->stream);
+    if(r == cudaSuccess)
+        r = cudaStreamSynchronize(e->stream);
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "kernel timing");
+    float f = 0;
+    if(ms_conv)
+        *ms_conv = cudaEventElapsedTime(&f, t0, t1) == cudaSuccess ? f : 0.0;
+    if(ms_grid)
+        *ms_grid = cudaEventElapsedTime(&f, t1, t2) == cudaSuccess ? f : 0.0;
+    if(ms_event)
+        *ms_event = cudaEventElapsedTime(&f, t2, t3) == cudaSuccess ? f : 0.0;
     return GF_OK;
 }
 

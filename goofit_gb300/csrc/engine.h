@@ -27,6 +27,9 @@ struct GfArgs {
     const int *toy_nchunks;
     const long long *toy_nevents;
     double *vals;
+    const void *Pr;
+    void *Nq;
+    int *qflag;
     int n_chunks;
     int n_toys;
     int metric;
@@ -60,6 +63,7 @@ struct gf_engine {
     GfModule mod;
     int block = 256;
     int chunk = 8192;
+    bool chunk_fixed = false;
     int evt_ctas_per_sm = 4;
 
     int n_toys = 1;
@@ -86,8 +90,12 @@ struct gf_engine {
     int64_t stage_cap = 0;
     int *d_uperr = nullptr;
     int *h_uperr = nullptr;
-    // pinned host mirrors
+    void *d_Nq = nullptr;   // [toy][nq] R numeric normalisation factors
+    int *d_qflag = nullptr; // [toy]
+    // pinned host mirrors; h_P is one block: [toy][n_params] FP64, then [toy][npr] R records
     double *h_P = nullptr;
+    size_t pblock_bytes = 0;
+    std::vector<int> host_flag; // per toy: status bits from host-computed analytic factors
     int *h_active = nullptr;
     double *h_out = nullptr;
 
@@ -97,6 +105,7 @@ struct gf_engine {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     double last_ms_total = 0, last_ms_evt = 0;
     bool use_graph = true;
+    bool use_pdl   = true;
 };
 
 // helpers shared between translation units

@@ -93,6 +93,25 @@ inline double bin_centre(double lo, double hi, int nbins, int b) {
     return x;
 }
 
+// Where every normalisation factor lives during an evaluation.
+//   record (type R, one per toy): [0, n_params) parameters, then the analytic factors the host computes
+//   from the parameters before each launch (ExpPdf::integrate and GaussianPdf::integrate run on the host
+//   in the reference too, src/PDFs/basic/ExpPdf.cu:121-132, src/PDFs/basic/GaussianPdf.cu:28-35);
+//   numeric array (type R, one per toy): the factors of numerically normalised nodes, written by the
+//   finishing CTA of the grid kernel.
+struct NormLayout {
+    struct Analytic {
+        int node = -1, kind = 0, slotN = -1;
+        std::vector<std::pair<int, int>> dN; // (gradient slot, record index)
+    };
+    int npr = 0; // record length
+    std::vector<Analytic> analytic;
+    int nq = 0;                                        // numeric slots per toy
+    std::vector<int> qN;                               // per numeric node q: slot of N
+    std::vector<std::vector<std::pair<int, int>>> qdN; // per q: (gradient slot, slot of dN)
+};
+NormLayout norm_layout(const Tree &t);
+
 // Generates the CUDA source of the fused kernel set for a tree.
 struct KernelPlan {
     std::string source;
@@ -105,8 +124,9 @@ struct KernelPlan {
     int max_grid_blocks = 0;
     int64_t ctab_per_toy_grad = 0, ctab_per_toy_nograd = 0; // table elements per toy
     std::vector<int64_t> ctab_off_grad, ctab_off_nograd;    // per conv
-    std::vector<int> ctab_comps_grad;                       // per conv
+    std::vector<int> ctab_cp_grad, ctab_cp_nograd;          // per conv: padded components per table row
     std::vector<int> obs_used_evt;                          // observables the event kernel loads
+    NormLayout nl;
 };
 
 KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, int chunk);

@@ -195,6 +195,12 @@ class Engine:
         self._L.gf_last_timing(self._h, C.byref(a), C.byref(b))
         return a.value, b.value
 
+    def time_kernels(self, grad: bool = True, toy: int = 0) -> tuple[float, float, float]:
+        """(conv, grid, event) kernel times in ms, each launched alone with CUDA events."""
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        self._check(self._L.gf_time_kernels(self._h, toy, 1 if grad else 0, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
     def launches_per_eval(self, grad: bool = True) -> int:
         return self._L.gf_launches_per_eval(self._h, 1 if grad else 0)
 
