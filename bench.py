@@ -300,6 +300,73 @@ def run_engine(args) -> dict | None:
     return line
 
 
+def run_toys(args) -> dict:
+    """C4: lockstep MIGRAD fits of n toys of the composite model, one batched graph launch per round."""
+    import numpy as np
+    import torch
+
+    import goofit_gb300 as gf
+    from goofit_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    study = W.make_c4(n_toys=args.toys, seed=4)
+    nodes, params, obs = study.pdf._flatten()
+    olist = [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs]
+    mask = [0 if v.fixed else 1 for v in params]
+    names = [v.name for v in params]
+    x0 = np.array([study.start.get(v.name, v.value) for v in params])
+    err = np.array([v.error for v in params])
+    lo = np.array([v.lowerlimit for v in params])
+    hi = np.array([v.upperlimit for v in params])
+    fixed = np.array([1 if v.fixed else 0 for v in params], np.int32)
+    limited = np.array([0 if v.fixed else 1 for v in params], np.int32)
+    n_events = int(sum(d.shape[1] for d in study.datas))
+    out = {"metric": METRIC, "config": {"workload": f"c4: {args.toys} toys of the composite model, Poisson(20000) "
+                                                    "events clipped to [5000, 60000], +-10% jittered truths",
+                                        "events_total": n_events}}
+    for label, prec, grad in (("mixed_analytic", "mixed", True), ("fp64_numerical", "fp64", False)):
+        eng = gf.Engine(prec)
+        eng.set_tree(nodes, olist, len(params), mask)
+        eng.set_num_toys(args.toys)
+        for t, d in enumerate(study.datas):
+            eng.upload(d, toy=t)
+        P = np.tile(x0, (args.toys, 1))
+        for _ in range(3):
+            eng.nll_batch(P, grad=True)
+        torch.cuda.synchronize()
+        rt = []
+        for _ in range(10):
+            eng.nll_batch(P, grad=True)
+            rt.append(eng.last_timing()[0])
+        X0 = np.tile(x0, (args.toys, 1))
+        t0 = time.perf_counter()
+        res = eng.fit_batch(X0, err, lo, hi, limited, fixed, tolerance=0.1, use_grad=grad)
+        wall = time.perf_counter() - t0
+        vals = np.array([r.values for r in res])
+        errs = np.array([r.errors for r in res])
+        pulls = {}
+        for i, nm in enumerate(names):
+            if fixed[i]:
+                continue
+            truth = np.array([tr[nm] for tr in study.truths])
+            pl = (vals[:, i] - truth) / np.where(errs[:, i] > 0, errs[:, i], np.nan)
+            pulls[nm] = {"mean": float(np.nanmean(pl)), "std": float(np.nanstd(pl))}
+        out[label] = {"fit_wall_s": wall, "fits_per_s": args.toys / wall,
+                      "valid": int(sum(r.valid for r in res)), "mean_nfcn": float(np.mean([r.nfcn for r in res])),
+                      "round_ms_with_grad": float(np.mean(rt)),
+                      "event_nll_evals_per_s": n_events / (np.mean(rt) / 1e3), "pulls": pulls}
+        out.setdefault("_vals", {})[label] = (vals, errs)
+        eng.close()
+    vm, em = out["_vals"].pop("mixed_analytic")
+    vf, ef = out["_vals"].pop("fp64_numerical")
+    del out["_vals"]
+    free = [i for i in range(len(params)) if not fixed[i]]
+    dsig = np.abs(vm[:, free] - vf[:, free]) / ef[:, free]
+    out["mixed_vs_fp64_max_dsigma"] = float(np.nanmax(dsig))
+    out["speedup_wall"] = out["fp64_numerical"]["fit_wall_s"] / out["mixed_analytic"]["fit_wall_s"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -311,9 +378,14 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=100_000)
     ap.add_argument("--no-fit", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", default="c2", choices=["c2", "c4"])
+    ap.add_argument("--toys", type=int, default=1024)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
+    if args.config == "c4":
+        print(json.dumps(run_toys(args)))
+        return
     if args.impl == "reference":
         if rank != 0:
             return

@@ -119,3 +119,30 @@ def make_c2(n: int = 2_000_000, seed: int = 2, truth: dict | None = None) -> Wor
     start = {"alpha": -0.6, "mu": 0.05, "sigma": 0.35, "fsig": 0.65}
     return Workload("c2-conv-2e6", pdf, data, tr, start,
                     {"alpha": alpha, "mu": mu, "sigma": sigma, "c0": c0, "fsig": fsig}, [x])
+
+
+@dataclass
+class ToyStudy:
+    name: str
+    pdf: G.GooPdf
+    variables: dict
+    truths: list  # per toy: dict of generation parameters
+    datas: list   # per toy: (1, n) float64 arrays
+    start: dict
+
+
+def make_c4(n_toys: int = 1024, mean_events: float = 20_000, lo: int = 5_000, hi: int = 60_000,
+            seed: int = 4) -> ToyStudy:
+    """C4: toys of the C2 model; Poisson(mean) event counts clipped to [lo, hi]; each toy's generation
+    parameters jittered uniformly by +-10% around the C2 truth (mu jittered by +-0.1 sigma_res)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    base = make_c2(16, seed=0)
+    counts = np.clip(rng.poisson(mean_events, n_toys), lo, hi)
+    truths, datas = [], []
+    for t in range(n_toys):
+        j = rng.uniform(-0.1, 0.1, 4)
+        tr = dict(alpha=(-1 / 1.5) * (1 + j[0]), mu=0.3 * j[1], sigma=0.3 * (1 + j[2]), fsig=0.7 * (1 + j[3]))
+        truths.append(tr)
+        datas.append(c2_data(int(counts[t]), seed=10_000 + seed * 100_000 + t, alpha=tr["alpha"], mu=tr["mu"],
+                             sigma=tr["sigma"], fsig=tr["fsig"]).reshape(1, -1))
+    return ToyStudy("c4-toys", base.pdf, base.variables, truths, datas, dict(base.start))
