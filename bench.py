@@ -353,6 +353,10 @@ def run_toys(args) -> dict:
             pulls[nm] = {"mean": float(np.nanmean(pl)), "std": float(np.nanstd(pl))}
         out[label] = {"fit_wall_s": wall, "fits_per_s": args.toys / wall,
                       "valid": int(sum(r.valid for r in res)), "mean_nfcn": float(np.mean([r.nfcn for r in res])),
+                      "max_nfcn": int(max(r.nfcn for r in res)),
+                      "invalid_reasons": {"call_limit": int(sum(r.call_limit for r in res)),
+                                          "above_max_edm": int(sum(r.above_max_edm for r in res)),
+                                          "no_covariance": int(sum(not r.has_covariance for r in res))},
                       "round_ms_with_grad": float(np.mean(rt)),
                       "event_nll_evals_per_s": n_events / (np.mean(rt) / 1e3), "pulls": pulls}
         out.setdefault("_vals", {})[label] = (vals, errs)

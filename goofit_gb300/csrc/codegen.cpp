@@ -389,6 +389,13 @@ __device__ __forceinline__ float gf_group_sum(float v, int width) {
     }
     return hi + lo;
 }
+// s + c += v with a two-sum correction term c.
+__device__ __forceinline__ void gf_comp_add(float &s, float &c, float v) {
+    float t, e;
+    gf_two_sum(s, v, t, e);
+    s = t;
+    c += e;
+}
 // Partial sums as an unevaluated pair hi + lo of FP32 values (about 48 significant bits).
 typedef float2 ACC;
 __device__ __forceinline__ ACC acc_zero() { return make_float2(0.f, 0.f); }
@@ -433,6 +440,7 @@ __device__ __forceinline__ double gf_group_sum(double v, int width) {
         v += __shfl_down_sync(0xffffffffu, v, o, width);
     return v;
 }
+__device__ __forceinline__ void gf_comp_add(double &s, double &c, double v) { s += v; }
 typedef double ACC;
 __device__ __forceinline__ ACC acc_zero() { return 0.0; }
 __device__ __forceinline__ ACC acc_of(double v) { return v; }
@@ -625,7 +633,8 @@ struct Gen {
             os << "    const int c0 = " << KB - 1 << " - kt * " << KT << ";\n";
             os << "    const int mlo = (" << cv.nM << " * ms) / " << MS << ", mhi = (" << cv.nM << " * (ms + 1)) / " << MS
                << ";\n";
-            os << "    R acc[" << KT << "];\n#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) acc[j] = R(0);\n";
+            os << "    R acc[" << KT << "], cmp[" << KT << "];\n#pragma unroll\n    for(int j = 0; j < " << KT
+               << "; ++j) { acc[j] = R(0); cmp[j] = R(0); }\n";
             os << "    if(live) {\n";
             os << "      const R *mA[2] = {nullptr, nullptr}; const R *rA[2] = {nullptr, nullptr};\n";
             os << "      switch(comp) {\n";
@@ -653,12 +662,19 @@ struct Gen {
             os << "        const R *M = mA[t]; const R *Rw = rA[t] + c0;\n";
             os << "        R rv[" << KT << "];\n#pragma unroll\n        for(int j = 0; j < " << KT
                << "; ++j) rv[j] = Rw[mlo - j];\n";
-            os << "        for(int m = mlo; m < mhi; ++m) {\n";
-            os << "          const R mv = M[m];\n";
-            os << "#pragma unroll\n          for(int j = 0; j < " << KT << "; ++j) acc[j] = fma(mv, rv[j], acc[j]);\n";
-            os << "#pragma unroll\n          for(int j = " << KT - 1 << "; j > 0; --j) rv[j] = rv[j - 1];\n";
-            os << "          rv[0] = Rw[m + 1];\n";
+            // blocks of 8 products are summed plainly, blocks are added with a two-sum correction (mixed)
+            os << "        for(int mb = mlo; mb < mhi; mb += 8) {\n";
+            os << "          R bs[" << KT << "];\n#pragma unroll\n          for(int j = 0; j < " << KT << "; ++j) bs[j] = R(0);\n";
+            os << "          const int me = min(mb + 8, mhi);\n";
+            os << "          for(int m = mb; m < me; ++m) {\n";
+            os << "            const R mv = M[m];\n";
+            os << "#pragma unroll\n            for(int j = 0; j < " << KT << "; ++j) bs[j] = fma(mv, rv[j], bs[j]);\n";
+            os << "#pragma unroll\n            for(int j = " << KT - 1 << "; j > 0; --j) rv[j] = rv[j - 1];\n";
+            os << "            rv[0] = Rw[m + 1];\n";
+            os << "          }\n";
+            os << "#pragma unroll\n          for(int j = 0; j < " << KT << "; ++j) gf_comp_add(acc[j], cmp[j], bs[j]);\n";
             os << "        }\n      }\n    }\n";
+            os << "#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) acc[j] += cmp[j];\n";
             os << "#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) {\n";
             os << "      const R t = gf_group_sum(acc[j], " << MS << ");\n";
             os << "      const int k = kt0 + j;\n";

@@ -340,7 +340,11 @@ Minimizer::Task Minimizer::lineSearch(const std::vector<double> &xi, double f0, 
     co_await evalAt(at(1.0), g);
     double f1 = f_;
     std::vector<double> g1 = gi_;
-    if(g && f1 <= f0 + ftol && std::isfinite(f1)) {
+    // approximate Wolfe conditions (Hager & Zhang): with an analytic gradient a step is acceptable when the
+    // directional derivative has dropped to sigma*slope or below while not turning up by more than
+    // (1 - 2 delta)|slope|, and the value has not risen beyond its rounding noise
+    const bool wolfe = g && std::isfinite(f1) && f1 <= f0 + ftol && dslope() >= 0.9 * slope && dslope() <= -0.8 * slope;
+    if(g && std::isfinite(f1) && (f1 <= f0 + ftol || wolfe)) {
         double s1  = dslope();
         ls_lambda_ = 1.0;
         ls_f_      = f1;

@@ -121,6 +121,11 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
         case GF_OP_ADD_EXT: ok = C >= 1 && P == C; break;
         case GF_OP_PROD: ok = C >= 1; break;
         case GF_OP_CONVOLUTION: ok = C == 2 && n.consts.size() >= 3 && n.obs.size() >= 1 && n.consts[2] > 0; break;
+        case GF_OP_MULTIPOLYNOMIAL: ok = n.obs.size() >= 1 && n.consts.size() >= 1 && P >= n.obs.size() + 1 && C == 0; break;
+        case GF_OP_RES_RBW: ok = P == 2 && n.consts.size() >= 3 && C == 0; break;
+        case GF_OP_AMP3BODY:
+            ok = n.consts.size() >= 8 && n.obs.size() >= 2 && C >= 2 && P == 2 * (C - 1) && (int)n.consts[0] == (int)C - 1;
+            break;
         default: return "node " + std::to_string(i) + ": operator " + std::to_string(n.op) + " not supported";
         }
         if(!ok)
@@ -177,6 +182,11 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
         } else if(n.op == GF_OP_CONVOLUTION) {
             nk[i]       = NK_NUMERIC;
             childForced = true;
+        } else if(n.op == GF_OP_AMP3BODY) {
+            nk[i]       = NK_AMP3;
+            childForced = true;
+        } else if(n.op == GF_OP_RES_RBW) {
+            nk[i] = NK_ONE;
         } else if(isExpOp(n.op) && n.params.size() == 1) {
             nk[i] = NK_EXP;
         } else if(n.op == GF_OP_GAUSSIAN) {
@@ -212,8 +222,22 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
             used.erase(std::unique(used.begin(), used.end()), used.end());
             v = used;
         }
+        if(n.op == GF_OP_AMP3BODY) {
+            // value gradient: coefficients (and an efficiency's free parameters); resonance parameters
+            // enter through the cached amplitudes, whose derivatives the engine does not provide
+            v = own;
+            for(int c : n.children)
+                if(nodes[c].op == GF_OP_RES_RBW && !dep_val[c].empty())
+                    return "Amp3Body: analytic gradients with respect to resonance parameters are not provided; "
+                           "fix them or leave them out of the gradient mask";
+            int eff = n.children.back();
+            if(!dep_val[eff].empty())
+                return "Amp3Body: analytic gradients with respect to efficiency parameters are not provided";
+        }
         dep_val[i] = v;
-        if(nk[i] == NK_EXP) {
+        if(nk[i] == NK_AMP3) {
+            dep_norm[i] = own;
+        } else if(nk[i] == NK_EXP) {
             int s = gslot[n.params[0]];
             if(s >= 0)
                 dep_norm[i] = {s};
@@ -273,6 +297,52 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
     if(convs.size() > 8)
         return "at most 8 ConvolutionPdf nodes per tree";
 
+    // Amp3Body nodes
+    amp3_of.assign(n_nodes, -1);
+    amp3s.clear();
+    n_amp_cols = 0;
+    for(int i = 0; i < n_nodes; ++i) {
+        const TNode &n = nodes[i];
+        if(n.op != GF_OP_AMP3BODY)
+            continue;
+        Amp3Info a;
+        a.node = i;
+        a.nRes = (int)n.consts[0];
+        for(int r = 0; r < a.nRes; ++r) {
+            int rn = n.children[r];
+            if(nodes[rn].op != GF_OP_RES_RBW)
+                return "Amp3Body node " + std::to_string(i) + ": only relativistic Breit-Wigner resonances are supported";
+            a.res.push_back(rn);
+        }
+        a.eff = n.children[a.nRes];
+        a.o12 = n.obs[0];
+        a.o13 = n.obs[1];
+        a.M = n.consts[2], a.m1 = n.consts[3], a.m2 = n.consts[4], a.m3 = n.consts[5];
+        a.r = n.consts[6], a.rm = n.consts[7];
+        a.nb12  = obs[a.o12].nbins;
+        a.nb13  = obs[a.o13].nbins;
+        a.nb13q = a.nb12;
+        double b12 = (obs[a.o12].hi - obs[a.o12].lo) / a.nb12, b13 = (obs[a.o13].hi - obs[a.o13].lo) / a.nb13;
+        a.area = 1;
+        a.area *= b12;
+        a.area *= b13;
+        for(int j = i + 1; j < n_nodes; ++j)
+            if(inSubtree(i, j)) {
+                if(nodes[j].op == GF_OP_CONVOLUTION || nodes[j].op == GF_OP_AMP3BODY)
+                    return "Amp3Body node " + std::to_string(i) + ": convolutions or Dalitz PDFs below it are not supported";
+                for(int p : nodes[j].params)
+                    a.cache_params.push_back(p);
+            }
+        std::sort(a.cache_params.begin(), a.cache_params.end());
+        a.cache_params.erase(std::unique(a.cache_params.begin(), a.cache_params.end()), a.cache_params.end());
+        a.col0 = n_amp_cols;
+        n_amp_cols += a.nRes;
+        amp3_of[i] = (int)amp3s.size();
+        amp3s.push_back(a);
+    }
+    if(amp3s.size() > 4)
+        return "at most 4 Amp3Body nodes per tree";
+
     // numeric grids
     num_of.assign(n_nodes, -1);
     nums.clear();
@@ -280,6 +350,9 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
     for(int i = 0; i < n_nodes; ++i) {
         if(nk[i] != NK_NUMERIC)
             continue;
+        for(int j = i + 1; j < n_nodes; ++j)
+            if(inSubtree(i, j) && nodes[j].op == GF_OP_AMP3BODY)
+                return "a numerically normalised node cannot contain an Amp3Body";
         NumInfo g;
         g.node = i;
         g.obs  = nodes[i].obs;

@@ -17,7 +17,9 @@ enum NormKind {
                     // recursiveSetNormalization (src/goofit/PdfBase.cpp:29-38)
     NK_EXP     = 1, // ExpPdf::integrate        (src/PDFs/basic/ExpPdf.cu:121-132)
     NK_GAUSS   = 2, // GaussianPdf::integrate   (src/PDFs/basic/GaussianPdf.cu:28-35)
-    NK_NUMERIC = 3  // grid sum                 (src/PDFs/GooPdf.cu:366-395)
+    NK_NUMERIC = 3, // grid sum                 (src/PDFs/GooPdf.cu:366-395)
+    NK_AMP3    = 4  // Amp3Body::normalize: c^H I c over the cached resonance integrals
+                    // (src/PDFs/physics/Amp3Body.cu:238-359), evaluated on the host
 };
 
 struct TNode {
@@ -37,6 +39,19 @@ struct ConvInfo {
     int nM = 0, nR = 0, offset = 0;
     int kmin = 0, kmax = 0, nK = 0; // bin-offset range of x in [obs.lo, obs.hi]
     std::vector<int> dep;           // gradient slots the table depends on
+};
+
+// One Amp3Body node (src/PDFs/physics/Amp3Body.cu:127-196): resonances, efficiency, decay constants and
+// the normalisation grid (m12^2 x m13^2 bin centres; the m13 bin count is read from the m12 slot as
+// src/PDFs/physics/detail/SpecialResonanceIntegrator.cu:72 does).
+struct Amp3Info {
+    int node = -1, nRes = 0, eff = -1, o12 = -1, o13 = -1;
+    std::vector<int> res;     // resonance nodes
+    int col0 = 0;             // first amplitude column of this node
+    double M = 0, m1 = 0, m2 = 0, m3 = 0, r = 0, rm = 0;
+    int nb12 = 0, nb13 = 0, nb13q = 0;
+    double area = 0;          // bin size of m12 times bin size of m13
+    std::vector<int> cache_params; // parameters the cached amplitudes and integrals depend on
 };
 
 // One numerically normalised node: grid over its observables.
@@ -66,6 +81,9 @@ struct Tree {
     std::vector<NumInfo> nums;
     std::vector<int> num_of; // node -> index in nums or -1
     std::vector<int> kgrid;  // host copy of all grid k tables
+    std::vector<Amp3Info> amp3s;
+    std::vector<int> amp3_of; // node -> index in amp3s or -1
+    int n_amp_cols = 0;       // complex amplitude columns per toy
     bool extended_root = false;
 
     // Returns "" on success, else the reason the tree is rejected.

@@ -207,7 +207,7 @@ class Engine:
     # ---- fits ----
     def default_fnoise(self) -> float:
         """Relative rounding noise of the NLL: FP32 per-event terms in the mixed path."""
-        return 2e-9 if self.precision == "mixed" else 0.0
+        return 1e-8 if self.precision == "mixed" else 0.0
 
     def fit(self, x0, err, lo, hi, limited, fixed, *, up=0.5, tolerance=0.1, strategy=1, maxfcn=0,
             use_grad=True, toy: int = 0, fnoise_rel=None) -> FitResult:

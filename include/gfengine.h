@@ -64,8 +64,15 @@ enum gf_op {
     GF_OP_ADD_EXT           = 9,  /* device_AddPdfsExt     src/PDFs/combine/AddPdf.cu:53-80   params [N1..Nn] children n */
     GF_OP_PROD              = 10, /* device_ProdPdfs       src/PDFs/combine/ProdPdf.cu:9-26   consts [nComps] children n */
     GF_OP_CONVOLUTION       = 11, /* device_ConvolvePdfs   src/PDFs/combine/ConvolutionPdf.cu:27-75 consts [lo, hi, step] children [model, resolution] */
-    GF_OP_AMP3BODY          = 12, /* device_DalitzPlot     src/PDFs/physics/Amp3Body.cu:60-122 (see gfengine_amp.h) */
-    GF_OP_AMP4BODY          = 13  /* device_DP             src/PDFs/physics/Amp4Body.cu:53-90  (see gfengine_amp.h) */
+    GF_OP_AMP3BODY          = 12, /* device_DalitzPlot     src/PDFs/physics/Amp3Body.cu:60-122
+                                     consts [nRes, cache, M, m1, m2, m3, mesonRadius, motherRadius]
+                                     params [Re c0, Im c0, Re c1, ...] obs [m12^2, m13^2, eventNumber]
+                                     children [resonance 0 .. n-1, efficiency] */
+    GF_OP_AMP4BODY          = 13, /* device_DP             src/PDFs/physics/Amp4Body.cu:53-90 */
+    GF_OP_MULTIPOLYNOMIAL   = 14, /* device_MultiPolynomial src/PDFs/basic/PolynomialPdf.cu:46-107
+                                     consts [maxDegree, maxDegree+1+i ...] params [offsets (nObs), coefficients] */
+    GF_OP_RES_RBW           = 20  /* plainBW<1|2>          src/PDFs/physics/resonances/RBW.cu:9-86
+                                     params [mass, width] consts [spin, cyclic index, norm, symmetric] */
 };
 
 /* node flags */

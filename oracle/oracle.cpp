@@ -18,6 +18,7 @@
 #include "../include/gfengine.h"
 
 #include <cmath>
+#include <complex>
 #include <cstdint>
 #include <cstring>
 #include <map>
@@ -52,6 +53,132 @@ struct ConvWork {
     int kmin = 0, kmax = -1;
 };
 
+typedef std::complex<double> cplx;
+
+// inDalitz (src/PDFs/physics/DalitzPlotHelpers.cu:14-59)
+bool inDalitz(double m12, double m13, double bigM, double dm1, double dm2, double dm3) {
+    double dm1pdm2  = dm1 + dm2;
+    double bigMmdm3 = bigM - dm3;
+    double bigMmdm1 = bigM - dm1;
+    double m23      = bigM * bigM + dm1 * dm1 + dm2 * dm2 + dm3 * dm3 - m12 - m13;
+    if(m23 < 0. || m23 > bigMmdm1 * bigMmdm1)
+        return false;
+    bool m12less   = (m12 < dm1pdm2 * dm1pdm2) ? false : true;
+    bool m12grea   = (m12 > bigMmdm3 * bigMmdm3) ? false : true;
+    double sqrtM12 = std::sqrt(m12);
+    double dm11 = dm1 * dm1, dm22 = dm2 * dm2, dm33 = dm3 * dm3;
+    double e1star    = 0.5 * (m12 - dm22 + dm11) / sqrtM12;
+    double e3star    = 0.5 * (bigM * bigM - m12 - dm33) / sqrtM12;
+    double rte1mdm11 = std::sqrt(e1star * e1star - dm11);
+    double rte3mdm33 = std::sqrt(e3star * e3star - dm33);
+    double minimum   = (e1star + e3star) * (e1star + e3star) - (rte1mdm11 + rte3mdm33) * (rte1mdm11 + rte3mdm33);
+    bool m13less     = (m13 < minimum) ? false : true;
+    double maximum   = (e1star + e3star) * (e1star + e3star) - (rte1mdm11 - rte3mdm33) * (rte1mdm11 - rte3mdm33);
+    bool m13grea     = (m13 > maximum) ? false : true;
+    return m12less && m12grea && m13less && m13grea;
+}
+
+// Resonance helpers (src/PDFs/physics/resonances/Resonance.cu:48-155)
+double twoBodyCMmom(double rMassSq, double d1m, double d2m) {
+    double kin1 = 1 - (d1m + d2m) * (d1m + d2m) / rMassSq;
+    kin1        = kin1 >= 0 ? std::sqrt(kin1) : 1;
+    double kin2 = 1 - (d1m - d2m) * (d1m - d2m) / rMassSq;
+    kin2        = kin2 >= 0 ? std::sqrt(kin2) : 1;
+    return 0.5 * std::sqrt(rMassSq) * kin1 * kin2;
+}
+double twoBodyCMMothermom(double rMassSq, double dm, double d3m) {
+    double kin1 = 1 - (dm + d3m) * (dm + d3m) / rMassSq;
+    kin1        = kin1 >= 0 ? std::sqrt(kin1) : 1;
+    double kin2 = 1 - (dm - d3m) * (dm - d3m) / rMassSq;
+    kin2        = kin2 >= 0 ? std::sqrt(kin2) : 1;
+    return 0.5 * rMassSq * kin1 * kin2 / dm;
+}
+double dampingFactorSquare(double cmmom, int spin, double mRadius) {
+    double square  = mRadius * mRadius * cmmom * cmmom;
+    double dfsq    = 2 * square;
+    double dfsqres = 13 * square / std::pow(square - 3, 2) + 9 * square * square;
+    return (spin == 2) ? dfsqres : dfsq;
+}
+double dampingFactorSquareNorm(double cmmom, int spin, double mRadius) {
+    double square  = mRadius * mRadius * cmmom * cmmom;
+    double dfsq    = 1 + square;
+    double dfsqres = dfsq + 8 + 2 * square + square * square;
+    return (spin == 2) ? dfsqres : dfsq;
+}
+double spinFactor(unsigned spin, double motherMass, double daug1Mass, double daug2Mass, double daug3Mass, double m12,
+                  double m13, double m23, unsigned cyclic_index) {
+    if(0 == spin)
+        return 1;
+    double _mA  = (0 == cyclic_index ? daug1Mass : (1 == cyclic_index ? daug3Mass : daug2Mass));
+    double _mB  = (0 == cyclic_index ? daug2Mass : (1 == cyclic_index ? daug1Mass : daug3Mass));
+    double _mC  = (0 == cyclic_index ? daug3Mass : (1 == cyclic_index ? daug2Mass : daug1Mass));
+    double _mAC = (0 == cyclic_index ? m13 : (1 == cyclic_index ? m23 : m12));
+    double _mBC = (0 == cyclic_index ? m23 : (1 == cyclic_index ? m12 : m13));
+    double _mAB = (0 == cyclic_index ? m12 : (1 == cyclic_index ? m13 : m23));
+    double massFactor = 1.0 / (_mAB);
+    double sFactor    = -1;
+    sFactor *= ((_mBC - _mAC) + (massFactor * (motherMass * motherMass - _mC * _mC) * (_mA * _mA - _mB * _mB)));
+    if(2 == spin) {
+        sFactor *= sFactor;
+        double extraterm = ((_mAB - (2 * motherMass * motherMass) - (2 * _mC * _mC))
+                            + massFactor * (motherMass * motherMass - _mC * _mC) * (motherMass * motherMass - _mC * _mC));
+        extraterm *= ((_mAB - (2 * _mA * _mA) - (2 * _mB * _mB)) + massFactor * (_mA * _mA - _mB * _mB) * (_mA * _mA - _mB * _mB));
+        extraterm /= 3;
+        sFactor -= extraterm;
+    }
+    return sFactor;
+}
+
+struct Decay3 {
+    double M, m1, m2, m3, r, rm;
+};
+
+// plainBW<I> (src/PDFs/physics/resonances/RBW.cu:9-86)
+cplx plainBW(int I, double resmass, double reswidth, unsigned spin, unsigned cyclic_index, bool norm, double m12,
+             double m13, double m23, const Decay3 &d) {
+    cplx result(0.0, 0.0);
+    double resmass2 = resmass * resmass;
+    for(int i = 0; i < I; i++) {
+        double rMassSq      = (0 == cyclic_index ? m12 : (1 == cyclic_index ? m13 : m23));
+        double mass_daug1   = 2 == cyclic_index ? d.m2 : d.m1;
+        double mass_daug2   = 0 == cyclic_index ? d.m2 : d.m3;
+        double bachelorMass = (0 == cyclic_index ? d.m3 : (1 == cyclic_index ? d.m2 : d.m1));
+        double frFactor = 1, frFactorMother = 1;
+        double measureDaughterMoms = twoBodyCMmom(rMassSq, mass_daug1, mass_daug2);
+        double nominalDaughterMoms = twoBodyCMmom(resmass2, mass_daug1, mass_daug2);
+        double measureDaughterMomsMother, nominalDaughterMomsMother = 0;
+        if(norm) {
+            measureDaughterMomsMother = twoBodyCMMothermom(rMassSq, d.M, bachelorMass);
+            nominalDaughterMomsMother = twoBodyCMMothermom(resmass2, d.M, bachelorMass);
+        } else {
+            measureDaughterMomsMother = twoBodyCMmom(d.M * d.M, std::sqrt(rMassSq), bachelorMass);
+        }
+        if(0 != spin) {
+            if(norm) {
+                frFactor = dampingFactorSquareNorm(nominalDaughterMoms, spin, d.r)
+                           / dampingFactorSquareNorm(measureDaughterMoms, spin, d.r);
+                frFactorMother = dampingFactorSquareNorm(nominalDaughterMomsMother, spin, d.rm)
+                                 / dampingFactorSquareNorm(measureDaughterMomsMother, spin, d.rm);
+            } else {
+                frFactor       = dampingFactorSquare(measureDaughterMoms, spin, d.r);
+                frFactorMother = dampingFactorSquare(measureDaughterMomsMother, spin, d.rm);
+            }
+        }
+        double A = (resmass2 - rMassSq);
+        double B = resmass2 * reswidth * std::pow(measureDaughterMoms / nominalDaughterMoms, 2.0 * spin + 1) * frFactor
+                   / std::sqrt(rMassSq);
+        double C = 1.0 / (A * A + B * B);
+        cplx ret(A * C, B * C);
+        ret *= std::sqrt(frFactor);
+        ret *= std::sqrt(frFactorMother);
+        ret *= spinFactor(spin, d.M, d.m1, d.m2, d.m3, m12, m13, m23, cyclic_index);
+        result += ret;
+        if(I > 1)
+            cyclic_index = (cyclic_index + 1) % 3;
+    }
+    return result;
+}
+
 struct Oracle {
     std::vector<Node> nodes;
     std::vector<gf_observable> obs;
@@ -59,6 +186,7 @@ struct Oracle {
     std::vector<double> norm;     // host_normalizations[normalIdx + 1]
     std::vector<double> integral; // value returned by normalize()
     std::map<int, ConvWork> conv;
+    std::map<int, std::vector<cplx>> amp3I; // Amp3Body node -> n x n integrals I_ij
     bool brute_force = false;
     std::string err;
 
@@ -189,6 +317,8 @@ struct Oracle {
             integral[i] = 1.0;
             return 1.0;
         }
+        if(n.op == GF_OP_AMP3BODY)
+            return normalizeAmp3(i);
         if(n.op == GF_OP_CONVOLUTION) {
             // ConvolutionPdf::normalize (src/PDFs/combine/ConvolutionPdf.cu:313-358)
             recursiveSetNormalization(i, 1.0);
@@ -419,9 +549,144 @@ struct Oracle {
             ret *= norm[n.children[1]];
             return ret;
         }
+        case GF_OP_MULTIPOLYNOMIAL: { // src/PDFs/basic/PolynomialPdf.cu:46-107
+            int num_observables = (int)n.obs.size();
+            int maxDegree       = (int)n.consts.at(0) + 1;
+            int numBoxes        = 1;
+            for(int k = 0; k < num_observables; ++k)
+                numBoxes *= maxDegree;
+            int coeffNumber = num_observables;
+            double ret      = par(i, coeffNumber);
+            coeffNumber++;
+            for(int b = 1; b < numBoxes; ++b) {
+                double currTerm  = 1;
+                int currIndex    = b;
+                int sumOfIndices = 0;
+                for(int j = 0; j < num_observables; ++j) {
+                    double x = evt[n.obs[j]];
+                    x -= par(i, j);
+                    int currPower = currIndex % maxDegree;
+                    currIndex /= maxDegree;
+                    currTerm *= std::pow(x, (double)currPower);
+                    sumOfIndices += currPower;
+                }
+                if(sumOfIndices >= maxDegree)
+                    continue;
+                currTerm *= par(i, coeffNumber);
+                coeffNumber++;
+                ret += currTerm;
+            }
+            return ret;
+        }
+        case GF_OP_AMP3BODY: { // device_DalitzPlot, src/PDFs/physics/Amp3Body.cu:60-122
+            const Decay3 d = decay3(i);
+            double m12 = evt[n.obs[0]], m13 = evt[n.obs[1]];
+            if(!inDalitz(m12, m13, d.M, d.m1, d.m2, d.m3))
+                return 0;
+            double m23 = d.M * d.M + d.m1 * d.m1 + d.m2 * d.m2 + d.m3 * d.m3 - m12 - m13;
+            int nRes   = (int)n.consts.at(0);
+            cplx totalAmp(0, 0);
+            for(int r = 0; r < nRes; ++r) {
+                cplx amp(par(i, 2 * r), par(i, 2 * r + 1));
+                totalAmp += amp * resonance(n.children[r], m12, m13, m23, d);
+            }
+            double ret = std::norm(totalAmp);
+            ret *= eval(n.children[nRes], evt);
+            return ret;
+        }
         default:
             throw std::runtime_error("oracle: unsupported op " + std::to_string(n.op));
         }
+    }
+
+    Decay3 decay3(int i) const {
+        const Node &n = nodes[i];
+        return Decay3{n.consts.at(2), n.consts.at(3), n.consts.at(4), n.consts.at(5), n.consts.at(6), n.consts.at(7)};
+    }
+
+    cplx resonance(int r, double m12, double m13, double m23, const Decay3 &d) const {
+        const Node &rn = nodes[r];
+        if(rn.op != GF_OP_RES_RBW)
+            throw std::runtime_error("oracle: unsupported resonance op");
+        int I = (rn.consts.size() > 3 && rn.consts[3] != 0) ? 2 : 1;
+        return plainBW(I, par(r, 0), par(r, 1), (unsigned)rn.consts.at(0), (unsigned)rn.consts.at(1), rn.consts.at(2) != 0,
+                       m12, m13, m23, d);
+    }
+
+    // Amp3Body::normalize (src/PDFs/physics/Amp3Body.cu:238-359) with the integrals of
+    // SpecialResonanceIntegrator (src/PDFs/physics/detail/SpecialResonanceIntegrator.cu:7-121); the m13
+    // bin count is read from the m12 slot as the reference does (line 72).
+    double normalizeAmp3(int i) {
+        const Node &n = nodes[i];
+        recursiveSetNormalization(i, 1.0);
+        const Decay3 d = decay3(i);
+        int nRes       = (int)n.consts.at(0);
+        int eff        = n.children[nRes];
+        const gf_observable &o12 = obs[n.obs[0]], &o13 = obs[n.obs[1]];
+        int nb12 = o12.nbins, nb13 = o13.nbins;
+        int nb13q = (int)std::floor((double)nb12 + 0.5);
+        int64_t totalBins = (int64_t)nb12 * nb13;
+        int nthreads      = 1;
+#ifdef _OPENMP
+        nthreads = omp_get_max_threads();
+#endif
+        std::vector<std::vector<cplx>> part(nthreads, std::vector<cplx>(nRes * nRes, cplx(0, 0)));
+#pragma omp parallel
+        {
+            int tid = 0;
+#ifdef _OPENMP
+            tid = omp_get_thread_num();
+#endif
+            std::vector<cplx> B(nRes);
+            std::vector<double> evt(obs.size(), 0.0);
+#pragma omp for schedule(static)
+            for(int64_t b = 0; b < totalBins; ++b) {
+                int binNumberM12 = (int)(b % nb12);
+                double c12       = o12.hi - o12.lo;
+                c12 /= nb12;
+                c12 *= (binNumberM12 + 0.5);
+                c12 += o12.lo;
+                int64_t g   = b / nb12;
+                double c13  = o13.hi - o13.lo;
+                c13 /= nb13q;
+                c13 *= (g + 0.5);
+                c13 += o13.lo;
+                if(!inDalitz(c12, c13, d.M, d.m1, d.m2, d.m3))
+                    continue;
+                double m23 = d.M * d.M + d.m1 * d.m1 + d.m2 * d.m2 + d.m3 * d.m3 - c12 - c13;
+                for(int r = 0; r < nRes; ++r)
+                    B[r] = resonance(n.children[r], c12, c13, m23, d);
+                if(!evt.empty())
+                    evt[0] = 2;
+                evt[n.obs[0]] = c12;
+                evt[n.obs[1]] = c13;
+                double e      = eval(eff, evt.data());
+                for(int r = 0; r < nRes; ++r)
+                    for(int q = 0; q < nRes; ++q)
+                        part[tid][r * nRes + q] += B[r] * std::conj(B[q]) * e;
+            }
+        }
+        std::vector<cplx> I(nRes * nRes, cplx(0, 0));
+        for(auto &p : part)
+            for(int k = 0; k < nRes * nRes; ++k)
+                I[k] += p[k];
+        amp3I[i] = I;
+        cplx sumIntegral(0, 0);
+        for(int r = 0; r < nRes; ++r) {
+            cplx ai(par(i, 2 * r), par(i, 2 * r + 1));
+            for(int q = 0; q < nRes; ++q) {
+                cplx aj(par(i, 2 * q), -par(i, 2 * q + 1));
+                sumIntegral += ai * aj * I[r * nRes + q];
+            }
+        }
+        double ret           = sumIntegral.real();
+        double binSizeFactor = 1;
+        binSizeFactor *= (o12.hi - o12.lo) / o12.nbins;
+        binSizeFactor *= (o13.hi - o13.lo) / o13.nbins;
+        ret *= binSizeFactor;
+        norm[i]     = 1.0 / ret;
+        integral[i] = ret;
+        return ret;
     }
 
     // Pre-builds conv memo tables over the k range of the given events (no effect on values).
@@ -578,6 +843,59 @@ int oracle_nll(const gf_node *nodes,
         g_err = ex.what();
         return 1;
     }
+}
+
+// The Amp3Body integrals I_ij (n x n complex, interleaved re/im) of node `node` at the given parameters.
+int oracle_amp3_integrals(const gf_node *nodes,
+                          int n_nodes,
+                          const gf_observable *obs,
+                          int n_obs,
+                          const double *params,
+                          int n_params,
+                          int node,
+                          double *out) {
+    try {
+        Oracle O;
+        load(O, nodes, n_nodes, obs, n_obs, params, n_params, 0);
+        O.normalize(node);
+        const auto &I = O.amp3I.at(node);
+        for(size_t k = 0; k < I.size(); ++k) {
+            out[2 * k]     = I[k].real();
+            out[2 * k + 1] = I[k].imag();
+        }
+        return 0;
+    } catch(std::exception &ex) {
+        g_err = ex.what();
+        return 1;
+    }
+}
+
+// Amplitude of resonance node `res` (child of Amp3Body `node`) at (m12, m13), interleaved re/im.
+int oracle_amp3_resonance(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, const double *params,
+                          int n_params, int node, int res, const double *m12, const double *m13, int64_t n,
+                          double *out) {
+    try {
+        Oracle O;
+        load(O, nodes, n_nodes, obs, n_obs, params, n_params, 0);
+        const Decay3 d = O.decay3(node);
+        for(int64_t e = 0; e < n; ++e) {
+            cplx v(0, 0);
+            if(inDalitz(m12[e], m13[e], d.M, d.m1, d.m2, d.m3)) {
+                double m23 = d.M * d.M + d.m1 * d.m1 + d.m2 * d.m2 + d.m3 * d.m3 - m12[e] - m13[e];
+                v          = O.resonance(res, m12[e], m13[e], m23, d);
+            }
+            out[2 * e]     = v.real();
+            out[2 * e + 1] = v.imag();
+        }
+        return 0;
+    } catch(std::exception &ex) {
+        g_err = ex.what();
+        return 1;
+    }
+}
+
+int oracle_in_dalitz(double m12, double m13, double M, double d1, double d2, double d3) {
+    return inDalitz(m12, m13, M, d1, d2, d3) ? 1 : 0;
 }
 
 // std::mt19937(seed) + std::exponential_distribution<>(lambda), the generator of the
