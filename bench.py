@@ -33,6 +33,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "MIGRAD fit wall-time & event-NLL evals/s: mixed-prec vs FP64 on GB300 at 1e-6 rel NLL"
+# DRAM bytes of one gf_evt_g launch over 2e6 events, from one ncu capture (profiles/gf_evt_g_c2_composite_2e6.md)
+EVT_DRAM_BYTES_PER_LAUNCH = 8_080_640
+EVT_DRAM_EVENTS = 2_000_000
 N_EVENTS = 2_000_000
 WORKLOAD = "c2: AddPdf(0.7 Conv(Exp tau=1.5, Gauss mu=0 sigma=0.3) + 0.3 flat Poly), x in [-5,10], 2e6 events"
 
@@ -288,7 +291,9 @@ def run_engine(args) -> dict | None:
                 "h2d_bytes_per_step": N_EVENTS * 8 + len(params) * 8, "d2h_bytes_per_step": (2 + eng.n_grad) * 8,
                 "ms_per_step": e2e},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": "gf_evt_g",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": EVT_DRAM_BYTES_PER_LAUNCH * N_EVENTS / EVT_DRAM_EVENTS,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/gf_evt_g_c2_composite_2e6.md",
+                     "kernel": "gf_evt_g",
                      "kernel_ms": evt, "bytes_per_event": bytes_per_event, "peak_source": peaks["src"],
                      "kernels_alone_ms": {"gf_conv_g": float(kt[0]), "gf_grid_g": float(kt[1]), "gf_evt_g": float(kt[2])}},
         "cpu_baseline": cpu,

@@ -55,6 +55,7 @@ struct Ctx {
     std::function<std::string(int)> k;           // conv index -> int expression
     std::function<std::string(int, int)> tab;    // conv index, component -> expression
     std::vector<int> *xused;
+    std::function<std::string(int, int)> amp; // Amp3Body index, resonance -> R2 amplitude expression
     int uid = 0;
     std::string tmp(const char *p) { return std::string(p) + std::to_string(uid++); }
 };
@@ -316,6 +317,83 @@ Val emit(Ctx &c, int i) {
         }
         break;
     }
+    case GF_OP_MULTIPOLYNOMIAL: {
+        // device_MultiPolynomial (src/PDFs/basic/PolynomialPdf.cu:46-107): sum over the monomials of total
+        // degree <= maxDegree, coefficients in the order the box index enumerates them
+        const int nO = (int)n.obs.size(), deg = (int)n.consts[0] + 1;
+        std::vector<std::string> d(nO);
+        for(int j = 0; j < nO; ++j) {
+            d[j] = c.tmp("d");
+            os << "    const R " << d[j] << " = " << c.x(n.obs[j]) << " - " << P(n.params[j]) << ";\n";
+        }
+        std::string v = c.tmp("v");
+        os << "    R " << v << " = " << P(n.params[nO]) << ";\n";
+        gadd(c, out, slot(c, n.params[nO]), "R(1)");
+        int64_t boxes = 1;
+        for(int j = 0; j < nO; ++j)
+            boxes *= deg;
+        int coeff = nO + 1;
+        for(int64_t b = 1; b < boxes; ++b) {
+            std::vector<int> pw(nO);
+            int64_t ci = b;
+            int sum    = 0;
+            for(int j = 0; j < nO; ++j) {
+                pw[j] = (int)(ci % deg);
+                ci /= deg;
+                sum += pw[j];
+            }
+            if(sum >= deg)
+                continue;
+            auto term = [&](int skip) {
+                std::string e;
+                for(int j = 0; j < nO; ++j) {
+                    int q = pw[j] - (j == skip ? 1 : 0);
+                    if(q > 0)
+                        e += (e.empty() ? "" : " * ") + powi(c, d[j], q);
+                }
+                return e.empty() ? std::string("R(1)") : e;
+            };
+            std::string t = c.tmp("t");
+            os << "    const R " << t << " = " << term(-1) << ";\n";
+            os << "    " << v << " += " << P(n.params[coeff]) << " * " << t << ";\n";
+            gadd(c, out, slot(c, n.params[coeff]), t);
+            for(int j = 0; j < nO; ++j)
+                if(pw[j] > 0)
+                    gadd(c, out, slot(c, n.params[j]),
+                         "-R(" + std::to_string(pw[j]) + ") * " + P(n.params[coeff]) + " * " + term(j));
+            ++coeff;
+        }
+        out.v = v;
+        break;
+    }
+    case GF_OP_AMP3BODY: {
+        // device_DalitzPlot (src/PDFs/physics/Amp3Body.cu:60-122): |sum_r c_r B_r|^2 * efficiency, with the
+        // resonance amplitudes B_r read from the per-event cache
+        if(!c.amp)
+            throw std::runtime_error("codegen: Amp3Body outside the event pass");
+        const int ai      = c.T.amp3_of[i];
+        const Amp3Info &A = c.T.amp3s[ai];
+        Val ev            = emit(c, A.eff);
+        std::string tr = c.tmp("tr"), ti = c.tmp("ti"), v = c.tmp("v");
+        os << "    R " << tr << " = R(0), " << ti << " = R(0);\n";
+        for(int r = 0; r < A.nRes; ++r) {
+            std::string b = c.amp(ai, r), cr = P(n.params[2 * r]), cim = P(n.params[2 * r + 1]);
+            os << "    " << tr << " += " << cr << " * " << b << ".x - " << cim << " * " << b << ".y;\n";
+            os << "    " << ti << " += " << cr << " * " << b << ".y + " << cim << " * " << b << ".x;\n";
+        }
+        os << "    const R " << v << " = (" << tr << " * " << tr << " + " << ti << " * " << ti << ") * " << ev.v << ";\n";
+        out.v = v;
+        for(int r = 0; r < A.nRes; ++r) {
+            std::string b = c.amp(ai, r);
+            gadd(c, out, slot(c, n.params[2 * r]),
+                 "R(2) * (" + tr + " * " + b + ".x + " + ti + " * " + b + ".y) * " + ev.v);
+            gadd(c, out, slot(c, n.params[2 * r + 1]),
+                 "R(2) * (" + ti + " * " + b + ".x - " + tr + " * " + b + ".y) * " + ev.v);
+        }
+        break;
+    }
+    case GF_OP_RES_RBW:
+    case GF_OP_RES_NONRES: throw std::runtime_error("codegen: resonances are evaluated by the amplitude kernels only");
     default: throw std::runtime_error("codegen: unsupported operator");
     }
     materialise(c, out);
@@ -345,6 +423,11 @@ struct GfArgs {
     const void *Pr;  /* [toy][npr] R: parameters, then host-computed analytic factors */
     void *Nq;        /* [toy][nq] R: numeric factors from the grid kernel */
     int *qflag;      /* [toy] bit 1 NaN, bit 2 non-positive numeric integral */
+    const void *const *acol;   /* [toy][amplitude column] R2 cached resonance amplitudes */
+    const double *const *dcol; /* [toy][observable] FP64 event columns (Dalitz variables) */
+    const unsigned *dgrid;     /* in-Dalitz normalisation bins of every Amp3Body, b12 | b13 << 16 */
+    double *gram;              /* integral partials [toy][tile][CTA][2 * pairs] */
+    const int *dirty;          /* [toy] amplitude caches to rebuild */
     int n_chunks;
     int n_toys;
     int metric;
@@ -452,12 +535,138 @@ __device__ __forceinline__ double acc_r(ACC a) { return a; }
 #define GF_CENTRE(lo, w, b) gf_centre(lo, w, b)
 )CUDA";
 
+// Dalitz-plot helpers: the kinematic boundary in FP64 with every rounding explicit (no contraction, as the
+// host restatement compiles it), and the relativistic Breit-Wigner of src/PDFs/physics/resonances/RBW.cu:9-86
+// with its helpers (src/PDFs/physics/resonances/Resonance.cu:48-155).  The amplitude works in R; the squared
+// masses and their differences with the resonance mass come in FP64, so that an FP32 amplitude loses nothing
+// to cancellation near the pole.
+const char *kPreludeAmp = R"CUDA(
+__device__ __forceinline__ bool gf_in_dalitz(double m12, double m13, double M, double m1, double m2, double m3) {
+    const double dm1pdm2 = __dadd_rn(m1, m2), bigMmdm3 = __dsub_rn(M, m3), bigMmdm1 = __dsub_rn(M, m1);
+    const double MM = __dmul_rn(M, M), m11 = __dmul_rn(m1, m1), m22 = __dmul_rn(m2, m2), m33 = __dmul_rn(m3, m3);
+    const double m23 = __dsub_rn(__dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(MM, m11), m22), m33), m12), m13);
+    if(m23 < 0. || m23 > __dmul_rn(bigMmdm1, bigMmdm1))
+        return false;
+    const bool a = !(m12 < __dmul_rn(dm1pdm2, dm1pdm2)), b = !(m12 > __dmul_rn(bigMmdm3, bigMmdm3));
+    const double rt = __dsqrt_rn(m12);
+    const double e1 = __ddiv_rn(__dmul_rn(0.5, __dadd_rn(__dsub_rn(m12, m22), m11)), rt);
+    const double e3 = __ddiv_rn(__dmul_rn(0.5, __dsub_rn(__dsub_rn(MM, m12), m33)), rt);
+    const double p1 = __dsqrt_rn(__dsub_rn(__dmul_rn(e1, e1), m11));
+    const double p3 = __dsqrt_rn(__dsub_rn(__dmul_rn(e3, e3), m33));
+    const double s = __dadd_rn(e1, e3), u = __dadd_rn(p1, p3), w = __dsub_rn(p1, p3);
+    const double lo = __dsub_rn(__dmul_rn(s, s), __dmul_rn(u, u)), hi = __dsub_rn(__dmul_rn(s, s), __dmul_rn(w, w));
+    return a && b && !(m13 < lo) && !(m13 > hi);
+}
+__device__ __forceinline__ double gf_m23(double m12, double m13, double M, double m1, double m2, double m3) {
+    return __dsub_rn(__dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(M, M), __dmul_rn(m1, m1)), __dmul_rn(m2, m2)),
+                                          __dmul_rn(m3, m3)), m12), m13);
+}
+__device__ __forceinline__ R gf_tb_mom(R s, R a, R b) {
+    R k1 = R(1) - (a + b) * (a + b) / s;
+    k1   = k1 >= R(0) ? sqrt(k1) : R(1);
+    R k2 = R(1) - (a - b) * (a - b) / s;
+    k2   = k2 >= R(0) ? sqrt(k2) : R(1);
+    return R(0.5) * sqrt(s) * k1 * k2;
+}
+__device__ __forceinline__ R gf_tb_mom_mother(R s, R M, R c) {
+    R k1 = R(1) - (M + c) * (M + c) / s;
+    k1   = k1 >= R(0) ? sqrt(k1) : R(1);
+    R k2 = R(1) - (M - c) * (M - c) / s;
+    k2   = k2 >= R(0) ? sqrt(k2) : R(1);
+    return R(0.5) * s * k1 * k2 / M;
+}
+__device__ __forceinline__ R gf_damp2(R p, int spin, R r) {
+    const R sq = r * r * p * p;
+    return spin == 2 ? R(13) * sq / ((sq - R(3)) * (sq - R(3))) + R(9) * sq * sq : R(2) * sq;
+}
+__device__ __forceinline__ R gf_damp2n(R p, int spin, R r) {
+    const R sq = r * r * p * p;
+    const R d  = R(1) + sq;
+    return spin == 2 ? d + R(8) + R(2) * sq + sq * sq : d;
+}
+// Zemach spin factor (Resonance.cu spinFactor); the event-dependent differences are formed in FP64.
+__device__ __forceinline__ R gf_spin(int spin, double M, double m1, double m2, double m3, double m12, double m13,
+                                     double m23, int cyc) {
+    if(spin == 0)
+        return R(1);
+    const double mA = cyc == 0 ? m1 : (cyc == 1 ? m3 : m2), mB = cyc == 0 ? m2 : (cyc == 1 ? m1 : m3);
+    const double mC = cyc == 0 ? m3 : (cyc == 1 ? m2 : m1);
+    const double mAC = cyc == 0 ? m13 : (cyc == 1 ? m23 : m12), mBC = cyc == 0 ? m23 : (cyc == 1 ? m12 : m13);
+    const double mAB = cyc == 0 ? m12 : (cyc == 1 ? m13 : m23);
+    const R massFactor = R(1) / (R)mAB;
+    const R MC = (R)(M * M - mC * mC), AB = (R)(mA * mA - mB * mB);
+    R sf = -((R)(mBC - mAC) + massFactor * MC * AB);
+    if(spin == 2) {
+        sf *= sf;
+        R ex = ((R)(mAB - 2 * M * M - 2 * mC * mC) + massFactor * MC * MC);
+        ex *= ((R)(mAB - 2 * mA * mA - 2 * mB * mB) + massFactor * AB * AB);
+        ex /= R(3);
+        sf -= ex;
+    }
+    return sf;
+}
+template <int I>
+__device__ __forceinline__ R2 gf_rbw(double m12, double m13, double m23, double mass, double width, int spin, int cyc,
+                                     bool norm, double M, double m1, double m2, double m3, double rr, double rmm) {
+    R re = R(0), im = R(0);
+    const double rm2 = mass * mass;
+    const R rs = (R)rm2, r = (R)rr, rm = (R)rmm;
+#pragma unroll
+    for(int it = 0; it < I; ++it) {
+        const double sq = cyc == 0 ? m12 : (cyc == 1 ? m13 : m23);
+        const R d1 = (R)(cyc == 2 ? m2 : m1), d2 = (R)(cyc == 0 ? m2 : m3);
+        const R bach = (R)(cyc == 0 ? m3 : (cyc == 1 ? m2 : m1));
+        const R s = (R)sq;
+        R fr = R(1), frM = R(1);
+        const R pm = gf_tb_mom(s, d1, d2), pn = gf_tb_mom(rs, d1, d2);
+        R pmM, pnM = R(0);
+        if(norm) {
+            pmM = gf_tb_mom_mother(s, (R)M, bach);
+            pnM = gf_tb_mom_mother(rs, (R)M, bach);
+        } else
+            pmM = gf_tb_mom((R)(M * M), sqrt(s), bach);
+        if(spin != 0) {
+            if(norm) {
+                fr  = gf_damp2n(pn, spin, r) / gf_damp2n(pm, spin, r);
+                frM = gf_damp2n(pnM, spin, rm) / gf_damp2n(pmM, spin, rm);
+            } else {
+                fr  = gf_damp2(pm, spin, r);
+                frM = gf_damp2(pmM, spin, rm);
+            }
+        }
+        const R A = (R)(rm2 - sq);
+        const R q = pm / pn;
+        R qp      = q;
+        for(int k = 0; k < 2 * spin; ++k)
+            qp *= q;
+        const R B = rs * (R)width * qp * fr / sqrt(s);
+        const R C = R(1) / (A * A + B * B);
+        R xr = A * C, xi = B * C;
+        const R f1 = sqrt(fr), f2 = sqrt(frM), sf = gf_spin(spin, M, m1, m2, m3, m12, m13, m23, cyc);
+        xr *= f1;
+        xi *= f1;
+        xr *= f2;
+        xi *= f2;
+        xr *= sf;
+        xi *= sf;
+        re += xr;
+        im += xi;
+        if(I > 1)
+            cyc = (cyc + 1) % 3;
+    }
+    R2 o;
+    o.x = re;
+    o.y = im;
+    return o;
+}
+)CUDA";
+
 // Where every normalisation factor is kept (see NormLayout in tree.h).
 NormLayout computeNormLayout(const Tree &T) {
     NormLayout nl;
     nl.npr = T.n_params;
     for(size_t i = 0; i < T.nodes.size(); ++i) {
-        if(T.nk[i] != NK_EXP && T.nk[i] != NK_GAUSS)
+        if(T.nk[i] != NK_EXP && T.nk[i] != NK_GAUSS && T.nk[i] != NK_AMP3)
             continue;
         NormLayout::Analytic a;
         a.node  = (int)i;
@@ -826,6 +1035,153 @@ struct Gen {
         os << "    }\n  }\n}\n\n";
     }
 
+    // ---------------- Amp3Body amplitude caches and integrals ----------------
+    // Rebuilt only for toys flagged in a.dirty (the resonance or efficiency parameters changed), as
+    // Amp3Body::normalize does with its per-resonance redoIntegral flags
+    // (src/PDFs/physics/Amp3Body.cu:263-330).
+    //   gf_amp   B_r(event) for every resonance into the R2 columns, zero outside the kinematic boundary
+    //            (SpecialResonanceCalculator, src/PDFs/physics/detail/SpecialResonanceCalculator.cu:12-45)
+    //   gf_gram  I_ij = sum over in-Dalitz bins of B_i conj(B_j) eff, i <= j, per-CTA FP64 partials
+    //            (SpecialResonanceIntegrator, src/PDFs/physics/detail/SpecialResonanceIntegrator.cu:7-121)
+    std::string resCall(const Amp3Info &A, int r, const char *m12, const char *m13, const char *m23) {
+        const TNode &rn = T.nodes[A.res[r]];
+        if(rn.op == GF_OP_RES_NONRES)
+            return mixed ? "make_float2(1.0f, 0.0f)" : "make_double2(1.0, 0.0)";
+        const int I = (rn.consts.size() > 3 && rn.consts[3] != 0) ? 2 : 1;
+        std::ostringstream o;
+        o << "gf_rbw<" << I << ">(" << m12 << ", " << m13 << ", " << m23 << ", P[" << rn.params[0] << "], P["
+          << rn.params[1] << "], " << (int)rn.consts[0] << ", " << (int)rn.consts[1] << ", "
+          << (rn.consts[2] != 0 ? "true" : "false") << ", " << lit(A.M) << ", " << lit(A.m1) << ", " << lit(A.m2)
+          << ", " << lit(A.m3) << ", " << lit(A.r) << ", " << lit(A.rm) << ")";
+        return o.str();
+    }
+    std::string dalitzArgs(const Amp3Info &A) {
+        return lit(A.M) + ", " + lit(A.m1) + ", " + lit(A.m2) + ", " + lit(A.m3);
+    }
+
+    void ampKernels() {
+        if(T.amp3s.empty())
+            return;
+        const int NA = T.n_amp_cols, NO = (int)T.obs.size(), np = std::max(1, T.n_params);
+        os << "extern \"C\" __global__ void __launch_bounds__(256) gf_amp(const GfArgs a) {\n";
+        os << "  const int toy = blockIdx.y, k = blockIdx.z, tid = threadIdx.x;\n";
+        os << "  if(!a.dirty[toy]) return;\n";
+        os << "  const i64 n = a.toy_nevents[toy], npad = n < 8 ? 8 : (n + 7) / 8 * 8;\n";
+        os << "  const double *P = a.P + (i64)toy * " << np << "; (void)P;\n";
+        os << "  R2 *const *ac = reinterpret_cast<R2 *const *>(a.acol) + (i64)toy * " << NA << ";\n";
+        os << "  switch(k) {\n";
+        for(size_t ai = 0; ai < T.amp3s.size(); ++ai) {
+            const Amp3Info &A = T.amp3s[ai];
+            os << "  case " << ai << ": {\n";
+            os << "    const double *x12 = a.dcol[(i64)toy * " << NO << " + " << A.o12 << "];\n";
+            os << "    const double *x13 = a.dcol[(i64)toy * " << NO << " + " << A.o13 << "];\n";
+            os << "    for(i64 i = (i64)blockIdx.x * 256 + tid; i < npad; i += (i64)gridDim.x * 256) {\n";
+            for(int r = 0; r < A.nRes; ++r)
+                os << "      R2 b" << r << "; b" << r << ".x = R(0); b" << r << ".y = R(0);\n";
+            os << "      if(i < n) {\n";
+            os << "        const double m12 = x12[i], m13 = x13[i];\n";
+            os << "        if(gf_in_dalitz(m12, m13, " << dalitzArgs(A) << ")) {\n";
+            os << "          const double m23 = gf_m23(m12, m13, " << dalitzArgs(A) << ");\n";
+            for(int r = 0; r < A.nRes; ++r)
+                os << "          b" << r << " = " << resCall(A, r, "m12", "m13", "m23") << ";\n";
+            os << "        }\n      }\n";
+            for(int r = 0; r < A.nRes; ++r)
+                os << "      ac[" << A.col0 + r << "][i] = b" << r << ";\n";
+            os << "    }\n    break; }\n";
+        }
+        os << "  default: break;\n  }\n}\n\n";
+
+        // integrals: tiles of at most 36 pairs per CTA row
+        plan.gram_tiles.clear();
+        plan.gram_pairs_max = 0;
+        plan.dgrid_off.clear();
+        int64_t goff = 0;
+        for(size_t ai = 0; ai < T.amp3s.size(); ++ai) {
+            const int n = T.amp3s[ai].nRes, npairs = n * (n + 1) / 2;
+            for(int p0 = 0; p0 < npairs; p0 += 36) {
+                KernelPlan::GramTile t{(int)ai, p0, std::min(npairs, p0 + 36)};
+                plan.gram_tiles.push_back(t);
+                plan.gram_pairs_max = std::max(plan.gram_pairs_max, t.p1 - t.p0);
+            }
+            plan.dgrid_off.push_back(goff);
+            goff += (int64_t)T.amp3s[ai].grid.size();
+        }
+        const int PM = plan.gram_pairs_max, NW = 256 / 32;
+        os << "extern \"C\" __global__ void __launch_bounds__(256) gf_gram(const GfArgs a) {\n";
+        os << "  const int toy = blockIdx.y, z = blockIdx.z, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;\n";
+        os << "  if(!a.dirty[toy]) return;\n";
+        os << "  const double *P = a.P + (i64)toy * " << np << "; (void)P;\n";
+        os << "  const R *Pr = reinterpret_cast<const R *>(a.Pr) + (i64)toy * " << plan.nl.npr << "; (void)Pr;\n";
+        for(int j = 0; j < T.n_params; ++j)
+            os << "  const R p" << j << " = Pr[" << j << "]; (void)p" << j << ";\n";
+        os << "  __shared__ double red[" << NW << "][" << 2 * PM << "];\n";
+        os << "  double *out = a.gram + (((i64)toy * " << plan.gram_tiles.size() << " + z) * gridDim.x + blockIdx.x) * "
+           << 2 * PM << ";\n";
+        os << "  switch(z) {\n";
+        for(size_t ti = 0; ti < plan.gram_tiles.size(); ++ti) {
+            const auto &tile  = plan.gram_tiles[ti];
+            const Amp3Info &A = T.amp3s[tile.amp];
+            std::vector<std::pair<int, int>> pairs;
+            for(int i = 0, q = 0; i < A.nRes; ++i)
+                for(int j = i; j < A.nRes; ++j, ++q)
+                    if(q >= tile.p0 && q < tile.p1)
+                        pairs.push_back({i, j});
+            std::vector<int> need(A.nRes, 0);
+            for(auto &pr : pairs)
+                need[pr.first] = need[pr.second] = 1;
+            const int npr = (int)pairs.size();
+            const gf_observable &g12 = T.obs[A.o12], &g13 = T.obs[A.o13];
+            double w12 = g12.hi - g12.lo;
+            w12 /= A.nb12;
+            double w13 = g13.hi - g13.lo;
+            w13 /= A.nb13q;
+            os << "  case " << ti << ": {\n";
+            for(int q = 0; q < npr; ++q)
+                os << "    R sr" << q << " = R(0), si" << q << " = R(0);\n";
+            os << "    const unsigned *pts = a.dgrid + " << plan.dgrid_off[tile.amp] << "LL;\n";
+            os << "    for(int p = blockIdx.x * 256 + tid; p < " << A.grid.size() << "; p += gridDim.x * 256) {\n";
+            os << "      const unsigned q = pts[p];\n";
+            os << "      const double c12 = gf_centre(" << lit(g12.lo) << ", " << lit(w12) << ", (int)(q & 0xffffu));\n";
+            os << "      const double c13 = gf_centre(" << lit(g13.lo) << ", " << lit(w13) << ", (int)(q >> 16));\n";
+            os << "      const double m23 = gf_m23(c12, c13, " << dalitzArgs(A) << ");\n";
+            for(int r = 0; r < A.nRes; ++r)
+                if(need[r])
+                    os << "      const R2 b" << r << " = " << resCall(A, r, "c12", "c13", "m23") << ";\n";
+            // the efficiency at the bin centre; the reference's fake event holds 2 in slot 0
+            std::ostringstream body;
+            Ctx c{body, T, false, false, nullptr, nullptr, nullptr, nullptr};
+            c.x = [&](int o) -> std::string {
+                if(o == A.o12)
+                    return "((R)c12)";
+                if(o == A.o13)
+                    return "((R)c13)";
+                return "R(2)";
+            };
+            c.k   = [&](int) -> std::string { throw std::runtime_error("codegen: convolution in an efficiency"); };
+            c.tab = [&](int, int) -> std::string { throw std::runtime_error("codegen: convolution in an efficiency"); };
+            Val ev = emit(c, A.eff);
+            os << "      {\n" << body.str();
+            os << "      const R e = " << ev.v << ";\n";
+            for(int q = 0; q < npr; ++q) {
+                int i = pairs[q].first, j = pairs[q].second;
+                os << "      sr" << q << " += (b" << i << ".x * b" << j << ".x + b" << i << ".y * b" << j << ".y) * e;\n";
+                os << "      si" << q << " += (b" << i << ".y * b" << j << ".x - b" << i << ".x * b" << j << ".y) * e;\n";
+            }
+            os << "      }\n    }\n";
+            for(int q = 0; q < npr; ++q) {
+                os << "    { const double t = gf_warp_sum((double)sr" << q << "); if(lane == 0) red[wid][" << 2 * q
+                   << "] = t; }\n";
+                os << "    { const double t = gf_warp_sum((double)si" << q << "); if(lane == 0) red[wid][" << 2 * q + 1
+                   << "] = t; }\n";
+            }
+            os << "    __syncthreads();\n";
+            os << "    if(tid < " << 2 * npr << ") { double t = 0.0; for(int w = 0; w < " << NW
+               << "; ++w) t += red[w][tid]; out[tid] = t; }\n";
+            os << "    break; }\n";
+        }
+        os << "  default: break;\n  }\n}\n\n";
+    }
+
     // ---------------- event pass ----------------
     // Persistent CTAs take contiguous ranges of the chunk list and stage a toy's conv tables once; each
     // thread streams 8 events per iteration with 16-byte loads.  Partial sums: FP32 per thread, then
@@ -837,7 +1193,10 @@ struct Gen {
         const int NC  = (int)T.convs.size();
         const int NO  = (int)T.obs.size();
         const int NW  = block / 32;
-        const int VEC = 8;
+        const int NA  = T.n_amp_cols;
+        // events per thread and iteration: 8 (16-byte loads of FP32 columns), 2 when cached amplitudes
+        // (one R2 per event and resonance) are streamed as well
+        const int VEC = NA > 0 ? 2 : 8;
         auto &off     = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
         auto &cps     = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
         const int64_t ctabTotal = grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd;
@@ -863,6 +1222,7 @@ struct Gen {
                 return "tq" + std::to_string(ci) + fld[comp];
             return "tq" + std::to_string(ci) + "_" + std::to_string(comp / 4) + fld[comp % 4];
         };
+        c.amp = [&](int ai, int r) { return "am" + std::to_string(T.amp3s[ai].col0 + r); };
         Val root = emit(c, 0);
         if(!values && !grad) {
             plan.obs_used_evt.clear();
@@ -896,6 +1256,9 @@ struct Gen {
         for(int ci = 0; ci < NC; ++ci)
             os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(a.kcol[(i64)toy * " << NC << " + " << ci
                << "] + i0));\n";
+        for(int ac = 0; ac < NA; ++ac)
+            os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(reinterpret_cast<const R2 *>(a.acol[(i64)toy * "
+               << NA << " + " << ac << "]) + i0));\n";
         os << "      }\n    }\n  }\n";
         os << "  gf_pdl_wait();\n";
         os << "  __syncthreads();\n";
@@ -928,13 +1291,35 @@ struct Gen {
                    << "]);\n";
         for(int ci = 0; ci < NC; ++ci)
             os << "    const int *kc" << ci << " = a.kcol[(i64)toy * " << NC << " + " << ci << "];\n";
+        for(int ac = 0; ac < NA; ++ac)
+            os << "    const R2 *acp" << ac << " = reinterpret_cast<const R2 *>(a.acol[(i64)toy * " << NA << " + " << ac
+               << "]);\n";
         if(!values) {
             os << "    R av = R(0);\n";
             for(int s = 0; s < NGp - 1; ++s)
                 os << "    R ag" << s << " = R(0);\n";
         }
         os << "    for(i64 i0 = b0 + " << VEC << " * (i64)tid; i0 < e0; i0 += " << VEC << " * " << block << ") {\n";
-        for(int o = 0; o < NO; ++o)
+        for(int o = 0; o < NO && VEC == 2; ++o)
+            if(xused[o]) {
+                if(mixed)
+                    os << "      const float2 xv" << o << " = *reinterpret_cast<const float2 *>(col" << o << " + i0);\n";
+                else
+                    os << "      const double2 xv" << o << " = *reinterpret_cast<const double2 *>(col" << o << " + i0);\n";
+                os << "      const R xa" << o << "[2] = {xv" << o << ".x, xv" << o << ".y};\n";
+            }
+        for(int ci = 0; ci < NC && VEC == 2; ++ci)
+            os << "      const int2 kv" << ci << " = *reinterpret_cast<const int2 *>(kc" << ci << " + i0);\n"
+               << "      const int ka" << ci << "[2] = {kv" << ci << ".x, kv" << ci << ".y};\n";
+        for(int ac = 0; ac < NA; ++ac) {
+            if(mixed)
+                os << "      const float4 av" << ac << " = *reinterpret_cast<const float4 *>(acp" << ac << " + i0);\n"
+                   << "      const R2 aa" << ac << "[2] = {make_float2(av" << ac << ".x, av" << ac
+                   << ".y), make_float2(av" << ac << ".z, av" << ac << ".w)};\n";
+            else
+                os << "      const R2 aa" << ac << "[2] = {acp" << ac << "[i0], acp" << ac << "[i0 + 1]};\n";
+        }
+        for(int o = 0; o < NO && VEC == 8; ++o)
             if(xused[o]) {
                 if(mixed)
                     os << "      const float4 xv" << o << "a = *reinterpret_cast<const float4 *>(col" << o
@@ -948,7 +1333,7 @@ struct Gen {
                        << o << " + i0 + 2 * h); xa" << o << "[2 * h] = t.x; xa" << o << "[2 * h + 1] = t.y; }\n";
                 }
             }
-        for(int ci = 0; ci < NC; ++ci)
+        for(int ci = 0; ci < NC && VEC == 8; ++ci)
             os << "      const int4 kv" << ci << "a = *reinterpret_cast<const int4 *>(kc" << ci << " + i0), kv" << ci
                << "b = *reinterpret_cast<const int4 *>(kc" << ci << " + i0 + 4);\n"
                << "      const int ka" << ci << "[8] = {kv" << ci << "a.x, kv" << ci << "a.y, kv" << ci << "a.z, kv" << ci
@@ -957,6 +1342,8 @@ struct Gen {
         for(int o = 0; o < NO; ++o)
             if(xused[o])
                 os << "        const R ex" << o << " = xa" << o << "[j];\n";
+        for(int ac = 0; ac < NA; ++ac)
+            os << "        const R2 am" << ac << " = aa" << ac << "[j];\n";
         for(int ci = 0; ci < NC; ++ci) {
             const ConvInfo &cv = T.convs[ci];
             int cp             = cps[ci];
@@ -1054,10 +1441,12 @@ KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, int chunk)
     Gen g{t, mixed, evt_block, chunk, plan, {}};
     g.os << "// generated likelihood kernels\n";
     if(mixed)
-        g.os << "typedef float R;\n#define GF_EXP(x) expf(x)\n#define GF_LOG(x) logf(x)\n";
+        g.os << "typedef float R;\ntypedef float2 R2;\n#define GF_EXP(x) expf(x)\n#define GF_LOG(x) logf(x)\n";
     else
-        g.os << "typedef double R;\n#define GF_EXP(x) exp(x)\n#define GF_LOG(x) log(x)\n";
+        g.os << "typedef double R;\ntypedef double2 R2;\n#define GF_EXP(x) exp(x)\n#define GF_LOG(x) log(x)\n";
     g.os << kPrelude;
+    if(!t.amp3s.empty())
+        g.os << kPreludeAmp;
     if(mixed)
         g.os << kPreludeF32;
     else
@@ -1068,6 +1457,7 @@ KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, int chunk)
     g.convKernel(false);
     g.gridKernel(true);
     g.gridKernel(false);
+    g.ampKernels();
     g.eventKernel(true, false);
     g.eventKernel(false, false);
     g.eventKernel(false, true);

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <complex>
 #include <cstring>
 #include <new>
 
@@ -82,7 +83,16 @@ void freeToy(GfToy &t) {
         }
     for(int c = 0; c < 8; ++c)
         t.kcols[c] = nullptr;
-    t.loaded = false;
+    if(t.abase)
+        cudaFree(t.abase);
+    t.abase = nullptr;
+    for(auto &p : t.acols)
+        p = nullptr;
+    for(auto &p : t.dcols)
+        p = nullptr;
+    t.loaded    = false;
+    t.amp_valid = false;
+    t.amp_I.clear();
     t.n = t.npad = 0;
 }
 
@@ -127,6 +137,13 @@ void freeLayout(gf_engine *e) {
     dfree(e->d_toy_nevents);
     dfree(e->d_Nq);
     dfree(e->d_qflag);
+    dfree(e->d_acols);
+    dfree(e->d_dcols);
+    dfree(e->d_dgrid);
+    dfree(e->d_gram);
+    dfree(e->d_dirty);
+    hfree(e->h_gram);
+    hfree(e->h_dirty);
     hfree(e->h_P);
     hfree(e->h_active);
     hfree(e->h_out);
@@ -228,8 +245,40 @@ int buildLayout(gf_engine *e) {
     chk(dalloc(e, e->d_toy_chunk0, NT));
     chk(dalloc(e, e->d_toy_nchunks, NT));
     chk(dalloc(e, e->d_toy_nevents, NT));
+    const int NA = T.n_amp_cols, NTILE = (int)e->plan.gram_tiles.size();
+    size_t ngrid = 0;
+    for(auto &A : T.amp3s)
+        ngrid += A.grid.size();
+    e->gram_blocks = 2 * std::max(1, e->sm_count);
+    chk(dalloc(e, e->d_acols, (size_t)NT * std::max(1, NA)));
+    chk(dalloc(e, e->d_dcols, (size_t)NT * NO));
+    chk(dalloc(e, e->d_dgrid, std::max<size_t>(1, ngrid)));
+    chk(dalloc(e, e->d_gram, (size_t)NT * std::max(1, NTILE) * e->gram_blocks * std::max(1, 2 * e->plan.gram_pairs_max)));
+    chk(dalloc(e, e->d_dirty, NT));
     if(rc != GF_OK)
         return rc;
+    if(cudaMallocHost((void **)&e->h_gram, sizeof(double) * (size_t)NT * std::max(1, NTILE) * e->gram_blocks *
+                                               std::max(1, 2 * e->plan.gram_pairs_max)) != cudaSuccess ||
+       cudaMallocHost((void **)&e->h_dirty, sizeof(int) * NT) != cudaSuccess)
+        return gf_fail(e, GF_ERR_OOM, "cudaMallocHost");
+    {
+        std::vector<void *> ac((size_t)NT * std::max(1, NA), nullptr);
+        std::vector<double *> dc((size_t)NT * NO, nullptr);
+        for(int t = 0; t < NT; ++t) {
+            for(int c = 0; c < NA; ++c)
+                ac[(size_t)t * NA + c] = e->toys[t].acols[c];
+            for(int o = 0; o < NO; ++o)
+                dc[(size_t)t * NO + o] = e->toys[t].dcols[o];
+        }
+        std::vector<unsigned> g;
+        g.reserve(ngrid);
+        for(auto &A : T.amp3s)
+            g.insert(g.end(), A.grid.begin(), A.grid.end());
+        cudaMemcpy(e->d_acols, ac.data(), sizeof(void *) * ac.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(e->d_dcols, dc.data(), sizeof(double *) * dc.size(), cudaMemcpyHostToDevice);
+        if(!g.empty())
+            cudaMemcpy(e->d_dgrid, g.data(), sizeof(unsigned) * g.size(), cudaMemcpyHostToDevice);
+    }
     if(cudaMallocHost((void **)&e->h_P, e->pblock_bytes) != cudaSuccess ||
        cudaMallocHost((void **)&e->h_active, sizeof(int) * NT) != cudaSuccess ||
        cudaMallocHost((void **)&e->h_out, sizeof(double) * (size_t)NT * (NGp + 1)) != cudaSuccess)
@@ -283,6 +332,11 @@ GfArgs makeArgs(gf_engine *e) {
     a.Pr          = (const char *)e->d_P + sizeof(double) * (size_t)e->n_toys * std::max(1, e->tree.n_params);
     a.Nq          = e->d_Nq;
     a.qflag       = e->d_qflag;
+    a.acol        = (const void *const *)e->d_acols;
+    a.dcol        = (const double *const *)e->d_dcols;
+    a.dgrid       = e->d_dgrid;
+    a.gram        = e->d_gram;
+    a.dirty       = e->d_dirty;
     a.n_chunks    = e->n_chunks;
     a.n_toys      = e->n_toys;
     a.metric      = 1;
@@ -400,6 +454,9 @@ int loadModule(gf_engine *e) {
        (rc = get(e->mod.evt_g, "gf_evt_g", true)) || (rc = get(e->mod.evt_n, "gf_evt_n", true)) ||
        (rc = get(e->mod.val_n, "gf_val_n", true)))
         return rc;
+    const bool hasAmp = !e->tree.amp3s.empty();
+    if((rc = get(e->mod.amp, "gf_amp", hasAmp)) || (rc = get(e->mod.gram, "gf_gram", hasAmp)))
+        return rc;
     auto smem = [&](cudaKernel_t k, size_t bytes) -> int {
         if(!k || bytes <= 48 * 1024)
             return GF_OK;
@@ -416,6 +473,55 @@ int loadModule(gf_engine *e) {
     if(e->plan.conv_smem_grad > maxSmem || e->plan.evt_smem_grad > maxSmem)
         return gf_fail(e, GF_ERR_BAD_TREE, "convolution workspaces exceed shared memory");
     return GF_OK;
+}
+
+// binSizeFactor of Amp3Body::normalize (src/PDFs/physics/Amp3Body.cu:350-353).
+double amp3BinSize(const gf::Tree &T, int node) {
+    const gf::Amp3Info &A = T.amp3s[T.amp3_of[node]];
+    const gf_observable &o12 = T.obs[A.o12], &o13 = T.obs[A.o13];
+    double f = 1;
+    f *= (o12.hi - o12.lo) / o12.nbins;
+    f *= (o13.hi - o13.lo) / o13.nbins;
+    return f;
+}
+
+// Amp3Body normalisation integral (src/PDFs/physics/Amp3Body.cu:334-356): the real part of
+// sum_ij c_i conj(c_j) I_ij times the bin size factor, from the cached integrals; dQ[k] receives the
+// derivative of the real part with respect to the k-th entry of an.dN (before the bin size factor).
+double amp3Integral(const gf_engine *e, int t, int node, const double *P, const gf::NormLayout::Analytic &an,
+                    double *dQ) {
+    typedef std::complex<double> C;
+    const gf::Tree &T     = e->tree;
+    const gf::TNode &nd   = T.nodes[node];
+    const int n           = T.amp3s[T.amp3_of[node]].nRes;
+    const std::vector<double> &I = e->toys[t].amp_I[T.amp3_of[node]];
+    auto Iij = [&](int i, int j) { return C(I[2 * (i * n + j)], I[2 * (i * n + j) + 1]); };
+    C sum(0, 0);
+    for(int i = 0; i < n; ++i) {
+        C ai(P[nd.params[2 * i]], P[nd.params[2 * i + 1]]);
+        for(int j = 0; j < n; ++j) {
+            C aj(P[nd.params[2 * j]], -P[nd.params[2 * j + 1]]);
+            sum += ai * aj * Iij(i, j);
+        }
+    }
+    for(size_t k = 0; k < an.dN.size() && k < 64; ++k) {
+        const int p = T.gparam[an.dN[k].first];
+        std::vector<C> dc(n);
+        for(int i = 0; i < n; ++i)
+            dc[i] = C(nd.params[2 * i] == p ? 1.0 : 0.0, nd.params[2 * i + 1] == p ? 1.0 : 0.0);
+        C d(0, 0);
+        for(int i = 0; i < n; ++i) {
+            C ci(P[nd.params[2 * i]], P[nd.params[2 * i + 1]]);
+            for(int j = 0; j < n; ++j) {
+                C cj(P[nd.params[2 * j]], P[nd.params[2 * j + 1]]);
+                d += (dc[i] * std::conj(cj) + ci * std::conj(dc[j])) * Iij(i, j);
+            }
+        }
+        dQ[k] = d.real();
+    }
+    double ret = sum.real();
+    ret *= amp3BinSize(T, node);
+    return ret;
 }
 
 // Host part of every evaluation: the per-toy records the kernels read (parameters as R, then the
@@ -438,6 +544,22 @@ void fillRecordsT(gf_engine *e) {
             r[j] = (R)P[j];
         for(auto &an : nl.analytic) {
             const gf::TNode &nd = T.nodes[an.node];
+            if(an.kind == gf::NK_AMP3) {
+                double dQ[64];
+                const double Iv = amp3Integral(e, t, an.node, P, an, dQ);
+                const double f  = amp3BinSize(T, an.node);
+                const double N  = 1.0 / Iv;
+                r[an.slotN]     = (R)N;
+                for(size_t k = 0; k < an.dN.size(); ++k)
+                    r[an.dN[k].second] = (R)(-N * N * f * dQ[k]);
+                if(an.node == 0) {
+                    if(std::isnan(Iv))
+                        e->host_flag[t] |= 1;
+                    else if(!(N > 0))
+                        e->host_flag[t] |= 2;
+                }
+                continue;
+            }
             double I = 1, dI;
             if(an.kind == gf::NK_EXP) {
                 const gf_observable &o = T.obs[nd.obs[0]];
@@ -477,6 +599,95 @@ void fillRecords(gf_engine *e) {
         fillRecordsT<float>(e);
     else
         fillRecordsT<double>(e);
+}
+
+// Rebuilds the resonance amplitude caches and the normalisation integrals of the active toys whose
+// resonance or efficiency parameters changed since the last build (Amp3Body::normalize's redoIntegral
+// logic, src/PDFs/physics/Amp3Body.cu:263-330).  Runs outside the captured evaluation graph; the
+// evaluations that follow read the caches and the host copies of the integrals.
+int updateAmpCaches(gf_engine *e) {
+    const gf::Tree &T = e->tree;
+    if(T.amp3s.empty())
+        return GF_OK;
+    const int NT = e->n_toys, np = T.n_params, NTILE = (int)e->plan.gram_tiles.size();
+    const int PM2 = 2 * e->plan.gram_pairs_max;
+    std::vector<int> cp;
+    for(auto &A : T.amp3s)
+        cp.insert(cp.end(), A.cache_params.begin(), A.cache_params.end());
+    std::sort(cp.begin(), cp.end());
+    cp.erase(std::unique(cp.begin(), cp.end()), cp.end());
+    bool any = false;
+    int64_t maxpad = 8;
+    std::vector<std::vector<double>> snap(NT);
+    for(int t = 0; t < NT; ++t) {
+        e->h_dirty[t] = 0;
+        if(!e->h_active[t])
+            continue;
+        const double *P = e->h_P + (size_t)t * np;
+        for(int p : cp)
+            snap[t].push_back(P[p]);
+        GfToy &ty = e->toys[t];
+        if(!ty.amp_valid || ty.amp_params != snap[t]) {
+            e->h_dirty[t] = 1;
+            any           = true;
+            maxpad        = std::max<int64_t>(maxpad, ty.npad);
+        }
+    }
+    if(!any)
+        return GF_OK;
+    fillRecords(e); // R copies of the parameters for the efficiency in the integral kernel
+    GfArgs a      = makeArgs(e);
+    cudaError_t r = cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
+    if(r == cudaSuccess)
+        r = cudaMemcpyAsync(e->d_dirty, e->h_dirty, sizeof(int) * NT, cudaMemcpyHostToDevice, e->stream);
+    if(r == cudaSuccess) {
+        const int64_t bx = std::min<int64_t>((maxpad + 255) / 256, (int64_t)std::max(1, e->sm_count) * 8);
+        r = launch(e->mod.amp, dim3((unsigned)bx, NT, (unsigned)T.amp3s.size()), dim3(256), 0, e->stream, a);
+    }
+    if(r == cudaSuccess)
+        r = launch(e->mod.gram, dim3(e->gram_blocks, NT, NTILE), dim3(256), 0, e->stream, a);
+    const size_t gbytes = sizeof(double) * (size_t)NT * NTILE * e->gram_blocks * PM2;
+    if(r == cudaSuccess)
+        r = cudaMemcpyAsync(e->h_gram, e->d_gram, gbytes, cudaMemcpyDeviceToHost, e->stream);
+    if(r == cudaSuccess)
+        r = cudaStreamSynchronize(e->stream);
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "Dalitz amplitude caches");
+    for(int t = 0; t < NT; ++t) {
+        if(!e->h_dirty[t])
+            continue;
+        GfToy &ty = e->toys[t];
+        ty.amp_I.assign(T.amp3s.size(), {});
+        for(size_t ai = 0; ai < T.amp3s.size(); ++ai) {
+            const int n = T.amp3s[ai].nRes;
+            std::vector<double> I(2 * (size_t)n * n, 0.0);
+            for(int z = 0; z < NTILE; ++z) {
+                const auto &tile = e->plan.gram_tiles[z];
+                if(tile.amp != (int)ai)
+                    continue;
+                for(int i = 0, q = 0; i < n; ++i)
+                    for(int j = i; j < n; ++j, ++q) {
+                        if(q < tile.p0 || q >= tile.p1)
+                            continue;
+                        const int l = q - tile.p0;
+                        double re = 0, im = 0;
+                        for(int b = 0; b < e->gram_blocks; ++b) {
+                            const double *g = e->h_gram + (((size_t)t * NTILE + z) * e->gram_blocks + b) * PM2;
+                            re += g[2 * l];
+                            im += g[2 * l + 1];
+                        }
+                        I[2 * (i * n + j)]     = re;
+                        I[2 * (i * n + j) + 1] = im;
+                        I[2 * (j * n + i)]     = re;
+                        I[2 * (j * n + i) + 1] = i == j ? im : -im;
+                    }
+            }
+            ty.amp_I[ai] = I;
+        }
+        ty.amp_params = snap[t];
+        ty.amp_valid  = true;
+    }
+    return GF_OK;
 }
 
 // Host completion of one toy's result o = [nll, status, grad...]: status bits of host-computed factors and
@@ -519,6 +730,8 @@ int gf_cuda_check(gf_engine *e, cudaError_t r, const char *what) {
 int gf_run(gf_engine *e, bool grad, int, int) {
     int rc = buildLayout(e);
     if(rc)
+        return rc;
+    if((rc = updateAmpCaches(e)))
         return rc;
     fillRecords(e);
     cudaError_t r;
@@ -704,7 +917,31 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
             ty.cols[o] = (char *)base + colBytes * o;
         for(int c = 0; c < NC; ++c)
             ty.kcols[c] = (int *)((char *)base + colBytes * NO + kBytes * c);
+        // Amp3Body: cached amplitudes (R2 per event and resonance) and, in mixed precision, FP64 copies of
+        // the Dalitz variables for the amplitude kernel
+        const int NA = T.n_amp_cols;
+        if(NA > 0) {
+            std::vector<int> dob;
+            for(auto &A : T.amp3s)
+                for(int o : {A.o12, A.o13})
+                    if(std::find(dob.begin(), dob.end(), o) == dob.end())
+                        dob.push_back(o);
+            const bool mixed = e->precision == GF_MIXED;
+            size_t aBytes    = (size_t)npad * 2 * rs;
+            size_t bytes     = aBytes * NA + (mixed ? (size_t)npad * 8 * dob.size() : 0) + 256;
+            r                = cudaMalloc(&ty.abase, bytes);
+            if(r != cudaSuccess) {
+                freeToy(ty);
+                return gf_cuda_check(e, r, "cudaMalloc amplitude cache");
+            }
+            for(int c = 0; c < NA; ++c)
+                ty.acols[c] = (char *)ty.abase + aBytes * c;
+            for(size_t k = 0; k < dob.size(); ++k)
+                ty.dcols[dob[k]] = mixed ? (double *)((char *)ty.abase + aBytes * NA + (size_t)npad * 8 * k)
+                                         : (double *)ty.cols[dob[k]];
+        }
     }
+    ty.amp_valid = false;
     const int64_t need = std::max<int64_t>(1, n) * NO;
     if(e->stage_cap < need) {
         dfree(e->d_stage);
@@ -756,6 +993,11 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
         gf_convert_events<float><<<blocks, 256, 0, e->stream>>>(a);
     else
         gf_convert_events<double><<<blocks, 256, 0, e->stream>>>(a);
+    if(e->precision == GF_MIXED && n > 0)
+        for(int o = 0; o < NO; ++o)
+            if(ty.dcols[o])
+                cudaMemcpyAsync(ty.dcols[o], stage + (size_t)o * n, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                e->stream);
     cudaMemcpyAsync(e->h_uperr, derr, sizeof(int), cudaMemcpyDeviceToHost, e->stream);
     r        = cudaStreamSynchronize(e->stream);
     int herr = *e->h_uperr;
@@ -881,6 +1123,8 @@ int gf_normalize(gf_engine *e, int toy, double *integral, double *norm) {
     const int NT = e->n_toys, NQ = (int)T.nums.size(), np = T.n_params;
     for(int t = 0; t < NT; ++t)
         e->h_active[t] = (t == toy);
+    if((rc = updateAmpCaches(e)))
+        return rc;
     fillRecords(e);
     GfArgs a = makeArgs(e);
     cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
@@ -901,7 +1145,8 @@ int gf_normalize(gf_engine *e, int toy, double *integral, double *norm) {
     std::vector<char> forced(n, 0);
     for(int i = 0; i < n; ++i) {
         const gf::TNode &nd = T.nodes[i];
-        bool f = forced[i] || (nd.op == GF_OP_CONVOLUTION) || (nd.op == GF_OP_PROD && T.nk[i] == gf::NK_NUMERIC);
+        bool f = forced[i] || (nd.op == GF_OP_CONVOLUTION) || (nd.op == GF_OP_AMP3BODY) ||
+                 (nd.op == GF_OP_PROD && T.nk[i] == gf::NK_NUMERIC);
         for(int c : nd.children)
             forced[c] = forced[c] || f;
     }
@@ -920,6 +1165,13 @@ int gf_normalize(gf_engine *e, int toy, double *integral, double *norm) {
             s *= std::sqrt(2.0) * std::sqrt(std::atan2(0.0, -1.0));
             I[i] = s;
             N[i] = 1.0 / s;
+            break;
+        }
+        case gf::NK_AMP3: {
+            gf::NormLayout::Analytic none;
+            none.node = i;
+            I[i]      = amp3Integral(e, toy, i, P, none, nullptr);
+            N[i]      = 1.0 / I[i];
             break;
         }
         case gf::NK_NUMERIC: {
@@ -986,9 +1238,11 @@ int gf_eval_events(gf_engine *e, int toy, int node, int metric, double *out, int
             return GF_ERR_OOM;
         e->vals_cap = ty.npad;
     }
-    const int NT = e->n_toys, np = e->tree.n_params;
+    const int NT = e->n_toys;
     for(int t = 0; t < NT; ++t)
         e->h_active[t] = (t == toy);
+    if((rc = updateAmpCaches(e)))
+        return rc;
     fillRecords(e);
     GfArgs a  = makeArgs(e);
     a.metric  = metric;
@@ -1027,6 +1281,8 @@ int gf_time_kernels(gf_engine *e, int toy, int with_grad, double *ms_conv, doubl
     const gf::Tree &T = e->tree;
     for(int t = 0; t < e->n_toys; ++t)
         e->h_active[t] = (t == toy);
+    if((rc = updateAmpCaches(e)))
+        return rc;
     fillRecords(e);
     GfArgs a = makeArgs(e);
     cudaError_t r = cudaMemsetAsync(e->d_qflag, 0, sizeof(int) * e->n_toys, e->stream);
@@ -1070,6 +1326,55 @@ int gf_launches_per_eval(const gf_engine *e, int) {
     if(!e || !e->has_tree)
         return 0;
     return 1 + (e->tree.convs.empty() ? 0 : 1) + (e->tree.nums.empty() ? 0 : 1);
+}
+
+static int ampNode(gf_engine *e, int toy, int node, int *ai) {
+    if(!e || !e->has_tree)
+        return gf_fail(e, GF_ERR_STATE, "no tree");
+    if(toy < 0 || toy >= e->n_toys || node < 0 || node >= (int)e->tree.nodes.size() || e->tree.amp3_of[node] < 0)
+        return gf_fail(e, GF_ERR_INVALID, "not an Amp3Body node, or toy index out of range");
+    cudaSetDevice(e->device);
+    int rc = buildLayout(e);
+    if(rc)
+        return rc;
+    for(int t = 0; t < e->n_toys; ++t)
+        e->h_active[t] = (t == toy);
+    *ai = e->tree.amp3_of[node];
+    return updateAmpCaches(e);
+}
+
+int gf_amp3_integrals(gf_engine *e, int toy, int node, double *out, int cap) {
+    int ai = -1, rc = ampNode(e, toy, node, &ai);
+    if(rc)
+        return rc;
+    const std::vector<double> &I = e->toys[toy].amp_I[ai];
+    if(!out || cap < (int)I.size())
+        return gf_fail(e, GF_ERR_INVALID, "output holds fewer than 2 n^2 values");
+    std::memcpy(out, I.data(), sizeof(double) * I.size());
+    return GF_OK;
+}
+
+int gf_amp3_cached_wave(gf_engine *e, int toy, int node, int res, double *out, int64_t n_out) {
+    int ai = -1, rc = ampNode(e, toy, node, &ai);
+    if(rc)
+        return rc;
+    const gf::Amp3Info &A = e->tree.amp3s[ai];
+    GfToy &ty             = e->toys[toy];
+    if(res < 0 || res >= A.nRes || !out || n_out < ty.n)
+        return gf_fail(e, GF_ERR_INVALID, "bad resonance index or output size");
+    const size_t rs = rsize(e);
+    std::vector<char> buf((size_t)std::max<int64_t>(1, ty.n) * 2 * rs);
+    cudaError_t r = cudaSuccess;
+    if(ty.n > 0)
+        r = cudaMemcpyAsync(buf.data(), ty.acols[A.col0 + res], (size_t)ty.n * 2 * rs, cudaMemcpyDeviceToHost, e->stream);
+    if(r == cudaSuccess)
+        r = cudaStreamSynchronize(e->stream);
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "reading the amplitude cache");
+    for(int64_t i = 0; i < 2 * ty.n; ++i)
+        out[i] = rs == 4 ? (double)reinterpret_cast<const float *>(buf.data())[i]
+                         : reinterpret_cast<const double *>(buf.data())[i];
+    return GF_OK;
 }
 
 int gf_generated_source(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,

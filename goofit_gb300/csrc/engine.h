@@ -30,6 +30,11 @@ struct GfArgs {
     const void *Pr;
     void *Nq;
     int *qflag;
+    const void *const *acol;
+    const double *const *dcol;
+    const unsigned *dgrid;
+    double *gram;
+    const int *dirty;
     int n_chunks;
     int n_toys;
     int metric;
@@ -41,13 +46,20 @@ struct GfToy {
     int64_t npad = 0;
     void *cols[16] = {nullptr};
     int *kcols[8]  = {nullptr};
+    void *abase    = nullptr;           // cached resonance amplitudes and FP64 Dalitz columns (one allocation)
+    void *acols[64] = {nullptr};        // R2 per event, one column per resonance of every Amp3Body
+    double *dcols[16] = {nullptr};      // FP64 event columns of the Dalitz variables
     bool loaded    = false;
+    bool amp_valid = false;             // the amplitude cache matches amp_params
+    std::vector<double> amp_params;     // parameter values the cache and integrals were built with
+    std::vector<std::vector<double>> amp_I; // per Amp3Body: n x n complex integrals, interleaved
 };
 
 struct GfModule {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t conv_g = nullptr, conv_n = nullptr, grid_g = nullptr, grid_n = nullptr;
     cudaKernel_t evt_g = nullptr, evt_n = nullptr, val_n = nullptr;
+    cudaKernel_t amp = nullptr, gram = nullptr;
 };
 
 struct gf_engine {
@@ -90,6 +102,13 @@ struct gf_engine {
     int64_t stage_cap = 0;
     int *d_uperr = nullptr;
     int *h_uperr = nullptr;
+    void **d_acols = nullptr;    // [toy][amplitude column]
+    double **d_dcols = nullptr;  // [toy][observable]
+    unsigned *d_dgrid = nullptr; // in-Dalitz bins of every Amp3Body
+    double *d_gram = nullptr;    // integral partials [toy][tile][CTA][2 * pairs]
+    double *h_gram = nullptr;
+    int *d_dirty = nullptr, *h_dirty = nullptr;
+    int gram_blocks = 0;
     void *d_Nq = nullptr;   // [toy][nq] R numeric normalisation factors
     int *d_qflag = nullptr; // [toy]
     // pinned host mirrors; h_P is one block: [toy][n_params] FP64, then [toy][npr] R records

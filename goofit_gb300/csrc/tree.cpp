@@ -7,6 +7,7 @@
 #include "tree.h"
 
 #include <algorithm>
+#include <cmath>
 #include <set>
 #include <sstream>
 
@@ -25,6 +26,21 @@ bool isExpOp(int op) {
 }
 
 } // namespace
+
+bool in_dalitz(double m12, double m13, double bigM, double dm1, double dm2, double dm3) {
+    const double dm1pdm2 = dm1 + dm2, bigMmdm3 = bigM - dm3, bigMmdm1 = bigM - dm1;
+    const double m23 = bigM * bigM + dm1 * dm1 + dm2 * dm2 + dm3 * dm3 - m12 - m13;
+    if(m23 < 0. || m23 > bigMmdm1 * bigMmdm1)
+        return false;
+    const bool m12lo = !(m12 < dm1pdm2 * dm1pdm2), m12hi = !(m12 > bigMmdm3 * bigMmdm3);
+    const double rt = std::sqrt(m12), dm11 = dm1 * dm1, dm22 = dm2 * dm2, dm33 = dm3 * dm3;
+    const double e1 = 0.5 * (m12 - dm22 + dm11) / rt;
+    const double e3 = 0.5 * (bigM * bigM - m12 - dm33) / rt;
+    const double p1 = std::sqrt(e1 * e1 - dm11), p3 = std::sqrt(e3 * e3 - dm33);
+    const double lo = (e1 + e3) * (e1 + e3) - (p1 + p3) * (p1 + p3);
+    const double hi = (e1 + e3) * (e1 + e3) - (p1 - p3) * (p1 - p3);
+    return m12lo && m12hi && !(m13 < lo) && !(m13 > hi);
+}
 
 std::vector<int> Tree::subtreeObs(int i) const {
     std::vector<int> r = nodes[i].obs;
@@ -121,8 +137,31 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
         case GF_OP_ADD_EXT: ok = C >= 1 && P == C; break;
         case GF_OP_PROD: ok = C >= 1; break;
         case GF_OP_CONVOLUTION: ok = C == 2 && n.consts.size() >= 3 && n.obs.size() >= 1 && n.consts[2] > 0; break;
-        case GF_OP_MULTIPOLYNOMIAL: ok = n.obs.size() >= 1 && n.consts.size() >= 1 && P >= n.obs.size() + 1 && C == 0; break;
-        case GF_OP_RES_RBW: ok = P == 2 && n.consts.size() >= 3 && C == 0; break;
+        case GF_OP_MULTIPOLYNOMIAL: {
+            ok = n.obs.size() >= 1 && n.obs.size() <= 8 && n.consts.size() >= 1 && n.consts[0] >= 0 &&
+                 n.consts[0] <= 16 && C == 0;
+            if(ok) {
+                // monomials of total degree <= maxDegree (device_MultiPolynomial's coefficient count)
+                const int deg = (int)n.consts[0] + 1;
+                int64_t boxes = 1, count = 0;
+                for(size_t k = 0; k < n.obs.size(); ++k)
+                    boxes *= deg;
+                ok = boxes <= (1 << 20);
+                for(int64_t b = 0; ok && b < boxes; ++b) {
+                    int64_t ci = b, sum = 0;
+                    for(size_t k = 0; k < n.obs.size(); ++k) {
+                        sum += ci % deg;
+                        ci /= deg;
+                    }
+                    count += sum < deg;
+                }
+                ok = ok && (int64_t)P >= (int64_t)n.obs.size() + count;
+            }
+            break;
+        }
+        case GF_OP_RES_RBW: ok = P == 2 && n.consts.size() >= 3 && C == 0 && n.consts[0] >= 0 && n.consts[0] <= 2 &&
+                                 n.consts[1] >= 0 && n.consts[1] <= 2; break;
+        case GF_OP_RES_NONRES: ok = P == 0 && C == 0; break;
         case GF_OP_AMP3BODY:
             ok = n.consts.size() >= 8 && n.obs.size() >= 2 && C >= 2 && P == 2 * (C - 1) && (int)n.consts[0] == (int)C - 1;
             break;
@@ -185,7 +224,7 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
         } else if(n.op == GF_OP_AMP3BODY) {
             nk[i]       = NK_AMP3;
             childForced = true;
-        } else if(n.op == GF_OP_RES_RBW) {
+        } else if(n.op == GF_OP_RES_RBW || n.op == GF_OP_RES_NONRES) {
             nk[i] = NK_ONE;
         } else if(isExpOp(n.op) && n.params.size() == 1) {
             nk[i] = NK_EXP;
@@ -226,8 +265,8 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
             // value gradient: coefficients (and an efficiency's free parameters); resonance parameters
             // enter through the cached amplitudes, whose derivatives the engine does not provide
             v = own;
-            for(int c : n.children)
-                if(nodes[c].op == GF_OP_RES_RBW && !dep_val[c].empty())
+            for(size_t r = 0; r + 1 < n.children.size(); ++r)
+                if(!dep_val[n.children[r]].empty())
                     return "Amp3Body: analytic gradients with respect to resonance parameters are not provided; "
                            "fix them or leave them out of the gradient mask";
             int eff = n.children.back();
@@ -310,8 +349,9 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
         a.nRes = (int)n.consts[0];
         for(int r = 0; r < a.nRes; ++r) {
             int rn = n.children[r];
-            if(nodes[rn].op != GF_OP_RES_RBW)
-                return "Amp3Body node " + std::to_string(i) + ": only relativistic Breit-Wigner resonances are supported";
+            if(nodes[rn].op != GF_OP_RES_RBW && nodes[rn].op != GF_OP_RES_NONRES)
+                return "Amp3Body node " + std::to_string(i) + ": resonance " + std::to_string(r) +
+                       " must be RBW or NonRes";
             a.res.push_back(rn);
         }
         a.eff = n.children[a.nRes];
@@ -333,6 +373,34 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
                 for(int p : nodes[j].params)
                     a.cache_params.push_back(p);
             }
+        if(nodes[a.eff].op == GF_OP_RES_RBW || nodes[a.eff].op == GF_OP_RES_NONRES)
+            return "Amp3Body node " + std::to_string(i) + ": the last child must be the efficiency";
+        for(int o : subtreeObs(a.eff))
+            if(o != a.o12 && o != a.o13 && o != 0)
+                return "Amp3Body node " + std::to_string(i) +
+                       ": the efficiency may depend on the two Dalitz variables only";
+        if(a.nb12 > 65535 || a.nb13 > 65535)
+            return "Amp3Body node " + std::to_string(i) + ": at most 65535 bins per Dalitz axis";
+        {
+            // normalisation bins inside the kinematic boundary; bin centres as
+            // src/PDFs/physics/detail/SpecialResonanceIntegrator.cu:61-78 computes them
+            const gf_observable &g12 = obs[a.o12], &g13 = obs[a.o13];
+            a.grid.clear();
+            for(int b13 = 0; b13 < a.nb13; ++b13) {
+                double c13 = g13.hi - g13.lo;
+                c13 /= a.nb13q;
+                c13 *= (b13 + 0.5);
+                c13 += g13.lo;
+                for(int b12 = 0; b12 < a.nb12; ++b12) {
+                    double c12 = g12.hi - g12.lo;
+                    c12 /= a.nb12;
+                    c12 *= (b12 + 0.5);
+                    c12 += g12.lo;
+                    if(in_dalitz(c12, c13, a.M, a.m1, a.m2, a.m3))
+                        a.grid.push_back((uint32_t)b12 | ((uint32_t)b13 << 16));
+                }
+            }
+        }
         std::sort(a.cache_params.begin(), a.cache_params.end());
         a.cache_params.erase(std::unique(a.cache_params.begin(), a.cache_params.end()), a.cache_params.end());
         a.col0 = n_amp_cols;

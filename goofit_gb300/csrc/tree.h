@@ -52,7 +52,11 @@ struct Amp3Info {
     int nb12 = 0, nb13 = 0, nb13q = 0;
     double area = 0;          // bin size of m12 times bin size of m13
     std::vector<int> cache_params; // parameters the cached amplitudes and integrals depend on
+    std::vector<uint32_t> grid;    // in-Dalitz normalisation bins, b12 | b13 << 16 (FP64 inDalitz)
 };
+
+// inDalitz (src/PDFs/physics/DalitzPlotHelpers.cu:14-59), FP64 without contraction.
+bool in_dalitz(double m12, double m13, double bigM, double dm1, double dm2, double dm3);
 
 // One numerically normalised node: grid over its observables.
 struct NumInfo {
@@ -144,6 +148,13 @@ struct KernelPlan {
     std::vector<int64_t> ctab_off_grad, ctab_off_nograd;    // per conv
     std::vector<int> ctab_cp_grad, ctab_cp_nograd;          // per conv: padded components per table row
     std::vector<int> obs_used_evt;                          // observables the event kernel loads
+    // Amp3Body integrals: pairs (i <= j) of each node split into tiles; one CTA row per tile
+    struct GramTile {
+        int amp, p0, p1; // node index in Tree::amp3s, pair range
+    };
+    std::vector<GramTile> gram_tiles;
+    int gram_pairs_max = 0;                                 // most pairs in one tile
+    std::vector<int64_t> dgrid_off;                         // per Amp3Body: offset of its bins in the bin list
     NormLayout nl;
 };
 

@@ -70,9 +70,11 @@ enum gf_op {
                                      children [resonance 0 .. n-1, efficiency] */
     GF_OP_AMP4BODY          = 13, /* device_DP             src/PDFs/physics/Amp4Body.cu:53-90 */
     GF_OP_MULTIPOLYNOMIAL   = 14, /* device_MultiPolynomial src/PDFs/basic/PolynomialPdf.cu:46-107
-                                     consts [maxDegree, maxDegree+1+i ...] params [offsets (nObs), coefficients] */
-    GF_OP_RES_RBW           = 20  /* plainBW<1|2>          src/PDFs/physics/resonances/RBW.cu:9-86
+                                     consts [maxDegree] params [offsets (one per observable), coefficients] */
+    GF_OP_RES_RBW           = 20, /* plainBW<1|2>          src/PDFs/physics/resonances/RBW.cu:9-86
                                      params [mass, width] consts [spin, cyclic index, norm, symmetric] */
+    GF_OP_RES_NONRES        = 21  /* nonres                src/PDFs/physics/resonances/NonRes.cu:8-11
+                                     amplitude 1 + 0i; no parameters */
 };
 
 /* node flags */
@@ -253,6 +255,16 @@ int gf_fit_batch(gf_engine *eng, int n_toys, const gf_fit_options *opt, const do
 int gf_nll_exp_noalloc(const float *x, int64_t n_events, double alpha, double lo, double hi, double *out,
                        void *stream);
 const char *gf_noalloc_last_error(void);
+
+/* Amp3Body normalisation integrals I_ij = sum over in-Dalitz bins of B_i conj(B_j) eff (before the bin size
+   factor), n x n complex interleaved [re, im] row-major, at the toy's current parameters: the integrals
+   Amp3Body::normalize caches (src/PDFs/physics/Amp3Body.cu:304-330; its fit_fractions() reads them).
+   `node` is the Amp3Body's index in the tree; `cap` counts doubles (>= 2 n^2). */
+int gf_amp3_integrals(gf_engine *eng, int toy, int node, double *out, int cap);
+
+/* Cached amplitude B_res of every event of the toy, complex interleaved (2 n doubles; FP32 values widened in
+   GF_MIXED): Amp3Body::getCachedWave (include/goofit/PDFs/physics/Amp3Body.h:61). */
+int gf_amp3_cached_wave(gf_engine *eng, int toy, int node, int res, double *out, int64_t n_out);
 
 /* ---- diagnostics: code generation without a device ---- */
 /* Generated CUDA source for a tree (precision as in gf_engine_create); *len gets the full length. */
