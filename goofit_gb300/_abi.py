@@ -42,6 +42,9 @@ GF_OP_PROD = 10
 GF_OP_CONVOLUTION = 11
 GF_OP_AMP3BODY = 12
 GF_OP_AMP4BODY = 13
+GF_OP_MULTIPOLYNOMIAL = 14
+GF_OP_RES_RBW = 20
+GF_OP_RES_NONRES = 21
 
 GF_FLAG_COMMON_NORM = 1
 GF_FLAG_SEPARATE_NORM = 2
@@ -129,6 +132,8 @@ SIGNATURES = [
     ("gf_grad_params", C.c_int, [_vp, _i32p, C.c_int]),
     ("gf_normalize", C.c_int, [_vp, C.c_int, _f64p, _f64p]),
     ("gf_eval_events", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _f64p, C.c_int64]),
+    ("gf_amp3_integrals", C.c_int, [_vp, C.c_int, C.c_int, _f64p, C.c_int]),
+    ("gf_amp3_cached_wave", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _f64p, C.c_int64]),
     ("gf_last_timing", C.c_int, [_vp, _f64p, _f64p]),
     ("gf_launches_per_eval", C.c_int, [_vp, C.c_int]),
     ("gf_time_kernels", C.c_int, [_vp, C.c_int, C.c_int, _f64p, _f64p, _f64p]),
