@@ -1,18 +1,22 @@
 """GB300-native GooFit fit path.
 
 The GooFit host API (Observable, Variable, UnbinnedDataSet, ExpPdf,
-GaussianPdf, PolynomialPdf, AddPdf, ProdPdf, ConvolutionPdf, FitManager)
+GaussianPdf, PolynomialPdf, AddPdf, ProdPdf, ConvolutionPdf, Amp3Body with RBW/NonRes
+resonances, FitManager)
 over libgfengine.so: per-tree generated sm_103a kernels behind a C ABI
 (include/gfengine.h).
 """
-from .api import (AddPdf, CombinePdf, ConvolutionPdf, DataSet, EvalFunc, EventNumber, ExpPdf, FitManager,
-                  FitManagerMinuit2, GaussianPdf, GeneralError, GooPdf, Observable, OutOfRange, PdfBase,
-                  PolynomialPdf, ProdPdf, UnbinnedDataSet, Variable, get_precision, set_precision)
+from .api import (PAIR_12, PAIR_13, PAIR_23, RBW, AddPdf, Amp3Body, CombinePdf, ConvolutionPdf, DataSet,
+                  DaughterPair, DecayInfo3, EvalFunc, EventNumber, ExpPdf, FitManager, FitManagerMinuit2,
+                  GaussianPdf, GeneralError, GooPdf, MultiPolynomialPdf, NonRes, Observable, OutOfRange, PdfBase,
+                  PolynomialPdf, ProdPdf, ResonancePdf, Resonances, UnbinnedDataSet, Variable, get_precision,
+                  set_precision)
 from .engine import Engine, FitResult, Minimizer
 
 __all__ = [
     "AddPdf", "CombinePdf", "ConvolutionPdf", "DataSet", "EvalFunc", "EventNumber", "ExpPdf", "FitManager",
     "FitManagerMinuit2", "GaussianPdf", "GeneralError", "GooPdf", "Observable", "OutOfRange", "PdfBase",
     "PolynomialPdf", "ProdPdf", "UnbinnedDataSet", "Variable", "Engine", "FitResult", "Minimizer",
-    "get_precision", "set_precision",
+    "get_precision", "set_precision", "Amp3Body", "DecayInfo3", "DaughterPair", "PAIR_12", "PAIR_13", "PAIR_23",
+    "ResonancePdf", "Resonances", "RBW", "NonRes", "MultiPolynomialPdf",
 ]

@@ -482,7 +482,8 @@ class PdfBase:
         """Engine with this PDF as root and `data` uploaded; cached per (precision, data)."""
         precision = precision or _DEFAULT_PRECISION
         nodes, params, obs = self._flatten()
-        mask = [0 if v.fixed else 1 for v in params]
+        nd = self._nondiff_all()
+        mask = [0 if (v.fixed or id(v) in nd) else 1 for v in params]
         olist = [(o.lowerlimit, o.upperlimit, o.numbins, 1 if o.is_event_number else 0) for o in obs]
         key = repr((nodes, olist, mask))
         ent = self._engines.get(precision)
@@ -497,6 +498,16 @@ class PdfBase:
             eng.upload(cols)
             ent["data"], ent["version"] = data, getattr(data, "version", 0)
         return eng, params
+
+    def _nondiff_params(self) -> set:
+        """ids of parameters the engine provides no analytic derivative for (below this node)."""
+        return set()
+
+    def _nondiff_all(self) -> set:
+        ids = set(self._nondiff_params())
+        for c in self.components:
+            ids |= c._nondiff_all()
+        return ids
 
     @staticmethod
     def _param_values(params: Sequence[Variable]) -> np.ndarray:
@@ -674,6 +685,11 @@ class GaussianPdf(GooPdf):
 class PolynomialPdf(GooPdf):
     """include/goofit/PDFs/basic/PolynomialPdf.h (one-observable forms)."""
 
+    def __new__(cls, name: str, x, *args, **kw):
+        if cls is PolynomialPdf and isinstance(x, (list, tuple)):
+            return MultiPolynomialPdf(name, x, *args, **kw)
+        return super().__new__(cls)
+
     def __init__(self, name: str, x: Observable, weights: Sequence[Variable], *args):
         super().__init__("PolynomialPdf", name, x)
         x0 = None
@@ -746,6 +762,195 @@ class ConvolutionPdf(CombinePdf):
         self.constantsList[0:3] = [float(lo), float(hi), float(step)]
 
 
+class MultiPolynomialPdf(GooPdf):
+    """Multivariate form of PolynomialPdf (src/PDFs/basic/PolynomialPdf.cu:154-207): offsets, then the
+    C(maxDegree + n, n) coefficients of the monomials of total degree <= maxDegree; missing coefficients
+    and offsets are padded with constants at zero, as the reference does."""
+    op = A.GF_OP_MULTIPOLYNOMIAL
+
+    def __init__(self, name: str, obses: Sequence[Observable], coeffs: Sequence[Variable],
+                 offsets: Sequence[Variable] = (), maxDegree: int = 1):
+        super().__init__("PolynomialPdf", name)
+        self.registerConstant(maxDegree)
+        npar = 1
+        for i, o in enumerate(obses):
+            self.registerObservable(o)
+            npar *= maxDegree + 1 + i
+            self.registerConstant(maxDegree + 1 + i)
+        for i in range(len(self.observablesList), 1, -1):
+            npar //= i
+        coeffs, offsets = list(coeffs), list(offsets)
+        while npar > len(coeffs):
+            coeffs.append(Variable(f"{name}_extra_coeff_{len(coeffs)}", 0))
+        while len(offsets) < len(obses):
+            offsets.append(Variable(f"{name}_extra_offset_{len(offsets)}", 0))
+        for v in offsets:
+            self.registerParameter(v)
+        for v in coeffs:
+            self.registerParameter(v)
+
+
+# ---------------------------------------------------------------- Dalitz plots
+class DaughterPair(enum.IntEnum):
+    """include/goofit/PDFs/physics/DalitzPlotHelpers.h: the resonance's daughter pair (cyclic index)."""
+    PAIR_12 = 0
+    PAIR_13 = 1
+    PAIR_23 = 2
+
+
+PAIR_12, PAIR_13, PAIR_23 = DaughterPair.PAIR_12, DaughterPair.PAIR_13, DaughterPair.PAIR_23
+
+
+class DecayInfo3:
+    """include/goofit/PDFs/physics/DalitzPlotHelpers.h:88-97.  mother_meson_radius defaults to 0 (the
+    reference leaves it uninitialised)."""
+
+    def __init__(self):
+        self.motherMass = 0.0
+        self.daug1Mass = 0.0
+        self.daug2Mass = 0.0
+        self.daug3Mass = 0.0
+        self.meson_radius = 0.0
+        self.mother_meson_radius = 0.0
+        self.resonances: list[ResonancePdf] = []
+
+    def add_resonance(self, r: "ResonancePdf") -> None:
+        self.resonances.append(r)
+
+
+class ResonancePdf(GooPdf):
+    """include/goofit/PDFs/physics/resonances/Resonance.h: a resonance carries its complex coefficient
+    (registered on the Amp3Body) and its own line-shape parameters."""
+
+    def __init__(self, pdf_name: str, name: str, ar: Variable, ai: Variable):
+        super().__init__(pdf_name, name)
+        self.amp_real, self.amp_imag = ar, ai
+
+    def setParameterConstantness(self, constant: bool = True) -> None:
+        for v in self.parametersList:
+            v.setFixed(constant)
+
+
+class RBW(ResonancePdf):
+    """Resonances::RBW (src/PDFs/physics/resonances/RBW.cu:93-114)."""
+    op = A.GF_OP_RES_RBW
+
+    def __init__(self, name: str, ar: Variable, ai: Variable, mass: Variable, width: Variable, sp: int, cyc: int,
+                 norm: bool = True, sym: bool = False):
+        super().__init__("RBW", name, ar, ai)
+        self.registerParameter(mass)
+        self.registerParameter(width)
+        self.registerConstant(int(sp))
+        self.registerConstant(int(cyc))
+        self.registerConstant(1 if norm else 0)
+        self.registerConstant(1 if sym else 0)
+
+
+class NonRes(ResonancePdf):
+    """Resonances::NonRes (src/PDFs/physics/resonances/NonRes.cu:8-20): constant amplitude 1."""
+    op = A.GF_OP_RES_NONRES
+
+    def __init__(self, name: str, ar: Variable, ai: Variable):
+        super().__init__("NonRes", name, ar, ai)
+
+
+class Resonances:
+    """Namespace of the resonance shapes (GooFit::Resonances)."""
+    RBW = RBW
+    NonRes = NonRes
+
+
+class Amp3Body(GooPdf):
+    """include/goofit/PDFs/physics/Amp3Body.h, src/PDFs/physics/Amp3Body.cu:127-196: coherent sum of
+    resonances times an efficiency, normalised over the m12 x m13 bin grid of the two observables.
+
+    Without an efficiency a constant one (degree-0 MultiPolynomialPdf at 1) is used."""
+    op = A.GF_OP_AMP3BODY
+    cacheCount = 0
+
+    def __init__(self, name: str, m12: Observable, m13: Observable, eventNumber: EventNumber, decay: DecayInfo3,
+                 eff: GooPdf | None = None):
+        super().__init__("Amp3Body", name, m12, m13, eventNumber)
+        self.decayInfo = decay
+        self._m12, self._m13, self._eventNumber = m12, m13, eventNumber
+        if eff is None:
+            eff = MultiPolynomialPdf(f"{name}_constantEff", [m12, m13], [Variable(f"{name}_constantOne", 1)],
+                                     [Variable(f"{name}_zero0", 0), Variable(f"{name}_zero1", 0)], 0)
+        self.efficiency = eff
+        self.registerConstant(len(decay.resonances))
+        self.cacheToUse = Amp3Body.cacheCount
+        Amp3Body.cacheCount += 1
+        self.registerConstant(self.cacheToUse)
+        for c in (decay.motherMass, decay.daug1Mass, decay.daug2Mass, decay.daug3Mass, decay.meson_radius,
+                  decay.mother_meson_radius):
+            self.registerConstant(c)
+        for r in decay.resonances:
+            self.registerParameter(r.amp_real)
+            self.registerParameter(r.amp_imag)
+            self.components.append(r)
+        self.components.append(eff)
+        self.setSeparateNorm()
+
+    @staticmethod
+    def resetCacheCounter() -> None:
+        Amp3Body.cacheCount = 0
+
+    def getDecayInfo(self) -> DecayInfo3:
+        return self.decayInfo
+
+    def setDataSize(self, dataSize: int, evtSize: int = 3, offset: int = 0) -> None:
+        """The amplitude cache is sized by the uploaded data; kept for interface compatibility."""
+        if evtSize < 3:
+            raise GeneralError(f"totalEventSize {evtSize} must be 3 or more")
+
+    def setForceIntegrals(self, f: bool = True) -> None:
+        """Integrals are rebuilt whenever a resonance or efficiency parameter changes."""
+
+    def _nondiff_params(self) -> set:
+        ids = set()
+        for c in self.components:
+            ids |= {id(v) for v in c.getParameters()}
+        return ids
+
+    def _node_index(self) -> int:
+        return 0
+
+    def _root_engine(self):
+        if self.data is None:
+            raise GeneralError("no data set")
+        eng, params = self._engine_for(self.data)
+        eng.set_params(self._param_values(params))
+        return eng
+
+    def getCachedWave(self, i: int) -> np.ndarray:
+        """Amplitude of resonance i at every data event (Amp3Body::getCachedWave)."""
+        return self._root_engine().amp3_cached_wave(self._node_index(), i)
+
+    def sumCachedWave(self, i: int) -> complex:
+        return complex(self.getCachedWave(i).sum())
+
+    def integrals(self) -> np.ndarray:
+        """The n x n normalisation integrals I_ij the engine caches (before the bin size factor)."""
+        return self._root_engine().amp3_integrals(self._node_index(), len(self.decayInfo.resonances))
+
+    def fit_fractions(self) -> list[list[float]]:
+        """Amp3Body::fit_fractions (src/PDFs/physics/Amp3Body.cu:376-427): from the data-event caches."""
+        n = len(self.decayInfo.resonances)
+        eng = self._root_engine()
+        waves = [eng.amp3_cached_wave(self._node_index(), i) for i in range(n)]
+        coefs = [complex(r.amp_real.value, r.amp_imag.value) for r in self.decayInfo.resonances]
+        ne = len(waves[0])
+        amps = [[0.0] * n for _ in range(n)]
+        total = 0.0
+        for i in range(n):
+            for j in range(n):
+                b = float(np.sum((coefs[i] * np.conj(coefs[j]) * waves[i] * np.conj(waves[j])).real))
+                total += b
+                amps[i][j] = b / ne
+        total /= ne
+        return [[amps[i][j] / total for j in range(n)] for i in range(n)]
+
+
 # ---------------------------------------------------------------- fitting
 class FitManager:
     """FitManagerMinuit2 surface (include/goofit/fitting/FitManagerMinuit2.h) on the project MIGRAD.
@@ -801,9 +1006,12 @@ class FitManager:
         limited = np.array([0 if (v.fixed or v.lowerlimit == v.upperlimit) else 1 for v in params], dtype=np.int32)
         for i, v in enumerate(params):
             v.fitter_index = i
+        nd = pdf._nondiff_all()
+        use_grad = self.gradient == "analytic" and not any(id(v) in nd for v in params if not v.fixed)
+        self.used_gradient = "analytic" if use_grad else "numerical"
         t0 = time.perf_counter()
         res = eng.fit(x0, err, lo, hi, limited, fixed, tolerance=self.tolerance, strategy=self.strategy,
-                      maxfcn=self.max_calls, use_grad=(self.gradient == "analytic"))
+                      maxfcn=self.max_calls, use_grad=use_grad)
         self.wall_seconds = time.perf_counter() - t0
         for i, v in enumerate(params):
             v.value = res.values[i] + blind[i]

@@ -61,10 +61,14 @@ def _compile(src: str) -> Path:
         return obj
     inc = [f"-I{INCLUDE}", f"-I{CSRC}", f"-I{CUDA_HOME / 'include'}"]
     if src.endswith(".cu"):
-        cmd = [NVCC, *GENCODE, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-c", str(s), "-o", str(obj), *inc]
+        cmd = [NVCC, *GENCODE, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-c", str(s),
+               "-o", str(obj), *inc]
     else:
         std = "-std=c++20" if src in CXX20_SOURCES else "-std=c++17"
-        cmd = ["g++", std, "-O2", "-fPIC", "-Wall", "-Wno-unused-variable", "-c", str(s), "-o", str(obj), *inc]
+        # no floating-point contraction: host arithmetic (analytic norms, bin centres, the kinematic boundary)
+        # rounds like the FP64 restatement it is checked against, on x86-64 and on aarch64 alike
+        cmd = ["g++", std, "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-variable", "-c", str(s), "-o",
+               str(obj), *inc]
     _run(cmd)
     return obj
 

@@ -323,6 +323,25 @@ Val emit(Ctx &c, int i) {
         const int nO = (int)n.obs.size(), deg = (int)n.consts[0] + 1;
         std::vector<std::string> d(nO);
         for(int j = 0; j < nO; ++j) {
+            // x_j is read only when some monomial has a positive power of it
+            bool used   = false;
+            int64_t bx  = 1;
+            for(int k = 0; k < nO; ++k)
+                bx *= deg;
+            for(int64_t b = 1; b < bx && !used; ++b) {
+                int64_t ci = b;
+                int sum = 0, pj = 0;
+                for(int k = 0; k < nO; ++k) {
+                    const int pk = (int)(ci % deg);
+                    ci /= deg;
+                    sum += pk;
+                    if(k == j)
+                        pj = pk;
+                }
+                used = sum < deg && pj > 0;
+            }
+            if(!used)
+                continue;
             d[j] = c.tmp("d");
             os << "    const R " << d[j] << " = " << c.x(n.obs[j]) << " - " << P(n.params[j]) << ";\n";
         }
@@ -1068,7 +1087,7 @@ struct Gen {
         os << "  if(!a.dirty[toy]) return;\n";
         os << "  const i64 n = a.toy_nevents[toy], npad = n < 8 ? 8 : (n + 7) / 8 * 8;\n";
         os << "  const double *P = a.P + (i64)toy * " << np << "; (void)P;\n";
-        os << "  R2 *const *ac = reinterpret_cast<R2 *const *>(a.acol) + (i64)toy * " << NA << ";\n";
+        os << "  R2 *const *ac = reinterpret_cast<R2 *const *>(const_cast<void **>(a.acol)) + (i64)toy * " << NA << ";\n";
         os << "  switch(k) {\n";
         for(size_t ai = 0; ai < T.amp3s.size(); ++ai) {
             const Amp3Info &A = T.amp3s[ai];

@@ -494,6 +494,11 @@ double amp3Integral(const gf_engine *e, int t, int node, const double *P, const 
     const gf::Tree &T     = e->tree;
     const gf::TNode &nd   = T.nodes[node];
     const int n           = T.amp3s[T.amp3_of[node]].nRes;
+    if((int)e->toys[t].amp_I.size() <= T.amp3_of[node]) { // integrals not built yet for this toy
+        for(size_t k = 0; k < an.dN.size() && k < 64; ++k)
+            dQ[k] = 0;
+        return NAN;
+    }
     const std::vector<double> &I = e->toys[t].amp_I[T.amp3_of[node]];
     auto Iij = [&](int i, int j) { return C(I[2 * (i * n + j)], I[2 * (i * n + j) + 1]); };
     C sum(0, 0);

@@ -190,6 +190,19 @@ class Engine:
         self._check(self._L.gf_eval_events(self._h, toy, 0, metric, out.ctypes.data_as(A._f64p), n))
         return out[:n]
 
+    def amp3_integrals(self, node: int, n_res: int, toy: int = 0) -> np.ndarray:
+        """Amp3Body normalisation integrals I_ij (n x n complex) at the toy's current parameters."""
+        out = np.zeros(2 * n_res * n_res)
+        self._check(self._L.gf_amp3_integrals(self._h, toy, node, out.ctypes.data_as(A._f64p), len(out)))
+        return (out[0::2] + 1j * out[1::2]).reshape(n_res, n_res)
+
+    def amp3_cached_wave(self, node: int, res: int, toy: int = 0) -> np.ndarray:
+        """Cached amplitude of resonance `res` for every event of the toy (complex128)."""
+        n = self._n_events.get(toy, 0)
+        out = np.zeros(max(2, 2 * n))
+        self._check(self._L.gf_amp3_cached_wave(self._h, toy, node, res, out.ctypes.data_as(A._f64p), n))
+        return out[0:2 * n:2] + 1j * out[1:2 * n:2]
+
     def last_timing(self) -> tuple[float, float]:
         a, b = C.c_double(), C.c_double()
         self._L.gf_last_timing(self._h, C.byref(a), C.byref(b))

@@ -10,6 +10,10 @@ C2  AddPdf(f_sig; ConvolutionPdf(ExpPdf(alpha), GaussianPdf(mu, sigma)), Polynom
     integration constants are (0, 10, 0.01): the exponential is a decay starting at t = 0, smeared by
     the resolution.  (With the default (-10, 10) range the exponential is not truncated inside the
     observable range, so mu and sigma would only rescale the normalisation and be unidentifiable.)
+C3  Amp3Body for D0 -> pi0 pi+ pi- with 8 relativistic Breit-Wigners (rho(770)+-0, rho(1450)+-0, f0(980),
+    f2(1270)); m12 = m^2(pi0 pi+), m13 = m^2(pi0 pi-) on [0, 3] GeV^2 with 1500 x 1500 normalisation bins;
+    constant efficiency; 14 floated amplitude components (the rho+ coefficient is the fixed reference);
+    5e5 events by accept-reject on the model density evaluated by the FP64 engine (needs a GPU).
 """
 from __future__ import annotations
 
@@ -146,3 +150,90 @@ def make_c4(n_toys: int = 1024, mean_events: float = 20_000, lo: int = 5_000, hi
         datas.append(c2_data(int(counts[t]), seed=10_000 + seed * 100_000 + t, alpha=tr["alpha"], mu=tr["mu"],
                              sigma=tr["sigma"], fsig=tr["fsig"]).reshape(1, -1))
     return ToyStudy("c4-toys", base.pdf, base.variables, truths, datas, dict(base.start))
+
+
+# D0 -> pi0 pi+ pi- masses (GeV) and the resonance set of the C3 configuration
+C3_MD0, C3_MPIC, C3_MPI0 = 1.86484, 0.13957018, 0.1349766
+C3_RESONANCES = [
+    # name, mass, width, spin, pair, (Re, Im) coefficient, coefficient floated
+    ("rhop", 0.7758, 0.1503, 1, G.PAIR_12, (1.0, 0.0), False),
+    ("rhom", 0.7758, 0.1503, 1, G.PAIR_13, (0.714, -0.025), True),
+    ("rho0", 0.7758, 0.1503, 1, G.PAIR_23, (0.565, 0.164), True),
+    ("rhop_1450", 1.465, 0.400, 1, G.PAIR_12, (-0.174, -0.117), True),
+    ("rho0_1450", 1.465, 0.400, 1, G.PAIR_23, (0.325, 0.057), True),
+    ("rhom_1450", 1.465, 0.400, 1, G.PAIR_13, (0.788, 0.226), True),
+    ("f0_980", 0.980, 0.044, 0, G.PAIR_23, (0.008 * -C3_MD0 ** 2, -0.013 * -C3_MD0 ** 2), True),
+    ("f2_1270", 1.2754, 0.1851, 2, G.PAIR_23, (-1.027 * -1 / C3_MD0 ** 2, -0.162 * -1 / C3_MD0 ** 2), True),
+]
+
+
+def c3_model(bins: int = 1500, n_res: int = 8):
+    """The C3 Amp3Body tree (no data attached); returns (pdf, variables, observables)."""
+    m12 = G.Observable("m12", 0.0, 3.0)
+    m13 = G.Observable("m13", 0.0, 3.0)
+    m12.setNumBins(bins)
+    m13.setNumBins(bins)
+    evt = G.EventNumber("eventNumber")
+    d = G.DecayInfo3()
+    d.motherMass, d.daug1Mass, d.daug2Mass, d.daug3Mass = C3_MD0, C3_MPI0, C3_MPIC, C3_MPIC
+    d.meson_radius, d.mother_meson_radius = 1.5, 5.0
+    variables = {}
+    for name, mass, width, spin, pair, (re, im), free in C3_RESONANCES[:n_res]:
+        if free:
+            ar = G.Variable(f"{name}_amp_real", re, 0.001, 0, 0)
+            ai = G.Variable(f"{name}_amp_imag", im, 0.001, 0, 0)
+            variables[ar.name], variables[ai.name] = ar, ai
+        else:
+            ar, ai = G.Variable(f"{name}_amp_real", re), G.Variable(f"{name}_amp_imag", im)
+        m = G.Variable(f"{name}_mass", mass)
+        w = G.Variable(f"{name}_width", width)
+        d.add_resonance(G.RBW(name, ar, ai, m, w, spin, int(pair)))
+    eff = G.PolynomialPdf("constantEff", [m12, m13], [G.Variable("constantOne", 1)],
+                          [G.Variable("constantZero0", 0), G.Variable("constantZero1", 0)], 0)
+    pdf = G.Amp3Body("signalPDF", m12, m13, evt, d, eff)
+    return pdf, variables, [m12, m13, evt]
+
+
+def c3_generate(pdf, n: int, seed: int, batch: int = 4_000_000) -> np.ndarray:
+    """Accept-reject sample of the Amp3Body density: uniform candidates in the (m12, m13) box, weights from
+    the FP64 engine's per-event values.  Returns a (3, n) array [m12, m13, eventNumber]."""
+    from .engine import Engine
+    from . import _abi as A
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nodes, params, obs = pdf._flatten()
+    eng = Engine("fp64")
+    eng.set_tree(nodes, [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs],
+                 len(params), [0] * len(params))
+    pv = np.array([v.value for v in params])
+    lo, hi = obs[0].lowerlimit, obs[0].upperlimit
+    out12, out13, vmax, have = [], [], None, 0
+    while have < n:
+        c = np.empty((3, batch))
+        c[0] = rng.uniform(lo, hi, batch)
+        c[1] = rng.uniform(obs[1].lowerlimit, obs[1].upperlimit, batch)
+        c[2] = np.arange(batch, dtype=np.float64)
+        eng.upload(c)
+        eng.set_params(pv)
+        v = eng.eval_events(A.GF_METRIC_EVAL)
+        if vmax is None:
+            vmax = 1.2 * float(v.max())
+        vmax = max(vmax, float(v.max()))
+        keep = rng.random(batch) * vmax < v
+        out12.append(c[0][keep])
+        out13.append(c[1][keep])
+        have += int(keep.sum())
+    m12 = np.concatenate(out12)[:n]
+    m13 = np.concatenate(out13)[:n]
+    return np.vstack([m12, m13, np.arange(n, dtype=np.float64)])
+
+
+def make_c3(n: int = 500_000, seed: int = 3, bins: int = 1500, n_res: int = 8, data: np.ndarray | None = None) -> Workload:
+    pdf, variables, obs = c3_model(bins, n_res)
+    truth = {k: v.value for k, v in variables.items()}
+    cols = data if data is not None else c3_generate(pdf, n, seed)
+    ds = G.UnbinnedDataSet(obs)
+    ds.from_numpy(cols)
+    pdf.setData(ds)
+    # start 5% away from the truth
+    start = {k: v * 1.05 for k, v in truth.items()}
+    return Workload(f"c3-amp3body-{n}", pdf, ds, truth, start, variables, obs)

@@ -606,6 +606,8 @@ struct Oracle {
 
     cplx resonance(int r, double m12, double m13, double m23, const Decay3 &d) const {
         const Node &rn = nodes[r];
+        if(rn.op == GF_OP_RES_NONRES) // nonres, src/PDFs/physics/resonances/NonRes.cu:8-11
+            return cplx(1.0, 0.0);
         if(rn.op != GF_OP_RES_RBW)
             throw std::runtime_error("oracle: unsupported resonance op");
         int I = (rn.consts.size() > 3 && rn.consts[3] != 0) ? 2 : 1;

@@ -40,6 +40,14 @@ def lib() -> C.CDLL:
         L.oracle_last_error.restype = C.c_char_p
         L.oracle_mt19937_exponential.argtypes = [C.c_uint32, C.c_double, C.c_int64, f64p]
         L.oracle_num_threads.restype = C.c_int
+        L.oracle_amp3_integrals.argtypes = [C.POINTER(A.gf_node), C.c_int, C.POINTER(A.gf_observable), C.c_int,
+                                            f64p, C.c_int, C.c_int, f64p]
+        L.oracle_amp3_integrals.restype = C.c_int
+        L.oracle_amp3_resonance.argtypes = [C.POINTER(A.gf_node), C.c_int, C.POINTER(A.gf_observable), C.c_int,
+                                            f64p, C.c_int, C.c_int, C.c_int, f64p, f64p, C.c_int64, f64p]
+        L.oracle_amp3_resonance.restype = C.c_int
+        L.oracle_in_dalitz.argtypes = [C.c_double] * 6
+        L.oracle_in_dalitz.restype = C.c_int
         _lib = L
     return _lib
 
@@ -108,3 +116,32 @@ def mt19937_exponential(seed: int, lam: float, n: int) -> np.ndarray:
 
 def num_threads() -> int:
     return lib().oracle_num_threads()
+
+
+def amp3_integrals(nodes, observables, params, node: int, n_res: int) -> np.ndarray:
+    """Amp3Body integrals I_ij (n x n complex, before the bin size factor) of `node`."""
+    nl, obs, p, pp, _ = _prep(nodes, observables, params, np.zeros((len(observables), 1)))
+    out = np.zeros(2 * n_res * n_res)
+    rc = lib().oracle_amp3_integrals(nl.arr, nl.n, obs, len(observables), pp, len(p), node,
+                                     out.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc:
+        raise OracleError(lib().oracle_last_error().decode())
+    return (out[0::2] + 1j * out[1::2]).reshape(n_res, n_res)
+
+
+def amp3_resonance(nodes, observables, params, node: int, res: int, m12, m13) -> np.ndarray:
+    """Amplitude of resonance node `res` of Amp3Body `node` at the given points (zero outside the plot)."""
+    nl, obs, p, pp, _ = _prep(nodes, observables, params, np.zeros((len(observables), 1)))
+    a = np.ascontiguousarray(m12, dtype=np.float64)
+    b = np.ascontiguousarray(m13, dtype=np.float64)
+    out = np.zeros(2 * len(a))
+    f64p = C.POINTER(C.c_double)
+    rc = lib().oracle_amp3_resonance(nl.arr, nl.n, obs, len(observables), pp, len(p), node, res,
+                                     a.ctypes.data_as(f64p), b.ctypes.data_as(f64p), len(a), out.ctypes.data_as(f64p))
+    if rc:
+        raise OracleError(lib().oracle_last_error().decode())
+    return out[0::2] + 1j * out[1::2]
+
+
+def in_dalitz(m12: float, m13: float, M: float, d1: float, d2: float, d3: float) -> bool:
+    return bool(lib().oracle_in_dalitz(m12, m13, M, d1, d2, d3))

@@ -38,15 +38,19 @@ def test_version_string():
 def _tree(pdf):
     nodes, params, obs = pdf._flatten()
     olist = [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs]
-    mask = [0 if v.fixed else 1 for v in params]
+    nd = pdf._nondiff_all()
+    mask = [0 if (v.fixed or id(v) in nd) else 1 for v in params]
     return nodes, olist, params, mask
 
 
 @pytest.mark.parametrize("prec", [A.GF_MIXED, A.GF_FP64])
-@pytest.mark.parametrize("which", ["c1", "c2"])
+@pytest.mark.parametrize("which", ["c1", "c2", "c3"])
 def test_generated_kernels_compile_for_sm103a(which, prec):
-    wl = W.make_c1(1000) if which == "c1" else W.make_c2(2000)
-    nodes, olist, params, mask = _tree(wl.pdf)
+    if which == "c3":
+        pdf = W.c3_model(1500)[0]
+    else:
+        pdf = (W.make_c1(1000) if which == "c1" else W.make_c2(2000)).pdf
+    nodes, olist, params, mask = _tree(pdf)
     nl = A.NodeList(nodes)
     obs = A.observables_array(olist)
     marr, mp = A.i32(mask)
@@ -68,6 +72,8 @@ def test_bad_trees_are_rejected():
         [dict(op=99, obs=[0])],                                              # unknown operator
         [dict(op=A.GF_OP_EXP, params=[5], obs=[0])],                          # parameter out of range
         [dict(op=A.GF_OP_EXP, params=[0], obs=[0], flags=A.GF_FLAG_COMMON_NORM)],
+        [dict(op=A.GF_OP_RES_RBW, params=[0, 1], consts=[3, 0, 1], obs=[])],  # spin 3
+        [dict(op=A.GF_OP_MULTIPOLYNOMIAL, params=[0], consts=[1], obs=[0])],   # too few coefficients
     ]
     for nodes in cases:
         nl = A.NodeList(nodes)
@@ -85,3 +91,33 @@ def test_engine_without_device_reports_no_device():
     assert rc == A.GF_ERR_NO_DEVICE
     with pytest.raises(A.EngineError):
         gf.Engine("mixed")
+
+
+def test_amp3body_tree_checks():
+    """Amp3Body trees: the resonance parameters have no analytic derivative, and the normalisation bins
+    inside the kinematic boundary are found by the FP64 boundary test."""
+    from oracle import oracle as O
+    pdf = W.c3_model(60)[0]
+    nodes, olist, params, mask = _tree(pdf)
+    L = A.lib()
+    nl = A.NodeList(nodes)
+    obs = A.observables_array(olist)
+    n = C.c_int64()
+    full = [0 if v.fixed else 1 for v in params]
+    for v in params:
+        if v.name == "rho0_mass":
+            v.fixed = False
+    full = [0 if v.fixed else 1 for v in params]
+    marr, mp = A.i32(full)
+    rc = L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, A.GF_MIXED, None, 0, C.byref(n))
+    assert rc == A.GF_ERR_BAD_TREE and b"resonance parameters" in L.gf_last_error(None)
+    # the generated integral kernel loops over exactly the in-Dalitz bins of a 60 x 60 grid
+    marr, mp = A.i32(mask)
+    rc = L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, A.GF_FP64, None, 0, C.byref(n))
+    buf = C.create_string_buffer(n.value + 1)
+    L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, A.GF_FP64, buf, n.value + 1, C.byref(n))
+    src = buf.value.decode()
+    inside = sum(O.in_dalitz(3.0 / 60 * (a + 0.5), 3.0 / 60 * (b + 0.5), W.C3_MD0, W.C3_MPI0, W.C3_MPIC, W.C3_MPIC)
+                 for a in range(60) for b in range(60))
+    assert 0 < inside < 3600
+    assert f"p < {inside}; p += gridDim.x * 256" in src
