@@ -413,7 +413,7 @@ def run_dalitz(args) -> dict:
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
 
     # one-time build of the amplitude cache and the integrals (a resonance parameter changes)
-    im = names.index("rho0_mass")
+    im = names.index("rho770_mass")
     build_ms = []
     for k in range(4):
         p = pv.copy()
@@ -493,7 +493,7 @@ def run_dalitz(args) -> dict:
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-events/f64-reductions" if args.precision == "mixed" else "f64",
         "data": f"synthetic (accept-reject on the model density, generated in {gen_s:.1f} s)",
-        "config": {"workload": "c3: Amp3Body D0->pi0 pi+ pi-, 8 RBW, 1500x1500 normalisation bins", "events": n,
+        "config": {"workload": "c3: Amp3Body 1.865 -> 0.4937 + 0.13957 + 0.13498 GeV, 8 RBW, seeded coefficients, 1500x1500 normalisation bins", "events": n,
                    "precision": args.precision,
                    "step": "one FCN: NLL + analytic gradient of 14 amplitude components, caches built",
                    "l2": "flushed (256 MB write) before every timed step", "parallelism": "single GPU"},

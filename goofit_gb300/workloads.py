@@ -10,10 +10,12 @@ C2  AddPdf(f_sig; ConvolutionPdf(ExpPdf(alpha), GaussianPdf(mu, sigma)), Polynom
     integration constants are (0, 10, 0.01): the exponential is a decay starting at t = 0, smeared by
     the resolution.  (With the default (-10, 10) range the exponential is not truncated inside the
     observable range, so mu and sigma would only rescale the normalisation and be unidentifiable.)
-C3  Amp3Body for D0 -> pi0 pi+ pi- with 8 relativistic Breit-Wigners (rho(770)+-0, rho(1450)+-0, f0(980),
-    f2(1270)); m12 = m^2(pi0 pi+), m13 = m^2(pi0 pi-) on [0, 3] GeV^2 with 1500 x 1500 normalisation bins;
-    constant efficiency; 14 floated amplitude components (the rho+ coefficient is the fixed reference);
-    5e5 events by accept-reject on the model density evaluated by the FP64 engine (needs a GPU).
+C3  Amp3Body for a 1.865 GeV parent to daughters of 0.4937 (K), 0.13957 (pi) and 0.13498 (pi0) GeV with 8
+    relativistic Breit-Wigners (masses/widths 0.775/0.149, 0.892/0.050, 1.414/0.232, 1.425/0.270,
+    0.980/0.050, 1.465/0.400, 1.720/0.250, 1.275/0.185; spins 0-2); seeded coefficients with magnitude
+    U[0.1, 2] and phase U[0, 2 pi) (the first one fixed: the overall scale and phase are not measurable);
+    m12 = m^2(K pi), m13 = m^2(K pi0) on [0, 3] GeV^2 with 1500 x 1500 normalisation bins; constant
+    efficiency; 5e5 events by accept-reject on the model density evaluated by the FP64 engine (needs a GPU).
 """
 from __future__ import annotations
 
@@ -152,22 +154,29 @@ def make_c4(n_toys: int = 1024, mean_events: float = 20_000, lo: int = 5_000, hi
     return ToyStudy("c4-toys", base.pdf, base.variables, truths, datas, dict(base.start))
 
 
-# D0 -> pi0 pi+ pi- masses (GeV) and the resonance set of the C3 configuration
-C3_MD0, C3_MPIC, C3_MPI0 = 1.86484, 0.13957018, 0.1349766
+# parent and daughter masses (GeV) and the resonance set of the C3 configuration
+C3_M, C3_MK, C3_MPI, C3_MPI0 = 1.865, 0.4937, 0.13957, 0.13498
 C3_RESONANCES = [
-    # name, mass, width, spin, pair, (Re, Im) coefficient, coefficient floated
-    ("rhop", 0.7758, 0.1503, 1, G.PAIR_12, (1.0, 0.0), False),
-    ("rhom", 0.7758, 0.1503, 1, G.PAIR_13, (0.714, -0.025), True),
-    ("rho0", 0.7758, 0.1503, 1, G.PAIR_23, (0.565, 0.164), True),
-    ("rhop_1450", 1.465, 0.400, 1, G.PAIR_12, (-0.174, -0.117), True),
-    ("rho0_1450", 1.465, 0.400, 1, G.PAIR_23, (0.325, 0.057), True),
-    ("rhom_1450", 1.465, 0.400, 1, G.PAIR_13, (0.788, 0.226), True),
-    ("f0_980", 0.980, 0.044, 0, G.PAIR_23, (0.008 * -C3_MD0 ** 2, -0.013 * -C3_MD0 ** 2), True),
-    ("f2_1270", 1.2754, 0.1851, 2, G.PAIR_23, (-1.027 * -1 / C3_MD0 ** 2, -0.162 * -1 / C3_MD0 ** 2), True),
+    # name, mass, width, spin, daughter pair
+    ("rho770", 0.775, 0.149, 1, G.PAIR_23),
+    ("kst892", 0.892, 0.050, 1, G.PAIR_12),
+    ("kst1410", 1.414, 0.232, 1, G.PAIR_13),
+    ("k0st1430", 1.425, 0.270, 0, G.PAIR_12),
+    ("f0_980", 0.980, 0.050, 0, G.PAIR_23),
+    ("rho1450", 1.465, 0.400, 1, G.PAIR_23),
+    ("rho1700", 1.720, 0.250, 1, G.PAIR_23),
+    ("f2_1270", 1.275, 0.185, 2, G.PAIR_23),
 ]
 
 
-def c3_model(bins: int = 1500, n_res: int = 8):
+def c3_coefficients(n_res: int = 8, seed: int = 3) -> list[complex]:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    mag = rng.uniform(0.1, 2.0, n_res)
+    ph = rng.uniform(0.0, 2 * np.pi, n_res)
+    return [complex(m * np.cos(p), m * np.sin(p)) for m, p in zip(mag, ph)]
+
+
+def c3_model(bins: int = 1500, n_res: int = 8, coef_seed: int = 3):
     """The C3 Amp3Body tree (no data attached); returns (pdf, variables, observables)."""
     m12 = G.Observable("m12", 0.0, 3.0)
     m13 = G.Observable("m13", 0.0, 3.0)
@@ -175,10 +184,12 @@ def c3_model(bins: int = 1500, n_res: int = 8):
     m13.setNumBins(bins)
     evt = G.EventNumber("eventNumber")
     d = G.DecayInfo3()
-    d.motherMass, d.daug1Mass, d.daug2Mass, d.daug3Mass = C3_MD0, C3_MPI0, C3_MPIC, C3_MPIC
+    d.motherMass, d.daug1Mass, d.daug2Mass, d.daug3Mass = C3_M, C3_MK, C3_MPI, C3_MPI0
     d.meson_radius, d.mother_meson_radius = 1.5, 5.0
     variables = {}
-    for name, mass, width, spin, pair, (re, im), free in C3_RESONANCES[:n_res]:
+    coefs = c3_coefficients(n_res, coef_seed)
+    for k, (name, mass, width, spin, pair) in enumerate(C3_RESONANCES[:n_res]):
+        re, im, free = coefs[k].real, coefs[k].imag, k > 0
         if free:
             ar = G.Variable(f"{name}_amp_real", re, 0.001, 0, 0)
             ai = G.Variable(f"{name}_amp_imag", im, 0.001, 0, 0)

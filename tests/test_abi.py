@@ -105,7 +105,7 @@ def test_amp3body_tree_checks():
     n = C.c_int64()
     full = [0 if v.fixed else 1 for v in params]
     for v in params:
-        if v.name == "rho0_mass":
+        if v.name == "rho770_mass":
             v.fixed = False
     full = [0 if v.fixed else 1 for v in params]
     marr, mp = A.i32(full)
@@ -117,7 +117,7 @@ def test_amp3body_tree_checks():
     buf = C.create_string_buffer(n.value + 1)
     L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, A.GF_FP64, buf, n.value + 1, C.byref(n))
     src = buf.value.decode()
-    inside = sum(O.in_dalitz(3.0 / 60 * (a + 0.5), 3.0 / 60 * (b + 0.5), W.C3_MD0, W.C3_MPI0, W.C3_MPIC, W.C3_MPIC)
+    inside = sum(O.in_dalitz(3.0 / 60 * (a + 0.5), 3.0 / 60 * (b + 0.5), W.C3_M, W.C3_MK, W.C3_MPI, W.C3_MPI0)
                  for a in range(60) for b in range(60))
     assert 0 < inside < 3600
     assert f"p < {inside}; p += gridDim.x * 256" in src

@@ -48,7 +48,7 @@ def engine(pdf, cols, prec):
 def test_generated_events_lie_in_the_dalitz_plot(c3_events):
     assert c3_events.shape == (3, 20_000)
     for k in range(0, 20_000, 997):
-        assert O.in_dalitz(c3_events[0, k], c3_events[1, k], W.C3_MD0, W.C3_MPI0, W.C3_MPIC, W.C3_MPIC)
+        assert O.in_dalitz(c3_events[0, k], c3_events[1, k], W.C3_M, W.C3_MK, W.C3_MPI, W.C3_MPI0)
 
 
 @pytest.mark.parametrize("prec", ["mixed", "fp64"])
@@ -111,14 +111,14 @@ def test_normalisation_follows_the_coefficients(c3_events):
     eng, nodes, olist, params, mask, pv = engine(pdf, c3_events, "fp64")
     names = [v.name for v in params]
     p = pv.copy()
-    p[names.index("rhom_amp_real")] *= 1.3
+    p[names.index("kst892_amp_real")] *= 1.3
     eng.set_params(p)
     Ie, Ne = eng.normalize()
     _, Io, No = O.evaluate(nodes, olist, p, c3_events[:, :1], metric=A.GF_METRIC_EVAL)
     assert Ie[0] == pytest.approx(Io[0], rel=1e-10)
     assert Ne[0] == pytest.approx(No[0], rel=1e-10)
     p2 = p.copy()
-    p2[names.index("rho0_mass")] = 0.78
+    p2[names.index("rho770_mass")] = 0.78
     ref = O.nll(nodes, olist, p2, c3_events)
     assert eng.nll(p2) == pytest.approx(ref, rel=1e-10)
     assert eng.nll(p) == pytest.approx(O.nll(nodes, olist, p, c3_events), rel=1e-10)
