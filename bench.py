@@ -377,10 +377,11 @@ def run_toys(args) -> dict:
 
 
 def run_dalitz(args) -> dict:
-    """C3: Amp3Body with 8 RBW resonances, 5e5 events, 1500 x 1500 normalisation bins.  A step is one FCN
-    (NLL + analytic gradient of the 14 floated amplitude components) with the amplitude caches and the
-    integrals built (resonance parameters fixed, as in the reference's Dalitz fits); the one-time cache and
-    integral build is timed separately."""
+    """C3: Amp3Body with 8 RBW resonances, 5e5 events, 1500 x 1500 normalisation bins; C5: Amp4Body with 6
+    decay chains, 3e5 events, 2e6 normalisation events.  A step is one FCN (NLL + analytic gradient of the
+    floated amplitude coefficients) with the amplitude caches and the integrals built (resonance / line-shape
+    parameters fixed, as in the reference's amplitude fits); the one-time cache and integral build is timed
+    separately."""
     import ctypes as C
 
     import numpy as np
@@ -391,9 +392,10 @@ def run_dalitz(args) -> dict:
     from goofit_gb300 import workloads as W
 
     torch.cuda.set_device(0)
-    n = args.events or 500_000
+    c5 = args.config == "c5"
+    n = args.events or (300_000 if c5 else 500_000)
     t0 = time.perf_counter()
-    wl = W.make_c3(n, seed=3)
+    wl = W.make_c5(n, 2_000_000, seed=5) if c5 else W.make_c3(n, seed=3)
     gen_s = time.perf_counter() - t0
     nodes, params, obs = wl.pdf._flatten()
     olist = [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs]
@@ -404,6 +406,8 @@ def run_dalitz(args) -> dict:
     cols = wl.data.to_numpy()
     eng = gf.Engine(args.precision)
     eng.set_tree(nodes, olist, len(params), mask)
+    for i, p in enumerate(wl.pdf._flat_order):
+        p._engine_setup(eng, i)
     host = torch.empty(cols.shape, dtype=torch.float64, pin_memory=True)
     host.numpy()[:] = cols
     hp = C.cast(host.data_ptr(), C.POINTER(C.c_double))
@@ -413,7 +417,7 @@ def run_dalitz(args) -> dict:
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
 
     # one-time build of the amplitude cache and the integrals (a resonance parameter changes)
-    im = names.index("rho770_mass")
+    im = names.index("rho_mass" if c5 else "rho770_mass")
     build_ms = []
     for k in range(4):
         p = pv.copy()
@@ -456,9 +460,10 @@ def run_dalitz(args) -> dict:
             e2e_ms.append(1e3 * (time.perf_counter() - t1))
     e2e = float(np.mean(e2e_ms))
 
-    # algorithmic bytes of the event pass: one complex amplitude per resonance and event (R2)
+    # algorithmic bytes of the event pass: one complex amplitude per resonance / amplitude and event (R2)
     rbytes = 4 if args.precision == "mixed" else 8
-    bytes_per_event = 8 * 2 * rbytes
+    n_amp = 6 if c5 else 8
+    bytes_per_event = n_amp * 2 * rbytes
     peaks = load_peaks()
     achieved = n * bytes_per_event / (evt / 1e3) / 1e9
 
@@ -481,21 +486,27 @@ def run_dalitz(args) -> dict:
     if not args.no_cpu:
         from oracle import oracle as O
         sample = min(n, 100_000)
+        if c5:
+            O.set_amp4_norm_events(wl.pdf.norm_events)
         O.nll(nodes, olist, pv, cols[:, :sample])
         t1 = time.perf_counter()
         O.nll(nodes, olist, pv, cols[:, :sample])
         dt = time.perf_counter() - t1
+        integ = "the 2e6-event normalisation sum" if c5 else "the 1500 x 1500 integrals"
         cpu = {"value": sample / dt, "unit": "event-NLL evals/s", "cores": O.num_threads(), "kind": "port",
-               "sample": f"{sample} events, one NLL (FP64 restatement: amplitudes per event and the 1500 x 1500 "
-                         "integrals recomputed every call, no cache)"}
+               "sample": f"{sample} events, one NLL (FP64 restatement: amplitudes per event and {integ} "
+                         "recomputed every call, no cache)"}
     return {
         "metric": METRIC, "value": n / (ms / 1e3), "unit": "event-NLL evals/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32-events/f64-reductions" if args.precision == "mixed" else "f64",
         "data": f"synthetic (accept-reject on the model density, generated in {gen_s:.1f} s)",
-        "config": {"workload": "c3: Amp3Body 1.865 -> 0.4937 + 0.13957 + 0.13498 GeV, 8 RBW, seeded coefficients, 1500x1500 normalisation bins", "events": n,
-                   "precision": args.precision,
-                   "step": "one FCN: NLL + analytic gradient of 14 amplitude components, caches built",
+        "config": {"workload": ("c5: Amp4Body 1.865 -> pi+ pi- K- pi+, 6 decay chains (BW/SBW), seeded coefficients, "
+                                "2e6 flat phase-space normalisation events") if c5 else
+                               ("c3: Amp3Body 1.865 -> 0.4937 + 0.13957 + 0.13498 GeV, 8 RBW, seeded coefficients, "
+                                "1500x1500 normalisation bins"),
+                   "events": n, "precision": args.precision,
+                   "step": f"one FCN: NLL + analytic gradient of {int(sum(mask))} amplitude components, caches built",
                    "l2": "flushed (256 MB write) before every timed step", "parallelism": "single GPU"},
         "e2e": {"value": n / (e2e / 1e3), "unit": "event-NLL evals/s", "h2d_bytes_per_step": int(cols.nbytes),
                 "d2h_bytes_per_step": (2 + eng.n_grad) * 8, "ms_per_step": e2e,
@@ -523,7 +534,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=100_000)
     ap.add_argument("--no-fit", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="c2", choices=["c2", "c3", "c4"])
+    ap.add_argument("--config", default="c2", choices=["c2", "c3", "c4", "c5"])
     ap.add_argument("--toys", type=int, default=1024)
     ap.add_argument("--events", type=int, default=0)
     args = ap.parse_args()
@@ -532,7 +543,7 @@ def main():
     if args.config == "c4":
         print(json.dumps(run_toys(args)))
         return
-    if args.config == "c3":
+    if args.config in ("c3", "c5"):
         print(json.dumps(run_dalitz(args)))
         return
     if args.impl == "reference":

@@ -6,7 +6,8 @@ resonances, FitManager)
 over libgfengine.so: per-tree generated sm_103a kernels behind a C ABI
 (include/gfengine.h).
 """
-from .api import (PAIR_12, PAIR_13, PAIR_23, RBW, AddPdf, Amp3Body, CombinePdf, ConvolutionPdf, DataSet,
+from .api import (FF, PAIR_12, PAIR_13, PAIR_23, RBW, SF_4Body, AddPdf, Amp3Body, Amp4Body, Amplitude, AmpComponent,
+                  CombinePdf, ConvolutionPdf, DataSet, DecayInfo4, DP4Pair, Lineshape, Lineshapes, SpinFactor,
                   DaughterPair, DecayInfo3, EvalFunc, EventNumber, ExpPdf, FitManager, FitManagerMinuit2,
                   GaussianPdf, GeneralError, GooPdf, MultiPolynomialPdf, NonRes, Observable, OutOfRange, PdfBase,
                   PolynomialPdf, ProdPdf, ResonancePdf, Resonances, UnbinnedDataSet, Variable, get_precision,
@@ -18,5 +19,6 @@ __all__ = [
     "FitManagerMinuit2", "GaussianPdf", "GeneralError", "GooPdf", "Observable", "OutOfRange", "PdfBase",
     "PolynomialPdf", "ProdPdf", "UnbinnedDataSet", "Variable", "Engine", "FitResult", "Minimizer",
     "get_precision", "set_precision", "Amp3Body", "DecayInfo3", "DaughterPair", "PAIR_12", "PAIR_13", "PAIR_23",
-    "ResonancePdf", "Resonances", "RBW", "NonRes", "MultiPolynomialPdf",
+    "ResonancePdf", "Resonances", "RBW", "NonRes", "MultiPolynomialPdf", "Amp4Body", "Amplitude", "AmpComponent",
+    "DecayInfo4", "DP4Pair", "FF", "Lineshape", "Lineshapes", "SF_4Body", "SpinFactor",
 ]

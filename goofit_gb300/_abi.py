@@ -45,6 +45,10 @@ GF_OP_AMP4BODY = 13
 GF_OP_MULTIPOLYNOMIAL = 14
 GF_OP_RES_RBW = 20
 GF_OP_RES_NONRES = 21
+GF_OP_AMPLITUDE = 15
+GF_OP_LS_RBW = 22
+GF_OP_LS_SBW = 23
+GF_OP_SPINFACTOR = 24
 
 GF_FLAG_COMMON_NORM = 1
 GF_FLAG_SEPARATE_NORM = 2
@@ -134,6 +138,7 @@ SIGNATURES = [
     ("gf_eval_events", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _f64p, C.c_int64]),
     ("gf_amp3_integrals", C.c_int, [_vp, C.c_int, C.c_int, _f64p, C.c_int]),
     ("gf_amp3_cached_wave", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _f64p, C.c_int64]),
+    ("gf_set_norm_events", C.c_int, [_vp, C.c_int, _f64p, C.c_int64]),
     ("gf_last_timing", C.c_int, [_vp, _f64p, _f64p]),
     ("gf_launches_per_eval", C.c_int, [_vp, C.c_int]),
     ("gf_time_kernels", C.c_int, [_vp, C.c_int, C.c_int, _f64p, _f64p, _f64p]),

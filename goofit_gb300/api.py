@@ -466,9 +466,12 @@ class PdfBase:
         oidx = {id(o): i for i, o in enumerate(obs)}
         nodes: list = []
 
+        order: list = []
+
         def visit(p: "PdfBase") -> int:
             i = len(nodes)
             nodes.append(None)
+            order.append(p)
             kids = [visit(c) for c in p.components]
             nodes[i] = dict(op=p.op, flags=p.flags, params=[pidx[id(v)] for v in p.parametersList],
                             consts=list(p._node_consts()), obs=[oidx[id(o)] for o in p.observablesList],
@@ -476,7 +479,11 @@ class PdfBase:
             return i
 
         visit(self)
+        self._flat_order = order
         return nodes, params, obs
+
+    def _engine_setup(self, eng, node: int) -> None:
+        """Per-node engine state beyond the tree (Amp4Body: its normalisation events)."""
 
     def _engine_for(self, data, precision: str | None = None):
         """Engine with this PDF as root and `data` uploaded; cached per (precision, data)."""
@@ -490,6 +497,8 @@ class PdfBase:
         if ent is None or ent["key"] != key:
             eng = ent["engine"] if ent else Engine(precision)
             eng.set_tree(nodes, olist, len(params), mask)
+            for i, p in enumerate(self._flat_order):
+                p._engine_setup(eng, i)
             ent = dict(engine=eng, key=key, data=None, version=-1)
             self._engines[precision] = ent
         eng = ent["engine"]
@@ -949,6 +958,222 @@ class Amp3Body(GooPdf):
                 amps[i][j] = b / ne
         total /= ne
         return [[amps[i][j] / total for j in range(n)] for i in range(n)]
+
+
+# ---------------------------------------------------------------- 4-body amplitudes
+class SF_4Body(enum.IntEnum):
+    """include/goofit/PDFs/physics/SpinFactors.h:18-35"""
+    DtoPP1_PtoSP2_StoP3P4 = 0
+    DtoPP1_PtoVP2_VtoP3P4 = 1
+    DtoV1V2_V1toP1P2_V2toP3P4_S = 2
+    DtoV1V2_V1toP1P2_V2toP3P4_P = 3
+    DtoV1V2_V1toP1P2_V2toP3P4_D = 4
+    DtoAP1_AtoVP2_VtoP3P4 = 5
+    DtoAP1_AtoVP2Dwave_VtoP3P4 = 6
+    DtoVS_VtoP1P2_StoP3P4 = 7
+    DtoV1P1_V1toV2P2_V2toP3P4 = 8
+    DtoAP1_AtoSP2_StoP3P4 = 9
+    DtoTP1_TtoVP2_VtoP3P4 = 10
+    FF_12_34_L1 = 11
+    FF_12_34_L2 = 12
+    FF_123_4_L1 = 13
+    FF_123_4_L2 = 14
+    ONE = 15
+
+
+class FF(enum.IntEnum):
+    """Form factors of a line shape (include/goofit/PDFs/physics/lineshapes/Lineshape.h:18)."""
+    One = 0
+    BL = 1
+    BL_Prime = 2
+    BL2 = 3
+
+
+class DP4Pair(enum.IntEnum):
+    """Daughter combinations of a 4-body line shape (include/goofit/PDFs/physics/DalitzPlotHelpers.h:58-77)."""
+    M_12 = 0
+    M_34 = 1
+    M_13 = 2
+    M_14 = 3
+    M_23 = 4
+    M_24 = 5
+    M_12_3 = 6
+    M_13_2 = 7
+    M_23_1 = 8
+    M_12_4 = 9
+    M_14_2 = 10
+    M_24_1 = 11
+    M_13_4 = 12
+    M_14_3 = 13
+    M_34_1 = 14
+    M_23_4 = 15
+    M_24_3 = 16
+    M_34_2 = 17
+
+
+for _p in DP4Pair:
+    globals()[_p.name] = _p
+
+
+class AmpComponent(GooPdf):
+    """include/goofit/PDFs/physics/AmpComponent.h: a building block of a 4-body amplitude."""
+
+
+class SpinFactor(AmpComponent):
+    """SpinFactor(name, SF, mD0, P0, P1, P2, P3) (src/PDFs/physics/SpinFactors.cu:586-664)."""
+    op = A.GF_OP_SPINFACTOR
+
+    def __init__(self, name: str, SF: SF_4Body, mD0: float, P0: int, P1: int, P2: int, P3: int):
+        super().__init__("SpinFactor", name)
+        self._SF, self._P = SF_4Body(SF), (P0, P1, P2, P3)
+        for c in (int(SF), mD0, P0, P1, P2, P3):
+            self.registerConstant(c)
+
+
+class Lineshape(AmpComponent):
+    """include/goofit/PDFs/physics/lineshapes/Lineshape.h: a line shape of a daughter combination."""
+
+    def __init__(self, pdf_name: str, name: str, mass: Variable, width: Variable, L: int, Mpair: int,
+                 FormFac: FF = FF.BL_Prime, radius: float = 1.5):
+        super().__init__("Lineshapes::" + pdf_name, name)
+        self._L, self._Mpair, self._FormFac, self._radius = int(L), int(Mpair), FF(FormFac), float(radius)
+        self.registerParameter(mass)
+        self.registerParameter(width)
+        for c in (int(Mpair), int(L), int(FormFac), float(radius)):
+            self.registerConstant(c)
+
+    def setParameterConstantness(self, constant: bool = True) -> None:
+        for v in self.parametersList:
+            v.setFixed(constant)
+
+
+class _RBWLineshape(Lineshape):
+    """Lineshapes::RBW (src/PDFs/physics/lineshapes/BW.cu:14-68, 136-151): mass-dependent width."""
+    op = A.GF_OP_LS_RBW
+
+    def __init__(self, name, mass, width, L, Mpair, FormFac=FF.BL_Prime, radius=1.5):
+        super().__init__("RBW", name, mass, width, L, Mpair, FormFac, radius)
+
+
+class _SBWLineshape(Lineshape):
+    """Lineshapes::SBW (src/PDFs/physics/lineshapes/BW.cu:70-110, 155-170): constant width."""
+    op = A.GF_OP_LS_SBW
+
+    def __init__(self, name, mass, width, L, Mpair, FormFac=FF.BL_Prime, radius=1.5):
+        super().__init__("SBW", name, mass, width, L, Mpair, FormFac, radius)
+
+
+class Lineshapes:
+    """Namespace of the 4-body line shapes (GooFit::Lineshapes); RBW and SBW are provided."""
+    RBW = _RBWLineshape
+    SBW = _SBWLineshape
+
+
+class Amplitude(AmpComponent):
+    """Amplitude(uniqueDecayStr, ar, ai, LS, SF, nPerm) (src/PDFs/physics/Amplitude.cu:11-31): the sum over
+    nPerm permutations of products of its line shapes and spin factors, divided by sqrt(nPerm)."""
+    op = A.GF_OP_AMPLITUDE
+
+    def __init__(self, uniqueDecayStr: str, ar: Variable, ai: Variable, LS: Sequence[Lineshape],
+                 SF: Sequence[SpinFactor], nPerm: int = 1):
+        super().__init__("Amplitude", uniqueDecayStr)
+        self._uniqueDecayStr = uniqueDecayStr
+        self._ar, self._ai = ar, ai
+        self._LS, self._SF, self._nPerm = list(LS), list(SF), int(nPerm)
+        if len(self._LS) % self._nPerm or len(self._SF) % self._nPerm:
+            raise GeneralError("line shape and spin factor counts must be multiples of nPerm")
+        self.components = self._LS + self._SF
+        for c in (self._nPerm, len(self._LS), len(self._SF)):
+            self.registerConstant(c)
+
+    def getLineShapes(self) -> list:
+        return self._LS
+
+    def getSpinFactors(self) -> list:
+        return self._SF
+
+
+class DecayInfo4:
+    """include/goofit/PDFs/physics/DalitzPlotHelpers.h:114-120: particle_masses = [M, m1, m2, m3, m4]."""
+
+    def __init__(self):
+        self.particle_masses: list[float] = []
+        self.meson_radius = 1.5
+        self.amplitudes: list[Amplitude] = []
+        self.amplitudes_B: list[Amplitude] = []
+
+
+class Amp4Body(GooPdf):
+    """Amp4Body(name, observables, decay, eff, MCeventsNorm) (src/PDFs/physics/Amp4Body.cu:94-292):
+    |sum_a c_a A_a|^2 * efficiency over (m12, m34, cos12, cos34, phi[, eventNumber]), normalised by the mean
+    of |sum_a c_a A_a|^2 over flat phase-space events.  The normalisation events are generated here
+    (MCeventsNorm of them kept after unweighting, seeded by norm_seed); the reference draws them with
+    MCBooster and keeps the accepted part of MCeventsNorm."""
+    op = A.GF_OP_AMP4BODY
+    cacheCount = 0
+
+    def __init__(self, name: str, observables: Sequence[Observable], decay: DecayInfo4, eff: GooPdf | None = None,
+                 MCeventsNorm: int = 5_000_000, norm_seed: int = 4242):
+        from . import phasespace
+        super().__init__("Amp4Body", name)
+        obs = list(observables)
+        if len(obs) < 5:
+            raise GeneralError("Amp4Body needs the observables m12, m34, cos12, cos34, phi (and eventNumber)")
+        for o in obs:
+            self.registerObservable(o)
+        self.decayInfo = decay
+        masses = list(decay.particle_masses)
+        if len(masses) != 5:
+            raise GeneralError("DecayInfo4.particle_masses must hold the parent and four daughter masses")
+        for m in masses:
+            self.registerConstant(m)
+        self.cacheToUse = Amp4Body.cacheCount
+        Amp4Body.cacheCount += 1
+        self.registerConstant(self.cacheToUse)
+        for amp in decay.amplitudes:
+            self.registerParameter(amp._ar)
+            self.registerParameter(amp._ai)
+            self.components.append(amp)
+        if eff is None:
+            eff = MultiPolynomialPdf(f"{name}_constantEff", obs[:2], [Variable(f"{name}_constantOne", 1)],
+                                     [Variable(f"{name}_zero0", 0), Variable(f"{name}_zero1", 0)], 0)
+        self.efficiency = eff
+        self.components.append(eff)
+        self.MCevents = int(MCeventsNorm)
+        self.norm_events = phasespace.norm_events(masses[0], masses[1:], self.MCevents, norm_seed)
+        self.setSeparateNorm()
+
+    def _engine_setup(self, eng, node: int) -> None:
+        eng.set_norm_events(node, self.norm_events)
+
+    def _nondiff_params(self) -> set:
+        ids = set()
+        for c in self.components:
+            ids |= {id(v) for v in c.getParameters()}
+        return ids
+
+    def setDataSize(self, dataSize: int, evtSize: int = 6) -> None:
+        """The amplitude cache is sized by the uploaded data; kept for interface compatibility."""
+        if evtSize < 3:
+            raise GeneralError(f"totalEventSize {evtSize} should be 3 or more")
+
+    def setForceIntegrals(self, f: bool = True) -> None:
+        """Caches are rebuilt whenever a line-shape parameter changes."""
+
+    def _root_engine(self):
+        if self.data is None:
+            raise GeneralError("no data set")
+        eng, params = self._engine_for(self.data)
+        eng.set_params(self._param_values(params))
+        return eng
+
+    def getCachedAmplitude(self, i: int) -> np.ndarray:
+        """Amplitude i at every data event (the reference's cachedAMPs column)."""
+        return self._root_engine().amp3_cached_wave(0, i)
+
+    def normalisation_sums(self) -> np.ndarray:
+        """G_ab = sum over the normalisation events of A_a conj(A_b)."""
+        return self._root_engine().amp3_integrals(0, len(self.decayInfo.amplitudes))
 
 
 # ---------------------------------------------------------------- fitting

@@ -385,24 +385,26 @@ Val emit(Ctx &c, int i) {
         out.v = v;
         break;
     }
-    case GF_OP_AMP3BODY: {
-        // device_DalitzPlot (src/PDFs/physics/Amp3Body.cu:60-122): |sum_r c_r B_r|^2 * efficiency, with the
-        // resonance amplitudes B_r read from the per-event cache
+    case GF_OP_AMP3BODY:
+    case GF_OP_AMP4BODY: {
+        // device_DalitzPlot (src/PDFs/physics/Amp3Body.cu:60-122) and device_DP
+        // (src/PDFs/physics/Amp4Body.cu:53-90): |sum_r c_r B_r|^2 * efficiency, with the amplitudes B_r
+        // read from the per-event cache
         if(!c.amp)
-            throw std::runtime_error("codegen: Amp3Body outside the event pass");
-        const int ai      = c.T.amp3_of[i];
-        const Amp3Info &A = c.T.amp3s[ai];
-        Val ev            = emit(c, A.eff);
+            throw std::runtime_error("codegen: amplitude PDF outside the event pass");
+        const int ai   = c.T.amp_index(i);
+        const int nRes = c.T.amp_count(ai);
+        Val ev         = emit(c, n.children.back());
         std::string tr = c.tmp("tr"), ti = c.tmp("ti"), v = c.tmp("v");
         os << "    R " << tr << " = R(0), " << ti << " = R(0);\n";
-        for(int r = 0; r < A.nRes; ++r) {
+        for(int r = 0; r < nRes; ++r) {
             std::string b = c.amp(ai, r), cr = P(n.params[2 * r]), cim = P(n.params[2 * r + 1]);
             os << "    " << tr << " += " << cr << " * " << b << ".x - " << cim << " * " << b << ".y;\n";
             os << "    " << ti << " += " << cr << " * " << b << ".y + " << cim << " * " << b << ".x;\n";
         }
         os << "    const R " << v << " = (" << tr << " * " << tr << " + " << ti << " * " << ti << ") * " << ev.v << ";\n";
         out.v = v;
-        for(int r = 0; r < A.nRes; ++r) {
+        for(int r = 0; r < nRes; ++r) {
             std::string b = c.amp(ai, r);
             gadd(c, out, slot(c, n.params[2 * r]),
                  "R(2) * (" + tr + " * " + b + ".x + " + ti + " * " + b + ".y) * " + ev.v);
@@ -412,7 +414,11 @@ Val emit(Ctx &c, int i) {
         break;
     }
     case GF_OP_RES_RBW:
-    case GF_OP_RES_NONRES: throw std::runtime_error("codegen: resonances are evaluated by the amplitude kernels only");
+    case GF_OP_RES_NONRES:
+    case GF_OP_AMPLITUDE:
+    case GF_OP_LS_RBW:
+    case GF_OP_LS_SBW:
+    case GF_OP_SPINFACTOR: throw std::runtime_error("codegen: amplitude components are evaluated by the amplitude kernels only");
     default: throw std::runtime_error("codegen: unsupported operator");
     }
     materialise(c, out);
@@ -447,6 +453,8 @@ struct GfArgs {
     const unsigned *dgrid;     /* in-Dalitz normalisation bins of every Amp3Body, b12 | b13 << 16 */
     double *gram;              /* integral partials [toy][tile][CTA][2 * pairs] */
     const int *dirty;          /* [toy] amplitude caches to rebuild */
+    const double *const *nevt; /* per Amp4Body: normalisation events, SoA 5 x nnorm */
+    const i64 *nnorm;
     int n_chunks;
     int n_toys;
     int metric;
@@ -680,12 +688,198 @@ __device__ __forceinline__ R2 gf_rbw(double m12, double m13, double m23, double 
 }
 )CUDA";
 
+// 4-body amplitude helpers in FP64: daughter 4-vectors from the five variables (get4Vecs,
+// src/PDFs/physics/DalitzPlotHelpers.cu:77-156), invariant masses of daughter combinations (getmass,
+// :158-232), the Zemach spin-factor algebra (include/goofit/PDFs/physics/detail/SpinHelper.h), the spin
+// factors (src/PDFs/physics/SpinFactors.cu:83-568) and the BW / SBW line shapes with their Blatt-Weisskopf
+// factors (src/PDFs/physics/lineshapes/BW.cu:14-110, Common.cu:8-51).  Vectors are (x, y, z, E).
+const char *kPreludeAmp4 = R"CUDA(
+struct GfLV { double x, y, z, e; };
+__device__ __forceinline__ GfLV lv(double x, double y, double z, double e) { GfLV v; v.x = x; v.y = y; v.z = z; v.e = e; return v; }
+__device__ __forceinline__ GfLV operator+(GfLV a, GfLV b) { return lv(a.x + b.x, a.y + b.y, a.z + b.z, a.e + b.e); }
+__device__ __forceinline__ GfLV operator-(GfLV a, GfLV b) { return lv(a.x - b.x, a.y - b.y, a.z - b.z, a.e - b.e); }
+__device__ __forceinline__ GfLV operator*(GfLV a, double s) { return lv(a.x * s, a.y * s, a.z * s, a.e * s); }
+__device__ __forceinline__ GfLV operator*(double s, GfLV a) { return lv(a.x * s, a.y * s, a.z * s, a.e * s); }
+__device__ __forceinline__ double ldot(GfLV a, GfLV b) { return a.e * b.e - a.x * b.x - a.y * b.y - a.z * b.z; }
+__device__ __forceinline__ double lmass(GfLV a) { return sqrt(ldot(a, a)); }
+// spin-1 Zemach tensor q - (q.p) p / mR^2 and the spin sum of a vector, -v + p (p.v) / mR^2
+__device__ __forceinline__ GfLV zt1(GfLV q, GfLV p, double mR) { return q - ldot(q, p) * p * (1. / (mR * mR)); }
+__device__ __forceinline__ GfLV ssv(GfLV p, double mR, GfLV v) { return -1.0 * v + p * (ldot(p, v) / (mR * mR)); }
+__device__ __forceinline__ double ssvs(GfLV p, double mR, GfLV l, GfLV r) { return ldot(l, ssv(p, mR, r)); }
+__device__ __forceinline__ double ssts(GfLV p, double mR, GfLV lm, GfLV ln, GfLV ra, GfLV rb) {
+    const double manb = ssvs(p, mR, lm, ra) * ssvs(p, mR, ln, rb);
+    const double mbna = ssvs(p, mR, lm, rb) * ssvs(p, mR, ln, ra);
+    const double mnab = ssvs(p, mR, lm, ln) * ssvs(p, mR, ra, rb);
+    return (1. / 2.) * (manb + mbna) - (1. / 3.) * mnab;
+}
+// spin-2 Zemach tensor contracted with a vector: T(q, p) . v with T = t t - |t|^2 / 3 (g - p p / mR^2)
+__device__ __forceinline__ GfLV zt2c(GfLV q, GfLV p, double mR, GfLV v) {
+    const GfLV t = zt1(q, p, mR);
+    const double f = (1. / 3.) * ldot(t, t), iu = 1. / (mR * mR);
+    const double tc[4] = {t.x, t.y, t.z, t.e}, pc[4] = {p.x, p.y, p.z, p.e};
+    const double g[4][4] = {{-1, 0, 0, 0}, {0, -1, 0, 0}, {0, 0, -1, 0}, {0, 0, 0, 1}};
+    GfLV row[4];
+#pragma unroll
+    for(int i = 0; i < 4; ++i) {
+        double r[4];
+#pragma unroll
+        for(int j = 0; j < 4; ++j)
+            r[j] = tc[i] * tc[j] - f * (g[i][j] - pc[i] * pc[j] * iu);
+        row[i] = lv(r[0], r[1], r[2], r[3]);
+    }
+    return v.e * row[3] - v.x * row[0] - v.y * row[1] - v.z * row[2];
+}
+__device__ __forceinline__ GfLV leps3(GfLV a, GfLV b, GfLV c) {
+    GfLV v;
+    v.e = -1. * a.x * (b.y * c.z - b.z * c.y) - a.y * (b.z * c.x - b.x * c.z) - a.z * (b.x * c.y - b.y * c.x);
+    v.z = a.x * (b.e * c.y - b.y * c.e) + a.y * (b.x * c.e - b.e * c.x) + a.e * (b.y * c.x - b.x * c.y);
+    v.y = a.x * (b.z * c.e - b.e * c.z) + a.z * (b.e * c.x - b.x * c.e) + a.e * (b.x * c.z - b.z * c.x);
+    v.x = a.y * (b.e * c.z - b.z * c.e) + a.z * (b.y * c.e - b.e * c.y) + a.e * (b.z * c.y - b.y * c.z);
+    return v;
+}
+__device__ __forceinline__ void gf_get4vecs(GfLV *P, double m12, double m34, double cos12, double cos34, double phi,
+                                            double M, double m1, double m2, double m3, double m4) {
+    const double E1 = (m12 * m12 + m1 * m1 - m2 * m2) / (2 * m12), E2 = (m12 * m12 - m1 * m1 + m2 * m2) / (2 * m12);
+    const double E3 = (m34 * m34 + m3 * m3 - m4 * m4) / (2 * m34), E4 = (m34 * m34 - m3 * m3 + m4 * m4) / (2 * m34);
+    const double p1 = sqrt(E1 * E1 - m1 * m1), p3 = sqrt(E3 * E3 - m3 * m3);
+    const double sin12 = sqrt(1 - cos12 * cos12), sin34 = sqrt(1 - cos34 * cos34);
+    const double ED1 = (M * M + m12 * m12 - m34 * m34) / (2 * m12), PD1 = sqrt(ED1 * ED1 - M * M);
+    const double beta1 = PD1 / ED1, gamma1 = 1.0 / sqrt(1 - beta1 * beta1);
+    const double ED2 = (M * M - m12 * m12 + m34 * m34) / (2 * m34), PD2 = sqrt(ED2 * ED2 - M * M);
+    const double beta2 = -PD2 / ED2, gamma2 = 1.0 / sqrt(1 - beta2 * beta2);
+    const double x[4] = {cos12 * p1, -cos12 * p1, -cos34 * p3, cos34 * p3};
+    const double y[4] = {sin12 * p1, -sin12 * p1, -sin34 * p3, sin34 * p3};
+    const double E[4] = {E1, E2, E3, E4};
+    const double cp = cos(phi), sp = sin(phi);
+#pragma unroll
+    for(int k = 0; k < 4; ++k) {
+        const double g = k < 2 ? gamma1 : gamma2, b = k < 2 ? beta1 : beta2;
+        P[k].e = g * (E[k] + b * x[k]);
+        P[k].x = g * (x[k] + b * E[k]);
+        P[k].z = k < 2 ? sp * y[k] : 0.0;
+        P[k].y = k < 2 ? cp * y[k] : y[k];
+    }
+}
+// invariant mass of a daughter combination (DP4Pair code) and the masses it decays to
+__device__ __forceinline__ double gf_pairmass(int pair, const GfLV *P, double m1, double m2, double m3, double m4,
+                                              double &d1, double &d2) {
+    switch(pair) {
+    case 0: d1 = m1; d2 = m2; return lmass(P[0] + P[1]);
+    case 1: d1 = m3; d2 = m4; return lmass(P[2] + P[3]);
+    case 2: d1 = m1; d2 = m3; return lmass(P[0] + P[2]);
+    case 3: d1 = m1; d2 = m4; return lmass(P[0] + P[3]);
+    case 4: d1 = m2; d2 = m3; return lmass(P[1] + P[2]);
+    case 5: d1 = m2; d2 = m4; return lmass(P[1] + P[3]);
+    case 6: d1 = lmass(P[0] + P[1]); d2 = m3; return lmass(P[0] + P[1] + P[2]);
+    case 7: d1 = lmass(P[0] + P[2]); d2 = m2; return lmass(P[0] + P[1] + P[2]);
+    case 8: d1 = lmass(P[1] + P[2]); d2 = m1; return lmass(P[0] + P[1] + P[2]);
+    case 9: d1 = lmass(P[0] + P[1]); d2 = m4; return lmass(P[0] + P[1] + P[3]);
+    case 10: d1 = lmass(P[0] + P[3]); d2 = m2; return lmass(P[0] + P[1] + P[3]);
+    case 11: d1 = lmass(P[1] + P[3]); d2 = m1; return lmass(P[0] + P[1] + P[3]);
+    case 12: d1 = lmass(P[0] + P[2]); d2 = m4; return lmass(P[0] + P[2] + P[3]);
+    case 13: d1 = lmass(P[0] + P[3]); d2 = m3; return lmass(P[0] + P[2] + P[3]);
+    case 14: d1 = lmass(P[2] + P[3]); d2 = m1; return lmass(P[0] + P[2] + P[3]);
+    case 15: d1 = lmass(P[1] + P[2]); d2 = m4; return lmass(P[1] + P[2] + P[3]);
+    case 16: d1 = lmass(P[1] + P[3]); d2 = m3; return lmass(P[1] + P[2] + P[3]);
+    default: d1 = lmass(P[2] + P[3]); d2 = m2; return lmass(P[1] + P[2] + P[3]);
+    }
+}
+__device__ __forceinline__ double gf_spinfactor(int kind, double mD0, GfLV P1, GfLV P2, GfLV P3, GfLV P4) {
+    switch(kind) {
+    case 1: { const GfLV pV = P3 + P4, qV = P3 - P4, pP = pV + P2, qP = pV - P2;
+              return ldot(zt1(qP, pP, lmass(pP)), zt1(qV, pV, lmass(pV))); }
+    case 2: { const GfLV pV1 = P1 + P2, qV1 = P1 - P2, pV2 = P3 + P4, qV2 = P3 - P4;
+              const double MV1 = sqrt(ldot(pV1, pV1)), MV2 = sqrt(ldot(pV2, pV2));
+              return (ldot(qV1, qV2) - ldot(qV1, pV1) * ldot(pV1, qV2) / (MV1 * MV1) -
+                      ldot(qV1, pV2) * ldot(pV2, qV2) / (MV2 * MV2) +
+                      ldot(qV1, pV1) * ldot(pV1, pV2) * ldot(pV2, qV2) / (MV1 * MV1 * MV2 * MV2)); }
+    case 3: { const GfLV pV1 = P1 + P2, qV1 = P2 - P1, pV2 = P3 + P4, qV2 = P4 - P3, pD = pV1 + pV2, qD = pV1 - pV2;
+              const double MV1 = sqrt(ldot(pV1, pV1)), MV2 = sqrt(ldot(pV2, pV2));
+              return -ldot(leps3(pD, zt1(qD, pD, lmass(pD)), zt1(qV1, pV1, MV1)), zt1(qV2, pV2, MV2)); }
+    case 4: { const GfLV pV1 = P1 + P2, qV1 = P1 - P2, pV2 = P3 + P4, qV2 = P3 - P4, pD = pV1 + pV2, qD = pV1 - pV2;
+              return ldot(zt1(qV1, pV1, lmass(pV1)), zt2c(qD, pD, lmass(pD), zt1(qV2, pV2, lmass(pV2)))); }
+    case 5: { const GfLV pV = P3 + P4, qV = P3 - P4, pA = P2 + pV, pD = P1 + pA, qD = pA - P1;
+              return -ldot(zt1(qD, pD, lmass(pD)), ssv(pA, lmass(pA), zt1(qV, pV, lmass(pV)))); }
+    case 6: { const GfLV pV = P3 + P4, qV = P3 - P4, pA = P2 + pV, qA = P2 - pV, pD = P1 + pA, qD = pA - P1;
+              return ldot(zt1(qD, pD, lmass(pD)), zt2c(qA, pA, lmass(pA), zt1(qV, pV, lmass(pV)))); }
+    case 7: { const GfLV pS = P3 + P4, pV = P1 + P2, qV = P1 - P2, pD = pV + pS, qD = pV - pS;
+              return ldot(zt1(qD, pD, lmass(pD)), zt1(qV, pV, lmass(pV))); }
+    case 8: { const GfLV pV1 = P2 + P3 + P4, pV2 = P3 + P4, qV1 = (P3 + P4) - P2, qV2 = P3 - P4;
+              const double MV1 = lmass(pV1), MV2 = lmass(pV2);
+              const GfLV pD = pV1 + P1, qD = pV1 - P1;
+              return ldot(leps3(pV1, zt1(qV1, pV1, MV1), zt1(qV2, pV2, MV2)), ssv(pV1, MV1, zt1(qD, pD, lmass(pD)))); }
+    case 9: { const GfLV pS = P3 + P4, pA = P2 + pS, qA = pS - P2, pD = pA + P1, qD = pA - P1;
+              return ldot(zt1(qD, pD, lmass(pD)), zt1(qA, pA, lmass(pA))); }
+    case 10: { const GfLV pV = P3 + P4, qV = P3 - P4, pT = P2 + pV, qT = pV - P2, pD = P1 + pT, qD = pT - P1;
+               const double mT = lmass(pT);
+               const GfLV tV = zt1(qV, pV, lmass(pV)), tD = zt1(qD, pD, lmass(pD)), t1T = zt1(qT, pT, mT);
+               const GfLV tmp = leps3(t1T, pT, ssv(pT, mT, tV));
+               return ssts(pT, mT, tD, tD, tmp, t1T) + 1. / 3. * ldot(tD, tD) / ldot(pT, pT) * ssts(pT, mT, pD, pD, tmp, t1T); }
+    case 11: case 12: case 13: case 14: {
+        const bool l12 = kind == 11 || kind == 12;
+        const double a = l12 ? ldot(P1 + P2, P1 + P2) : ldot(P1 + P2 + P3, P1 + P2 + P3);
+        const double b = l12 ? ldot(P3 + P4, P3 + P4) : ldot(P4, P4);
+        const GfLV T = P1 + P2 + P3 + P4;
+        const double s = ldot(T, T);
+        const double q2 = s / 4. - (a + b) / 2. + (a - b) * (a - b) / (4 * s);
+        const double z2 = q2 * mD0 * mD0;
+        const double ff = (kind == 11 || kind == 13) ? 1.0 / (1 + z2) : 1.0 / (z2 * z2 + 3 * z2 + 9);
+        return sqrt(ff); }
+    default: return 1.0; // DtoPP1_PtoSP2_StoP3P4 and ONE
+    }
+}
+__device__ __forceinline__ double gf_blp(double z2, double z02, int L) {
+    return L == 0 ? 1.0 : (L == 1 ? (1 + z02) / (1 + z2) : (z02 * z02 + 3 * z02 + 9) / (z2 * z2 + 3 * z2 + 9));
+}
+__device__ __forceinline__ double gf_bl(double z2, int L) {
+    return L == 0 ? 1.0 : (L == 1 ? 2 * z2 / (1 + z2) : (13 * z2 * z2) / (z2 * z2 + 3 * z2 + 9));
+}
+__device__ __forceinline__ double gf_bl2(double z2, int L) {
+    return L == 0 ? 1.0 : (L == 1 ? 1.0 / (1 + z2) : 1.0 / (z2 * z2 + 3 * z2 + 9));
+}
+// BW (RBW, with mass-dependent width) or SBW (constant width) line shape
+__device__ __forceinline__ double2 gf_lineshape(bool sbw, double Mpair, double m1, double m2, double mass, double width,
+                                                int orbital, int FF, double radius) {
+    const double mr2 = Mpair * Mpair;
+    const double mpsq = (m1 + m2) * (m1 + m2), mmsq = (m1 - m2) * (m1 - m2);
+    const double num = (mr2 - mpsq) * (mr2 - mmsq), num2 = (mass * mass - mpsq) * (mass * mass - mmsq);
+    const double pABSq = num / (4 * mr2);
+    double prSq = num2 / (4 * mass * mass);
+    const double prSq2 = prSq < 0 ? 0 : prSq;
+    prSq = fabs(prSq);
+    const double r2 = radius * radius;
+    double fr = 1;
+    if(0 != orbital && 0 != FF) {
+        fr = (FF == 1 ? gf_bl(pABSq * r2, orbital) : gf_blp(pABSq * r2, prSq2 * r2, orbital));
+        fr = (FF == 3 ? gf_bl2(pABSq * r2, orbital) : fr);
+    }
+    double GofM, k;
+    if(!sbw) {
+        const double pratio = sqrt(pABSq / prSq);
+        double pj = 1;
+        for(int i = 0; i < 2 * orbital + 1; i++)
+            pj *= pratio;
+        GofM = width * pj * (mass / Mpair) * gf_blp(pABSq * r2, prSq * r2, orbital);
+        const double gamma = mass * sqrt((mass * mass + width * width));
+        k = (2.0 * sqrt(2.0) / 3.14159265358979323846) * mass * width * gamma / sqrt(mass * mass + gamma);
+    } else {
+        GofM = width;
+        const double gamma = sqrt(mass * mass * (mass * mass + width * width));
+        k = mass * width * gamma / sqrt(mass * mass + gamma);
+    }
+    const double den = (mass * mass - mr2) * (mass * mass - mr2) + mass * GofM * mass * GofM;
+    const double f = sqrt(k * fr) / den;
+    return make_double2(f * (mass * mass - mr2), f * (mass * GofM));
+}
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+)CUDA";
+
 // Where every normalisation factor is kept (see NormLayout in tree.h).
 NormLayout computeNormLayout(const Tree &T) {
     NormLayout nl;
     nl.npr = T.n_params;
     for(size_t i = 0; i < T.nodes.size(); ++i) {
-        if(T.nk[i] != NK_EXP && T.nk[i] != NK_GAUSS && T.nk[i] != NK_AMP3)
+        if(T.nk[i] != NK_EXP && T.nk[i] != NK_GAUSS && T.nk[i] != NK_AMP3 && T.nk[i] != NK_AMP4)
             continue;
         NormLayout::Analytic a;
         a.node  = (int)i;
@@ -1078,10 +1272,63 @@ struct Gen {
         return lit(A.M) + ", " + lit(A.m1) + ", " + lit(A.m2) + ", " + lit(A.m3);
     }
 
+    // Device function computing every amplitude of Amp4Body node k at one point of the five variables:
+    // distinct line shapes and spin factors once, then AmpCalc's sum over permutations of their products
+    // (src/PDFs/physics/detail/AmpCalc.cu:29-56).
+    void amp4Function(int k) {
+        const Amp4Info &A = T.amp4s[k];
+        const double m1 = A.m[0], m2 = A.m[1], m3 = A.m[2], m4 = A.m[3];
+        os << "__device__ void gf_amp4_" << k
+           << "(double m12, double m34, double c12, double c34, double phi, const double *P, double2 *A) {\n";
+        os << "  GfLV V[4];\n";
+        os << "  gf_get4vecs(V, m12, m34, c12, c34, phi, " << lit(A.M) << ", " << lit(m1) << ", " << lit(m2) << ", "
+           << lit(m3) << ", " << lit(m4) << ");\n";
+        os << "  double d1, d2, mp; (void)d1; (void)d2; (void)mp;\n";
+        for(size_t u = 0; u < A.ls.size(); ++u) {
+            const TNode &L = T.nodes[A.ls[u]];
+            const int pair = (int)L.consts[0];
+            if(pair < 2)
+                os << "  mp = " << (pair == 0 ? "m12" : "m34") << "; d1 = " << lit(pair == 0 ? m1 : m3) << "; d2 = "
+                   << lit(pair == 0 ? m2 : m4) << ";\n";
+            else
+                os << "  mp = gf_pairmass(" << pair << ", V, " << lit(m1) << ", " << lit(m2) << ", " << lit(m3) << ", "
+                   << lit(m4) << ", d1, d2);\n";
+            os << "  const double2 L" << u << " = gf_lineshape(" << (L.op == GF_OP_LS_SBW ? "true" : "false")
+               << ", mp, d1, d2, P[" << L.params[0] << "], P[" << L.params[1] << "], " << (int)L.consts[1] << ", "
+               << (int)L.consts[2] << ", " << lit(L.consts[3]) << ");\n";
+        }
+        for(size_t u = 0; u < A.sf.size(); ++u) {
+            const TNode &S = T.nodes[A.sf[u]];
+            os << "  const double S" << u << " = gf_spinfactor(" << (int)S.consts[0] << ", " << lit(S.consts[1]) << ", V["
+               << (int)S.consts[2] << "], V[" << (int)S.consts[3] << "], V[" << (int)S.consts[4] << "], V["
+               << (int)S.consts[5] << "]);\n";
+        }
+        for(int a = 0; a < A.nAmp; ++a) {
+            const Amp4Info::Amp &am = A.amps[a];
+            const int ls_step = (int)am.ls.size() / am.nPerm, sf_step = (int)am.sf.size() / am.nPerm;
+            os << "  {\n    double2 r2 = make_double2(0.0, 0.0);\n";
+            for(int p = 0; p < am.nPerm; ++p) {
+                os << "    { double2 r = make_double2(1.0, 0.0);\n";
+                for(int j = p * ls_step; j < (p + 1) * ls_step; ++j)
+                    os << "      r = cmul(r, L" << am.ls[j] << ");\n";
+                for(int j = p * sf_step; j < (p + 1) * sf_step; ++j)
+                    os << "      r.x *= S" << am.sf[j] << "; r.y *= S" << am.sf[j] << ";\n";
+                os << "      r2.x += r.x; r2.y += r.y; }\n";
+            }
+            os << "    const double f = 1 / sqrt((double)" << am.nPerm << ");\n";
+            os << "    A[" << a << "] = make_double2(r2.x * f, r2.y * f);\n  }\n";
+        }
+        os << "}\n\n";
+    }
+
     void ampKernels() {
-        if(T.amp3s.empty())
+        const int NAN_ = T.n_amp_nodes();
+        if(NAN_ == 0)
             return;
+        for(size_t k = 0; k < T.amp4s.size(); ++k)
+            amp4Function((int)k);
         const int NA = T.n_amp_cols, NO = (int)T.obs.size(), np = std::max(1, T.n_params);
+        const int n3 = (int)T.amp3s.size();
         os << "extern \"C\" __global__ void __launch_bounds__(256) gf_amp(const GfArgs a) {\n";
         os << "  const int toy = blockIdx.y, k = blockIdx.z, tid = threadIdx.x;\n";
         os << "  if(!a.dirty[toy]) return;\n";
@@ -1089,7 +1336,7 @@ struct Gen {
         os << "  const double *P = a.P + (i64)toy * " << np << "; (void)P;\n";
         os << "  R2 *const *ac = reinterpret_cast<R2 *const *>(const_cast<void **>(a.acol)) + (i64)toy * " << NA << ";\n";
         os << "  switch(k) {\n";
-        for(size_t ai = 0; ai < T.amp3s.size(); ++ai) {
+        for(int ai = 0; ai < n3; ++ai) {
             const Amp3Info &A = T.amp3s[ai];
             os << "  case " << ai << ": {\n";
             os << "    const double *x12 = a.dcol[(i64)toy * " << NO << " + " << A.o12 << "];\n";
@@ -1108,6 +1355,20 @@ struct Gen {
                 os << "      ac[" << A.col0 + r << "][i] = b" << r << ";\n";
             os << "    }\n    break; }\n";
         }
+        for(size_t k4 = 0; k4 < T.amp4s.size(); ++k4) {
+            const Amp4Info &A = T.amp4s[k4];
+            os << "  case " << n3 + (int)k4 << ": {\n";
+            for(int v = 0; v < 5; ++v)
+                os << "    const double *x" << v << " = a.dcol[(i64)toy * " << NO << " + " << A.obs[v] << "];\n";
+            os << "    double2 A[" << A.nAmp << "];\n";
+            os << "    for(i64 i = (i64)blockIdx.x * 256 + tid; i < npad; i += (i64)gridDim.x * 256) {\n";
+            os << "      if(i < n) gf_amp4_" << k4 << "(x0[i], x1[i], x2[i], x3[i], x4[i], P, A);\n";
+            os << "      else for(int q = 0; q < " << A.nAmp << "; ++q) A[q] = make_double2(0.0, 0.0);\n";
+            for(int q = 0; q < A.nAmp; ++q)
+                os << "      { R2 b; b.x = (R)A[" << q << "].x; b.y = (R)A[" << q << "].y; ac[" << A.col0 + q
+                   << "][i] = b; }\n";
+            os << "    }\n    break; }\n";
+        }
         os << "  default: break;\n  }\n}\n\n";
 
         // integrals: tiles of at most 36 pairs per CTA row
@@ -1115,15 +1376,17 @@ struct Gen {
         plan.gram_pairs_max = 0;
         plan.dgrid_off.clear();
         int64_t goff = 0;
-        for(size_t ai = 0; ai < T.amp3s.size(); ++ai) {
-            const int n = T.amp3s[ai].nRes, npairs = n * (n + 1) / 2;
+        for(int ai = 0; ai < NAN_; ++ai) {
+            const int n = T.amp_count(ai), npairs = n * (n + 1) / 2;
             for(int p0 = 0; p0 < npairs; p0 += 36) {
-                KernelPlan::GramTile t{(int)ai, p0, std::min(npairs, p0 + 36)};
+                KernelPlan::GramTile t{ai, p0, std::min(npairs, p0 + 36)};
                 plan.gram_tiles.push_back(t);
                 plan.gram_pairs_max = std::max(plan.gram_pairs_max, t.p1 - t.p0);
             }
-            plan.dgrid_off.push_back(goff);
-            goff += (int64_t)T.amp3s[ai].grid.size();
+            if(ai < n3) {
+                plan.dgrid_off.push_back(goff);
+                goff += (int64_t)T.amp3s[ai].grid.size();
+            }
         }
         const int PM = plan.gram_pairs_max, NW = 256 / 32;
         os << "extern \"C\" __global__ void __launch_bounds__(256) gf_gram(const GfArgs a) {\n";
@@ -1138,49 +1401,69 @@ struct Gen {
            << 2 * PM << ";\n";
         os << "  switch(z) {\n";
         for(size_t ti = 0; ti < plan.gram_tiles.size(); ++ti) {
-            const auto &tile  = plan.gram_tiles[ti];
-            const Amp3Info &A = T.amp3s[tile.amp];
+            const auto &tile = plan.gram_tiles[ti];
+            const int nAmp   = T.amp_count(tile.amp);
             std::vector<std::pair<int, int>> pairs;
-            for(int i = 0, q = 0; i < A.nRes; ++i)
-                for(int j = i; j < A.nRes; ++j, ++q)
+            for(int i = 0, q = 0; i < nAmp; ++i)
+                for(int j = i; j < nAmp; ++j, ++q)
                     if(q >= tile.p0 && q < tile.p1)
                         pairs.push_back({i, j});
-            std::vector<int> need(A.nRes, 0);
+            std::vector<int> need(nAmp, 0);
             for(auto &pr : pairs)
                 need[pr.first] = need[pr.second] = 1;
             const int npr = (int)pairs.size();
-            const gf_observable &g12 = T.obs[A.o12], &g13 = T.obs[A.o13];
-            double w12 = g12.hi - g12.lo;
-            w12 /= A.nb12;
-            double w13 = g13.hi - g13.lo;
-            w13 /= A.nb13q;
             os << "  case " << ti << ": {\n";
             for(int q = 0; q < npr; ++q)
                 os << "    R sr" << q << " = R(0), si" << q << " = R(0);\n";
-            os << "    const unsigned *pts = a.dgrid + " << plan.dgrid_off[tile.amp] << "LL;\n";
-            os << "    for(int p = blockIdx.x * 256 + tid; p < " << A.grid.size() << "; p += gridDim.x * 256) {\n";
-            os << "      const unsigned q = pts[p];\n";
-            os << "      const double c12 = gf_centre(" << lit(g12.lo) << ", " << lit(w12) << ", (int)(q & 0xffffu));\n";
-            os << "      const double c13 = gf_centre(" << lit(g13.lo) << ", " << lit(w13) << ", (int)(q >> 16));\n";
-            os << "      const double m23 = gf_m23(c12, c13, " << dalitzArgs(A) << ");\n";
-            for(int r = 0; r < A.nRes; ++r)
-                if(need[r])
-                    os << "      const R2 b" << r << " = " << resCall(A, r, "c12", "c13", "m23") << ";\n";
-            // the efficiency at the bin centre; the reference's fake event holds 2 in slot 0
-            std::ostringstream body;
-            Ctx c{body, T, false, false, nullptr, nullptr, nullptr, nullptr};
-            c.x = [&](int o) -> std::string {
-                if(o == A.o12)
-                    return "((R)c12)";
-                if(o == A.o13)
-                    return "((R)c13)";
-                return "R(2)";
-            };
-            c.k   = [&](int) -> std::string { throw std::runtime_error("codegen: convolution in an efficiency"); };
-            c.tab = [&](int, int) -> std::string { throw std::runtime_error("codegen: convolution in an efficiency"); };
-            Val ev = emit(c, A.eff);
-            os << "      {\n" << body.str();
-            os << "      const R e = " << ev.v << ";\n";
+            std::string effv = "R(1)";
+            if(tile.amp < n3) {
+                const Amp3Info &A = T.amp3s[tile.amp];
+                const gf_observable &g12 = T.obs[A.o12], &g13 = T.obs[A.o13];
+                double w12 = g12.hi - g12.lo;
+                w12 /= A.nb12;
+                double w13 = g13.hi - g13.lo;
+                w13 /= A.nb13q;
+                os << "    const unsigned *pts = a.dgrid + " << plan.dgrid_off[tile.amp] << "LL;\n";
+                os << "    for(int p = blockIdx.x * 256 + tid; p < " << A.grid.size() << "; p += gridDim.x * 256) {\n";
+                os << "      const unsigned q = pts[p];\n";
+                os << "      const double c12 = gf_centre(" << lit(g12.lo) << ", " << lit(w12) << ", (int)(q & 0xffffu));\n";
+                os << "      const double c13 = gf_centre(" << lit(g13.lo) << ", " << lit(w13) << ", (int)(q >> 16));\n";
+                os << "      const double m23 = gf_m23(c12, c13, " << dalitzArgs(A) << ");\n";
+                for(int r = 0; r < A.nRes; ++r)
+                    if(need[r])
+                        os << "      const R2 b" << r << " = " << resCall(A, r, "c12", "c13", "m23") << ";\n";
+                // the efficiency at the bin centre; the reference's fake event holds 2 in slot 0
+                std::ostringstream body;
+                Ctx c{body, T, false, false, nullptr, nullptr, nullptr, nullptr};
+                c.x = [&](int o) -> std::string {
+                    if(o == A.o12)
+                        return "((R)c12)";
+                    if(o == A.o13)
+                        return "((R)c13)";
+                    return "R(2)";
+                };
+                c.k   = [&](int) -> std::string { throw std::runtime_error("codegen: convolution in an efficiency"); };
+                c.tab = [&](int, int) -> std::string { throw std::runtime_error("codegen: convolution in an efficiency"); };
+                Val ev = emit(c, A.eff);
+                os << "      {\n" << body.str();
+                effv = ev.v;
+            } else {
+                // Amp4Body: the flat phase-space events; the efficiency does not enter
+                // (NormIntegrator, src/PDFs/physics/detail/NormIntegrator.cu:15-68)
+                const int k4 = tile.amp - n3;
+                const Amp4Info &A = T.amp4s[k4];
+                os << "    const double *ne = a.nevt[" << k4 << "];\n";
+                os << "    const i64 nn = a.nnorm[" << k4 << "];\n";
+                os << "    double2 A[" << A.nAmp << "];\n";
+                os << "    for(i64 p = (i64)blockIdx.x * 256 + tid; p < nn; p += (i64)gridDim.x * 256) {\n";
+                os << "      gf_amp4_" << k4 << "(ne[p], ne[nn + p], ne[2 * nn + p], ne[3 * nn + p], ne[4 * nn + p], P, A);\n";
+                for(int r = 0; r < nAmp; ++r)
+                    if(need[r])
+                        os << "      R2 b" << r << "; b" << r << ".x = (R)A[" << r << "].x; b" << r << ".y = (R)A[" << r
+                           << "].y;\n";
+                os << "      {\n";
+            }
+            os << "      const R e = " << effv << ";\n";
             for(int q = 0; q < npr; ++q) {
                 int i = pairs[q].first, j = pairs[q].second;
                 os << "      sr" << q << " += (b" << i << ".x * b" << j << ".x + b" << i << ".y * b" << j << ".y) * e;\n";
@@ -1241,7 +1524,7 @@ struct Gen {
                 return "tq" + std::to_string(ci) + fld[comp];
             return "tq" + std::to_string(ci) + "_" + std::to_string(comp / 4) + fld[comp % 4];
         };
-        c.amp = [&](int ai, int r) { return "am" + std::to_string(T.amp3s[ai].col0 + r); };
+        c.amp = [&](int ai, int r) { return "am" + std::to_string(T.amp_col0(ai) + r); };
         Val root = emit(c, 0);
         if(!values && !grad) {
             plan.obs_used_evt.clear();
@@ -1466,6 +1749,8 @@ KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, int chunk)
     g.os << kPrelude;
     if(!t.amp3s.empty())
         g.os << kPreludeAmp;
+    if(!t.amp4s.empty())
+        g.os << kPreludeAmp4;
     if(mixed)
         g.os << kPreludeF32;
     else

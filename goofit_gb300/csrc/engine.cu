@@ -150,6 +150,15 @@ void freeLayout(gf_engine *e) {
     e->layout_ready = false;
 }
 
+void freeNormEvents(gf_engine *e) {
+    for(auto &b : e->norm_buf)
+        dfree(b);
+    e->norm_buf.clear();
+    e->norm_n.clear();
+    dfree(e->d_nevt);
+    dfree(e->d_nnorm);
+}
+
 void freeModule(gf_engine *e) {
     if(e->mod.lib)
         cudaLibraryUnload(e->mod.lib);
@@ -337,6 +346,8 @@ GfArgs makeArgs(gf_engine *e) {
     a.dgrid       = e->d_dgrid;
     a.gram        = e->d_gram;
     a.dirty       = e->d_dirty;
+    a.nevt        = (const double *const *)e->d_nevt;
+    a.nnorm       = e->d_nnorm;
     a.n_chunks    = e->n_chunks;
     a.n_toys      = e->n_toys;
     a.metric      = 1;
@@ -454,7 +465,7 @@ int loadModule(gf_engine *e) {
        (rc = get(e->mod.evt_g, "gf_evt_g", true)) || (rc = get(e->mod.evt_n, "gf_evt_n", true)) ||
        (rc = get(e->mod.val_n, "gf_val_n", true)))
         return rc;
-    const bool hasAmp = !e->tree.amp3s.empty();
+    const bool hasAmp = e->tree.n_amp_nodes() > 0;
     if((rc = get(e->mod.amp, "gf_amp", hasAmp)) || (rc = get(e->mod.gram, "gf_gram", hasAmp)))
         return rc;
     auto smem = [&](cudaKernel_t k, size_t bytes) -> int {
@@ -475,8 +486,15 @@ int loadModule(gf_engine *e) {
     return GF_OK;
 }
 
-// binSizeFactor of Amp3Body::normalize (src/PDFs/physics/Amp3Body.cu:350-353).
-double amp3BinSize(const gf::Tree &T, int node) {
+// Scale of an amplitude node's quadratic form: binSizeFactor of Amp3Body::normalize
+// (src/PDFs/physics/Amp3Body.cu:350-353), or 1 / (number of normalisation events) for Amp4Body
+// (src/PDFs/physics/Amp4Body.cu:542-545).
+double ampScale(const gf_engine *e, int node) {
+    const gf::Tree &T = e->tree;
+    if(T.amp3_of[node] < 0) {
+        const int k4 = T.amp4_of[node];
+        return k4 < (int)e->norm_n.size() && e->norm_n[k4] > 0 ? 1.0 / (double)e->norm_n[k4] : NAN;
+    }
     const gf::Amp3Info &A = T.amp3s[T.amp3_of[node]];
     const gf_observable &o12 = T.obs[A.o12], &o13 = T.obs[A.o13];
     double f = 1;
@@ -485,28 +503,29 @@ double amp3BinSize(const gf::Tree &T, int node) {
     return f;
 }
 
-// Amp3Body normalisation integral (src/PDFs/physics/Amp3Body.cu:334-356): the real part of
-// sum_ij c_i conj(c_j) I_ij times the bin size factor, from the cached integrals; dQ[k] receives the
-// derivative of the real part with respect to the k-th entry of an.dN (before the bin size factor).
-double amp3Integral(const gf_engine *e, int t, int node, const double *P, const gf::NormLayout::Analytic &an,
-                    double *dQ) {
+// Normalisation integral of an amplitude node (Amp3Body.cu:334-356, Amp4Body.cu:531-545): the real part
+// of sum_ij c_i conj(c_j) I_ij times the node's scale, from the cached integrals; dQ[k] receives the
+// derivative of the real part with respect to the k-th entry of an.dN (before the scale).
+double ampIntegral(const gf_engine *e, int t, int node, const double *P, const gf::NormLayout::Analytic &an,
+                   double *dQ) {
     typedef std::complex<double> C;
-    const gf::Tree &T     = e->tree;
-    const gf::TNode &nd   = T.nodes[node];
-    const int n           = T.amp3s[T.amp3_of[node]].nRes;
-    if((int)e->toys[t].amp_I.size() <= T.amp3_of[node]) { // integrals not built yet for this toy
+    const gf::Tree &T   = e->tree;
+    const gf::TNode &nd = T.nodes[node];
+    const int ai        = T.amp_index(node);
+    const int n         = T.amp_count(ai);
+    if((int)e->toys[t].amp_I.size() <= ai) { // integrals not built yet for this toy
         for(size_t k = 0; k < an.dN.size() && k < 64; ++k)
             dQ[k] = 0;
         return NAN;
     }
-    const std::vector<double> &I = e->toys[t].amp_I[T.amp3_of[node]];
+    const std::vector<double> &I = e->toys[t].amp_I[ai];
     auto Iij = [&](int i, int j) { return C(I[2 * (i * n + j)], I[2 * (i * n + j) + 1]); };
     C sum(0, 0);
     for(int i = 0; i < n; ++i) {
-        C ai(P[nd.params[2 * i]], P[nd.params[2 * i + 1]]);
+        C ai_(P[nd.params[2 * i]], P[nd.params[2 * i + 1]]);
         for(int j = 0; j < n; ++j) {
             C aj(P[nd.params[2 * j]], -P[nd.params[2 * j + 1]]);
-            sum += ai * aj * Iij(i, j);
+            sum += ai_ * aj * Iij(i, j);
         }
     }
     for(size_t k = 0; k < an.dN.size() && k < 64; ++k) {
@@ -525,7 +544,7 @@ double amp3Integral(const gf_engine *e, int t, int node, const double *P, const 
         dQ[k] = d.real();
     }
     double ret = sum.real();
-    ret *= amp3BinSize(T, node);
+    ret *= ampScale(e, node);
     return ret;
 }
 
@@ -549,10 +568,10 @@ void fillRecordsT(gf_engine *e) {
             r[j] = (R)P[j];
         for(auto &an : nl.analytic) {
             const gf::TNode &nd = T.nodes[an.node];
-            if(an.kind == gf::NK_AMP3) {
+            if(an.kind == gf::NK_AMP3 || an.kind == gf::NK_AMP4) {
                 double dQ[64];
-                const double Iv = amp3Integral(e, t, an.node, P, an, dQ);
-                const double f  = amp3BinSize(T, an.node);
+                const double Iv = ampIntegral(e, t, an.node, P, an, dQ);
+                const double f  = ampScale(e, an.node);
                 const double N  = 1.0 / Iv;
                 r[an.slotN]     = (R)N;
                 for(size_t k = 0; k < an.dN.size(); ++k)
@@ -612,13 +631,18 @@ void fillRecords(gf_engine *e) {
 // evaluations that follow read the caches and the host copies of the integrals.
 int updateAmpCaches(gf_engine *e) {
     const gf::Tree &T = e->tree;
-    if(T.amp3s.empty())
+    const int NAN_    = T.n_amp_nodes();
+    if(NAN_ == 0)
         return GF_OK;
+    for(size_t k = 0; k < T.amp4s.size(); ++k)
+        if(k >= e->norm_n.size() || e->norm_n[k] <= 0)
+            return gf_fail(e, GF_ERR_STATE, "Amp4Body node " + std::to_string(T.amp4s[k].node) +
+                                                " has no normalisation events (gf_set_norm_events)");
     const int NT = e->n_toys, np = T.n_params, NTILE = (int)e->plan.gram_tiles.size();
     const int PM2 = 2 * e->plan.gram_pairs_max;
     std::vector<int> cp;
-    for(auto &A : T.amp3s)
-        cp.insert(cp.end(), A.cache_params.begin(), A.cache_params.end());
+    for(int k = 0; k < NAN_; ++k)
+        cp.insert(cp.end(), T.amp_cache_params(k).begin(), T.amp_cache_params(k).end());
     std::sort(cp.begin(), cp.end());
     cp.erase(std::unique(cp.begin(), cp.end()), cp.end());
     bool any = false;
@@ -647,7 +671,7 @@ int updateAmpCaches(gf_engine *e) {
         r = cudaMemcpyAsync(e->d_dirty, e->h_dirty, sizeof(int) * NT, cudaMemcpyHostToDevice, e->stream);
     if(r == cudaSuccess) {
         const int64_t bx = std::min<int64_t>((maxpad + 255) / 256, (int64_t)std::max(1, e->sm_count) * 8);
-        r = launch(e->mod.amp, dim3((unsigned)bx, NT, (unsigned)T.amp3s.size()), dim3(256), 0, e->stream, a);
+        r = launch(e->mod.amp, dim3((unsigned)bx, NT, (unsigned)NAN_), dim3(256), 0, e->stream, a);
     }
     if(r == cudaSuccess)
         r = launch(e->mod.gram, dim3(e->gram_blocks, NT, NTILE), dim3(256), 0, e->stream, a);
@@ -662,13 +686,13 @@ int updateAmpCaches(gf_engine *e) {
         if(!e->h_dirty[t])
             continue;
         GfToy &ty = e->toys[t];
-        ty.amp_I.assign(T.amp3s.size(), {});
-        for(size_t ai = 0; ai < T.amp3s.size(); ++ai) {
-            const int n = T.amp3s[ai].nRes;
+        ty.amp_I.assign(NAN_, {});
+        for(int ai = 0; ai < NAN_; ++ai) {
+            const int n = T.amp_count(ai);
             std::vector<double> I(2 * (size_t)n * n, 0.0);
             for(int z = 0; z < NTILE; ++z) {
                 const auto &tile = e->plan.gram_tiles[z];
-                if(tile.amp != (int)ai)
+                if(tile.amp != ai)
                     continue;
                 for(int i = 0, q = 0; i < n; ++i)
                     for(int j = i; j < n; ++j, ++q) {
@@ -839,6 +863,7 @@ int gf_engine_destroy(gf_engine *e) {
     freeLayout(e);
     for(auto &t : e->toys)
         freeToy(t);
+    freeNormEvents(e);
     dfree(e->d_vals);
     dfree(e->d_stage);
     dfree(e->d_uperr);
@@ -865,8 +890,19 @@ int gf_set_tree(gf_engine *e, const gf_node *nodes, int n_nodes, const gf_observ
     freeLayout(e);
     for(auto &ty : e->toys)
         freeToy(ty);
+    freeNormEvents(e);
     e->tree     = t;
     e->has_tree = false;
+    if(!t.amp4s.empty()) {
+        const size_t k = t.amp4s.size();
+        e->norm_buf.assign(k, nullptr);
+        e->norm_n.assign(k, 0);
+        int rc = dalloc(e, e->d_nevt, k);
+        if(!rc)
+            rc = dalloc(e, e->d_nnorm, k);
+        if(rc)
+            return rc;
+    }
     try {
         e->plan = gf::generate_kernels(e->tree, e->precision == GF_MIXED, e->block, e->chunk);
     } catch(std::exception &ex) {
@@ -929,6 +965,10 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
             std::vector<int> dob;
             for(auto &A : T.amp3s)
                 for(int o : {A.o12, A.o13})
+                    if(std::find(dob.begin(), dob.end(), o) == dob.end())
+                        dob.push_back(o);
+            for(auto &A : T.amp4s)
+                for(int o : A.obs)
                     if(std::find(dob.begin(), dob.end(), o) == dob.end())
                         dob.push_back(o);
             const bool mixed = e->precision == GF_MIXED;
@@ -1150,7 +1190,7 @@ int gf_normalize(gf_engine *e, int toy, double *integral, double *norm) {
     std::vector<char> forced(n, 0);
     for(int i = 0; i < n; ++i) {
         const gf::TNode &nd = T.nodes[i];
-        bool f = forced[i] || (nd.op == GF_OP_CONVOLUTION) || (nd.op == GF_OP_AMP3BODY) ||
+        bool f = forced[i] || (nd.op == GF_OP_CONVOLUTION) || (nd.op == GF_OP_AMP3BODY) || (nd.op == GF_OP_AMP4BODY) ||
                  (nd.op == GF_OP_PROD && T.nk[i] == gf::NK_NUMERIC);
         for(int c : nd.children)
             forced[c] = forced[c] || f;
@@ -1172,10 +1212,11 @@ int gf_normalize(gf_engine *e, int toy, double *integral, double *norm) {
             N[i] = 1.0 / s;
             break;
         }
-        case gf::NK_AMP3: {
+        case gf::NK_AMP3:
+        case gf::NK_AMP4: {
             gf::NormLayout::Analytic none;
             none.node = i;
-            I[i]      = amp3Integral(e, toy, i, P, none, nullptr);
+            I[i]      = ampIntegral(e, toy, i, P, none, nullptr);
             N[i]      = 1.0 / I[i];
             break;
         }
@@ -1333,18 +1374,46 @@ int gf_launches_per_eval(const gf_engine *e, int) {
     return 1 + (e->tree.convs.empty() ? 0 : 1) + (e->tree.nums.empty() ? 0 : 1);
 }
 
+int gf_set_norm_events(gf_engine *e, int node, const double *soa5, int64_t n) {
+    if(!e || !e->has_tree)
+        return gf_fail(e, GF_ERR_STATE, "no tree");
+    if(node < 0 || node >= (int)e->tree.nodes.size() || e->tree.amp4_of[node] < 0)
+        return gf_fail(e, GF_ERR_INVALID, "not an Amp4Body node");
+    if(n <= 0 || !soa5)
+        return gf_fail(e, GF_ERR_INVALID, "normalisation events: n must be positive");
+    cudaSetDevice(e->device);
+    const int k = e->tree.amp4_of[node];
+    dfree(e->norm_buf[k]);
+    e->norm_n[k] = 0;
+    int rc = dalloc(e, e->norm_buf[k], (size_t)5 * n, false);
+    if(rc)
+        return rc;
+    cudaError_t r = cudaMemcpy(e->norm_buf[k], soa5, sizeof(double) * 5 * (size_t)n, cudaMemcpyHostToDevice);
+    const long long nn = n;
+    if(r == cudaSuccess)
+        r = cudaMemcpy(e->d_nevt + k, &e->norm_buf[k], sizeof(double *), cudaMemcpyHostToDevice);
+    if(r == cudaSuccess)
+        r = cudaMemcpy(e->d_nnorm + k, &nn, sizeof(long long), cudaMemcpyHostToDevice);
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "normalisation events");
+    e->norm_n[k] = n;
+    for(auto &ty : e->toys)
+        ty.amp_valid = false;
+    return GF_OK;
+}
+
 static int ampNode(gf_engine *e, int toy, int node, int *ai) {
     if(!e || !e->has_tree)
         return gf_fail(e, GF_ERR_STATE, "no tree");
-    if(toy < 0 || toy >= e->n_toys || node < 0 || node >= (int)e->tree.nodes.size() || e->tree.amp3_of[node] < 0)
-        return gf_fail(e, GF_ERR_INVALID, "not an Amp3Body node, or toy index out of range");
+    if(toy < 0 || toy >= e->n_toys || node < 0 || node >= (int)e->tree.nodes.size() || e->tree.amp_index(node) < 0)
+        return gf_fail(e, GF_ERR_INVALID, "not an Amp3Body or Amp4Body node, or toy index out of range");
     cudaSetDevice(e->device);
     int rc = buildLayout(e);
     if(rc)
         return rc;
     for(int t = 0; t < e->n_toys; ++t)
         e->h_active[t] = (t == toy);
-    *ai = e->tree.amp3_of[node];
+    *ai = e->tree.amp_index(node);
     return updateAmpCaches(e);
 }
 
@@ -1363,15 +1432,15 @@ int gf_amp3_cached_wave(gf_engine *e, int toy, int node, int res, double *out, i
     int ai = -1, rc = ampNode(e, toy, node, &ai);
     if(rc)
         return rc;
-    const gf::Amp3Info &A = e->tree.amp3s[ai];
-    GfToy &ty             = e->toys[toy];
-    if(res < 0 || res >= A.nRes || !out || n_out < ty.n)
+    GfToy &ty = e->toys[toy];
+    if(res < 0 || res >= e->tree.amp_count(ai) || !out || n_out < ty.n)
         return gf_fail(e, GF_ERR_INVALID, "bad resonance index or output size");
     const size_t rs = rsize(e);
     std::vector<char> buf((size_t)std::max<int64_t>(1, ty.n) * 2 * rs);
     cudaError_t r = cudaSuccess;
     if(ty.n > 0)
-        r = cudaMemcpyAsync(buf.data(), ty.acols[A.col0 + res], (size_t)ty.n * 2 * rs, cudaMemcpyDeviceToHost, e->stream);
+        r = cudaMemcpyAsync(buf.data(), ty.acols[e->tree.amp_col0(ai) + res], (size_t)ty.n * 2 * rs,
+                            cudaMemcpyDeviceToHost, e->stream);
     if(r == cudaSuccess)
         r = cudaStreamSynchronize(e->stream);
     if(r != cudaSuccess)

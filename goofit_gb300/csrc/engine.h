@@ -35,6 +35,8 @@ struct GfArgs {
     const unsigned *dgrid;
     double *gram;
     const int *dirty;
+    const double *const *nevt;
+    const long long *nnorm;
     int n_chunks;
     int n_toys;
     int metric;
@@ -109,6 +111,11 @@ struct gf_engine {
     double *h_gram = nullptr;
     int *d_dirty = nullptr, *h_dirty = nullptr;
     int gram_blocks = 0;
+    // Amp4Body normalisation events, one FP64 SoA [5][n] buffer per Amp4Body node (gf_set_norm_events)
+    std::vector<double *> norm_buf;
+    std::vector<int64_t> norm_n;
+    double **d_nevt = nullptr;
+    long long *d_nnorm = nullptr;
     void *d_Nq = nullptr;   // [toy][nq] R numeric normalisation factors
     int *d_qflag = nullptr; // [toy]
     // pinned host mirrors; h_P is one block: [toy][n_params] FP64, then [toy][npr] R records

@@ -162,6 +162,24 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
         case GF_OP_RES_RBW: ok = P == 2 && n.consts.size() >= 3 && C == 0 && n.consts[0] >= 0 && n.consts[0] <= 2 &&
                                  n.consts[1] >= 0 && n.consts[1] <= 2; break;
         case GF_OP_RES_NONRES: ok = P == 0 && C == 0; break;
+        case GF_OP_AMP4BODY:
+            ok = n.consts.size() >= 5 && n.obs.size() >= 5 && C >= 2 && P == 2 * (C - 1);
+            break;
+        case GF_OP_AMPLITUDE:
+            ok = n.consts.size() >= 3 && n.consts[0] >= 1 && n.consts[1] >= 0 && n.consts[2] >= 0 && P == 0 &&
+                 (int)C == (int)n.consts[1] + (int)n.consts[2] && ((int)n.consts[1] % (int)n.consts[0]) == 0 &&
+                 ((int)n.consts[2] % (int)n.consts[0]) == 0;
+            break;
+        case GF_OP_LS_RBW:
+        case GF_OP_LS_SBW:
+            ok = P == 2 && C == 0 && n.consts.size() >= 4 && n.consts[0] >= 0 && n.consts[0] <= 17 && n.consts[1] >= 0 &&
+                 n.consts[1] <= 2 && n.consts[2] >= 0 && n.consts[2] <= 3;
+            break;
+        case GF_OP_SPINFACTOR:
+            ok = P == 0 && C == 0 && n.consts.size() >= 6 && n.consts[0] >= 0 && n.consts[0] <= 15;
+            for(int k = 2; ok && k < 6; ++k)
+                ok = n.consts[k] >= 0 && n.consts[k] <= 3;
+            break;
         case GF_OP_AMP3BODY:
             ok = n.consts.size() >= 8 && n.obs.size() >= 2 && C >= 2 && P == 2 * (C - 1) && (int)n.consts[0] == (int)C - 1;
             break;
@@ -224,7 +242,11 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
         } else if(n.op == GF_OP_AMP3BODY) {
             nk[i]       = NK_AMP3;
             childForced = true;
-        } else if(n.op == GF_OP_RES_RBW || n.op == GF_OP_RES_NONRES) {
+        } else if(n.op == GF_OP_AMP4BODY) {
+            nk[i]       = NK_AMP4;
+            childForced = true;
+        } else if(n.op == GF_OP_RES_RBW || n.op == GF_OP_RES_NONRES || n.op == GF_OP_AMPLITUDE ||
+                  n.op == GF_OP_LS_RBW || n.op == GF_OP_LS_SBW || n.op == GF_OP_SPINFACTOR) {
             nk[i] = NK_ONE;
         } else if(isExpOp(n.op) && n.params.size() == 1) {
             nk[i] = NK_EXP;
@@ -273,8 +295,17 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
             if(!dep_val[eff].empty())
                 return "Amp3Body: analytic gradients with respect to efficiency parameters are not provided";
         }
+        if(n.op == GF_OP_AMP4BODY) {
+            v = own;
+            for(size_t a = 0; a + 1 < n.children.size(); ++a)
+                if(!dep_val[n.children[a]].empty())
+                    return "Amp4Body: analytic gradients with respect to line-shape parameters are not provided; "
+                           "fix them or leave them out of the gradient mask";
+            if(!dep_val[n.children.back()].empty())
+                return "Amp4Body: analytic gradients with respect to efficiency parameters are not provided";
+        }
         dep_val[i] = v;
-        if(nk[i] == NK_AMP3) {
+        if(nk[i] == NK_AMP3 || nk[i] == NK_AMP4) {
             dep_norm[i] = own;
         } else if(nk[i] == NK_EXP) {
             int s = gslot[n.params[0]];
@@ -411,6 +442,75 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
     if(amp3s.size() > 4)
         return "at most 4 Amp3Body nodes per tree";
 
+    // Amp4Body nodes: distinct line shapes and spin factors (by operator, parameters and constants)
+    amp4_of.assign(n_nodes, -1);
+    amp4s.clear();
+    for(int i = 0; i < n_nodes; ++i) {
+        const TNode &n = nodes[i];
+        if(n.op != GF_OP_AMP4BODY)
+            continue;
+        Amp4Info a;
+        a.node = i;
+        a.nAmp = (int)n.children.size() - 1;
+        a.eff  = n.children.back();
+        for(int k = 0; k < 5; ++k)
+            a.obs[k] = n.obs[k];
+        a.M = n.consts[0];
+        for(int k = 0; k < 4; ++k)
+            a.m[k] = n.consts[1 + k];
+        auto same = [&](int x, int y) {
+            return nodes[x].op == nodes[y].op && nodes[x].params == nodes[y].params && nodes[x].consts == nodes[y].consts;
+        };
+        for(int k = 0; k < a.nAmp; ++k) {
+            const int an = n.children[k];
+            if(nodes[an].op != GF_OP_AMPLITUDE)
+                return "Amp4Body node " + std::to_string(i) + ": child " + std::to_string(k) + " must be an Amplitude";
+            const TNode &A = nodes[an];
+            Amp4Info::Amp am;
+            am.node  = an;
+            am.nPerm = (int)A.consts[0];
+            const int nLS = (int)A.consts[1];
+            for(size_t c = 0; c < A.children.size(); ++c) {
+                const int cn = A.children[c];
+                const bool isLS = (int)c < nLS;
+                const int want  = isLS ? 1 : 2;
+                const int op    = nodes[cn].op;
+                if((want == 1) != (op == GF_OP_LS_RBW || op == GF_OP_LS_SBW) || (want == 2) != (op == GF_OP_SPINFACTOR))
+                    return "Amplitude node " + std::to_string(an) + ": line shapes first, then spin factors";
+                std::vector<int> &uniq = isLS ? a.ls : a.sf;
+                int found = -1;
+                for(size_t u = 0; u < uniq.size(); ++u)
+                    if(same(uniq[u], cn))
+                        found = (int)u;
+                if(found < 0) {
+                    found = (int)uniq.size();
+                    uniq.push_back(cn);
+                }
+                (isLS ? am.ls : am.sf).push_back(found);
+            }
+            a.amps.push_back(am);
+        }
+        if(nodes[a.eff].op == GF_OP_AMPLITUDE)
+            return "Amp4Body node " + std::to_string(i) + ": the last child must be the efficiency";
+        for(int j = i + 1; j < n_nodes; ++j)
+            if(inSubtree(i, j)) {
+                if(nodes[j].op == GF_OP_CONVOLUTION || nodes[j].op == GF_OP_AMP3BODY || nodes[j].op == GF_OP_AMP4BODY)
+                    return "Amp4Body node " + std::to_string(i) + ": convolutions or amplitude PDFs below it are not supported";
+                if(inSubtree(a.eff, j))
+                    continue;
+                for(int p : nodes[j].params)
+                    a.cache_params.push_back(p);
+            }
+        std::sort(a.cache_params.begin(), a.cache_params.end());
+        a.cache_params.erase(std::unique(a.cache_params.begin(), a.cache_params.end()), a.cache_params.end());
+        a.col0 = n_amp_cols;
+        n_amp_cols += a.nAmp;
+        amp4_of[i] = (int)amp4s.size();
+        amp4s.push_back(a);
+    }
+    if(n_amp_cols > 64)
+        return "at most 64 amplitude columns (resonances and amplitudes) per tree";
+
     // numeric grids
     num_of.assign(n_nodes, -1);
     nums.clear();
@@ -419,8 +519,8 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
         if(nk[i] != NK_NUMERIC)
             continue;
         for(int j = i + 1; j < n_nodes; ++j)
-            if(inSubtree(i, j) && nodes[j].op == GF_OP_AMP3BODY)
-                return "a numerically normalised node cannot contain an Amp3Body";
+            if(inSubtree(i, j) && (nodes[j].op == GF_OP_AMP3BODY || nodes[j].op == GF_OP_AMP4BODY))
+                return "a numerically normalised node cannot contain an Amp3Body or Amp4Body";
         NumInfo g;
         g.node = i;
         g.obs  = nodes[i].obs;

@@ -18,8 +18,10 @@ enum NormKind {
     NK_EXP     = 1, // ExpPdf::integrate        (src/PDFs/basic/ExpPdf.cu:121-132)
     NK_GAUSS   = 2, // GaussianPdf::integrate   (src/PDFs/basic/GaussianPdf.cu:28-35)
     NK_NUMERIC = 3, // grid sum                 (src/PDFs/GooPdf.cu:366-395)
-    NK_AMP3    = 4  // Amp3Body::normalize: c^H I c over the cached resonance integrals
+    NK_AMP3    = 4, // Amp3Body::normalize: c^H I c over the cached resonance integrals
                     // (src/PDFs/physics/Amp3Body.cu:238-359), evaluated on the host
+    NK_AMP4    = 5  // Amp4Body::normalize: c^H G c / N over the flat phase-space events
+                    // (src/PDFs/physics/Amp4Body.cu:398-558), evaluated on the host
 };
 
 struct TNode {
@@ -55,6 +57,22 @@ struct Amp3Info {
     std::vector<uint32_t> grid;    // in-Dalitz normalisation bins, b12 | b13 << 16 (FP64 inDalitz)
 };
 
+// One Amp4Body node (src/PDFs/physics/Amp4Body.cu:94-292): amplitudes built from line shapes and spin
+// factors, both de-duplicated by value across amplitudes as the constructor does (lines 122-158).
+struct Amp4Info {
+    int node = -1, nAmp = 0, eff = -1;
+    int obs[5] = {-1, -1, -1, -1, -1}; // m12, m34, cos12, cos34, phi
+    double M = 0, m[4] = {0, 0, 0, 0};
+    std::vector<int> ls, sf; // representative node of every distinct line shape / spin factor
+    struct Amp {
+        int node = -1, nPerm = 1;
+        std::vector<int> ls, sf; // indices into Amp4Info::ls / sf, in the amplitude's child order
+    };
+    std::vector<Amp> amps;
+    int col0 = 0;                  // first amplitude column of this node
+    std::vector<int> cache_params; // line-shape (and efficiency) parameters
+};
+
 // inDalitz (src/PDFs/physics/DalitzPlotHelpers.cu:14-59), FP64 without contraction.
 bool in_dalitz(double m12, double m13, double bigM, double dm1, double dm2, double dm3);
 
@@ -87,6 +105,19 @@ struct Tree {
     std::vector<int> kgrid;  // host copy of all grid k tables
     std::vector<Amp3Info> amp3s;
     std::vector<int> amp3_of; // node -> index in amp3s or -1
+    std::vector<Amp4Info> amp4s;
+    std::vector<int> amp4_of; // node -> index in amp4s or -1
+    // amplitude nodes of both kinds share one numbering: Amp3Body nodes first, then Amp4Body nodes
+    int n_amp_nodes() const { return (int)(amp3s.size() + amp4s.size()); }
+    int amp_index(int node) const {
+        return amp3_of[node] >= 0 ? amp3_of[node] : (amp4_of[node] >= 0 ? (int)amp3s.size() + amp4_of[node] : -1);
+    }
+    int amp_count(int k) const { return k < (int)amp3s.size() ? amp3s[k].nRes : amp4s[k - amp3s.size()].nAmp; }
+    int amp_node(int k) const { return k < (int)amp3s.size() ? amp3s[k].node : amp4s[k - amp3s.size()].node; }
+    int amp_col0(int k) const { return k < (int)amp3s.size() ? amp3s[k].col0 : amp4s[k - amp3s.size()].col0; }
+    const std::vector<int> &amp_cache_params(int k) const {
+        return k < (int)amp3s.size() ? amp3s[k].cache_params : amp4s[k - amp3s.size()].cache_params;
+    }
     int n_amp_cols = 0;       // complex amplitude columns per toy
     bool extended_root = false;
 

@@ -190,6 +190,11 @@ class Engine:
         self._check(self._L.gf_eval_events(self._h, toy, 0, metric, out.ctypes.data_as(A._f64p), n))
         return out[:n]
 
+    def set_norm_events(self, node: int, soa5: np.ndarray) -> None:
+        """Flat phase-space normalisation events (5, n) of Amp4Body node `node`."""
+        a = np.ascontiguousarray(soa5, dtype=np.float64)
+        self._check(self._L.gf_set_norm_events(self._h, node, a.ctypes.data_as(A._f64p), a.shape[1]))
+
     def amp3_integrals(self, node: int, n_res: int, toy: int = 0) -> np.ndarray:
         """Amp3Body normalisation integrals I_ij (n x n complex) at the toy's current parameters."""
         out = np.zeros(2 * n_res * n_res)

@@ -16,6 +16,13 @@ C3  Amp3Body for a 1.865 GeV parent to daughters of 0.4937 (K), 0.13957 (pi) and
     U[0.1, 2] and phase U[0, 2 pi) (the first one fixed: the overall scale and phase are not measurable);
     m12 = m^2(K pi), m13 = m^2(K pi0) on [0, 3] GeV^2 with 1500 x 1500 normalisation bins; constant
     efficiency; 5e5 events by accept-reject on the model density evaluated by the FP64 engine (needs a GPU).
+C5  Amp4Body for a 1.865 GeV parent to (pi+, pi-, K-, pi+) with masses (0.13957, 0.13957, 0.4937, 0.13957)
+    GeV (the daughter order of the reference's DP4 example); observables (m12, m34, cos12, cos34, phi,
+    eventNumber); 6 Bose-symmetrised decay chains with BW/SBW line shapes (masses 0.5-1.5 GeV, widths
+    0.05-0.4 GeV): K*rho in S, P and D wave (vector-vector), K1(1270) -> rho K and a1(1260) -> rho pi
+    (axial-vector + pseudoscalar), K* f0(500) (vector + scalar); seeded coefficients with magnitude
+    U[0.1, 2] and phase U[0, 2 pi) (the first fixed); 2,000,000 flat phase-space normalisation events;
+    300,000 events by accept-reject on the model density evaluated by the FP64 engine (needs a GPU).
 """
 from __future__ import annotations
 
@@ -248,3 +255,126 @@ def make_c3(n: int = 500_000, seed: int = 3, bins: int = 1500, n_res: int = 8, d
     # start 5% away from the truth
     start = {k: v * 1.05 for k, v in truth.items()}
     return Workload(f"c3-amp3body-{n}", pdf, ds, truth, start, variables, obs)
+
+
+C5_M = 1.865
+C5_MASSES = [0.13957, 0.13957, 0.4937, 0.13957]
+
+
+def c5_model(n_norm: int = 2_000_000, coef_seed: int = 5, norm_seed: int = 55, float_lineshapes: bool = False):
+    """The C5 Amp4Body tree (no data attached); returns (pdf, variables, observables, lineshape variables)."""
+    m12 = G.Observable("m12", 0, 3)
+    m34 = G.Observable("m34", 0, 3)
+    c12 = G.Observable("cos12", -1, 1)
+    c34 = G.Observable("cos34", -1, 1)
+    phi = G.Observable("phi", -3.5, 3.5)
+    evt = G.EventNumber("eventNumber")
+    obs = [m12, m34, c12, c34, phi, evt]
+    d = G.DecayInfo4()
+    d.particle_masses = [C5_M] + C5_MASSES
+    d.meson_radius = 1.5
+
+    def var(name, v):
+        return G.Variable(name, v, 0.01 * v, 0.5 * v, 1.5 * v) if float_lineshapes else G.Variable(name, v)
+
+    ls_vars = {k: var(k, v) for k, v in [("rho_mass", 0.775), ("rho_width", 0.149), ("Kst_mass", 0.892),
+                                           ("Kst_width", 0.050), ("K1_mass", 1.272), ("K1_width", 0.090),
+                                           ("a1_mass", 1.230), ("a1_width", 0.400), ("f0_mass", 0.500),
+                                           ("f0_width", 0.400)]}
+    V = ls_vars
+    RBW, SBW, SF = G.Lineshapes.RBW, G.Lineshapes.SBW, G.SpinFactor
+    P = G.DP4Pair
+
+    def krho():
+        return [RBW("rho(770)", V["rho_mass"], V["rho_width"], 1, P.M_12),
+                RBW("K*(892)", V["Kst_mass"], V["Kst_width"], 1, P.M_34),
+                RBW("rho(770)", V["rho_mass"], V["rho_width"], 1, P.M_24),
+                RBW("K*(892)", V["Kst_mass"], V["Kst_width"], 1, P.M_13)]
+
+    def sf(kind, a, b):
+        return [SF("SF", kind, C5_M, *a), SF("SF", kind, C5_M, *b)]
+
+    S4 = G.SF_4Body
+    chains = [
+        ("K*rho_S", krho(), sf(S4.DtoV1V2_V1toP1P2_V2toP3P4_S, (0, 1, 2, 3), (3, 1, 2, 0))),
+        ("K*rho_P", krho(), sf(S4.DtoV1V2_V1toP1P2_V2toP3P4_P, (0, 1, 2, 3), (3, 1, 2, 0))),
+        ("K*rho_D", krho(), sf(S4.DtoV1V2_V1toP1P2_V2toP3P4_D, (0, 1, 2, 3), (3, 1, 2, 0))),
+        ("K1rho", [SBW("K1(1270)", V["K1_mass"], V["K1_width"], 0, P.M_12_3),
+                   RBW("rho(770)", V["rho_mass"], V["rho_width"], 1, P.M_12),
+                   SBW("K1(1270)", V["K1_mass"], V["K1_width"], 0, P.M_24_3),
+                   RBW("rho(770)", V["rho_mass"], V["rho_width"], 1, P.M_24)],
+         sf(S4.DtoAP1_AtoVP2_VtoP3P4, (3, 2, 0, 1), (0, 2, 3, 1))),
+        ("a1rho", [SBW("a1(1260)", V["a1_mass"], V["a1_width"], 0, P.M_12_4),
+                   RBW("rho(770)", V["rho_mass"], V["rho_width"], 1, P.M_12),
+                   SBW("a1(1260)", V["a1_mass"], V["a1_width"], 0, P.M_24_1),
+                   RBW("rho(770)", V["rho_mass"], V["rho_width"], 1, P.M_24)],
+         sf(S4.DtoAP1_AtoVP2_VtoP3P4, (2, 3, 0, 1), (2, 0, 3, 1))),
+        ("K*f0", [RBW("K*(892)", V["Kst_mass"], V["Kst_width"], 1, P.M_34),
+                  RBW("f0(500)", V["f0_mass"], V["f0_width"], 0, P.M_12),
+                  RBW("K*(892)", V["Kst_mass"], V["Kst_width"], 1, P.M_13),
+                  RBW("f0(500)", V["f0_mass"], V["f0_width"], 0, P.M_24)],
+         sf(S4.DtoVS_VtoP1P2_StoP3P4, (2, 3, 0, 1), (2, 0, 3, 1))),
+    ]
+    rng = np.random.Generator(np.random.PCG64(coef_seed))
+    mag = rng.uniform(0.1, 2.0, len(chains))
+    ph = rng.uniform(0.0, 2 * np.pi, len(chains))
+    variables = {}
+    for k, (name, ls, sfs) in enumerate(chains):
+        re, im = mag[k] * np.cos(ph[k]), mag[k] * np.sin(ph[k])
+        if k == 0:
+            ar, ai = G.Variable(f"{name}_re", re), G.Variable(f"{name}_im", im)
+        else:
+            ar = G.Variable(f"{name}_re", re, 0.01, 0, 0)
+            ai = G.Variable(f"{name}_im", im, 0.01, 0, 0)
+            variables[ar.name], variables[ai.name] = ar, ai
+        d.amplitudes.append(G.Amplitude(name, ar, ai, ls, sfs, 2))
+    eff = G.PolynomialPdf("constantEff", [m12, m34], [G.Variable("constantOne", 1)],
+                          [G.Variable("constantZero0", 0), G.Variable("constantZero1", 0)], 0)
+    pdf = G.Amp4Body("DK3pi", obs, d, eff, n_norm, norm_seed)
+    return pdf, variables, obs, ls_vars
+
+
+def c5_generate(pdf, n: int, seed: int, batch: int = 2_000_000) -> np.ndarray:
+    """Accept-reject sample of the Amp4Body density over flat phase space; weights from the FP64 engine's
+    per-event values.  Returns a (6, n) array [m12, m34, cos12, cos34, phi, eventNumber]."""
+    from . import phasespace
+    from .engine import Engine
+    from . import _abi as A
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nodes, params, obs = pdf._flatten()
+    eng = Engine("fp64")
+    eng.set_tree(nodes, [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs],
+                 len(params), [0] * len(params))
+    for i, p in enumerate(pdf._flat_order):
+        p._engine_setup(eng, i)
+    pv = np.array([v.value for v in params])
+    masses = pdf.decayInfo.particle_masses
+    out, vmax, have = [], None, 0
+    while have < n:
+        v5 = phasespace.dim5(phasespace.generate(masses[0], masses[1:], batch, rng))
+        c = np.vstack([v5, np.arange(batch, dtype=np.float64)])
+        eng.upload(c)
+        eng.set_params(pv)
+        w = eng.eval_events(A.GF_METRIC_EVAL)
+        if vmax is None:
+            vmax = 1.2 * float(w.max())
+        vmax = max(vmax, float(w.max()))
+        keep = rng.random(batch) * vmax < w
+        out.append(v5[:, keep])
+        have += int(keep.sum())
+    v = np.concatenate(out, axis=1)[:, :n]
+    return np.vstack([v, np.arange(n, dtype=np.float64)])
+
+
+def make_c5(n: int = 300_000, n_norm: int = 2_000_000, seed: int = 5, data: np.ndarray | None = None,
+            float_lineshapes: bool = False) -> Workload:
+    pdf, variables, obs, ls_vars = c5_model(n_norm, float_lineshapes=float_lineshapes)
+    if float_lineshapes:
+        variables.update(ls_vars)
+    truth = {k: v.value for k, v in variables.items()}
+    cols = data if data is not None else c5_generate(pdf, n, seed)
+    ds = G.UnbinnedDataSet(obs)
+    ds.from_numpy(cols)
+    pdf.setData(ds)
+    start = {k: v * 1.05 for k, v in truth.items()}
+    return Workload(f"c5-amp4body-{n}", pdf, ds, truth, start, variables, obs)

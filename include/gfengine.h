@@ -68,13 +68,25 @@ enum gf_op {
                                      consts [nRes, cache, M, m1, m2, m3, mesonRadius, motherRadius]
                                      params [Re c0, Im c0, Re c1, ...] obs [m12^2, m13^2, eventNumber]
                                      children [resonance 0 .. n-1, efficiency] */
-    GF_OP_AMP4BODY          = 13, /* device_DP             src/PDFs/physics/Amp4Body.cu:53-90 */
+    GF_OP_AMP4BODY          = 13, /* device_DP             src/PDFs/physics/Amp4Body.cu:53-90
+                                     consts [M, m1, m2, m3, m4, cache] params [Re c0, Im c0, ...]
+                                     obs [m12, m34, cos12, cos34, phi, eventNumber]
+                                     children [amplitude 0 .. n-1, efficiency]; normalised over the flat
+                                     phase-space events given with gf_set_norm_events */
     GF_OP_MULTIPOLYNOMIAL   = 14, /* device_MultiPolynomial src/PDFs/basic/PolynomialPdf.cu:46-107
                                      consts [maxDegree] params [offsets (one per observable), coefficients] */
     GF_OP_RES_RBW           = 20, /* plainBW<1|2>          src/PDFs/physics/resonances/RBW.cu:9-86
                                      params [mass, width] consts [spin, cyclic index, norm, symmetric] */
-    GF_OP_RES_NONRES        = 21  /* nonres                src/PDFs/physics/resonances/NonRes.cu:8-11
+    GF_OP_RES_NONRES        = 21, /* nonres                src/PDFs/physics/resonances/NonRes.cu:8-11
                                      amplitude 1 + 0i; no parameters */
+    GF_OP_AMPLITUDE         = 15, /* Amplitude             src/PDFs/physics/Amplitude.cu:11-31, AmpCalc
+                                     src/PDFs/physics/detail/AmpCalc.cu:14-59
+                                     consts [nPerm, nLS, nSF] children [line shapes..., spin factors...] */
+    GF_OP_LS_RBW            = 22, /* BW (ptr_to_BW_DP4)    src/PDFs/physics/lineshapes/BW.cu:14-68
+                                     params [mass, width] consts [Mpair (DP4Pair), L, FF, radius] */
+    GF_OP_LS_SBW            = 23, /* SBW                   src/PDFs/physics/lineshapes/BW.cu:70-110 (as GF_OP_LS_RBW) */
+    GF_OP_SPINFACTOR        = 24  /* SpinFactor            src/PDFs/physics/SpinFactors.cu:83-568
+                                     consts [SF_4Body kind, mD0, P0, P1, P2, P3] */
 };
 
 /* node flags */
@@ -256,15 +268,23 @@ int gf_nll_exp_noalloc(const float *x, int64_t n_events, double alpha, double lo
                        void *stream);
 const char *gf_noalloc_last_error(void);
 
-/* Amp3Body normalisation integrals I_ij = sum over in-Dalitz bins of B_i conj(B_j) eff (before the bin size
-   factor), n x n complex interleaved [re, im] row-major, at the toy's current parameters: the integrals
-   Amp3Body::normalize caches (src/PDFs/physics/Amp3Body.cu:304-330; its fit_fractions() reads them).
-   `node` is the Amp3Body's index in the tree; `cap` counts doubles (>= 2 n^2). */
+/* Normalisation integrals of an amplitude node at the toy's current parameters, n x n complex interleaved
+   [re, im] row-major; `cap` counts doubles (>= 2 n^2).  Amp3Body: I_ij = sum over in-Dalitz bins of
+   B_i conj(B_j) eff, before the bin size factor (the integrals Amp3Body::normalize caches,
+   src/PDFs/physics/Amp3Body.cu:304-330).  Amp4Body: G_ab = sum over the normalisation events of
+   A_a conj(A_b), before the 1/N (NormIntegrator's sum, src/PDFs/physics/detail/NormIntegrator.cu:15-68,
+   taken apart by amplitude pairs). */
 int gf_amp3_integrals(gf_engine *eng, int toy, int node, double *out, int cap);
 
-/* Cached amplitude B_res of every event of the toy, complex interleaved (2 n doubles; FP32 values widened in
-   GF_MIXED): Amp3Body::getCachedWave (include/goofit/PDFs/physics/Amp3Body.h:61). */
+/* Cached amplitude of resonance / amplitude `res` of an Amp3Body or Amp4Body node for every event of the toy,
+   complex interleaved (2 n doubles; FP32 values widened in GF_MIXED): Amp3Body::getCachedWave
+   (include/goofit/PDFs/physics/Amp3Body.h:61) and Amp4Body's cachedAMPs (src/PDFs/physics/Amp4Body.cu:381-386). */
 int gf_amp3_cached_wave(gf_engine *eng, int toy, int node, int res, double *out, int64_t n_out);
+
+/* Flat phase-space normalisation events of an Amp4Body node, SoA [m12 | m34 | cos12 | cos34 | phi], n each
+   (copied).  Replaces the MCBooster generation inside the Amp4Body constructor
+   (src/PDFs/physics/Amp4Body.cu:243-290); call after gf_set_tree, before evaluating. */
+int gf_set_norm_events(gf_engine *eng, int node, const double *soa5, int64_t n);
 
 /* ---- diagnostics: code generation without a device ---- */
 /* Generated CUDA source for a tree (precision as in gf_engine_create); *len gets the full length. */

@@ -16,6 +16,7 @@
 // uninitialised; the oracle evaluates the proper N-D grid.  1-D grids (all
 // configs) are identical.
 #include "../include/gfengine.h"
+#include "amp4.h"
 
 #include <cmath>
 #include <complex>
@@ -179,6 +180,12 @@ cplx plainBW(int I, double resmass, double reswidth, unsigned spin, unsigned cyc
     return result;
 }
 
+// Flat phase-space normalisation events of Amp4Body trees, SoA [m12, m34, cos12, cos34, phi] x n
+// (set by oracle_set_amp4_norm_events; the reference generates them with MCBooster in the Amp4Body
+// constructor, src/PDFs/physics/Amp4Body.cu:243-290).
+std::vector<double> g_norm_events;
+int64_t g_n_norm = 0;
+
 struct Oracle {
     std::vector<Node> nodes;
     std::vector<gf_observable> obs;
@@ -187,6 +194,7 @@ struct Oracle {
     std::vector<double> integral; // value returned by normalize()
     std::map<int, ConvWork> conv;
     std::map<int, std::vector<cplx>> amp3I; // Amp3Body node -> n x n integrals I_ij
+    std::map<int, std::vector<cplx>> amp4G; // Amp4Body node -> n x n sums of A_a conj(A_b) over norm events
     bool brute_force = false;
     std::string err;
 
@@ -319,6 +327,8 @@ struct Oracle {
         }
         if(n.op == GF_OP_AMP3BODY)
             return normalizeAmp3(i);
+        if(n.op == GF_OP_AMP4BODY)
+            return normalizeAmp4(i);
         if(n.op == GF_OP_CONVOLUTION) {
             // ConvolutionPdf::normalize (src/PDFs/combine/ConvolutionPdf.cu:313-358)
             recursiveSetNormalization(i, 1.0);
@@ -594,9 +604,118 @@ struct Oracle {
             ret *= eval(n.children[nRes], evt);
             return ret;
         }
+        case GF_OP_AMP4BODY: { // device_DP, src/PDFs/physics/Amp4Body.cu:53-90
+            const double v[5] = {evt[n.obs[0]], evt[n.obs[1]], evt[n.obs[2]], evt[n.obs[3]], evt[n.obs[4]]};
+            const int nAmp    = (int)n.children.size() - 1;
+            std::vector<cplx> A(nAmp);
+            amp4Amplitudes(i, v, A.data());
+            cplx totalAmp(0, 0);
+            for(int a = 0; a < nAmp; ++a)
+                totalAmp += A[a] * cplx(par(i, 2 * a), par(i, 2 * a + 1));
+            double ret = std::norm(totalAmp);
+            ret *= eval(n.children[nAmp], evt);
+            return ret;
+        }
         default:
             throw std::runtime_error("oracle: unsupported op " + std::to_string(n.op));
         }
+    }
+
+    // Amplitudes A_a of Amp4Body node i at one point of the 5 variables: AmpCalc
+    // (src/PDFs/physics/detail/AmpCalc.cu:14-59) over the line shapes (LSCalculator,
+    // src/PDFs/physics/detail/LSCalculator.cu:11-68) and spin factors (SFCalculator, SFCalculator.cu:11-55).
+    void amp4Amplitudes(int i, const double *v, cplx *A) const {
+        const Node &n = nodes[i];
+        const double M = n.consts.at(0), m1 = n.consts.at(1), m2 = n.consts.at(2), m3 = n.consts.at(3),
+                     m4 = n.consts.at(4);
+        double V[16];
+        amp4::get4Vecs(V, v[0], v[1], v[2], v[3], v[4], M, m1, m2, m3, m4);
+        const int nAmp = (int)n.children.size() - 1;
+        for(int a = 0; a < nAmp; ++a) {
+            const Node &an = nodes[n.children[a]];
+            const int nPerm = (int)an.consts.at(0), nLS = (int)an.consts.at(1), nSF = (int)an.consts.at(2);
+            const int LS_step = nLS / nPerm, SF_step = nSF / nPerm;
+            cplx ret2(0, 0);
+            for(int p = 0; p < nPerm; ++p) {
+                cplx ret(1, 0);
+                for(int j = p * LS_step; j < (p + 1) * LS_step; ++j) {
+                    const Node &ls = nodes[an.children[j]];
+                    const unsigned pair = (unsigned)ls.consts.at(0);
+                    double d1, d2, mres;
+                    if(pair < 2) {
+                        mres = pair == 0 ? v[0] : v[1];
+                        d1   = pair == 0 ? m1 : m3;
+                        d2   = pair == 0 ? m2 : m4;
+                    } else
+                        mres = amp4::getmass(pair, d1, d2, V, m1, m2, m3, m4);
+                    ret *= amp4::lineshape(ls.op == GF_OP_LS_SBW, mres, d1, d2, P.at(ls.params.at(0)),
+                                           P.at(ls.params.at(1)), (unsigned)ls.consts.at(1), (unsigned)ls.consts.at(2),
+                                           ls.consts.at(3));
+                }
+                for(int j = p * SF_step; j < (p + 1) * SF_step; ++j) {
+                    const Node &sf = nodes[an.children[nLS + j]];
+                    const int pp[4] = {(int)sf.consts.at(2), (int)sf.consts.at(3), (int)sf.consts.at(4),
+                                       (int)sf.consts.at(5)};
+                    ret *= amp4::spinFactor((int)sf.consts.at(0), sf.consts.at(1), pp, V);
+                }
+                ret2 += ret;
+            }
+            ret2 *= (1 / std::sqrt((double)nPerm));
+            A[a] = ret2;
+        }
+    }
+
+    // Amp4Body::normalize (src/PDFs/physics/Amp4Body.cu:398-558) with NormIntegrator
+    // (src/PDFs/physics/detail/NormIntegrator.cu:15-68): mean of |sum_a c_a A_a|^2 over the flat
+    // phase-space events; the efficiency does not enter.
+    double normalizeAmp4(int i) {
+        const Node &n = nodes[i];
+        recursiveSetNormalization(i, 1.0);
+        if(g_n_norm <= 0)
+            throw std::runtime_error("oracle: Amp4Body without normalisation events");
+        const int nAmp = (int)n.children.size() - 1;
+        std::vector<cplx> c(nAmp);
+        for(int a = 0; a < nAmp; ++a)
+            c[a] = cplx(par(i, 2 * a), par(i, 2 * a + 1));
+        int nthreads = 1;
+#ifdef _OPENMP
+        nthreads = omp_get_max_threads();
+#endif
+        std::vector<double> part(nthreads, 0.0);
+        std::vector<cplx> gram(nAmp * nAmp, cplx(0, 0));
+        std::vector<std::vector<cplx>> gpart(nthreads, std::vector<cplx>(nAmp * nAmp, cplx(0, 0)));
+#pragma omp parallel
+        {
+            int tid = 0;
+#ifdef _OPENMP
+            tid = omp_get_thread_num();
+#endif
+            std::vector<cplx> A(nAmp);
+#pragma omp for schedule(static)
+            for(int64_t e = 0; e < g_n_norm; ++e) {
+                const double v[5] = {g_norm_events[e], g_norm_events[g_n_norm + e], g_norm_events[2 * g_n_norm + e],
+                                     g_norm_events[3 * g_n_norm + e], g_norm_events[4 * g_n_norm + e]};
+                amp4Amplitudes(i, v, A.data());
+                cplx t(0, 0);
+                for(int a = 0; a < nAmp; ++a)
+                    t += A[a] * c[a];
+                part[tid] += std::norm(t);
+                for(int a = 0; a < nAmp; ++a)
+                    for(int b = 0; b < nAmp; ++b)
+                        gpart[tid][a * nAmp + b] += A[a] * std::conj(A[b]);
+            }
+        }
+        double sumIntegral = 0;
+        for(double p : part)
+            sumIntegral += p;
+        for(auto &g : gpart)
+            for(int k = 0; k < nAmp * nAmp; ++k)
+                gram[k] += g[k];
+        amp4G[i] = gram;
+        sumIntegral /= (double)g_n_norm;
+        norm[i]     = 1.0 / sumIntegral;
+        integral[i] = sumIntegral;
+        return sumIntegral;
     }
 
     Decay3 decay3(int i) const {
@@ -894,6 +1013,59 @@ int oracle_amp3_resonance(const gf_node *nodes, int n_nodes, const gf_observable
         g_err = ex.what();
         return 1;
     }
+}
+
+void oracle_set_amp4_norm_events(const double *soa5, int64_t n) {
+    g_norm_events.assign(soa5, soa5 + 5 * std::max<int64_t>(n, 0));
+    g_n_norm = n;
+}
+
+// The Amp4Body sums G_ab = sum over norm events of A_a conj(A_b) (n x n complex, interleaved).
+int oracle_amp4_gram(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, const double *params,
+                     int n_params, int node, double *out) {
+    try {
+        Oracle O;
+        load(O, nodes, n_nodes, obs, n_obs, params, n_params, 0);
+        O.normalize(node);
+        const auto &G = O.amp4G.at(node);
+        for(size_t k = 0; k < G.size(); ++k) {
+            out[2 * k]     = G[k].real();
+            out[2 * k + 1] = G[k].imag();
+        }
+        return 0;
+    } catch(std::exception &ex) {
+        g_err = ex.what();
+        return 1;
+    }
+}
+
+// Amplitudes A_a of Amp4Body `node` at n points (SoA 5 x n), interleaved complex [point][amplitude].
+int oracle_amp4_amplitudes(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs,
+                           const double *params, int n_params, int node, const double *soa5, int64_t n, double *out) {
+    try {
+        Oracle O;
+        load(O, nodes, n_nodes, obs, n_obs, params, n_params, 0);
+        const int nAmp = (int)O.nodes.at(node).children.size() - 1;
+        std::vector<cplx> A(nAmp);
+        for(int64_t e = 0; e < n; ++e) {
+            const double v[5] = {soa5[e], soa5[n + e], soa5[2 * n + e], soa5[3 * n + e], soa5[4 * n + e]};
+            O.amp4Amplitudes(node, v, A.data());
+            for(int a = 0; a < nAmp; ++a) {
+                out[2 * (e * nAmp + a)]     = A[a].real();
+                out[2 * (e * nAmp + a) + 1] = A[a].imag();
+            }
+        }
+        return 0;
+    } catch(std::exception &ex) {
+        g_err = ex.what();
+        return 1;
+    }
+}
+
+// get4Vecs at one point (16 values, (x, y, z, E) per daughter).
+void oracle_get4vecs(const double *v5, const double *masses5, double *out16) {
+    amp4::get4Vecs(out16, v5[0], v5[1], v5[2], v5[3], v5[4], masses5[0], masses5[1], masses5[2], masses5[3],
+                   masses5[4]);
 }
 
 int oracle_in_dalitz(double m12, double m13, double M, double d1, double d2, double d3) {

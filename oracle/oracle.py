@@ -27,7 +27,7 @@ def build() -> Path:
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
-        if not LIB.exists() or LIB.stat().st_mtime < (HERE / "oracle.cpp").stat().st_mtime:
+        if not LIB.exists() or LIB.stat().st_mtime < max((HERE / f).stat().st_mtime for f in ("oracle.cpp", "amp4.h")):
             build()
         L = C.CDLL(str(LIB))
         f64p, i32p = C.POINTER(C.c_double), C.POINTER(C.c_int32)
@@ -46,6 +46,14 @@ def lib() -> C.CDLL:
         L.oracle_amp3_resonance.argtypes = [C.POINTER(A.gf_node), C.c_int, C.POINTER(A.gf_observable), C.c_int,
                                             f64p, C.c_int, C.c_int, C.c_int, f64p, f64p, C.c_int64, f64p]
         L.oracle_amp3_resonance.restype = C.c_int
+        L.oracle_set_amp4_norm_events.argtypes = [f64p, C.c_int64]
+        L.oracle_amp4_gram.argtypes = [C.POINTER(A.gf_node), C.c_int, C.POINTER(A.gf_observable), C.c_int, f64p,
+                                       C.c_int, C.c_int, f64p]
+        L.oracle_amp4_gram.restype = C.c_int
+        L.oracle_amp4_amplitudes.argtypes = [C.POINTER(A.gf_node), C.c_int, C.POINTER(A.gf_observable), C.c_int,
+                                             f64p, C.c_int, C.c_int, f64p, C.c_int64, f64p]
+        L.oracle_amp4_amplitudes.restype = C.c_int
+        L.oracle_get4vecs.argtypes = [f64p, f64p, f64p]
         L.oracle_in_dalitz.argtypes = [C.c_double] * 6
         L.oracle_in_dalitz.restype = C.c_int
         _lib = L
@@ -145,3 +153,44 @@ def amp3_resonance(nodes, observables, params, node: int, res: int, m12, m13) ->
 
 def in_dalitz(m12: float, m13: float, M: float, d1: float, d2: float, d3: float) -> bool:
     return bool(lib().oracle_in_dalitz(m12, m13, M, d1, d2, d3))
+
+
+def set_amp4_norm_events(soa5) -> None:
+    """Flat phase-space normalisation events (5, n) used by every later Amp4Body normalisation."""
+    a = np.ascontiguousarray(soa5, dtype=np.float64)
+    lib().oracle_set_amp4_norm_events(a.ctypes.data_as(C.POINTER(C.c_double)), a.shape[1])
+
+
+def amp4_gram(nodes, observables, params, node: int, n_amp: int) -> np.ndarray:
+    """G_ab = sum over the normalisation events of A_a conj(A_b) of Amp4Body `node`."""
+    nl, obs, p, pp, _ = _prep(nodes, observables, params, np.zeros((len(observables), 1)))
+    out = np.zeros(2 * n_amp * n_amp)
+    rc = lib().oracle_amp4_gram(nl.arr, nl.n, obs, len(observables), pp, len(p), node,
+                                out.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc:
+        raise OracleError(lib().oracle_last_error().decode())
+    return (out[0::2] + 1j * out[1::2]).reshape(n_amp, n_amp)
+
+
+def amp4_amplitudes(nodes, observables, params, node: int, n_amp: int, soa5) -> np.ndarray:
+    """Amplitudes (n, n_amp) complex of Amp4Body `node` at the points soa5 (5, n)."""
+    nl, obs, p, pp, _ = _prep(nodes, observables, params, np.zeros((len(observables), 1)))
+    v = np.ascontiguousarray(soa5, dtype=np.float64)
+    n = v.shape[1]
+    out = np.zeros(2 * n * n_amp)
+    f64p = C.POINTER(C.c_double)
+    rc = lib().oracle_amp4_amplitudes(nl.arr, nl.n, obs, len(observables), pp, len(p), node, v.ctypes.data_as(f64p), n,
+                                      out.ctypes.data_as(f64p))
+    if rc:
+        raise OracleError(lib().oracle_last_error().decode())
+    return (out[0::2] + 1j * out[1::2]).reshape(n, n_amp)
+
+
+def get4vecs(v5, masses5) -> np.ndarray:
+    """get4Vecs at one point: (4, 4) daughter 4-vectors (x, y, z, E)."""
+    f64p = C.POINTER(C.c_double)
+    a = np.ascontiguousarray(v5, dtype=np.float64)
+    m = np.ascontiguousarray(masses5, dtype=np.float64)
+    out = np.zeros(16)
+    lib().oracle_get4vecs(a.ctypes.data_as(f64p), m.ctypes.data_as(f64p), out.ctypes.data_as(f64p))
+    return out.reshape(4, 4)

@@ -1,0 +1,132 @@
+"""GPU parity of the Amp4Body path (4-body amplitudes from line shapes and spin factors) against the FP64
+oracle on the same data and the same flat phase-space normalisation events.
+
+Tolerances (written per test): NLL 1e-6 relative for the mixed path and 1e-10 for FP64; cached amplitudes
+and normalisation sums 2e-5 (mixed) and 1e-10 (FP64) relative to the largest entry; fitted parameters of
+the mixed path within 0.01 sigma of the FP64 path.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import goofit_gb300 as gf
+from goofit_gb300 import _abi as A
+from goofit_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+NLL_RTOL = {"mixed": 1e-6, "fp64": 1e-10}
+AMP_RTOL = {"mixed": 2e-5, "fp64": 1e-10}
+N_NORM = 100_000
+
+
+def tree(pdf):
+    nodes, params, obs = pdf._flatten()
+    olist = [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs]
+    nd = pdf._nondiff_all()
+    mask = [0 if (v.fixed or id(v) in nd) else 1 for v in params]
+    pv = np.array([v.value for v in params])
+    return nodes, olist, params, mask, pv
+
+
+@pytest.fixture(scope="module")
+def c5():
+    pdf = W.c5_model(N_NORM)[0]
+    cols = W.c5_generate(pdf, 20_000, seed=51, batch=400_000)
+    return pdf, cols
+
+
+def engine(pdf, cols, prec, mask=None):
+    nodes, olist, params, m, pv = tree(pdf)
+    eng = gf.Engine(prec)
+    eng.set_tree(nodes, olist, len(params), m if mask is None else mask)
+    eng.set_norm_events(0, pdf.norm_events)
+    eng.upload(cols)
+    eng.set_params(pv)
+    O.set_amp4_norm_events(pdf.norm_events)
+    return eng, nodes, olist, params, m, pv
+
+
+def test_events_are_physical(c5):
+    _, cols = c5
+    assert cols.shape == (6, 20_000)
+    assert np.all(np.abs(cols[2:4]) <= 1) and np.all(np.abs(cols[4]) <= np.pi)
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_cached_amplitudes_match_oracle(c5, prec):
+    pdf, cols = c5
+    eng, nodes, olist, params, mask, pv = engine(pdf, cols, prec)
+    ref = O.amp4_amplitudes(nodes, olist, pv, 0, 6, cols[:5])
+    for a in range(6):
+        got = eng.amp3_cached_wave(0, a)
+        err = np.abs(got - ref[:, a]).max() / np.abs(ref[:, a]).max()
+        assert err < AMP_RTOL[prec], (a, err)
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_normalisation_sums_match_oracle(c5, prec):
+    pdf, cols = c5
+    eng, nodes, olist, params, mask, pv = engine(pdf, cols, prec)
+    got = eng.amp3_integrals(0, 6)
+    ref = O.amp4_gram(nodes, olist, pv, 0, 6)
+    err = np.abs(got - ref).max() / np.abs(np.diag(ref)).max()
+    assert err < AMP_RTOL[prec], err
+    np.testing.assert_array_equal(got, got.conj().T)
+    I, N = eng.normalize()
+    _, Io, No = O.evaluate(nodes, olist, pv, cols[:, :1], metric=A.GF_METRIC_EVAL)
+    assert I[0] == pytest.approx(Io[0], rel=AMP_RTOL[prec])
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_nll_and_gradient_match_oracle(c5, prec):
+    pdf, cols = c5
+    eng, nodes, olist, params, mask, pv = engine(pdf, cols, prec)
+    free = [i for i, m in enumerate(mask) if m]
+    assert len(free) == 10
+    rng = np.random.default_rng(8)
+    for trial in range(3):
+        p = pv.copy()
+        if trial:
+            p[free] *= 1 + 0.05 * rng.standard_normal(len(free))
+        ref = O.nll(nodes, olist, p, cols)
+        got, g = eng.nll_grad(p)
+        assert got == pytest.approx(ref, rel=NLL_RTOL[prec]), (trial, got, ref)
+        fd = O.fd_grad(nodes, olist, p, cols, free, h=1e-6)
+        n = cols.shape[1]
+        np.testing.assert_allclose(g, fd, rtol=2e-4, atol=2e-3 * math.sqrt(n))
+
+
+def test_lineshape_parameter_change_rebuilds_the_caches(c5):
+    pdf, cols = c5
+    eng, nodes, olist, params, mask, pv = engine(pdf, cols, "fp64")
+    names = [v.name for v in params]
+    for name, val in (("rho_mass", 0.78), ("K1_width", 0.1)):
+        p = pv.copy()
+        p[names.index(name)] = val
+        assert eng.nll(p) == pytest.approx(O.nll(nodes, olist, p, cols), rel=1e-10), name
+    assert eng.nll(pv) == pytest.approx(O.nll(nodes, olist, pv, cols), rel=1e-10)
+
+
+def test_mixed_fit_matches_fp64_fit(c5):
+    _, cols = c5
+    out = {}
+    for prec in ("fp64", "mixed"):
+        pdf, variables, obs, _ = W.c5_model(N_NORM)
+        ds = gf.UnbinnedDataSet(obs)
+        ds.from_numpy(cols)
+        pdf.setData(ds)
+        for v in variables.values():
+            v.value *= 1.05
+        fm = gf.FitManager(pdf, precision=prec)
+        fm.verbosity = 0
+        r = fm.fit()
+        assert r.valid, prec
+        assert fm.used_gradient == "analytic"
+        out[prec] = {k: (v.value, v.error) for k, v in variables.items()}
+    for k, (v64, e64) in out["fp64"].items():
+        vm, em = out["mixed"][k]
+        assert abs(vm - v64) < 0.01 * e64, (k, vm, v64, e64)
+        assert em == pytest.approx(e64, rel=0.01), k
