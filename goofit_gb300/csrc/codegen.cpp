@@ -56,6 +56,7 @@ struct Ctx {
     std::function<std::string(int, int)> tab;    // conv index, component -> expression
     std::vector<int> *xused;
     std::function<std::string(int, int)> amp; // Amp3Body index, resonance -> R2 amplitude expression
+    bool lohi = false;                        // normalisation factors as FP32 hi + lo pairs
     int uid = 0;
     std::string tmp(const char *p) { return std::string(p) + std::to_string(uid++); }
 };
@@ -68,6 +69,15 @@ std::string normExpr(Ctx &c, int i) {
     if(!c.event)
         throw std::runtime_error("codegen: non-unit norm referenced outside the event pass");
     return "N" + std::to_string(i);
+}
+// x times the normalisation factor of node i (x itself for unit factors): x * (hi + lo) with one rounding
+std::string normMul(Ctx &c, int i, const std::string &x) {
+    std::string ne = normExpr(c, i);
+    if(ne.empty())
+        return x;
+    if(c.lohi)
+        return "gf_nm(" + x + ", N" + std::to_string(i) + ", NL" + std::to_string(i) + ")";
+    return "(" + x + " * " + ne + ")";
 }
 std::string dnormExpr(Ctx &c, int i, int s) {
     const auto &d = c.T.dep_norm[i];
@@ -203,21 +213,16 @@ Val emit(Ctx &c, int i) {
         for(size_t k = 0; k < n.params.size(); ++k)
             os << "    " << tw << " += " << P(n.params[k]) << ";\n";
         std::vector<std::string> u; // weight-free normalised child values v_c * N_c
-        for(size_t k = 0; k < ch.size(); ++k) {
-            std::string ne = normExpr(c, n.children[k]);
-            u.push_back(ne.empty() ? ch[k].v : "(" + ch[k].v + " * " + ne + ")");
-        }
+        for(size_t k = 0; k < ch.size(); ++k)
+            u.push_back(normMul(c, n.children[k], ch[k].v));
         os << "    R " << v << " = R(0);\n";
         size_t nw = ext ? ch.size() : ch.size() - 1;
-        for(size_t k = 0; k < nw; ++k) {
-            std::string ne = normExpr(c, n.children[k]);
-            os << "    " << v << " += (" << P(n.params[k]) << " * " << ch[k].v << ")"
-               << (ne.empty() ? "" : " * " + ne) << ";\n";
-        }
+        for(size_t k = 0; k < nw; ++k)
+            os << "    " << v << " += " << normMul(c, n.children[k], "(" + P(n.params[k]) + " * " + ch[k].v + ")")
+               << ";\n";
         if(!ext) {
-            std::string ne = normExpr(c, n.children.back());
-            os << "    " << v << " += ((R(1) - " << tw << ") * " << ch.back().v << ")"
-               << (ne.empty() ? "" : " * " + ne) << ";\n";
+            os << "    " << v << " += "
+               << normMul(c, n.children.back(), "((R(1) - " + tw + ") * " + ch.back().v + ")") << ";\n";
         } else {
             os << "    " << v << " /= " << tw << ";\n";
         }
@@ -271,8 +276,8 @@ Val emit(Ctx &c, int i) {
             ch.push_back(emit(c, cidx));
         std::vector<std::string> u;
         for(size_t k = 0; k < ch.size(); ++k) {
-            std::string ne = normExpr(c, n.children[k]), un = c.tmp("u");
-            os << "    const R " << un << " = " << ch[k].v << (ne.empty() ? "" : " * " + ne) << ";\n";
+            std::string un = c.tmp("u");
+            os << "    const R " << un << " = " << normMul(c, n.children[k], ch[k].v) << ";\n";
             u.push_back(un);
         }
         std::string v = c.tmp("v");
@@ -541,6 +546,8 @@ __device__ __forceinline__ ACC warp_acc2(ACC a) {
 }
 __device__ __forceinline__ double acc_value(ACC a) { return (double)a.x + (double)a.y; }
 __device__ __forceinline__ float acc_r(ACC a) { return a.x + a.y; }
+// x * (h + l) for a normalisation factor kept as an FP32 pair: one rounding, no bias from rounding the factor
+__device__ __forceinline__ float gf_nm(float x, float h, float l) { return fmaf(x, h, x * l); }
 #define GF_CENTRE(lo, w, b) ((float)(lo) + (float)(w) * ((float)(b) + 0.5f))
 )CUDA";
 
@@ -559,6 +566,7 @@ __device__ __forceinline__ ACC warp_acc(double v) { return gf_warp_sum(v); }
 __device__ __forceinline__ ACC warp_acc2(ACC a) { return gf_warp_sum(a); }
 __device__ __forceinline__ double acc_value(ACC a) { return a; }
 __device__ __forceinline__ double acc_r(ACC a) { return a; }
+__device__ __forceinline__ double gf_nm(double x, double h, double l) { return x * h; }
 #define GF_CENTRE(lo, w, b) gf_centre(lo, w, b)
 )CUDA";
 
@@ -882,18 +890,21 @@ NormLayout computeNormLayout(const Tree &T) {
         if(T.nk[i] != NK_EXP && T.nk[i] != NK_GAUSS && T.nk[i] != NK_AMP3 && T.nk[i] != NK_AMP4)
             continue;
         NormLayout::Analytic a;
-        a.node  = (int)i;
-        a.kind  = T.nk[i];
-        a.slotN = nl.npr++;
+        a.node   = (int)i;
+        a.kind   = T.nk[i];
+        a.slotN  = nl.npr++;
+        a.slotNL = nl.npr++;
         for(int s : T.dep_norm[i])
             a.dN.push_back({s, nl.npr++});
         nl.analytic.push_back(a);
     }
     nl.qN.assign(T.nums.size(), -1);
+    nl.qNL.assign(T.nums.size(), -1);
     nl.qdN.assign(T.nums.size(), {});
     for(size_t q = 0; q < T.nums.size(); ++q) {
-        int i    = T.nums[q].node;
-        nl.qN[q] = nl.nq++;
+        int i     = T.nums[q].node;
+        nl.qN[q]  = nl.nq++;
+        nl.qNL[q] = nl.nq++;
         for(int s : T.dep_norm[i])
             nl.qdN[q].push_back({s, nl.nq++});
     }
@@ -912,14 +923,16 @@ void emitNormReads(std::ostream &os, const Tree &T, bool grad, const NormLayout 
     if(nl.nq > 0)
         os << ind << "const R *Nq = reinterpret_cast<const R *>(a.Nq) + (i64)toy * " << nl.nq << ";\n";
     for(auto &an : nl.analytic) {
-        os << ind << "const R N" << an.node << " = Pr[" << an.slotN << "];\n";
+        os << ind << "const R N" << an.node << " = Pr[" << an.slotN << "], NL" << an.node << " = Pr[" << an.slotNL
+           << "]; (void)NL" << an.node << ";\n";
         if(grad)
             for(auto &d : an.dN)
                 os << ind << "const R dN" << an.node << "_" << d.first << " = Pr[" << d.second << "];\n";
     }
     for(size_t q = 0; q < T.nums.size(); ++q) {
         int i = T.nums[q].node;
-        os << ind << "const R N" << i << " = Nq[" << nl.qN[q] << "];\n";
+        os << ind << "const R N" << i << " = Nq[" << nl.qN[q] << "], NL" << i << " = Nq[" << nl.qNL[q] << "]; (void)NL"
+           << i << ";\n";
         if(grad)
             for(auto &d : nl.qdN[q])
                 os << ind << "const R dN" << i << "_" << d.first << " = Nq[" << d.second << "];\n";
@@ -1234,11 +1247,10 @@ struct Gen {
             c /= (double)g.total;
             os << "    case " << q << ": {\n";
             os << "      const double I = " << lit(c) << " * S;\n";
-            if(mixed)
-                os << "      const R N = 1.0f / (float)I;\n";
-            else
-                os << "      const R N = 1.0 / I;\n";
+            os << "      const double Nd = 1.0 / I;\n";
+            os << "      const R N = (R)Nd;\n";
             os << "      Nq[" << nl.qN[q] << "] = N;\n";
+            os << "      Nq[" << nl.qNL[q] << "] = (R)(Nd - (double)N);\n";
             if(grad)
                 for(auto &d : nl.qdN[q])
                     os << "      Nq[" << d.second << "] = -N * N * (R)" << lit(c) << " * (R)acc_r(tot[" << 1 + d.first
@@ -1508,7 +1520,8 @@ struct Gen {
         std::vector<int> xused(NO, 0);
         std::ostringstream body;
         Ctx c{body, T, grad, true, nullptr, nullptr, nullptr, &xused};
-        c.x = [&](int o) {
+        c.lohi = mixed;
+        c.x    = [&](int o) {
             xused[o] = 1;
             return "ex" + std::to_string(o);
         };
@@ -1664,7 +1677,7 @@ struct Gen {
             }
         }
         os << "        {\n" << body.str();
-        os << "        const R pv = " << root.v << (rootN.empty() ? "" : " * " + rootN) << ";\n";
+        os << "        const R pv = " << normMul(c, 0, root.v) << ";\n";
         if(values) {
             os << "        if(i0 + j < e0) {\n";
             os << "          double r;\n";

@@ -574,6 +574,7 @@ void fillRecordsT(gf_engine *e) {
                 const double f  = ampScale(e, an.node);
                 const double N  = 1.0 / Iv;
                 r[an.slotN]     = (R)N;
+                r[an.slotNL]    = (R)(N - (double)(R)N);
                 for(size_t k = 0; k < an.dN.size(); ++k)
                     r[an.dN[k].second] = (R)(-N * N * f * dQ[k]);
                 if(an.node == 0) {
@@ -606,6 +607,7 @@ void fillRecordsT(gf_engine *e) {
             }
             const double N = 1.0 / I;
             r[an.slotN]    = (R)N;
+            r[an.slotNL]   = (R)(N - (double)(R)N);
             for(auto &d : an.dN)
                 r[d.second] = (R)(-N * N * dI);
             if(an.node == 0) {

@@ -153,14 +153,17 @@ inline double bin_centre(double lo, double hi, int nbins, int b) {
 //   numeric array (type R, one per toy): the factors of numerically normalised nodes, written by the
 //   finishing CTA of the grid kernel.
 struct NormLayout {
+    // every factor N is kept as hi + lo (lo = N - hi rounded; 0 in FP64), so that FP32 products v * N carry
+    // no systematic rounding of N
     struct Analytic {
-        int node = -1, kind = 0, slotN = -1;
+        int node = -1, kind = 0, slotN = -1, slotNL = -1;
         std::vector<std::pair<int, int>> dN; // (gradient slot, record index)
     };
     int npr = 0; // record length
     std::vector<Analytic> analytic;
     int nq = 0;                                        // numeric slots per toy
     std::vector<int> qN;                               // per numeric node q: slot of N
+    std::vector<int> qNL;                              // per numeric node q: slot of the low part of N
     std::vector<std::vector<std::pair<int, int>>> qdN; // per q: (gradient slot, slot of dN)
 };
 NormLayout norm_layout(const Tree &t);
