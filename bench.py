@@ -475,7 +475,9 @@ def run_dalitz(args) -> dict:
             fm.verbosity = 0
             r = fm.fit()
             free = [v for v in params if not v.fixed and id(v) not in nd]
-            fits[label] = {"wall_s": fm.wall_seconds, "nfcn": r.nfcn, "valid": r.valid, "fmin": r.fmin,
+            fits[label] = {"wall_s": fm.wall_seconds, "nfcn": r.nfcn, "valid": r.valid, "fmin": r.fmin, "edm": r.edm,
+                           "call_limit": r.call_limit, "above_max_edm": r.above_max_edm,
+                           "has_covariance": r.has_covariance, "hesse_failed": r.hesse_failed,
                            "values": {v.name: v.value for v in free}, "errors": {v.name: v.error for v in free}}
         fits["speedup_wall"] = fits["fp64_numerical"]["wall_s"] / fits["mixed_analytic"]["wall_s"]
         fits["rel_dnll"] = abs(fits["mixed_analytic"]["fmin"] - fits["fp64_numerical"]["fmin"]) / \

@@ -562,10 +562,16 @@ void fillRecordsT(gf_engine *e) {
         e->host_flag[t] = 0;
         if(!e->h_active[t])
             continue;
-        const double *P = e->h_P + (size_t)t * np;
-        R *r            = rec + (size_t)t * nl.npr;
-        for(int j = 0; j < np; ++j)
-            r[j] = (R)P[j];
+        // the kernels see the parameters rounded to R; the factors computed here use the same rounded values,
+        // so that the NLL is one function of the rounded parameters (an event part evaluated at rounded and a
+        // normalisation at unrounded parameters would differ by steps of n * ulp * |d(event part)/dp|)
+        std::vector<double> Pq(std::max(1, np));
+        R *r = rec + (size_t)t * nl.npr;
+        for(int j = 0; j < np; ++j) {
+            r[j]  = (R)e->h_P[(size_t)t * np + j];
+            Pq[j] = (double)r[j];
+        }
+        const double *P = Pq.data();
         for(auto &an : nl.analytic) {
             const gf::TNode &nd = T.nodes[an.node];
             if(an.kind == gf::NK_AMP3 || an.kind == gf::NK_AMP4) {
@@ -727,10 +733,12 @@ void postToy(gf_engine *e, int t, double *o) {
     const gf::Tree &T = e->tree;
     int st            = (int)o[1] | e->host_flag[t];
     if(T.extended_root && !(st & 4)) {
+        // the yields as the kernels saw them (rounded to R in GF_MIXED)
         const double *P = e->h_P + (size_t)t * T.n_params;
+        auto q          = [&](int p) { return e->precision == GF_MIXED ? (double)(float)P[p] : P[p]; };
         double ex       = 0;
         for(int p : T.nodes[0].params)
-            ex += P[p];
+            ex += q(p);
         const double ne = (double)e->toys[t].n;
         o[0] += (ex - ne * std::log(ex));
         for(int p : T.nodes[0].params)

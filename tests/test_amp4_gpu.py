@@ -120,7 +120,9 @@ def test_mixed_fit_matches_fp64_fit(c5):
         pdf.setData(ds)
         for v in variables.values():
             v.value *= 1.05
-        fm = gf.FitManager(pdf, precision=prec)
+        # tolerance 0.01 (EDM < 1e-5): each fit then sits within ~0.005 sigma of its minimum, so that
+        # the 0.01 sigma comparison measures the precision of the NLL, not the stopping rule
+        fm = gf.FitManager(pdf, precision=prec, tolerance=0.01)
         fm.verbosity = 0
         r = fm.fit()
         assert r.valid, prec
