@@ -916,10 +916,8 @@ class Amp3Body(GooPdf):
         """Integrals are rebuilt whenever a resonance or efficiency parameter changes."""
 
     def _nondiff_params(self) -> set:
-        ids = set()
-        for c in self.components:
-            ids |= {id(v) for v in c.getParameters()}
-        return ids
+        """The efficiency's parameters (the resonance parameters have analytic derivatives)."""
+        return {id(v) for v in self.efficiency.getParameters()}
 
     def _node_index(self) -> int:
         return 0
@@ -1147,10 +1145,8 @@ class Amp4Body(GooPdf):
         eng.set_norm_events(node, self.norm_events)
 
     def _nondiff_params(self) -> set:
-        ids = set()
-        for c in self.components:
-            ids |= {id(v) for v in c.getParameters()}
-        return ids
+        """The efficiency's parameters (the line-shape parameters have analytic derivatives)."""
+        return {id(v) for v in self.efficiency.getParameters()}
 
     def setDataSize(self, dataSize: int, evtSize: int = 6) -> None:
         """The amplitude cache is sized by the uploaded data; kept for interface compatibility."""

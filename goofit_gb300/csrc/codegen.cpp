@@ -55,7 +55,8 @@ struct Ctx {
     std::function<std::string(int)> k;           // conv index -> int expression
     std::function<std::string(int, int)> tab;    // conv index, component -> expression
     std::vector<int> *xused;
-    std::function<std::string(int, int)> amp; // Amp3Body index, resonance -> R2 amplitude expression
+    std::function<std::string(int, int)> amp; // amplitude node, amplitude -> R2 amplitude expression
+    std::function<std::string(int)> ampcol;   // amplitude / derivative column -> R2 expression
     bool lohi = false;                        // normalisation factors as FP32 hi + lo pairs
     int uid = 0;
     std::string tmp(const char *p) { return std::string(p) + std::to_string(uid++); }
@@ -416,6 +417,19 @@ Val emit(Ctx &c, int i) {
             gadd(c, out, slot(c, n.params[2 * r + 1]),
                  "R(2) * (" + ti + " * " + b + ".x - " + tr + " * " + b + ".y) * " + ev.v);
         }
+        // resonance / line-shape parameters: d|T|^2/dt = 2 Re(conj(T) sum_a c_a dA_a/dt)
+        if(c.grad && c.ampcol)
+            for(const AmpTheta &t : c.T.amp_theta(ai)) {
+                std::string dr = c.tmp("dr"), di = c.tmp("di");
+                os << "    R " << dr << " = R(0), " << di << " = R(0);\n";
+                for(size_t j = 0; j < t.amps.size(); ++j) {
+                    const int a = t.amps[j];
+                    std::string d = c.ampcol(t.col0 + (int)j), cr = P(n.params[2 * a]), cim = P(n.params[2 * a + 1]);
+                    os << "    " << dr << " += " << cr << " * " << d << ".x - " << cim << " * " << d << ".y;\n";
+                    os << "    " << di << " += " << cr << " * " << d << ".y + " << cim << " * " << d << ".x;\n";
+                }
+                gadd(c, out, t.slot, "R(2) * (" + tr + " * " + dr + " + " + ti + " * " + di + ") * " + ev.v);
+            }
         break;
     }
     case GF_OP_RES_RBW:
@@ -460,10 +474,11 @@ struct GfArgs {
     const int *dirty;          /* [toy] amplitude caches to rebuild */
     const double *const *nevt; /* per Amp4Body: normalisation events, SoA 5 x nnorm */
     const i64 *nnorm;
+    void *const *nscr;         /* per amplitude node: normalisation-point columns of toy gtoy */
     int n_chunks;
     int n_toys;
     int metric;
-    int pad;
+    int gtoy;                  /* toy of the normalisation pass */
 };
 
 __device__ __forceinline__ double gf_warp_sum(double v) {
@@ -845,41 +860,192 @@ __device__ __forceinline__ double gf_bl(double z2, int L) {
 __device__ __forceinline__ double gf_bl2(double z2, int L) {
     return L == 0 ? 1.0 : (L == 1 ? 1.0 / (1 + z2) : 1.0 / (z2 * z2 + 3 * z2 + 9));
 }
-// BW (RBW, with mass-dependent width) or SBW (constant width) line shape
+// BW (RBW, with mass-dependent width) or SBW (constant width) line shape; the body is gf_lineshape_t
 __device__ __forceinline__ double2 gf_lineshape(bool sbw, double Mpair, double m1, double m2, double mass, double width,
-                                                int orbital, int FF, double radius) {
+                                                int orbital, int FF, double radius);
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+)CUDA";
+
+// The 4-body line shapes for double or dual mass / width (the value path uses T = double).
+const char *kPreludeAmp4T = R"CUDA(
+template <typename T>
+__device__ __forceinline__ T gf_blp_t(T z2, T z02, int L) {
+    return L == 0 ? T(1.0) : (L == 1 ? (1 + z02) / (1 + z2) : (z02 * z02 + 3 * z02 + 9) / (z2 * z2 + 3 * z2 + 9));
+}
+template <typename T>
+__device__ __forceinline__ void gf_lineshape_t(bool sbw, double Mpair, double m1, double m2, T mass, T width,
+                                               int orbital, int FF, double radius, T &re, T &im) {
     const double mr2 = Mpair * Mpair;
     const double mpsq = (m1 + m2) * (m1 + m2), mmsq = (m1 - m2) * (m1 - m2);
-    const double num = (mr2 - mpsq) * (mr2 - mmsq), num2 = (mass * mass - mpsq) * (mass * mass - mmsq);
+    const double num = (mr2 - mpsq) * (mr2 - mmsq);
+    const T num2 = (mass * mass - mpsq) * (mass * mass - mmsq);
     const double pABSq = num / (4 * mr2);
-    double prSq = num2 / (4 * mass * mass);
-    const double prSq2 = prSq < 0 ? 0 : prSq;
+    T prSq = num2 / (4 * mass * mass);
+    const T prSq2 = dval(prSq) < 0 ? T(0.0) : prSq;
     prSq = fabs(prSq);
     const double r2 = radius * radius;
-    double fr = 1;
+    T fr = T(1.0);
     if(0 != orbital && 0 != FF) {
-        fr = (FF == 1 ? gf_bl(pABSq * r2, orbital) : gf_blp(pABSq * r2, prSq2 * r2, orbital));
-        fr = (FF == 3 ? gf_bl2(pABSq * r2, orbital) : fr);
+        fr = (FF == 1 ? T(gf_bl(pABSq * r2, orbital)) : gf_blp_t<T>(T(pABSq * r2), prSq2 * r2, orbital));
+        fr = (FF == 3 ? T(gf_bl2(pABSq * r2, orbital)) : fr);
     }
-    double GofM, k;
+    T GofM, k;
     if(!sbw) {
-        const double pratio = sqrt(pABSq / prSq);
-        double pj = 1;
+        const T pratio = sqrt(pABSq / prSq);
+        T pj = T(1.0);
         for(int i = 0; i < 2 * orbital + 1; i++)
-            pj *= pratio;
-        GofM = width * pj * (mass / Mpair) * gf_blp(pABSq * r2, prSq * r2, orbital);
-        const double gamma = mass * sqrt((mass * mass + width * width));
+            pj = pj * pratio;
+        GofM = width * pj * (mass / Mpair) * gf_blp_t<T>(T(pABSq * r2), prSq * r2, orbital);
+        const T gamma = mass * sqrt((mass * mass + width * width));
         k = (2.0 * sqrt(2.0) / 3.14159265358979323846) * mass * width * gamma / sqrt(mass * mass + gamma);
     } else {
         GofM = width;
-        const double gamma = sqrt(mass * mass * (mass * mass + width * width));
+        const T gamma = sqrt(mass * mass * (mass * mass + width * width));
         k = mass * width * gamma / sqrt(mass * mass + gamma);
     }
-    const double den = (mass * mass - mr2) * (mass * mass - mr2) + mass * GofM * mass * GofM;
-    const double f = sqrt(k * fr) / den;
-    return make_double2(f * (mass * mass - mr2), f * (mass * GofM));
+    const T den = (mass * mass - mr2) * (mass * mass - mr2) + mass * GofM * mass * GofM;
+    const T f = sqrt(k * fr) / den;
+    re = f * (mass * mass - mr2);
+    im = f * (mass * GofM);
 }
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+)CUDA";
+
+// The 3-body relativistic Breit-Wigner for double or dual mass / width, FP64 (the derivative path).
+const char *kPreludeAmp3T = R"CUDA(
+template <typename T>
+__device__ __forceinline__ T gf_tb_mom_t(T s, double a, double b) {
+    T k1 = 1.0 - (a + b) * (a + b) / s;
+    k1   = dval(k1) >= 0 ? sqrt(k1) : T(1.0);
+    T k2 = 1.0 - (a - b) * (a - b) / s;
+    k2   = dval(k2) >= 0 ? sqrt(k2) : T(1.0);
+    return 0.5 * sqrt(s) * k1 * k2;
+}
+template <typename T>
+__device__ __forceinline__ T gf_tb_mom_mother_t(T s, double M, double c) {
+    T k1 = 1.0 - (M + c) * (M + c) / s;
+    k1   = dval(k1) >= 0 ? sqrt(k1) : T(1.0);
+    T k2 = 1.0 - (M - c) * (M - c) / s;
+    k2   = dval(k2) >= 0 ? sqrt(k2) : T(1.0);
+    return 0.5 * s * k1 * k2 / M;
+}
+template <typename T>
+__device__ __forceinline__ T gf_damp2_t(T p, int spin, double r) {
+    const T sq = r * r * p * p;
+    return spin == 2 ? 13.0 * sq / ((sq - 3.0) * (sq - 3.0)) + 9.0 * sq * sq : 2.0 * sq;
+}
+template <typename T>
+__device__ __forceinline__ T gf_damp2n_t(T p, int spin, double r) {
+    const T sq = r * r * p * p;
+    const T d  = 1.0 + sq;
+    return spin == 2 ? d + 8.0 + 2.0 * sq + sq * sq : d;
+}
+__device__ __forceinline__ double gf_spin_d(int spin, double M, double m1, double m2, double m3, double m12, double m13,
+                                            double m23, int cyc) {
+    if(spin == 0)
+        return 1.0;
+    const double mA = cyc == 0 ? m1 : (cyc == 1 ? m3 : m2), mB = cyc == 0 ? m2 : (cyc == 1 ? m1 : m3);
+    const double mC = cyc == 0 ? m3 : (cyc == 1 ? m2 : m1);
+    const double mAC = cyc == 0 ? m13 : (cyc == 1 ? m23 : m12), mBC = cyc == 0 ? m23 : (cyc == 1 ? m12 : m13);
+    const double mAB = cyc == 0 ? m12 : (cyc == 1 ? m13 : m23);
+    const double massFactor = 1.0 / mAB;
+    const double MC = M * M - mC * mC, AB = mA * mA - mB * mB;
+    double sf = -((mBC - mAC) + massFactor * MC * AB);
+    if(spin == 2) {
+        sf *= sf;
+        double ex = ((mAB - 2 * M * M - 2 * mC * mC) + massFactor * MC * MC);
+        ex *= ((mAB - 2 * mA * mA - 2 * mB * mB) + massFactor * AB * AB);
+        ex /= 3;
+        sf -= ex;
+    }
+    return sf;
+}
+template <int I, typename T>
+__device__ __forceinline__ void gf_rbw_t(double m12, double m13, double m23, T mass, T width, int spin, int cyc,
+                                         bool norm, double M, double m1, double m2, double m3, double r, double rm,
+                                         T &re, T &im) {
+    re = T(0.0);
+    im = T(0.0);
+    const T rm2 = mass * mass;
+#pragma unroll
+    for(int it = 0; it < I; ++it) {
+        const double sq = cyc == 0 ? m12 : (cyc == 1 ? m13 : m23);
+        const double d1 = cyc == 2 ? m2 : m1, d2 = cyc == 0 ? m2 : m3;
+        const double bach = cyc == 0 ? m3 : (cyc == 1 ? m2 : m1);
+        T fr = T(1.0), frM = T(1.0);
+        const double pm = gf_tb_mom_t<double>(sq, d1, d2);
+        const T pn      = gf_tb_mom_t<T>(rm2, d1, d2);
+        double pmM;
+        T pnM = T(0.0);
+        if(norm) {
+            pmM = gf_tb_mom_mother_t<double>(sq, M, bach);
+            pnM = gf_tb_mom_mother_t<T>(rm2, M, bach);
+        } else
+            pmM = gf_tb_mom_t<double>(M * M, sqrt(sq), bach);
+        if(spin != 0) {
+            if(norm) {
+                fr  = gf_damp2n_t<T>(pn, spin, r) / gf_damp2n_t<double>(pm, spin, r);
+                frM = gf_damp2n_t<T>(pnM, spin, rm) / gf_damp2n_t<double>(pmM, spin, rm);
+            } else {
+                fr  = T(gf_damp2_t<double>(pm, spin, r));
+                frM = T(gf_damp2_t<double>(pmM, spin, rm));
+            }
+        }
+        const T A = rm2 - sq;
+        const T q = pm / pn;
+        T qp      = q;
+        for(int k = 0; k < 2 * spin; ++k)
+            qp = qp * q;
+        const T B = rm2 * width * qp * fr / sqrt(sq);
+        const T C = 1.0 / (A * A + B * B);
+        T xr = A * C, xi = B * C;
+        const T f1 = sqrt(fr), f2 = sqrt(frM);
+        const double sf = gf_spin_d(spin, M, m1, m2, m3, m12, m13, m23, cyc);
+        xr = xr * f1 * f2 * sf;
+        xi = xi * f1 * f2 * sf;
+        re = re + xr;
+        im = im + xi;
+        if(I > 1)
+            cyc = (cyc + 1) % 3;
+    }
+}
+)CUDA";
+
+// Forward-mode dual numbers (value and the derivatives with respect to a resonance's mass and width) for the
+// analytic gradient of the cached amplitudes, and the relativistic Breit-Wigner of the 3-body path written
+// once for double and for duals (FP64 throughout: it runs only when those parameters change).
+const char *kPreludeDual = R"CUDA(
+struct GfDual {
+    double v, a, b;
+    __device__ __forceinline__ GfDual(double v_ = 0, double a_ = 0, double b_ = 0) : v(v_), a(a_), b(b_) {}
+};
+__device__ __forceinline__ double dval(double x) { return x; }
+__device__ __forceinline__ double dval(const GfDual &x) { return x.v; }
+__device__ __forceinline__ GfDual operator+(GfDual x, GfDual y) { return GfDual(x.v + y.v, x.a + y.a, x.b + y.b); }
+__device__ __forceinline__ GfDual operator-(GfDual x, GfDual y) { return GfDual(x.v - y.v, x.a - y.a, x.b - y.b); }
+__device__ __forceinline__ GfDual operator-(GfDual x) { return GfDual(-x.v, -x.a, -x.b); }
+__device__ __forceinline__ GfDual operator*(GfDual x, GfDual y) {
+    return GfDual(x.v * y.v, x.a * y.v + x.v * y.a, x.b * y.v + x.v * y.b);
+}
+__device__ __forceinline__ GfDual operator/(GfDual x, GfDual y) {
+    const double q = x.v / y.v;
+    return GfDual(q, (x.a - q * y.a) / y.v, (x.b - q * y.b) / y.v);
+}
+__device__ __forceinline__ GfDual operator+(GfDual x, double y) { return GfDual(x.v + y, x.a, x.b); }
+__device__ __forceinline__ GfDual operator+(double y, GfDual x) { return GfDual(x.v + y, x.a, x.b); }
+__device__ __forceinline__ GfDual operator-(GfDual x, double y) { return GfDual(x.v - y, x.a, x.b); }
+__device__ __forceinline__ GfDual operator-(double y, GfDual x) { return GfDual(y - x.v, -x.a, -x.b); }
+__device__ __forceinline__ GfDual operator*(GfDual x, double y) { return GfDual(x.v * y, x.a * y, x.b * y); }
+__device__ __forceinline__ GfDual operator*(double y, GfDual x) { return GfDual(x.v * y, x.a * y, x.b * y); }
+__device__ __forceinline__ GfDual operator/(GfDual x, double y) { return GfDual(x.v / y, x.a / y, x.b / y); }
+__device__ __forceinline__ GfDual operator/(double y, GfDual x) {
+    const double q = y / x.v;
+    return GfDual(q, -q * x.a / x.v, -q * x.b / x.v);
+}
+__device__ __forceinline__ GfDual sqrt(GfDual x) {
+    const double r = sqrt(x.v);
+    return GfDual(r, x.a / (2 * r), x.b / (2 * r));
+}
+__device__ __forceinline__ GfDual fabs(GfDual x) { return x.v < 0 ? -x : x; }
 )CUDA";
 
 // Where every normalisation factor is kept (see NormLayout in tree.h).
@@ -1284,18 +1450,89 @@ struct Gen {
         return lit(A.M) + ", " + lit(A.m1) + ", " + lit(A.m2) + ", " + lit(A.m3);
     }
 
-    // Device function computing every amplitude of Amp4Body node k at one point of the five variables:
-    // distinct line shapes and spin factors once, then AmpCalc's sum over permutations of their products
-    // (src/PDFs/physics/detail/AmpCalc.cu:29-56).
-    void amp4Function(int k) {
-        const Amp4Info &A = T.amp4s[k];
+    // ---- amplitude nodes: values and derivative columns at one point ----
+    int nDeriv(int k) const {
+        int n = 0;
+        for(auto &t : T.amp_theta(k))
+            n += (int)t.amps.size();
+        return n;
+    }
+    bool thetaParam(int k, int p) const {
+        for(auto &t : T.amp_theta(k))
+            if(t.param == p)
+                return true;
+        return false;
+    }
+    // d(component)/d(theta t) from the partials with respect to the component's mass (pm) and width (pw)
+    std::string dPart(int t_param, int mass_p, int width_p, const std::string &dm, const std::string &dw) {
+        std::string e;
+        if(mass_p == t_param)
+            e = dm;
+        if(width_p == t_param)
+            e = e.empty() ? dw : "make_double2(" + e + ".x + " + dw + ".x, " + e + ".y + " + dw + ".y)";
+        return e;
+    }
+
+    // __device__ gf_ampv_<k>(point, P, A, dA): the amplitudes of amplitude node k (unified numbering) at one
+    // point and, for every floated resonance / line-shape parameter t, dA_a/dt of the amplitudes depending on
+    // it (in AmpTheta order).  Amp3Body: SpecialResonanceCalculator (zero outside the kinematic boundary);
+    // Amp4Body: the line shapes and spin factors once, then AmpCalc's sum over permutations
+    // (src/PDFs/physics/detail/AmpCalc.cu:29-56) and its derivatives by the product rule.
+    void ampFunction(int k) {
+        const int n3 = (int)T.amp3s.size();
+        const auto &theta = T.amp_theta(k);
+        const int ND = std::max(1, nDeriv(k));
+        std::vector<int> toff;
+        for(int t = 0, o = 0; t < (int)theta.size(); ++t) {
+            toff.push_back(o);
+            o += (int)theta[t].amps.size();
+        }
+        if(k < n3) {
+            const Amp3Info &A = T.amp3s[k];
+            os << "__device__ void gf_ampv_" << k << "(double m12, double m13, const double *P, R2 *A, R2 *dA) {\n";
+            os << "  for(int q = 0; q < " << A.nRes << "; ++q) { A[q].x = R(0); A[q].y = R(0); }\n";
+            os << "  for(int q = 0; q < " << ND << "; ++q) { dA[q].x = R(0); dA[q].y = R(0); }\n";
+            os << "  if(!gf_in_dalitz(m12, m13, " << dalitzArgs(A) << ")) return;\n";
+            os << "  const double m23 = gf_m23(m12, m13, " << dalitzArgs(A) << ");\n";
+            for(int r = 0; r < A.nRes; ++r) {
+                const TNode &rn = T.nodes[A.res[r]];
+                const bool dep = rn.op == GF_OP_RES_RBW && (thetaParam(k, rn.params[0]) || thetaParam(k, rn.params[1]));
+                if(!dep) {
+                    os << "  A[" << r << "] = " << resCall(A, r, "m12", "m13", "m23") << ";\n";
+                    continue;
+                }
+                const int I = (rn.consts.size() > 3 && rn.consts[3] != 0) ? 2 : 1;
+                os << "  { GfDual re, im;\n";
+                os << "    gf_rbw_t<" << I << ", GfDual>(m12, m13, m23, GfDual(P[" << rn.params[0] << "], 1.0, 0.0), GfDual(P["
+                   << rn.params[1] << "], 0.0, 1.0), " << (int)rn.consts[0] << ", " << (int)rn.consts[1] << ", "
+                   << (rn.consts[2] != 0 ? "true" : "false") << ", " << lit(A.M) << ", " << lit(A.m1) << ", " << lit(A.m2)
+                   << ", " << lit(A.m3) << ", " << lit(A.r) << ", " << lit(A.rm) << ", re, im);\n";
+                os << "    A[" << r << "].x = (R)re.v; A[" << r << "].y = (R)im.v;\n";
+                os << "    const double2 dm = make_double2(re.a, im.a), dw = make_double2(re.b, im.b); (void)dm; (void)dw;\n";
+                for(int t = 0; t < (int)theta.size(); ++t) {
+                    auto it = std::find(theta[t].amps.begin(), theta[t].amps.end(), r);
+                    if(it == theta[t].amps.end())
+                        continue;
+                    std::string e = dPart(theta[t].param, rn.params[0], rn.params[1], "dm", "dw");
+                    const int idx = toff[t] + (int)(it - theta[t].amps.begin());
+                    os << "    { const double2 d = " << e << "; dA[" << idx << "].x = (R)d.x; dA[" << idx
+                       << "].y = (R)d.y; }\n";
+                }
+                os << "  }\n";
+            }
+            os << "}\n\n";
+            return;
+        }
+        const Amp4Info &A = T.amp4s[k - n3];
         const double m1 = A.m[0], m2 = A.m[1], m3 = A.m[2], m4 = A.m[3];
-        os << "__device__ void gf_amp4_" << k
-           << "(double m12, double m34, double c12, double c34, double phi, const double *P, double2 *A) {\n";
+        os << "__device__ void gf_ampv_" << k
+           << "(double m12, double m34, double c12, double c34, double phi, const double *P, R2 *A, R2 *dA) {\n";
+        os << "  for(int q = 0; q < " << ND << "; ++q) { dA[q].x = R(0); dA[q].y = R(0); }\n";
         os << "  GfLV V[4];\n";
         os << "  gf_get4vecs(V, m12, m34, c12, c34, phi, " << lit(A.M) << ", " << lit(m1) << ", " << lit(m2) << ", "
            << lit(m3) << ", " << lit(m4) << ");\n";
         os << "  double d1, d2, mp; (void)d1; (void)d2; (void)mp;\n";
+        std::vector<int> lsDep(A.ls.size(), 0);
         for(size_t u = 0; u < A.ls.size(); ++u) {
             const TNode &L = T.nodes[A.ls[u]];
             const int pair = (int)L.consts[0];
@@ -1305,9 +1542,21 @@ struct Gen {
             else
                 os << "  mp = gf_pairmass(" << pair << ", V, " << lit(m1) << ", " << lit(m2) << ", " << lit(m3) << ", "
                    << lit(m4) << ", d1, d2);\n";
-            os << "  const double2 L" << u << " = gf_lineshape(" << (L.op == GF_OP_LS_SBW ? "true" : "false")
-               << ", mp, d1, d2, P[" << L.params[0] << "], P[" << L.params[1] << "], " << (int)L.consts[1] << ", "
-               << (int)L.consts[2] << ", " << lit(L.consts[3]) << ");\n";
+            lsDep[u] = thetaParam(k, L.params[0]) || thetaParam(k, L.params[1]);
+            const std::string sbw = L.op == GF_OP_LS_SBW ? "true" : "false";
+            if(!lsDep[u]) {
+                os << "  const double2 L" << u << " = gf_lineshape(" << sbw << ", mp, d1, d2, P[" << L.params[0] << "], P["
+                   << L.params[1] << "], " << (int)L.consts[1] << ", " << (int)L.consts[2] << ", " << lit(L.consts[3])
+                   << ");\n";
+            } else {
+                os << "  double2 L" << u << ", Lm" << u << ", Lw" << u << ";\n";
+                os << "  { GfDual re, im;\n";
+                os << "    gf_lineshape_t<GfDual>(" << sbw << ", mp, d1, d2, GfDual(P[" << L.params[0]
+                   << "], 1.0, 0.0), GfDual(P[" << L.params[1] << "], 0.0, 1.0), " << (int)L.consts[1] << ", "
+                   << (int)L.consts[2] << ", " << lit(L.consts[3]) << ", re, im);\n";
+                os << "    L" << u << " = make_double2(re.v, im.v); Lm" << u << " = make_double2(re.a, im.a); Lw" << u
+                   << " = make_double2(re.b, im.b); }\n";
+            }
         }
         for(size_t u = 0; u < A.sf.size(); ++u) {
             const TNode &S = T.nodes[A.sf[u]];
@@ -1315,32 +1564,82 @@ struct Gen {
                << (int)S.consts[2] << "], V[" << (int)S.consts[3] << "], V[" << (int)S.consts[4] << "], V["
                << (int)S.consts[5] << "]);\n";
         }
+        // product of one permutation's factors, with factor `skip` (a line-shape position) replaced by `repl`
+        auto product = [&](const Amp4Info::Amp &am, int p, int skip, const std::string &repl) {
+            const int ls_step = (int)am.ls.size() / am.nPerm, sf_step = (int)am.sf.size() / am.nPerm;
+            std::ostringstream o;
+            o << "    { double2 r = make_double2(1.0, 0.0);\n";
+            for(int j = p * ls_step; j < (p + 1) * ls_step; ++j)
+                o << "      r = cmul(r, " << (j == skip ? repl : "L" + std::to_string(am.ls[j])) << ");\n";
+            for(int j = p * sf_step; j < (p + 1) * sf_step; ++j)
+                o << "      r.x *= S" << am.sf[j] << "; r.y *= S" << am.sf[j] << ";\n";
+            o << "      r2.x += r.x; r2.y += r.y; }\n";
+            return o.str();
+        };
         for(int a = 0; a < A.nAmp; ++a) {
             const Amp4Info::Amp &am = A.amps[a];
-            const int ls_step = (int)am.ls.size() / am.nPerm, sf_step = (int)am.sf.size() / am.nPerm;
             os << "  {\n    double2 r2 = make_double2(0.0, 0.0);\n";
-            for(int p = 0; p < am.nPerm; ++p) {
-                os << "    { double2 r = make_double2(1.0, 0.0);\n";
-                for(int j = p * ls_step; j < (p + 1) * ls_step; ++j)
-                    os << "      r = cmul(r, L" << am.ls[j] << ");\n";
-                for(int j = p * sf_step; j < (p + 1) * sf_step; ++j)
-                    os << "      r.x *= S" << am.sf[j] << "; r.y *= S" << am.sf[j] << ";\n";
-                os << "      r2.x += r.x; r2.y += r.y; }\n";
-            }
+            for(int p = 0; p < am.nPerm; ++p)
+                os << product(am, p, -1, "");
             os << "    const double f = 1 / sqrt((double)" << am.nPerm << ");\n";
-            os << "    A[" << a << "] = make_double2(r2.x * f, r2.y * f);\n  }\n";
+            os << "    A[" << a << "].x = (R)(r2.x * f); A[" << a << "].y = (R)(r2.y * f);\n  }\n";
         }
+        for(int t = 0; t < (int)theta.size(); ++t)
+            for(size_t j = 0; j < theta[t].amps.size(); ++j) {
+                const int a = theta[t].amps[j];
+                const Amp4Info::Amp &am = A.amps[a];
+                const int ls_step = (int)am.ls.size() / am.nPerm;
+                os << "  {\n    double2 r2 = make_double2(0.0, 0.0);\n";
+                for(int p = 0; p < am.nPerm; ++p)
+                    for(int pos = p * ls_step; pos < (p + 1) * ls_step; ++pos) {
+                        const int u = am.ls[pos];
+                        if(!lsDep[u])
+                            continue;
+                        const TNode &L = T.nodes[A.ls[u]];
+                        std::string d = dPart(theta[t].param, L.params[0], L.params[1], "Lm" + std::to_string(u),
+                                              "Lw" + std::to_string(u));
+                        if(d.empty())
+                            continue;
+                        os << product(am, p, pos, d);
+                    }
+                os << "    const double f = 1 / sqrt((double)" << am.nPerm << ");\n";
+                const int idx = toff[t] + (int)j;
+                os << "    dA[" << idx << "].x = (R)(r2.x * f); dA[" << idx << "].y = (R)(r2.y * f);\n  }\n";
+            }
         os << "}\n\n";
     }
 
+    // Entries of the normalisation reduction of amplitude node k: the pairs i <= j of the Gram matrix
+    // I_ij = sum_p A_i conj(A_j) e_p, then for every floated parameter t and dependent amplitude a the row
+    // H_t,ab = sum_p dA_a/dt conj(A_b) e_p (e_p the efficiency at an Amp3Body bin, 1 for Amp4Body).
+    struct Entry {
+        bool h;
+        int i, j; // value columns (pairs) or derivative index (i) and value column (j)
+    };
+    std::vector<Entry> entries(int k) {
+        std::vector<Entry> e;
+        const int n = T.amp_count(k);
+        for(int i = 0; i < n; ++i)
+            for(int j = i; j < n; ++j)
+                e.push_back({false, i, j});
+        int d = 0;
+        for(auto &t : T.amp_theta(k))
+            for(size_t q = 0; q < t.amps.size(); ++q, ++d)
+                for(int b = 0; b < n; ++b)
+                    e.push_back({true, d, b});
+        return e;
+    }
+
     void ampKernels() {
-        const int NAN_ = T.n_amp_nodes();
-        if(NAN_ == 0)
+        const int NK = T.n_amp_nodes();
+        if(NK == 0)
             return;
-        for(size_t k = 0; k < T.amp4s.size(); ++k)
-            amp4Function((int)k);
+        for(int k = 0; k < NK; ++k)
+            ampFunction(k);
         const int NA = T.n_amp_cols, NO = (int)T.obs.size(), np = std::max(1, T.n_params);
         const int n3 = (int)T.amp3s.size();
+
+        // data events -> value and derivative columns of every dirty toy
         os << "extern \"C\" __global__ void __launch_bounds__(256) gf_amp(const GfArgs a) {\n";
         os << "  const int toy = blockIdx.y, k = blockIdx.z, tid = threadIdx.x;\n";
         os << "  if(!a.dirty[toy]) return;\n";
@@ -1348,102 +1647,66 @@ struct Gen {
         os << "  const double *P = a.P + (i64)toy * " << np << "; (void)P;\n";
         os << "  R2 *const *ac = reinterpret_cast<R2 *const *>(const_cast<void **>(a.acol)) + (i64)toy * " << NA << ";\n";
         os << "  switch(k) {\n";
-        for(int ai = 0; ai < n3; ++ai) {
-            const Amp3Info &A = T.amp3s[ai];
-            os << "  case " << ai << ": {\n";
-            os << "    const double *x12 = a.dcol[(i64)toy * " << NO << " + " << A.o12 << "];\n";
-            os << "    const double *x13 = a.dcol[(i64)toy * " << NO << " + " << A.o13 << "];\n";
+        for(int k = 0; k < NK; ++k) {
+            const int nAmp = T.amp_count(k), ND = std::max(1, nDeriv(k));
+            const auto &theta = T.amp_theta(k);
+            os << "  case " << k << ": {\n";
+            const int nv = k < n3 ? 2 : 5;
+            std::vector<int> ob;
+            if(k < n3)
+                ob = {T.amp3s[k].o12, T.amp3s[k].o13};
+            else
+                ob.assign(T.amp4s[k - n3].obs, T.amp4s[k - n3].obs + 5);
+            for(int v = 0; v < nv; ++v)
+                os << "    const double *x" << v << " = a.dcol[(i64)toy * " << NO << " + " << ob[v] << "];\n";
+            os << "    R2 A[" << nAmp << "], dA[" << ND << "];\n";
             os << "    for(i64 i = (i64)blockIdx.x * 256 + tid; i < npad; i += (i64)gridDim.x * 256) {\n";
-            for(int r = 0; r < A.nRes; ++r)
-                os << "      R2 b" << r << "; b" << r << ".x = R(0); b" << r << ".y = R(0);\n";
-            os << "      if(i < n) {\n";
-            os << "        const double m12 = x12[i], m13 = x13[i];\n";
-            os << "        if(gf_in_dalitz(m12, m13, " << dalitzArgs(A) << ")) {\n";
-            os << "          const double m23 = gf_m23(m12, m13, " << dalitzArgs(A) << ");\n";
-            for(int r = 0; r < A.nRes; ++r)
-                os << "          b" << r << " = " << resCall(A, r, "m12", "m13", "m23") << ";\n";
-            os << "        }\n      }\n";
-            for(int r = 0; r < A.nRes; ++r)
-                os << "      ac[" << A.col0 + r << "][i] = b" << r << ";\n";
-            os << "    }\n    break; }\n";
-        }
-        for(size_t k4 = 0; k4 < T.amp4s.size(); ++k4) {
-            const Amp4Info &A = T.amp4s[k4];
-            os << "  case " << n3 + (int)k4 << ": {\n";
-            for(int v = 0; v < 5; ++v)
-                os << "    const double *x" << v << " = a.dcol[(i64)toy * " << NO << " + " << A.obs[v] << "];\n";
-            os << "    double2 A[" << A.nAmp << "];\n";
-            os << "    for(i64 i = (i64)blockIdx.x * 256 + tid; i < npad; i += (i64)gridDim.x * 256) {\n";
-            os << "      if(i < n) gf_amp4_" << k4 << "(x0[i], x1[i], x2[i], x3[i], x4[i], P, A);\n";
-            os << "      else for(int q = 0; q < " << A.nAmp << "; ++q) A[q] = make_double2(0.0, 0.0);\n";
-            for(int q = 0; q < A.nAmp; ++q)
-                os << "      { R2 b; b.x = (R)A[" << q << "].x; b.y = (R)A[" << q << "].y; ac[" << A.col0 + q
-                   << "][i] = b; }\n";
+            os << "      if(i < n) gf_ampv_" << k << "(" << (k < n3 ? "x0[i], x1[i]" : "x0[i], x1[i], x2[i], x3[i], x4[i]")
+               << ", P, A, dA);\n";
+            os << "      else { for(int q = 0; q < " << nAmp << "; ++q) { A[q].x = R(0); A[q].y = R(0); }\n";
+            os << "             for(int q = 0; q < " << ND << "; ++q) { dA[q].x = R(0); dA[q].y = R(0); } }\n";
+            for(int q = 0; q < nAmp; ++q)
+                os << "      ac[" << T.amp_col0(k) + q << "][i] = A[" << q << "];\n";
+            for(int t = 0, d = 0; t < (int)theta.size(); ++t)
+                for(size_t j = 0; j < theta[t].amps.size(); ++j, ++d)
+                    os << "      ac[" << theta[t].col0 + (int)j << "][i] = dA[" << d << "];\n";
             os << "    }\n    break; }\n";
         }
         os << "  default: break;\n  }\n}\n\n";
 
-        // integrals: tiles of at most 36 pairs per CTA row
-        plan.gram_tiles.clear();
-        plan.gram_pairs_max = 0;
-        plan.dgrid_off.clear();
-        int64_t goff = 0;
-        for(int ai = 0; ai < NAN_; ++ai) {
-            const int n = T.amp_count(ai), npairs = n * (n + 1) / 2;
-            for(int p0 = 0; p0 < npairs; p0 += 36) {
-                KernelPlan::GramTile t{ai, p0, std::min(npairs, p0 + 36)};
-                plan.gram_tiles.push_back(t);
-                plan.gram_pairs_max = std::max(plan.gram_pairs_max, t.p1 - t.p0);
-            }
-            if(ai < n3) {
-                plan.dgrid_off.push_back(goff);
-                goff += (int64_t)T.amp3s[ai].grid.size();
-            }
-        }
-        const int PM = plan.gram_pairs_max, NW = 256 / 32;
-        os << "extern \"C\" __global__ void __launch_bounds__(256) gf_gram(const GfArgs a) {\n";
-        os << "  const int toy = blockIdx.y, z = blockIdx.z, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;\n";
-        os << "  if(!a.dirty[toy]) return;\n";
+        // normalisation points of toy a.gtoy -> scratch columns [value | derivative][point], then the efficiency
+        os << "extern \"C\" __global__ void __launch_bounds__(256) gf_ampn(const GfArgs a) {\n";
+        os << "  const int toy = a.gtoy, k = blockIdx.z, tid = threadIdx.x;\n";
         os << "  const double *P = a.P + (i64)toy * " << np << "; (void)P;\n";
         os << "  const R *Pr = reinterpret_cast<const R *>(a.Pr) + (i64)toy * " << plan.nl.npr << "; (void)Pr;\n";
         for(int j = 0; j < T.n_params; ++j)
             os << "  const R p" << j << " = Pr[" << j << "]; (void)p" << j << ";\n";
-        os << "  __shared__ double red[" << NW << "][" << 2 * PM << "];\n";
-        os << "  double *out = a.gram + (((i64)toy * " << plan.gram_tiles.size() << " + z) * gridDim.x + blockIdx.x) * "
-           << 2 * PM << ";\n";
-        os << "  switch(z) {\n";
-        for(size_t ti = 0; ti < plan.gram_tiles.size(); ++ti) {
-            const auto &tile = plan.gram_tiles[ti];
-            const int nAmp   = T.amp_count(tile.amp);
-            std::vector<std::pair<int, int>> pairs;
-            for(int i = 0, q = 0; i < nAmp; ++i)
-                for(int j = i; j < nAmp; ++j, ++q)
-                    if(q >= tile.p0 && q < tile.p1)
-                        pairs.push_back({i, j});
-            std::vector<int> need(nAmp, 0);
-            for(auto &pr : pairs)
-                need[pr.first] = need[pr.second] = 1;
-            const int npr = (int)pairs.size();
-            os << "  case " << ti << ": {\n";
-            for(int q = 0; q < npr; ++q)
-                os << "    R sr" << q << " = R(0), si" << q << " = R(0);\n";
-            std::string effv = "R(1)";
-            if(tile.amp < n3) {
-                const Amp3Info &A = T.amp3s[tile.amp];
+        os << "  switch(k) {\n";
+        plan.dgrid_off.clear();
+        int64_t goff = 0;
+        for(int k = 0; k < NK; ++k) {
+            const int nAmp = T.amp_count(k), ND = std::max(1, nDeriv(k)), NC = nAmp + nDeriv(k);
+            os << "  case " << k << ": {\n";
+            os << "    R2 *sc = reinterpret_cast<R2 *>(a.nscr[" << k << "]);\n";
+            os << "    R2 A[" << nAmp << "], dA[" << ND << "];\n";
+            if(k < n3) {
+                const Amp3Info &A = T.amp3s[k];
+                plan.dgrid_off.push_back(goff);
                 const gf_observable &g12 = T.obs[A.o12], &g13 = T.obs[A.o13];
                 double w12 = g12.hi - g12.lo;
                 w12 /= A.nb12;
                 double w13 = g13.hi - g13.lo;
                 w13 /= A.nb13q;
-                os << "    const unsigned *pts = a.dgrid + " << plan.dgrid_off[tile.amp] << "LL;\n";
-                os << "    for(int p = blockIdx.x * 256 + tid; p < " << A.grid.size() << "; p += gridDim.x * 256) {\n";
+                const int64_t npts = (int64_t)A.grid.size();
+                os << "    const i64 npts = " << npts << "LL;\n";
+                os << "    R *se = reinterpret_cast<R *>(sc + " << NC << " * npts);\n";
+                os << "    const unsigned *pts = a.dgrid + " << goff << "LL;\n";
+                goff += npts;
+                os << "    for(i64 p = (i64)blockIdx.x * 256 + tid; p < npts; p += (i64)gridDim.x * 256) {\n";
                 os << "      const unsigned q = pts[p];\n";
                 os << "      const double c12 = gf_centre(" << lit(g12.lo) << ", " << lit(w12) << ", (int)(q & 0xffffu));\n";
                 os << "      const double c13 = gf_centre(" << lit(g13.lo) << ", " << lit(w13) << ", (int)(q >> 16));\n";
-                os << "      const double m23 = gf_m23(c12, c13, " << dalitzArgs(A) << ");\n";
-                for(int r = 0; r < A.nRes; ++r)
-                    if(need[r])
-                        os << "      const R2 b" << r << " = " << resCall(A, r, "c12", "c13", "m23") << ";\n";
+                os << "      gf_ampv_" << k << "(c12, c13, P, A, dA);\n";
                 // the efficiency at the bin centre; the reference's fake event holds 2 in slot 0
                 std::ostringstream body;
                 Ctx c{body, T, false, false, nullptr, nullptr, nullptr, nullptr};
@@ -1457,31 +1720,77 @@ struct Gen {
                 c.k   = [&](int) -> std::string { throw std::runtime_error("codegen: convolution in an efficiency"); };
                 c.tab = [&](int, int) -> std::string { throw std::runtime_error("codegen: convolution in an efficiency"); };
                 Val ev = emit(c, A.eff);
-                os << "      {\n" << body.str();
-                effv = ev.v;
+                os << "      {\n" << body.str() << "      se[p] = " << ev.v << ";\n      }\n";
             } else {
-                // Amp4Body: the flat phase-space events; the efficiency does not enter
-                // (NormIntegrator, src/PDFs/physics/detail/NormIntegrator.cu:15-68)
-                const int k4 = tile.amp - n3;
-                const Amp4Info &A = T.amp4s[k4];
+                const int k4 = k - n3;
                 os << "    const double *ne = a.nevt[" << k4 << "];\n";
-                os << "    const i64 nn = a.nnorm[" << k4 << "];\n";
-                os << "    double2 A[" << A.nAmp << "];\n";
-                os << "    for(i64 p = (i64)blockIdx.x * 256 + tid; p < nn; p += (i64)gridDim.x * 256) {\n";
-                os << "      gf_amp4_" << k4 << "(ne[p], ne[nn + p], ne[2 * nn + p], ne[3 * nn + p], ne[4 * nn + p], P, A);\n";
-                for(int r = 0; r < nAmp; ++r)
-                    if(need[r])
-                        os << "      R2 b" << r << "; b" << r << ".x = (R)A[" << r << "].x; b" << r << ".y = (R)A[" << r
-                           << "].y;\n";
-                os << "      {\n";
+                os << "    const i64 npts = a.nnorm[" << k4 << "];\n";
+                os << "    for(i64 p = (i64)blockIdx.x * 256 + tid; p < npts; p += (i64)gridDim.x * 256) {\n";
+                os << "      gf_ampv_" << k << "(ne[p], ne[npts + p], ne[2 * npts + p], ne[3 * npts + p], ne[4 * npts + p], P, A, dA);\n";
             }
-            os << "      const R e = " << effv << ";\n";
+            for(int q = 0; q < nAmp; ++q)
+                os << "      sc[" << q << " * npts + p] = A[" << q << "];\n";
+            for(int d = 0; d < nDeriv(k); ++d)
+                os << "      sc[" << nAmp + d << " * npts + p] = dA[" << d << "];\n";
+            os << "    }\n    break; }\n";
+        }
+        os << "  default: break;\n  }\n}\n\n";
+
+        // reduction of the scratch columns into the integral entries, tiles of at most 36 entries
+        plan.gram_tiles.clear();
+        plan.gram_pairs_max = 0;
+        for(int k = 0; k < NK; ++k) {
+            const int ne = (int)entries(k).size();
+            for(int p0 = 0; p0 < ne; p0 += 36) {
+                KernelPlan::GramTile t{k, p0, std::min(ne, p0 + 36)};
+                plan.gram_tiles.push_back(t);
+                plan.gram_pairs_max = std::max(plan.gram_pairs_max, t.p1 - t.p0);
+            }
+        }
+        const int PM = plan.gram_pairs_max, NW = 256 / 32;
+        os << "extern \"C\" __global__ void __launch_bounds__(256) gf_gram(const GfArgs a) {\n";
+        os << "  const int z = blockIdx.z, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;\n";
+        os << "  __shared__ double red[" << NW << "][" << 2 * PM << "];\n";
+        os << "  double *out = a.gram + ((i64)z * gridDim.x + blockIdx.x) * " << 2 * PM << ";\n";
+        os << "  switch(z) {\n";
+        for(size_t ti = 0; ti < plan.gram_tiles.size(); ++ti) {
+            const auto &tile = plan.gram_tiles[ti];
+            const int k = tile.amp, nAmp = T.amp_count(k), NC = nAmp + nDeriv(k);
+            const std::vector<Entry> all = entries(k);
+            std::vector<Entry> es(all.begin() + tile.p0, all.begin() + tile.p1);
+            std::vector<int> needV(nAmp, 0), needD(std::max(1, nDeriv(k)), 0);
+            for(auto &e : es) {
+                if(e.h) {
+                    needD[e.i] = 1;
+                    needV[e.j] = 1;
+                } else
+                    needV[e.i] = needV[e.j] = 1;
+            }
+            const int npr = (int)es.size();
+            os << "  case " << ti << ": {\n";
+            for(int q = 0; q < npr; ++q)
+                os << "    R sr" << q << " = R(0), si" << q << " = R(0);\n";
+            os << "    const R2 *sc = reinterpret_cast<const R2 *>(a.nscr[" << k << "]);\n";
+            if(k < n3)
+                os << "    const i64 npts = " << (int64_t)T.amp3s[k].grid.size() << "LL;\n"
+                   << "    const R *se = reinterpret_cast<const R *>(sc + " << NC << " * npts);\n";
+            else
+                os << "    const i64 npts = a.nnorm[" << k - n3 << "];\n";
+            os << "    for(i64 p = (i64)blockIdx.x * 256 + tid; p < npts; p += (i64)gridDim.x * 256) {\n";
+            os << "      const R e = " << (k < n3 ? "se[p]" : "R(1)") << ";\n";
+            for(int v = 0; v < nAmp; ++v)
+                if(needV[v])
+                    os << "      const R2 b" << v << " = sc[" << v << " * npts + p];\n";
+            for(int d = 0; d < nDeriv(k); ++d)
+                if(needD[d])
+                    os << "      const R2 g" << d << " = sc[" << nAmp + d << " * npts + p];\n";
             for(int q = 0; q < npr; ++q) {
-                int i = pairs[q].first, j = pairs[q].second;
-                os << "      sr" << q << " += (b" << i << ".x * b" << j << ".x + b" << i << ".y * b" << j << ".y) * e;\n";
-                os << "      si" << q << " += (b" << i << ".y * b" << j << ".x - b" << i << ".x * b" << j << ".y) * e;\n";
+                const std::string x = es[q].h ? "g" + std::to_string(es[q].i) : "b" + std::to_string(es[q].i);
+                const std::string y = "b" + std::to_string(es[q].j);
+                os << "      sr" << q << " += (" << x << ".x * " << y << ".x + " << x << ".y * " << y << ".y) * e;\n";
+                os << "      si" << q << " += (" << x << ".y * " << y << ".x - " << x << ".x * " << y << ".y) * e;\n";
             }
-            os << "      }\n    }\n";
+            os << "    }\n";
             for(int q = 0; q < npr; ++q) {
                 os << "    { const double t = gf_warp_sum((double)sr" << q << "); if(lane == 0) red[wid][" << 2 * q
                    << "] = t; }\n";
@@ -1537,7 +1846,15 @@ struct Gen {
                 return "tq" + std::to_string(ci) + fld[comp];
             return "tq" + std::to_string(ci) + "_" + std::to_string(comp / 4) + fld[comp % 4];
         };
-        c.amp = [&](int ai, int r) { return "am" + std::to_string(T.amp_col0(ai) + r); };
+        std::vector<int> aused(std::max(1, NA), 0);
+        c.amp = [&](int ai, int r) {
+            aused[T.amp_col0(ai) + r] = 1;
+            return "am" + std::to_string(T.amp_col0(ai) + r);
+        };
+        c.ampcol = [&](int col) {
+            aused[col] = 1;
+            return "am" + std::to_string(col);
+        };
         Val root = emit(c, 0);
         if(!values && !grad) {
             plan.obs_used_evt.clear();
@@ -1572,8 +1889,9 @@ struct Gen {
             os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(a.kcol[(i64)toy * " << NC << " + " << ci
                << "] + i0));\n";
         for(int ac = 0; ac < NA; ++ac)
-            os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(reinterpret_cast<const R2 *>(a.acol[(i64)toy * "
-               << NA << " + " << ac << "]) + i0));\n";
+            if(aused[ac])
+                os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(reinterpret_cast<const R2 *>(a.acol[(i64)toy * "
+                   << NA << " + " << ac << "]) + i0));\n";
         os << "      }\n    }\n  }\n";
         os << "  gf_pdl_wait();\n";
         os << "  __syncthreads();\n";
@@ -1607,8 +1925,9 @@ struct Gen {
         for(int ci = 0; ci < NC; ++ci)
             os << "    const int *kc" << ci << " = a.kcol[(i64)toy * " << NC << " + " << ci << "];\n";
         for(int ac = 0; ac < NA; ++ac)
-            os << "    const R2 *acp" << ac << " = reinterpret_cast<const R2 *>(a.acol[(i64)toy * " << NA << " + " << ac
-               << "]);\n";
+            if(aused[ac])
+                os << "    const R2 *acp" << ac << " = reinterpret_cast<const R2 *>(a.acol[(i64)toy * " << NA << " + " << ac
+                   << "]);\n";
         if(!values) {
             os << "    R av = R(0);\n";
             for(int s = 0; s < NGp - 1; ++s)
@@ -1627,6 +1946,8 @@ struct Gen {
             os << "      const int2 kv" << ci << " = *reinterpret_cast<const int2 *>(kc" << ci << " + i0);\n"
                << "      const int ka" << ci << "[2] = {kv" << ci << ".x, kv" << ci << ".y};\n";
         for(int ac = 0; ac < NA; ++ac) {
+            if(!aused[ac])
+                continue;
             if(mixed)
                 os << "      const float4 av" << ac << " = *reinterpret_cast<const float4 *>(acp" << ac << " + i0);\n"
                    << "      const R2 aa" << ac << "[2] = {make_float2(av" << ac << ".x, av" << ac
@@ -1658,7 +1979,8 @@ struct Gen {
             if(xused[o])
                 os << "        const R ex" << o << " = xa" << o << "[j];\n";
         for(int ac = 0; ac < NA; ++ac)
-            os << "        const R2 am" << ac << " = aa" << ac << "[j];\n";
+            if(aused[ac])
+                os << "        const R2 am" << ac << " = aa" << ac << "[j];\n";
         for(int ci = 0; ci < NC; ++ci) {
             const ConvInfo &cv = T.convs[ci];
             int cp             = cps[ci];
@@ -1760,10 +2082,17 @@ KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, int chunk)
     else
         g.os << "typedef double R;\ntypedef double2 R2;\n#define GF_EXP(x) exp(x)\n#define GF_LOG(x) log(x)\n";
     g.os << kPrelude;
+    if(t.n_amp_nodes() > 0)
+        g.os << kPreludeDual;
     if(!t.amp3s.empty())
-        g.os << kPreludeAmp;
+        g.os << kPreludeAmp << kPreludeAmp3T;
     if(!t.amp4s.empty())
-        g.os << kPreludeAmp4;
+        g.os << kPreludeAmp4 << kPreludeAmp4T
+             << "__device__ __forceinline__ double2 gf_lineshape(bool sbw, double Mpair, double m1, double m2, double mass,\n"
+                "    double width, int orbital, int FF, double radius) {\n"
+                "  double re, im;\n"
+                "  gf_lineshape_t<double>(sbw, Mpair, m1, m2, mass, width, orbital, FF, radius, re, im);\n"
+                "  return make_double2(re, im);\n}\n";
     if(mixed)
         g.os << kPreludeF32;
     else

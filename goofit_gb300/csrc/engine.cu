@@ -11,6 +11,7 @@
 #include "rtc.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -151,6 +152,12 @@ void freeLayout(gf_engine *e) {
 }
 
 void freeNormEvents(gf_engine *e) {
+    for(auto &p : e->nscr)
+        if(p)
+            cudaFree(p);
+    e->nscr.clear();
+    e->nscr_bytes.clear();
+    dfree(e->d_nscr);
     for(auto &b : e->norm_buf)
         dfree(b);
     e->norm_buf.clear();
@@ -348,6 +355,8 @@ GfArgs makeArgs(gf_engine *e) {
     a.dirty       = e->d_dirty;
     a.nevt        = (const double *const *)e->d_nevt;
     a.nnorm       = e->d_nnorm;
+    a.nscr        = (void *const *)e->d_nscr;
+    a.gtoy        = 0;
     a.n_chunks    = e->n_chunks;
     a.n_toys      = e->n_toys;
     a.metric      = 1;
@@ -466,7 +475,8 @@ int loadModule(gf_engine *e) {
        (rc = get(e->mod.val_n, "gf_val_n", true)))
         return rc;
     const bool hasAmp = e->tree.n_amp_nodes() > 0;
-    if((rc = get(e->mod.amp, "gf_amp", hasAmp)) || (rc = get(e->mod.gram, "gf_gram", hasAmp)))
+    if((rc = get(e->mod.amp, "gf_amp", hasAmp)) || (rc = get(e->mod.ampn, "gf_ampn", hasAmp)) ||
+       (rc = get(e->mod.gram, "gf_gram", hasAmp)))
         return rc;
     auto smem = [&](cudaKernel_t k, size_t bytes) -> int {
         if(!k || bytes <= 48 * 1024)
@@ -528,8 +538,33 @@ double ampIntegral(const gf_engine *e, int t, int node, const double *P, const g
             sum += ai_ * aj * Iij(i, j);
         }
     }
+    const auto &theta = T.amp_theta(ai);
+    const std::vector<double> &H = e->toys[t].amp_H.size() > (size_t)ai ? e->toys[t].amp_H[ai] : I;
     for(size_t k = 0; k < an.dN.size() && k < 64; ++k) {
         const int p = T.gparam[an.dN[k].first];
+        // a resonance / line-shape parameter: dQ = 2 Re sum_{a dep} sum_b c_a conj(c_b) H_ab
+        int row = 0, th = -1;
+        for(size_t q = 0; q < theta.size(); ++q) {
+            if(theta[q].param == p) {
+                th = (int)q;
+                break;
+            }
+            row += (int)theta[q].amps.size();
+        }
+        if(th >= 0) {
+            C d(0, 0);
+            for(size_t j = 0; j < theta[th].amps.size(); ++j) {
+                const int a = theta[th].amps[j];
+                C ca(P[nd.params[2 * a]], P[nd.params[2 * a + 1]]);
+                for(int b = 0; b < n; ++b) {
+                    C cb(P[nd.params[2 * b]], P[nd.params[2 * b + 1]]);
+                    const size_t h = 2 * ((size_t)(row + (int)j) * n + b);
+                    d += ca * std::conj(cb) * C(H[h], H[h + 1]);
+                }
+            }
+            dQ[k] = 2 * d.real();
+            continue;
+        }
         std::vector<C> dc(n);
         for(int i = 0; i < n; ++i)
             dc[i] = C(nd.params[2 * i] == p ? 1.0 : 0.0, nd.params[2 * i + 1] == p ? 1.0 : 0.0);
@@ -633,6 +668,57 @@ void fillRecords(gf_engine *e) {
         fillRecordsT<double>(e);
 }
 
+// Number of normalisation points of amplitude node k: in-Dalitz bins (Amp3Body) or phase-space events.
+int64_t ampPoints(const gf_engine *e, int k) {
+    const gf::Tree &T = e->tree;
+    if(k < (int)T.amp3s.size())
+        return (int64_t)T.amp3s[k].grid.size();
+    const int k4 = k - (int)T.amp3s.size();
+    return k4 < (int)e->norm_n.size() ? e->norm_n[k4] : 0;
+}
+
+// Scratch columns of the normalisation pass: per amplitude node, (values + derivatives) R2 columns and an R
+// efficiency column over its points.
+int ensureScratch(gf_engine *e) {
+    const gf::Tree &T = e->tree;
+    const int NK      = T.n_amp_nodes();
+    const size_t rs   = rsize(e);
+    if((int)e->nscr.size() != NK) {
+        for(auto &p : e->nscr)
+            if(p)
+                cudaFree(p);
+        e->nscr.assign(NK, nullptr);
+        e->nscr_bytes.assign(NK, 0);
+        dfree(e->d_nscr);
+        if(int rc = dalloc(e, e->d_nscr, std::max(1, NK)))
+            return rc;
+    }
+    bool changed = false;
+    for(int k = 0; k < NK; ++k) {
+        int nd = 0;
+        for(auto &th : T.amp_theta(k))
+            nd += (int)th.amps.size();
+        const size_t bytes = (size_t)std::max<int64_t>(1, ampPoints(e, k)) * ((T.amp_count(k) + nd) * 2 * rs + rs) + 256;
+        if(bytes == e->nscr_bytes[k])
+            continue;
+        if(e->nscr[k])
+            cudaFree(e->nscr[k]);
+        e->nscr[k]       = nullptr;
+        e->nscr_bytes[k] = 0;
+        cudaError_t r    = cudaMalloc(&e->nscr[k], bytes);
+        if(r != cudaSuccess)
+            return gf_cuda_check(e, r, "cudaMalloc normalisation scratch");
+        e->nscr_bytes[k] = bytes;
+        changed          = true;
+    }
+    if(changed) {
+        cudaError_t r = cudaMemcpy(e->d_nscr, e->nscr.data(), sizeof(void *) * NK, cudaMemcpyHostToDevice);
+        if(r != cudaSuccess)
+            return gf_cuda_check(e, r, "scratch table");
+    }
+    return GF_OK;
+}
+
 // Rebuilds the resonance amplitude caches and the normalisation integrals of the active toys whose
 // resonance or efficiency parameters changed since the last build (Amp3Body::normalize's redoIntegral
 // logic, src/PDFs/physics/Amp3Body.cu:263-330).  Runs outside the captured evaluation graph; the
@@ -673,6 +759,9 @@ int updateAmpCaches(gf_engine *e) {
     if(!any)
         return GF_OK;
     fillRecords(e); // R copies of the parameters for the efficiency in the integral kernel
+    int rc = ensureScratch(e);
+    if(rc)
+        return rc;
     GfArgs a      = makeArgs(e);
     cudaError_t r = cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
     if(r == cudaSuccess)
@@ -681,49 +770,74 @@ int updateAmpCaches(gf_engine *e) {
         const int64_t bx = std::min<int64_t>((maxpad + 255) / 256, (int64_t)std::max(1, e->sm_count) * 8);
         r = launch(e->mod.amp, dim3((unsigned)bx, NT, (unsigned)NAN_), dim3(256), 0, e->stream, a);
     }
-    if(r == cudaSuccess)
-        r = launch(e->mod.gram, dim3(e->gram_blocks, NT, NTILE), dim3(256), 0, e->stream, a);
-    const size_t gbytes = sizeof(double) * (size_t)NT * NTILE * e->gram_blocks * PM2;
-    if(r == cudaSuccess)
-        r = cudaMemcpyAsync(e->h_gram, e->d_gram, gbytes, cudaMemcpyDeviceToHost, e->stream);
-    if(r == cudaSuccess)
-        r = cudaStreamSynchronize(e->stream);
-    if(r != cudaSuccess)
-        return gf_cuda_check(e, r, "Dalitz amplitude caches");
-    for(int t = 0; t < NT; ++t) {
+    int64_t maxpts = 1;
+    for(int k = 0; k < NAN_; ++k)
+        maxpts = std::max<int64_t>(maxpts, ampPoints(e, k));
+    const int64_t bn    = std::min<int64_t>((maxpts + 255) / 256, (int64_t)std::max(1, e->sm_count) * 8);
+    const size_t gbytes = sizeof(double) * (size_t)NTILE * e->gram_blocks * PM2;
+    for(int t = 0; t < NT && r == cudaSuccess; ++t) {
         if(!e->h_dirty[t])
             continue;
+        // the normalisation points of this toy: amplitudes (and derivatives), then their reduction
+        a.gtoy = t;
+        r      = launch(e->mod.ampn, dim3((unsigned)bn, 1, (unsigned)NAN_), dim3(256), 0, e->stream, a);
+        if(r == cudaSuccess)
+            r = launch(e->mod.gram, dim3(e->gram_blocks, 1, NTILE), dim3(256), 0, e->stream, a);
+        if(r == cudaSuccess)
+            r = cudaMemcpyAsync(e->h_gram, e->d_gram, gbytes, cudaMemcpyDeviceToHost, e->stream);
+        if(r == cudaSuccess)
+            r = cudaStreamSynchronize(e->stream);
+        if(r != cudaSuccess)
+            break;
         GfToy &ty = e->toys[t];
         ty.amp_I.assign(NAN_, {});
-        for(int ai = 0; ai < NAN_; ++ai) {
-            const int n = T.amp_count(ai);
-            std::vector<double> I(2 * (size_t)n * n, 0.0);
+        ty.amp_H.assign(NAN_, {});
+        for(int k = 0; k < NAN_; ++k) {
+            const int n = T.amp_count(k);
+            int nd      = 0;
+            for(auto &th : T.amp_theta(k))
+                nd += (int)th.amps.size();
+            std::vector<double> I(2 * (size_t)n * n, 0.0), H(2 * (size_t)std::max(1, nd) * n, 0.0);
+            // entry q of the node: pairs i <= j, then derivative rows d x n (the generator's order)
+            std::vector<std::array<int, 3>> ent;
+            for(int i = 0; i < n; ++i)
+                for(int j = i; j < n; ++j)
+                    ent.push_back({0, i, j});
+            for(int d = 0; d < nd; ++d)
+                for(int b = 0; b < n; ++b)
+                    ent.push_back({1, d, b});
             for(int z = 0; z < NTILE; ++z) {
                 const auto &tile = e->plan.gram_tiles[z];
-                if(tile.amp != ai)
+                if(tile.amp != k)
                     continue;
-                for(int i = 0, q = 0; i < n; ++i)
-                    for(int j = i; j < n; ++j, ++q) {
-                        if(q < tile.p0 || q >= tile.p1)
-                            continue;
-                        const int l = q - tile.p0;
-                        double re = 0, im = 0;
-                        for(int b = 0; b < e->gram_blocks; ++b) {
-                            const double *g = e->h_gram + (((size_t)t * NTILE + z) * e->gram_blocks + b) * PM2;
-                            re += g[2 * l];
-                            im += g[2 * l + 1];
-                        }
+                for(int q = tile.p0; q < tile.p1; ++q) {
+                    const int l = q - tile.p0;
+                    double re = 0, im = 0;
+                    for(int b = 0; b < e->gram_blocks; ++b) {
+                        const double *g = e->h_gram + ((size_t)z * e->gram_blocks + b) * PM2;
+                        re += g[2 * l];
+                        im += g[2 * l + 1];
+                    }
+                    const int i = ent[q][1], j = ent[q][2];
+                    if(ent[q][0] == 0) {
                         I[2 * (i * n + j)]     = re;
                         I[2 * (i * n + j) + 1] = im;
                         I[2 * (j * n + i)]     = re;
                         I[2 * (j * n + i) + 1] = i == j ? im : -im;
+                    } else {
+                        H[2 * (i * n + j)]     = re;
+                        H[2 * (i * n + j) + 1] = im;
                     }
+                }
             }
-            ty.amp_I[ai] = I;
+            ty.amp_I[k] = I;
+            ty.amp_H[k] = H;
         }
         ty.amp_params = snap[t];
         ty.amp_valid  = true;
     }
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "amplitude caches");
     return GF_OK;
 }
 

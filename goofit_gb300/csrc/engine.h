@@ -37,10 +37,11 @@ struct GfArgs {
     const int *dirty;
     const double *const *nevt;
     const long long *nnorm;
+    void *const *nscr;
     int n_chunks;
     int n_toys;
     int metric;
-    int pad;
+    int gtoy;
 };
 
 struct GfToy {
@@ -49,19 +50,20 @@ struct GfToy {
     void *cols[16] = {nullptr};
     int *kcols[8]  = {nullptr};
     void *abase    = nullptr;           // cached resonance amplitudes and FP64 Dalitz columns (one allocation)
-    void *acols[64] = {nullptr};        // R2 per event, one column per resonance of every Amp3Body
+    void *acols[128] = {nullptr};       // R2 per event: amplitude columns, then derivative columns
     double *dcols[16] = {nullptr};      // FP64 event columns of the Dalitz variables
     bool loaded    = false;
     bool amp_valid = false;             // the amplitude cache matches amp_params
     std::vector<double> amp_params;     // parameter values the cache and integrals were built with
-    std::vector<std::vector<double>> amp_I; // per Amp3Body: n x n complex integrals, interleaved
+    std::vector<std::vector<double>> amp_I; // per amplitude node: n x n complex integrals, interleaved
+    std::vector<std::vector<double>> amp_H; // per amplitude node: (derivative rows) x n complex, interleaved
 };
 
 struct GfModule {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t conv_g = nullptr, conv_n = nullptr, grid_g = nullptr, grid_n = nullptr;
     cudaKernel_t evt_g = nullptr, evt_n = nullptr, val_n = nullptr;
-    cudaKernel_t amp = nullptr, gram = nullptr;
+    cudaKernel_t amp = nullptr, ampn = nullptr, gram = nullptr;
 };
 
 struct gf_engine {
@@ -116,6 +118,10 @@ struct gf_engine {
     std::vector<int64_t> norm_n;
     double **d_nevt = nullptr;
     long long *d_nnorm = nullptr;
+    // normalisation-point columns per amplitude node (values, derivatives, efficiency) of one toy at a time
+    std::vector<void *> nscr;
+    std::vector<size_t> nscr_bytes;
+    void **d_nscr = nullptr;
     void *d_Nq = nullptr;   // [toy][nq] R numeric normalisation factors
     int *d_qflag = nullptr; // [toy]
     // pinned host mirrors; h_P is one block: [toy][n_params] FP64, then [toy][npr] R records

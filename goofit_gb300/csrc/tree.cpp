@@ -7,6 +7,7 @@
 #include "tree.h"
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <set>
 #include <sstream>
@@ -283,30 +284,19 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
             used.erase(std::unique(used.begin(), used.end()), used.end());
             v = used;
         }
-        if(n.op == GF_OP_AMP3BODY) {
-            // value gradient: coefficients (and an efficiency's free parameters); resonance parameters
-            // enter through the cached amplitudes, whose derivatives the engine does not provide
+        if(n.op == GF_OP_AMP3BODY || n.op == GF_OP_AMP4BODY) {
+            // value gradient: the coefficients and, through derivative columns of the cached amplitudes, the
+            // resonance / line-shape parameters; the efficiency's parameters have no analytic derivative
             v = own;
             for(size_t r = 0; r + 1 < n.children.size(); ++r)
-                if(!dep_val[n.children[r]].empty())
-                    return "Amp3Body: analytic gradients with respect to resonance parameters are not provided; "
-                           "fix them or leave them out of the gradient mask";
-            int eff = n.children.back();
-            if(!dep_val[eff].empty())
-                return "Amp3Body: analytic gradients with respect to efficiency parameters are not provided";
-        }
-        if(n.op == GF_OP_AMP4BODY) {
-            v = own;
-            for(size_t a = 0; a + 1 < n.children.size(); ++a)
-                if(!dep_val[n.children[a]].empty())
-                    return "Amp4Body: analytic gradients with respect to line-shape parameters are not provided; "
-                           "fix them or leave them out of the gradient mask";
+                v = merge(v, dep_val[n.children[r]]);
             if(!dep_val[n.children.back()].empty())
-                return "Amp4Body: analytic gradients with respect to efficiency parameters are not provided";
+                return std::string(n.op == GF_OP_AMP3BODY ? "Amp3Body" : "Amp4Body") +
+                       ": analytic gradients with respect to efficiency parameters are not provided";
         }
         dep_val[i] = v;
         if(nk[i] == NK_AMP3 || nk[i] == NK_AMP4) {
-            dep_norm[i] = own;
+            dep_norm[i] = v;
         } else if(nk[i] == NK_EXP) {
             int s = gslot[n.params[0]];
             if(s >= 0)
@@ -508,8 +498,51 @@ std::string Tree::build(const gf_node *in, int n_nodes, const gf_observable *ob,
         amp4_of[i] = (int)amp4s.size();
         amp4s.push_back(a);
     }
-    if(n_amp_cols > 64)
-        return "at most 64 amplitude columns (resonances and amplitudes) per tree";
+    // derivative columns for the floated resonance / line-shape parameters
+    auto thetas = [&](int node, int nAmp, std::function<bool(int, int)> depends) {
+        std::vector<AmpTheta> out;
+        std::vector<int> own;
+        for(int p : nodes[node].params)
+            if(gslot[p] >= 0)
+                own.push_back(gslot[p]);
+        for(int sl : dep_val[node]) {
+            if(std::find(own.begin(), own.end(), sl) != own.end())
+                continue;
+            AmpTheta t;
+            t.slot  = sl;
+            t.param = gparam[sl];
+            for(int a = 0; a < nAmp; ++a)
+                if(depends(a, t.param))
+                    t.amps.push_back(a);
+            if(!t.amps.empty())
+                out.push_back(t);
+        }
+        return out;
+    };
+    auto hasParam = [&](int node, int p) {
+        return std::find(nodes[node].params.begin(), nodes[node].params.end(), p) != nodes[node].params.end();
+    };
+    for(auto &A : amp3s)
+        A.theta = thetas(A.node, A.nRes, [&](int r, int p) { return hasParam(A.res[r], p); });
+    for(auto &A : amp4s)
+        A.theta = thetas(A.node, A.nAmp, [&](int a, int p) {
+            for(int u : A.amps[a].ls)
+                if(hasParam(A.ls[u], p))
+                    return true;
+            return false;
+        });
+    for(auto &A : amp3s)
+        for(auto &t : A.theta) {
+            t.col0 = n_amp_cols;
+            n_amp_cols += (int)t.amps.size();
+        }
+    for(auto &A : amp4s)
+        for(auto &t : A.theta) {
+            t.col0 = n_amp_cols;
+            n_amp_cols += (int)t.amps.size();
+        }
+    if(n_amp_cols > 128)
+        return "at most 128 amplitude and derivative columns per tree";
 
     // numeric grids
     num_of.assign(n_nodes, -1);

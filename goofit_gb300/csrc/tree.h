@@ -43,6 +43,15 @@ struct ConvInfo {
     std::vector<int> dep;           // gradient slots the table depends on
 };
 
+// A floated resonance / line-shape parameter of an amplitude node with an analytic gradient: the amplitudes
+// that depend on it get one derivative column each (dA_a / dparam per event), and the normalisation one
+// matrix H_ab = sum over normalisation points of dA_a/dparam conj(A_b) (times the efficiency for Amp3Body).
+struct AmpTheta {
+    int slot = -1, param = -1;
+    std::vector<int> amps; // dependent amplitudes (indices within the node)
+    int col0 = 0;          // first derivative column
+};
+
 // One Amp3Body node (src/PDFs/physics/Amp3Body.cu:127-196): resonances, efficiency, decay constants and
 // the normalisation grid (m12^2 x m13^2 bin centres; the m13 bin count is read from the m12 slot as
 // src/PDFs/physics/detail/SpecialResonanceIntegrator.cu:72 does).
@@ -55,6 +64,7 @@ struct Amp3Info {
     double area = 0;          // bin size of m12 times bin size of m13
     std::vector<int> cache_params; // parameters the cached amplitudes and integrals depend on
     std::vector<uint32_t> grid;    // in-Dalitz normalisation bins, b12 | b13 << 16 (FP64 inDalitz)
+    std::vector<AmpTheta> theta;
 };
 
 // One Amp4Body node (src/PDFs/physics/Amp4Body.cu:94-292): amplitudes built from line shapes and spin
@@ -71,6 +81,7 @@ struct Amp4Info {
     std::vector<Amp> amps;
     int col0 = 0;                  // first amplitude column of this node
     std::vector<int> cache_params; // line-shape (and efficiency) parameters
+    std::vector<AmpTheta> theta;
 };
 
 // inDalitz (src/PDFs/physics/DalitzPlotHelpers.cu:14-59), FP64 without contraction.
@@ -117,6 +128,9 @@ struct Tree {
     int amp_col0(int k) const { return k < (int)amp3s.size() ? amp3s[k].col0 : amp4s[k - amp3s.size()].col0; }
     const std::vector<int> &amp_cache_params(int k) const {
         return k < (int)amp3s.size() ? amp3s[k].cache_params : amp4s[k - amp3s.size()].cache_params;
+    }
+    const std::vector<AmpTheta> &amp_theta(int k) const {
+        return k < (int)amp3s.size() ? amp3s[k].theta : amp4s[k - amp3s.size()].theta;
     }
     int n_amp_cols = 0;       // complex amplitude columns per toy
     bool extended_root = false;

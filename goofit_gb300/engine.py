@@ -8,6 +8,7 @@ path.
 from __future__ import annotations
 
 import ctypes as C
+import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -223,16 +224,19 @@ class Engine:
         return self._L.gf_launches_per_eval(self._h, 1 if grad else 0)
 
     # ---- fits ----
-    def default_fnoise(self) -> float:
-        """Relative rounding noise of the NLL in the mixed path: FP32 per-event terms summed into
-        compensated pairs leave random rounding of about 1e-7 / sqrt(events) relative; 2e-9 covers the
-        smallest toys of the batched study with a margin."""
-        return 2e-9 if self.precision == "mixed" else 0.0
+    def default_fnoise(self, n_events: int | None = None) -> float:
+        """Relative rounding noise of the NLL in the mixed path.  FP32 per-event terms summed into
+        compensated pairs leave a random rounding of about 1e-7 * sqrt(n) absolute, 1e-7 / sqrt(n)
+        relative; the line search treats changes below 15 times that as ties (clamped to [1e-9, 2e-8])."""
+        if self.precision != "mixed":
+            return 0.0
+        n = n_events if n_events else max(self._n_events.values(), default=1)
+        return float(min(2e-8, max(1e-9, 1.5e-6 / math.sqrt(max(1, n)))))
 
     def fit(self, x0, err, lo, hi, limited, fixed, *, up=0.5, tolerance=0.1, strategy=1, maxfcn=0,
             use_grad=True, toy: int = 0, fnoise_rel=None) -> FitResult:
         n = self.n_params
-        fn = self.default_fnoise() if fnoise_rel is None else fnoise_rel
+        fn = self.default_fnoise(self._n_events.get(toy)) if fnoise_rel is None else fnoise_rel
         o, keep = _fit_options(n, err, lo, hi, limited, fixed, up, tolerance, strategy, maxfcn, use_grad, fn)
         xa, xp = A.f64(x0)
         x = np.zeros(n)
@@ -246,7 +250,8 @@ class Engine:
                   use_grad=True, fnoise_rel=None) -> list[FitResult]:
         n = self.n_params
         T = self.n_toys
-        fn = self.default_fnoise() if fnoise_rel is None else fnoise_rel
+        # one tolerance for the batch: that of the smallest toy
+        fn = self.default_fnoise(min(self._n_events.values(), default=1)) if fnoise_rel is None else fnoise_rel
         o, keep = _fit_options(n, err, lo, hi, limited, fixed, up, tolerance, strategy, maxfcn, use_grad, fn)
         X0 = np.ascontiguousarray(X0, dtype=np.float64).reshape(T, n)
         X = np.zeros((T, n))

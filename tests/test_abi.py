@@ -94,8 +94,8 @@ def test_engine_without_device_reports_no_device():
 
 
 def test_amp3body_tree_checks():
-    """Amp3Body trees: the resonance parameters have no analytic derivative, and the normalisation bins
-    inside the kinematic boundary are found by the FP64 boundary test."""
+    """Amp3Body trees: the efficiency's parameters have no analytic derivative (the resonances' do), and the
+    normalisation bins inside the kinematic boundary are found by the FP64 boundary test."""
     from oracle import oracle as O
     pdf = W.c3_model(60)[0]
     nodes, olist, params, mask = _tree(pdf)
@@ -105,13 +105,19 @@ def test_amp3body_tree_checks():
     n = C.c_int64()
     full = [0 if v.fixed else 1 for v in params]
     for v in params:
-        if v.name == "rho770_mass":
+        if v.name in ("rho770_mass", "constantOne"):
             v.fixed = False
     full = [0 if v.fixed else 1 for v in params]
     marr, mp = A.i32(full)
     rc = L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, A.GF_MIXED, None, 0, C.byref(n))
-    assert rc == A.GF_ERR_BAD_TREE and b"resonance parameters" in L.gf_last_error(None)
-    # the generated integral kernel loops over exactly the in-Dalitz bins of a 60 x 60 grid
+    assert rc == A.GF_ERR_BAD_TREE and b"efficiency" in L.gf_last_error(None)
+    full = [0 if (v.fixed or v.name == "constantOne") else 1 for v in params]
+    marr, mp = A.i32(full)
+    assert L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, A.GF_MIXED, None, 0, C.byref(n)) == 0
+    for v in params:
+        if v.name in ("rho770_mass", "constantOne"):
+            v.fixed = True
+    # the generated normalisation pass loops over exactly the in-Dalitz bins of a 60 x 60 grid
     marr, mp = A.i32(mask)
     rc = L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, A.GF_FP64, None, 0, C.byref(n))
     buf = C.create_string_buffer(n.value + 1)
@@ -120,4 +126,4 @@ def test_amp3body_tree_checks():
     inside = sum(O.in_dalitz(3.0 / 60 * (a + 0.5), 3.0 / 60 * (b + 0.5), W.C3_M, W.C3_MK, W.C3_MPI, W.C3_MPI0)
                  for a in range(60) for b in range(60))
     assert 0 < inside < 3600
-    assert f"p < {inside}; p += gridDim.x * 256" in src
+    assert f"const i64 npts = {inside}LL;" in src

@@ -158,3 +158,23 @@ def test_mixed_fit_matches_fp64_fit(c3_events):
         vm, em = out["mixed"][k]
         assert abs(vm - v64) < 0.01 * e64, (k, vm, v64, e64)
         assert em == pytest.approx(e64, rel=0.01), k
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_resonance_gradient_matches_central_differences(c3_events, prec):
+    """dNLL/d(resonance mass, width) through the derivative columns, against central finite differences of
+    the FP64 oracle with h = 1e-5."""
+    pdf, _, _ = W.c3_model(300)
+    for v in pdf.getParameters():
+        if v.name in ("rho770_mass", "rho770_width", "kst892_mass", "f2_1270_width"):
+            v.fixed = False
+    eng, nodes, olist, params, mask, pv = engine(pdf, c3_events, prec)
+    free = [i for i, m in enumerate(mask) if m]
+    assert len(free) == 18
+    p = pv.copy()
+    ref = O.nll(nodes, olist, p, c3_events)
+    got, g = eng.nll_grad(p)
+    assert got == pytest.approx(ref, rel=NLL_RTOL[prec])
+    fd = O.fd_grad(nodes, olist, p, c3_events, free, h=1e-5)
+    n = c3_events.shape[1]
+    np.testing.assert_allclose(g, fd, rtol=2e-4 if prec == "mixed" else 1e-6, atol=2e-3 * math.sqrt(n))

@@ -67,14 +67,26 @@ def test_amp4body_kernels_compile_for_sm103a(prec):
         L.gf_last_error(None)
 
 
-def test_amp4body_lineshape_parameters_have_no_analytic_gradient():
+def test_amp4body_lineshape_parameters_get_derivative_columns():
+    """Floated line-shape masses and widths have analytic derivatives (dual numbers through the line shapes);
+    the efficiency's parameters do not."""
     pdf, _, _, ls = W.c5_model(1000, float_lineshapes=True)
-    nodes, olist, params, _ = _tree(pdf)
-    full = [0 if v.fixed else 1 for v in params]
+    nodes, olist, params, mask = _tree(pdf)
+    assert sum(mask) == 20
     L = A.lib()
     nl = A.NodeList(nodes)
     obs = A.observables_array(olist)
-    marr, mp = A.i32(full)
+    marr, mp = A.i32(mask)
     n = C.c_int64()
+    assert L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, A.GF_MIXED, None, 0, C.byref(n)) == 0
+    buf = C.create_string_buffer(n.value + 1)
+    L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, A.GF_MIXED, buf, n.value + 1, C.byref(n))
+    src = buf.value.decode()
+    assert "gf_lineshape_t<GfDual>" in src and "gf_ampn" in src
+    full = [0 if v.fixed else 1 for v in params]
+    for i, v in enumerate(params):
+        if v.name == "constantOne":
+            full[i] = 1
+    marr, mp = A.i32(full)
     rc = L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, A.GF_MIXED, None, 0, C.byref(n))
-    assert rc == A.GF_ERR_BAD_TREE and b"line-shape" in L.gf_last_error(None)
+    assert rc == A.GF_ERR_BAD_TREE and b"efficiency" in L.gf_last_error(None)

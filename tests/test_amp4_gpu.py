@@ -132,3 +132,23 @@ def test_mixed_fit_matches_fp64_fit(c5):
         vm, em = out["mixed"][k]
         assert abs(vm - v64) < 0.01 * e64, (k, vm, v64, e64)
         assert em == pytest.approx(e64, rel=0.01), k
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_lineshape_gradient_matches_central_differences(prec):
+    """dNLL/d(coefficients, masses, widths) against central finite differences of the FP64 oracle with
+    h = 1e-5 (relative to max(1, |p|))."""
+    pdf = W.c5_model(N_NORM, float_lineshapes=True)[0]
+    cols = W.c5_generate(W.c5_model(N_NORM)[0], 10_000, seed=52, batch=200_000)
+    eng, nodes, olist, params, mask, pv = engine(pdf, cols, prec)
+    free = [i for i, m in enumerate(mask) if m]
+    assert len(free) == 20
+    p = pv.copy()
+    p[free] *= 1 + 0.02 * np.random.default_rng(3).standard_normal(len(free))
+    got, g = eng.nll_grad(p)
+    ref = O.nll(nodes, olist, p, cols)
+    assert got == pytest.approx(ref, rel=NLL_RTOL[prec])
+    fd = O.fd_grad(nodes, olist, p, cols, free, h=1e-5)
+    n = cols.shape[1]
+    # the finite differences carry ~1e-16 * NLL / h of rounding; the gradient scale is n
+    np.testing.assert_allclose(g, fd, rtol=2e-4 if prec == "mixed" else 1e-6, atol=2e-3 * math.sqrt(n))
