@@ -2060,7 +2060,7 @@ struct Gen {
         os << "        double *o = a.out + (i64)toy * " << NGs + 1 << ";\n";
         os << "        const double v = acc_value(t);\n";
         os << "        o[tid == 0 ? 0 : 1 + tid] = v;\n";
-        os << "        if(tid == 0) { int st = a.qflag[toy]; if(v == 0.0) st |= 4; o[1] = (double)st; a.counter[toy] = 0u; }\n";
+        os << "        if(tid == 0) { int st = a.qflag[toy]; if(v == 0.0) st |= 4; o[1] = (double)st; a.counter[toy] = 0u; a.qflag[toy] = 0; }\n";
         os << "      }\n";
         os << "    }\n";
         os << "    __syncthreads();\n";

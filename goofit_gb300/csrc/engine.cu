@@ -121,7 +121,7 @@ void dropGraphs(gf_engine *e) {
 void freeLayout(gf_engine *e) {
     dropGraphs(e);
     dfree(e->d_P);
-    dfree(e->d_active);
+    e->d_active = nullptr; // inside d_P
     dfree(e->d_cols);
     dfree(e->d_kcols);
     dfree(e->d_ctab);
@@ -146,7 +146,7 @@ void freeLayout(gf_engine *e) {
     hfree(e->h_gram);
     hfree(e->h_dirty);
     hfree(e->h_P);
-    hfree(e->h_active);
+    e->h_active = nullptr; // inside h_P
     hfree(e->h_out);
     e->layout_ready = false;
 }
@@ -227,8 +227,11 @@ int buildLayout(gf_engine *e) {
             rc = r;
     };
     const gf::NormLayout &nl = e->plan.nl;
+    // one host-to-device block per evaluation: [toy][param] FP64, [toy][record] R, then the active flags
     e->pblock_bytes = sizeof(double) * (size_t)NT * std::max(1, T.n_params) + rsize(e) * (size_t)NT * std::max(1, nl.npr);
     e->pblock_bytes = (e->pblock_bytes + 15) / 16 * 16;
+    e->active_off   = e->pblock_bytes;
+    e->pblock_bytes = (e->pblock_bytes + sizeof(int) * (size_t)NT + 15) / 16 * 16;
     chk(dalloc(e, e->d_P, e->pblock_bytes / sizeof(double)));
     {
         void *p = nullptr;
@@ -237,7 +240,7 @@ int buildLayout(gf_engine *e) {
         e->d_Nq = p;
     }
     chk(dalloc(e, e->d_qflag, NT));
-    chk(dalloc(e, e->d_active, NT));
+    e->d_active = reinterpret_cast<int *>(reinterpret_cast<char *>(e->d_P) + e->active_off);
     chk(dalloc(e, e->d_cols, (size_t)NT * NO));
     chk(dalloc(e, e->d_kcols, (size_t)NT * std::max(1, NC)));
     int64_t ctab = std::max(e->plan.ctab_per_toy_grad, e->plan.ctab_per_toy_nograd);
@@ -296,10 +299,10 @@ int buildLayout(gf_engine *e) {
             cudaMemcpy(e->d_dgrid, g.data(), sizeof(unsigned) * g.size(), cudaMemcpyHostToDevice);
     }
     if(cudaMallocHost((void **)&e->h_P, e->pblock_bytes) != cudaSuccess ||
-       cudaMallocHost((void **)&e->h_active, sizeof(int) * NT) != cudaSuccess ||
        cudaMallocHost((void **)&e->h_out, sizeof(double) * (size_t)NT * (NGp + 1)) != cudaSuccess)
         return gf_fail(e, GF_ERR_OOM, "cudaMallocHost");
     std::memset(e->h_P, 0, e->pblock_bytes);
+    e->h_active = reinterpret_cast<int *>(reinterpret_cast<char *>(e->h_P) + e->active_off);
     e->host_flag.assign(NT, 0);
     for(int t = 0; t < NT; ++t)
         e->h_active[t] = 1;
@@ -413,13 +416,10 @@ cudaError_t enqueueEval(gf_engine *e, bool grad) {
     const gf::Tree &T = e->tree;
     const int NT = e->n_toys, NGp = 1 + T.NG;
     GfArgs a         = makeArgs(e);
-    cudaError_t r    = cudaEventRecordWithFlags(e->ev[0], e->stream, cudaEventRecordExternal);
-    if(r == cudaSuccess)
-        r = cudaMemsetAsync(e->d_qflag, 0, sizeof(int) * NT, e->stream);
+    // qflag is zero between evaluations: the event kernel's finisher clears it after reading it
+    cudaError_t r = cudaEventRecordWithFlags(e->ev[0], e->stream, cudaEventRecordExternal);
     if(r == cudaSuccess)
         r = cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
-    if(r == cudaSuccess)
-        r = cudaMemcpyAsync(e->d_active, e->h_active, sizeof(int) * NT, cudaMemcpyHostToDevice, e->stream);
     bool kernelLast = false;
     if(r == cudaSuccess)
         r = enqueuePrep(e, grad, a, &kernelLast);
@@ -1297,13 +1297,13 @@ int gf_normalize(gf_engine *e, int toy, double *integral, double *norm) {
     fillRecords(e);
     GfArgs a = makeArgs(e);
     cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
-    cudaMemcpyAsync(e->d_active, e->h_active, sizeof(int) * NT, cudaMemcpyHostToDevice, e->stream);
     cudaError_t r = enqueuePrep(e, false, a);
     if(r != cudaSuccess)
         return gf_cuda_check(e, r, "normalisation kernels");
     std::vector<double> gsum((size_t)NT * std::max(1, NQ));
     if(NQ > 0)
         cudaMemcpyAsync(gsum.data(), e->d_gsum, sizeof(double) * (size_t)NT * NQ, cudaMemcpyDeviceToHost, e->stream);
+    cudaMemsetAsync(e->d_qflag, 0, sizeof(int) * NT, e->stream); // zero between evaluations
     r = cudaStreamSynchronize(e->stream);
     if(r != cudaSuccess)
         return gf_cuda_check(e, r, "normalisation");
@@ -1417,12 +1417,13 @@ int gf_eval_events(gf_engine *e, int toy, int node, int metric, double *out, int
     GfArgs a  = makeArgs(e);
     a.metric  = metric;
     cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
-    cudaMemcpyAsync(e->d_active, e->h_active, sizeof(int) * NT, cudaMemcpyHostToDevice, e->stream);
     cudaError_t r = enqueuePrep(e, false, a);
     if(r == cudaSuccess)
         r = launch(e->mod.val_n, dim3(evtGrid(e)), dim3(e->block), e->plan.evt_smem_nograd, e->stream, a);
     if(r == cudaSuccess && ty.n > 0)
         r = cudaMemcpyAsync(out, e->d_vals, sizeof(double) * ty.n, cudaMemcpyDeviceToHost, e->stream);
+    if(r == cudaSuccess)
+        r = cudaMemsetAsync(e->d_qflag, 0, sizeof(int) * NT, e->stream); // zero between evaluations
     if(r == cudaSuccess)
         r = cudaStreamSynchronize(e->stream);
     return gf_cuda_check(e, r, "per-event evaluation");
@@ -1458,8 +1459,6 @@ int gf_time_kernels(gf_engine *e, int toy, int with_grad, double *ms_conv, doubl
     cudaError_t r = cudaMemsetAsync(e->d_qflag, 0, sizeof(int) * e->n_toys, e->stream);
     if(r == cudaSuccess)
         r = cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
-    if(r == cudaSuccess)
-        r = cudaMemcpyAsync(e->d_active, e->h_active, sizeof(int) * e->n_toys, cudaMemcpyHostToDevice, e->stream);
     cudaEvent_t t0 = e->ev[0], t1 = e->ev[1], t2 = e->ev[2], t3 = e->ev[3];
     if(r == cudaSuccess)
         r = cudaEventRecord(t0, e->stream);

@@ -127,6 +127,7 @@ struct gf_engine {
     // pinned host mirrors; h_P is one block: [toy][n_params] FP64, then [toy][npr] R records
     double *h_P = nullptr;
     size_t pblock_bytes = 0;
+    size_t active_off   = 0; // byte offset of the active flags inside the parameter block
     std::vector<int> host_flag; // per toy: status bits from host-computed analytic factors
     int *h_active = nullptr;
     double *h_out = nullptr;
