@@ -7,6 +7,7 @@ over libgfengine.so: per-tree generated sm_103a kernels behind a C ABI
 (include/gfengine.h).
 """
 from .api import (FF, PAIR_12, PAIR_13, PAIR_23, RBW, SF_4Body, AddPdf, Amp3Body, Amp4Body, Amplitude, AmpComponent,
+                  BinnedChisqFit, BinnedDataSet, BinnedErrorFit, BinnedNllFit, FitControl, UnbinnedNllFit,
                   CombinePdf, ConvolutionPdf, DataSet, DecayInfo4, DP4Pair, Lineshape, Lineshapes, SpinFactor,
                   DaughterPair, DecayInfo3, EvalFunc, EventNumber, ExpPdf, FitManager, FitManagerMinuit2,
                   GaussianPdf, GeneralError, GooPdf, MultiPolynomialPdf, NonRes, Observable, OutOfRange, PdfBase,
@@ -20,5 +21,6 @@ __all__ = [
     "PolynomialPdf", "ProdPdf", "UnbinnedDataSet", "Variable", "Engine", "FitResult", "Minimizer",
     "get_precision", "set_precision", "Amp3Body", "DecayInfo3", "DaughterPair", "PAIR_12", "PAIR_13", "PAIR_23",
     "ResonancePdf", "Resonances", "RBW", "NonRes", "MultiPolynomialPdf", "Amp4Body", "Amplitude", "AmpComponent",
-    "DecayInfo4", "DP4Pair", "FF", "Lineshape", "Lineshapes", "SF_4Body", "SpinFactor",
+    "DecayInfo4", "DP4Pair", "FF", "Lineshape", "Lineshapes", "SF_4Body", "SpinFactor", "BinnedDataSet",
+    "FitControl", "UnbinnedNllFit", "BinnedNllFit", "BinnedErrorFit", "BinnedChisqFit",
 ]

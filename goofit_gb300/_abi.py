@@ -56,6 +56,10 @@ GF_FLAG_SEPARATE_NORM = 2
 GF_METRIC_EVAL = 0
 GF_METRIC_NLL = 1
 GF_METRIC_PROB = 2
+GF_FIT_UNBINNED_NLL = 0
+GF_FIT_BINNED_NLL = 1
+GF_FIT_BINNED_ERROR = 2
+GF_FIT_BINNED_CHISQ = 3
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -139,6 +143,7 @@ SIGNATURES = [
     ("gf_amp3_integrals", C.c_int, [_vp, C.c_int, C.c_int, _f64p, C.c_int]),
     ("gf_amp3_cached_wave", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _f64p, C.c_int64]),
     ("gf_set_norm_events", C.c_int, [_vp, C.c_int, _f64p, C.c_int64]),
+    ("gf_set_fit_metric", C.c_int, [_vp, C.c_int]),
     ("gf_last_timing", C.c_int, [_vp, _f64p, _f64p]),
     ("gf_launches_per_eval", C.c_int, [_vp, C.c_int]),
     ("gf_time_kernels", C.c_int, [_vp, C.c_int, C.c_int, _f64p, _f64p, _f64p]),

@@ -360,6 +360,147 @@ class UnbinnedDataSet(DataSet):
 
 
 # ---------------------------------------------------------------- PDFs
+class BinnedDataSet(DataSet):
+    """include/goofit/BinnedDataSet.h, src/goofit/BinnedDataSet.cpp: counts on the observables' bin grid
+    (global bin = sum local_i * prod_{j<i} nbins_j)."""
+
+    def __init__(self, observables, name: str = ""):
+        super().__init__(observables, name)
+        self.binsizes = [o.getNumBins() for o in self.observables]
+        self.binvalues = np.zeros(int(np.prod(self.binsizes)))
+        self.binerrors: np.ndarray | None = None
+        self.version = 0
+
+    def getNumBins(self) -> int:
+        return len(self.binvalues)
+
+    def _local(self, global_bin: int) -> list[int]:
+        out = []
+        for n in self.binsizes:
+            out.append(global_bin % n)
+            global_bin //= n
+        return out
+
+    def getBinNumber(self) -> int:
+        ret, prior = 0, 1
+        for o, n in zip(self.observables, self.binsizes):
+            b = int(np.floor((o.value - o.lowerlimit) / ((o.upperlimit - o.lowerlimit) / n)))
+            ret += b * prior
+            prior *= n
+        return ret
+
+    def addEvent(self) -> None:
+        self.checkAllVars()
+        self.binvalues[self.getBinNumber()] += 1
+        self.numEventsAdded += 1
+        self.version += 1
+
+    def addWeightedEvent(self, weight: float) -> None:
+        self.checkAllVars()
+        self.binvalues[self.getBinNumber()] += weight
+        self.numEventsAdded += 1
+        self.version += 1
+
+    def fill(self, values: np.ndarray, weights: np.ndarray | None = None) -> None:
+        """Adds many events at once: values (n_obs, n) inside the observables' ranges."""
+        v = np.atleast_2d(np.asarray(values, dtype=np.float64))
+        g = np.zeros(v.shape[1], dtype=np.int64)
+        prior = 1
+        for k, (o, n) in enumerate(zip(self.observables, self.binsizes)):
+            b = np.floor((v[k] - o.lowerlimit) / ((o.upperlimit - o.lowerlimit) / n)).astype(np.int64)
+            g += np.clip(b, 0, n - 1) * prior
+            prior *= n
+        np.add.at(self.binvalues, g, 1.0 if weights is None else np.asarray(weights, dtype=np.float64))
+        self.numEventsAdded += v.shape[1]
+        self.version += 1
+
+    def getBinContent(self, b: int) -> float:
+        return float(self.binvalues[b])
+
+    def setBinContent(self, b: int, value: float) -> None:
+        self.binvalues[b] = value
+        self.version += 1
+
+    def getBinSize(self, ivar: int) -> float:
+        o = self.observables[ivar]
+        return (o.upperlimit - o.lowerlimit) / self.binsizes[ivar]
+
+    def getBinCenter(self, var, b: int) -> float:
+        ivar = var if isinstance(var, int) else self.indexOfVariable(var)
+        ret = self.getBinSize(ivar)
+        ret *= self._local(b)[ivar] + 0.5
+        ret += self.observables[ivar].lowerlimit
+        return ret
+
+    def getBinVolume(self, b: int) -> float:
+        ret = 1.0
+        for i in range(len(self.observables)):
+            ret *= self.getBinSize(i)
+        return ret
+
+    def getBinError(self, b: int) -> float:
+        if self.binerrors is None:
+            return math.sqrt(self.binvalues[b])
+        return float(self.binerrors[b])
+
+    def setBinError(self, b: int, value: float) -> None:
+        # the first explicit error switches every bin to explicit errors, zero where unset (as the reference)
+        if self.binerrors is None:
+            self.binerrors = np.zeros_like(self.binvalues)
+        self.binerrors[b] = value
+        self.version += 1
+
+    def getNumWeightedEvents(self) -> float:
+        return float(self.binvalues.sum())
+
+    def engine_columns(self, obs: list[Observable], errors: bool) -> np.ndarray:
+        """Bin centres of `obs`, then contents, then volumes (or errors): PdfBase::setData's binned layout."""
+        n = self.getNumBins()
+        rows = []
+        idx = np.arange(n)
+        for o in obs:
+            ivar = self.indexOfVariable(o)
+            prior = int(np.prod(self.binsizes[:ivar])) if ivar else 1
+            local = (idx // prior) % self.binsizes[ivar]
+            rows.append(self.getBinSize(ivar) * (local + 0.5) + o.lowerlimit)
+        rows.append(self.binvalues.copy())
+        if errors:
+            rows.append(self.binerrors.copy() if self.binerrors is not None else np.sqrt(self.binvalues))
+        else:
+            rows.append(np.full(n, self.getBinVolume(0)))
+        return np.vstack(rows)
+
+
+# ---------------------------------------------------------------- fit controls
+class FitControl:
+    """include/goofit/FitControl.h: which metric the fit minimises."""
+    metric = A.GF_FIT_UNBINNED_NLL
+    binned = False
+    errors_on_bins = False
+
+    def binnedFit(self) -> bool:
+        return self.binned
+
+    def binErrors(self) -> bool:
+        return self.errors_on_bins
+
+
+class UnbinnedNllFit(FitControl):
+    metric = A.GF_FIT_UNBINNED_NLL
+
+
+class BinnedNllFit(FitControl):
+    metric, binned = A.GF_FIT_BINNED_NLL, True
+
+
+class BinnedErrorFit(FitControl):
+    metric, binned, errors_on_bins = A.GF_FIT_BINNED_ERROR, True, True
+
+
+class BinnedChisqFit(FitControl):
+    metric, binned = A.GF_FIT_BINNED_CHISQ, True
+
+
 def _unique(seq: Iterable) -> list:
     out, seen = [], set()
     for x in seq:
@@ -384,6 +525,7 @@ class PdfBase:
         self.integrationBins = 0
         self.flags = 0
         self.data = None
+        self.fitControl: FitControl = UnbinnedNllFit()
         self._engines: dict = {}
         for r in registered:
             if isinstance(r, Observable):
@@ -447,7 +589,14 @@ class PdfBase:
         return bool(self.flags & A.GF_FLAG_SEPARATE_NORM)
 
     def setData(self, data) -> None:
+        """PdfBase::setData: a BinnedDataSet switches an unbinned fit control to BinnedNllFit
+        (src/PDFs/PdfBase.cu:444-445)."""
         self.data = data
+        if isinstance(data, BinnedDataSet) and not self.fitControl.binnedFit():
+            self.fitControl = BinnedNllFit()
+
+    def setFitControl(self, fc: "FitControl") -> None:
+        self.fitControl = fc
 
     def getData(self):
         return self.data
@@ -492,18 +641,26 @@ class PdfBase:
         nd = self._nondiff_all()
         mask = [0 if (v.fixed or id(v) in nd) else 1 for v in params]
         olist = [(o.lowerlimit, o.upperlimit, o.numbins, 1 if o.is_event_number else 0) for o in obs]
-        key = repr((nodes, olist, mask))
+        metric = self.fitControl.metric if isinstance(data, BinnedDataSet) else A.GF_FIT_UNBINNED_NLL
+        key = repr((nodes, olist, mask, metric))
         ent = self._engines.get(precision)
         if ent is None or ent["key"] != key:
-            eng = ent["engine"] if ent else Engine(precision)
+            eng = ent["engine"] if ent and ent["metric"] == metric else Engine(precision)
+            if metric != A.GF_FIT_UNBINNED_NLL:
+                eng.set_fit_metric(metric)
             eng.set_tree(nodes, olist, len(params), mask)
             for i, p in enumerate(self._flat_order):
                 p._engine_setup(eng, i)
-            ent = dict(engine=eng, key=key, data=None, version=-1)
+            ent = dict(engine=eng, key=key, data=None, version=-1, metric=metric)
             self._engines[precision] = ent
         eng = ent["engine"]
         if data is not None and (ent["data"] is not data or ent["version"] != getattr(data, "version", 0)):
-            cols = np.vstack([data.column(o) for o in obs]) if data.getNumEvents() else np.zeros((len(obs), 0))
+            if isinstance(data, BinnedDataSet):
+                cols = data.engine_columns(obs, self.fitControl.binErrors())
+            elif data.getNumEvents():
+                cols = np.vstack([data.column(o) for o in obs])
+            else:
+                cols = np.zeros((len(obs), 0))
             eng.upload(cols)
             ent["data"], ent["version"] = data, getattr(data, "version", 0)
         return eng, params

@@ -1847,6 +1847,10 @@ struct Gen {
             return "tq" + std::to_string(ci) + "_" + std::to_string(comp / 4) + fld[comp % 4];
         };
         std::vector<int> aused(std::max(1, NA), 0);
+        if(T.fit_metric != GF_FIT_UNBINNED_NLL && !values) {
+            c.x(NO - 2);
+            c.x(NO - 1);
+        }
         c.amp = [&](int ai, int r) {
             aused[T.amp_col0(ai) + r] = 1;
             return "am" + std::to_string(T.amp_col0(ai) + r);
@@ -1918,6 +1922,8 @@ struct Gen {
         }
         emitParamsR(os, T, plan.nl, "    ");
         emitNormReads(os, T, grad, plan.nl, "    ");
+        if(T.fit_metric != GF_FIT_UNBINNED_NLL && !values)
+            os << "    const R Tn = (R)a.toy_nevents[toy]; // c_totalEvents: the number of bins\n";
         for(int o = 0; o < NO; ++o)
             if(xused[o])
                 os << "    const R *col" << o << " = reinterpret_cast<const R *>(a.col[(i64)toy * " << NO << " + " << o
@@ -2008,23 +2014,76 @@ struct Gen {
             os << "          else r = pv > R(0) ? -(double)GF_LOG(pv) : 0.0;\n";
             os << "          a.vals[i0 + j] = r;\n        }\n";
         } else {
-            os << "        if(i0 + j < e0 && pv > R(0)) {\n";
-            os << "          av -= GF_LOG(pv);\n";
-            if(grad && T.NG > 0) {
-                os << "          const R inv = R(1) / pv;\n";
-                for(int s = 0; s < T.NG; ++s) {
-                    std::string e;
-                    auto it = root.g.find(s);
-                    if(it != root.g.end())
-                        e = rootN.empty() ? it->second : it->second + " * " + rootN;
-                    std::string dn = T.nk[0] == NK_ONE ? "" : dnormExpr(c, 0, s);
-                    if(!dn.empty())
-                        e += (e.empty() ? "" : " + ") + root.v + " * " + dn;
-                    if(!e.empty())
-                        os << "          ag" << s << " -= (" << e << ") * inv;\n";
+            // d(P norm)/dp (with the normalisation's derivative) and d(P)/dp for every gradient slot
+            auto dpv = [&](int s) {
+                std::string e;
+                auto it = root.g.find(s);
+                if(it != root.g.end())
+                    e = rootN.empty() ? it->second : it->second + " * " + rootN;
+                std::string dn = T.nk[0] == NK_ONE ? "" : dnormExpr(c, 0, s);
+                if(!dn.empty())
+                    e += (e.empty() ? "" : " + ") + root.v + " * " + dn;
+                return e;
+            };
+            const std::string nc = "ex" + std::to_string(NO - 2), vw = "ex" + std::to_string(NO - 1);
+            switch(T.fit_metric) {
+            case GF_FIT_BINNED_NLL: // calculateBinAvg, src/PDFs/MetricPointer.cu:23-37
+                os << "        const R raw = pv * " << vw << ";\n";
+                os << "        if(i0 + j < e0 && raw > R(0)) {\n";
+                os << "          const R mu = Tn * raw;\n";
+                os << "          av += mu - " << nc << " * GF_LOG(mu);\n";
+                if(grad && T.NG > 0) {
+                    os << "          const R w = Tn * " << vw << " * (R(1) - " << nc << " / mu);\n";
+                    for(int s = 0; s < T.NG; ++s) {
+                        std::string e = dpv(s);
+                        if(!e.empty())
+                            os << "          ag" << s << " += (" << e << ") * w;\n";
+                    }
                 }
+                os << "        }\n";
+                break;
+            case GF_FIT_BINNED_ERROR: // calculateBinWithError, MetricPointer.cu:39-52: P unnormalised
+                os << "        if(i0 + j < e0) {\n";
+                os << "          const R d = (" << root.v << " - " << nc << ") / " << vw << ";\n";
+                os << "          av += d * d;\n";
+                if(grad && T.NG > 0) {
+                    os << "          const R w = R(2) * d / " << vw << ";\n";
+                    for(int s = 0; s < T.NG; ++s) {
+                        auto it = root.g.find(s);
+                        if(it != root.g.end())
+                            os << "          ag" << s << " += (" << it->second << ") * w;\n";
+                    }
+                }
+                os << "        }\n";
+                break;
+            case GF_FIT_BINNED_CHISQ: // calculateChisq, MetricPointer.cu:54-60
+                os << "        if(i0 + j < e0) {\n";
+                os << "          const R dd = pv * " << vw << " * Tn - " << nc << ";\n";
+                os << "          const R den = " << nc << " > R(1) ? " << nc << " : R(1);\n";
+                os << "          av += dd * dd / den;\n";
+                if(grad && T.NG > 0) {
+                    os << "          const R w = R(2) * dd / den * Tn * " << vw << ";\n";
+                    for(int s = 0; s < T.NG; ++s) {
+                        std::string e = dpv(s);
+                        if(!e.empty())
+                            os << "          ag" << s << " += (" << e << ") * w;\n";
+                    }
+                }
+                os << "        }\n";
+                break;
+            default: // calculateNLL, MetricPointer.cu:13-16
+                os << "        if(i0 + j < e0 && pv > R(0)) {\n";
+                os << "          av -= GF_LOG(pv);\n";
+                if(grad && T.NG > 0) {
+                    os << "          const R inv = R(1) / pv;\n";
+                    for(int s = 0; s < T.NG; ++s) {
+                        std::string e = dpv(s);
+                        if(!e.empty())
+                            os << "          ag" << s << " -= (" << e << ") * inv;\n";
+                    }
+                }
+                os << "        }\n";
             }
-            os << "        }\n";
         }
         os << "        }\n      }\n    }\n";
         if(values) {

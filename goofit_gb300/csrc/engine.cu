@@ -853,7 +853,7 @@ void postToy(gf_engine *e, int t, double *o) {
         double ex       = 0;
         for(int p : T.nodes[0].params)
             ex += q(p);
-        const double ne = (double)e->toys[t].n;
+        const double ne = e->toys[t].total;
         o[0] += (ex - ne * std::log(ex));
         for(int p : T.nodes[0].params)
             if(T.gslot[p] >= 0)
@@ -1008,7 +1008,14 @@ int gf_set_tree(gf_engine *e, const gf_node *nodes, int n_nodes, const gf_observ
         return gf_fail(nullptr, GF_ERR_INVALID, "null engine");
     cudaSetDevice(e->device);
     gf::Tree t;
-    std::string why = t.build(nodes, n_nodes, obs, n_obs, n_params, grad_mask);
+    // binned metrics: two more columns after the observables, the bin content and the volume / error
+    std::vector<gf_observable> ob(obs, obs + std::max(0, n_obs));
+    if(e->fit_metric != GF_FIT_UNBINNED_NLL) {
+        ob.push_back(gf_observable{-1e300, 1e300, 1, 0});
+        ob.push_back(gf_observable{-1e300, 1e300, 1, 0});
+    }
+    t.fit_metric    = e->fit_metric;
+    std::string why = t.build(nodes, n_nodes, ob.data(), (int)ob.size(), n_params, grad_mask);
     if(!why.empty())
         return gf_fail(e, GF_ERR_BAD_TREE, why);
     freeLayout(e);
@@ -1036,6 +1043,17 @@ int gf_set_tree(gf_engine *e, const gf_node *nodes, int n_nodes, const gf_observ
     if(rc)
         return rc;
     e->has_tree = true;
+    return GF_OK;
+}
+
+int gf_set_fit_metric(gf_engine *e, int fit_metric) {
+    if(!e)
+        return gf_fail(nullptr, GF_ERR_INVALID, "null engine");
+    if(fit_metric < GF_FIT_UNBINNED_NLL || fit_metric > GF_FIT_BINNED_CHISQ)
+        return gf_fail(e, GF_ERR_INVALID, "unknown fit metric");
+    if(e->has_tree && fit_metric != e->fit_metric)
+        return gf_fail(e, GF_ERR_STATE, "gf_set_fit_metric must come before gf_set_tree");
+    e->fit_metric = fit_metric;
     return GF_OK;
 }
 
@@ -1175,6 +1193,12 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
     ty.n      = n;
     ty.npad   = npad;
     ty.loaded = true;
+    ty.total  = (double)n;
+    if(e->fit_metric != GF_FIT_UNBINNED_NLL) {
+        ty.total = 0;
+        for(int64_t i = 0; i < n; ++i)
+            ty.total += soa[(int64_t)(NO - 2) * n + i];
+    }
     if(herr)
         return gf_fail(e, GF_ERR_INVALID, "event outside the observable range of a ConvolutionPdf");
     return GF_OK;

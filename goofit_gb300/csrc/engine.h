@@ -47,6 +47,7 @@ struct GfArgs {
 struct GfToy {
     int64_t n    = 0;
     int64_t npad = 0;
+    double total = 0; // number of events: n, or the summed bin contents of binned data
     void *cols[16] = {nullptr};
     int *kcols[8]  = {nullptr};
     void *abase    = nullptr;           // cached resonance amplitudes and FP64 Dalitz columns (one allocation)
@@ -82,6 +83,7 @@ struct gf_engine {
     bool chunk_fixed = false;
     int evt_ctas_per_sm = 4;
 
+    int fit_metric = GF_FIT_UNBINNED_NLL;
     int n_toys = 1;
     std::vector<GfToy> toys;
 

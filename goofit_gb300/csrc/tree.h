@@ -114,6 +114,7 @@ struct Tree {
     std::vector<NumInfo> nums;
     std::vector<int> num_of; // node -> index in nums or -1
     std::vector<int> kgrid;  // host copy of all grid k tables
+    int fit_metric = GF_FIT_UNBINNED_NLL; // binned metrics: the last two observables are content and volume/error
     std::vector<Amp3Info> amp3s;
     std::vector<int> amp3_of; // node -> index in amp3s or -1
     std::vector<Amp4Info> amp4s;

@@ -115,6 +115,11 @@ class Engine:
         A.check(rc, self._h)
 
     # ---- tree / data ----
+    def set_fit_metric(self, metric: int) -> None:
+        """GF_FIT_UNBINNED_NLL (default) or a binned metric; before set_tree."""
+        self._check(self._L.gf_set_fit_metric(self._h, metric))
+        self.fit_metric = metric
+
     def set_tree(self, nodes: list[dict], observables: list[tuple], n_params: int, grad_mask=None) -> None:
         self._nodes = A.NodeList(nodes)
         self._obs = A.observables_array(observables)
@@ -123,7 +128,8 @@ class Engine:
         self._check(self._L.gf_set_tree(self._h, self._nodes.arr, self._nodes.n, self._obs, len(observables),
                                         n_params, mp))
         self.n_params = n_params
-        self.n_obs = len(observables)
+        # binned metrics carry two more rows: bin contents and volumes (or errors)
+        self.n_obs = len(observables) + (2 if getattr(self, "fit_metric", 0) else 0)
         self.n_grad = self._L.gf_num_grad(self._h)
         buf = (C.c_int32 * max(1, self.n_grad))()
         self._L.gf_grad_params(self._h, buf, self.n_grad)

@@ -122,6 +122,20 @@ typedef struct gf_observable {
 /* What a per-event evaluation returns (include/goofit/FitControl.h:11). */
 enum gf_metric { GF_METRIC_EVAL = 0, GF_METRIC_NLL = 1, GF_METRIC_PROB = 2 };
 
+/* What the fit minimises (the FitControl classes, include/goofit/FitControl.h:40-76, and their metric functions
+   src/PDFs/MetricPointer.cu:13-58).  The binned metrics take bins as events: the observable columns hold the bin
+   centres, followed by two more columns, the bin content and the bin volume (GF_FIT_BINNED_ERROR: the bin
+   error), as PdfBase::setData lays out a BinnedDataSet (src/PDFs/PdfBase.cu:439-495).  The expected number of
+   events of a bin is c_totalEvents * P * norm * volume with c_totalEvents = the number of bins, as the
+   reference sets it (src/PDFs/PdfBase.cu:527). */
+enum gf_fit_metric {
+    GF_FIT_UNBINNED_NLL = 0, /* UnbinnedNllFit: -sum log(P norm) */
+    GF_FIT_BINNED_NLL   = 1, /* BinnedNllFit (BinAvg): sum (mu - n log mu), mu = T P norm V */
+    GF_FIT_BINNED_ERROR = 2, /* BinnedErrorFit (BinWithError): sum ((P - n) / err)^2, P unnormalised */
+    GF_FIT_BINNED_CHISQ = 3  /* BinnedChisqFit (Chisq): sum (T P norm V - n)^2 / max(n, 1) */
+};
+
+
 typedef struct gf_engine gf_engine;
 
 /* ---- engine lifetime ---- */
@@ -140,6 +154,9 @@ int gf_set_tree(gf_engine *eng,
                 int n_obs,
                 int n_params,
                 const int32_t *grad_mask);
+/* Selects the fit metric (enum gf_fit_metric, default GF_FIT_UNBINNED_NLL).  A binned metric adds the two bin
+   columns to the observables of the next gf_set_tree (call it before gf_set_tree). */
+int gf_set_fit_metric(gf_engine *eng, int fit_metric);
 
 /* Number of independent datasets ("toys"), each with its own parameter vector. */
 int gf_set_num_toys(gf_engine *eng, int n_toys);

@@ -966,6 +966,61 @@ int oracle_nll(const gf_node *nodes,
     }
 }
 
+// A binned fit's objective (MetricPointer.cu:23-60 over PdfBase::setData's binned layout,
+// src/PDFs/PdfBase.cu:439-527): soa holds n_obs - 2 centre columns, the bin contents and the bin volumes
+// (metric 2: the bin errors); c_totalEvents is the number of bins.
+int oracle_binned(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, const double *params,
+                  int n_params, const double *soa, int64_t n_bins, int metric, double *out) {
+    try {
+        Oracle O;
+        load(O, nodes, n_nodes, obs, n_obs, params, n_params, 0);
+        O.normalize(0);
+        O.prepareConvTables(soa, n_bins);
+        const double rootNorm = O.norm[0];
+        const double T        = (double)n_bins;
+        const double *cont = soa + (int64_t)(n_obs - 2) * n_bins, *vw = soa + (int64_t)(n_obs - 1) * n_bins;
+        double ret = 0, total = 0;
+#pragma omp parallel for reduction(+ : ret, total) schedule(static)
+        for(int64_t e = 0; e < n_bins; ++e) {
+            double evt[16];
+            for(int o = 0; o < n_obs; ++o)
+                evt[o] = soa[o * n_bins + e];
+            const double rawPdf = O.eval(0, evt);
+            total += cont[e];
+            if(metric == 1) {
+                double r = rawPdf * rootNorm;
+                r *= vw[e];
+                if(r > 0) {
+                    const double expEvents = T * r;
+                    ret += (expEvents - cont[e] * std::log(expEvents));
+                }
+            } else if(metric == 2) {
+                double r = rawPdf;
+                r -= cont[e];
+                r /= vw[e];
+                r *= r;
+                ret += r;
+            } else {
+                double r = rawPdf * rootNorm;
+                r *= vw[e];
+                const double d = r * T - cont[e];
+                ret += d * d / (cont[e] > 1 ? cont[e] : 1);
+            }
+        }
+        if(O.nodes[0].op == GF_OP_ADD_EXT) {
+            double expEvents = 0;
+            for(size_t k = 0; k < O.nodes[0].params.size(); ++k)
+                expEvents += O.par(0, (int)k);
+            ret += (expEvents - total * std::log(expEvents));
+        }
+        *out = ret;
+        return 0;
+    } catch(std::exception &ex) {
+        g_err = ex.what();
+        return 1;
+    }
+}
+
 // The Amp3Body integrals I_ij (n x n complex, interleaved re/im) of node `node` at the given parameters.
 int oracle_amp3_integrals(const gf_node *nodes,
                           int n_nodes,

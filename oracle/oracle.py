@@ -46,6 +46,9 @@ def lib() -> C.CDLL:
         L.oracle_amp3_resonance.argtypes = [C.POINTER(A.gf_node), C.c_int, C.POINTER(A.gf_observable), C.c_int,
                                             f64p, C.c_int, C.c_int, C.c_int, f64p, f64p, C.c_int64, f64p]
         L.oracle_amp3_resonance.restype = C.c_int
+        L.oracle_binned.argtypes = [C.POINTER(A.gf_node), C.c_int, C.POINTER(A.gf_observable), C.c_int, f64p,
+                                    C.c_int, f64p, C.c_int64, C.c_int, f64p]
+        L.oracle_binned.restype = C.c_int
         L.oracle_set_amp4_norm_events.argtypes = [f64p, C.c_int64]
         L.oracle_amp4_gram.argtypes = [C.POINTER(A.gf_node), C.c_int, C.POINTER(A.gf_observable), C.c_int, f64p,
                                        C.c_int, C.c_int, f64p]
@@ -194,3 +197,15 @@ def get4vecs(v5, masses5) -> np.ndarray:
     out = np.zeros(16)
     lib().oracle_get4vecs(a.ctypes.data_as(f64p), m.ctypes.data_as(f64p), out.ctypes.data_as(f64p))
     return out.reshape(4, 4)
+
+
+def binned(nodes, observables, params, soa, metric: int) -> float:
+    """A binned fit's objective; soa = bin centres of the observables, contents, volumes (or errors)."""
+    obs_all = list(observables) + [(-1e300, 1e300, 1, 0), (-1e300, 1e300, 1, 0)]
+    nl, obs, p, pp, s = _prep(nodes, obs_all, params, soa)
+    out = C.c_double()
+    rc = lib().oracle_binned(nl.arr, nl.n, obs, len(obs_all), pp, len(p), s.ctypes.data_as(C.POINTER(C.c_double)),
+                             s.shape[1], metric, C.byref(out))
+    if rc:
+        raise OracleError(lib().oracle_last_error().decode())
+    return out.value
