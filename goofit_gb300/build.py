@@ -25,7 +25,7 @@ CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["engine.cu", "noalloc.cu"]
+CU_SOURCES = ["engine.cu", "noalloc.cu", "gram_tc.cu"]
 CXX17_SOURCES = ["tree.cpp", "codegen.cpp", "rtc.cpp"]
 CXX20_SOURCES = ["migrad.cpp", "fit.cpp"]
 

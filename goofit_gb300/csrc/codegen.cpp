@@ -58,6 +58,11 @@ struct Ctx {
     std::function<std::string(int, int)> amp; // amplitude node, amplitude -> R2 amplitude expression
     std::function<std::string(int)> ampcol;   // amplitude / derivative column -> R2 expression
     bool lohi = false;                        // normalisation factors as FP32 hi + lo pairs
+    // the root, when it is an amplitude PDF: |T|^2 = tr^2 + ti^2 and, per gradient slot, the inner term
+    // d|T|^2/dp / 2 (its gradient divided by the value needs no efficiency)
+    bool ampRoot = false;
+    std::string ampTr, ampTi;
+    std::map<int, std::string> ampInner;
     int uid = 0;
     std::string tmp(const char *p) { return std::string(p) + std::to_string(uid++); }
 };
@@ -410,12 +415,25 @@ Val emit(Ctx &c, int i) {
         }
         os << "    const R " << v << " = (" << tr << " * " << tr << " + " << ti << " * " << ti << ") * " << ev.v << ";\n";
         out.v = v;
+        auto inner = [&](int s, const std::string &e) {
+            if(s < 0 || !c.grad || i != 0)
+                return;
+            auto it = c.ampInner.find(s);
+            c.ampInner[s] = it == c.ampInner.end() ? "(" + e + ")" : "(" + it->second + " + " + e + ")";
+        };
+        if(i == 0) {
+            c.ampRoot = true;
+            c.ampTr   = tr;
+            c.ampTi   = ti;
+        }
         for(int r = 0; r < nRes; ++r) {
             std::string b = c.amp(ai, r);
             gadd(c, out, slot(c, n.params[2 * r]),
                  "R(2) * (" + tr + " * " + b + ".x + " + ti + " * " + b + ".y) * " + ev.v);
             gadd(c, out, slot(c, n.params[2 * r + 1]),
                  "R(2) * (" + ti + " * " + b + ".x - " + tr + " * " + b + ".y) * " + ev.v);
+            inner(slot(c, n.params[2 * r]), tr + " * " + b + ".x + " + ti + " * " + b + ".y");
+            inner(slot(c, n.params[2 * r + 1]), ti + " * " + b + ".x - " + tr + " * " + b + ".y");
         }
         // resonance / line-shape parameters: d|T|^2/dt = 2 Re(conj(T) sum_a c_a dA_a/dt)
         if(c.grad && c.ampcol)
@@ -429,6 +447,7 @@ Val emit(Ctx &c, int i) {
                     os << "    " << di << " += " << cr << " * " << d << ".y + " << cim << " * " << d << ".x;\n";
                 }
                 gadd(c, out, t.slot, "R(2) * (" + tr + " * " + dr + " + " + ti + " * " + di + ") * " + ev.v);
+                inner(t.slot, tr + " * " + dr + " + " + ti + " * " + di);
             }
         break;
     }
@@ -559,6 +578,9 @@ __device__ __forceinline__ ACC warp_acc2(ACC a) {
     }
     return a;
 }
+__device__ __forceinline__ ACC acc_shfl_xor(ACC a, int o) {
+    return make_float2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
+}
 __device__ __forceinline__ double acc_value(ACC a) { return (double)a.x + (double)a.y; }
 __device__ __forceinline__ float acc_r(ACC a) { return a.x + a.y; }
 // x * (h + l) for a normalisation factor kept as an FP32 pair: one rounding, no bias from rounding the factor
@@ -579,6 +601,7 @@ __device__ __forceinline__ ACC acc_of(double v) { return v; }
 __device__ __forceinline__ ACC acc_add(ACC a, ACC b) { return a + b; }
 __device__ __forceinline__ ACC warp_acc(double v) { return gf_warp_sum(v); }
 __device__ __forceinline__ ACC warp_acc2(ACC a) { return gf_warp_sum(a); }
+__device__ __forceinline__ ACC acc_shfl_xor(ACC a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
 __device__ __forceinline__ double acc_value(ACC a) { return a; }
 __device__ __forceinline__ double acc_r(ACC a) { return a; }
 __device__ __forceinline__ double gf_nm(double x, double h, double l) { return x * h; }
@@ -1107,6 +1130,50 @@ void emitNormReads(std::ostream &os, const Tree &T, bool grad, const NormLayout 
 
 int padComps(int c) { return c <= 1 ? 1 : c <= 2 ? 2 : (c + 3) / 4 * 4; }
 
+// Sums K per-thread values over a warp into red[wid][0..K) by a transposed butterfly (recursive halving):
+// at each of the five exchange steps a lane keeps one half of its values and sends the other half to its
+// partner, so that a warp exchanges about K values instead of 5 K.  Components go in groups of at most 32;
+// after the exchanges a lane holds one component, summed over the warp.  Ends with __syncthreads().
+void emitCtaReduce(std::ostream &os, const std::vector<std::string> &vals, const std::string &ind) {
+    const int K = (int)vals.size();
+    for(int g0 = 0; g0 < K; g0 += 32) {
+        const int k = std::min(32, K - g0);
+        int kp      = 1;
+        while(kp < k)
+            kp <<= 1;
+        os << ind << "{\n";
+        for(int i = 0; i < kp; ++i)
+            os << ind << "  ACC t" << i << " = " << (i < k ? "acc_of(" + vals[g0 + i] + ")" : std::string("acc_zero()"))
+               << ";\n";
+        int m = kp, dup = 0;
+        std::vector<std::pair<int, int>> halves;
+        for(int o = 16; o > 0; o >>= 1) {
+            if(m >= 2) {
+                const int h = m / 2;
+                os << ind << "  { const bool b = (lane & " << o << ") != 0;\n";
+                for(int i = 0; i < h; ++i)
+                    os << ind << "    { const ACC s = b ? t" << i << " : t" << i + h << ", q = b ? t" << i + h << " : t"
+                       << i << "; t" << i << " = acc_add(q, acc_shfl_xor(s, " << o << ")); }\n";
+                os << ind << "  }\n";
+                halves.push_back({o, h});
+                m = h;
+            } else {
+                os << ind << "  t0 = acc_add(t0, acc_shfl_xor(t0, " << o << "));\n";
+                dup |= o;
+            }
+        }
+        os << ind << "  if((lane & " << dup << ") == 0) {\n";
+        os << ind << "    const int c = " << g0;
+        for(auto &hv : halves)
+            os << " + ((lane & " << hv.first << ") ? " << hv.second << " : 0)";
+        os << ";\n";
+        os << ind << "    if(c < " << g0 + k << ") red[wid][c] = t0;\n";
+        os << ind << "  }\n";
+        os << ind << "}\n";
+    }
+    os << ind << "__syncthreads();\n";
+}
+
 struct Gen {
     const Tree &T;
     bool mixed;
@@ -1371,32 +1438,31 @@ struct Gen {
         os << "  __shared__ ACC red[" << NW << "][" << NGp << "];\n";
         os << "  __shared__ ACC tot[" << NGp << "];\n";
         os << "  __shared__ int last;\n";
-        os << "  { const ACC t = warp_acc(av); if(lane == 0) red[wid][0] = t; }\n";
-        for(int s = 0; s < NGp - 1; ++s)
-            os << "  { const ACC t = warp_acc(ag" << s << "); if(lane == 0) red[wid][" << 1 + s << "] = t; }\n";
-        os << "  __syncthreads();\n";
-        os << "  ACC *gp = reinterpret_cast<ACC *>(a.gpartial) + (((i64)toy * " << NQ << " + q) * " << plan.max_grid_blocks
-           << " + blockIdx.x) * " << NGs << ";\n";
+        {
+            std::vector<std::string> comps{"av"};
+            for(int s = 0; s < NGp - 1; ++s)
+                comps.push_back("ag" + std::to_string(s));
+            emitCtaReduce(os, comps, "  ");
+        }
+        // block partials are component-major: gpartial[toy][q][comp][block]
+        os << "  ACC *gp = reinterpret_cast<ACC *>(a.gpartial) + ((i64)toy * " << NQ << " + q) * " << NGs << " * "
+           << plan.max_grid_blocks << ";\n";
         os << "  if(tid < " << NGp << ") { ACC t = acc_zero(); for(int w = 0; w < " << NW
-           << "; ++w) t = acc_add(t, red[w][tid]); gp[tid] = t; }\n";
+           << "; ++w) t = acc_add(t, red[w][tid]); gp[(i64)tid * " << plan.max_grid_blocks << " + blockIdx.x] = t; }\n";
         os << "  __threadfence();\n  __syncthreads();\n";
         os << "  if(tid == 0) { unsigned prev = atomicAdd(&a.gcounter[toy * " << NQ
            << " + q], 1u); last = (prev == (unsigned)(nblk - 1)); }\n";
         os << "  __syncthreads();\n";
         os << "  if(!last) return;\n";
         os << "  __threadfence();\n";
-        os << "  const ACC *g0 = reinterpret_cast<const ACC *>(a.gpartial) + ((i64)toy * " << NQ << " + q) * "
-           << plan.max_grid_blocks << " * " << NGs << ";\n";
-        os << "  {\n";
-        os << "    ACC s[" << NGp << "];\n";
-        os << "#pragma unroll\n    for(int comp = 0; comp < " << NGp << "; ++comp) s[comp] = acc_zero();\n";
-        os << "    for(int bi = tid; bi < nblk; bi += " << block << ") {\n";
-        os << "#pragma unroll\n      for(int comp = 0; comp < " << NGp << "; ++comp) s[comp] = acc_add(s[comp], g0[bi * " << NGs << " + comp]);\n";
-        os << "    }\n";
-        os << "#pragma unroll\n    for(int comp = 0; comp < " << NGp << "; ++comp) { const ACC t = warp_acc2(s[comp]); if(lane == 0) red[wid][comp] = t; }\n";
+        // one warp per component: contiguous loads of that component's block partials, then a warp reduction
+        os << "  for(int comp = wid; comp < " << NGp << "; comp += " << NW << ") {\n";
+        os << "    const ACC *pc = gp + (i64)comp * " << plan.max_grid_blocks << ";\n";
+        os << "    ACC t = acc_zero();\n";
+        os << "#pragma unroll 4\n    for(int bi = lane; bi < nblk; bi += 32) t = acc_add(t, pc[bi]);\n";
+        os << "    t = warp_acc2(t);\n";
+        os << "    if(lane == 0) tot[comp] = t;\n";
         os << "  }\n";
-        os << "  __syncthreads();\n";
-        os << "  if(tid < " << NGp << ") { ACC t = acc_zero(); for(int w = 0; w < " << NW << "; ++w) t = acc_add(t, red[w][tid]); tot[tid] = t; }\n";
         os << "  __syncthreads();\n";
         os << "  if(tid == 0) {\n";
         os << "    a.gcounter[toy * " << NQ << " + q] = 0u;\n";
@@ -1867,13 +1933,18 @@ struct Gen {
                     plan.obs_used_evt.push_back(o);
         }
         const std::string rootN = T.nk[0] == NK_ONE ? "" : "N0";
+        // a host-computed root normalisation is applied on the host (plan.factor_root)
+        const bool factorRoot = !values && T.fit_metric == GF_FIT_UNBINNED_NLL &&
+                                (T.nk[0] == NK_EXP || T.nk[0] == NK_GAUSS || T.nk[0] == NK_AMP3 || T.nk[0] == NK_AMP4);
+        plan.factor_root = T.fit_metric == GF_FIT_UNBINNED_NLL &&
+                           (T.nk[0] == NK_EXP || T.nk[0] == NK_GAUSS || T.nk[0] == NK_AMP3 || T.nk[0] == NK_AMP4);
 
         os << "extern \"C\" __global__ void __launch_bounds__(" << block << ") " << name << "(const GfArgs a) {\n";
         os << "  extern __shared__ __align__(16) unsigned char smraw[];\n";
         os << "  R *stab = reinterpret_cast<R *>(smraw); (void)stab;\n";
         os << "  __shared__ int s_toy, last;\n";
         if(!values)
-            os << "  __shared__ ACC red[" << NW << "][" << NGp << "];\n";
+            os << "  __shared__ ACC red[" << NW << "][" << NGp + 1 << "];\n";
         os << "  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5; (void)lane; (void)wid;\n";
         os << "  const int cb = (int)(((i64)a.n_chunks * blockIdx.x) / gridDim.x);\n";
         os << "  const int ce = (int)(((i64)a.n_chunks * (blockIdx.x + 1)) / gridDim.x);\n";
@@ -1935,7 +2006,7 @@ struct Gen {
                 os << "    const R2 *acp" << ac << " = reinterpret_cast<const R2 *>(a.acol[(i64)toy * " << NA << " + " << ac
                    << "]);\n";
         if(!values) {
-            os << "    R av = R(0);\n";
+            os << "    R av = R(0), nv = R(0); (void)nv;\n";
             for(int s = 0; s < NGp - 1; ++s)
                 os << "    R ag" << s << " = R(0);\n";
         }
@@ -2072,6 +2143,34 @@ struct Gen {
                 os << "        }\n";
                 break;
             default: // calculateNLL, MetricPointer.cu:13-16
+                if(factorRoot) {
+                    // -log(P N) = -log P - log N: the event pass sums -log P and -dP/P and counts the events
+                    // with P > 0; the host adds count * (-log N) and count * (-dN/N) in FP64
+                    os << "        if(i0 + j < e0 && " << root.v << " > R(0)) {\n";
+                    os << "          av -= GF_LOG(" << root.v << ");\n";
+                    os << "          nv += R(1);\n";
+                    if(grad && T.NG > 0) {
+                        if(c.ampRoot) {
+                            // |T|^2 eff: d/dp over the value is 2 inner / |T|^2, the efficiency cancels
+                            os << "          const R iT = R(2) / (" << c.ampTr << " * " << c.ampTr << " + " << c.ampTi
+                               << " * " << c.ampTi << ");\n";
+                            for(int s = 0; s < T.NG; ++s) {
+                                auto it = c.ampInner.find(s);
+                                if(it != c.ampInner.end())
+                                    os << "          ag" << s << " -= " << it->second << " * iT;\n";
+                            }
+                        } else {
+                            os << "          const R inv = R(1) / " << root.v << ";\n";
+                            for(int s = 0; s < T.NG; ++s) {
+                                auto it = root.g.find(s);
+                                if(it != root.g.end())
+                                    os << "          ag" << s << " -= (" << it->second << ") * inv;\n";
+                            }
+                        }
+                    }
+                    os << "        }\n";
+                    break;
+                }
                 os << "        if(i0 + j < e0 && pv > R(0)) {\n";
                 os << "          av -= GF_LOG(pv);\n";
                 if(grad && T.NG > 0) {
@@ -2090,36 +2189,45 @@ struct Gen {
             os << "  }\n}\n\n";
             return;
         }
-        os << "    { const ACC t = warp_acc(av); if(lane == 0) red[wid][0] = t; }\n";
-        for(int s = 0; s < NGp - 1; ++s)
-            os << "    { const ACC t = warp_acc(ag" << s << "); if(lane == 0) red[wid][" << 1 + s << "] = t; }\n";
-        os << "    __syncthreads();\n";
+        // components: value, gradient slots, and (factored root normalisation) the count of events with P > 0,
+        // which lands in out[2 + NG]; partials have stride 2 + NG, results 3 + NG
+        const int NGc = NGp + (factorRoot ? 1 : 0);
+        const int OS  = NGs + 2;
+        {
+            std::vector<std::string> comps{"av"};
+            for(int s = 0; s < NGp - 1; ++s)
+                comps.push_back("ag" + std::to_string(s));
+            if(factorRoot)
+                comps.push_back("nv");
+            emitCtaReduce(os, comps, "    ");
+        }
+        // chunk partials are component-major: part[comp][chunk], so that the finisher's loads are contiguous
         os << "    ACC *part = reinterpret_cast<ACC *>(a.partial);\n";
-        os << "    if(tid < " << NGp << ") { ACC t = acc_zero(); for(int w = 0; w < " << NW
-           << "; ++w) t = acc_add(t, red[w][tid]); part[(i64)ch * " << NGs << " + tid] = t; }\n";
+        os << "    if(tid < " << NGc << ") { ACC t = acc_zero(); for(int w = 0; w < " << NW
+           << "; ++w) t = acc_add(t, red[w][tid]); part[(i64)tid * a.n_chunks + ch] = t; }\n";
         os << "    __threadfence();\n    __syncthreads();\n";
         os << "    if(tid == 0) { unsigned prev = atomicAdd(&a.counter[toy], 1u); last = (prev == "
               "(unsigned)(a.toy_nchunks[toy] - 1)); }\n";
         os << "    __syncthreads();\n";
-        // finishing CTA of the toy: every thread loads a strided share of the chunk partials (independent
-        // loads), then a warp and a CTA reduction of the compensated pairs
+        // finishing CTA of the toy: one warp per component sums that component's chunk partials (contiguous,
+        // independent loads) and reduces them across its lanes
         os << "    if(last) {\n";
         os << "      __threadfence();\n";
         os << "      const int c0 = a.toy_chunk0[toy], nc = a.toy_nchunks[toy];\n";
-        os << "      ACC s[" << NGp << "];\n";
-        os << "#pragma unroll\n      for(int comp = 0; comp < " << NGp << "; ++comp) s[comp] = acc_zero();\n";
-        os << "#pragma unroll 4\n      for(int c = tid; c < nc; c += " << block << ") {\n";
-        os << "        const ACC *pc = part + (i64)(c0 + c) * " << NGs << ";\n";
-        os << "#pragma unroll\n        for(int comp = 0; comp < " << NGp << "; ++comp) s[comp] = acc_add(s[comp], pc[comp]);\n";
-        os << "      }\n";
-        os << "#pragma unroll\n      for(int comp = 0; comp < " << NGp << "; ++comp) { const ACC t = warp_acc2(s[comp]); if(lane == 0) red[wid][comp] = t; }\n";
-        os << "      __syncthreads();\n";
-        os << "      if(tid < " << NGp << ") {\n";
-        os << "        ACC t = acc_zero(); for(int w = 0; w < " << NW << "; ++w) t = acc_add(t, red[w][tid]);\n";
-        os << "        double *o = a.out + (i64)toy * " << NGs + 1 << ";\n";
-        os << "        const double v = acc_value(t);\n";
-        os << "        o[tid == 0 ? 0 : 1 + tid] = v;\n";
-        os << "        if(tid == 0) { int st = a.qflag[toy]; if(v == 0.0) st |= 4; o[1] = (double)st; a.counter[toy] = 0u; a.qflag[toy] = 0; }\n";
+        os << "      double *o = a.out + (i64)toy * " << OS << ";\n";
+        os << "      for(int comp = wid; comp < " << NGc << "; comp += " << NW << ") {\n";
+        os << "        const ACC *pc = part + (i64)comp * a.n_chunks + c0;\n";
+        os << "        ACC t = acc_zero();\n";
+        os << "#pragma unroll 4\n        for(int c = lane; c < nc; c += 32) t = acc_add(t, pc[c]);\n";
+        os << "        t = warp_acc2(t);\n";
+        os << "        if(lane == 0) {\n";
+        os << "          const double v = acc_value(t);\n";
+        os << "          o[comp == 0 ? 0 : (comp == " << NGp << " && " << (factorRoot ? 1 : 0) << " ? " << 2 + T.NG
+           << " : 1 + comp)] = v;\n";
+        // a zero NLL is flagged here, or on the host after the factored normalisation is added
+        os << "          if(comp == 0) { int st = a.qflag[toy]; " << (factorRoot ? "" : "if(v == 0.0) st |= 4; ")
+           << "o[1] = (double)st; a.counter[toy] = 0u; a.qflag[toy] = 0; }\n";
+        os << "        }\n";
         os << "      }\n";
         os << "    }\n";
         os << "    __syncthreads();\n";

@@ -142,6 +142,10 @@ void freeLayout(gf_engine *e) {
     dfree(e->d_dcols);
     dfree(e->d_dgrid);
     dfree(e->d_gram);
+    dfree(e->d_gtc_part);
+    dfree(e->d_gtc_out);
+    dfree(e->d_gtc_err);
+    e->gtc_part_n = e->gtc_out_n = 0;
     dfree(e->d_dirty);
     hfree(e->h_gram);
     hfree(e->h_dirty);
@@ -185,6 +189,14 @@ int dalloc(gf_engine *e, T *&p, size_t count, bool zero = true) {
     return GF_OK;
 }
 
+// complex scratch columns of amplitude node k: its amplitudes, then one derivative column per (theta, amplitude)
+int ampColumns(const gf::Tree &T, int k) {
+    int nd = 0;
+    for(auto &th : T.amp_theta(k))
+        nd += (int)th.amps.size();
+    return T.amp_count(k) + nd;
+}
+
 int buildLayout(gf_engine *e) {
     if(e->layout_ready)
         return GF_OK;
@@ -195,15 +207,16 @@ int buildLayout(gf_engine *e) {
     for(int t = 0; t < NT; ++t)
         if(!e->toys[t].loaded)
             return gf_fail(e, GF_ERR_STATE, "toy " + std::to_string(t) + " has no events");
-    // chunk size: about one chunk per resident event CTA, a multiple of 8 events x 256 threads
+    // chunk size: one chunk per resident event CTA (SMs x the event kernel's occupancy), so that a single
+    // wave covers every SM with equal work; a multiple of 256 events (a warp's pass at 8 events per thread)
     if(!e->chunk_fixed) {
         int64_t total = 0;
         for(int t = 0; t < NT; ++t)
             total += e->toys[t].n;
         const int64_t target = (int64_t)std::max(1, e->sm_count) * e->evt_ctas_per_sm;
         int64_t ch           = (total + target - 1) / target;
-        ch                   = (ch + 2047) / 2048 * 2048;
-        e->chunk             = (int)std::min<int64_t>(std::max<int64_t>(ch, 2048), 1 << 20);
+        ch                   = (ch + 255) / 256 * 256;
+        e->chunk             = (int)std::min<int64_t>(std::max<int64_t>(ch, 256), 1 << 20);
     }
     std::vector<long long> chunks;
     std::vector<int> c0(NT), nc(NT);
@@ -257,9 +270,9 @@ int buildLayout(gf_engine *e) {
     chk(dalloc(e, e->d_gsum, (size_t)NT * std::max(1, NQ)));
     chk(dalloc(e, e->d_gpartial, (size_t)NT * std::max(1, NQ) * std::max(1, e->plan.max_grid_blocks) * NGp));
     chk(dalloc(e, e->d_gcounter, (size_t)NT * std::max(1, NQ)));
-    chk(dalloc(e, e->d_partial, (size_t)e->n_chunks * NGp));
+    chk(dalloc(e, e->d_partial, (size_t)e->n_chunks * (NGp + 1)));
     chk(dalloc(e, e->d_counter, NT));
-    chk(dalloc(e, e->d_out, (size_t)NT * (NGp + 1)));
+    chk(dalloc(e, e->d_out, (size_t)NT * (NGp + 2)));
     chk(dalloc(e, e->d_chunks, chunks.size()));
     chk(dalloc(e, e->d_toy_chunk0, NT));
     chk(dalloc(e, e->d_toy_nchunks, NT));
@@ -274,6 +287,29 @@ int buildLayout(gf_engine *e) {
     chk(dalloc(e, e->d_dgrid, std::max<size_t>(1, ngrid)));
     chk(dalloc(e, e->d_gram, (size_t)NT * std::max(1, NTILE) * e->gram_blocks * std::max(1, 2 * e->plan.gram_pairs_max)));
     chk(dalloc(e, e->d_dirty, NT));
+    // the integrals of the mixed-precision engine go through the tensor-core Gram kernel when every amplitude
+    // node has at most 32 complex columns (values and derivatives); GF_GRAM=cuda keeps the CUDA-core kernel
+    e->gram_tc = false;
+    if(e->precision == GF_MIXED && T.n_amp_nodes() > 0) {
+        const char *g = std::getenv("GF_GRAM");
+        e->gram_tc    = !(g && std::string(g) == "cuda");
+        size_t np = 0, no = 0;
+        for(int k = 0; k < T.n_amp_nodes(); ++k) {
+            const int nc = ampColumns(T, k);
+            if(gf_gram_tc_width(nc) == 0)
+                e->gram_tc = false;
+            np = std::max(np, gf_gram_tc_part_doubles(nc, std::max(1, e->sm_count)));
+            no = std::max(no, (size_t)4 * nc * nc);
+        }
+        if(e->gram_tc) {
+            chk(dalloc(e, e->d_gtc_part, np));
+            chk(dalloc(e, e->d_gtc_out, no));
+            chk(dalloc(e, e->d_gtc_err, 1));
+            e->gtc_part_n = np;
+            e->gtc_out_n  = no;
+            e->h_gtc.assign(no, 0.0);
+        }
+    }
     if(rc != GF_OK)
         return rc;
     if(cudaMallocHost((void **)&e->h_gram, sizeof(double) * (size_t)NT * std::max(1, NTILE) * e->gram_blocks *
@@ -299,7 +335,7 @@ int buildLayout(gf_engine *e) {
             cudaMemcpy(e->d_dgrid, g.data(), sizeof(unsigned) * g.size(), cudaMemcpyHostToDevice);
     }
     if(cudaMallocHost((void **)&e->h_P, e->pblock_bytes) != cudaSuccess ||
-       cudaMallocHost((void **)&e->h_out, sizeof(double) * (size_t)NT * (NGp + 1)) != cudaSuccess)
+       cudaMallocHost((void **)&e->h_out, sizeof(double) * (size_t)NT * (NGp + 2)) != cudaSuccess)
         return gf_fail(e, GF_ERR_OOM, "cudaMallocHost");
     std::memset(e->h_P, 0, e->pblock_bytes);
     e->h_active = reinterpret_cast<int *>(reinterpret_cast<char *>(e->h_P) + e->active_off);
@@ -427,7 +463,7 @@ cudaError_t enqueueEval(gf_engine *e, bool grad) {
         r = launch(grad ? e->mod.evt_g : e->mod.evt_n, dim3(evtGrid(e)), dim3(e->block),
                    grad ? e->plan.evt_smem_grad : e->plan.evt_smem_nograd, e->stream, a, kernelLast && e->use_pdl);
     if(r == cudaSuccess)
-        r = cudaMemcpyAsync(e->h_out, e->d_out, sizeof(double) * (size_t)NT * (NGp + 1), cudaMemcpyDeviceToHost,
+        r = cudaMemcpyAsync(e->h_out, e->d_out, sizeof(double) * (size_t)NT * (NGp + 2), cudaMemcpyDeviceToHost,
                             e->stream);
     if(r == cudaSuccess)
         r = cudaEventRecordWithFlags(e->ev[3], e->stream, cudaEventRecordExternal);
@@ -592,6 +628,8 @@ void fillRecordsT(gf_engine *e) {
     const gf::NormLayout &nl = e->plan.nl;
     const int NT = e->n_toys, np = T.n_params;
     R *rec = reinterpret_cast<R *>(reinterpret_cast<char *>(e->h_P) + sizeof(double) * (size_t)NT * std::max(1, np));
+    e->root_N.assign(NT, 1.0);
+    e->root_dN.assign((size_t)NT * std::max(1, T.NG), 0.0);
     static const double rootPi = std::sqrt(std::atan2(0.0, -1.0)), root2 = std::sqrt(2.0);
     for(int t = 0; t < NT; ++t) {
         e->host_flag[t] = 0;
@@ -618,6 +656,11 @@ void fillRecordsT(gf_engine *e) {
                 r[an.slotNL]    = (R)(N - (double)(R)N);
                 for(size_t k = 0; k < an.dN.size(); ++k)
                     r[an.dN[k].second] = (R)(-N * N * f * dQ[k]);
+                if(an.node == 0) {
+                    e->root_N[t] = N;
+                    for(size_t k = 0; k < an.dN.size(); ++k)
+                        e->root_dN[(size_t)t * std::max(1, T.NG) + an.dN[k].first] = -N * N * f * dQ[k];
+                }
                 if(an.node == 0) {
                     if(std::isnan(Iv))
                         e->host_flag[t] |= 1;
@@ -651,6 +694,11 @@ void fillRecordsT(gf_engine *e) {
             r[an.slotNL]   = (R)(N - (double)(R)N);
             for(auto &d : an.dN)
                 r[d.second] = (R)(-N * N * dI);
+            if(an.node == 0) {
+                e->root_N[t] = N;
+                for(auto &d : an.dN)
+                    e->root_dN[(size_t)t * std::max(1, T.NG) + d.first] = -N * N * dI;
+            }
             if(an.node == 0) {
                 if(std::isnan(I))
                     e->host_flag[t] |= 1;
@@ -781,6 +829,62 @@ int updateAmpCaches(gf_engine *e) {
         // the normalisation points of this toy: amplitudes (and derivatives), then their reduction
         a.gtoy = t;
         r      = launch(e->mod.ampn, dim3((unsigned)bn, 1, (unsigned)NAN_), dim3(256), 0, e->stream, a);
+        GfToy &ty = e->toys[t];
+        ty.amp_I.assign(NAN_, {});
+        ty.amp_H.assign(NAN_, {});
+        if(e->gram_tc) {
+            // tensor cores: the real Gram matrix G of each node's columns, then I and H from its blocks
+            for(int k = 0; k < NAN_ && r == cudaSuccess; ++k) {
+                const int n = T.amp_count(k), nc = ampColumns(T, k), m = 2 * nc;
+                const int64_t npts = ampPoints(e, k);
+                const float2 *sc   = reinterpret_cast<const float2 *>(e->nscr[k]);
+                const float *eff   = k < (int)T.amp3s.size() ? reinterpret_cast<const float *>(sc + (size_t)nc * npts) : nullptr;
+                int herr           = 0;
+                r = cudaMemsetAsync(e->d_gtc_err, 0, sizeof(int), e->stream);
+                if(r == cudaSuccess)
+                    r = gf_gram_tc_launch(sc, npts, nc, eff, std::max(1, e->sm_count), e->d_gtc_part, e->d_gtc_out,
+                                          e->d_gtc_err, e->stream);
+                if(r == cudaSuccess)
+                    r = cudaMemcpyAsync(e->h_gtc.data(), e->d_gtc_out, sizeof(double) * (size_t)m * m,
+                                        cudaMemcpyDeviceToHost, e->stream);
+                if(r == cudaSuccess)
+                    r = cudaMemcpyAsync(&herr, e->d_gtc_err, sizeof(int), cudaMemcpyDeviceToHost, e->stream);
+                if(r == cudaSuccess)
+                    r = cudaStreamSynchronize(e->stream);
+                if(r != cudaSuccess)
+                    break;
+                if(herr)
+                    return gf_fail(e, GF_ERR_CUDA, "tensor-core Gram kernel: a bounded wait ran out");
+                const double *G = e->h_gtc.data();
+                // X_a conj(X_b) summed: Re = G(re a, re b) + G(im a, im b), Im = G(im a, re b) - G(re a, im b)
+                auto ent = [&](int u, int v, double &re, double &im) {
+                    re = G[(size_t)(2 * u) * m + 2 * v] + G[(size_t)(2 * u + 1) * m + 2 * v + 1];
+                    im = G[(size_t)(2 * u + 1) * m + 2 * v] - G[(size_t)(2 * u) * m + 2 * v + 1];
+                };
+                std::vector<double> I(2 * (size_t)n * n, 0.0), H(2 * (size_t)std::max(1, nc - n) * n, 0.0);
+                for(int i = 0; i < n; ++i)
+                    for(int j = i; j < n; ++j) {
+                        double re, im;
+                        ent(i, j, re, im);
+                        if(i == j)
+                            im = 0.0;
+                        I[2 * (i * n + j)]     = re;
+                        I[2 * (i * n + j) + 1] = im;
+                        I[2 * (j * n + i)]     = re;
+                        I[2 * (j * n + i) + 1] = -im;
+                    }
+                for(int d = 0; d < nc - n; ++d)
+                    for(int b = 0; b < n; ++b)
+                        ent(n + d, b, H[2 * (d * n + b)], H[2 * (d * n + b) + 1]);
+                ty.amp_I[k] = I;
+                ty.amp_H[k] = H;
+            }
+            if(r != cudaSuccess)
+                break;
+            ty.amp_params = snap[t];
+            ty.amp_valid  = true;
+            continue;
+        }
         if(r == cudaSuccess)
             r = launch(e->mod.gram, dim3(e->gram_blocks, 1, NTILE), dim3(256), 0, e->stream, a);
         if(r == cudaSuccess)
@@ -789,9 +893,6 @@ int updateAmpCaches(gf_engine *e) {
             r = cudaStreamSynchronize(e->stream);
         if(r != cudaSuccess)
             break;
-        GfToy &ty = e->toys[t];
-        ty.amp_I.assign(NAN_, {});
-        ty.amp_H.assign(NAN_, {});
         for(int k = 0; k < NAN_; ++k) {
             const int n = T.amp_count(k);
             int nd      = 0;
@@ -846,6 +947,15 @@ int updateAmpCaches(gf_engine *e) {
 void postToy(gf_engine *e, int t, double *o) {
     const gf::Tree &T = e->tree;
     int st            = (int)o[1] | e->host_flag[t];
+    if(e->plan.factor_root && !(st & 3)) {
+        // -log(P N) summed: the kernels returned sum -log P (and -dP/P) and the count of events with P > 0
+        const double cnt = o[2 + T.NG], N = e->root_N[t];
+        o[0] += -cnt * std::log(N);
+        for(int s = 0; s < T.NG; ++s)
+            o[2 + s] += -cnt * e->root_dN[(size_t)t * std::max(1, T.NG) + s] / N;
+        if(o[0] == 0.0)
+            st |= 4;
+    }
     if(T.extended_root && !(st & 4)) {
         // the yields as the kernels saw them (rounded to R in GF_MIXED)
         const double *P = e->h_P + (size_t)t * T.n_params;
@@ -967,13 +1077,15 @@ int gf_engine_create(gf_engine **out, int device, int precision) {
     if(const char *g = std::getenv("GF_NO_GRAPH"))
         e->use_graph = !(g[0] == '1');
     if(const char *c = std::getenv("GF_CHUNK")) {
-        e->chunk       = std::max(2048, (atoi(c) / 2048) * 2048);
+        e->chunk       = std::max(256, (atoi(c) / 256) * 256);
         e->chunk_fixed = true;
     }
     if(const char *p = std::getenv("GF_NO_PDL"))
         e->use_pdl = !(p[0] == '1');
-    if(const char *c = std::getenv("GF_EVT_CTAS_PER_SM"))
-        e->evt_ctas_per_sm = std::max(1, atoi(c));
+    if(const char *c = std::getenv("GF_EVT_CTAS_PER_SM")) {
+        e->evt_ctas_per_sm   = std::max(1, atoi(c));
+        e->evt_ctas_fixed    = true;
+    }
     e->toys.assign(1, GfToy());
     *out = e;
     return GF_OK;
@@ -1042,7 +1154,18 @@ int gf_set_tree(gf_engine *e, const gf_node *nodes, int n_nodes, const gf_observ
     int rc = loadModule(e);
     if(rc)
         return rc;
-    e->has_tree = true;
+    if(!e->evt_ctas_fixed) {
+        // resident CTAs per SM of the gradient event kernel (the one a fit runs), for the chunk layout
+        int occ = 0;
+        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)e->mod.evt_g, e->block,
+                                                         e->plan.evt_smem_grad) != cudaSuccess) {
+            cudaGetLastError();
+            occ = 0;
+        }
+        e->evt_ctas_per_sm = std::min(8, std::max(1, occ));
+    }
+    e->layout_ready = false;
+    e->has_tree     = true;
     return GF_OK;
 }
 
@@ -1232,7 +1355,7 @@ static int evalOne(gf_engine *e, int toy, bool grad, double *nll, double *g) {
     if(rc)
         return rc;
     const int NGp = 1 + e->tree.NG;
-    double *o     = e->h_out + (size_t)toy * (NGp + 1);
+    double *o     = e->h_out + (size_t)toy * (NGp + 2);
     postToy(e, toy, o);
     if(nll)
         *nll = o[0];
@@ -1285,7 +1408,7 @@ int gf_nll_batch(gf_engine *e, int n_toys, const double *P, const int32_t *activ
     for(int t = 0; t < n_toys; ++t) {
         if(!e->h_active[t])
             continue;
-        double *o = e->h_out + (size_t)t * (NGp + 1);
+        double *o = e->h_out + (size_t)t * (NGp + 2);
         postToy(e, t, o);
         nll[t] = o[0];
         if(grad)

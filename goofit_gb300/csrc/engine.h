@@ -81,7 +81,8 @@ struct gf_engine {
     int block = 256;
     int chunk = 8192;
     bool chunk_fixed = false;
-    int evt_ctas_per_sm = 4;
+    int evt_ctas_per_sm = 4;      // resident event CTAs per SM: the gradient event kernel's occupancy
+    bool evt_ctas_fixed = false;
 
     int fit_metric = GF_FIT_UNBINNED_NLL;
     int n_toys = 1;
@@ -121,6 +122,13 @@ struct gf_engine {
     double **d_nevt = nullptr;
     long long *d_nnorm = nullptr;
     // normalisation-point columns per amplitude node (values, derivatives, efficiency) of one toy at a time
+    // tensor-core Gram (mixed precision): per-CTA FP64 partials, the summed real Gram matrix, a status word
+    bool gram_tc         = false;
+    double *d_gtc_part   = nullptr;
+    double *d_gtc_out    = nullptr;
+    int *d_gtc_err       = nullptr;
+    size_t gtc_part_n    = 0, gtc_out_n = 0;
+    std::vector<double> h_gtc;
     std::vector<void *> nscr;
     std::vector<size_t> nscr_bytes;
     void **d_nscr = nullptr;
@@ -131,6 +139,7 @@ struct gf_engine {
     size_t pblock_bytes = 0;
     size_t active_off   = 0; // byte offset of the active flags inside the parameter block
     std::vector<int> host_flag; // per toy: status bits from host-computed analytic factors
+    std::vector<double> root_N, root_dN; // per toy: the root's normalisation and its derivatives, FP64
     int *h_active = nullptr;
     double *h_out = nullptr;
 
@@ -145,5 +154,14 @@ struct gf_engine {
 
 // helpers shared between translation units
 int gf_fail(gf_engine *e, int code, const std::string &msg);
+
+// tensor-core Gram matrix of ncol complex FP32 columns (gram_tc.cu): real columns per slice (16, 32 or 64),
+// 0 when 2 ncol > 64
+int gf_gram_tc_width(int ncol);
+size_t gf_gram_tc_part_doubles(int ncol, int grid);
+// G (2 ncol x 2 ncol, FP64) = sum_p x_r(p) eff(p) x_s(p) of the columns sc[c * npts + p] into out; part holds
+// gf_gram_tc_part_doubles(ncol, sm_count) doubles; *err gets bit 0 when a bounded wait ran out
+cudaError_t gf_gram_tc_launch(const float2 *sc, long long npts, int ncol, const float *eff, int sm_count,
+                              double *part, double *out, int *err, cudaStream_t s);
 int gf_cuda_check(gf_engine *e, cudaError_t r, const char *what);
 int gf_run(gf_engine *e, bool grad, int metric_values_toy, int metric);

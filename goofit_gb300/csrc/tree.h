@@ -204,6 +204,9 @@ struct KernelPlan {
     std::vector<GramTile> gram_tiles;
     int gram_pairs_max = 0;                                 // most pairs in one tile
     std::vector<int64_t> dgrid_off;                         // per Amp3Body: offset of its bins in the bin list
+    // the root's normalisation is applied on the host: the event pass returns sum -log P, sum -dP/P and the
+    // count of events with P > 0 (out[2 + NG]); the host adds count * (-log N) and count * (-dN/N)
+    bool factor_root = false;
     NormLayout nl;
 };
 

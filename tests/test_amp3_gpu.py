@@ -178,3 +178,22 @@ def test_resonance_gradient_matches_central_differences(c3_events, prec):
     fd = O.fd_grad(nodes, olist, p, c3_events, free, h=1e-5)
     n = c3_events.shape[1]
     np.testing.assert_allclose(g, fd, rtol=2e-4 if prec == "mixed" else 1e-6, atol=2e-3 * math.sqrt(n))
+
+
+@pytest.mark.parametrize("bins", [300, 1500])
+def test_tensor_core_gram_matches_cuda_core_gram(c3_events, bins, monkeypatch):
+    """The mixed engine's integrals from the tcgen05 Gram kernel (split-TF32 products, FP32 accumulation
+    in tensor memory for 256 points per slice, FP64 beyond) against the CUDA-core kernel (FP32 products,
+    FP64 per-CTA sums): within 2e-6 of the largest diagonal entry; the matrix is exactly Hermitian."""
+    pdf, _, _ = W.c3_model(bins)
+    out = {}
+    for mode in ("tc", "cuda"):
+        if mode == "cuda":
+            monkeypatch.setenv("GF_GRAM", "cuda")
+        else:
+            monkeypatch.delenv("GF_GRAM", raising=False)
+        eng, *_ = engine(pdf, c3_events, "mixed")
+        out[mode] = eng.amp3_integrals(0, 8)
+    scale = np.abs(np.diag(out["cuda"])).max()
+    assert np.abs(out["tc"] - out["cuda"]).max() / scale < 2e-6
+    np.testing.assert_array_equal(out["tc"], out["tc"].conj().T)
