@@ -22,6 +22,7 @@
 #include "tree.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <functional>
 #include <map>
@@ -1174,12 +1175,20 @@ void emitCtaReduce(std::ostream &os, const std::vector<std::string> &vals, const
     os << ind << "__syncthreads();\n";
 }
 
+// convolution tables in the event pass: read through L1 (default) or staged in shared memory per CTA
+// (GF_CTAB=smem)
+bool ctabThroughL1() {
+    const char *v = std::getenv("GF_CTAB");
+    return !(v && std::string(v) == "smem");
+}
+
 struct Gen {
     const Tree &T;
     bool mixed;
     int block, chunk;
     KernelPlan &plan;
     std::ostringstream os;
+    const bool ctabL1 = ctabThroughL1();
 
     int convComps(int ci, bool grad) const { return 1 + (grad ? (int)T.convs[ci].dep.size() : 0); }
 
@@ -1211,7 +1220,12 @@ struct Gen {
         const int NC    = (int)T.convs.size();
         if(NC == 0)
             return;
-        const int MS = 8, KT = 8;
+        // m split across the 32 lanes of a warp when every table has at most 8 components (more CTAs of
+        // fewer k each: the tables are short and latency-bound), else across 8 lanes
+        int maxComps = 0;
+        for(int ci = 0; ci < NC; ++ci)
+            maxComps = std::max(maxComps, convComps(ci, grad));
+        const int MS = maxComps <= block / 32 ? 32 : 8, KT = 8;
         const int items = block / MS;
         auto &off       = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
         auto &cps       = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
@@ -1740,7 +1754,8 @@ struct Gen {
         }
         os << "  default: break;\n  }\n}\n\n";
 
-        // normalisation points of toy a.gtoy -> scratch columns [value | derivative][point], then the efficiency
+        // normalisation points of toy a.gtoy -> scratch columns [value | derivative][point], then the efficiency;
+        // columns are nst = npts rounded up to 4 points apart, so that every column starts on 32 bytes
         os << "extern \"C\" __global__ void __launch_bounds__(256) gf_ampn(const GfArgs a) {\n";
         os << "  const int toy = a.gtoy, k = blockIdx.z, tid = threadIdx.x;\n";
         os << "  const double *P = a.P + (i64)toy * " << np << "; (void)P;\n";
@@ -1764,8 +1779,8 @@ struct Gen {
                 double w13 = g13.hi - g13.lo;
                 w13 /= A.nb13q;
                 const int64_t npts = (int64_t)A.grid.size();
-                os << "    const i64 npts = " << npts << "LL;\n";
-                os << "    R *se = reinterpret_cast<R *>(sc + " << NC << " * npts);\n";
+                os << "    const i64 npts = " << npts << "LL, nst = (npts + 3) & ~3LL;\n";
+                os << "    R *se = reinterpret_cast<R *>(sc + " << NC << " * nst);\n";
                 os << "    const unsigned *pts = a.dgrid + " << goff << "LL;\n";
                 goff += npts;
                 os << "    for(i64 p = (i64)blockIdx.x * 256 + tid; p < npts; p += (i64)gridDim.x * 256) {\n";
@@ -1790,14 +1805,14 @@ struct Gen {
             } else {
                 const int k4 = k - n3;
                 os << "    const double *ne = a.nevt[" << k4 << "];\n";
-                os << "    const i64 npts = a.nnorm[" << k4 << "];\n";
+                os << "    const i64 npts = a.nnorm[" << k4 << "], nst = (npts + 3) & ~3LL;\n";
                 os << "    for(i64 p = (i64)blockIdx.x * 256 + tid; p < npts; p += (i64)gridDim.x * 256) {\n";
                 os << "      gf_ampv_" << k << "(ne[p], ne[npts + p], ne[2 * npts + p], ne[3 * npts + p], ne[4 * npts + p], P, A, dA);\n";
             }
             for(int q = 0; q < nAmp; ++q)
-                os << "      sc[" << q << " * npts + p] = A[" << q << "];\n";
+                os << "      sc[" << q << " * nst + p] = A[" << q << "];\n";
             for(int d = 0; d < nDeriv(k); ++d)
-                os << "      sc[" << nAmp + d << " * npts + p] = dA[" << d << "];\n";
+                os << "      sc[" << nAmp + d << " * nst + p] = dA[" << d << "];\n";
             os << "    }\n    break; }\n";
         }
         os << "  default: break;\n  }\n}\n\n";
@@ -1838,18 +1853,18 @@ struct Gen {
                 os << "    R sr" << q << " = R(0), si" << q << " = R(0);\n";
             os << "    const R2 *sc = reinterpret_cast<const R2 *>(a.nscr[" << k << "]);\n";
             if(k < n3)
-                os << "    const i64 npts = " << (int64_t)T.amp3s[k].grid.size() << "LL;\n"
-                   << "    const R *se = reinterpret_cast<const R *>(sc + " << NC << " * npts);\n";
+                os << "    const i64 npts = " << (int64_t)T.amp3s[k].grid.size() << "LL, nst = (npts + 3) & ~3LL;\n"
+                   << "    const R *se = reinterpret_cast<const R *>(sc + " << NC << " * nst);\n";
             else
-                os << "    const i64 npts = a.nnorm[" << k - n3 << "];\n";
+                os << "    const i64 npts = a.nnorm[" << k - n3 << "], nst = (npts + 3) & ~3LL;\n";
             os << "    for(i64 p = (i64)blockIdx.x * 256 + tid; p < npts; p += (i64)gridDim.x * 256) {\n";
             os << "      const R e = " << (k < n3 ? "se[p]" : "R(1)") << ";\n";
             for(int v = 0; v < nAmp; ++v)
                 if(needV[v])
-                    os << "      const R2 b" << v << " = sc[" << v << " * npts + p];\n";
+                    os << "      const R2 b" << v << " = sc[" << v << " * nst + p];\n";
             for(int d = 0; d < nDeriv(k); ++d)
                 if(needD[d])
-                    os << "      const R2 g" << d << " = sc[" << nAmp + d << " * npts + p];\n";
+                    os << "      const R2 g" << d << " = sc[" << nAmp + d << " * nst + p];\n";
             for(int q = 0; q < npr; ++q) {
                 const std::string x = es[q].h ? "g" + std::to_string(es[q].i) : "b" + std::to_string(es[q].i);
                 const std::string y = "b" + std::to_string(es[q].j);
@@ -1890,7 +1905,7 @@ struct Gen {
         auto &cps     = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
         const int64_t ctabTotal = grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd;
         if(!values)
-            (grad ? plan.evt_smem_grad : plan.evt_smem_nograd) = (size_t)ctabTotal * (mixed ? 4 : 8);
+            (grad ? plan.evt_smem_grad : plan.evt_smem_nograd) = ctabL1 ? 0 : (size_t)ctabTotal * (mixed ? 4 : 8);
 
         std::vector<int> xused(NO, 0);
         std::ostringstream body;
@@ -1974,7 +1989,11 @@ struct Gen {
         os << "    const i64 *cd = a.chunks + 3 * (i64)ch;\n";
         os << "    const int toy = (int)cd[0]; const i64 b0 = cd[1], e0 = cd[2];\n";
         os << "    if(a.active && !a.active[toy]) continue;\n";
-        if(NC > 0) {
+        if(NC > 0 && ctabL1) {
+            // the toy's tables are read through L1 (read-only loads): every CTA on an SM shares one copy
+            os << "    const R *ttab = reinterpret_cast<const R *>(a.ctab) + (i64)toy * " << ctabTotal << ";\n";
+        } else if(NC > 0) {
+            os << "    const R *ttab = stab;\n";
             os << "    if(toy != s_toy) {\n";
             os << "      __syncthreads();\n";
             if(mixed)
@@ -2062,17 +2081,19 @@ struct Gen {
             const ConvInfo &cv = T.convs[ci];
             int cp             = cps[ci];
             os << "        const int ek" << ci << " = ka" << ci << "[j];\n";
-            os << "        const R *tp" << ci << " = stab + " << off[ci] << " + (ek" << ci << " - " << cv.kmin << ") * "
+            os << "        const R *tp" << ci << " = ttab + " << off[ci] << " + (ek" << ci << " - " << cv.kmin << ") * "
                << cp << "; (void)tp" << ci << ";\n";
             if(mixed) {
+                const char *ld = ctabL1 ? "__ldg(" : "*(";
                 if(cp == 1)
-                    os << "        const float tq" << ci << " = tp" << ci << "[0];\n";
+                    os << "        const float tq" << ci << " = " << ld << "tp" << ci << ");\n";
                 else if(cp == 2)
-                    os << "        const float2 tq" << ci << " = *reinterpret_cast<const float2 *>(tp" << ci << ");\n";
+                    os << "        const float2 tq" << ci << " = " << ld << "reinterpret_cast<const float2 *>(tp" << ci
+                       << "));\n";
                 else
                     for(int g4 = 0; g4 < cp / 4; ++g4)
-                        os << "        const float4 tq" << ci << "_" << g4 << " = *reinterpret_cast<const float4 *>(tp"
-                           << ci << " + " << 4 * g4 << ");\n";
+                        os << "        const float4 tq" << ci << "_" << g4 << " = " << ld
+                           << "reinterpret_cast<const float4 *>(tp" << ci << " + " << 4 * g4 << "));\n";
             }
         }
         os << "        {\n" << body.str();

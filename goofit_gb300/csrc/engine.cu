@@ -725,6 +725,9 @@ int64_t ampPoints(const gf_engine *e, int k) {
     return k4 < (int)e->norm_n.size() ? e->norm_n[k4] : 0;
 }
 
+// column stride of the scratch columns: the points rounded up to a multiple of 4
+int64_t ampStride(const gf_engine *e, int k) { return (std::max<int64_t>(1, ampPoints(e, k)) + 3) / 4 * 4; }
+
 // Scratch columns of the normalisation pass: per amplitude node, (values + derivatives) R2 columns and an R
 // efficiency column over its points.
 int ensureScratch(gf_engine *e) {
@@ -746,7 +749,7 @@ int ensureScratch(gf_engine *e) {
         int nd = 0;
         for(auto &th : T.amp_theta(k))
             nd += (int)th.amps.size();
-        const size_t bytes = (size_t)std::max<int64_t>(1, ampPoints(e, k)) * ((T.amp_count(k) + nd) * 2 * rs + rs) + 256;
+        const size_t bytes = (size_t)ampStride(e, k) * ((T.amp_count(k) + nd) * 2 * rs + rs) + 256;
         if(bytes == e->nscr_bytes[k])
             continue;
         if(e->nscr[k])
@@ -836,14 +839,14 @@ int updateAmpCaches(gf_engine *e) {
             // tensor cores: the real Gram matrix G of each node's columns, then I and H from its blocks
             for(int k = 0; k < NAN_ && r == cudaSuccess; ++k) {
                 const int n = T.amp_count(k), nc = ampColumns(T, k), m = 2 * nc;
-                const int64_t npts = ampPoints(e, k);
+                const int64_t npts = ampPoints(e, k), nst = ampStride(e, k);
                 const float2 *sc   = reinterpret_cast<const float2 *>(e->nscr[k]);
-                const float *eff   = k < (int)T.amp3s.size() ? reinterpret_cast<const float *>(sc + (size_t)nc * npts) : nullptr;
+                const float *eff   = k < (int)T.amp3s.size() ? reinterpret_cast<const float *>(sc + (size_t)nc * nst) : nullptr;
                 int herr           = 0;
                 r = cudaMemsetAsync(e->d_gtc_err, 0, sizeof(int), e->stream);
                 if(r == cudaSuccess)
-                    r = gf_gram_tc_launch(sc, npts, nc, eff, std::max(1, e->sm_count), e->d_gtc_part, e->d_gtc_out,
-                                          e->d_gtc_err, e->stream);
+                    r = gf_gram_tc_launch(sc, npts, nst, nc, eff, std::max(1, e->sm_count), e->d_gtc_part,
+                                          e->d_gtc_out, e->d_gtc_err, e->stream);
                 if(r == cudaSuccess)
                     r = cudaMemcpyAsync(e->h_gtc.data(), e->d_gtc_out, sizeof(double) * (size_t)m * m,
                                         cudaMemcpyDeviceToHost, e->stream);

@@ -159,9 +159,10 @@ int gf_fail(gf_engine *e, int code, const std::string &msg);
 // 0 when 2 ncol > 64
 int gf_gram_tc_width(int ncol);
 size_t gf_gram_tc_part_doubles(int ncol, int grid);
-// G (2 ncol x 2 ncol, FP64) = sum_p x_r(p) eff(p) x_s(p) of the columns sc[c * npts + p] into out; part holds
-// gf_gram_tc_part_doubles(ncol, sm_count) doubles; *err gets bit 0 when a bounded wait ran out
-cudaError_t gf_gram_tc_launch(const float2 *sc, long long npts, int ncol, const float *eff, int sm_count,
-                              double *part, double *out, int *err, cudaStream_t s);
+// G (2 ncol x 2 ncol, FP64) = sum_{p < npts} x_r(p) eff(p) x_s(p) of the columns sc[c * nst + p] (nst a
+// multiple of 4, sc and eff 16-byte aligned) into out; part holds gf_gram_tc_part_doubles(ncol, sm_count)
+// doubles; *err gets bit 0 when a bounded wait ran out
+cudaError_t gf_gram_tc_launch(const float2 *sc, long long npts, long long nst, int ncol, const float *eff,
+                              int sm_count, double *part, double *out, int *err, cudaStream_t s);
 int gf_cuda_check(gf_engine *e, cudaError_t r, const char *what);
 int gf_run(gf_engine *e, bool grad, int metric_values_toy, int metric);

@@ -34,7 +34,7 @@
 
 namespace {
 
-constexpr int kThreads = 128; // four warps; warp w reads tensor-memory lanes 32w .. 32w + 31 (D rows)
+constexpr int kThreads = 256; // eight warps; warps 0-3 read tensor-memory lanes 32w .. 32w + 31 (D rows)
 constexpr int kRows    = 128; // MMA M = N = 128 rows: S slices x W real columns
 constexpr int kKS      = 32;  // points of one slice per stage: four MMA K-steps of 8 (kind::tf32)
 constexpr int kOpBytes = kRows * kKS * 4;   // one operand split of one stage: 16 KB
@@ -45,8 +45,10 @@ constexpr uint32_t kColSmall = 256;         // hi.hi products (one per stage par
 constexpr uint32_t kTmemCols = 512;         // allocation (a power of two): one CTA per SM
 constexpr int kOperandBytes  = 2 * 4 * kOpBytes;  // two stages of A_hi, A_lo, B_hi, B_lo: 128 KB
 constexpr int kRawSlots      = 3;                 // raw stages: two in flight while one is transformed
-constexpr int kRawUnits      = 64;                // (slice, column group, 8 points) units per stage, at most
-constexpr int kSmemBytes     = kOperandBytes + kRawSlots * kRawUnits * 32 * 12; // + float2 and efficiency
+constexpr int kRawRow        = kKS * 8 + 16;      // one (slice, column) row of a raw stage: 32 float2 + pad
+constexpr int kRawCplx       = 64 * kRawRow;      // at most S x C = 64 rows
+constexpr int kRawSlot       = kRawCplx + 8 * kKS * 4; // + the efficiency of S <= 8 slices
+constexpr int kSmemBytes     = kOperandBytes + kRawSlots * kRawSlot;
 constexpr unsigned long long kWaitNs = 2000000000ull; // 2 s: an mbarrier wait that takes longer fails
 
 // Instruction descriptor of tcgen05.mma kind::tf32: D F32 (bits 4-5 = 1), A and B TF32 (bits 7-9 and
@@ -75,11 +77,9 @@ __device__ __forceinline__ uint32_t op_off(int r, int k) {
     return (uint32_t)(r >> 3) * kSBO + (uint32_t)(k >> 2) * kLBO + (uint32_t)(r & 7) * 16u + (uint32_t)(k & 3) * 4u;
 }
 
-__device__ __forceinline__ float tf32_rna(float x) {
-    uint32_t y;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(y) : "f"(x));
-    return __uint_as_float(y);
-}
+// x rounded to TF32 (11 significant bits, ties away from zero) by integer operations; x - tf32_hi(x) is
+// exact in FP32 and at most half a TF32 unit, and the tensor core reads it truncated to TF32 (~22 bits in all)
+__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u); }
 
 __device__ __forceinline__ unsigned long long globaltimer() {
     unsigned long long t;
@@ -122,11 +122,8 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
 }
 
 // asynchronous global -> shared copies (cp.async); a source size of 0 writes zeros
-__device__ __forceinline__ void cp_async8(uint32_t dst, const void *src, uint32_t src_bytes) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
-}
-__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src, uint32_t src_bytes) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, uint32_t src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
@@ -160,12 +157,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
         v[i] = __uint_as_float(r[i]);
 }
 
-// W real columns per slice (2C <= W), S = 128 / W slices.  weighted: an efficiency column multiplies B.
+// W real columns per slice (2C <= W), S = 128 / W slices.  eff != nullptr: the efficiency multiplies B.
+// Columns sc[c * nst + p], nst a multiple of 4; sc and eff 16-byte aligned.
 template <int W>
 __global__ void __launch_bounds__(kThreads, 1)
-    gf_gram_tc(const float2 *__restrict__ sc, long long npts, int ncol, const float *__restrict__ eff,
+    gf_gram_tc(const float2 *__restrict__ sc, long long npts, long long nst, int ncol, const float *__restrict__ eff,
                long long per_cta, double *__restrict__ part, int *__restrict__ err) {
-    constexpr int S = kRows / W;
+    constexpr int S  = kRows / W;
+    constexpr int KC = kKS / 4; // 16-byte chunks of 4 points per row and stage
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) unsigned long long mbar[2];
     __shared__ uint32_t tmem_slot;
@@ -177,9 +176,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     const long long b0  = (long long)blockIdx.x * per_cta;
     const long long L   = per_cta / S;      // points per slice
     const int T         = (int)(L / kKS);   // stages
-    const int twoC      = 2 * ncol;
 
-    // zero both stages once: rows beyond 2C of every slice stay zero
+    // zero both operand stages once: rows beyond 2C of every slice stay zero
     for(int i = tid; i < kOperandBytes / 16; i += kThreads)
         reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
     if(tid == 0) {
@@ -200,21 +198,19 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
 
-    // this thread's D row and the slice block it reads back
-    const int row = 32 * warp + lane, slice = row / W;
-    float acc_h[W], acc_l[W]; // compensated FP32 sums of the drained stage blocks
+    // warps 0-3: this thread's D row and its slice; compensated FP32 sums of the drained stage blocks
+    const int row = 32 * (warp & 3) + lane, slice = row / W;
+    float acc_h[W], acc_l[W];
 #pragma unroll
     for(int j = 0; j < W; ++j)
         acc_h[j] = acc_l[j] = 0.f;
+    const uint32_t lanebase = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+    int issued_last         = -1; // last stage whose MMAs were committed
 
-    const int CG    = (ncol + 3) / 4;        // column groups of 4 complex columns
-    const int units = S * CG * (kKS / 8);    // (slice, column group, 8-point group) units per stage
-    const int cq = lane >> 3, kq = lane & 7; // lane -> (column in group, point in group)
-    const uint32_t lanebase = tmem + ((uint32_t)(32 * warp) << 16);
-    int issued_last = -1;                    // last stage whose MMAs were committed
-
-    // adds the W x W block of this thread's slice from tensor-memory columns col0 .. col0 + 127
+    // adds the W x W block of this thread's slice from tensor-memory columns col0 .. col0 + 127 (warps 0-3)
     auto drain = [&](uint32_t col0) {
+        if(warp >= 4)
+            return;
         float v[16];
         if(W == 16) {
             // warp w holds slices 2w (lanes 0-15) and 2w + 1 (lanes 16-31)
@@ -240,25 +236,29 @@ __global__ void __launch_bounds__(kThreads, 1)
         return !__syncthreads_or(!ok);
     };
 
-    // raw stage ring after the operand stages: per unit and lane one float2 (and one efficiency value);
-    // every thread copies, waits for and reads only its own elements, so no barrier guards the ring
-    float2 *raw2 = reinterpret_cast<float2 *>(smem + kOperandBytes);
-    float *rawe  = reinterpret_cast<float *>(smem + kOperandBytes + (size_t)kRawSlots * kRawUnits * 32 * 8);
+    // raw stage ring after the operand stages: per (slice, column) a row of 32 points (float2), padded so
+    // that rows of consecutive columns fall in different banks, then the efficiency of each slice
+    unsigned char *rawbase = smem + kOperandBytes;
+    const int nrow         = S * ncol;
     auto copy_stage = [&](int t) {
-        const int slot = t % kRawSlots;
-        for(int u = warp; u < units; u += kThreads / 32) {
-            const int kg = u % (kKS / 8), rest = u / (kKS / 8);
-            const int cg = rest % CG, s = rest / CG;
-            const int c = cg * 4 + cq, k = kg * 8 + kq;
-            const long long p = b0 + (long long)s * L + (long long)t * kKS + k;
-            const bool ok     = c < ncol && p < npts;
-            const size_t q    = ((size_t)slot * kRawUnits + u) * 32 + lane;
-            // out of range: zero-filled (source size 0; the source address is only a valid placeholder)
-            cp_async8(smem_u32(raw2 + q), ok ? (const void *)(sc + (long long)c * npts + p) : (const void *)sc,
-                      ok ? 8u : 0u);
-            if(weighted)
-                cp_async4(smem_u32(rawe + q), ok ? (const void *)(eff + p) : (const void *)eff, ok ? 4u : 0u);
+        unsigned char *slot = rawbase + (size_t)(t % kRawSlots) * kRawSlot;
+        // 16-byte copies of 2 points; consecutive threads take consecutive chunks of one column
+        for(int j = tid; j < nrow * (kKS / 2); j += kThreads) {
+            const int rr = j / (kKS / 2), h = j % (kKS / 2);
+            const int s = rr / ncol, c = rr % ncol;
+            const long long p = b0 + (long long)s * L + (long long)t * kKS + 2 * h;
+            const long long n = p < npts ? (npts - p < 2 ? npts - p : 2) : 0;
+            cp_async16(smem_u32(slot + rr * kRawRow + h * 16), n > 0 ? (const void *)(sc + (long long)c * nst + p) : (const void *)sc,
+                       (uint32_t)(8 * n));
         }
+        if(weighted)
+            for(int j = tid; j < S * KC; j += kThreads) {
+                const int s = j / KC, h = j % KC;
+                const long long p = b0 + (long long)s * L + (long long)t * kKS + 4 * h;
+                const long long n = p < npts ? (npts - p < 4 ? npts - p : 4) : 0;
+                cp_async16(smem_u32(slot + kRawCplx + (s * kKS + 4 * h) * 4), n > 0 ? (const void *)(eff + p) : (const void *)eff,
+                           (uint32_t)(4 * n));
+            }
         cp_async_commit();
     };
     for(int t = 0; t < kRawSlots - 1; ++t) {
@@ -269,42 +269,42 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 
     for(int t = 0; t < T; ++t) {
-        const int buf      = t & 1;
-        unsigned char *st  = smem + (size_t)buf * nops * kOpBytes;
-        // keep kRawSlots - 1 stages of loads in flight; stage t's copies are complete after the wait
+        const int buf     = t & 1;
+        unsigned char *st = smem + (size_t)buf * nops * kOpBytes;
+        // keep kRawSlots - 1 stages of loads in flight (the slot written now was last read in stage t - 1,
+        // before that stage's barrier); after the wait and the barrier stage t's raw data is complete
         if(t + kRawSlots - 1 < T)
             copy_stage(t + kRawSlots - 1);
         else
             cp_async_commit();
         cp_async_wait<kRawSlots - 1>();
-        // the MMAs of stage t - 2 have read this buffer (waited for already by the drain of stage t - 1)
+        // the MMAs of stage t - 2 have read this operand buffer (waited for already by the drain of t - 1)
         if(t >= 2 && !mbar_wait(smem_u32(&mbar[buf]), (uint32_t)(((t - 2) >> 1) & 1)))
             s_fail = 1;
-        const int slot = t % kRawSlots;
-        for(int u = warp; u < units; u += kThreads / 32) {
-            const int kg = u % (kKS / 8), rest = u / (kKS / 8);
-            const int cg = rest % CG, s = rest / CG;
-            const int c = cg * 4 + cq, k = kg * 8 + kq;
-            if(c < ncol) {
-                const size_t q = ((size_t)slot * kRawUnits + u) * 32 + lane;
-                const float2 v = raw2[q];
-                const int rx   = s * W + 2 * c;
-                const float xh = tf32_rna(v.x), yh = tf32_rna(v.y);
-                const float xl = tf32_rna(v.x - xh), yl = tf32_rna(v.y - yh);
-                const uint32_t ox = op_off(rx, k), oy = op_off(rx + 1, k);
-                *reinterpret_cast<float *>(st + ox)            = xh;
-                *reinterpret_cast<float *>(st + oy)            = yh;
-                *reinterpret_cast<float *>(st + kOpBytes + ox) = xl;
-                *reinterpret_cast<float *>(st + kOpBytes + oy) = yl;
-                if(weighted) {
-                    const float e  = rawe[q];
-                    const float bx = v.x * e, by = v.y * e;
-                    const float bxh = tf32_rna(bx), byh = tf32_rna(by);
-                    *reinterpret_cast<float *>(st + 2 * kOpBytes + ox) = bxh;
-                    *reinterpret_cast<float *>(st + 2 * kOpBytes + oy) = byh;
-                    *reinterpret_cast<float *>(st + 3 * kOpBytes + ox) = tf32_rna(bx - bxh);
-                    *reinterpret_cast<float *>(st + 3 * kOpBytes + oy) = tf32_rna(by - byh);
-                }
+        __syncthreads();
+        // one task = one real row x 4 points: 8 consecutive lanes write the 8 rows of one core matrix
+        const unsigned char *slot = rawbase + (size_t)(t % kRawSlots) * kRawSlot;
+        for(int u = warp; u < 2 * (kRows / 8); u += kThreads / 32) {
+            const int r = 8 * (u >> 1) + (lane & 7), kc = 4 * (u & 1) + (lane >> 3);
+            const int s = r / W, i = r % W, c = i >> 1;
+            if(c >= ncol)
+                continue;
+            const float4 *src = reinterpret_cast<const float4 *>(slot + (s * ncol + c) * kRawRow + kc * 32);
+            const float4 q0 = src[0], q1 = src[1]; // (x0, y0, x1, y1), (x2, y2, x3, y3)
+            const float4 v  = (i & 1) ? make_float4(q0.y, q0.w, q1.y, q1.w) : make_float4(q0.x, q0.z, q1.x, q1.z);
+            float4 h, l;
+            h.x = tf32_hi(v.x); h.y = tf32_hi(v.y); h.z = tf32_hi(v.z); h.w = tf32_hi(v.w);
+            l.x = v.x - h.x; l.y = v.y - h.y; l.z = v.z - h.z; l.w = v.w - h.w;
+            const uint32_t o = op_off(r, 4 * kc);
+            *reinterpret_cast<float4 *>(st + o)            = h;
+            *reinterpret_cast<float4 *>(st + kOpBytes + o) = l;
+            if(weighted) {
+                const float4 e = *reinterpret_cast<const float4 *>(slot + kRawCplx + (s * kKS + 4 * kc) * 4);
+                const float4 b = make_float4(v.x * e.x, v.y * e.y, v.z * e.z, v.w * e.w);
+                h.x = tf32_hi(b.x); h.y = tf32_hi(b.y); h.z = tf32_hi(b.z); h.w = tf32_hi(b.w);
+                l.x = b.x - h.x; l.y = b.y - h.y; l.z = b.z - h.z; l.w = b.w - h.w;
+                *reinterpret_cast<float4 *>(st + 2 * kOpBytes + o) = h;
+                *reinterpret_cast<float4 *>(st + 3 * kOpBytes + o) = l;
             }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -345,6 +345,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc_fence_before();
         }
     }
+    cp_async_wait<0>();
     __syncthreads();
     if(!s_fail && T > 0) {
         if(stage_done(T - 1)) {
@@ -371,15 +372,18 @@ __global__ void __launch_bounds__(kThreads, 1)
     if(failed)
         return;
 
-    // sum the S slices' blocks in shared memory (the stage buffers are free now), FP64
+    // sum the S slices' blocks in shared memory (the operand stages are free now), FP64
     double *red = reinterpret_cast<double *>(smem);
+    if(warp < 4) {
 #pragma unroll
-    for(int j = 0; j < W; ++j)
-        red[(size_t)row * W + j] = (double)acc_h[j] + (double)acc_l[j];
+        for(int j = 0; j < W; ++j)
+            red[(size_t)row * W + j] = (double)acc_h[j] + (double)acc_l[j];
+    }
     __syncthreads();
-    double *out = part + (long long)blockIdx.x * twoC * twoC;
-    for(int q = tid; q < twoC * twoC; q += kThreads) {
-        const int i = q / twoC, j = q % twoC;
+    const int m = 2 * ncol;
+    double *out = part + (long long)blockIdx.x * m * m;
+    for(int q = tid; q < m * m; q += kThreads) {
+        const int i = q / m, j = q % m;
         double s = 0.0;
         for(int sl = 0; sl < S; ++sl)
             s += red[(size_t)(sl * W + i) * W + j];
@@ -406,19 +410,17 @@ __global__ void __launch_bounds__(128) gf_gram_tc_sum(const double *__restrict__
 }
 
 template <int W>
-cudaError_t launchW(const float2 *sc, long long npts, int ncol, const float *eff, int grid, long long per_cta,
-                    double *part, int *err, cudaStream_t s) {
-    // both variants request the full size: one CTA per SM, so the 512-column allocation never waits
-    const size_t smem = (size_t)kSmemBytes;
-    static bool attr  = false;
+cudaError_t launchW(const float2 *sc, long long npts, long long nst, int ncol, const float *eff, int grid,
+                    long long per_cta, double *part, int *err, cudaStream_t s) {
+    static bool attr = false;
     if(!attr) {
-        cudaError_t r = cudaFuncSetAttribute(gf_gram_tc<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             kSmemBytes);
+        cudaError_t r = cudaFuncSetAttribute(gf_gram_tc<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
         if(r != cudaSuccess)
             return r;
         attr = true;
     }
-    gf_gram_tc<W><<<grid, kThreads, smem, s>>>(sc, npts, ncol, eff, per_cta, part, err);
+    // every launch requests the full size: one CTA per SM, so the 512-column allocation never waits
+    gf_gram_tc<W><<<grid, kThreads, kSmemBytes, s>>>(sc, npts, nst, ncol, eff, per_cta, part, err);
     return cudaGetLastError();
 }
 
@@ -431,20 +433,21 @@ int gf_gram_tc_width(int ncol) {
 
 size_t gf_gram_tc_part_doubles(int ncol, int grid) { return (size_t)grid * 4 * ncol * ncol; }
 
-cudaError_t gf_gram_tc_launch(const float2 *sc, long long npts, int ncol, const float *eff, int sm_count,
-                              double *part, double *out, int *err, cudaStream_t s) {
+cudaError_t gf_gram_tc_launch(const float2 *sc, long long npts, long long nst, int ncol, const float *eff,
+                              int sm_count, double *part, double *out, int *err, cudaStream_t s) {
     const int W = gf_gram_tc_width(ncol);
-    if(W == 0 || npts <= 0)
+    if(W == 0 || ncol < 1 || npts <= 0 || nst < npts || nst % 4 != 0 || ((uintptr_t)sc & 15) != 0 ||
+       (eff && ((uintptr_t)eff & 15) != 0))
         return cudaErrorInvalidValue;
     const long long unit = (long long)(kRows / W) * kKS; // points per stage
     long long per_cta    = (npts + sm_count - 1) / sm_count;
     per_cta              = (per_cta + unit - 1) / unit * unit;
     const int grid       = (int)((npts + per_cta - 1) / per_cta);
-    // red[] at the end needs 128 x W doubles of the stage buffers
-    static_assert((size_t)kRows * 64 * 8 <= (size_t)2 * 2 * kOpBytes, "slice reduction does not fit");
-    cudaError_t r = W == 16   ? launchW<16>(sc, npts, ncol, eff, grid, per_cta, part, err, s)
-                    : W == 32 ? launchW<32>(sc, npts, ncol, eff, grid, per_cta, part, err, s)
-                              : launchW<64>(sc, npts, ncol, eff, grid, per_cta, part, err, s);
+    static_assert((size_t)kRows * 64 * 8 <= (size_t)kOperandBytes, "slice reduction does not fit");
+    static_assert(kSmemBytes <= 227 * 1024, "shared memory");
+    cudaError_t r = W == 16   ? launchW<16>(sc, npts, nst, ncol, eff, grid, per_cta, part, err, s)
+                    : W == 32 ? launchW<32>(sc, npts, nst, ncol, eff, grid, per_cta, part, err, s)
+                              : launchW<64>(sc, npts, nst, ncol, eff, grid, per_cta, part, err, s);
     if(r != cudaSuccess)
         return r;
     const int nent = 4 * ncol * ncol;

@@ -190,7 +190,7 @@ struct KernelPlan {
     size_t conv_smem_grad = 0, conv_smem_nograd = 0;
     int conv_tk = 64;      // table entries per conv CTA
     int conv_blocks = 0;   // CTAs per (toy, conv) of the table kernel
-    int grid_bins_per_block = 1024;
+    int grid_bins_per_block = 256;
     std::vector<int> grid_blocks; // per numeric node
     int max_grid_blocks = 0;
     int64_t ctab_per_toy_grad = 0, ctab_per_toy_nograd = 0; // table elements per toy

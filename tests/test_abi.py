@@ -126,4 +126,4 @@ def test_amp3body_tree_checks():
     inside = sum(O.in_dalitz(3.0 / 60 * (a + 0.5), 3.0 / 60 * (b + 0.5), W.C3_M, W.C3_MK, W.C3_MPI, W.C3_MPI0)
                  for a in range(60) for b in range(60))
     assert 0 < inside < 3600
-    assert f"const i64 npts = {inside}LL;" in src
+    assert f"const i64 npts = {inside}LL," in src
