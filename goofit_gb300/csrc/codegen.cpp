@@ -499,7 +499,24 @@ struct GfArgs {
     int n_toys;
     int metric;
     int gtoy;                  /* toy of the normalisation pass */
+    i64 chunk;                 /* events per chunk */
+    i64 nevt0;                 /* events of toy 0 */
+    const void *p0[192];       /* one toy: its observable, bin-offset and amplitude columns, no table lookup */
 };
+
+// chunk ch of the event list: with one toy its bounds follow from the chunk size, else from the table
+__device__ __forceinline__ void gf_chunk(const GfArgs &a, int ch, int &toy, i64 &b0, i64 &e0) {
+    if(a.n_toys == 1) {
+        toy = 0;
+        b0  = (i64)ch * a.chunk;
+        e0  = b0 + a.chunk < a.nevt0 ? b0 + a.chunk : a.nevt0;
+    } else {
+        const i64 *cd = a.chunks + 3 * (i64)ch;
+        toy = (int)cd[0];
+        b0  = cd[1];
+        e0  = cd[2];
+    }
+}
 
 __device__ __forceinline__ double gf_warp_sum(double v) {
 #pragma unroll
@@ -1189,6 +1206,12 @@ struct Gen {
     KernelPlan &plan;
     std::ostringstream os;
     const bool ctabL1 = ctabThroughL1();
+
+    // per-toy column pointer i of table `tab` (n per toy); one toy: from the kernel arguments at p0[off + i]
+    static std::string p0ptr(const char *tab, int n, int i, int off) {
+        return "(a.n_toys == 1 ? a.p0[" + std::to_string(off + i) + "] : (const void *)" + tab + "[(i64)toy * " +
+               std::to_string(n) + " + " + std::to_string(i) + "])";
+    }
 
     int convComps(int ci, bool grad) const { return 1 + (grad ? (int)T.convs[ci].dep.size() : 0); }
 
@@ -1967,28 +1990,27 @@ struct Gen {
         os << "  gf_pdl_trigger();\n";
         // event columns do not depend on the preceding kernels: pull the first chunk towards L2 meanwhile
         os << "  if(cb < ce) {\n";
-        os << "    const i64 *cd = a.chunks + 3 * (i64)cb;\n";
-        os << "    const int toy = (int)cd[0]; const i64 b0 = cd[1], e0 = cd[2];\n";
-        os << "    if(!a.active || a.active[toy]) {\n";
+        os << "    int toy; i64 b0, e0; gf_chunk(a, cb, toy, b0, e0);\n";
+        os << "    {\n";
         os << "      for(i64 i0 = b0 + " << VEC << " * (i64)tid; i0 < e0; i0 += " << VEC << " * " << block << ") {\n";
         for(int o = 0; o < NO; ++o)
             if(xused[o])
-                os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(reinterpret_cast<const R *>(a.col[(i64)toy * "
-                   << NO << " + " << o << "]) + i0));\n";
+                os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(reinterpret_cast<const R *>("
+                   << p0ptr("a.col", NO, o, 0) << ") + i0));\n";
         for(int ci = 0; ci < NC; ++ci)
-            os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(a.kcol[(i64)toy * " << NC << " + " << ci
-               << "] + i0));\n";
+            os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(reinterpret_cast<const int *>("
+               << p0ptr("a.kcol", NC, ci, NO) << ") + i0));\n";
         for(int ac = 0; ac < NA; ++ac)
             if(aused[ac])
-                os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(reinterpret_cast<const R2 *>(a.acol[(i64)toy * "
-                   << NA << " + " << ac << "]) + i0));\n";
+                os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(reinterpret_cast<const R2 *>("
+                   << p0ptr("a.acol", NA, ac, NO + NC) << ") + i0));\n";
         os << "      }\n    }\n  }\n";
         os << "  gf_pdl_wait();\n";
         os << "  __syncthreads();\n";
         os << "  for(int ch = cb; ch < ce; ++ch) {\n";
-        os << "    const i64 *cd = a.chunks + 3 * (i64)ch;\n";
-        os << "    const int toy = (int)cd[0]; const i64 b0 = cd[1], e0 = cd[2];\n";
-        os << "    if(a.active && !a.active[toy]) continue;\n";
+        os << "    int toy; i64 b0, e0; gf_chunk(a, ch, toy, b0, e0);\n";
+        // the activity flag is read beside the parameters (independent loads), the branch comes after them
+        os << "    const bool toy_on = !a.active || a.active[toy];\n";
         if(NC > 0 && ctabL1) {
             // the toy's tables are read through L1 (read-only loads): every CTA on an SM shares one copy
             os << "    const R *ttab = reinterpret_cast<const R *>(a.ctab) + (i64)toy * " << ctabTotal << ";\n";
@@ -2016,14 +2038,14 @@ struct Gen {
             os << "    const R Tn = (R)a.toy_nevents[toy]; // c_totalEvents: the number of bins\n";
         for(int o = 0; o < NO; ++o)
             if(xused[o])
-                os << "    const R *col" << o << " = reinterpret_cast<const R *>(a.col[(i64)toy * " << NO << " + " << o
-                   << "]);\n";
+                os << "    const R *col" << o << " = reinterpret_cast<const R *>(" << p0ptr("a.col", NO, o, 0) << ");\n";
         for(int ci = 0; ci < NC; ++ci)
-            os << "    const int *kc" << ci << " = a.kcol[(i64)toy * " << NC << " + " << ci << "];\n";
+            os << "    const int *kc" << ci << " = reinterpret_cast<const int *>(" << p0ptr("a.kcol", NC, ci, NO) << ");\n";
         for(int ac = 0; ac < NA; ++ac)
             if(aused[ac])
-                os << "    const R2 *acp" << ac << " = reinterpret_cast<const R2 *>(a.acol[(i64)toy * " << NA << " + " << ac
-                   << "]);\n";
+                os << "    const R2 *acp" << ac << " = reinterpret_cast<const R2 *>(" << p0ptr("a.acol", NA, ac, NO + NC)
+                   << ");\n";
+        os << "    if(!toy_on) continue;\n";
         if(!values) {
             os << "    R av = R(0), nv = R(0); (void)nv;\n";
             for(int s = 0; s < NGp - 1; ++s)
@@ -2228,13 +2250,13 @@ struct Gen {
            << "; ++w) t = acc_add(t, red[w][tid]); part[(i64)tid * a.n_chunks + ch] = t; }\n";
         os << "    __threadfence();\n    __syncthreads();\n";
         os << "    if(tid == 0) { unsigned prev = atomicAdd(&a.counter[toy], 1u); last = (prev == "
-              "(unsigned)(a.toy_nchunks[toy] - 1)); }\n";
+              "(unsigned)((a.n_toys == 1 ? a.n_chunks : a.toy_nchunks[toy]) - 1)); }\n";
         os << "    __syncthreads();\n";
         // finishing CTA of the toy: one warp per component sums that component's chunk partials (contiguous,
         // independent loads) and reduces them across its lanes
         os << "    if(last) {\n";
         os << "      __threadfence();\n";
-        os << "      const int c0 = a.toy_chunk0[toy], nc = a.toy_nchunks[toy];\n";
+        os << "      const int c0 = a.n_toys == 1 ? 0 : a.toy_chunk0[toy], nc = a.n_toys == 1 ? a.n_chunks : a.toy_nchunks[toy];\n";
         os << "      double *o = a.out + (i64)toy * " << OS << ";\n";
         os << "      for(int comp = wid; comp < " << NGc << "; comp += " << NW << ") {\n";
         os << "        const ACC *pc = part + (i64)comp * a.n_chunks + c0;\n";

@@ -396,6 +396,20 @@ GfArgs makeArgs(gf_engine *e) {
     a.nnorm       = e->d_nnorm;
     a.nscr        = (void *const *)e->d_nscr;
     a.gtoy        = 0;
+    a.chunk       = e->chunk;
+    a.nevt0       = e->toys.empty() ? 0 : e->toys[0].n;
+    if(!e->toys.empty()) {
+        // toy 0's column pointers by value: the kernels of a single fit read no pointer table
+        const gf::Tree &T = e->tree;
+        const int NO = (int)T.obs.size(), NC = (int)T.convs.size(), NA = T.n_amp_cols;
+        const GfToy &t0 = e->toys[0];
+        for(int o = 0; o < NO && o < 192; ++o)
+            a.p0[o] = t0.cols[o];
+        for(int c = 0; c < NC && NO + c < 192; ++c)
+            a.p0[NO + c] = t0.kcols[c];
+        for(int c = 0; c < NA && NO + NC + c < 192; ++c)
+            a.p0[NO + NC + c] = t0.acols[c];
+    }
     a.n_chunks    = e->n_chunks;
     a.n_toys      = e->n_toys;
     a.metric      = 1;

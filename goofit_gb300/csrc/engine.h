@@ -42,6 +42,9 @@ struct GfArgs {
     int n_toys;
     int metric;
     int gtoy;
+    long long chunk;      // events per chunk
+    long long nevt0;      // events of toy 0
+    const void *p0[192];  // toy 0: observable columns, bin-offset columns, amplitude columns (one toy only)
 };
 
 struct GfToy {
