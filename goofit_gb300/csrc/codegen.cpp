@@ -907,6 +907,144 @@ __device__ __forceinline__ double2 gf_lineshape(bool sbw, double Mpair, double m
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 )CUDA";
 
+// FP32 arithmetic of the 4-body amplitudes for the mixed-precision engine: spin factors on FP32 four-vectors
+// (rounded from the FP64 kinematic inversion) and line shapes whose cancelling differences (the squared
+// masses against the pair mass and the thresholds) come in FP64.  Same formulas and order as the FP64
+// functions above.
+const char *kPreludeAmp4F = R"CUDA(
+struct GfLVf { float x, y, z, e; };
+__device__ __forceinline__ GfLVf lvf(float x, float y, float z, float e) { GfLVf v; v.x = x; v.y = y; v.z = z; v.e = e; return v; }
+__device__ __forceinline__ GfLVf lvf(GfLV a) { return lvf((float)a.x, (float)a.y, (float)a.z, (float)a.e); }
+__device__ __forceinline__ GfLVf operator+(GfLVf a, GfLVf b) { return lvf(a.x + b.x, a.y + b.y, a.z + b.z, a.e + b.e); }
+__device__ __forceinline__ GfLVf operator-(GfLVf a, GfLVf b) { return lvf(a.x - b.x, a.y - b.y, a.z - b.z, a.e - b.e); }
+__device__ __forceinline__ GfLVf operator*(GfLVf a, float s) { return lvf(a.x * s, a.y * s, a.z * s, a.e * s); }
+__device__ __forceinline__ GfLVf operator*(float s, GfLVf a) { return lvf(a.x * s, a.y * s, a.z * s, a.e * s); }
+__device__ __forceinline__ float ldot(GfLVf a, GfLVf b) { return a.e * b.e - a.x * b.x - a.y * b.y - a.z * b.z; }
+__device__ __forceinline__ float lmass(GfLVf a) { return sqrtf(ldot(a, a)); }
+__device__ __forceinline__ GfLVf zt1(GfLVf q, GfLVf p, float mR) { return q - ldot(q, p) * p * (1.f / (mR * mR)); }
+__device__ __forceinline__ GfLVf ssv(GfLVf p, float mR, GfLVf v) { return -1.0f * v + p * (ldot(p, v) / (mR * mR)); }
+__device__ __forceinline__ float ssvs(GfLVf p, float mR, GfLVf l, GfLVf r) { return ldot(l, ssv(p, mR, r)); }
+__device__ __forceinline__ float ssts(GfLVf p, float mR, GfLVf lm, GfLVf ln, GfLVf ra, GfLVf rb) {
+    const float manb = ssvs(p, mR, lm, ra) * ssvs(p, mR, ln, rb);
+    const float mbna = ssvs(p, mR, lm, rb) * ssvs(p, mR, ln, ra);
+    const float mnab = ssvs(p, mR, lm, ln) * ssvs(p, mR, ra, rb);
+    return 0.5f * (manb + mbna) - (1.f / 3.f) * mnab;
+}
+__device__ __forceinline__ GfLVf zt2c(GfLVf q, GfLVf p, float mR, GfLVf v) {
+    const GfLVf t = zt1(q, p, mR);
+    const float f = (1.f / 3.f) * ldot(t, t), iu = 1.f / (mR * mR);
+    const float tc[4] = {t.x, t.y, t.z, t.e}, pc[4] = {p.x, p.y, p.z, p.e};
+    const float g[4][4] = {{-1, 0, 0, 0}, {0, -1, 0, 0}, {0, 0, -1, 0}, {0, 0, 0, 1}};
+    GfLVf row[4];
+#pragma unroll
+    for(int i = 0; i < 4; ++i) {
+        float r[4];
+#pragma unroll
+        for(int j = 0; j < 4; ++j)
+            r[j] = tc[i] * tc[j] - f * (g[i][j] - pc[i] * pc[j] * iu);
+        row[i] = lvf(r[0], r[1], r[2], r[3]);
+    }
+    return v.e * row[3] - v.x * row[0] - v.y * row[1] - v.z * row[2];
+}
+__device__ __forceinline__ GfLVf leps3(GfLVf a, GfLVf b, GfLVf c) {
+    GfLVf v;
+    v.e = -1.f * a.x * (b.y * c.z - b.z * c.y) - a.y * (b.z * c.x - b.x * c.z) - a.z * (b.x * c.y - b.y * c.x);
+    v.z = a.x * (b.e * c.y - b.y * c.e) + a.y * (b.x * c.e - b.e * c.x) + a.e * (b.y * c.x - b.x * c.y);
+    v.y = a.x * (b.z * c.e - b.e * c.z) + a.z * (b.e * c.x - b.x * c.e) + a.e * (b.x * c.z - b.z * c.x);
+    v.x = a.y * (b.e * c.z - b.z * c.e) + a.z * (b.y * c.e - b.e * c.y) + a.e * (b.z * c.y - b.y * c.z);
+    return v;
+}
+__device__ __forceinline__ float gf_spinfactor_f(int kind, float mD0, GfLVf P1, GfLVf P2, GfLVf P3, GfLVf P4) {
+    switch(kind) {
+    case 1: { const GfLVf pV = P3 + P4, qV = P3 - P4, pP = pV + P2, qP = pV - P2;
+              return ldot(zt1(qP, pP, lmass(pP)), zt1(qV, pV, lmass(pV))); }
+    case 2: { const GfLVf pV1 = P1 + P2, qV1 = P1 - P2, pV2 = P3 + P4, qV2 = P3 - P4;
+              const float MV1 = sqrtf(ldot(pV1, pV1)), MV2 = sqrtf(ldot(pV2, pV2));
+              return (ldot(qV1, qV2) - ldot(qV1, pV1) * ldot(pV1, qV2) / (MV1 * MV1) -
+                      ldot(qV1, pV2) * ldot(pV2, qV2) / (MV2 * MV2) +
+                      ldot(qV1, pV1) * ldot(pV1, pV2) * ldot(pV2, qV2) / (MV1 * MV1 * MV2 * MV2)); }
+    case 3: { const GfLVf pV1 = P1 + P2, qV1 = P2 - P1, pV2 = P3 + P4, qV2 = P4 - P3, pD = pV1 + pV2, qD = pV1 - pV2;
+              const float MV1 = sqrtf(ldot(pV1, pV1)), MV2 = sqrtf(ldot(pV2, pV2));
+              return -ldot(leps3(pD, zt1(qD, pD, lmass(pD)), zt1(qV1, pV1, MV1)), zt1(qV2, pV2, MV2)); }
+    case 4: { const GfLVf pV1 = P1 + P2, qV1 = P1 - P2, pV2 = P3 + P4, qV2 = P3 - P4, pD = pV1 + pV2, qD = pV1 - pV2;
+              return ldot(zt1(qV1, pV1, lmass(pV1)), zt2c(qD, pD, lmass(pD), zt1(qV2, pV2, lmass(pV2)))); }
+    case 5: { const GfLVf pV = P3 + P4, qV = P3 - P4, pA = P2 + pV, pD = P1 + pA, qD = pA - P1;
+              return -ldot(zt1(qD, pD, lmass(pD)), ssv(pA, lmass(pA), zt1(qV, pV, lmass(pV)))); }
+    case 6: { const GfLVf pV = P3 + P4, qV = P3 - P4, pA = P2 + pV, qA = P2 - pV, pD = P1 + pA, qD = pA - P1;
+              return ldot(zt1(qD, pD, lmass(pD)), zt2c(qA, pA, lmass(pA), zt1(qV, pV, lmass(pV)))); }
+    case 7: { const GfLVf pS = P3 + P4, pV = P1 + P2, qV = P1 - P2, pD = pV + pS, qD = pV - pS;
+              return ldot(zt1(qD, pD, lmass(pD)), zt1(qV, pV, lmass(pV))); }
+    case 8: { const GfLVf pV1 = P2 + P3 + P4, pV2 = P3 + P4, qV1 = (P3 + P4) - P2, qV2 = P3 - P4;
+              const float MV1 = lmass(pV1), MV2 = lmass(pV2);
+              const GfLVf pD = pV1 + P1, qD = pV1 - P1;
+              return ldot(leps3(pV1, zt1(qV1, pV1, MV1), zt1(qV2, pV2, MV2)), ssv(pV1, MV1, zt1(qD, pD, lmass(pD)))); }
+    case 9: { const GfLVf pS = P3 + P4, pA = P2 + pS, qA = pS - P2, pD = pA + P1, qD = pA - P1;
+              return ldot(zt1(qD, pD, lmass(pD)), zt1(qA, pA, lmass(pA))); }
+    case 10: { const GfLVf pV = P3 + P4, qV = P3 - P4, pT = P2 + pV, qT = pV - P2, pD = P1 + pT, qD = pT - P1;
+               const float mT = lmass(pT);
+               const GfLVf tV = zt1(qV, pV, lmass(pV)), tD = zt1(qD, pD, lmass(pD)), t1T = zt1(qT, pT, mT);
+               const GfLVf tmp = leps3(t1T, pT, ssv(pT, mT, tV));
+               return ssts(pT, mT, tD, tD, tmp, t1T) + (1.f / 3.f) * ldot(tD, tD) / ldot(pT, pT) * ssts(pT, mT, pD, pD, tmp, t1T); }
+    case 11: case 12: case 13: case 14: {
+        const bool l12 = kind == 11 || kind == 12;
+        const float a = l12 ? ldot(P1 + P2, P1 + P2) : ldot(P1 + P2 + P3, P1 + P2 + P3);
+        const float b = l12 ? ldot(P3 + P4, P3 + P4) : ldot(P4, P4);
+        const GfLVf T = P1 + P2 + P3 + P4;
+        const float s = ldot(T, T);
+        const float q2 = s / 4.f - (a + b) / 2.f + (a - b) * (a - b) / (4 * s);
+        const float z2 = q2 * mD0 * mD0;
+        const float ff = (kind == 11 || kind == 13) ? 1.0f / (1 + z2) : 1.0f / (z2 * z2 + 3 * z2 + 9);
+        return sqrtf(ff); }
+    default: return 1.0f;
+    }
+}
+__device__ __forceinline__ float gf_blp_f(float z2, float z02, int L) {
+    return L == 0 ? 1.0f : (L == 1 ? (1 + z02) / (1 + z2) : (z02 * z02 + 3 * z02 + 9) / (z2 * z2 + 3 * z2 + 9));
+}
+__device__ __forceinline__ float gf_bl_f(float z2, int L) {
+    return L == 0 ? 1.0f : (L == 1 ? 2 * z2 / (1 + z2) : (13 * z2 * z2) / (z2 * z2 + 3 * z2 + 9));
+}
+__device__ __forceinline__ float gf_bl2_f(float z2, int L) {
+    return L == 0 ? 1.0f : (L == 1 ? 1.0f / (1 + z2) : 1.0f / (z2 * z2 + 3 * z2 + 9));
+}
+__device__ __forceinline__ float2 gf_lineshape_f(bool sbw, double Mpair, double m1, double m2, double mass, double width,
+                                                 int orbital, int FF, double radius) {
+    const double mr2 = Mpair * Mpair;
+    const double mpsq = (m1 + m2) * (m1 + m2), mmsq = (m1 - m2) * (m1 - m2);
+    const double ms2 = mass * mass;
+    const float pABSq = (float)((mr2 - mpsq) * (mr2 - mmsq) / (4 * mr2));
+    float prSq        = (float)((ms2 - mpsq) * (ms2 - mmsq) / (4 * ms2));
+    const float prSq2 = prSq < 0 ? 0.0f : prSq;
+    prSq              = fabsf(prSq);
+    const float r2    = (float)(radius * radius);
+    float fr          = 1.0f;
+    if(0 != orbital && 0 != FF) {
+        fr = (FF == 1 ? gf_bl_f(pABSq * r2, orbital) : gf_blp_f(pABSq * r2, prSq2 * r2, orbital));
+        fr = (FF == 3 ? gf_bl2_f(pABSq * r2, orbital) : fr);
+    }
+    const float m = (float)mass, w = (float)width;
+    float GofM, k;
+    if(!sbw) {
+        const float pratio = sqrtf(pABSq / prSq);
+        float pj           = 1.0f;
+        for(int i = 0; i < 2 * orbital + 1; i++)
+            pj = pj * pratio;
+        GofM = w * pj * (m / (float)Mpair) * gf_blp_f(pABSq * r2, prSq * r2, orbital);
+        const float gamma = m * sqrtf((m * m + w * w));
+        k = 0.90031631615710606f * m * w * gamma / sqrtf(m * m + gamma); // 2 sqrt(2) / pi
+    } else {
+        GofM = w;
+        const float gamma = sqrtf(m * m * (m * m + w * w));
+        k = m * w * gamma / sqrtf(m * m + gamma);
+    }
+    const float dm2 = (float)(ms2 - mr2);
+    const float den = dm2 * dm2 + m * GofM * m * GofM;
+    const float f   = sqrtf(k * fr) / den;
+    return make_float2(f * dm2, f * (m * GofM));
+}
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+)CUDA";
+
 // The 4-body line shapes for double or dual mass / width (the value path uses T = double).
 const char *kPreludeAmp4T = R"CUDA(
 template <typename T>
@@ -1567,12 +1705,13 @@ struct Gen {
         return false;
     }
     // d(component)/d(theta t) from the partials with respect to the component's mass (pm) and width (pw)
-    std::string dPart(int t_param, int mass_p, int width_p, const std::string &dm, const std::string &dw) {
+    std::string dPart(int t_param, int mass_p, int width_p, const std::string &dm, const std::string &dw,
+                      const std::string &mk = "make_double2") {
         std::string e;
         if(mass_p == t_param)
             e = dm;
         if(width_p == t_param)
-            e = e.empty() ? dw : "make_double2(" + e + ".x + " + dw + ".x, " + e + ".y + " + dw + ".y)";
+            e = e.empty() ? dw : mk + "(" + e + ".x + " + dw + ".x, " + e + ".y + " + dw + ".y)";
         return e;
     }
 
@@ -1628,12 +1767,19 @@ struct Gen {
         }
         const Amp4Info &A = T.amp4s[k - n3];
         const double m1 = A.m[0], m2 = A.m[1], m3 = A.m[2], m4 = A.m[3];
+        // mixed precision: FP64 kinematic inversion and pair masses, FP32 spin factors, line shapes and
+        // products; FP64 engine: FP64 throughout
+        const std::string C2 = mixed ? "float2" : "double2", MK = mixed ? "make_float2" : "make_double2";
+        const std::string F = mixed ? "float" : "double";
         os << "__device__ void gf_ampv_" << k
            << "(double m12, double m34, double c12, double c34, double phi, const double *P, R2 *A, R2 *dA) {\n";
         os << "  for(int q = 0; q < " << ND << "; ++q) { dA[q].x = R(0); dA[q].y = R(0); }\n";
         os << "  GfLV V[4];\n";
         os << "  gf_get4vecs(V, m12, m34, c12, c34, phi, " << lit(A.M) << ", " << lit(m1) << ", " << lit(m2) << ", "
            << lit(m3) << ", " << lit(m4) << ");\n";
+        if(mixed)
+            os << "  const GfLVf W[4] = {lvf(V[0]), lvf(V[1]), lvf(V[2]), lvf(V[3])};\n";
+        const char *vv = mixed ? "W" : "V";
         os << "  double d1, d2, mp; (void)d1; (void)d2; (void)mp;\n";
         std::vector<int> lsDep(A.ls.size(), 0);
         for(size_t u = 0; u < A.ls.size(); ++u) {
@@ -1648,30 +1794,32 @@ struct Gen {
             lsDep[u] = thetaParam(k, L.params[0]) || thetaParam(k, L.params[1]);
             const std::string sbw = L.op == GF_OP_LS_SBW ? "true" : "false";
             if(!lsDep[u]) {
-                os << "  const double2 L" << u << " = gf_lineshape(" << sbw << ", mp, d1, d2, P[" << L.params[0] << "], P["
-                   << L.params[1] << "], " << (int)L.consts[1] << ", " << (int)L.consts[2] << ", " << lit(L.consts[3])
-                   << ");\n";
+                os << "  const " << C2 << " L" << u << " = " << (mixed ? "gf_lineshape_f(" : "gf_lineshape(") << sbw
+                   << ", mp, d1, d2, P[" << L.params[0] << "], P[" << L.params[1] << "], " << (int)L.consts[1] << ", "
+                   << (int)L.consts[2] << ", " << lit(L.consts[3]) << ");\n";
             } else {
-                os << "  double2 L" << u << ", Lm" << u << ", Lw" << u << ";\n";
+                // value and derivatives from the FP64 dual-number line shape
+                os << "  " << C2 << " L" << u << ", Lm" << u << ", Lw" << u << ";\n";
                 os << "  { GfDual re, im;\n";
                 os << "    gf_lineshape_t<GfDual>(" << sbw << ", mp, d1, d2, GfDual(P[" << L.params[0]
                    << "], 1.0, 0.0), GfDual(P[" << L.params[1] << "], 0.0, 1.0), " << (int)L.consts[1] << ", "
                    << (int)L.consts[2] << ", " << lit(L.consts[3]) << ", re, im);\n";
-                os << "    L" << u << " = make_double2(re.v, im.v); Lm" << u << " = make_double2(re.a, im.a); Lw" << u
-                   << " = make_double2(re.b, im.b); }\n";
+                os << "    L" << u << " = " << MK << "(re.v, im.v); Lm" << u << " = " << MK << "(re.a, im.a); Lw" << u
+                   << " = " << MK << "(re.b, im.b); }\n";
             }
         }
         for(size_t u = 0; u < A.sf.size(); ++u) {
             const TNode &S = T.nodes[A.sf[u]];
-            os << "  const double S" << u << " = gf_spinfactor(" << (int)S.consts[0] << ", " << lit(S.consts[1]) << ", V["
-               << (int)S.consts[2] << "], V[" << (int)S.consts[3] << "], V[" << (int)S.consts[4] << "], V["
-               << (int)S.consts[5] << "]);\n";
+            os << "  const " << F << " S" << u << " = " << (mixed ? "gf_spinfactor_f(" : "gf_spinfactor(")
+               << (int)S.consts[0] << ", " << (mixed ? "(float)" : "") << lit(S.consts[1]) << ", " << vv << "["
+               << (int)S.consts[2] << "], " << vv << "[" << (int)S.consts[3] << "], " << vv << "[" << (int)S.consts[4]
+               << "], " << vv << "[" << (int)S.consts[5] << "]);\n";
         }
         // product of one permutation's factors, with factor `skip` (a line-shape position) replaced by `repl`
         auto product = [&](const Amp4Info::Amp &am, int p, int skip, const std::string &repl) {
             const int ls_step = (int)am.ls.size() / am.nPerm, sf_step = (int)am.sf.size() / am.nPerm;
             std::ostringstream o;
-            o << "    { double2 r = make_double2(1.0, 0.0);\n";
+            o << "    { " << C2 << " r = " << MK << "(1.0, 0.0);\n";
             for(int j = p * ls_step; j < (p + 1) * ls_step; ++j)
                 o << "      r = cmul(r, " << (j == skip ? repl : "L" + std::to_string(am.ls[j])) << ");\n";
             for(int j = p * sf_step; j < (p + 1) * sf_step; ++j)
@@ -1679,12 +1827,18 @@ struct Gen {
             o << "      r2.x += r.x; r2.y += r.y; }\n";
             return o.str();
         };
+        auto norm = [&](int nPerm) {
+            // 1 / sqrt(nPerm): evaluated in FP64 (FP64 engine, as the reference) or as an FP32 literal
+            if(!mixed)
+                return std::string("    const double f = 1 / sqrt((double)") + std::to_string(nPerm) + ");\n";
+            return std::string("    const float f = (float)") + lit(1.0 / std::sqrt((double)nPerm)) + ";\n";
+        };
         for(int a = 0; a < A.nAmp; ++a) {
             const Amp4Info::Amp &am = A.amps[a];
-            os << "  {\n    double2 r2 = make_double2(0.0, 0.0);\n";
+            os << "  {\n    " << C2 << " r2 = " << MK << "(0.0, 0.0);\n";
             for(int p = 0; p < am.nPerm; ++p)
                 os << product(am, p, -1, "");
-            os << "    const double f = 1 / sqrt((double)" << am.nPerm << ");\n";
+            os << norm(am.nPerm);
             os << "    A[" << a << "].x = (R)(r2.x * f); A[" << a << "].y = (R)(r2.y * f);\n  }\n";
         }
         for(int t = 0; t < (int)theta.size(); ++t)
@@ -1692,7 +1846,7 @@ struct Gen {
                 const int a = theta[t].amps[j];
                 const Amp4Info::Amp &am = A.amps[a];
                 const int ls_step = (int)am.ls.size() / am.nPerm;
-                os << "  {\n    double2 r2 = make_double2(0.0, 0.0);\n";
+                os << "  {\n    " << C2 << " r2 = " << MK << "(0.0, 0.0);\n";
                 for(int p = 0; p < am.nPerm; ++p)
                     for(int pos = p * ls_step; pos < (p + 1) * ls_step; ++pos) {
                         const int u = am.ls[pos];
@@ -1700,12 +1854,12 @@ struct Gen {
                             continue;
                         const TNode &L = T.nodes[A.ls[u]];
                         std::string d = dPart(theta[t].param, L.params[0], L.params[1], "Lm" + std::to_string(u),
-                                              "Lw" + std::to_string(u));
+                                              "Lw" + std::to_string(u), MK);
                         if(d.empty())
                             continue;
                         os << product(am, p, pos, d);
                     }
-                os << "    const double f = 1 / sqrt((double)" << am.nPerm << ");\n";
+                os << norm(am.nPerm);
                 const int idx = toff[t] + (int)j;
                 os << "    dA[" << idx << "].x = (R)(r2.x * f); dA[" << idx << "].y = (R)(r2.y * f);\n  }\n";
             }
@@ -2296,13 +2450,16 @@ KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, int chunk)
         g.os << kPreludeDual;
     if(!t.amp3s.empty())
         g.os << kPreludeAmp << kPreludeAmp3T;
-    if(!t.amp4s.empty())
+    if(!t.amp4s.empty()) {
         g.os << kPreludeAmp4 << kPreludeAmp4T
              << "__device__ __forceinline__ double2 gf_lineshape(bool sbw, double Mpair, double m1, double m2, double mass,\n"
                 "    double width, int orbital, int FF, double radius) {\n"
                 "  double re, im;\n"
                 "  gf_lineshape_t<double>(sbw, Mpair, m1, m2, mass, width, orbital, FF, radius, re, im);\n"
                 "  return make_double2(re, im);\n}\n";
+        if(mixed)
+            g.os << kPreludeAmp4F;
+    }
     if(mixed)
         g.os << kPreludeF32;
     else
