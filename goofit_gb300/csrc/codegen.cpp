@@ -567,6 +567,7 @@ __device__ __forceinline__ void gf_comp_add(float &s, float &c, float v) {
 typedef float2 ACC;
 __device__ __forceinline__ ACC acc_zero() { return make_float2(0.f, 0.f); }
 __device__ __forceinline__ ACC acc_of(float v) { return make_float2(v, 0.f); }
+__device__ __forceinline__ ACC acc_pair(float hi, float lo) { return make_float2(hi, lo); }
 __device__ __forceinline__ ACC acc_add(ACC a, ACC b) {
     float s, e;
     gf_two_sum(a.x, b.x, s, e);
@@ -616,6 +617,7 @@ __device__ __forceinline__ void gf_comp_add(double &s, double &c, double v) { s 
 typedef double ACC;
 __device__ __forceinline__ ACC acc_zero() { return 0.0; }
 __device__ __forceinline__ ACC acc_of(double v) { return v; }
+__device__ __forceinline__ ACC acc_pair(double hi, double lo) { return hi + lo; }
 __device__ __forceinline__ ACC acc_add(ACC a, ACC b) { return a + b; }
 __device__ __forceinline__ ACC warp_acc(double v) { return gf_warp_sum(v); }
 __device__ __forceinline__ ACC warp_acc2(ACC a) { return gf_warp_sum(a); }
@@ -1286,8 +1288,8 @@ void emitNormReads(std::ostream &os, const Tree &T, bool grad, const NormLayout 
 
 int padComps(int c) { return c <= 1 ? 1 : c <= 2 ? 2 : (c + 3) / 4 * 4; }
 
-// Sums K per-thread values over a warp into red[wid][0..K) by a transposed butterfly (recursive halving):
-// at each of the five exchange steps a lane keeps one half of its values and sends the other half to its
+// Sums K per-thread values (ACC expressions) over a warp into red[wid][0..K) by a transposed butterfly
+// (recursive halving): at each of the five exchange steps a lane keeps one half of its values and sends the other half to its
 // partner, so that a warp exchanges about K values instead of 5 K.  Components go in groups of at most 32;
 // after the exchanges a lane holds one component, summed over the warp.  Ends with __syncthreads().
 void emitCtaReduce(std::ostream &os, const std::vector<std::string> &vals, const std::string &ind) {
@@ -1299,8 +1301,7 @@ void emitCtaReduce(std::ostream &os, const std::vector<std::string> &vals, const
             kp <<= 1;
         os << ind << "{\n";
         for(int i = 0; i < kp; ++i)
-            os << ind << "  ACC t" << i << " = " << (i < k ? "acc_of(" + vals[g0 + i] + ")" : std::string("acc_zero()"))
-               << ";\n";
+            os << ind << "  ACC t" << i << " = " << (i < k ? vals[g0 + i] : std::string("acc_zero()")) << ";\n";
         int m = kp, dup = 0;
         std::vector<std::pair<int, int>> halves;
         for(int o = 16; o > 0; o >>= 1) {
@@ -1330,17 +1331,18 @@ void emitCtaReduce(std::ostream &os, const std::vector<std::string> &vals, const
     os << ind << "__syncthreads();\n";
 }
 
-// convolution tables in the event pass: read through L1 (default) or staged in shared memory per CTA
-// (GF_CTAB=smem)
+// convolution tables in the event pass: staged in shared memory per CTA (default) or read through L1
+// (GF_CTAB=l1)
 bool ctabThroughL1() {
     const char *v = std::getenv("GF_CTAB");
-    return !(v && std::string(v) == "smem");
+    return v && std::string(v) == "l1";
 }
 
 struct Gen {
     const Tree &T;
     bool mixed;
-    int block, chunk;
+    int block;
+    bool batch; // many toys per launch: fewer, larger CTAs for the tables and grids
     KernelPlan &plan;
     std::ostringstream os;
     const bool ctabL1 = ctabThroughL1();
@@ -1381,12 +1383,12 @@ struct Gen {
         const int NC    = (int)T.convs.size();
         if(NC == 0)
             return;
-        // m split across the 32 lanes of a warp when every table has at most 8 components (more CTAs of
-        // fewer k each: the tables are short and latency-bound), else across 8 lanes
+        // one toy: m split across the 32 lanes of a warp when every table has at most 8 components (more CTAs
+        // of fewer k each: one table is short and latency-bound); batches of toys, or more components: 8 lanes
         int maxComps = 0;
         for(int ci = 0; ci < NC; ++ci)
             maxComps = std::max(maxComps, convComps(ci, grad));
-        const int MS = maxComps <= block / 32 ? 32 : 8, KT = 8;
+        const int MS = (!batch && maxComps <= block / 32) ? 32 : 8, KT = 8;
         const int items = block / MS;
         auto &off       = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
         auto &cps       = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
@@ -1614,9 +1616,9 @@ struct Gen {
         os << "  __shared__ ACC tot[" << NGp << "];\n";
         os << "  __shared__ int last;\n";
         {
-            std::vector<std::string> comps{"av"};
+            std::vector<std::string> comps{"acc_of(av)"};
             for(int s = 0; s < NGp - 1; ++s)
-                comps.push_back("ag" + std::to_string(s));
+                comps.push_back("acc_of(ag" + std::to_string(s) + ")");
             emitCtaReduce(os, comps, "  ");
         }
         // block partials are component-major: gpartial[toy][q][comp][block]
@@ -2131,7 +2133,9 @@ struct Gen {
         plan.factor_root = T.fit_metric == GF_FIT_UNBINNED_NLL &&
                            (T.nk[0] == NK_EXP || T.nk[0] == NK_GAUSS || T.nk[0] == NK_AMP3 || T.nk[0] == NK_AMP4);
 
-        os << "extern \"C\" __global__ void __launch_bounds__(" << block << ") " << name << "(const GfArgs a) {\n";
+        // at least two CTAs per SM: the register cap (128 at 256 threads) keeps the amplitude event kernels
+        // at two resident CTAs instead of one
+        os << "extern \"C\" __global__ void __launch_bounds__(" << block << ", 2) " << name << "(const GfArgs a) {\n";
         os << "  extern __shared__ __align__(16) unsigned char smraw[];\n";
         os << "  R *stab = reinterpret_cast<R *>(smraw); (void)stab;\n";
         os << "  __shared__ int s_toy, last;\n";
@@ -2200,12 +2204,19 @@ struct Gen {
                 os << "    const R2 *acp" << ac << " = reinterpret_cast<const R2 *>(" << p0ptr("a.acol", NA, ac, NO + NC)
                    << ");\n";
         os << "    if(!toy_on) continue;\n";
+        // per-thread sums: each iteration's VEC events are summed plainly (av, ag), then added to a two-sum
+        // compensated pair (avh + avl, agh + agl), so that a thread's many events add no rounding noise
         if(!values) {
-            os << "    R av = R(0), nv = R(0); (void)nv;\n";
+            os << "    R avh = R(0), avl = R(0), nv = R(0); (void)nv;\n";
             for(int s = 0; s < NGp - 1; ++s)
-                os << "    R ag" << s << " = R(0);\n";
+                os << "    R agh" << s << " = R(0), agl" << s << " = R(0);\n";
         }
         os << "    for(i64 i0 = b0 + " << VEC << " * (i64)tid; i0 < e0; i0 += " << VEC << " * " << block << ") {\n";
+        if(!values) {
+            os << "      R av = R(0);\n";
+            for(int s = 0; s < NGp - 1; ++s)
+                os << "      R ag" << s << " = R(0);\n";
+        }
         for(int o = 0; o < NO && VEC == 2; ++o)
             if(xused[o]) {
                 if(mixed)
@@ -2381,7 +2392,13 @@ struct Gen {
                 os << "        }\n";
             }
         }
-        os << "        }\n      }\n    }\n";
+        os << "        }\n      }\n";
+        if(!values) {
+            os << "      gf_comp_add(avh, avl, av);\n";
+            for(int s = 0; s < NGp - 1; ++s)
+                os << "      gf_comp_add(agh" << s << ", agl" << s << ", ag" << s << ");\n";
+        }
+        os << "    }\n";
         if(values) {
             os << "  }\n}\n\n";
             return;
@@ -2391,11 +2408,11 @@ struct Gen {
         const int NGc = NGp + (factorRoot ? 1 : 0);
         const int OS  = NGs + 2;
         {
-            std::vector<std::string> comps{"av"};
+            std::vector<std::string> comps{"acc_pair(avh, avl)"};
             for(int s = 0; s < NGp - 1; ++s)
-                comps.push_back("ag" + std::to_string(s));
+                comps.push_back("acc_pair(agh" + std::to_string(s) + ", agl" + std::to_string(s) + ")");
             if(factorRoot)
-                comps.push_back("nv");
+                comps.push_back("acc_of(nv)");
             emitCtaReduce(os, comps, "    ");
         }
         // chunk partials are component-major: part[comp][chunk], so that the finisher's loads are contiguous
@@ -2436,10 +2453,11 @@ struct Gen {
 
 NormLayout norm_layout(const Tree &t) { return computeNormLayout(t); }
 
-KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, int chunk) {
+KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, bool batch) {
     KernelPlan plan;
-    plan.nl = norm_layout(t);
-    Gen g{t, mixed, evt_block, chunk, plan, {}};
+    plan.nl                  = norm_layout(t);
+    plan.grid_bins_per_block = batch ? 1024 : 256;
+    Gen g{t, mixed, evt_block, batch, plan, {}};
     g.os << "// generated likelihood kernels\n";
     if(mixed)
         g.os << "typedef float R;\ntypedef float2 R2;\n#define GF_EXP(x) expf(x)\n#define GF_LOG(x) logf(x)\n";

@@ -1131,6 +1131,8 @@ int gf_engine_destroy(gf_engine *e) {
     return GF_OK;
 }
 
+static int compileTree(gf_engine *e);
+
 int gf_set_tree(gf_engine *e, const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
                 const int32_t *grad_mask) {
     if(!e)
@@ -1163,8 +1165,20 @@ int gf_set_tree(gf_engine *e, const gf_node *nodes, int n_nodes, const gf_observ
         if(rc)
             return rc;
     }
+    int rc = compileTree(e);
+    if(rc)
+        return rc;
+    e->layout_ready = false;
+    e->has_tree     = true;
+    return GF_OK;
+}
+
+// Generates and loads the kernels of the engine's tree, shaped for one toy or for a batch of toys, and
+// sizes the event chunks from the gradient event kernel's occupancy.
+static int compileTree(gf_engine *e) {
+    e->batch_kernels = e->n_toys > 1;
     try {
-        e->plan = gf::generate_kernels(e->tree, e->precision == GF_MIXED, e->block, e->chunk);
+        e->plan = gf::generate_kernels(e->tree, e->precision == GF_MIXED, e->block, e->batch_kernels);
     } catch(std::exception &ex) {
         return gf_fail(e, GF_ERR_BAD_TREE, ex.what());
     }
@@ -1181,8 +1195,6 @@ int gf_set_tree(gf_engine *e, const gf_node *nodes, int n_nodes, const gf_observ
         }
         e->evt_ctas_per_sm = std::min(8, std::max(1, occ));
     }
-    e->layout_ready = false;
-    e->has_tree     = true;
     return GF_OK;
 }
 
@@ -1206,6 +1218,9 @@ int gf_set_num_toys(gf_engine *e, int n) {
         freeToy(t);
     e->n_toys = n;
     e->toys.assign(n, GfToy());
+    // one toy and batches of toys use differently shaped table and grid kernels
+    if(e->has_tree && (n > 1) != e->batch_kernels)
+        return compileTree(e);
     return GF_OK;
 }
 
@@ -1746,7 +1761,7 @@ int gf_generated_source(const gf_node *nodes, int n_nodes, const gf_observable *
         return gf_fail(nullptr, GF_ERR_BAD_TREE, why);
     gf::KernelPlan p;
     try {
-        p = gf::generate_kernels(t, precision == GF_MIXED, 256, 8192);
+        p = gf::generate_kernels(t, precision == GF_MIXED, 256, false);
     } catch(std::exception &ex) {
         return gf_fail(nullptr, GF_ERR_BAD_TREE, ex.what());
     }
@@ -1768,7 +1783,7 @@ int gf_compile_tree(const gf_node *nodes, int n_nodes, const gf_observable *obs,
         return gf_fail(nullptr, GF_ERR_BAD_TREE, why);
     gf::KernelPlan p;
     try {
-        p = gf::generate_kernels(t, precision == GF_MIXED, 256, 8192);
+        p = gf::generate_kernels(t, precision == GF_MIXED, 256, false);
     } catch(std::exception &ex) {
         return gf_fail(nullptr, GF_ERR_BAD_TREE, ex.what());
     }

@@ -86,6 +86,7 @@ struct gf_engine {
     bool chunk_fixed = false;
     int evt_ctas_per_sm = 4;      // resident event CTAs per SM: the gradient event kernel's occupancy
     bool evt_ctas_fixed = false;
+    bool batch_kernels  = false;  // kernels generated for a batch of toys (n_toys > 1)
 
     int fit_metric = GF_FIT_UNBINNED_NLL;
     int n_toys = 1;

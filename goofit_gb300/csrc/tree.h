@@ -190,7 +190,7 @@ struct KernelPlan {
     size_t conv_smem_grad = 0, conv_smem_nograd = 0;
     int conv_tk = 64;      // table entries per conv CTA
     int conv_blocks = 0;   // CTAs per (toy, conv) of the table kernel
-    int grid_bins_per_block = 256;
+    int grid_bins_per_block = 256; // 1024 for batches of toys
     std::vector<int> grid_blocks; // per numeric node
     int max_grid_blocks = 0;
     int64_t ctab_per_toy_grad = 0, ctab_per_toy_nograd = 0; // table elements per toy
@@ -210,6 +210,7 @@ struct KernelPlan {
     NormLayout nl;
 };
 
-KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, int chunk);
+// batch: kernels shaped for many toys per launch (fewer, larger table and grid CTAs)
+KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, bool batch);
 
 } // namespace gf
