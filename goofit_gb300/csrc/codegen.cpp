@@ -2395,8 +2395,13 @@ struct Gen {
         os << "        }\n      }\n";
         if(!values) {
             os << "      gf_comp_add(avh, avl, av);\n";
+            // gradient sums are compensated where it is cheap (8 events per iteration) or many events per
+            // thread are expected (batches of toys); the amplitude kernels' 2-event iterations add them plainly
             for(int s = 0; s < NGp - 1; ++s)
-                os << "      gf_comp_add(agh" << s << ", agl" << s << ", ag" << s << ");\n";
+                if(VEC == 8 || batch)
+                    os << "      gf_comp_add(agh" << s << ", agl" << s << ", ag" << s << ");\n";
+                else
+                    os << "      agh" << s << " += ag" << s << ";\n";
         }
         os << "    }\n";
         if(values) {
