@@ -91,8 +91,9 @@ void freeToy(GfToy &t) {
         p = nullptr;
     for(auto &p : t.dcols)
         p = nullptr;
-    t.loaded    = false;
-    t.amp_valid = false;
+    t.loaded     = false;
+    t.amp_valid  = false;
+    t.norm_valid = false;
     t.amp_I.clear();
     t.n = t.npad = 0;
 }
@@ -804,9 +805,12 @@ int updateAmpCaches(gf_engine *e) {
         cp.insert(cp.end(), T.amp_cache_params(k).begin(), T.amp_cache_params(k).end());
     std::sort(cp.begin(), cp.end());
     cp.erase(std::unique(cp.begin(), cp.end()), cp.end());
-    bool any = false;
+    // new events invalidate only the per-event columns, new normalisation points only the integrals, a
+    // changed resonance / line-shape / efficiency parameter both
+    bool anyData = false, anyNorm = false;
     int64_t maxpad = 8;
     std::vector<std::vector<double>> snap(NT);
+    std::vector<char> normDirty(NT, 0);
     for(int t = 0; t < NT; ++t) {
         e->h_dirty[t] = 0;
         if(!e->h_active[t])
@@ -814,14 +818,23 @@ int updateAmpCaches(gf_engine *e) {
         const double *P = e->h_P + (size_t)t * np;
         for(int p : cp)
             snap[t].push_back(P[p]);
-        GfToy &ty = e->toys[t];
-        if(!ty.amp_valid || ty.amp_params != snap[t]) {
+        GfToy &ty       = e->toys[t];
+        const bool pchg = ty.amp_params != snap[t];
+        if(pchg || !ty.amp_valid) {
             e->h_dirty[t] = 1;
-            any           = true;
+            anyData       = true;
             maxpad        = std::max<int64_t>(maxpad, ty.npad);
         }
+        if(pchg || !ty.norm_valid) {
+            normDirty[t] = 1;
+            anyNorm      = true;
+        }
+        if(pchg) {
+            ty.amp_valid  = false;
+            ty.norm_valid = false;
+        }
     }
-    if(!any)
+    if(!anyData && !anyNorm)
         return GF_OK;
     fillRecords(e); // R copies of the parameters for the efficiency in the integral kernel
     int rc = ensureScratch(e);
@@ -831,17 +844,25 @@ int updateAmpCaches(gf_engine *e) {
     cudaError_t r = cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
     if(r == cudaSuccess)
         r = cudaMemcpyAsync(e->d_dirty, e->h_dirty, sizeof(int) * NT, cudaMemcpyHostToDevice, e->stream);
-    if(r == cudaSuccess) {
+    if(r == cudaSuccess && anyData) {
         const int64_t bx = std::min<int64_t>((maxpad + 255) / 256, (int64_t)std::max(1, e->sm_count) * 8);
         r = launch(e->mod.amp, dim3((unsigned)bx, NT, (unsigned)NAN_), dim3(256), 0, e->stream, a);
     }
+    if(r == cudaSuccess && anyData && !anyNorm)
+        r = cudaStreamSynchronize(e->stream);
+    if(r == cudaSuccess)
+        for(int t = 0; t < NT; ++t)
+            if(e->h_dirty[t]) {
+                e->toys[t].amp_valid  = true;
+                e->toys[t].amp_params = snap[t];
+            }
     int64_t maxpts = 1;
     for(int k = 0; k < NAN_; ++k)
         maxpts = std::max<int64_t>(maxpts, ampPoints(e, k));
     const int64_t bn    = std::min<int64_t>((maxpts + 255) / 256, (int64_t)std::max(1, e->sm_count) * 8);
     const size_t gbytes = sizeof(double) * (size_t)NTILE * e->gram_blocks * PM2;
     for(int t = 0; t < NT && r == cudaSuccess; ++t) {
-        if(!e->h_dirty[t])
+        if(!normDirty[t])
             continue;
         // the normalisation points of this toy: amplitudes (and derivatives), then their reduction
         a.gtoy = t;
@@ -899,7 +920,7 @@ int updateAmpCaches(gf_engine *e) {
             if(r != cudaSuccess)
                 break;
             ty.amp_params = snap[t];
-            ty.amp_valid  = true;
+            ty.norm_valid = true;
             continue;
         }
         if(r == cudaSuccess)
@@ -952,7 +973,7 @@ int updateAmpCaches(gf_engine *e) {
             ty.amp_H[k] = H;
         }
         ty.amp_params = snap[t];
-        ty.amp_valid  = true;
+        ty.norm_valid = true;
     }
     if(r != cudaSuccess)
         return gf_cuda_check(e, r, "amplitude caches");
@@ -1700,7 +1721,7 @@ int gf_set_norm_events(gf_engine *e, int node, const double *soa5, int64_t n) {
         return gf_cuda_check(e, r, "normalisation events");
     e->norm_n[k] = n;
     for(auto &ty : e->toys)
-        ty.amp_valid = false;
+        ty.norm_valid = false;
     return GF_OK;
 }
 

@@ -57,7 +57,8 @@ struct GfToy {
     void *acols[128] = {nullptr};       // R2 per event: amplitude columns, then derivative columns
     double *dcols[16] = {nullptr};      // FP64 event columns of the Dalitz variables
     bool loaded    = false;
-    bool amp_valid = false;             // the amplitude cache matches amp_params
+    bool amp_valid  = false;            // the per-event amplitude columns match amp_params and the events
+    bool norm_valid = false;            // the integrals (amp_I, amp_H) match amp_params
     std::vector<double> amp_params;     // parameter values the cache and integrals were built with
     std::vector<std::vector<double>> amp_I; // per amplitude node: n x n complex integrals, interleaved
     std::vector<std::vector<double>> amp_H; // per amplitude node: (derivative rows) x n complex, interleaved
