@@ -34,8 +34,11 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "MIGRAD fit wall-time & event-NLL evals/s: mixed-prec vs FP64 on GB300 at 1e-6 rel NLL"
 # DRAM bytes of one gf_evt_g launch over 2e6 events, from one ncu capture (profiles/gf_evt_g_c2_composite_2e6.md)
-EVT_DRAM_BYTES_PER_LAUNCH = 8_080_640
+EVT_DRAM_BYTES_PER_LAUNCH = 8_055_040
 EVT_DRAM_EVENTS = 2_000_000
+# DRAM bytes of one gf_evt_g launch of the amplitude workloads (profiles/gf_evt_g_amp3_amp4_c3_c5.md):
+# C3 over 5e5 events, C5 over 3e5 events
+EVT_DRAM_BYTES_AMP = {"c3": (32_034_048, 500_000), "c5": (14_432_256, 300_000)}
 N_EVENTS = 2_000_000
 WORKLOAD = "c2: AddPdf(0.7 Conv(Exp tau=1.5, Gauss mu=0 sigma=0.3) + 0.3 flat Poly), x in [-5,10], 2e6 events"
 
@@ -512,10 +515,14 @@ def run_dalitz(args) -> dict:
                    "l2": "flushed (256 MB write) before every timed step", "parallelism": "single GPU"},
         "e2e": {"value": n / (e2e / 1e3), "unit": "event-NLL evals/s", "h2d_bytes_per_step": int(cols.nbytes),
                 "d2h_bytes_per_step": (2 + eng.n_grad) * 8, "ms_per_step": e2e,
-                "note": "includes the upload and the amplitude-cache + integral rebuild it triggers"},
+                "note": "includes the upload and the per-event amplitude columns it invalidates (the integrals "
+                        "depend on parameters only and stay cached)"},
         "cache_and_integral_build_ms": float(np.median(build_ms)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": "gf_evt_g", "kernel_ms": evt,
+                     "frac": achieved / peaks["hbm_gbs"],
+                     "traffic": EVT_DRAM_BYTES_AMP[args.config][0] * n / EVT_DRAM_BYTES_AMP[args.config][1],
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                       "profiles/gf_evt_g_amp3_amp4_c3_c5.md", "kernel": "gf_evt_g", "kernel_ms": evt,
                      "bytes_per_event": bytes_per_event, "peak_source": peaks["src"]},
         "cpu_baseline": cpu,
         "gpu_launches": eng.launches_per_eval(True) * args.steps,
