@@ -12,7 +12,7 @@ from .api import (FF, PAIR_12, PAIR_13, PAIR_23, RBW, SF_4Body, AddPdf, Amp3Body
                   DaughterPair, DecayInfo3, EvalFunc, EventNumber, ExpPdf, FitManager, FitManagerMinuit2,
                   GaussianPdf, GeneralError, GooPdf, MultiPolynomialPdf, NonRes, Observable, OutOfRange, PdfBase,
                   PolynomialPdf, ProdPdf, ResonancePdf, Resonances, UnbinnedDataSet, Variable, get_precision,
-                  set_precision)
+                  readFromFile, readListOfNumbers, set_precision, writeToFile)
 from .engine import Engine, FitResult, Minimizer
 
 __all__ = [
@@ -22,5 +22,6 @@ __all__ = [
     "get_precision", "set_precision", "Amp3Body", "DecayInfo3", "DaughterPair", "PAIR_12", "PAIR_13", "PAIR_23",
     "ResonancePdf", "Resonances", "RBW", "NonRes", "MultiPolynomialPdf", "Amp4Body", "Amplitude", "AmpComponent",
     "DecayInfo4", "DP4Pair", "FF", "Lineshape", "Lineshapes", "SF_4Body", "SpinFactor", "BinnedDataSet",
-    "FitControl", "UnbinnedNllFit", "BinnedNllFit", "BinnedErrorFit", "BinnedChisqFit",
+    "FitControl", "UnbinnedNllFit", "BinnedNllFit", "BinnedErrorFit", "BinnedChisqFit", "writeToFile",
+    "readFromFile", "readListOfNumbers",
 ]

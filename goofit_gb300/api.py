@@ -1026,6 +1026,33 @@ class Resonances:
     NonRes = NonRes
 
 
+def _generate_sig(pdf: "GooPdf", particles: np.ndarray, columns: np.ndarray, rng: np.random.Generator):
+    """Weights and accept-reject flags of phase-space events for an amplitude PDF: the weight of an event is
+    the PDF's unnormalised value (|sum c A|^2 times the efficiency; the FP64 engine), flagged accepted with
+    probability weight / max weight (Amp3BodyBase::fillMCFlags, src/PDFs/physics/Amp3BodyBase.cu:13-21).
+    The phase-space events are flat already (unweighted), so their own weight is 1."""
+    from .engine import Engine
+    nodes, params, obs = pdf._flatten()
+    eng = Engine("fp64")
+    try:
+        eng.set_tree(nodes, [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs],
+                     len(params), [0] * len(params))
+        for i, p in enumerate(pdf._flat_order):
+            p._engine_setup(eng, i)
+        eng.upload(np.ascontiguousarray(columns, dtype=np.float64))
+        eng.set_params(np.array([v.value for v in params]))
+        weights = eng.eval_events(A.GF_METRIC_EVAL)
+    finally:
+        eng.close()
+    wmax = float(weights.max()) if weights.size else 0.0
+    flags = rng.random(weights.size) * wmax < weights
+    return [particles[:, i, :].copy() for i in range(particles.shape[1])], weights, flags
+
+
+def _generator(seed: int) -> np.random.Generator:
+    return np.random.Generator(np.random.PCG64(seed)) if seed else np.random.default_rng()
+
+
 class Amp3Body(GooPdf):
     """include/goofit/PDFs/physics/Amp3Body.h, src/PDFs/physics/Amp3Body.cu:127-196: coherent sum of
     resonances times an efficiency, normalised over the m12 x m13 bin grid of the two observables.
@@ -1096,6 +1123,25 @@ class Amp3Body(GooPdf):
     def integrals(self) -> np.ndarray:
         """The n x n normalisation integrals I_ij the engine caches (before the bin size factor)."""
         return self._root_engine().amp3_integrals(self._node_index(), len(self.decayInfo.resonances))
+
+    def GenerateSig(self, numEvents: int, seed: int = 0):
+        """Amp3Body::GenerateSig (src/PDFs/physics/Amp3Body.cu:430-547): numEvents flat phase-space events of
+        the decay, their invariant masses, weights (the amplitude density) and accept-reject flags.  Returns
+        (particles, variables, weights, flags): three (n, 4) arrays of daughter 4-vectors (px, py, pz, E) in
+        the parent frame, [m12^2, m23^2, m13^2] (the reference's VarSet order), and two length-n arrays."""
+        from . import phasespace
+        d = self.decayInfo
+        rng = _generator(seed)
+        p = phasespace.generate(d.motherMass, [d.daug1Mass, d.daug2Mass, d.daug3Mass], int(numEvents), rng)
+
+        def m2(a, b):
+            q = p[:, a] + p[:, b]
+            return q[:, 3] ** 2 - np.sum(q[:, :3] ** 2, axis=1)
+
+        m12, m13, m23 = m2(0, 1), m2(0, 2), m2(1, 2)
+        cols = np.vstack([m12, m13, np.arange(len(m12), dtype=np.float64)])
+        parts, w, f = _generate_sig(self, p, cols, rng)
+        return parts, [m12, m23, m13], w, f
 
     def fit_fractions(self) -> list[list[float]]:
         """Amp3Body::fit_fractions (src/PDFs/physics/Amp3Body.cu:376-427): from the data-event caches."""
@@ -1320,6 +1366,21 @@ class Amp4Body(GooPdf):
         eng.set_params(self._param_values(params))
         return eng
 
+    def GenerateSig(self, numEvents: int, seed: int = 0):
+        """Amp4Body::GenerateSig (src/PDFs/physics/Amp4Body.cu:560-677): numEvents flat phase-space events,
+        their Dim5 variables, weights (the amplitude density) and accept-reject flags.  Returns (particles,
+        variables, weights, flags): four (n, 4) arrays of daughter 4-vectors (px, py, pz, E),
+        [m12, m34, cos12, cos34, phi], and two length-n arrays."""
+        from . import phasespace
+        masses = list(self.decayInfo.particle_masses)
+        rng = _generator(seed)
+        p = phasespace.generate(masses[0], masses[1:], int(numEvents), rng)
+        v5 = phasespace.dim5(p)
+        cols = np.vstack([v5, np.arange(v5.shape[1], dtype=np.float64)])
+        nobs = len(self._flatten()[2])
+        parts, w, f = _generate_sig(self, p, cols[:nobs], rng)
+        return parts, [v5[i] for i in range(5)], w, f
+
     def getCachedAmplitude(self, i: int) -> np.ndarray:
         """Amplitude i at every data event (the reference's cachedAMPs column)."""
         return self._root_engine().amp3_cached_wave(0, i)
@@ -1366,8 +1427,8 @@ class FitManager:
         self.strategy = int(s)
 
     def setMinos(self, flag: bool = True) -> None:
-        if flag:
-            raise NotImplementedError("MINOS errors are not provided by this engine")
+        """Asymmetric MINOS errors after the fit (FitManagerMinuit2, src/goofit/FitManagerMinuit2.cpp:58-80)."""
+        self.minos = bool(flag)
 
     def fit(self) -> FitResult:
         pdf = self.pdf
@@ -1396,12 +1457,54 @@ class FitManager:
             v.error = res.errors[i]
         self.result = res
         self.retval = FitManager.Valid if res.valid else FitManager.InValid
+        self.minos_errors = {}
+        if self.minos and res.valid:
+            up = 0.5
+            for i, v in enumerate(params):
+                if v.fixed:
+                    continue
+                lohi = [self._minos_side(eng, res, i, sgn, err, lo, hi, limited, fixed, use_grad, up)
+                        for sgn in (-1.0, 1.0)]
+                v.minos_error = (lohi[0], lohi[1])
+                self.minos_errors[v.name] = v.minos_error
         if self.verbosity > 0:
             print(f"MIGRAD {'valid' if res.valid else 'INVALID'}: fmin={res.fmin:.10g} edm={res.edm:.3g} "
                   f"nfcn={res.nfcn} ({self.wall_seconds:.4f} s)")
             for v in params:
-                print("  ", v)
+                print("  ", v, f"MINOS {v.minos_error}" if getattr(v, "minos_error", None) else "")
         return res
+
+    def _minos_side(self, eng, res, i, sgn, err, lo, hi, limited, fixed, use_grad, up) -> float:
+        """Signed MINOS error of parameter i on one side: the offset d at which min over the other free
+        parameters of NLL(x_i = best + d) - fmin = up (F. James, MINUIT's MINOS; the reference runs
+        Minuit2's MnMinos).  Each trial is a MIGRAD fit with x_i fixed, started at the best point; the
+        offset is updated by d <- d sqrt(up / delta), exact for a parabolic profile, until delta is within
+        1% of up.  A parameter limit stops the search there."""
+        best = np.array(res.values)
+        sig = res.errors[i] if res.errors[i] > 0 else max(abs(err[i]), 1e-12)
+        fx = fixed.copy()
+        fx[i] = 1
+        d = sig
+        for _ in range(12):
+            x = best.copy()
+            x[i] = best[i] + sgn * d
+            at_limit = False
+            if limited[i] and lo[i] < hi[i]:
+                if x[i] <= lo[i] or x[i] >= hi[i]:
+                    x[i] = min(max(x[i], lo[i]), hi[i])
+                    at_limit = True
+            r = eng.fit(x, err, lo, hi, limited, fx, tolerance=self.tolerance, strategy=self.strategy,
+                        maxfcn=self.max_calls, use_grad=use_grad)
+            delta = r.fmin - res.fmin
+            if at_limit and delta < up:
+                return float(x[i] - best[i])
+            if not np.isfinite(delta) or delta <= 0:
+                d *= 2.0
+                continue
+            if abs(delta - up) < 0.01 * up:
+                return float(x[i] - best[i])
+            d *= float(np.sqrt(up / delta))
+        return float(sgn * d)
 
     def __bool__(self) -> bool:
         return self.retval == FitManager.Valid
@@ -1411,3 +1514,41 @@ class FitManager:
 
 
 FitManagerMinuit2 = FitManager
+
+
+# ---------------------------------------------------------------- parameter files
+def writeToFile(pdf: PdfBase, fname: str) -> None:
+    """writeToFile (src/goofit/FunctorWriter.cpp:9-21): one line per parameter of the PDF,
+    `name value error lower upper`.  Values are written with 17 significant digits (the reference streams
+    them at the default 6), so that a file read back restores the parameters exactly."""
+    with open(fname, "w") as w:
+        for v in pdf.getParameters():
+            w.write(f"{v.getName()} {v.value:.17g} {v.error:.17g} {v.lowerlimit:.17g} {v.upperlimit:.17g}\n")
+
+
+def readFromFile(pdf: PdfBase, fname: str) -> None:
+    """readFromFile (src/goofit/FunctorWriter.cpp:23-62): for every line whose first token names a
+    parameter of the PDF, set its value, error and limits from the next four numbers; other lines are
+    skipped; reading stops once every parameter has been set."""
+    byname = {v.getName(): v for v in pdf.getParameters()}
+    done = set()
+    with open(fname) as r:
+        for line in r:
+            tok = line.split()
+            if not tok or tok[0] not in byname:
+                continue
+            v = byname[tok[0]]
+            value, error, lower, upper = (float(t) for t in tok[1:5])
+            v.setValue(value)
+            v.setError(error)
+            v.setLowerLimit(lower)
+            v.setUpperLimit(upper)
+            done.add(tok[0])
+            if len(done) == len(byname):
+                break
+
+
+def readListOfNumbers(fname: str) -> list[float]:
+    """readListOfNumbers (src/goofit/FunctorWriter.cpp:64-...): whitespace-separated numbers of a file."""
+    with open(fname) as r:
+        return [float(t) for t in r.read().split()]

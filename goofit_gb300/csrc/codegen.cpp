@@ -1508,14 +1508,24 @@ struct Gen {
             os << "        R rv[" << KT << "];\n#pragma unroll\n        for(int j = 0; j < " << KT
                << "; ++j) rv[j] = Rw[mlo - j];\n";
             // blocks of 8 products are summed plainly, blocks are added with a two-sum correction (mixed)
+            // blocks of 8 m: full blocks fully unrolled (the window shifts become register renames), the
+            // last partial block stepwise; the same products in the same order either way
             os << "        for(int mb = mlo; mb < mhi; mb += 8) {\n";
             os << "          R bs[" << KT << "];\n#pragma unroll\n          for(int j = 0; j < " << KT << "; ++j) bs[j] = R(0);\n";
-            os << "          const int me = min(mb + 8, mhi);\n";
-            os << "          for(int m = mb; m < me; ++m) {\n";
-            os << "            const R mv = M[m];\n";
-            os << "#pragma unroll\n            for(int j = 0; j < " << KT << "; ++j) bs[j] = fma(mv, rv[j], bs[j]);\n";
-            os << "#pragma unroll\n            for(int j = " << KT - 1 << "; j > 0; --j) rv[j] = rv[j - 1];\n";
-            os << "            rv[0] = Rw[m + 1];\n";
+            os << "          if(mb + 8 <= mhi) {\n";
+            os << "#pragma unroll\n            for(int u = 0; u < 8; ++u) {\n";
+            os << "              const R mv = M[mb + u];\n";
+            os << "#pragma unroll\n              for(int j = 0; j < " << KT << "; ++j) bs[j] = fma(mv, rv[j], bs[j]);\n";
+            os << "#pragma unroll\n              for(int j = " << KT - 1 << "; j > 0; --j) rv[j] = rv[j - 1];\n";
+            os << "              rv[0] = Rw[mb + u + 1];\n";
+            os << "            }\n";
+            os << "          } else {\n";
+            os << "            for(int m = mb; m < mhi; ++m) {\n";
+            os << "              const R mv = M[m];\n";
+            os << "#pragma unroll\n              for(int j = 0; j < " << KT << "; ++j) bs[j] = fma(mv, rv[j], bs[j]);\n";
+            os << "#pragma unroll\n              for(int j = " << KT - 1 << "; j > 0; --j) rv[j] = rv[j - 1];\n";
+            os << "              rv[0] = Rw[m + 1];\n";
+            os << "            }\n";
             os << "          }\n";
             os << "#pragma unroll\n          for(int j = 0; j < " << KT << "; ++j) gf_comp_add(acc[j], cmp[j], bs[j]);\n";
             os << "        }\n      }\n    }\n";
