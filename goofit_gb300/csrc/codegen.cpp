@@ -568,6 +568,8 @@ typedef float2 ACC;
 __device__ __forceinline__ ACC acc_zero() { return make_float2(0.f, 0.f); }
 __device__ __forceinline__ ACC acc_of(float v) { return make_float2(v, 0.f); }
 __device__ __forceinline__ ACC acc_pair(float hi, float lo) { return make_float2(hi, lo); }
+// 1/x rounded to nearest (the same value as the IEEE division 1.0f / x)
+__device__ __forceinline__ float gf_rcp(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ ACC acc_add(ACC a, ACC b) {
     float s, e;
     gf_two_sum(a.x, b.x, s, e);
@@ -618,6 +620,7 @@ typedef double ACC;
 __device__ __forceinline__ ACC acc_zero() { return 0.0; }
 __device__ __forceinline__ ACC acc_of(double v) { return v; }
 __device__ __forceinline__ ACC acc_pair(double hi, double lo) { return hi + lo; }
+__device__ __forceinline__ double gf_rcp(double x) { return 1.0 / x; }
 __device__ __forceinline__ ACC acc_add(ACC a, ACC b) { return a + b; }
 __device__ __forceinline__ ACC warp_acc(double v) { return gf_warp_sum(v); }
 __device__ __forceinline__ ACC warp_acc2(ACC a) { return gf_warp_sum(a); }
@@ -2227,6 +2230,8 @@ struct Gen {
             for(int s = 0; s < NGp - 1; ++s)
                 os << "      R ag" << s << " = R(0);\n";
         }
+        // events of this iteration inside the chunk: a 32-bit bound per event instead of a 64-bit one
+        os << "      const int jn = e0 - i0 < " << VEC << " ? (int)(e0 - i0) : " << VEC << ";\n";
         for(int o = 0; o < NO && VEC == 2; ++o)
             if(xused[o]) {
                 if(mixed)
@@ -2296,7 +2301,7 @@ struct Gen {
         os << "        {\n" << body.str();
         os << "        const R pv = " << normMul(c, 0, root.v) << ";\n";
         if(values) {
-            os << "        if(i0 + j < e0) {\n";
+            os << "        if(j < jn) {\n";
             os << "          double r;\n";
             os << "          if(a.metric == 0) r = (double)" << root.v << ";\n";
             os << "          else if(a.metric == 2) r = (double)pv;\n";
@@ -2318,7 +2323,7 @@ struct Gen {
             switch(T.fit_metric) {
             case GF_FIT_BINNED_NLL: // calculateBinAvg, src/PDFs/MetricPointer.cu:23-37
                 os << "        const R raw = pv * " << vw << ";\n";
-                os << "        if(i0 + j < e0 && raw > R(0)) {\n";
+                os << "        if(j < jn && raw > R(0)) {\n";
                 os << "          const R mu = Tn * raw;\n";
                 os << "          av += mu - " << nc << " * GF_LOG(mu);\n";
                 if(grad && T.NG > 0) {
@@ -2332,7 +2337,7 @@ struct Gen {
                 os << "        }\n";
                 break;
             case GF_FIT_BINNED_ERROR: // calculateBinWithError, MetricPointer.cu:39-52: P unnormalised
-                os << "        if(i0 + j < e0) {\n";
+                os << "        if(j < jn) {\n";
                 os << "          const R d = (" << root.v << " - " << nc << ") / " << vw << ";\n";
                 os << "          av += d * d;\n";
                 if(grad && T.NG > 0) {
@@ -2346,7 +2351,7 @@ struct Gen {
                 os << "        }\n";
                 break;
             case GF_FIT_BINNED_CHISQ: // calculateChisq, MetricPointer.cu:54-60
-                os << "        if(i0 + j < e0) {\n";
+                os << "        if(j < jn) {\n";
                 os << "          const R dd = pv * " << vw << " * Tn - " << nc << ";\n";
                 os << "          const R den = " << nc << " > R(1) ? " << nc << " : R(1);\n";
                 os << "          av += dd * dd / den;\n";
@@ -2364,7 +2369,7 @@ struct Gen {
                 if(factorRoot) {
                     // -log(P N) = -log P - log N: the event pass sums -log P and -dP/P and counts the events
                     // with P > 0; the host adds count * (-log N) and count * (-dN/N) in FP64
-                    os << "        if(i0 + j < e0 && " << root.v << " > R(0)) {\n";
+                    os << "        if(j < jn && " << root.v << " > R(0)) {\n";
                     os << "          av -= GF_LOG(" << root.v << ");\n";
                     os << "          nv += R(1);\n";
                     if(grad && T.NG > 0) {
@@ -2378,7 +2383,7 @@ struct Gen {
                                     os << "          ag" << s << " -= " << it->second << " * iT;\n";
                             }
                         } else {
-                            os << "          const R inv = R(1) / " << root.v << ";\n";
+                            os << "          const R inv = gf_rcp(" << root.v << ");\n";
                             for(int s = 0; s < T.NG; ++s) {
                                 auto it = root.g.find(s);
                                 if(it != root.g.end())
@@ -2389,10 +2394,10 @@ struct Gen {
                     os << "        }\n";
                     break;
                 }
-                os << "        if(i0 + j < e0 && pv > R(0)) {\n";
+                os << "        if(j < jn && pv > R(0)) {\n";
                 os << "          av -= GF_LOG(pv);\n";
                 if(grad && T.NG > 0) {
-                    os << "          const R inv = R(1) / pv;\n";
+                    os << "          const R inv = gf_rcp(pv);\n";
                     for(int s = 0; s < T.NG; ++s) {
                         std::string e = dpv(s);
                         if(!e.empty())
