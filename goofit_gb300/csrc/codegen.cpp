@@ -568,6 +568,8 @@ typedef float2 ACC;
 __device__ __forceinline__ ACC acc_zero() { return make_float2(0.f, 0.f); }
 __device__ __forceinline__ ACC acc_of(float v) { return make_float2(v, 0.f); }
 __device__ __forceinline__ ACC acc_pair(float hi, float lo) { return make_float2(hi, lo); }
+// a b as an unevaluated pair (the product and its exact rounding error)
+__device__ __forceinline__ ACC gf_two_prod(float a, float b) { const float p = a * b; return make_float2(p, fmaf(a, b, -p)); }
 // 1/x rounded to nearest (the same value as the IEEE division 1.0f / x)
 __device__ __forceinline__ float gf_rcp(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ ACC acc_add(ACC a, ACC b) {
@@ -621,6 +623,7 @@ __device__ __forceinline__ ACC acc_zero() { return 0.0; }
 __device__ __forceinline__ ACC acc_of(double v) { return v; }
 __device__ __forceinline__ ACC acc_pair(double hi, double lo) { return hi + lo; }
 __device__ __forceinline__ double gf_rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ ACC gf_two_prod(double a, double b) { return a * b; }
 __device__ __forceinline__ ACC acc_add(ACC a, ACC b) { return a + b; }
 __device__ __forceinline__ ACC warp_acc(double v) { return gf_warp_sum(v); }
 __device__ __forceinline__ ACC warp_acc2(ACC a) { return gf_warp_sum(a); }
@@ -1376,6 +1379,96 @@ struct Gen {
         (grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd) = total;
     }
 
+    // ---------------- numeric-normalisation plan ----------------
+    struct ConvShape {
+        int MS = 8, KT = 8, items = 0;
+        std::vector<int> KB;
+    };
+    // m split across the 32 lanes of a warp for one toy when every table has at most 8 components (more
+    // CTAs of fewer k each: one table is short and latency-bound); batches of toys, or more components: 8
+    // lanes.  KB = table entries per CTA.
+    ConvShape convShape(bool grad) const {
+        ConvShape sh;
+        int maxComps = 0;
+        for(size_t ci = 0; ci < T.convs.size(); ++ci)
+            maxComps = std::max(maxComps, convComps((int)ci, grad));
+        sh.MS    = (!batch && maxComps <= block / 32) ? 32 : 8;
+        sh.items = block / sh.MS;
+        for(size_t ci = 0; ci < T.convs.size(); ++ci) {
+            const int comps = convComps((int)ci, grad);
+            if(comps > sh.items)
+                throw std::runtime_error("codegen: too many convolution derivative components");
+            sh.KB.push_back(sh.KT * (sh.items / comps));
+        }
+        return sh;
+    }
+    void planNumerics() {
+        const int NQ = (int)T.nums.size(), NC = (int)T.convs.size();
+        const int BPB = plan.grid_bins_per_block;
+        plan.grid_blocks.clear();
+        plan.max_grid_blocks = 0;
+        for(auto &g : T.nums) {
+            const int nb = (int)((g.total + BPB - 1) / BPB);
+            plan.grid_blocks.push_back(nb);
+            plan.max_grid_blocks = std::max(plan.max_grid_blocks, nb);
+        }
+        plan.conv_fold_q.assign(NC, -1);
+        plan.num_folded.assign(NQ, 0);
+        plan.grid_needs_conv = false;
+        for(int q = 0; q < NQ; ++q) {
+            const NumInfo &g = T.nums[q];
+            // batches only: for one toy the fold's finishing chain lengthens the table kernel by about what
+            // the grid kernel takes, so the serial grid launch is as fast
+            bool fold = batch && T.nodes[g.node].op == GF_OP_CONVOLUTION && g.obs.size() == 1 &&
+                        g.convs.size() == 1 && g.convs[0] == T.conv_of[g.node] && plan.conv_fold_q[g.convs[0]] < 0;
+            if(fold)
+                for(auto &d : plan.nl.qdN[q]) {
+                    const auto &dep = T.convs[g.convs[0]].dep;
+                    if(std::find(dep.begin(), dep.end(), d.first) == dep.end())
+                        fold = false;
+                }
+            if(!fold) {
+                if(!g.convs.empty())
+                    plan.grid_needs_conv = true;
+                continue;
+            }
+            const int ci = g.convs[0];
+            plan.conv_fold_q[ci] = q;
+            plan.num_folded[q]   = 1;
+            for(bool gr : {true, false}) {
+                const int KB = convShape(gr).KB[ci];
+                plan.max_grid_blocks = std::max(plan.max_grid_blocks, (T.convs[ci].nK + KB - 1) / KB);
+            }
+        }
+    }
+    // The normalisation factor of numeric node q (and its derivatives) from tot[0] = the grid sum and
+    // tot[1 + s] = its derivative for gradient slot s (GooPdf::normalize numeric branch,
+    // src/PDFs/GooPdf.cu:366-395), written to Nq; the grid sum to gsum; NaN / non-positive flags to qflag.
+    void emitNumFinish(int q, bool grad, const std::string &ind) {
+        const NumInfo &g  = T.nums[q];
+        const int NQ      = (int)T.nums.size();
+        const NormLayout &nl = plan.nl;
+        // ((1 * volume) / bins), the reference's order of operations, evaluated on the host
+        double c = 1.0;
+        c *= g.volume;
+        c /= (double)g.total;
+        os << ind << "{\n";
+        os << ind << "  R *Nq = reinterpret_cast<R *>(a.Nq) + (i64)toy * " << nl.nq << ";\n";
+        os << ind << "  const double S = acc_value(tot[0]);\n";
+        os << ind << "  a.gsum[(i64)toy * " << NQ << " + " << q << "] = S;\n";
+        os << ind << "  if(isnan(S)) atomicOr(&a.qflag[toy], 1); else if(!(S > 0.0)) atomicOr(&a.qflag[toy], 2);\n";
+        os << ind << "  const double I = " << lit(c) << " * S;\n";
+        os << ind << "  const double Nd = 1.0 / I;\n";
+        os << ind << "  const R N = (R)Nd;\n";
+        os << ind << "  Nq[" << nl.qN[q] << "] = N;\n";
+        os << ind << "  Nq[" << nl.qNL[q] << "] = (R)(Nd - (double)N);\n";
+        if(grad)
+            for(auto &d : nl.qdN[q])
+                os << ind << "  Nq[" << d.second << "] = -N * N * (R)" << lit(c) << " * (R)acc_r(tot[" << 1 + d.first
+                   << "]);\n";
+        os << ind << "}\n";
+    }
+
     // ---------------- convolution tables ----------------
     // T_c[k] = sum_m A_c[m] B_c[m + off - k] for k in [kmin, kmax].  One CTA covers KB consecutive k; a
     // thread owns KT consecutive k of one component over a contiguous slice of m (MS slices per k-tile),
@@ -1386,13 +1479,8 @@ struct Gen {
         const int NC    = (int)T.convs.size();
         if(NC == 0)
             return;
-        // one toy: m split across the 32 lanes of a warp when every table has at most 8 components (more CTAs
-        // of fewer k each: one table is short and latency-bound); batches of toys, or more components: 8 lanes
-        int maxComps = 0;
-        for(int ci = 0; ci < NC; ++ci)
-            maxComps = std::max(maxComps, convComps(ci, grad));
-        const int MS = (!batch && maxComps <= block / 32) ? 32 : 8, KT = 8;
-        const int items = block / MS;
+        const ConvShape sh = convShape(grad);
+        const int MS = sh.MS, KT = sh.KT, items = sh.items;
         auto &off       = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
         auto &cps       = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
         const int64_t total = grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd;
@@ -1401,11 +1489,7 @@ struct Gen {
         std::vector<int> KBs;
         for(int ci = 0; ci < NC; ++ci) {
             const ConvInfo &cv = T.convs[ci];
-            int comps          = convComps(ci, grad);
-            if(comps > items)
-                throw std::runtime_error("codegen: too many convolution derivative components");
-            int ktiles = items / comps;
-            int KB     = KT * ktiles;
+            const int KB       = sh.KB[ci];
             KBs.push_back(KB);
             int mcomp = 1 + (grad ? (int)T.dep_val[cv.model].size() : 0);
             int rcomp = 1 + (grad ? (int)T.dep_val[cv.resol].size() : 0);
@@ -1416,13 +1500,36 @@ struct Gen {
         (grad ? plan.conv_smem_grad : plan.conv_smem_nograd) = smem;
         plan.conv_blocks = std::max(plan.conv_blocks, maxBlocks);
 
+        if(grad)
+            for(int ci = 0; ci < NC; ++ci) {
+                const int q = plan.conv_fold_q[ci];
+                if(q < 0)
+                    continue;
+                // grid bins per table entry of the folded numeric node
+                const ConvInfo &cv = T.convs[ci];
+                const NumInfo &g   = T.nums[q];
+                std::vector<int> cnt(cv.nK, 0);
+                for(int lb = 0; lb < g.nbins[0]; ++lb) {
+                    const int k = T.kgrid[g.kgrid_off[0] + lb];
+                    if(k < cv.kmin || k > cv.kmax)
+                        throw std::runtime_error("codegen: grid bin offset outside the convolution table");
+                    ++cnt[k - cv.kmin];
+                }
+                os << "__device__ const int gf_kcount_" << ci << "[" << cv.nK << "] = {";
+                for(int k = 0; k < cv.nK; ++k)
+                    os << (k ? "," : "") << cnt[k];
+                os << "};\n";
+            }
         os << "extern \"C\" __global__ void __launch_bounds__(" << block << ") gf_conv_" << sfx
            << "(const GfArgs a) {\n";
         os << "  extern __shared__ __align__(16) unsigned char smraw[];\n";
         os << "  R *sm = reinterpret_cast<R *>(smraw);\n";
         os << "  const int toy = blockIdx.y; const int ci = blockIdx.z; const int tid = threadIdx.x;\n";
+        os << "  const int lane = tid & 31, wid = tid >> 5; (void)lane; (void)wid;\n";
         os << "  gf_pdl_trigger();\n";
-        os << "  if(a.active && !a.active[toy]) return;\n";
+        // launched after the grid kernel (which then needs no table), this kernel overlaps it and waits for
+        // it only before it completes, so that the event kernel's wait on this one covers both
+        os << "  if(a.active && !a.active[toy]) { gf_pdl_wait(); return; }\n";
         emitParamsR(os, T, plan.nl, "  ");
         os << "  R *ctab = reinterpret_cast<R *>(a.ctab) + (i64)toy * " << total << ";\n";
         os << "  switch(ci) {\n";
@@ -1435,7 +1542,7 @@ struct Gen {
             const int W1    = cv.nM + KB; // window entries (one spare for the last shift)
             os << "  case " << ci << ": {\n";
             os << "    const int k0 = " << cv.kmin << " + (int)blockIdx.x * " << KB << ";\n";
-            os << "    if(k0 > " << cv.kmax << ") return;\n";
+            os << "    if(k0 > " << cv.kmax << ") { gf_pdl_wait(); return; }\n";
             os << "    R *sM = sm; R *sR = sm + " << mcomp * cv.nM << ";\n";
             os << "    const int rbase = " << cv.offset << " - (k0 + " << KB - 1 << ");\n";
             const double wM = (cv.ic[1] - cv.ic[0]) / cv.nM, wR = (cv.ic[4] - cv.ic[3]) / cv.nR;
@@ -1533,15 +1640,73 @@ struct Gen {
             os << "#pragma unroll\n          for(int j = 0; j < " << KT << "; ++j) gf_comp_add(acc[j], cmp[j], bs[j]);\n";
             os << "        }\n      }\n    }\n";
             os << "#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) acc[j] += cmp[j];\n";
+            const int fq = plan.conv_fold_q[ci];
+            if(fq >= 0)
+                os << "    ACC fs = acc_zero();\n";
             os << "#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) {\n";
             os << "      const R t = gf_group_sum(acc[j], " << MS << ");\n";
             os << "      const int k = kt0 + j;\n";
-            os << "      if(live && ms == 0 && k <= " << cv.kmax << ") ctab[" << off[ci] << " + (k - " << cv.kmin << ") * "
-               << cp << " + comp] = t;\n";
+            if(fq < 0)
+                os << "      if(live && ms == 0 && k <= " << cv.kmax << ") ctab[" << off[ci] << " + (k - " << cv.kmin
+                   << ") * " << cp << " + comp] = t;\n";
+            else {
+                os << "      if(live && ms == 0 && k <= " << cv.kmax << ") {\n";
+                os << "        ctab[" << off[ci] << " + (k - " << cv.kmin << ") * " << cp << " + comp] = t;\n";
+                os << "        fs = acc_add(fs, gf_two_prod((R)gf_kcount_" << ci << "[k - " << cv.kmin << "], t));\n";
+                os << "      }\n";
+            }
             os << "    }\n";
+            if(fq >= 0)
+                emitConvFold(ci, fq, grad, comps, ktiles, MS, KB);
             os << "    break; }\n";
         }
-        os << "  }\n}\n\n";
+        os << "  }\n";
+        os << "  gf_pdl_wait();\n";
+        os << "}\n\n";
+    }
+
+    // The folded grid sum of numeric node q in the conv kernel: the CTA's sums of n_k T_comp[k] into the
+    // grid partials (component slot: 0 value, 1 + gradient slot), then the last CTA of (toy, q) sums the
+    // partials and finishes the node's normalisation.
+    void emitConvFold(int ci, int q, bool grad, int comps, int ktiles, int MS, int KB) {
+        const ConvInfo &cv = T.convs[ci];
+        const int NQ = (int)T.nums.size(), NGs = 1 + T.NG, NGp = 1 + (grad ? T.NG : 0), NW = block / 32;
+        const int MGB = plan.max_grid_blocks, nblk = (cv.nK + KB - 1) / KB;
+        os << "    {\n";
+        os << "      const int cs[" << comps << "] = {0";
+        for(int j = 1; j < comps; ++j)
+            os << ", " << 1 + cv.dep[j - 1];
+        os << "};\n";
+        os << "      __shared__ ACC fsh[" << (block / MS) << "];\n";
+        os << "      __shared__ ACC tot[" << NGp << "];\n";
+        os << "      __shared__ int flast;\n";
+        os << "      if(ms == 0) fsh[item] = fs;\n";
+        os << "      __syncthreads();\n";
+        os << "      ACC *gp = reinterpret_cast<ACC *>(a.gpartial) + ((i64)toy * " << NQ << " + " << q << ") * " << NGs
+           << " * " << MGB << ";\n";
+        os << "      if(tid < " << comps << ") { ACC t = acc_zero(); for(int kk = 0; kk < " << ktiles
+           << "; ++kk) t = acc_add(t, fsh[kk * " << comps << " + tid]); gp[(i64)cs[tid] * " << MGB
+           << " + blockIdx.x] = t; }\n";
+        os << "      __threadfence();\n      __syncthreads();\n";
+        os << "      if(tid == 0) { unsigned prev = atomicAdd(&a.gcounter[toy * " << NQ << " + " << q
+           << "], 1u); flast = (prev == " << nblk - 1 << "u); }\n";
+        os << "      __syncthreads();\n";
+        os << "      if(flast) {\n";
+        os << "        __threadfence();\n";
+        os << "        for(int cc = wid; cc < " << comps << "; cc += " << NW << ") {\n";
+        os << "          const ACC *pc = gp + (i64)cs[cc] * " << MGB << ";\n";
+        os << "          ACC t = acc_zero();\n";
+        os << "          for(int bi = lane; bi < " << nblk << "; bi += 32) t = acc_add(t, pc[bi]);\n";
+        os << "          t = warp_acc2(t);\n";
+        os << "          if(lane == 0) tot[cs[cc]] = t;\n";
+        os << "        }\n";
+        os << "        __syncthreads();\n";
+        os << "        if(tid == 0) {\n";
+        os << "          a.gcounter[toy * " << NQ << " + " << q << "] = 0u;\n";
+        emitNumFinish(q, grad, "          ");
+        os << "        }\n";
+        os << "      }\n";
+        os << "    }\n";
     }
 
     // ---------------- numeric grids ----------------
@@ -1557,13 +1722,6 @@ struct Gen {
         const int NGs = 1 + T.NG;              // buffer stride
         const int BPB = plan.grid_bins_per_block;
         const int NW  = block / 32;
-        plan.grid_blocks.clear();
-        plan.max_grid_blocks = 0;
-        for(auto &g : T.nums) {
-            int nb = (int)((g.total + BPB - 1) / BPB);
-            plan.grid_blocks.push_back(nb);
-            plan.max_grid_blocks = std::max(plan.max_grid_blocks, nb);
-        }
         const int64_t ctabTotal = grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd;
         auto &off               = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
         auto &cps               = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
@@ -1585,6 +1743,10 @@ struct Gen {
         os << "  switch(q) {\n";
         for(int q = 0; q < NQ; ++q) {
             const NumInfo &g = T.nums[q];
+            if(plan.num_folded[q]) {
+                os << "  case " << q << ": return; // folded into the convolution table kernel\n";
+                continue;
+            }
             os << "  case " << q << ": {\n";
             os << "    nblk = " << plan.grid_blocks[q] << ";\n";
             os << "    if((int)blockIdx.x >= nblk) return;\n";
@@ -1656,29 +1818,15 @@ struct Gen {
         os << "  __syncthreads();\n";
         os << "  if(tid == 0) {\n";
         os << "    a.gcounter[toy * " << NQ << " + q] = 0u;\n";
-        os << "    R *Nq = reinterpret_cast<R *>(a.Nq) + (i64)toy * " << nl.nq << ";\n";
-        os << "    const double S = acc_value(tot[0]);\n";
-        os << "    a.gsum[(i64)toy * " << NQ << " + q] = S;\n";
-        os << "    if(isnan(S)) atomicOr(&a.qflag[toy], 1); else if(!(S > 0.0)) atomicOr(&a.qflag[toy], 2);\n";
         os << "    switch(q) {\n";
         for(int q = 0; q < NQ; ++q) {
-            const NumInfo &g = T.nums[q];
-            // ((1 * volume) / bins), the reference's order of operations, evaluated on the host
-            double c = 1.0;
-            c *= g.volume;
-            c /= (double)g.total;
-            os << "    case " << q << ": {\n";
-            os << "      const double I = " << lit(c) << " * S;\n";
-            os << "      const double Nd = 1.0 / I;\n";
-            os << "      const R N = (R)Nd;\n";
-            os << "      Nq[" << nl.qN[q] << "] = N;\n";
-            os << "      Nq[" << nl.qNL[q] << "] = (R)(Nd - (double)N);\n";
-            if(grad)
-                for(auto &d : nl.qdN[q])
-                    os << "      Nq[" << d.second << "] = -N * N * (R)" << lit(c) << " * (R)acc_r(tot[" << 1 + d.first
-                       << "]);\n";
-            os << "      break; }\n";
+            if(plan.num_folded[q])
+                continue;
+            os << "    case " << q << ":\n";
+            emitNumFinish(q, grad, "      ");
+            os << "      break;\n";
         }
+        os << "    default: break;\n";
         os << "    }\n  }\n}\n\n";
     }
 
@@ -2504,6 +2652,7 @@ KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, bool batch
         g.os << kPreludeF64;
     g.tableLayout(true);
     g.tableLayout(false);
+    g.planNumerics();
     g.convKernel(true);
     g.convKernel(false);
     g.gridKernel(true);

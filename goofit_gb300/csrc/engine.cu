@@ -439,22 +439,40 @@ cudaError_t launch(cudaKernel_t k, dim3 g, dim3 b, size_t smem, cudaStream_t s, 
 // Enqueues the prep kernels (conv tables, grid sums) for one variant.
 // Enqueues the prep kernels (conv tables, grid sums) for one variant; returns whether a kernel was the last
 // operation, so that the next kernel can be chained programmatically.
+bool gridWork(const gf_engine *e) {
+    for(char f : e->plan.num_folded)
+        if(!f)
+            return true;
+    return false;
+}
+
 cudaError_t enqueuePrep(gf_engine *e, bool grad, GfArgs &a, bool *kernelLast = nullptr) {
     const gf::Tree &T = e->tree;
     cudaError_t r     = cudaSuccess;
     bool prevKernel   = false;
-    if(!T.convs.empty()) {
+    auto conv = [&]() {
         dim3 g(e->plan.conv_blocks, e->n_toys, (unsigned)T.convs.size());
         r = launch(grad ? e->mod.conv_g : e->mod.conv_n, g, dim3(e->block),
-                   grad ? e->plan.conv_smem_grad : e->plan.conv_smem_nograd, e->stream, a);
-        if(r != cudaSuccess)
-            return r;
+                   grad ? e->plan.conv_smem_grad : e->plan.conv_smem_nograd, e->stream, a, prevKernel && e->use_pdl);
         prevKernel = true;
-    }
-    if(!T.nums.empty()) {
+    };
+    auto grid = [&]() {
         dim3 g(e->plan.max_grid_blocks, e->n_toys, (unsigned)T.nums.size());
         r = launch(grad ? e->mod.grid_g : e->mod.grid_n, g, dim3(e->block), 0, e->stream, a, prevKernel && e->use_pdl);
         prevKernel = true;
+    };
+    const bool hasConv = !T.convs.empty(), hasGrid = !T.nums.empty() && gridWork(e);
+    if(hasConv && hasGrid && !e->plan.grid_needs_conv) {
+        // the grid needs no table (a convolution's own grid sum is folded into the table kernel): the table
+        // kernel starts while the grid kernel runs, and waits for it only before it completes
+        grid();
+        if(r == cudaSuccess)
+            conv();
+    } else {
+        if(hasConv)
+            conv();
+        if(r == cudaSuccess && hasGrid)
+            grid();
     }
     if(kernelLast)
         *kernelLast = prevKernel;
@@ -1667,7 +1685,7 @@ int gf_time_kernels(gf_engine *e, int toy, int with_grad, double *ms_conv, doubl
                    dim3(e->block), grad ? e->plan.conv_smem_grad : e->plan.conv_smem_nograd, e->stream, a);
     if(r == cudaSuccess)
         r = cudaEventRecord(t1, e->stream);
-    if(r == cudaSuccess && !T.nums.empty())
+    if(r == cudaSuccess && !T.nums.empty() && gridWork(e))
         r = launch(grad ? e->mod.grid_g : e->mod.grid_n, dim3(e->plan.max_grid_blocks, e->n_toys, (unsigned)T.nums.size()),
                    dim3(e->block), 0, e->stream, a);
     if(r == cudaSuccess)
@@ -1694,7 +1712,7 @@ int gf_time_kernels(gf_engine *e, int toy, int with_grad, double *ms_conv, doubl
 int gf_launches_per_eval(const gf_engine *e, int) {
     if(!e || !e->has_tree)
         return 0;
-    return 1 + (e->tree.convs.empty() ? 0 : 1) + (e->tree.nums.empty() ? 0 : 1);
+    return 1 + (e->tree.convs.empty() ? 0 : 1) + (e->tree.nums.empty() || !gridWork(e) ? 0 : 1);
 }
 
 int gf_set_norm_events(gf_engine *e, int node, const double *soa5, int64_t n) {

@@ -192,7 +192,13 @@ struct KernelPlan {
     int conv_blocks = 0;   // CTAs per (toy, conv) of the table kernel
     int grid_bins_per_block = 256; // 1024 for batches of toys
     std::vector<int> grid_blocks; // per numeric node
-    int max_grid_blocks = 0;
+    int max_grid_blocks = 0;      // also covers the conv kernel's folded grid sums
+    // A numeric node that is a ConvolutionPdf on a 1-D grid has the grid sum sum_b T[k(b)] = sum_k n_k T[k]
+    // (n_k: grid bins with bin offset k): in kernels shaped for batches of toys the conv kernel accumulates
+    // it and finishes the node's normalisation, and the grid kernel skips the node.
+    std::vector<int> conv_fold_q; // per conv: folded numeric node or -1
+    std::vector<char> num_folded; // per numeric node
+    bool grid_needs_conv = false; // an unfolded numeric node reads a convolution table
     int64_t ctab_per_toy_grad = 0, ctab_per_toy_nograd = 0; // table elements per toy
     std::vector<int64_t> ctab_off_grad, ctab_off_nograd;    // per conv
     std::vector<int> ctab_cp_grad, ctab_cp_nograd;          // per conv: padded components per table row
