@@ -412,13 +412,10 @@ __global__ void __launch_bounds__(128) gf_gram_tc_sum(const double *__restrict__
 template <int W>
 cudaError_t launchW(const float2 *sc, long long npts, long long nst, int ncol, const float *eff, int grid,
                     long long per_cta, double *part, int *err, cudaStream_t s) {
-    static bool attr = false;
-    if(!attr) {
-        cudaError_t r = cudaFuncSetAttribute(gf_gram_tc<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-        if(r != cudaSuccess)
-            return r;
-        attr = true;
-    }
+    // per launch: the attribute belongs to the current device, and the kernel runs once per cache rebuild
+    cudaError_t r = cudaFuncSetAttribute(gf_gram_tc<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if(r != cudaSuccess)
+        return r;
     // every launch requests the full size: one CTA per SM, so the 512-column allocation never waits
     gf_gram_tc<W><<<grid, kThreads, kSmemBytes, s>>>(sc, npts, nst, ncol, eff, per_cta, part, err);
     return cudaGetLastError();
