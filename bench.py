@@ -289,7 +289,8 @@ def run_engine(args) -> dict | None:
         "config": {"workload": WORKLOAD, "events": N_EVENTS, "precision": args.precision,
                    "step": "one FCN call: NLL + analytic gradient (4 floated parameters)",
                    "l2": "flushed (256 MB write) before every timed step",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "event_chunk": eng.event_chunk(), "event_chunk_autotuned": os.environ.get("GF_AUTOTUNE", "1") != "0"},
         "e2e": {"value": world * N_EVENTS / (e2e / 1e3), "unit": "event-NLL evals/s",
                 "h2d_bytes_per_step": N_EVENTS * 8 + len(params) * 8, "d2h_bytes_per_step": (2 + eng.n_grad) * 8,
                 "ms_per_step": e2e},
@@ -522,7 +523,8 @@ def run_dalitz(args) -> dict:
                                 "1500x1500 normalisation bins"),
                    "events": n, "precision": args.precision,
                    "step": f"one FCN: NLL + analytic gradient of {int(sum(mask))} amplitude components, caches built",
-                   "l2": "flushed (256 MB write) before every timed step", "parallelism": "single GPU"},
+                   "l2": "flushed (256 MB write) before every timed step", "parallelism": "single GPU",
+                   "event_chunk": eng.event_chunk(), "event_chunk_autotuned": os.environ.get("GF_AUTOTUNE", "1") != "0"},
         "e2e": {"value": n / (e2e / 1e3), "unit": "event-NLL evals/s", "h2d_bytes_per_step": int(cols.nbytes),
                 "d2h_bytes_per_step": (2 + eng.n_grad) * 8, "ms_per_step": e2e,
                 "note": "includes the upload and the per-event amplitude columns it invalidates (the integrals "

@@ -11,6 +11,9 @@
 #include "rtc.h"
 
 #include <algorithm>
+#include <functional>
+#include <map>
+#include <mutex>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -134,6 +137,7 @@ void freeLayout(gf_engine *e) {
     dfree(e->d_counter);
     dfree(e->d_out);
     dfree(e->d_chunks);
+    e->chunk_cap = 0;
     dfree(e->d_toy_chunk0);
     dfree(e->d_toy_nchunks);
     dfree(e->d_toy_nevents);
@@ -198,6 +202,51 @@ int ampColumns(const gf::Tree &T, int k) {
     return T.amp_count(k) + nd;
 }
 
+// Chunk tables for event chunks of `chunk` events (a chunk never spans two toys): the chunk list, each toy's
+// first chunk and chunk count, and the chunk partials, grown when needed.  Captured graphs are dropped.
+int setChunks(gf_engine *e, int chunk) {
+    const int NT = e->n_toys, NGp = 1 + e->tree.NG;
+    std::vector<long long> chunks;
+    std::vector<int> c0(NT), nc(NT);
+    for(int t = 0; t < NT; ++t) {
+        const int64_t n = e->toys[t].n;
+        const int k     = (int)std::max<int64_t>(1, (n + chunk - 1) / chunk);
+        c0[t]           = (int)(chunks.size() / 3);
+        nc[t]           = k;
+        for(int c = 0; c < k; ++c) {
+            chunks.push_back(t);
+            chunks.push_back((long long)c * chunk);
+            chunks.push_back(std::min<long long>((long long)(c + 1) * chunk, n));
+        }
+    }
+    const int n = (int)(chunks.size() / 3);
+    int rc      = GF_OK;
+    if(n > e->chunk_cap) {
+        dfree(e->d_chunks);
+        dfree(e->d_partial);
+        e->chunk_cap = 0;
+        if((rc = dalloc(e, e->d_chunks, (size_t)3 * n, false)) || (rc = dalloc(e, e->d_partial, (size_t)n * (NGp + 1), false)))
+            return rc;
+        e->chunk_cap = n;
+    }
+    cudaError_t r = cudaMemcpy(e->d_chunks, chunks.data(), sizeof(long long) * chunks.size(), cudaMemcpyHostToDevice);
+    if(r == cudaSuccess)
+        r = cudaMemcpy(e->d_toy_chunk0, c0.data(), sizeof(int) * NT, cudaMemcpyHostToDevice);
+    if(r == cudaSuccess)
+        r = cudaMemcpy(e->d_toy_nchunks, nc.data(), sizeof(int) * NT, cudaMemcpyHostToDevice);
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "chunk tables");
+    e->chunk    = chunk;
+    e->n_chunks = n;
+    dropGraphs(e);
+    return GF_OK;
+}
+
+bool autotuneEnabled() {
+    const char *v = std::getenv("GF_AUTOTUNE");
+    return !(v && v[0] == '0');
+}
+
 int buildLayout(gf_engine *e) {
     if(e->layout_ready)
         return GF_OK;
@@ -219,22 +268,11 @@ int buildLayout(gf_engine *e) {
         ch                   = (ch + 255) / 256 * 256;
         e->chunk             = (int)std::min<int64_t>(std::max<int64_t>(ch, 256), 1 << 20);
     }
-    std::vector<long long> chunks;
-    std::vector<int> c0(NT), nc(NT);
+    // the first evaluation times the event kernel at a few chunk sizes around this one and keeps the best
+    e->tune_pending = !e->chunk_fixed && autotuneEnabled();
     std::vector<long long> ne(NT);
-    for(int t = 0; t < NT; ++t) {
-        int64_t n = e->toys[t].n;
-        int k     = std::max<int64_t>(1, (n + e->chunk - 1) / e->chunk);
-        c0[t]     = (int)(chunks.size() / 3);
-        nc[t]     = k;
-        ne[t]     = n;
-        for(int c = 0; c < k; ++c) {
-            chunks.push_back(t);
-            chunks.push_back((long long)c * e->chunk);
-            chunks.push_back(std::min<long long>((long long)(c + 1) * e->chunk, n));
-        }
-    }
-    e->n_chunks = (int)(chunks.size() / 3);
+    for(int t = 0; t < NT; ++t)
+        ne[t] = e->toys[t].n;
     int rc      = GF_OK;
     auto chk    = [&](int r) {
         if(r != GF_OK && rc == GF_OK)
@@ -271,10 +309,8 @@ int buildLayout(gf_engine *e) {
     chk(dalloc(e, e->d_gsum, (size_t)NT * std::max(1, NQ)));
     chk(dalloc(e, e->d_gpartial, (size_t)NT * std::max(1, NQ) * std::max(1, e->plan.max_grid_blocks) * NGp));
     chk(dalloc(e, e->d_gcounter, (size_t)NT * std::max(1, NQ)));
-    chk(dalloc(e, e->d_partial, (size_t)e->n_chunks * (NGp + 1)));
     chk(dalloc(e, e->d_counter, NT));
     chk(dalloc(e, e->d_out, (size_t)NT * (NGp + 2)));
-    chk(dalloc(e, e->d_chunks, chunks.size()));
     chk(dalloc(e, e->d_toy_chunk0, NT));
     chk(dalloc(e, e->d_toy_nchunks, NT));
     chk(dalloc(e, e->d_toy_nevents, NT));
@@ -355,9 +391,9 @@ int buildLayout(gf_engine *e) {
     cudaMemcpy(e->d_kcols, kcols.data(), sizeof(int *) * kcols.size(), cudaMemcpyHostToDevice);
     if(!T.kgrid.empty())
         cudaMemcpy(e->d_kgrid, T.kgrid.data(), sizeof(int) * T.kgrid.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(e->d_chunks, chunks.data(), sizeof(long long) * chunks.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(e->d_toy_chunk0, c0.data(), sizeof(int) * NT, cudaMemcpyHostToDevice);
-    cudaMemcpy(e->d_toy_nchunks, nc.data(), sizeof(int) * NT, cudaMemcpyHostToDevice);
+    e->chunk_cap = 0;
+    if((rc = setChunks(e, e->chunk)))
+        return rc;
     cudaMemcpy(e->d_toy_nevents, ne.data(), sizeof(long long) * NT, cudaMemcpyHostToDevice);
     cudaError_t r = cudaDeviceSynchronize();
     if(r != cudaSuccess)
@@ -481,12 +517,20 @@ cudaError_t enqueuePrep(gf_engine *e, bool grad, GfArgs &a, bool *kernelLast = n
 
 int evtGrid(const gf_engine *e) { return std::max(1, std::min(e->n_chunks, e->sm_count * e->evt_ctas_per_sm)); }
 
+// An event record that a captured graph keeps as a node (external record) or a plain one outside capture.
+cudaError_t recordEvent(gf_engine *e, cudaEvent_t ev) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if(cudaStreamIsCapturing(e->stream, &st) == cudaSuccess && st == cudaStreamCaptureStatusActive)
+        return cudaEventRecordWithFlags(ev, e->stream, cudaEventRecordExternal);
+    return cudaEventRecord(ev, e->stream);
+}
+
 cudaError_t enqueueEval(gf_engine *e, bool grad) {
     const gf::Tree &T = e->tree;
     const int NT = e->n_toys, NGp = 1 + T.NG;
     GfArgs a         = makeArgs(e);
     // qflag is zero between evaluations: the event kernel's finisher clears it after reading it
-    cudaError_t r = cudaEventRecordWithFlags(e->ev[0], e->stream, cudaEventRecordExternal);
+    cudaError_t r = recordEvent(e, e->ev[0]);
     if(r == cudaSuccess)
         r = cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
     bool kernelLast = false;
@@ -499,7 +543,7 @@ cudaError_t enqueueEval(gf_engine *e, bool grad) {
         r = cudaMemcpyAsync(e->h_out, e->d_out, sizeof(double) * (size_t)NT * (NGp + 2), cudaMemcpyDeviceToHost,
                             e->stream);
     if(r == cudaSuccess)
-        r = cudaEventRecordWithFlags(e->ev[3], e->stream, cudaEventRecordExternal);
+        r = recordEvent(e, e->ev[3]);
     return r;
 }
 
@@ -1046,6 +1090,97 @@ int gf_cuda_check(gf_engine *e, cudaError_t r, const char *what) {
 }
 
 // Runs one evaluation of every active toy.  Results land in e->h_out.
+// The event-chunking autotuner, keyed by (tree, precision, toys, events): one full evaluation (so that the
+// tables, normalisations and caches the event kernel reads are valid), then the gradient event kernel timed
+// with CUDA events after an L2 flush (best of 5 after 2 warm-up launches) at chunk sizes base/2, base,
+// 2 base, 4 base; the fastest is kept for the engine and remembered for the process.
+int autotune(gf_engine *e) {
+    static std::mutex mu;
+    static std::map<std::string, int> cache;
+    int64_t total = 0;
+    for(auto &t : e->toys)
+        total += t.n;
+    const std::string key = std::to_string(std::hash<std::string>{}(e->plan.source)) + ":" +
+                            std::to_string(e->precision) + ":" + std::to_string(e->n_toys) + ":" + std::to_string(total);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if(it != cache.end())
+            return it->second == e->chunk ? GF_OK : setChunks(e, it->second);
+    }
+    {
+        GfArgs a0    = makeArgs(e);
+        cudaError_t r0 = cudaMemcpyAsync(e->d_P, e->h_P, e->pblock_bytes, cudaMemcpyHostToDevice, e->stream);
+        if(r0 == cudaSuccess)
+            r0 = enqueuePrep(e, true, a0);
+        if(r0 == cudaSuccess)
+            r0 = launch(e->mod.evt_g, dim3(evtGrid(e)), dim3(e->block), e->plan.evt_smem_grad, e->stream, a0);
+        if(r0 == cudaSuccess)
+            r0 = cudaStreamSynchronize(e->stream);
+        if(r0 != cudaSuccess)
+            return gf_cuda_check(e, r0, "autotune evaluation");
+    }
+    cudaError_t r = cudaSuccess;
+    // each timed launch starts from a cold L2 (a device buffer of twice the L2 size is overwritten before it),
+    // as for inputs larger than L2 and as the benchmark measures
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, e->device);
+    const size_t flushBytes = (size_t)std::max(l2, 1 << 20) * 2;
+    void *flush             = nullptr;
+    if(cudaMalloc(&flush, flushBytes) != cudaSuccess) {
+        cudaGetLastError();
+        flush = nullptr;
+    }
+    const int base = e->chunk;
+    std::vector<int> cands;
+    for(int64_t c : {(int64_t)base / 2, (int64_t)base, 2 * (int64_t)base, 4 * (int64_t)base}) {
+        c = std::min<int64_t>(std::max<int64_t>((c + 255) / 256 * 256, 256), 1 << 20);
+        if(std::find(cands.begin(), cands.end(), (int)c) == cands.end())
+            cands.push_back((int)c);
+    }
+    int best      = base;
+    float bestMs  = 1e30f;
+    for(int c : cands) {
+        int rc = setChunks(e, c);
+        if(rc)
+            return rc;
+        GfArgs a = makeArgs(e);
+        float mn = 1e30f;
+        for(int it = 0; it < 7 && r == cudaSuccess; ++it) {
+            if(flush)
+                r = cudaMemsetAsync(flush, it & 0xff, flushBytes, e->stream);
+            if(r == cudaSuccess)
+                r = cudaEventRecord(e->ev[1], e->stream);
+            if(r == cudaSuccess)
+                r = launch(e->mod.evt_g, dim3(evtGrid(e)), dim3(e->block), e->plan.evt_smem_grad, e->stream, a);
+            if(r == cudaSuccess)
+                r = cudaEventRecord(e->ev[2], e->stream);
+            if(r == cudaSuccess)
+                r = cudaStreamSynchronize(e->stream);
+            float ms = 0;
+            if(r == cudaSuccess && it >= 2 && cudaEventElapsedTime(&ms, e->ev[1], e->ev[2]) == cudaSuccess)
+                mn = std::min(mn, ms);
+        }
+        if(r != cudaSuccess) {
+            if(flush)
+                cudaFree(flush);
+            return gf_cuda_check(e, r, "autotune timing");
+        }
+        if(mn < bestMs) {
+            bestMs = mn;
+            best   = c;
+        }
+    }
+    if(flush)
+        cudaFree(flush);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        cache[key] = best;
+    }
+    e->tuned_chunk = best;
+    return best == e->chunk ? GF_OK : setChunks(e, best);
+}
+
 int gf_run(gf_engine *e, bool grad, int, int) {
     int rc = buildLayout(e);
     if(rc)
@@ -1053,6 +1188,11 @@ int gf_run(gf_engine *e, bool grad, int, int) {
     if((rc = updateAmpCaches(e)))
         return rc;
     fillRecords(e);
+    if(e->tune_pending) {
+        e->tune_pending = false;
+        if((rc = autotune(e)))
+            return rc;
+    }
     cudaError_t r;
     if(e->use_graph) {
         cudaGraphExec_t &ge = e->graph[grad ? 1 : 0];
@@ -1708,6 +1848,8 @@ int gf_time_kernels(gf_engine *e, int toy, int with_grad, double *ms_conv, doubl
         *ms_event = cudaEventElapsedTime(&f, t2, t3) == cudaSuccess ? f : 0.0;
     return GF_OK;
 }
+
+int64_t gf_event_chunk(const gf_engine *e) { return e && e->layout_ready ? e->chunk : 0; }
 
 int gf_launches_per_eval(const gf_engine *e, int) {
     if(!e || !e->has_tree)

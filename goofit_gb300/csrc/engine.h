@@ -88,6 +88,9 @@ struct gf_engine {
     int evt_ctas_per_sm = 4;      // resident event CTAs per SM: the gradient event kernel's occupancy
     bool evt_ctas_fixed = false;
     bool batch_kernels  = false;  // kernels generated for a batch of toys (n_toys > 1)
+    bool tune_pending   = false;  // the next evaluation runs the event-chunking autotuner
+    int tuned_chunk     = 0;      // chunk size the autotuner chose (0: not tuned)
+    int chunk_cap       = 0;      // chunks the chunk list and partials have room for
 
     int fit_metric = GF_FIT_UNBINNED_NLL;
     int n_toys = 1;

@@ -229,6 +229,10 @@ class Engine:
     def launches_per_eval(self, grad: bool = True) -> int:
         return self._L.gf_launches_per_eval(self._h, 1 if grad else 0)
 
+    def event_chunk(self) -> int:
+        """Events per chunk of the event pass (after the autotuner, once an evaluation has run)."""
+        return int(self._L.gf_event_chunk(self._h))
+
     # ---- fits ----
     def default_fnoise(self, n_events: int | None = None) -> float:
         """Relative rounding noise of the NLL in the mixed path.  FP32 per-event terms summed into

@@ -194,6 +194,9 @@ int gf_last_timing(const gf_engine *eng, double *ms_total, double *ms_event_kern
 int gf_time_kernels(gf_engine *eng, int toy, int with_grad, double *ms_conv, double *ms_grid, double *ms_event);
 /* Number of kernel launches issued by one gf_nll_grad / gf_nll_batch call. */
 int gf_launches_per_eval(const gf_engine *eng, int with_grad);
+/* Events per chunk of the event pass (chosen from the occupancy, then by the autotuner at the first
+   evaluation of a layout unless GF_AUTOTUNE=0 or GF_CHUNK is set); 0 before the first evaluation. */
+int64_t gf_event_chunk(const gf_engine *eng);
 
 /* ---- minimiser (Minuit2 MnMigrad surface, src/goofit/FitManagerMinuit2.cpp:31-119) ---- */
 typedef struct gf_minimizer gf_minimizer;
