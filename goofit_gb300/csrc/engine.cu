@@ -10,6 +10,8 @@
 #include "engine.h"
 #include "rtc.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <functional>
 #include <map>
@@ -1181,14 +1183,25 @@ int autotune(gf_engine *e) {
     return best == e->chunk ? GF_OK : setChunks(e, best);
 }
 
+// NVTX range for the scope of one FCN phase (visible in Nsight Systems / Nsight Compute; no cost otherwise)
+struct NvtxScope {
+    explicit NvtxScope(const char *name) { nvtxRangePushA(name); }
+    ~NvtxScope() { nvtxRangePop(); }
+};
+
 int gf_run(gf_engine *e, bool grad, int, int) {
+    NvtxScope fcn(grad ? "gf_fcn_grad" : "gf_fcn");
     int rc = buildLayout(e);
     if(rc)
         return rc;
-    if((rc = updateAmpCaches(e)))
-        return rc;
+    {
+        NvtxScope s("gf_amplitude_caches");
+        if((rc = updateAmpCaches(e)))
+            return rc;
+    }
     fillRecords(e);
     if(e->tune_pending) {
+        NvtxScope s("gf_autotune");
         e->tune_pending = false;
         if((rc = autotune(e)))
             return rc;
@@ -1217,6 +1230,7 @@ int gf_run(gf_engine *e, bool grad, int, int) {
                 return gf_cuda_check(e, r, "cudaGraphInstantiate");
             }
         }
+        NvtxScope s("gf_graph_launch");
         r = cudaGraphLaunch(ge, e->stream);
         if(r != cudaSuccess)
             return gf_cuda_check(e, r, "cudaGraphLaunch");
