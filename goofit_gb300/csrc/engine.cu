@@ -1495,10 +1495,24 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
     double *stage = e->d_stage;
     int *derr     = e->d_uperr;
     cudaMemsetAsync(derr, 0, sizeof(int), e->stream);
-    if(n > 0)
+    // page-locked host events are read by the conversion kernel in place (no staging copy); other host
+    // memory goes through the device staging buffer
+    const double *src = stage;
+    bool direct       = false;
+    {
+        cudaPointerAttributes pa{};
+        const char *st = std::getenv("GF_UPLOAD_STAGE");
+        if(n > 0 && !(st && st[0] == '1') && cudaPointerGetAttributes(&pa, soa) == cudaSuccess &&
+           pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+            src    = static_cast<const double *>(pa.devicePointer);
+            direct = true;
+        }
+        cudaGetLastError();
+    }
+    if(n > 0 && !direct)
         cudaMemcpyAsync(stage, soa, sizeof(double) * n * NO, cudaMemcpyHostToDevice, e->stream);
     ConvertArgs a{};
-    a.soa    = stage;
+    a.soa    = src;
     a.n      = n;
     a.npad   = npad;
     a.n_obs  = NO;
@@ -1531,8 +1545,7 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
     if(e->precision == GF_MIXED && n > 0)
         for(int o = 0; o < NO; ++o)
             if(ty.dcols[o])
-                cudaMemcpyAsync(ty.dcols[o], stage + (size_t)o * n, sizeof(double) * n, cudaMemcpyDeviceToDevice,
-                                e->stream);
+                cudaMemcpyAsync(ty.dcols[o], src + (size_t)o * n, sizeof(double) * n, cudaMemcpyDefault, e->stream);
     cudaMemcpyAsync(e->h_uperr, derr, sizeof(int), cudaMemcpyDeviceToHost, e->stream);
     r        = cudaStreamSynchronize(e->stream);
     int herr = *e->h_uperr;
