@@ -2372,7 +2372,47 @@ struct Gen {
             for(int s = 0; s < NGp - 1; ++s)
                 os << "    R agh" << s << " = R(0), agl" << s << " = R(0);\n";
         }
+        // software pipelining (mixed precision, 8 events per iteration, at most 3 streamed columns): the next
+        // iteration's 16-byte column loads are issued before this iteration's arithmetic
+        int nStream = NC;
+        for(int o = 0; o < NO; ++o)
+            nStream += xused[o] ? 1 : 0;
+        const bool pipe = mixed && VEC == 8 && nStream <= 3;
+        if(pipe) {
+            for(int o = 0; o < NO; ++o)
+                if(xused[o])
+                    os << "    float4 nx" << o << "a = make_float4(0.f, 0.f, 0.f, 0.f), nx" << o << "b = nx" << o << "a;\n";
+            for(int ci = 0; ci < NC; ++ci)
+                os << "    int4 nk" << ci << "a = make_int4(0, 0, 0, 0), nk" << ci << "b = nk" << ci << "a;\n";
+            os << "    if(b0 + " << VEC << " * (i64)tid < e0) {\n";
+            os << "      const i64 i1 = b0 + " << VEC << " * (i64)tid;\n";
+            for(int o = 0; o < NO; ++o)
+                if(xused[o])
+                    os << "      nx" << o << "a = *reinterpret_cast<const float4 *>(col" << o << " + i1); nx" << o
+                       << "b = *reinterpret_cast<const float4 *>(col" << o << " + i1 + 4);\n";
+            for(int ci = 0; ci < NC; ++ci)
+                os << "      nk" << ci << "a = *reinterpret_cast<const int4 *>(kc" << ci << " + i1); nk" << ci
+                   << "b = *reinterpret_cast<const int4 *>(kc" << ci << " + i1 + 4);\n";
+            os << "    }\n";
+        }
         os << "    for(i64 i0 = b0 + " << VEC << " * (i64)tid; i0 < e0; i0 += " << VEC << " * " << block << ") {\n";
+        if(pipe) {
+            for(int o = 0; o < NO; ++o)
+                if(xused[o])
+                    os << "      const float4 xv" << o << "a = nx" << o << "a, xv" << o << "b = nx" << o << "b;\n";
+            for(int ci = 0; ci < NC; ++ci)
+                os << "      const int4 kv" << ci << "a = nk" << ci << "a, kv" << ci << "b = nk" << ci << "b;\n";
+            os << "      {\n        const i64 i1 = i0 + " << VEC << " * " << block << ";\n";
+            os << "        if(i1 < e0) {\n";
+            for(int o = 0; o < NO; ++o)
+                if(xused[o])
+                    os << "          nx" << o << "a = *reinterpret_cast<const float4 *>(col" << o << " + i1); nx" << o
+                       << "b = *reinterpret_cast<const float4 *>(col" << o << " + i1 + 4);\n";
+            for(int ci = 0; ci < NC; ++ci)
+                os << "          nk" << ci << "a = *reinterpret_cast<const int4 *>(kc" << ci << " + i1); nk" << ci
+                   << "b = *reinterpret_cast<const int4 *>(kc" << ci << " + i1 + 4);\n";
+            os << "        }\n      }\n";
+        }
         if(!values) {
             os << "      R av = R(0);\n";
             for(int s = 0; s < NGp - 1; ++s)
@@ -2403,11 +2443,13 @@ struct Gen {
         }
         for(int o = 0; o < NO && VEC == 8; ++o)
             if(xused[o]) {
-                if(mixed)
-                    os << "      const float4 xv" << o << "a = *reinterpret_cast<const float4 *>(col" << o
-                       << " + i0), xv" << o << "b = *reinterpret_cast<const float4 *>(col" << o << " + i0 + 4);\n"
-                       << "      const R xa" << o << "[8] = {xv" << o << "a.x, xv" << o << "a.y, xv" << o << "a.z, xv" << o
+                if(mixed) {
+                    if(!pipe)
+                        os << "      const float4 xv" << o << "a = *reinterpret_cast<const float4 *>(col" << o
+                           << " + i0), xv" << o << "b = *reinterpret_cast<const float4 *>(col" << o << " + i0 + 4);\n";
+                    os << "      const R xa" << o << "[8] = {xv" << o << "a.x, xv" << o << "a.y, xv" << o << "a.z, xv" << o
                        << "a.w, xv" << o << "b.x, xv" << o << "b.y, xv" << o << "b.z, xv" << o << "b.w};\n";
+                }
                 else {
                     os << "      R xa" << o << "[8];\n";
                     os << "#pragma unroll\n      for(int h = 0; h < 4; ++h) { const double2 t = "
@@ -2415,11 +2457,13 @@ struct Gen {
                        << o << " + i0 + 2 * h); xa" << o << "[2 * h] = t.x; xa" << o << "[2 * h + 1] = t.y; }\n";
                 }
             }
-        for(int ci = 0; ci < NC && VEC == 8; ++ci)
-            os << "      const int4 kv" << ci << "a = *reinterpret_cast<const int4 *>(kc" << ci << " + i0), kv" << ci
-               << "b = *reinterpret_cast<const int4 *>(kc" << ci << " + i0 + 4);\n"
-               << "      const int ka" << ci << "[8] = {kv" << ci << "a.x, kv" << ci << "a.y, kv" << ci << "a.z, kv" << ci
+        for(int ci = 0; ci < NC && VEC == 8; ++ci) {
+            if(!pipe)
+                os << "      const int4 kv" << ci << "a = *reinterpret_cast<const int4 *>(kc" << ci << " + i0), kv" << ci
+                   << "b = *reinterpret_cast<const int4 *>(kc" << ci << " + i0 + 4);\n";
+            os << "      const int ka" << ci << "[8] = {kv" << ci << "a.x, kv" << ci << "a.y, kv" << ci << "a.z, kv" << ci
                << "a.w, kv" << ci << "b.x, kv" << ci << "b.y, kv" << ci << "b.z, kv" << ci << "b.w};\n";
+        }
         os << "#pragma unroll\n      for(int j = 0; j < " << VEC << "; ++j) {\n";
         for(int o = 0; o < NO; ++o)
             if(xused[o])
