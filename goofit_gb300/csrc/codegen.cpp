@@ -915,10 +915,8 @@ __device__ __forceinline__ double2 gf_lineshape(bool sbw, double Mpair, double m
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 )CUDA";
 
-// FP32 arithmetic of the 4-body amplitudes for the mixed-precision engine: spin factors on FP32 four-vectors
-// (rounded from the FP64 kinematic inversion) and line shapes whose cancelling differences (the squared
-// masses against the pair mass and the thresholds) come in FP64.  Same formulas and order as the FP64
-// functions above.
+// FP32 arithmetic of the 4-body amplitudes for the mixed-precision engine: the kinematic inversion, pair
+// masses, spin factors, line shapes and products.  Same formulas and order as the FP64 functions above.
 const char *kPreludeAmp4F = R"CUDA(
 struct GfLVf { float x, y, z, e; };
 __device__ __forceinline__ GfLVf lvf(float x, float y, float z, float e) { GfLVf v; v.x = x; v.y = y; v.z = z; v.e = e; return v; }
@@ -1015,29 +1013,31 @@ __device__ __forceinline__ float gf_bl_f(float z2, int L) {
 __device__ __forceinline__ float gf_bl2_f(float z2, int L) {
     return L == 0 ? 1.0f : (L == 1 ? 1.0f / (1 + z2) : 1.0f / (z2 * z2 + 3 * z2 + 9));
 }
-__device__ __forceinline__ float2 gf_lineshape_f(bool sbw, double Mpair, double m1, double m2, double mass, double width,
-                                                 int orbital, int FF, double radius) {
-    const double mr2 = Mpair * Mpair;
-    const double mpsq = (m1 + m2) * (m1 + m2), mmsq = (m1 - m2) * (m1 - m2);
-    const double ms2 = mass * mass;
-    const float pABSq = (float)((mr2 - mpsq) * (mr2 - mmsq) / (4 * mr2));
-    float prSq        = (float)((ms2 - mpsq) * (ms2 - mmsq) / (4 * ms2));
+// FP32 throughout: the pair mass comes from FP32 four-vectors, so an FP64 threshold or pole difference would
+// not recover precision; the pole term's absolute error (~5e-8) is far below the width term m Gamma(m)
+__device__ __forceinline__ float2 gf_lineshape_f(bool sbw, float Mpair, float m1, float m2, float mass, float width,
+                                                 int orbital, int FF, float radius) {
+    const float mr2 = Mpair * Mpair;
+    const float mpsq = (m1 + m2) * (m1 + m2), mmsq = (m1 - m2) * (m1 - m2);
+    const float ms2 = mass * mass;
+    const float pABSq = (mr2 - mpsq) * (mr2 - mmsq) / (4 * mr2);
+    float prSq        = (ms2 - mpsq) * (ms2 - mmsq) / (4 * ms2);
     const float prSq2 = prSq < 0 ? 0.0f : prSq;
     prSq              = fabsf(prSq);
-    const float r2    = (float)(radius * radius);
+    const float r2    = radius * radius;
     float fr          = 1.0f;
     if(0 != orbital && 0 != FF) {
         fr = (FF == 1 ? gf_bl_f(pABSq * r2, orbital) : gf_blp_f(pABSq * r2, prSq2 * r2, orbital));
         fr = (FF == 3 ? gf_bl2_f(pABSq * r2, orbital) : fr);
     }
-    const float m = (float)mass, w = (float)width;
+    const float m = mass, w = width;
     float GofM, k;
     if(!sbw) {
         const float pratio = sqrtf(pABSq / prSq);
         float pj           = 1.0f;
         for(int i = 0; i < 2 * orbital + 1; i++)
             pj = pj * pratio;
-        GofM = w * pj * (m / (float)Mpair) * gf_blp_f(pABSq * r2, prSq * r2, orbital);
+        GofM = w * pj * (m / Mpair) * gf_blp_f(pABSq * r2, prSq * r2, orbital);
         const float gamma = m * sqrtf((m * m + w * w));
         k = 0.90031631615710606f * m * w * gamma / sqrtf(m * m + gamma); // 2 sqrt(2) / pi
     } else {
@@ -1045,12 +1045,61 @@ __device__ __forceinline__ float2 gf_lineshape_f(bool sbw, double Mpair, double 
         const float gamma = sqrtf(m * m * (m * m + w * w));
         k = m * w * gamma / sqrtf(m * m + gamma);
     }
-    const float dm2 = (float)(ms2 - mr2);
+    const float dm2 = ms2 - mr2;
     const float den = dm2 * dm2 + m * GofM * m * GofM;
     const float f   = sqrtf(k * fr) / den;
     return make_float2(f * dm2, f * (m * GofM));
 }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+// get4Vecs (the FP64 gf_get4vecs above, same formulas and order) in FP32
+__device__ __forceinline__ void gf_get4vecs_f(GfLVf *P, float m12, float m34, float cos12, float cos34, float phi,
+                                              float M, float m1, float m2, float m3, float m4) {
+    const float E1 = (m12 * m12 + m1 * m1 - m2 * m2) / (2 * m12), E2 = (m12 * m12 - m1 * m1 + m2 * m2) / (2 * m12);
+    const float E3 = (m34 * m34 + m3 * m3 - m4 * m4) / (2 * m34), E4 = (m34 * m34 - m3 * m3 + m4 * m4) / (2 * m34);
+    const float p1 = sqrtf(fmaxf(E1 * E1 - m1 * m1, 0.f)), p3 = sqrtf(fmaxf(E3 * E3 - m3 * m3, 0.f));
+    const float sin12 = sqrtf(fmaxf(1 - cos12 * cos12, 0.f)), sin34 = sqrtf(fmaxf(1 - cos34 * cos34, 0.f));
+    const float ED1 = (M * M + m12 * m12 - m34 * m34) / (2 * m12), PD1 = sqrtf(fmaxf(ED1 * ED1 - M * M, 0.f));
+    const float beta1 = PD1 / ED1, gamma1 = 1.0f / sqrtf(1 - beta1 * beta1);
+    const float ED2 = (M * M - m12 * m12 + m34 * m34) / (2 * m34), PD2 = sqrtf(fmaxf(ED2 * ED2 - M * M, 0.f));
+    const float beta2 = -PD2 / ED2, gamma2 = 1.0f / sqrtf(1 - beta2 * beta2);
+    const float x[4] = {cos12 * p1, -cos12 * p1, -cos34 * p3, cos34 * p3};
+    const float y[4] = {sin12 * p1, -sin12 * p1, -sin34 * p3, sin34 * p3};
+    const float E[4] = {E1, E2, E3, E4};
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+#pragma unroll
+    for(int k = 0; k < 4; ++k) {
+        const float g = k < 2 ? gamma1 : gamma2, b = k < 2 ? beta1 : beta2;
+        P[k].e = g * (E[k] + b * x[k]);
+        P[k].x = g * (x[k] + b * E[k]);
+        P[k].z = k < 2 ? sp * y[k] : 0.0f;
+        P[k].y = k < 2 ? cp * y[k] : y[k];
+    }
+}
+// the pair / triple invariant masses of gf_pairmass in FP32
+__device__ __forceinline__ float gf_pairmass_f(int pair, const GfLVf *P, float m1, float m2, float m3, float m4,
+                                               float &d1, float &d2) {
+    switch(pair) {
+    case 0: d1 = m1; d2 = m2; return lmass(P[0] + P[1]);
+    case 1: d1 = m3; d2 = m4; return lmass(P[2] + P[3]);
+    case 2: d1 = m1; d2 = m3; return lmass(P[0] + P[2]);
+    case 3: d1 = m1; d2 = m4; return lmass(P[0] + P[3]);
+    case 4: d1 = m2; d2 = m3; return lmass(P[1] + P[2]);
+    case 5: d1 = m2; d2 = m4; return lmass(P[1] + P[3]);
+    case 6: d1 = lmass(P[0] + P[1]); d2 = m3; return lmass(P[0] + P[1] + P[2]);
+    case 7: d1 = lmass(P[0] + P[2]); d2 = m2; return lmass(P[0] + P[1] + P[2]);
+    case 8: d1 = lmass(P[1] + P[2]); d2 = m1; return lmass(P[0] + P[1] + P[2]);
+    case 9: d1 = lmass(P[0] + P[1]); d2 = m4; return lmass(P[0] + P[1] + P[3]);
+    case 10: d1 = lmass(P[0] + P[3]); d2 = m2; return lmass(P[0] + P[1] + P[3]);
+    case 11: d1 = lmass(P[1] + P[3]); d2 = m1; return lmass(P[0] + P[1] + P[3]);
+    case 12: d1 = lmass(P[0] + P[2]); d2 = m4; return lmass(P[0] + P[2] + P[3]);
+    case 13: d1 = lmass(P[0] + P[3]); d2 = m3; return lmass(P[0] + P[2] + P[3]);
+    case 14: d1 = lmass(P[2] + P[3]); d2 = m1; return lmass(P[0] + P[2] + P[3]);
+    case 15: d1 = lmass(P[1] + P[2]); d2 = m4; return lmass(P[1] + P[2] + P[3]);
+    case 16: d1 = lmass(P[1] + P[3]); d2 = m3; return lmass(P[1] + P[2] + P[3]);
+    default: d1 = lmass(P[2] + P[3]); d2 = m2; return lmass(P[1] + P[2] + P[3]);
+    }
+}
 )CUDA";
 
 // The 4-body line shapes for double or dual mass / width (the value path uses T = double).
@@ -1937,11 +1986,27 @@ struct Gen {
         os << "__device__ void gf_ampv_" << k
            << "(double m12, double m34, double c12, double c34, double phi, const double *P, R2 *A, R2 *dA) {\n";
         os << "  for(int q = 0; q < " << ND << "; ++q) { dA[q].x = R(0); dA[q].y = R(0); }\n";
-        os << "  GfLV V[4];\n";
-        os << "  gf_get4vecs(V, m12, m34, c12, c34, phi, " << lit(A.M) << ", " << lit(m1) << ", " << lit(m2) << ", "
-           << lit(m3) << ", " << lit(m4) << ");\n";
-        if(mixed)
-            os << "  const GfLVf W[4] = {lvf(V[0]), lvf(V[1]), lvf(V[2]), lvf(V[3])};\n";
+        // the mixed engine inverts the kinematics in FP32 unless a line shape's derivative column (dual
+        // numbers, FP64) needs the FP64 pair masses
+        bool anyDep = false;
+        for(size_t u = 0; u < A.ls.size(); ++u) {
+            const TNode &L = T.nodes[A.ls[u]];
+            anyDep |= thetaParam(k, L.params[0]) || thetaParam(k, L.params[1]);
+        }
+        const bool kin32 = mixed && !anyDep;
+        if(kin32) {
+            os << "  GfLVf W[4];\n";
+            os << "  gf_get4vecs_f(W, (float)m12, (float)m34, (float)c12, (float)c34, (float)phi, (float)" << lit(A.M)
+               << ", (float)" << lit(m1) << ", (float)" << lit(m2) << ", (float)" << lit(m3) << ", (float)" << lit(m4)
+               << ");\n";
+            os << "  float d1f, d2f; (void)d1f; (void)d2f;\n";
+        } else {
+            os << "  GfLV V[4];\n";
+            os << "  gf_get4vecs(V, m12, m34, c12, c34, phi, " << lit(A.M) << ", " << lit(m1) << ", " << lit(m2) << ", "
+               << lit(m3) << ", " << lit(m4) << ");\n";
+            if(mixed)
+                os << "  const GfLVf W[4] = {lvf(V[0]), lvf(V[1]), lvf(V[2]), lvf(V[3])};\n";
+        }
         const char *vv = mixed ? "W" : "V";
         os << "  double d1, d2, mp; (void)d1; (void)d2; (void)mp;\n";
         std::vector<int> lsDep(A.ls.size(), 0);
@@ -1951,15 +2016,23 @@ struct Gen {
             if(pair < 2)
                 os << "  mp = " << (pair == 0 ? "m12" : "m34") << "; d1 = " << lit(pair == 0 ? m1 : m3) << "; d2 = "
                    << lit(pair == 0 ? m2 : m4) << ";\n";
+            else if(kin32)
+                os << "  mp = gf_pairmass_f(" << pair << ", W, (float)" << lit(m1) << ", (float)" << lit(m2) << ", (float)"
+                   << lit(m3) << ", (float)" << lit(m4) << ", d1f, d2f); d1 = d1f; d2 = d2f;\n";  // exact widening
             else
                 os << "  mp = gf_pairmass(" << pair << ", V, " << lit(m1) << ", " << lit(m2) << ", " << lit(m3) << ", "
                    << lit(m4) << ", d1, d2);\n";
             lsDep[u] = thetaParam(k, L.params[0]) || thetaParam(k, L.params[1]);
             const std::string sbw = L.op == GF_OP_LS_SBW ? "true" : "false";
             if(!lsDep[u]) {
-                os << "  const " << C2 << " L" << u << " = " << (mixed ? "gf_lineshape_f(" : "gf_lineshape(") << sbw
-                   << ", mp, d1, d2, P[" << L.params[0] << "], P[" << L.params[1] << "], " << (int)L.consts[1] << ", "
-                   << (int)L.consts[2] << ", " << lit(L.consts[3]) << ");\n";
+                if(mixed)
+                    os << "  const float2 L" << u << " = gf_lineshape_f(" << sbw << ", (float)mp, (float)d1, (float)d2, (float)P["
+                       << L.params[0] << "], (float)P[" << L.params[1] << "], " << (int)L.consts[1] << ", "
+                       << (int)L.consts[2] << ", (float)" << lit(L.consts[3]) << ");\n";
+                else
+                    os << "  const double2 L" << u << " = gf_lineshape(" << sbw << ", mp, d1, d2, P[" << L.params[0]
+                       << "], P[" << L.params[1] << "], " << (int)L.consts[1] << ", " << (int)L.consts[2] << ", "
+                       << lit(L.consts[3]) << ");\n";
             } else {
                 // value and derivatives from the FP64 dual-number line shape
                 os << "  " << C2 << " L" << u << ", Lm" << u << ", Lw" << u << ";\n";
