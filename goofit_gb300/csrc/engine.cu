@@ -1827,7 +1827,7 @@ int gf_last_timing(const gf_engine *e, double *ms_total, double *ms_evt) {
 int gf_time_kernels(gf_engine *e, int toy, int with_grad, double *ms_conv, double *ms_grid, double *ms_event) {
     if(!e || !e->has_tree)
         return gf_fail(e, GF_ERR_STATE, "no tree");
-    if(toy < 0 || toy >= e->n_toys)
+    if(toy < -1 || toy >= e->n_toys)
         return gf_fail(e, GF_ERR_INVALID, "toy index out of range");
     cudaSetDevice(e->device);
     int rc = buildLayout(e);
@@ -1836,7 +1836,7 @@ int gf_time_kernels(gf_engine *e, int toy, int with_grad, double *ms_conv, doubl
     const bool grad = with_grad != 0;
     const gf::Tree &T = e->tree;
     for(int t = 0; t < e->n_toys; ++t)
-        e->h_active[t] = (t == toy);
+        e->h_active[t] = (toy < 0 || t == toy);
     if((rc = updateAmpCaches(e)))
         return rc;
     fillRecords(e);

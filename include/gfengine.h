@@ -190,7 +190,7 @@ int gf_eval_events(gf_engine *eng, int toy, int node, int metric, double *out, i
 /* Device time of the last evaluation's kernels in milliseconds (CUDA events). */
 int gf_last_timing(const gf_engine *eng, double *ms_total, double *ms_event_kernel);
 /* Device time of each kernel of one evaluation launched alone (no graph, no overlap), with CUDA events on
- * the engine's stream; a kernel a tree does not need reports 0. */
+ * the engine's stream; a kernel a tree does not need reports 0.  toy = -1: every toy active. */
 int gf_time_kernels(gf_engine *eng, int toy, int with_grad, double *ms_conv, double *ms_grid, double *ms_event);
 /* Number of kernel launches issued by one gf_nll_grad / gf_nll_batch call. */
 int gf_launches_per_eval(const gf_engine *eng, int with_grad);
