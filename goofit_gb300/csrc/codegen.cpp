@@ -1595,6 +1595,14 @@ struct Gen {
             os << "    R *sM = sm; R *sR = sm + " << mcomp * cv.nM << ";\n";
             os << "    const int rbase = " << cv.offset << " - (k0 + " << KB - 1 << ");\n";
             const double wM = (cv.ic[1] - cv.ic[0]) / cv.nM, wR = (cv.ic[4] - cv.ic[3]) / cv.nR;
+            // support of every staged array: the first and last index holding a nonzero value (products with
+            // an exact zero factor add nothing, so each item sums only the m range where both factors can
+            // be nonzero and splits that range over its lanes)
+            const int NA = mcomp + 1 + (grad ? (int)dr.size() : 0);
+            os << "    __shared__ int sup_lo[" << NA << "], sup_hi[" << NA << "];\n";
+            os << "    if(tid < " << NA << ") { sup_lo[tid] = 1 << 30; sup_hi[tid] = -(1 << 30); }\n";
+            os << "    int slo[" << NA << "], shi[" << NA << "];\n";
+            os << "#pragma unroll\n    for(int c = 0; c < " << NA << "; ++c) { slo[c] = 1 << 30; shi[c] = -(1 << 30); }\n";
             for(int pass = 0; pass < 2; ++pass) {
                 bool model = pass == 0;
                 int sub    = model ? cv.model : cv.resol;
@@ -1619,28 +1627,38 @@ struct Gen {
                 c.uid = model ? 0 : 1000;
                 Val v = emit(c, sub);
                 std::string idx = model ? "m" : "w";
+                auto store = [&](size_t slot, const std::string &expr) {
+                    const int arr = model ? (int)slot : mcomp + (int)slot;
+                    os << "      { const R sv = " << expr << "; " << (model ? "sM" : "sR") << "[" << slot * len
+                       << " + " << idx << "] = sv; if(sv != R(0)) { slo[" << arr << "] = min(slo[" << arr << "], "
+                       << idx << "); shi[" << arr << "] = max(shi[" << arr << "], " << idx << "); } }\n";
+                };
                 os << "      {\n" << body.str();
-                os << "      " << (model ? "sM" : "sR") << "[" << idx << "] = " << v.v << ";\n";
+                store(0, v.v);
                 if(grad)
                     for(size_t j = 0; j < dd.size(); ++j) {
                         auto it = v.g.find(dd[j]);
-                        os << "      " << (model ? "sM" : "sR") << "[" << (1 + j) * len << " + " << idx << "] = "
-                           << (it == v.g.end() ? std::string("R(0)") : it->second) << ";\n";
+                        store(1 + j, it == v.g.end() ? std::string("R(0)") : it->second);
                     }
                 os << "      }\n    }\n";
             }
+            os << "    __syncthreads();\n";
+            os << "#pragma unroll\n    for(int c = 0; c < " << NA << "; ++c) {\n";
+            os << "      const int lo = __reduce_min_sync(0xffffffffu, slo[c]), hi = __reduce_max_sync(0xffffffffu, "
+                  "shi[c]);\n";
+            os << "      if(lane == 0) { atomicMin(&sup_lo[c], lo); atomicMax(&sup_hi[c], hi); }\n";
+            os << "    }\n";
             os << "    __syncthreads();\n";
             os << "    const int ms = tid % " << MS << ", item = tid / " << MS << ", comp = item % " << comps
                << ", kt = item / " << comps << ";\n";
             os << "    const bool live = kt < " << ktiles << ";\n";
             os << "    const int kt0 = k0 + kt * " << KT << ";\n";
             os << "    const int c0 = " << KB - 1 << " - kt * " << KT << ";\n";
-            os << "    const int mlo = (" << cv.nM << " * ms) / " << MS << ", mhi = (" << cv.nM << " * (ms + 1)) / " << MS
-               << ";\n";
             os << "    R acc[" << KT << "], cmp[" << KT << "];\n#pragma unroll\n    for(int j = 0; j < " << KT
                << "; ++j) { acc[j] = R(0); cmp[j] = R(0); }\n";
             os << "    if(live) {\n";
             os << "      const R *mA[2] = {nullptr, nullptr}; const R *rA[2] = {nullptr, nullptr};\n";
+            os << "      int ma[2] = {0, 0}, ra[2] = {" << mcomp << ", " << mcomp << "};\n";
             os << "      switch(comp) {\n";
             os << "      case 0: mA[0] = sM; rA[0] = sR; break;\n";
             if(grad)
@@ -1651,11 +1669,13 @@ struct Gen {
                     os << "      case " << 1 + j << ": ";
                     int t = 0;
                     if(im != dm.end()) {
-                        os << "mA[" << t << "] = sM + " << (1 + (im - dm.begin())) * cv.nM << "; rA[" << t << "] = sR; ";
+                        os << "mA[" << t << "] = sM + " << (1 + (im - dm.begin())) * cv.nM << "; rA[" << t
+                           << "] = sR; ma[" << t << "] = " << 1 + (im - dm.begin()) << "; ";
                         ++t;
                     }
                     if(ir != dr.end()) {
-                        os << "mA[" << t << "] = sM; rA[" << t << "] = sR + " << (1 + (ir - dr.begin())) * W1 << "; ";
+                        os << "mA[" << t << "] = sM; rA[" << t << "] = sR + " << (1 + (ir - dr.begin())) * W1
+                           << "; ra[" << t << "] = " << mcomp + 1 + (ir - dr.begin()) << "; ";
                         ++t;
                     }
                     os << "break;\n";
@@ -1664,6 +1684,13 @@ struct Gen {
             os << "      for(int t = 0; t < 2; ++t) {\n";
             os << "        if(!mA[t]) break;\n";
             os << "        const R *M = mA[t]; const R *Rw = rA[t] + c0;\n";
+            // m with M[m] != 0 and R[c0 + m - j] != 0 for some j of the tile, split evenly over the lanes
+            os << "        const int s = max(max(sup_lo[ma[t]], sup_lo[ra[t]] - c0), 0);\n";
+            os << "        const int e = min(min(sup_hi[ma[t]] + 1, sup_hi[ra[t]] - c0 + " << KT << "), " << cv.nM
+               << ");\n";
+            os << "        if(e <= s) continue;\n";
+            os << "        const int mlo = s + ((e - s) * ms) / " << MS << ", mhi = s + ((e - s) * (ms + 1)) / " << MS
+               << ";\n";
             os << "        R rv[" << KT << "];\n#pragma unroll\n        for(int j = 0; j < " << KT
                << "; ++j) rv[j] = Rw[mlo - j];\n";
             // blocks of 8 products are summed plainly, blocks are added with a two-sum correction (mixed)
