@@ -50,14 +50,25 @@ __global__ void gf_convert_events(const ConvertArgs a) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if(i >= a.npad)
         return;
-    for(int o = 0; o < a.n_obs; ++o) {
-        double x = i < a.n ? a.soa[(long long)o * a.n + i] : a.pad_val[o];
-        reinterpret_cast<R *>(a.cols[o])[i] = (R)x;
-    }
+    // every value is read once (the source may be page-locked host memory read over the interconnect),
+    // all loads issued before the first store
+    double xs[16];
+#pragma unroll
+    for(int o = 0; o < 16; ++o)
+        if(o < a.n_obs)
+            xs[o] = i < a.n ? a.soa[(long long)o * a.n + i] : a.pad_val[o];
+#pragma unroll
+    for(int o = 0; o < 16; ++o)
+        if(o < a.n_obs)
+            reinterpret_cast<R *>(a.cols[o])[i] = (R)xs[o];
     for(int c = 0; c < a.n_conv; ++c) {
         int k;
         if(i < a.n) {
-            const double x0 = a.soa[(long long)a.conv_obs[c] * a.n + i];
+            double x0 = 0.0;
+#pragma unroll
+            for(int o = 0; o < 16; ++o)
+                if(o == a.conv_obs[c])
+                    x0 = xs[o];
             // FP32 estimate of x0/step - frac(lo/step); its error is below 3e-7 (|q| + 1), so away from
             // a bin edge its floor is the FP64 result, and near an edge the FP64 division decides
             const float qf = fmaf((float)x0, a.conv_inv_step[c], -a.conv_lbo_f[c]);
