@@ -1430,7 +1430,7 @@ struct Gen {
 
     // ---------------- numeric-normalisation plan ----------------
     struct ConvShape {
-        int MS = 8, KT = 8, items = 0;
+        int MS = 8, KT = 8, items = 0, KP = 1;
         std::vector<int> KB;
     };
     // m split across the 32 lanes of a warp for one toy when every table has at most 8 components (more
@@ -1443,11 +1443,14 @@ struct Gen {
             maxComps = std::max(maxComps, convComps((int)ci, grad));
         sh.MS    = (!batch && maxComps <= block / 32) ? 32 : 8;
         sh.items = block / sh.MS;
+        // batches: each item covers KP k-tiles in turn, so that one CTA's staged model and resolution
+        // arrays (whose evaluation is a third of the work at KP = 1) serve twice the table entries
+        sh.KP    = batch ? 2 : 1;
         for(size_t ci = 0; ci < T.convs.size(); ++ci) {
             const int comps = convComps((int)ci, grad);
             if(comps > sh.items)
                 throw std::runtime_error("codegen: too many convolution derivative components");
-            sh.KB.push_back(sh.KT * (sh.items / comps));
+            sh.KB.push_back(sh.KT * (sh.items / comps) * sh.KP);
         }
         return sh;
     }
@@ -1649,9 +1652,14 @@ struct Gen {
             os << "      if(lane == 0) { atomicMin(&sup_lo[c], lo); atomicMax(&sup_hi[c], hi); }\n";
             os << "    }\n";
             os << "    __syncthreads();\n";
+            const int fq = plan.conv_fold_q[ci];
             os << "    const int ms = tid % " << MS << ", item = tid / " << MS << ", comp = item % " << comps
-               << ", kt = item / " << comps << ";\n";
-            os << "    const bool live = kt < " << ktiles << ";\n";
+               << ", ktb = item / " << comps << ";\n";
+            os << "    const bool live = ktb < " << ktiles << ";\n";
+            if(fq >= 0)
+                os << "    ACC fs = acc_zero();\n";
+            os << "    for(int kp = 0; kp < " << sh.KP << "; ++kp) {\n";
+            os << "    const int kt = ktb + kp * " << ktiles << ";\n";
             os << "    const int kt0 = k0 + kt * " << KT << ";\n";
             os << "    const int c0 = " << KB - 1 << " - kt * " << KT << ";\n";
             os << "    R acc[" << KT << "], cmp[" << KT << "];\n#pragma unroll\n    for(int j = 0; j < " << KT
@@ -1716,9 +1724,6 @@ struct Gen {
             os << "#pragma unroll\n          for(int j = 0; j < " << KT << "; ++j) gf_comp_add(acc[j], cmp[j], bs[j]);\n";
             os << "        }\n      }\n    }\n";
             os << "#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) acc[j] += cmp[j];\n";
-            const int fq = plan.conv_fold_q[ci];
-            if(fq >= 0)
-                os << "    ACC fs = acc_zero();\n";
             os << "#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) {\n";
             os << "      const R t = gf_group_sum(acc[j], " << MS << ");\n";
             os << "      const int k = kt0 + j;\n";
@@ -1732,6 +1737,7 @@ struct Gen {
                 os << "      }\n";
             }
             os << "    }\n";
+            os << "    }\n"; // kp
             if(fq >= 0)
                 emitConvFold(ci, fq, grad, comps, ktiles, MS, KB);
             os << "    break; }\n";
