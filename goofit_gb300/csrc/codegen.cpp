@@ -1444,8 +1444,14 @@ struct Gen {
         sh.MS    = (!batch && maxComps <= block / 32) ? 32 : 8;
         sh.items = block / sh.MS;
         // batches: each item covers KP k-tiles in turn, so that one CTA's staged model and resolution
-        // arrays (whose evaluation is a third of the work at KP = 1) serve twice the table entries
-        sh.KP    = batch ? 2 : 1;
+        // arrays (whose evaluation is a third of the work at KP = 1) serve KP times the table entries;
+        // 1024 toys of the composite model: KP 1 / 2 / 3 / 4 / 6 -> table kernel 0.58 / 0.51 / 0.48 /
+        // 0.48 / 0.47 ms (GF_CONV_KP overrides)
+        sh.KP = 1;
+        if(batch) {
+            const char *v = std::getenv("GF_CONV_KP");
+            sh.KP         = v ? std::max(1, std::min(8, std::atoi(v))) : 4;
+        }
         for(size_t ci = 0; ci < T.convs.size(); ++ci) {
             const int comps = convComps((int)ci, grad);
             if(comps > sh.items)
