@@ -1409,6 +1409,9 @@ struct Gen {
     }
 
     int convComps(int ci, bool grad) const { return 1 + (grad ? (int)T.convs[ci].dep.size() : 0); }
+    // Strides of the conv kernel's staged arrays: multiples of 4 elements (16-byte loads of 4 FP32 values),
+    // congruent to 8 modulo 32 (successive arrays start 8 banks apart)
+    static int convStride(int n) { return n + (((8 - n) % 32) + 32) % 32; }
 
     // Table layout per toy: for each conv, AoS [k][cp] with cp = padded component count (16-byte rows).
     void tableLayout(bool grad) {
@@ -1551,7 +1554,7 @@ struct Gen {
             KBs.push_back(KB);
             int mcomp = 1 + (grad ? (int)T.dep_val[cv.model].size() : 0);
             int rcomp = 1 + (grad ? (int)T.dep_val[cv.resol].size() : 0);
-            size_t sm = (size_t)(mcomp * cv.nM + rcomp * (cv.nM + KB)) * (mixed ? 4 : 8);
+            size_t sm = (size_t)(mcomp * convStride(cv.nM) + rcomp * convStride(cv.nM + KB)) * (mixed ? 4 : 8);
             smem      = std::max(smem, sm);
             maxBlocks = std::max(maxBlocks, (cv.nK + KB - 1) / KB);
         }
@@ -1598,10 +1601,11 @@ struct Gen {
             const auto &dr = T.dep_val[cv.resol];
             const int mcomp = 1 + (grad ? (int)dm.size() : 0);
             const int W1    = cv.nM + KB; // window entries (one spare for the last shift)
+            const int nMp = convStride(cv.nM), W1p = convStride(W1);
             os << "  case " << ci << ": {\n";
             os << "    const int k0 = " << cv.kmin << " + (int)blockIdx.x * " << KB << ";\n";
             os << "    if(k0 > " << cv.kmax << ") { gf_pdl_wait(); return; }\n";
-            os << "    R *sM = sm; R *sR = sm + " << mcomp * cv.nM << ";\n";
+            os << "    R *sM = sm; R *sR = sm + " << mcomp * nMp << ";\n";
             os << "    const int rbase = " << cv.offset << " - (k0 + " << KB - 1 << ");\n";
             const double wM = (cv.ic[1] - cv.ic[0]) / cv.nM, wR = (cv.ic[4] - cv.ic[3]) / cv.nR;
             // support of every staged array: the first and last index holding a nonzero value (products with
@@ -1616,7 +1620,7 @@ struct Gen {
                 bool model = pass == 0;
                 int sub    = model ? cv.model : cv.resol;
                 const auto &dd = model ? dm : dr;
-                int len        = model ? cv.nM : W1;
+                int len        = model ? nMp : W1p; // array stride
                 if(model)
                     os << "    for(int m = tid; m < " << cv.nM << "; m += " << block << ") {\n"
                        << "      const R wx = (R)GF_CENTRE(" << lit(cv.ic[0]) << ", " << lit(wM) << ", m);\n";
@@ -1624,7 +1628,7 @@ struct Gen {
                     os << "    for(int w = tid; w < " << W1 << "; w += " << block << ") {\n"
                        << "      const int r = rbase + w;\n"
                        << "      if(r < 0 || r >= " << cv.nR << ") {\n"
-                       << "        for(int c = 0; c < " << 1 + (grad ? (int)dr.size() : 0) << "; ++c) sR[c * " << W1
+                       << "        for(int c = 0; c < " << 1 + (grad ? (int)dr.size() : 0) << "; ++c) sR[c * " << W1p
                        << " + w] = R(0);\n"
                        << "        continue;\n      }\n"
                        << "      const R wx = (R)GF_CENTRE(" << lit(cv.ic[3]) << ", " << lit(wR) << ", r);\n";
@@ -1683,12 +1687,12 @@ struct Gen {
                     os << "      case " << 1 + j << ": ";
                     int t = 0;
                     if(im != dm.end()) {
-                        os << "mA[" << t << "] = sM + " << (1 + (im - dm.begin())) * cv.nM << "; rA[" << t
+                        os << "mA[" << t << "] = sM + " << (1 + (im - dm.begin())) * nMp << "; rA[" << t
                            << "] = sR; ma[" << t << "] = " << 1 + (im - dm.begin()) << "; ";
                         ++t;
                     }
                     if(ir != dr.end()) {
-                        os << "mA[" << t << "] = sM; rA[" << t << "] = sR + " << (1 + (ir - dr.begin())) * W1
+                        os << "mA[" << t << "] = sM; rA[" << t << "] = sR + " << (1 + (ir - dr.begin())) * W1p
                            << "; ra[" << t << "] = " << mcomp + 1 + (ir - dr.begin()) << "; ";
                         ++t;
                     }
@@ -1703,22 +1707,47 @@ struct Gen {
             os << "        const int e = min(min(sup_hi[ma[t]] + 1, sup_hi[ra[t]] - c0 + " << KT << "), " << cv.nM
                << ");\n";
             os << "        if(e <= s) continue;\n";
-            os << "        const int mlo = s + ((e - s) * ms) / " << MS << ", mhi = s + ((e - s) * (ms + 1)) / " << MS
-               << ";\n";
+            // batches (8 lanes of long slices): blocks of 16 m, FP32 loads 16 bytes wide, lane slices
+            // starting at multiples of 4 (extending the range down to s & ~3 only adds products with a zero
+            // factor); one toy (32 lanes of short slices): blocks of 8 m, an even split
+            const int BM = batch ? 16 : 8;
+            const bool vec = batch && mixed;
+            if(vec) {
+                os << "        const int s4 = s & ~3, L = ((((e - s4 + " << MS - 1 << ") / " << MS << ") + 3) & ~7) + 4;\n";
+                os << "        const int mlo = min(s4 + ms * L, e), mhi = min(mlo + L, e);\n";
+            } else
+                os << "        const int mlo = s + ((e - s) * ms) / " << MS << ", mhi = s + ((e - s) * (ms + 1)) / " << MS
+                   << ";\n";
             os << "        R rv[" << KT << "];\n#pragma unroll\n        for(int j = 0; j < " << KT
                << "; ++j) rv[j] = Rw[mlo - j];\n";
-            // blocks of 8 products are summed plainly, blocks are added with a two-sum correction (mixed)
-            // blocks of 8 m: full blocks fully unrolled (the window shifts become register renames), the
-            // last partial block stepwise; the same products in the same order either way
-            os << "        for(int mb = mlo; mb < mhi; mb += 8) {\n";
+            // blocks of BM products are summed plainly, blocks are added with a two-sum correction (mixed);
+            // full blocks fully unrolled (the window shifts become register renames; batches in FP32: M and
+            // the window read as float4, M + mb and Rw + mb + 1 being 16-byte aligned), the last partial
+            // block stepwise; the same products in the same order either way
+            os << "        for(int mb = mlo; mb < mhi; mb += " << BM << ") {\n";
             os << "          R bs[" << KT << "];\n#pragma unroll\n          for(int j = 0; j < " << KT << "; ++j) bs[j] = R(0);\n";
-            os << "          if(mb + 8 <= mhi) {\n";
-            os << "#pragma unroll\n            for(int u = 0; u < 8; ++u) {\n";
-            os << "              const R mv = M[mb + u];\n";
-            os << "#pragma unroll\n              for(int j = 0; j < " << KT << "; ++j) bs[j] = fma(mv, rv[j], bs[j]);\n";
-            os << "#pragma unroll\n              for(int j = " << KT - 1 << "; j > 0; --j) rv[j] = rv[j - 1];\n";
-            os << "              rv[0] = Rw[mb + u + 1];\n";
-            os << "            }\n";
+            os << "          if(mb + " << BM << " <= mhi) {\n";
+            if(vec) {
+                os << "            const float4 *M4 = reinterpret_cast<const float4 *>(M + mb);\n";
+                os << "            const float4 *R4 = reinterpret_cast<const float4 *>(Rw + mb + 1);\n";
+                os << "#pragma unroll\n            for(int q = 0; q < 4; ++q) {\n";
+                os << "              const float4 mq = M4[q], rq = R4[q];\n";
+                os << "              const float mvs[4] = {mq.x, mq.y, mq.z, mq.w}, rvs[4] = {rq.x, rq.y, rq.z, rq.w};\n";
+                os << "#pragma unroll\n              for(int u = 0; u < 4; ++u) {\n";
+                os << "                const R mv = mvs[u];\n";
+                os << "#pragma unroll\n                for(int j = 0; j < " << KT << "; ++j) bs[j] = fma(mv, rv[j], bs[j]);\n";
+                os << "#pragma unroll\n                for(int j = " << KT - 1 << "; j > 0; --j) rv[j] = rv[j - 1];\n";
+                os << "                rv[0] = rvs[u];\n";
+                os << "              }\n";
+                os << "            }\n";
+            } else {
+                os << "#pragma unroll\n            for(int u = 0; u < " << BM << "; ++u) {\n";
+                os << "              const R mv = M[mb + u];\n";
+                os << "#pragma unroll\n              for(int j = 0; j < " << KT << "; ++j) bs[j] = fma(mv, rv[j], bs[j]);\n";
+                os << "#pragma unroll\n              for(int j = " << KT - 1 << "; j > 0; --j) rv[j] = rv[j - 1];\n";
+                os << "              rv[0] = Rw[mb + u + 1];\n";
+                os << "            }\n";
+            }
             os << "          } else {\n";
             os << "            for(int m = mb; m < mhi; ++m) {\n";
             os << "              const R mv = M[m];\n";
