@@ -80,7 +80,7 @@ __global__ void gf_convert_events(const ConvertArgs a) {
             else
                 k = (int)floor(x0 / a.conv_step[c] - a.conv_lbo[c]);
             if(k < a.conv_kmin[c] || k > a.conv_kmax[c]) {
-                atomicOr(a.err, 1);
+                *a.err = 1; // page-locked host flag: every writer stores the same value
                 k = a.conv_kmin[c];
             }
         } else
@@ -1323,7 +1323,6 @@ int gf_engine_destroy(gf_engine *e) {
     freeNormEvents(e);
     dfree(e->d_vals);
     dfree(e->d_stage);
-    dfree(e->d_uperr);
     hfree(e->h_uperr);
     freeModule(e);
     for(auto &ev : e->ev)
@@ -1498,14 +1497,17 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
         }
         e->stage_cap = need;
     }
-    if(!e->d_uperr) {
-        if((r = cudaMalloc((void **)&e->d_uperr, sizeof(int))) != cudaSuccess ||
-           (r = cudaMallocHost((void **)&e->h_uperr, sizeof(int))) != cudaSuccess)
-            return gf_cuda_check(e, r, "cudaMalloc flag");
+    if(!e->h_uperr) {
+        if((r = cudaHostAlloc((void **)&e->h_uperr, sizeof(int), cudaHostAllocMapped)) != cudaSuccess)
+            return gf_cuda_check(e, r, "cudaHostAlloc flag");
     }
     double *stage = e->d_stage;
-    int *derr     = e->d_uperr;
-    cudaMemsetAsync(derr, 0, sizeof(int), e->stream);
+    // the conversion kernel raises the range error in page-locked host memory, read after the synchronise
+    // below (no memset, no copy back)
+    int *derr = nullptr;
+    if((r = cudaHostGetDevicePointer((void **)&derr, e->h_uperr, 0)) != cudaSuccess)
+        return gf_cuda_check(e, r, "mapped flag");
+    *(volatile int *)e->h_uperr = 0;
     // page-locked host events are read by the conversion kernel in place (no staging copy); other host
     // memory goes through the device staging buffer
     const double *src = stage;
@@ -1557,9 +1559,8 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
         for(int o = 0; o < NO; ++o)
             if(ty.dcols[o])
                 cudaMemcpyAsync(ty.dcols[o], src + (size_t)o * n, sizeof(double) * n, cudaMemcpyDefault, e->stream);
-    cudaMemcpyAsync(e->h_uperr, derr, sizeof(int), cudaMemcpyDeviceToHost, e->stream);
     r        = cudaStreamSynchronize(e->stream);
-    int herr = *e->h_uperr;
+    int herr = *(volatile int *)e->h_uperr;
     if(r != cudaSuccess)
         return gf_cuda_check(e, r, "event conversion");
     ty.n      = n;

@@ -115,7 +115,6 @@ struct gf_engine {
     int64_t vals_cap = 0;
     double *d_stage = nullptr; // FP64 staging of uploads (grow-only)
     int64_t stage_cap = 0;
-    int *d_uperr = nullptr;
     int *h_uperr = nullptr;
     void **d_acols = nullptr;    // [toy][amplitude column]
     double **d_dcols = nullptr;  // [toy][observable]
