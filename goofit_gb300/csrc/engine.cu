@@ -148,7 +148,7 @@ void freeLayout(gf_engine *e) {
     dfree(e->d_gcounter);
     dfree(e->d_partial);
     dfree(e->d_counter);
-    dfree(e->d_out);
+    e->d_out = nullptr; // inside h_out
     dfree(e->d_chunks);
     e->chunk_cap = 0;
     dfree(e->d_toy_chunk0);
@@ -323,7 +323,6 @@ int buildLayout(gf_engine *e) {
     chk(dalloc(e, e->d_gpartial, (size_t)NT * std::max(1, NQ) * std::max(1, e->plan.max_grid_blocks) * NGp));
     chk(dalloc(e, e->d_gcounter, (size_t)NT * std::max(1, NQ)));
     chk(dalloc(e, e->d_counter, NT));
-    chk(dalloc(e, e->d_out, (size_t)NT * (NGp + 2)));
     chk(dalloc(e, e->d_toy_chunk0, NT));
     chk(dalloc(e, e->d_toy_nchunks, NT));
     chk(dalloc(e, e->d_toy_nevents, NT));
@@ -384,9 +383,13 @@ int buildLayout(gf_engine *e) {
         if(!g.empty())
             cudaMemcpy(e->d_dgrid, g.data(), sizeof(unsigned) * g.size(), cudaMemcpyHostToDevice);
     }
+    // results: the event kernel's finishing CTA stores them straight into mapped page-locked memory (no
+    // copy back at the end of each evaluation)
     if(cudaMallocHost((void **)&e->h_P, e->pblock_bytes) != cudaSuccess ||
-       cudaMallocHost((void **)&e->h_out, sizeof(double) * (size_t)NT * (NGp + 2)) != cudaSuccess)
+       cudaHostAlloc((void **)&e->h_out, sizeof(double) * (size_t)NT * (NGp + 2), cudaHostAllocMapped) != cudaSuccess ||
+       cudaHostGetDevicePointer((void **)&e->d_out, e->h_out, 0) != cudaSuccess)
         return gf_fail(e, GF_ERR_OOM, "cudaMallocHost");
+    std::memset(e->h_out, 0, sizeof(double) * (size_t)NT * (NGp + 2));
     std::memset(e->h_P, 0, e->pblock_bytes);
     e->h_active = reinterpret_cast<int *>(reinterpret_cast<char *>(e->h_P) + e->active_off);
     e->host_flag.assign(NT, 0);
@@ -552,9 +555,6 @@ cudaError_t enqueueEval(gf_engine *e, bool grad) {
     if(r == cudaSuccess)
         r = launch(grad ? e->mod.evt_g : e->mod.evt_n, dim3(evtGrid(e)), dim3(e->block),
                    grad ? e->plan.evt_smem_grad : e->plan.evt_smem_nograd, e->stream, a, kernelLast && e->use_pdl);
-    if(r == cudaSuccess)
-        r = cudaMemcpyAsync(e->h_out, e->d_out, sizeof(double) * (size_t)NT * (NGp + 2), cudaMemcpyDeviceToHost,
-                            e->stream);
     if(r == cudaSuccess)
         r = recordEvent(e, e->ev[3]);
     return r;
