@@ -2483,12 +2483,28 @@ struct Gen {
                 os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(reinterpret_cast<const R2 *>("
                    << p0ptr("a.acol", NA, ac, NO + NC) << ") + i0));\n";
         os << "      }\n    }\n  }\n";
+        // one toy: its parameters and activity flag (written by the host, possibly read in place from
+        // page-locked memory) are read once per CTA before the wait, the normalisation factors once after it
+        if(!batch) {
+            os << "  const int toy1 = 0;\n";
+            os << "  const bool toy_on1 = !a.active || a.active[toy1];\n";
+            os << "  const R *Pr1 = reinterpret_cast<const R *>(a.Pr); (void)Pr1;\n";
+            for(int j = 0; j < T.n_params; ++j)
+                os << "  const R p" << j << " = Pr1[" << j << "]; (void)p" << j << ";\n";
+        }
         os << "  gf_pdl_wait();\n";
         os << "  __syncthreads();\n";
+        if(!batch) {
+            os << "  const int toy = toy1;\n  const R *Pr = Pr1; (void)Pr;\n";
+            emitNormReads(os, T, grad, plan.nl, "  ");
+        }
         os << "  for(int ch = cb; ch < ce; ++ch) {\n";
         os << "    int toy; i64 b0, e0; gf_chunk(a, ch, toy, b0, e0);\n";
         // the activity flag is read beside the parameters (independent loads), the branch comes after them
-        os << "    const bool toy_on = !a.active || a.active[toy];\n";
+        if(batch)
+            os << "    const bool toy_on = !a.active || a.active[toy];\n";
+        else
+            os << "    const bool toy_on = toy_on1;\n";
         if(NC > 0 && ctabL1) {
             // the toy's tables are read through L1 (read-only loads): every CTA on an SM shares one copy
             os << "    const R *ttab = reinterpret_cast<const R *>(a.ctab) + (i64)toy * " << ctabTotal << ";\n";
@@ -2510,8 +2526,10 @@ struct Gen {
             os << "      __syncthreads();\n";
             os << "    }\n";
         }
-        emitParamsR(os, T, plan.nl, "    ");
-        emitNormReads(os, T, grad, plan.nl, "    ");
+        if(batch) {
+            emitParamsR(os, T, plan.nl, "    ");
+            emitNormReads(os, T, grad, plan.nl, "    ");
+        }
         if(T.fit_metric != GF_FIT_UNBINNED_NLL && !values)
             os << "    const R Tn = (R)a.toy_nevents[toy]; // c_totalEvents: the number of bins\n";
         for(int o = 0; o < NO; ++o)

@@ -1315,8 +1315,11 @@ int gf_engine_create(gf_engine **out, int device, int precision) {
         e->chunk       = std::max(256, (atoi(c) / 256) * 256);
         e->chunk_fixed = true;
     }
+    // programmatic dependent launch chains the mixed engine's kernels (C2 FCN 32.3 -> 30.0 us); in the FP64
+    // engine the early-resident event CTAs slowed the chain instead (C2 FCN 193 -> 455 us), so it is off there
+    e->use_pdl = precision == GF_MIXED;
     if(const char *p = std::getenv("GF_NO_PDL"))
-        e->use_pdl = !(p[0] == '1');
+        e->use_pdl = e->use_pdl && !(p[0] == '1');
     if(const char *c = std::getenv("GF_EVT_CTAS_PER_SM")) {
         e->evt_ctas_per_sm   = std::max(1, atoi(c));
         e->evt_ctas_fixed    = true;
