@@ -161,7 +161,10 @@ int gf_set_fit_metric(gf_engine *eng, int fit_metric);
 /* Number of independent datasets ("toys"), each with its own parameter vector. */
 int gf_set_num_toys(gf_engine *eng, int n_toys);
 
-/* Events of one toy as SoA FP64 columns: soa[o * n_events + e]. */
+/* Events of one toy as SoA FP64 columns: soa[o * n_events + e] (replaces PdfBase::setData,
+ * src/PDFs/PdfBase.cu:329-438).  Page-locked host memory is read in place by the conversion kernel; other
+ * host memory is staged through a device buffer.  Returns when the device columns are ready;
+ * GF_ERR_INVALID when an event lies outside a ConvolutionPdf's table range. */
 int gf_upload_events(gf_engine *eng, int toy, const double *soa, int64_t n_events);
 
 /* ---- evaluation: FCN::operator() + GooPdf::calculateNLL ---- */
