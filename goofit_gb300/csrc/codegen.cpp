@@ -571,7 +571,28 @@ __device__ __forceinline__ ACC acc_pair(float hi, float lo) { return make_float2
 // a b as an unevaluated pair (the product and its exact rounding error)
 __device__ __forceinline__ ACC gf_two_prod(float a, float b) { const float p = a * b; return make_float2(p, fmaf(a, b, -p)); }
 // 1/x rounded to nearest (the same value as the IEEE division 1.0f / x)
-__device__ __forceinline__ float gf_rcp(float x) { return __frcp_rn(x); }
+// 1/x: the hardware reciprocal approximation refined by one Newton-Raphson step r + r (1 - x r)
+__device__ __forceinline__ float gf_rcp(float x) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return fmaf(r, fmaf(-x, r, 1.0f), r);
+}
+// -log of a product of event probabilities: x = m 2^e with m in [0.75, 1.5) (exact bit operations), the
+// mantissas multiplied into lm (8 of them stay within [0.1, 26)) and the exponents added into le; zero,
+// subnormal, infinite and NaN x are added to av directly.  The caller adds -(log lm + le ln 2), with ln 2
+// split after Cody and Waite into GF_LN2_HI (13 significant bits: le * GF_LN2_HI is exact for |le| < 2^11)
+// and GF_LN2_LO = ln 2 - GF_LN2_HI.
+#define GF_LN2_HI 0.693115234375f
+#define GF_LN2_LO 3.1946183e-05f
+__device__ __forceinline__ void gf_log_acc(float x, float &lm, int &le, float &av) {
+    const int b = __float_as_int(x);
+    if((unsigned)(b - 0x00800000) < 0x7F000000u) {
+        const int e = (b - 0x3F400000) >> 23;
+        lm *= __int_as_float(b - (e << 23));
+        le += e;
+    } else
+        av -= logf(x);
+}
 __device__ __forceinline__ ACC acc_add(ACC a, ACC b) {
     float s, e;
     gf_two_sum(a.x, b.x, s, e);
@@ -2590,10 +2611,15 @@ struct Gen {
                    << "b = *reinterpret_cast<const int4 *>(kc" << ci << " + i1 + 4);\n";
             os << "        }\n      }\n";
         }
+        // FP32 one-toy/batch kernels with 8 events per iteration take one log per iteration, of the product
+        // of its events' probabilities (gf_log_acc); the amplitude kernels' 2-event iterations keep one per event
+        const bool logProd = mixed && !values && VEC == 8;
         if(!values) {
             os << "      R av = R(0);\n";
             for(int s = 0; s < NGp - 1; ++s)
                 os << "      R ag" << s << " = R(0);\n";
+            if(logProd)
+                os << "      float lm = 1.0f; int le = 0;\n";
         }
         // events of this iteration inside the chunk: a 32-bit bound per event instead of a 64-bit one
         os << "      const int jn = e0 - i0 < " << VEC << " ? (int)(e0 - i0) : " << VEC << ";\n";
@@ -2739,7 +2765,10 @@ struct Gen {
                     // -log(P N) = -log P - log N: the event pass sums -log P and -dP/P and counts the events
                     // with P > 0; the host adds count * (-log N) and count * (-dN/N) in FP64
                     os << "        if(j < jn && " << root.v << " > R(0)) {\n";
-                    os << "          av -= GF_LOG(" << root.v << ");\n";
+                    if(logProd)
+                        os << "          gf_log_acc(" << root.v << ", lm, le, av);\n";
+                    else
+                        os << "          av -= GF_LOG(" << root.v << ");\n";
                     os << "          nv += R(1);\n";
                     if(grad && T.NG > 0) {
                         if(c.ampRoot) {
@@ -2764,7 +2793,10 @@ struct Gen {
                     break;
                 }
                 os << "        if(j < jn && pv > R(0)) {\n";
-                os << "          av -= GF_LOG(pv);\n";
+                if(logProd)
+                    os << "          gf_log_acc(pv, lm, le, av);\n";
+                else
+                    os << "          av -= GF_LOG(pv);\n";
                 if(grad && T.NG > 0) {
                     os << "          const R inv = gf_rcp(pv);\n";
                     for(int s = 0; s < T.NG; ++s) {
@@ -2778,6 +2810,10 @@ struct Gen {
         }
         os << "        }\n      }\n";
         if(!values) {
+            if(logProd) {
+                os << "      av -= logf(lm) + (float)le * GF_LN2_LO;\n";
+                os << "      gf_comp_add(avh, avl, (float)(-le) * GF_LN2_HI);\n";
+            }
             os << "      gf_comp_add(avh, avl, av);\n";
             // gradient sums are compensated where it is cheap (8 events per iteration) or many events per
             // thread are expected (batches of toys); the amplitude kernels' 2-event iterations add them plainly
