@@ -2475,8 +2475,12 @@ struct Gen {
                            (T.nk[0] == NK_EXP || T.nk[0] == NK_GAUSS || T.nk[0] == NK_AMP3 || T.nk[0] == NK_AMP4);
 
         // at least two CTAs per SM: the register cap (128 at 256 threads) keeps the amplitude event kernels
-        // at two resident CTAs instead of one
-        os << "extern \"C\" __global__ void __launch_bounds__(" << block << ", 2) " << name << "(const GfArgs a) {\n";
+        // at two resident CTAs instead of one.  FP32 batch kernels with 8 events per iteration: four (58
+        // registers, no spills; 1024 toys of the composite model: event kernel 0.086 -> 0.068 ms); the one-toy
+        // kernel stays at two (three or four made the 2e6-event FCN 0.5 / 3 us slower)
+        const int minBlocks = (VEC == 8 && mixed && batch) ? 4 : 2;
+        os << "extern \"C\" __global__ void __launch_bounds__(" << block << ", " << minBlocks << ") " << name
+           << "(const GfArgs a) {\n";
         os << "  extern __shared__ __align__(16) unsigned char smraw[];\n";
         os << "  R *stab = reinterpret_cast<R *>(smraw); (void)stab;\n";
         os << "  __shared__ int s_toy, last;\n";
