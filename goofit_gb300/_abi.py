@@ -164,6 +164,8 @@ SIGNATURES = [
                                       _i32p, C.c_int, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
     ("gf_compile_tree", C.c_int, [C.POINTER(gf_node), C.c_int, C.POINTER(gf_observable), C.c_int, C.c_int,
                                   _i32p, C.c_int, C.POINTER(C.c_int64)]),
+    ("gf_compile_tree_batch", C.c_int, [C.POINTER(gf_node), C.c_int, C.POINTER(gf_observable), C.c_int, C.c_int,
+                                        _i32p, C.c_int, C.POINTER(C.c_int64)]),
 ]
 
 _lib = None

@@ -2012,15 +2012,15 @@ int gf_generated_source(const gf_node *nodes, int n_nodes, const gf_observable *
     return GF_OK;
 }
 
-int gf_compile_tree(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
-                    const int32_t *grad_mask, int precision, int64_t *cubin_bytes) {
+static int compileTreeShaped(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
+                             const int32_t *grad_mask, int precision, bool batch, int64_t *cubin_bytes) {
     gf::Tree t;
     std::string why = t.build(nodes, n_nodes, obs, n_obs, n_params, grad_mask);
     if(!why.empty())
         return gf_fail(nullptr, GF_ERR_BAD_TREE, why);
     gf::KernelPlan p;
     try {
-        p = gf::generate_kernels(t, precision == GF_MIXED, 256, false);
+        p = gf::generate_kernels(t, precision == GF_MIXED, 256, batch);
     } catch(std::exception &ex) {
         return gf_fail(nullptr, GF_ERR_BAD_TREE, ex.what());
     }
@@ -2031,6 +2031,16 @@ int gf_compile_tree(const gf_node *nodes, int n_nodes, const gf_observable *obs,
     if(cubin_bytes)
         *cubin_bytes = (int64_t)cubin.size();
     return GF_OK;
+}
+
+int gf_compile_tree(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
+                    const int32_t *grad_mask, int precision, int64_t *cubin_bytes) {
+    return compileTreeShaped(nodes, n_nodes, obs, n_obs, n_params, grad_mask, precision, false, cubin_bytes);
+}
+
+int gf_compile_tree_batch(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
+                          const int32_t *grad_mask, int precision, int64_t *cubin_bytes) {
+    return compileTreeShaped(nodes, n_nodes, obs, n_obs, n_params, grad_mask, precision, true, cubin_bytes);
 }
 
 } // extern "C"

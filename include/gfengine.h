@@ -316,6 +316,9 @@ int gf_generated_source(const gf_node *nodes, int n_nodes, const gf_observable *
 /* Compiles a tree's kernels for sm_103a without loading them; *cubin_bytes gets the image size. */
 int gf_compile_tree(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
                     const int32_t *grad_mask, int precision, int64_t *cubin_bytes);
+/* The same for the kernel shapes an engine uses with more than one toy (gf_set_num_toys > 1). */
+int gf_compile_tree_batch(const gf_node *nodes, int n_nodes, const gf_observable *obs, int n_obs, int n_params,
+                          const int32_t *grad_mask, int precision, int64_t *cubin_bytes);
 
 #ifdef __cplusplus
 }

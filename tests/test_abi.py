@@ -43,9 +43,12 @@ def _tree(pdf):
     return nodes, olist, params, mask
 
 
+@pytest.mark.parametrize("batch", [False, True])
 @pytest.mark.parametrize("prec", [A.GF_MIXED, A.GF_FP64])
 @pytest.mark.parametrize("which", ["c1", "c2", "c3"])
-def test_generated_kernels_compile_for_sm103a(which, prec):
+def test_generated_kernels_compile_for_sm103a(which, prec, batch):
+    """NVRTC compiles the kernels of every workload tree for sm_103a, in the one-toy and the toy-batch
+    shapes (different table, grid and event kernels), without a device."""
     if which == "c3":
         pdf = W.c3_model(1500)[0]
     else:
@@ -58,7 +61,8 @@ def test_generated_kernels_compile_for_sm103a(which, prec):
     L = A.lib()
     rc = L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, prec, None, 0, C.byref(n))
     assert rc == 0 and n.value > 1000
-    rc = L.gf_compile_tree(nl.arr, nl.n, obs, len(olist), len(params), mp, prec, C.byref(n))
+    compile_tree = L.gf_compile_tree_batch if batch else L.gf_compile_tree
+    rc = compile_tree(nl.arr, nl.n, obs, len(olist), len(params), mp, prec, C.byref(n))
     assert rc == 0, L.gf_last_error(None)
     assert n.value > 10000
 
