@@ -194,8 +194,6 @@ void freeModule(gf_engine *e) {
     e->mod = GfModule();
 }
 
-int nGradOf(const gf_engine *e) { return e->tree.NG; }
-
 template <typename T>
 int dalloc(gf_engine *e, T *&p, size_t count, bool zero = true) {
     size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
@@ -542,9 +540,7 @@ cudaError_t recordEvent(gf_engine *e, cudaEvent_t ev) {
 }
 
 cudaError_t enqueueEval(gf_engine *e, bool grad) {
-    const gf::Tree &T = e->tree;
-    const int NT = e->n_toys, NGp = 1 + T.NG;
-    GfArgs a         = makeArgs(e);
+    GfArgs a = makeArgs(e);
     // qflag is zero between evaluations: the event kernel's finisher clears it after reading it
     cudaError_t r = recordEvent(e, e->ev[0]);
     // one toy: the kernels read the parameter block from page-locked host memory in place (no copy
