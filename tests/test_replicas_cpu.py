@@ -1,6 +1,6 @@
-"""Replica runs of bench.py (one process per GPU, no data-path collective): the timing reduction across
-ranks, exercised with two CPU ranks over gloo, and the reference arm's rank rule (rank 0 alone measures and
-prints; the other ranks exit 0 without work)."""
+"""bench.py host logic without a GPU: replica runs (one process per GPU, no data-path collective) with the
+timing reduction across ranks exercised by two CPU ranks over gloo; the reference arm's rank rule (rank 0
+alone measures and prints; the other ranks exit 0 without work) and its JSON line."""
 import os
 import socket
 import subprocess
@@ -55,3 +55,26 @@ def test_reference_arm_prints_only_on_rank_zero():
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 0
     assert r.stdout.strip() == ""
+
+
+def test_reference_arm_json_line_contract():
+    """The reference arm (FP64 restatement of the reference's CPU path on the host cores) prints one JSON
+    line with the engine arm's metric and unit, its own cpu_baseline and an e2e entry without copies."""
+    import json
+
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "3", "--warmup", "3",
+                        "--ref-sample", "3000"], env=env, cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == "event-NLL evals/s"
+    assert d["steps"] == 3 and d["warmup"] == 3 and d["higher_is_better"] is True and d["value"] > 0
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["kind"] == "port"
+    assert d["cpu_baseline"]["cores"] >= 1 and "3000 events" in d["cpu_baseline"]["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"] == bench.WORKLOAD
