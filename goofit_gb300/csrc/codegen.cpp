@@ -570,8 +570,8 @@ __device__ __forceinline__ ACC acc_of(float v) { return make_float2(v, 0.f); }
 __device__ __forceinline__ ACC acc_pair(float hi, float lo) { return make_float2(hi, lo); }
 // a b as an unevaluated pair (the product and its exact rounding error)
 __device__ __forceinline__ ACC gf_two_prod(float a, float b) { const float p = a * b; return make_float2(p, fmaf(a, b, -p)); }
-// 1/x rounded to nearest (the same value as the IEEE division 1.0f / x)
-// 1/x: the hardware reciprocal approximation refined by one Newton-Raphson step r + r (1 - x r)
+// 1/x: the hardware reciprocal approximation refined by one Newton-Raphson step r + r (1 - x r); not
+// guaranteed to be correctly rounded (the generated kernels use it where 1/P feeds gradient sums)
 __device__ __forceinline__ float gf_rcp(float x) {
     float r;
     asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));

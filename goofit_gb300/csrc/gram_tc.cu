@@ -21,10 +21,11 @@
 // cross terms hi.lo + lo.hi, 2^-11 smaller, accumulate in a third accumulator over the CTA's points.  The
 // CTAs' partials are summed in FP64 by gf_gram_tc_sum.
 //
-// Pipeline per CTA (128 threads, one elected thread issues the MMAs): two shared-memory stages; the
-// threads load stage t+1 from HBM, split it and store it in the canonical no-swizzle K-major layout
-// while the tensor core works on stage t; tcgen05.commit arrives on the stage's mbarrier when its MMAs
-// have read it.  Every wait is bounded: a wait that runs out sets *err and the CTA stops issuing work,
+// Pipeline per CTA (256 threads, one elected thread issues the MMAs): cp.async 16-byte copies fill a
+// three-slot ring of raw (unsplit) stages two stages ahead; the threads split the oldest raw stage and
+// store it into one of two operand stages in the canonical no-swizzle K-major layout while the tensor
+// core works on the other; tcgen05.commit arrives on the operand stage's mbarrier when its MMAs have
+// read it.  Every wait is bounded: a wait that runs out sets *err and the CTA stops issuing work,
 // waits (bounded) for what it issued, frees its tensor memory and returns.
 #include <cuda_runtime.h>
 

@@ -280,12 +280,13 @@ int gf_fit_batch(gf_engine *eng, int n_toys, const gf_fit_options *opt, const do
  * analytic normalisation over [lo, hi] for n_events FP32 values x (device
  * memory), writing out[0] = NLL and out[1] = dNLL/dalpha (device memory, two
  * doubles).  Allocates nothing: its reduction scratch is a fixed device array
- * inside the library (16 KB per device, kept until exit) that limits a call to
- * 8,388,608 events; larger counts return GF_ERR_INVALID.  The first call on a
+ * inside the library (24 KB per device, kept until exit) that limits a call to
+ * 8,388,608 events; larger counts return GF_ERR_INVALID, and so does an alpha
+ * whose normalisation integral is not finite and positive.  The first call on a
  * device looks up that array's device address (make that first call before any
  * stream capture).  All calls share the array, so calls that overlap on the
  * GPU (other streams, other host threads) race: order them on one stream.
- * Asynchronous: errors that only the device can see (NaN) show in out[].
+ * Asynchronous: errors that only the device can see (NaN events) show in out[].
  * gf_noalloc_last_error() describes the last failure of this entry point. */
 int gf_nll_exp_noalloc(const float *x, int64_t n_events, double alpha, double lo, double hi, double *out,
                        void *stream);
