@@ -147,6 +147,7 @@ SIGNATURES = [
     ("gf_last_timing", C.c_int, [_vp, _f64p, _f64p]),
     ("gf_launches_per_eval", C.c_int, [_vp, C.c_int]),
     ("gf_event_chunk", C.c_int64, [_vp]),
+    ("gf_set_wait_limit", C.c_int, [_vp, C.c_uint64]),
     ("gf_time_kernels", C.c_int, [_vp, C.c_int, C.c_int, _f64p, _f64p, _f64p]),
     ("gf_minimizer_create", C.c_int, [C.POINTER(_vp), C.c_int, _f64p, _f64p, _f64p, _f64p, _i32p, _i32p,
                                       C.c_double, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double]),

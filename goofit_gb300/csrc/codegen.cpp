@@ -501,6 +501,14 @@ struct GfArgs {
     int gtoy;                  /* toy of the normalisation pass */
     i64 chunk;                 /* events per chunk */
     i64 nevt0;                 /* events of toy 0 */
+    unsigned *gbar;            /* grid barrier of the one-launch evaluation: [arrivals, generation, error] */
+    unsigned long long bar_ns; /* longest wait at that barrier (%globaltimer ns) before the kernel gives up */
+    int rec_n;                 /* one-launch evaluation: the toy's record passed by value in rec (R values) */
+    int stage_off;             /* one-launch evaluation: shared-memory offset of the CTA's staged events */
+    unsigned stage_cap;        /* and the bytes available there (0: events are read from global memory) */
+    int stage_pad;
+    double *hpart;             /* one-launch evaluation: per chunk [components..., status] in page-locked host memory */
+    alignas(16) unsigned char rec[512];
     const void *p0[192];       /* one toy: its observable, bin-offset and amplitude columns, no table lookup */
 };
 
@@ -525,10 +533,75 @@ __device__ __forceinline__ double gf_warp_sum(double v) {
     return v;
 }
 
+// The toy records the kernels read their parameters from: the argument block's (host-written) records in
+// the kernels, a shared-memory copy in the bodies the one-launch kernel calls.
+#define GF_PR a.Pr
+
 // Programmatic dependent launch: let the next kernel of the evaluation start its independent prologue,
 // and wait for the previous kernel's results (both are no-ops without a programmatic dependency).
 __device__ __forceinline__ void gf_pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void gf_pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Barrier over all CTAs of a cooperative launch (every CTA resident), bounded in time: thread 0 of each CTA
+// arrives on bar[0]; the last to arrive resets it and advances the generation bar[1]; the others wait for
+// the generation to move, at most `limit` ns of %globaltimer.  A wait that runs out sets bar[2] and makes
+// every thread of the CTA see false, so that the CTA stops (the host then reports the evaluation as failed
+// and clears the barrier words); no CTA gets past a barrier that not every CTA reached.
+__device__ __forceinline__ unsigned long long gf_globaltimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __noinline__ bool gf_grid_sync(unsigned *bar, unsigned long long limit) {
+    __shared__ int ok;
+    __syncthreads();
+    if(threadIdx.x == 0) {
+        int good = 1;
+        unsigned gen;
+        asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(gen) : "l"(bar + 1) : "memory");
+        // the arrival releases the CTA's writes (ordered before it by the __syncthreads above) and acquires
+        // the earlier arrivals' ones; the generation is released by the last arrival and acquired by the
+        // waiters, so every CTA sees every CTA's writes from before the barrier
+        unsigned prev;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(prev) : "l"(bar) : "memory");
+        if(prev == gridDim.x * gridDim.y * gridDim.z - 1) {
+            asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" :: "l"(bar) : "memory");
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" :: "l"(bar + 1) : "memory");
+        } else {
+            const unsigned long long t0 = gf_globaltimer();
+            for(;;) {
+                unsigned g;
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(bar + 1) : "memory");
+                if(g != gen)
+                    break;
+                if(gf_globaltimer() - t0 > limit) {
+                    atomicOr(bar + 2, 1u);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(20);
+            }
+        }
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Shared-memory mbarrier of a bulk copy (cp.async.bulk, the TMA unit): a wait that gives up after `limit` ns.
+__device__ __forceinline__ bool gf_mbar_wait(unsigned long long *mbar, unsigned parity, unsigned long long limit) {
+    const unsigned addr = (unsigned)__cvta_generic_to_shared(mbar);
+    const unsigned long long t0 = gf_globaltimer();
+    for(;;) {
+        unsigned done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n" : "=r"(done) : "r"(addr), "r"(parity) : "memory");
+        if(done)
+            return true;
+        if(gf_globaltimer() - t0 > limit)
+            return false;
+    }
+}
 
 // Bin centre lo + w (b + 1/2) with w = (hi - lo) / n from the host: the binned MetricTaker's
 // arithmetic (src/PDFs/MetricTaker.cu:76-82) with its two roundings kept separate.
@@ -1336,7 +1409,7 @@ NormLayout computeNormLayout(const Tree &T) {
 
 // Parameters (type R) of the toy from its record.
 void emitParamsR(std::ostream &os, const Tree &T, const NormLayout &nl, const char *ind) {
-    os << ind << "const R *Pr = reinterpret_cast<const R *>(a.Pr) + (i64)toy * " << nl.npr << "; (void)Pr;\n";
+    os << ind << "const R *Pr = reinterpret_cast<const R *>(GF_PR) + (i64)toy * " << nl.npr << "; (void)Pr;\n";
     for(int j = 0; j < T.n_params; ++j)
         os << ind << "const R p" << j << " = Pr[" << j << "]; (void)p" << j << ";\n";
 }
@@ -1409,6 +1482,12 @@ void emitCtaReduce(std::ostream &os, const std::vector<std::string> &vals, const
 
 // convolution tables in the event pass: staged in shared memory per CTA (default) or read through L1
 // (GF_CTAB=l1)
+// GF_EVT_TAB=0: the one-launch kernel evaluates the event function per event even where it could tabulate it
+bool tabDisabled() {
+    const char *v = std::getenv("GF_EVT_TAB");
+    return v && v[0] == '0';
+}
+
 bool ctabThroughL1() {
     const char *v = std::getenv("GF_CTAB");
     return v && std::string(v) == "l1";
@@ -1499,9 +1578,10 @@ struct Gen {
         plan.grid_needs_conv = false;
         for(int q = 0; q < NQ; ++q) {
             const NumInfo &g = T.nums[q];
-            // batches only: for one toy the fold's finishing chain lengthens the table kernel by about what
-            // the grid kernel takes, so the serial grid launch is as fast
-            bool fold = batch && T.nodes[g.node].op == GF_OP_CONVOLUTION && g.obs.size() == 1 &&
+            // one toy and batches: the one-launch evaluation then needs no barrier between tables and grids
+            // (with separate launches for one toy the fold's finishing chain lengthens the table kernel by
+            // about what the grid launch takes)
+            bool fold = T.nodes[g.node].op == GF_OP_CONVOLUTION && g.obs.size() == 1 &&
                         g.convs.size() == 1 && g.convs[0] == T.conv_of[g.node] && plan.conv_fold_q[g.convs[0]] < 0;
             if(fold)
                 for(auto &d : plan.nl.qdN[q]) {
@@ -1556,7 +1636,26 @@ struct Gen {
     // thread owns KT consecutive k of one component over a contiguous slice of m (MS slices per k-tile),
     // keeping a sliding window of the resolution values in registers (KT FMAs per two shared loads).
     // The MS lane partials are combined with a compensated (two-sum) shuffle reduction.
-    void convKernel(bool grad) {
+    // Kernel header, or (body) the same code as a device function over a virtual block index, which the
+    // one-launch evaluation kernel calls: blockIdx / gridDim stand for the function's arguments and the
+    // record pointer for its shared-memory copy until endBody() closes it.
+    void kernelHead(const std::string &name, const std::string &bounds, bool body, const std::string &extra = "") {
+        if(!body) {
+            os << "extern \"C\" __global__ void __launch_bounds__(" << bounds << ") " << name << "(const GfArgs a) {\n";
+            return;
+        }
+        os << "#define blockIdx gf_bid\n#define gridDim gf_gdim\n#undef GF_PR\n#define GF_PR gf_pr\n";
+        os << "__device__ __forceinline__ void " << name
+           << "_body(const GfArgs &a, const uint3 gf_bid, const uint3 gf_gdim, const void *gf_pr" << extra << ") {\n";
+    }
+    void endBody(bool body) {
+        if(body)
+            os << "#undef blockIdx\n#undef gridDim\n#undef GF_PR\n#define GF_PR a.Pr\n";
+    }
+
+    // foldPartials: a folded grid sum leaves only its per-CTA partials (the one-launch kernel's CTAs sum
+    // them after its barrier), without the completion counter and finishing CTA
+    void convKernel(bool grad, bool body = false, bool foldPartials = false) {
         const char *sfx = grad ? "g" : "n";
         const int NC    = (int)T.convs.size();
         if(NC == 0)
@@ -1582,7 +1681,7 @@ struct Gen {
         (grad ? plan.conv_smem_grad : plan.conv_smem_nograd) = smem;
         plan.conv_blocks = std::max(plan.conv_blocks, maxBlocks);
 
-        if(grad)
+        if(grad && !body)
             for(int ci = 0; ci < NC; ++ci) {
                 const int q = plan.conv_fold_q[ci];
                 if(q < 0)
@@ -1602,8 +1701,7 @@ struct Gen {
                     os << (k ? "," : "") << cnt[k];
                 os << "};\n";
             }
-        os << "extern \"C\" __global__ void __launch_bounds__(" << block << ") gf_conv_" << sfx
-           << "(const GfArgs a) {\n";
+        kernelHead(std::string("gf_conv_") + sfx, std::to_string(block), body);
         os << "  extern __shared__ __align__(16) unsigned char smraw[];\n";
         os << "  R *sm = reinterpret_cast<R *>(smraw);\n";
         os << "  const int toy = blockIdx.y; const int ci = blockIdx.z; const int tid = threadIdx.x;\n";
@@ -1795,18 +1893,19 @@ struct Gen {
             os << "    }\n";
             os << "    }\n"; // kp
             if(fq >= 0)
-                emitConvFold(ci, fq, grad, comps, ktiles, MS, KB);
+                emitConvFold(ci, fq, grad, comps, ktiles, MS, KB, foldPartials);
             os << "    break; }\n";
         }
         os << "  }\n";
         os << "  gf_pdl_wait();\n";
         os << "}\n\n";
+        endBody(body);
     }
 
     // The folded grid sum of numeric node q in the conv kernel: the CTA's sums of n_k T_comp[k] into the
     // grid partials (component slot: 0 value, 1 + gradient slot), then the last CTA of (toy, q) sums the
     // partials and finishes the node's normalisation.
-    void emitConvFold(int ci, int q, bool grad, int comps, int ktiles, int MS, int KB) {
+    void emitConvFold(int ci, int q, bool grad, int comps, int ktiles, int MS, int KB, bool partialsOnly = false) {
         const ConvInfo &cv = T.convs[ci];
         const int NQ = (int)T.nums.size(), NGs = 1 + T.NG, NGp = 1 + (grad ? T.NG : 0), NW = block / 32;
         const int MGB = plan.max_grid_blocks, nblk = (cv.nK + KB - 1) / KB;
@@ -1825,6 +1924,10 @@ struct Gen {
         os << "      if(tid < " << comps << ") { ACC t = acc_zero(); for(int kk = 0; kk < " << ktiles
            << "; ++kk) t = acc_add(t, fsh[kk * " << comps << " + tid]); gp[(i64)cs[tid] * " << MGB
            << " + blockIdx.x] = t; }\n";
+        if(partialsOnly) {
+            os << "    }\n";
+            return;
+        }
         os << "      __threadfence();\n      __syncthreads();\n";
         os << "      if(tid == 0) { unsigned prev = atomicAdd(&a.gcounter[toy * " << NQ << " + " << q
            << "], 1u); flast = (prev == " << nblk - 1 << "u); }\n";
@@ -1851,7 +1954,7 @@ struct Gen {
     // One CTA row per numeric node; the finishing CTA of a (toy, node) turns the grid sum into the node's
     // normalisation factor and its derivatives (GooPdf::normalize numeric branch,
     // src/PDFs/GooPdf.cu:366-395) and stores them for the event pass.
-    void gridKernel(bool grad) {
+    void gridKernel(bool grad, bool body = false) {
         const char *sfx = grad ? "g" : "n";
         const int NQ    = (int)T.nums.size();
         if(NQ == 0)
@@ -1864,8 +1967,7 @@ struct Gen {
         auto &off               = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
         auto &cps               = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
         const NormLayout &nl    = plan.nl;
-        os << "extern \"C\" __global__ void __launch_bounds__(" << block << ") gf_grid_" << sfx
-           << "(const GfArgs a) {\n";
+        kernelHead(std::string("gf_grid_") + sfx, std::to_string(block), body);
         os << "  const int toy = blockIdx.y; const int q = blockIdx.z; const int tid = threadIdx.x;\n";
         os << "  const int lane = tid & 31, wid = tid >> 5;\n";
         os << "  gf_pdl_trigger();\n";
@@ -1984,6 +2086,7 @@ struct Gen {
         }
         os << "    default: break;\n";
         os << "    }\n  }\n}\n\n";
+        endBody(body);
     }
 
     // ---------------- Amp3Body amplitude caches and integrals ----------------
@@ -2410,7 +2513,11 @@ struct Gen {
     // Persistent CTAs take contiguous ranges of the chunk list and stage a toy's conv tables once; each
     // thread streams 8 events per iteration with 16-byte loads.  Partial sums: FP32 per thread, then
     // compensated FP32 pairs across the warp, the CTA, the chunks of a toy; FP64 for the final value.
-    void eventKernel(bool grad, bool values) {
+    // asBody: the same event pass as a device function of the one-launch kernel.  tab (one toy, an event
+    // function that depends on the event only through one convolution's bin offset k): each CTA first
+    // tabulates the per-event terms -log P and -dP/P over the table's k range in shared memory, and the
+    // event loop gathers and adds them
+    void eventKernel(bool grad, bool values, bool asBody = false, bool tab = false) {
         const std::string name = values ? "gf_val_n" : (grad ? "gf_evt_g" : "gf_evt_n");
         const int NGp = 1 + (grad ? T.NG : 0);
         const int NGs = 1 + T.NG;
@@ -2424,8 +2531,9 @@ struct Gen {
         auto &off     = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
         auto &cps     = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
         const int64_t ctabTotal = grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd;
-        if(!values)
+        if(!values && !asBody)
             (grad ? plan.evt_smem_grad : plan.evt_smem_nograd) = ctabL1 ? 0 : (size_t)ctabTotal * (mixed ? 4 : 8);
+        bodySmem = ctabL1 ? 0 : (size_t)ctabTotal * (mixed ? 4 : 8);
 
         std::vector<int> xused(NO, 0);
         std::ostringstream body;
@@ -2473,14 +2581,36 @@ struct Gen {
                                 (T.nk[0] == NK_EXP || T.nk[0] == NK_GAUSS || T.nk[0] == NK_AMP3 || T.nk[0] == NK_AMP4);
         plan.factor_root = T.fit_metric == GF_FIT_UNBINNED_NLL &&
                            (T.nk[0] == NK_EXP || T.nk[0] == NK_GAUSS || T.nk[0] == NK_AMP3 || T.nk[0] == NK_AMP4);
+        // tabulated terms per k: [-log P, -dP/P per gradient slot, (factored root) 1 if P > 0], kept in
+        // blocks of 16 bytes (4 FP32 / 2 FP64 terms), each block its own array over k, the remainder in a
+        // narrower array, so that an event's gather reads no padding (C2: 16 + 4 bytes)
+        const int tabComps = NGp + (factorRoot ? 1 : 0);
+        const int vw = mixed ? 4 : 2;
+        std::vector<int> bw, boff; // per block: width (terms) and offset (elements) in ltab
+        int LP = 0;
+        for(int q0 = 0; q0 < tabComps; q0 += vw) {
+            int w = std::min(vw, tabComps - q0);
+            if(w == 3)
+                w = 4;
+            bw.push_back(w);
+            boff.push_back(LP * (tab ? T.convs[0].nK : 0));
+            LP += w;
+        }
+        if(tab)
+            bodySmem = (size_t)T.convs[0].nK * LP * (mixed ? 4 : 8);
+        auto vtype = [&](int w) -> std::string {
+            return mixed ? (w == 4 ? "float4" : w == 2 ? "float2" : "float") : (w == 2 ? "double2" : "double");
+        };
 
         // at least two CTAs per SM: the register cap (128 at 256 threads) keeps the amplitude event kernels
         // at two resident CTAs instead of one.  FP32 batch kernels with 8 events per iteration: four (58
         // registers, no spills; 1024 toys of the composite model: event kernel 0.086 -> 0.068 ms); the one-toy
         // kernel stays at two (three or four made the 2e6-event FCN 0.5 / 3 us slower)
         const int minBlocks = (VEC == 8 && mixed && batch) ? 4 : 2;
-        os << "extern \"C\" __global__ void __launch_bounds__(" << block << ", " << minBlocks << ") " << name
-           << "(const GfArgs a) {\n";
+        // the one-launch kernel may have bulk-copied the CTA's events into shared memory (gf_st != null):
+        // stream s at gf_st + gf_soff[s], event i at index i - gf_ib, complete once gf_mbar's phase 0 is
+        kernelHead(name, std::to_string(block) + ", " + std::to_string(minBlocks), asBody,
+                   ", const unsigned char *gf_st, const int *gf_soff, long long gf_ib, unsigned long long *gf_mbar");
         os << "  extern __shared__ __align__(16) unsigned char smraw[];\n";
         os << "  R *stab = reinterpret_cast<R *>(smraw); (void)stab;\n";
         os << "  __shared__ int s_toy, last;\n";
@@ -2492,7 +2622,8 @@ struct Gen {
         os << "  if(tid == 0) s_toy = -1;\n";
         os << "  gf_pdl_trigger();\n";
         // event columns do not depend on the preceding kernels: pull the first chunk towards L2 meanwhile
-        os << "  if(cb < ce) {\n";
+        // (the one-launch kernel bulk-copies or bulk-prefetches every CTA's events at its start instead)
+        os << "  if(" << (asBody ? "false && " : "") << "cb < ce) {\n";
         os << "    int toy; i64 b0, e0; gf_chunk(a, cb, toy, b0, e0);\n";
         os << "    {\n";
         os << "      for(i64 i0 = b0 + " << VEC << " * (i64)tid; i0 < e0; i0 += " << VEC << " * " << block << ") {\n";
@@ -2508,12 +2639,23 @@ struct Gen {
                 os << "        asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(reinterpret_cast<const R2 *>("
                    << p0ptr("a.acol", NA, ac, NO + NC) << ") + i0));\n";
         os << "      }\n    }\n  }\n";
+        evtStreams.clear();
+        if(!values && !asBody)
+            evtReadsObs[grad ? 1 : 0] = std::find(xused.begin(), xused.end(), 1) != xused.end();
+        for(int o = 0; o < NO; ++o)
+            if(xused[o])
+                evtStreams.push_back({p0ptr("a.col", NO, o, 0), mixed ? 4 : 8});
+        for(int ci = 0; ci < NC; ++ci)
+            evtStreams.push_back({p0ptr("a.kcol", NC, ci, NO), 4});
+        for(int ac = 0; ac < NA; ++ac)
+            if(aused[ac])
+                evtStreams.push_back({p0ptr("a.acol", NA, ac, NO + NC), mixed ? 8 : 16});
         // one toy: its parameters and activity flag (written by the host, possibly read in place from
         // page-locked memory) are read once per CTA before the wait, the normalisation factors once after it
         if(!batch) {
             os << "  const int toy1 = 0;\n";
             os << "  const bool toy_on1 = !a.active || a.active[toy1];\n";
-            os << "  const R *Pr1 = reinterpret_cast<const R *>(a.Pr); (void)Pr1;\n";
+            os << "  const R *Pr1 = reinterpret_cast<const R *>(GF_PR); (void)Pr1;\n";
             for(int j = 0; j < T.n_params; ++j)
                 os << "  const R p" << j << " = Pr1[" << j << "]; (void)p" << j << ";\n";
         }
@@ -2521,32 +2663,182 @@ struct Gen {
         os << "  __syncthreads();\n";
         if(!batch) {
             os << "  const int toy = toy1;\n  const R *Pr = Pr1; (void)Pr;\n";
-            emitNormReads(os, T, grad, plan.nl, "  ");
+            if(!tab)
+                emitNormReads(os, T, grad, plan.nl, "  ");
+            else {
+                // one pass over the toy's table: every thread loads its rows once (all loads in flight), the
+                // CTA sums the folded grid normalisation of the convolution's numeric node itself (from the
+                // table CTAs' partials of sum_k n_k T[k], so no finishing CTA), then each row's per-event
+                // terms go to shared memory
+                const ConvInfo &cv = T.convs[0];
+                const int cp = cps[0], per = std::min(cp, mixed ? 4 : 2), nvr = cp / per;
+                const int NR = (cv.nK + block - 1) / block;
+                const std::string vt = vtype(per);
+                const int fq = plan.conv_fold_q[0];
+                const int comps = convComps(0, grad);
+                os << "  R *ltab = stab;\n";
+                os << "  " << vt << " tv[" << NR << "][" << nvr << "];\n";
+                os << "  {\n    const R *gt = reinterpret_cast<const R *>(a.ctab) + " << off[0] << ";\n";
+                os << "#pragma unroll\n    for(int r = 0; r < " << NR << "; ++r) {\n      const int kk = tid + r * " << block
+                   << ";\n      if(kk < " << cv.nK << ") {\n";
+                os << "#pragma unroll\n        for(int v = 0; v < " << nvr << "; ++v) tv[r][v] = *reinterpret_cast<const " << vt
+                   << " *>(gt + kk * " << cp << " + " << per << " * v);\n";
+                os << "      }\n    }\n  }\n";
+                // the other normalisation factors as usual
+                {
+                    std::ostringstream nr;
+                    emitNormReads(nr, T, grad, plan.nl, "  ");
+                    std::string txt = nr.str();
+                    if(fq >= 0) {
+                        // drop the folded node's reads from Nq: its factors come from the CTA's own sum
+                        const int node = T.nums[fq].node;
+                        std::istringstream in(txt);
+                        std::string line, keep;
+                        const std::string a1 = "const R N" + std::to_string(node) + " = Nq[";
+                        const std::string a2 = "const R dN" + std::to_string(node) + "_";
+                        while(std::getline(in, line))
+                            if(line.find(a1) == std::string::npos && line.find(a2) == std::string::npos)
+                                keep += line + "\n";
+                        txt = keep;
+                    }
+                    os << txt;
+                }
+                if(fq >= 0) {
+                    const NumInfo &g = T.nums[fq];
+                    const int node   = g.node;
+                    const double cc  = g.volume / (double)g.total;
+                    os << "  __shared__ R s_fn[" << 2 + comps << "];\n";
+                    os << "  __shared__ int s_fbits;\n";
+                    // the table CTAs' partials of sum_k n_k T_c[k] (component c of gradient slot cs[c]), one per
+                    // table CTA, summed here by every CTA in the same order
+                    const int KB   = convShape(grad).KB[0];
+                    const int nblk = (cv.nK + KB - 1) / KB, MGB = plan.max_grid_blocks;
+                    const int NQ   = (int)T.nums.size(), NGs = 1 + T.NG;
+                    os << "  {\n";
+                    os << "    const ACC *gp = reinterpret_cast<const ACC *>(a.gpartial) + ((i64)toy * " << NQ << " + " << fq
+                       << ") * " << NGs << " * " << MGB << ";\n";
+                    for(int c = 0; c < comps; ++c) {
+                        const int cs = c == 0 ? 0 : 1 + cv.dep[c - 1];
+                        os << "    ACC fs" << c << " = acc_zero();\n";
+                        os << "    for(int bi = tid; bi < " << nblk << "; bi += " << block << ") fs" << c << " = acc_add(fs" << c
+                           << ", gp[" << cs * MGB << " + bi]);\n";
+                    }
+                    std::vector<std::string> vals;
+                    for(int c = 0; c < comps; ++c)
+                        vals.push_back("fs" + std::to_string(c));
+                    emitCtaReduce(os, vals, "    ");
+                    // GooPdf::normalize's numeric branch (src/PDFs/GooPdf.cu:366-395) on the CTA's sums
+                    os << "    if(tid == 0) {\n";
+                    os << "      ACC tt[" << comps << "];\n";
+                    os << "      for(int c = 0; c < " << comps << "; ++c) { tt[c] = acc_zero(); for(int w = 0; w < " << NW
+                       << "; ++w) tt[c] = acc_add(tt[c], red[w][c]); }\n";
+                    os << "      const double S = acc_value(tt[0]);\n";
+                    os << "      s_fbits = isnan(S) ? 1 : !(S > 0.0) ? 2 : 0;\n";
+                    os << "      const double I = " << lit(cc) << " * S;\n";
+                    os << "      const double Nd = 1.0 / I;\n";
+                    os << "      const R N = (R)Nd;\n";
+                    os << "      s_fn[0] = N;\n      s_fn[1] = (R)(Nd - (double)N);\n";
+                    if(grad)
+                        for(int j = 1; j < comps; ++j)
+                            os << "      s_fn[" << 1 + j << "] = -N * N * (R)" << lit(cc) << " * (R)acc_r(tt[" << j << "]);\n";
+                    os << "    }\n    __syncthreads();\n  }\n";
+                    os << "  const R N" << node << " = s_fn[0], NL" << node << " = s_fn[1]; (void)NL" << node << ";\n";
+                    if(grad)
+                        for(auto &d : plan.nl.qdN[fq]) {
+                            const auto &dep = cv.dep;
+                            const int j = (int)(std::find(dep.begin(), dep.end(), d.first) - dep.begin());
+                            os << "  const R dN" << node << "_" << d.first << " = s_fn[" << 2 + j << "];\n";
+                        }
+                }
+                // per-k terms
+                os << "#pragma unroll\n  for(int r = 0; r < " << NR << "; ++r) {\n    const int kk = tid + r * " << block
+                   << ";\n    if(kk < " << cv.nK << ") {\n";
+                os << "      const int ek0 = " << cv.kmin << " + kk; (void)ek0;\n";
+                if(mixed) {
+                    if(cp == 1)
+                        os << "      const float tq0 = tv[r][0];\n";
+                    else if(cp == 2)
+                        os << "      const float2 tq0 = tv[r][0];\n";
+                    else
+                        for(int g4 = 0; g4 < cp / 4; ++g4)
+                            os << "      const float4 tq0_" << g4 << " = tv[r][" << g4 << "];\n";
+                } else
+                    os << "      const R *tp0 = reinterpret_cast<const R *>(tv[r]); (void)tp0;\n";
+                os << "      {\n" << body.str();
+                const std::string pvE = factorRoot ? root.v : normMul(c, 0, root.v);
+                os << "      const R pv = " << pvE << ";\n";
+                os << "      R lt[" << LP << "];\n#pragma unroll\n      for(int q = 0; q < " << LP << "; ++q) lt[q] = R(0);\n";
+                os << "      if(pv > R(0)) {\n";
+                os << "        lt[0] = -GF_LOG(pv);\n";
+                if(grad && T.NG > 0) {
+                    os << "        const R inv = gf_rcp(pv);\n";
+                    for(int sl = 0; sl < T.NG; ++sl) {
+                        std::string e;
+                        auto it = root.g.find(sl);
+                        if(factorRoot) {
+                            if(it != root.g.end())
+                                e = it->second;
+                        } else {
+                            if(it != root.g.end())
+                                e = rootN.empty() ? it->second : it->second + " * " + rootN;
+                            std::string dn = T.nk[0] == NK_ONE ? "" : dnormExpr(c, 0, sl);
+                            if(!dn.empty())
+                                e += (e.empty() ? "" : " + ") + root.v + " * " + dn;
+                        }
+                        if(!e.empty())
+                            os << "        lt[" << 1 + sl << "] = -(" << e << ") * inv;\n";
+                    }
+                }
+                if(factorRoot)
+                    os << "        lt[" << tabComps - 1 << "] = R(1);\n";
+                os << "      }\n";
+                for(size_t b = 0; b < bw.size(); ++b)
+                    for(int q = 0; q < bw[b]; ++q)
+                        os << "      ltab[" << boff[b] << " + kk * " << bw[b] << " + " << q << "] = lt[" << vw * (int)b + q
+                           << "];\n";
+                os << "      }\n    }\n  }\n  __syncthreads();\n";
+            }
         }
-        os << "  for(int ch = cb; ch < ce; ++ch) {\n";
+        if(asBody) {
+            // staged events: every thread waits for the bulk copy (bounded); a copy that does not arrive leaves
+            // this CTA's chunks unevaluated, so that their rows stay unwritten and the host reports the failure
+            os << "  bool gf_ok = true;\n";
+            os << "  if(gf_st && !gf_mbar_wait(gf_mbar, 0u, 1000000000ull)) {\n";
+            os << "    gf_ok = false;\n    if(tid == 0 && a.gbar) atomicOr(a.gbar + 2, 2u);\n  }\n";
+            os << "  for(int ch = cb; gf_ok && ch < ce; ++ch) {\n";
+        } else
+            os << "  for(int ch = cb; ch < ce; ++ch) {\n";
         os << "    int toy; i64 b0, e0; gf_chunk(a, ch, toy, b0, e0);\n";
         // the activity flag is read beside the parameters (independent loads), the branch comes after them
         if(batch)
             os << "    const bool toy_on = !a.active || a.active[toy];\n";
         else
             os << "    const bool toy_on = toy_on1;\n";
-        if(NC > 0 && ctabL1) {
+        if(tab) {
+            // per-k terms were tabulated before the chunk loop
+        } else if(NC > 0 && ctabL1) {
             // the toy's tables are read through L1 (read-only loads): every CTA on an SM shares one copy
             os << "    const R *ttab = reinterpret_cast<const R *>(a.ctab) + (i64)toy * " << ctabTotal << ";\n";
         } else if(NC > 0) {
+            // all of a thread's 16-byte loads issued before its stores (one L2 round trip, not one per load)
+            const int perV = mixed ? 4 : 2;
+            const int64_t nv = ctabTotal / perV;
+            const int nr = (int)((nv + block - 1) / block);
+            const char *vt = mixed ? "float4" : "double2";
             os << "    const R *ttab = stab;\n";
             os << "    if(toy != s_toy) {\n";
             os << "      __syncthreads();\n";
-            if(mixed)
-                os << "      { const float4 *src = reinterpret_cast<const float4 *>(reinterpret_cast<const R *>(a.ctab) + "
-                      "(i64)toy * "
-                   << ctabTotal << "); float4 *dst = reinterpret_cast<float4 *>(stab);\n"
-                   << "        for(int i = tid; i < " << ctabTotal / 4 << "; i += " << block << ") dst[i] = src[i]; }\n";
-            else
-                os << "      { const double2 *src = reinterpret_cast<const double2 *>(reinterpret_cast<const R *>(a.ctab) "
-                      "+ (i64)toy * "
-                   << ctabTotal << "); double2 *dst = reinterpret_cast<double2 *>(stab);\n"
-                   << "        for(int i = tid; i < " << ctabTotal / 2 << "; i += " << block << ") dst[i] = src[i]; }\n";
+            os << "      { const " << vt << " *src = reinterpret_cast<const " << vt << " *>(reinterpret_cast<const R *>(a.ctab) + "
+                  "(i64)toy * " << ctabTotal << "); " << vt << " *dst = reinterpret_cast<" << vt << " *>(stab);\n";
+            if(nr <= 16) {
+                os << "        " << vt << " tv[" << nr << "];\n";
+                os << "#pragma unroll\n        for(int r = 0; r < " << nr << "; ++r) { const int i = tid + r * " << block
+                   << "; if(i < " << nv << ") tv[r] = src[i]; }\n";
+                os << "#pragma unroll\n        for(int r = 0; r < " << nr << "; ++r) { const int i = tid + r * " << block
+                   << "; if(i < " << nv << ") dst[i] = tv[r]; }\n";
+            } else
+                os << "        for(int i = tid; i < " << nv << "; i += " << block << ") dst[i] = src[i];\n";
+            os << "      }\n";
             os << "      if(tid == 0) s_toy = toy;\n";
             os << "      __syncthreads();\n";
             os << "    }\n";
@@ -2557,15 +2849,26 @@ struct Gen {
         }
         if(T.fit_metric != GF_FIT_UNBINNED_NLL && !values)
             os << "    const R Tn = (R)a.toy_nevents[toy]; // c_totalEvents: the number of bins\n";
+        // a staged stream's pointer is shifted by gf_ib events (integer arithmetic on the address), so that the
+        // loads below index it by the global event number as they index the column in global memory
+        int stream = 0;
+        auto colPtr = [&](const std::string &type, int bytes, const std::string &glob) {
+            std::string e = "reinterpret_cast<const " + type + " *>(" + glob + ")";
+            if(asBody)
+                e = "(gf_st ? reinterpret_cast<const " + type + " *>(reinterpret_cast<unsigned long long>(gf_st + gf_soff[" +
+                    std::to_string(stream) + "]) - (unsigned long long)gf_ib * " + std::to_string(bytes) + "ull) : " + e + ")";
+            ++stream;
+            return e;
+        };
         for(int o = 0; o < NO; ++o)
             if(xused[o])
-                os << "    const R *col" << o << " = reinterpret_cast<const R *>(" << p0ptr("a.col", NO, o, 0) << ");\n";
+                os << "    const R *col" << o << " = " << colPtr("R", mixed ? 4 : 8, p0ptr("a.col", NO, o, 0)) << ";\n";
         for(int ci = 0; ci < NC; ++ci)
-            os << "    const int *kc" << ci << " = reinterpret_cast<const int *>(" << p0ptr("a.kcol", NC, ci, NO) << ");\n";
+            os << "    const int *kc" << ci << " = " << colPtr("int", 4, p0ptr("a.kcol", NC, ci, NO)) << ";\n";
         for(int ac = 0; ac < NA; ++ac)
             if(aused[ac])
-                os << "    const R2 *acp" << ac << " = reinterpret_cast<const R2 *>(" << p0ptr("a.acol", NA, ac, NO + NC)
-                   << ");\n";
+                os << "    const R2 *acp" << ac << " = " << colPtr("R2", mixed ? 8 : 16, p0ptr("a.acol", NA, ac, NO + NC))
+                   << ";\n";
         os << "    if(!toy_on) continue;\n";
         // per-thread sums: each iteration's VEC events are summed plainly (av, ag), then added to a two-sum
         // compensated pair (avh + avl, agh + agl), so that a thread's many events add no rounding noise
@@ -2617,7 +2920,7 @@ struct Gen {
         }
         // FP32 one-toy/batch kernels with 8 events per iteration take one log per iteration, of the product
         // of its events' probabilities (gf_log_acc); the amplitude kernels' 2-event iterations keep one per event
-        const bool logProd = mixed && !values && VEC == 8;
+        const bool logProd = mixed && !values && VEC == 8 && !tab;
         if(!values) {
             os << "      R av = R(0);\n";
             for(int s = 0; s < NGp - 1; ++s)
@@ -2672,6 +2975,26 @@ struct Gen {
                << "a.w, kv" << ci << "b.x, kv" << ci << "b.y, kv" << ci << "b.z, kv" << ci << "b.w};\n";
         }
         os << "#pragma unroll\n      for(int j = 0; j < " << VEC << "; ++j) {\n";
+        if(tab) {
+            // gather the event's tabulated terms (16-byte and narrower shared loads) and add them
+            const ConvInfo &cv = T.convs[0];
+            const char *fld[] = {".x", ".y", ".z", ".w"};
+            os << "        const int lk = ka0[j] - " << cv.kmin << ";\n";
+            for(size_t b = 0; b < bw.size(); ++b)
+                os << "        const " << vtype(bw[b]) << " lq" << b << " = *reinterpret_cast<const " << vtype(bw[b])
+                   << " *>(ltab + " << boff[b] << " + lk * " << bw[b] << ");\n";
+            auto comp = [&](int q) {
+                const int b = q / vw;
+                return "lq" + std::to_string(b) + (bw[b] == 1 ? std::string("") : std::string(fld[q % vw]));
+            };
+            os << "        {\n        if(j < jn) {\n";
+            os << "          av += " << comp(0) << ";\n";
+            for(int sl = 0; sl < NGp - 1; ++sl)
+                os << "          ag" << sl << " += " << comp(1 + sl) << ";\n";
+            if(factorRoot)
+                os << "          nv += " << comp(tabComps - 1) << ";\n";
+            os << "        }\n";
+        } else {
         for(int o = 0; o < NO; ++o)
             if(xused[o])
                 os << "        const R ex" << o << " = xa" << o << "[j];\n";
@@ -2812,6 +3135,7 @@ struct Gen {
                 os << "        }\n";
             }
         }
+        } // not tab
         os << "        }\n      }\n";
         if(!values) {
             if(logProd) {
@@ -2830,6 +3154,7 @@ struct Gen {
         os << "    }\n";
         if(values) {
             os << "  }\n}\n\n";
+            endBody(asBody);
             return;
         }
         // components: value, gradient slots, and (factored root normalisation) the count of events with P > 0,
@@ -2843,6 +3168,21 @@ struct Gen {
             if(factorRoot)
                 comps.push_back("acc_of(nv)");
             emitCtaReduce(os, comps, "    ");
+        }
+        if(asBody) {
+            plan.fused_row[grad ? 1 : 0] = NGc + 1;
+            // one-launch evaluation: each chunk's sums and status go straight to page-locked host memory (row
+            // ch: [components..., status]); the host adds the rows in chunk order after the launch, so no CTA
+            // waits on a completion counter and no finishing CTA runs
+            const bool foldTab = tab && plan.conv_fold_q[0] >= 0;
+            os << "    if(tid < " << NGc << ") { ACC t = acc_zero(); for(int w = 0; w < " << NW
+               << "; ++w) t = acc_add(t, red[w][tid]); a.hpart[(i64)ch * " << NGc + 1 << " + tid] = acc_value(t); }\n";
+            os << "    if(tid == 0) a.hpart[(i64)ch * " << NGc + 1 << " + " << NGc << "] = (double)(a.qflag[toy]"
+               << (foldTab ? " | s_fbits" : "") << " | (a.gbar[2] ? 8 : 0));\n";
+            os << "    __syncthreads();\n";
+            os << "  }\n}\n\n";
+            endBody(asBody);
+            return;
         }
         // chunk partials are component-major: part[comp][chunk], so that the finisher's loads are contiguous
         os << "    ACC *part = reinterpret_cast<ACC *>(a.partial);\n";
@@ -2869,12 +3209,152 @@ struct Gen {
            << " : 1 + comp)] = v;\n";
         // a zero NLL is flagged here, or on the host after the factored normalisation is added
         os << "          if(comp == 0) { int st = a.qflag[toy]; " << (factorRoot ? "" : "if(v == 0.0) st |= 4; ")
-           << "o[1] = (double)st; a.counter[toy] = 0u; a.qflag[toy] = 0; }\n";
+           << "if(a.gbar && a.gbar[2]) st |= 8; o[1] = (double)st; a.counter[toy] = 0u; a.qflag[toy] = 0; }\n";
         os << "        }\n";
         os << "      }\n";
         os << "    }\n";
         os << "    __syncthreads();\n";
         os << "  }\n}\n\n";
+        endBody(asBody);
+    }
+
+    // event columns the event pass streams (pointer expression, bytes per event), set by eventKernel
+    std::vector<std::pair<std::string, int>> evtStreams;
+    // dynamic shared memory of the last body eventKernel emitted
+    size_t bodySmem = 0;
+    // [nograd, grad]: the event function reads an observable column (set by the standalone event kernels)
+    bool evtReadsObs[2] = {true, true};
+
+    // ---------------- one launch per evaluation (one toy) ----------------
+    // gf_fcn_*: a cooperative launch (every CTA resident) that runs the whole evaluation.  Each CTA first
+    // copies its own event chunks into shared memory with bulk copies (or, when they do not fit, prefetches
+    // them into L2), so that their HBM reads overlap the tables; then the convolution-table CTAs and the
+    // numeric-grid CTAs of the separate kernels run as virtual blocks spread over the launch, a bounded grid
+    // barrier follows (two when an unfolded numeric node reads a table), and the event pass runs over the same
+    // CTAs, writing per-chunk sums to host memory.  Replaces three dependent launches and the finishing CTA
+    // (GooPdf::calculateNLL's normalize + reduce, src/PDFs/GooPdf.cu:254-273) by one launch.
+    void fusedKernel(bool grad) {
+        const char *sfx = grad ? "g" : "n";
+        const int NC = (int)T.convs.size(), NQ = (int)T.nums.size();
+        bool hasGrid = false;
+        for(int q = 0; q < NQ; ++q)
+            hasGrid = hasGrid || !plan.num_folded[q];
+        if(NC == 0 && !hasGrid)
+            return;
+        // the per-event terms depend on the event only through one convolution's bin offset: tabulate them
+        // (at most 16 table rows per thread, held in registers)
+        const bool tab = NC == 1 && T.n_amp_cols == 0 && !evtReadsObs[grad ? 1 : 0] && !tabDisabled() &&
+                         (T.convs[0].nK + block - 1) / block <= 16;
+        // with the tabulated terms every CTA sums the folded grid normalisation itself from the table CTAs'
+        // partials: they skip the fold's completion counter and finishing CTA
+        if(NC > 0)
+            convKernel(grad, true, tab);
+        if(hasGrid)
+            gridKernel(grad, true);
+        eventKernel(grad, false, true, tab);
+        const size_t evtSmem = bodySmem;
+        const int CB = plan.conv_blocks, MGB = plan.max_grid_blocks;
+        const int nConvV = NC > 0 ? CB * NC : 0, nGridV = hasGrid ? MGB * NQ : 0;
+        os << "extern \"C\" __global__ void __launch_bounds__(" << block << ", 2) gf_fcn_" << sfx
+           << "(const GfArgs a) {\n";
+        os << "  const int toy = 0; (void)toy;\n";
+        // the toy's record (parameters, analytic factors), passed by value in the arguments (or, when too
+        // large, read from page-locked host memory): one copy per CTA in shared memory, read by every phase
+        const int npr = std::max(1, plan.nl.npr);
+        os << "  __shared__ __align__(16) R sPr[" << npr << "];\n";
+        os << "  for(int i = threadIdx.x; i < " << plan.nl.npr << "; i += blockDim.x)\n"
+           << "    sPr[i] = a.rec_n ? reinterpret_cast<const R *>(a.rec)[i] : reinterpret_cast<const R *>(a.Pr)[i];\n";
+        // the CTA's events (all its chunks, one contiguous range per stream): when they fit, one bulk copy per
+        // stream into shared memory (the TMA unit, completion on an mbarrier) that runs while the tables are
+        // built; otherwise a bulk prefetch into L2.  Chunk starts are multiples of 256 events (16-byte
+        // aligned sources) and the streams are padded to 8 events, so 16-byte-rounded sizes stay in bounds.
+        const int NS = (int)evtStreams.size();
+        os << "  extern __shared__ __align__(16) unsigned char gf_dyn[];\n";
+        os << "  __shared__ __align__(8) unsigned long long s_mbar;\n";
+        os << "  __shared__ int s_soff[" << std::max(1, NS) << "];\n";
+        os << "  __shared__ int s_staged;\n";
+        os << "  const int cb = (int)(((i64)a.n_chunks * blockIdx.x) / gridDim.x);\n";
+        os << "  const int ce = (int)(((i64)a.n_chunks * (blockIdx.x + 1)) / gridDim.x);\n";
+        os << "  const i64 sb0 = (i64)cb * a.chunk;\n";
+        os << "  if(threadIdx.x == 0) {\n";
+        os << "    int staged = 0;\n";
+        os << "    if(cb < ce) {\n";
+        os << "      const i64 e0 = (i64)ce * a.chunk < a.nevt0 ? (i64)ce * a.chunk : a.nevt0;\n";
+        os << "      unsigned nb[" << std::max(1, NS) << "], tot = 0;\n";
+        for(int i = 0; i < NS; ++i)
+            os << "      nb[" << i << "] = (unsigned)(((e0 - sb0) * " << evtStreams[i].second << " + 15) & ~15LL); s_soff["
+               << i << "] = (int)tot; tot += nb[" << i << "];\n";
+        os << "      if(a.stage_cap > 0u && tot <= a.stage_cap) {\n";
+        os << "        const unsigned mb = (unsigned)__cvta_generic_to_shared(&s_mbar);\n";
+        os << "        asm volatile(\"mbarrier.init.shared::cta.b64 [%0], 1;\" :: \"r\"(mb) : \"memory\");\n";
+        os << "        asm volatile(\"fence.mbarrier_init.release.cluster;\" ::: \"memory\");\n";
+        os << "        asm volatile(\"mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\" :: \"r\"(mb), \"r\"(tot) : \"memory\");\n";
+        os << "        const unsigned sd = (unsigned)__cvta_generic_to_shared(gf_dyn + a.stage_off);\n";
+        for(int i = 0; i < NS; ++i)
+            os << "        asm volatile(\"cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\" :: "
+                  "\"r\"(sd + (unsigned)s_soff[" << i << "]), \"l\"(reinterpret_cast<const char *>(" << evtStreams[i].first
+               << ") + sb0 * " << evtStreams[i].second << "), \"r\"(nb[" << i << "]), \"r\"(mb) : \"memory\");\n";
+        os << "        staged = 1;\n";
+        os << "      } else {\n";
+        for(int i = 0; i < NS; ++i)
+            os << "        asm volatile(\"cp.async.bulk.prefetch.L2.global [%0], %1;\" :: \"l\"(reinterpret_cast<const char *>("
+               << evtStreams[i].first << ") + sb0 * " << evtStreams[i].second << "), \"r\"(nb[" << i << "]) : \"memory\");\n";
+        os << "      }\n";
+        os << "    }\n";
+        os << "    s_staged = staged;\n";
+        os << "  }\n";
+        os << "  __syncthreads();\n";
+        // a CTA that leaves early still waits (bounded) for its own bulk copy, so that no copy writes the shared
+        // memory of a finished CTA
+        auto barrier = [&]() {
+            os << "  if(!gf_grid_sync(a.gbar, a.bar_ns)) {\n";
+            os << "    if(s_staged) gf_mbar_wait(&s_mbar, 0u, 1000000000ull);\n";
+            os << "    return;\n  }\n";
+        };
+        auto convLoop = [&]() {
+            os << "  for(unsigned vb = blockIdx.x; vb < " << nConvV << "u; vb += gridDim.x) {\n";
+            os << "    gf_conv_" << sfx << "_body(a, make_uint3(vb % " << CB << "u, 0u, vb / " << CB << "u), make_uint3("
+               << CB << "u, 1u, " << NC << "u), sPr);\n";
+            os << "    __syncthreads();\n  }\n";
+        };
+        auto gridLoop = [&](bool shifted) {
+            // grid virtual blocks after the table ones (same phase) or from block 0 (a phase of their own)
+            os << "  for(unsigned vb = blockIdx.x; vb < " << (shifted ? nConvV : 0) + nGridV << "u; vb += gridDim.x) {\n";
+            if(shifted)
+                os << "    if(vb < " << nConvV << "u) gf_conv_" << sfx << "_body(a, make_uint3(vb % " << CB
+                   << "u, 0u, vb / " << CB << "u), make_uint3(" << CB << "u, 1u, " << NC << "u), sPr);\n    else {\n"
+                   << "      const unsigned g = vb - " << nConvV << "u;\n";
+            else
+                os << "    {\n      const unsigned g = vb;\n";
+            os << "      gf_grid_" << sfx << "_body(a, make_uint3(g % " << MGB << "u, 0u, g / " << MGB << "u), make_uint3("
+               << MGB << "u, 1u, " << NQ << "u), sPr);\n    }\n";
+            os << "    __syncthreads();\n  }\n";
+        };
+        if(NC > 0 && hasGrid && !plan.grid_needs_conv)
+            gridLoop(true); // tables and grids in one phase
+        else {
+            if(NC > 0)
+                convLoop();
+            if(NC > 0 && hasGrid)
+                barrier();
+            if(hasGrid)
+                gridLoop(false);
+        }
+        barrier();
+        os << "  gf_evt_" << sfx << "_body(a, blockIdx, gridDim, sPr, s_staged ? gf_dyn + a.stage_off : nullptr, s_soff, sb0, "
+              "&s_mbar);\n";
+        os << "}\n\n";
+        plan.fused     = true;
+        plan.fused_tab = plan.fused_tab || tab;
+        const size_t work = std::max(grad ? plan.conv_smem_grad : plan.conv_smem_nograd, evtSmem);
+        const size_t soff = (work + 127) / 128 * 128;
+        // two resident CTAs per SM (228 KB of shared memory per SM, 1 KB of it reserved per CTA, a few KB of
+        // static arrays): the staged events get what is left of 109 KB, at most 64 KB
+        const size_t budget = 109 * 1024;
+        const size_t cap    = soff < budget ? std::min<size_t>(64 * 1024, (budget - soff) / 16 * 16) : 0;
+        plan.fused_stage_off[grad ? 1 : 0] = soff;
+        plan.fused_stage_cap[grad ? 1 : 0] = cap;
+        plan.fused_smem[grad ? 1 : 0]      = soff + cap;
     }
 };
 
@@ -2924,6 +3404,10 @@ KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, bool batch
     g.eventKernel(true, false);
     g.eventKernel(false, false);
     g.eventKernel(false, true);
+    if(!batch && t.fit_metric == GF_FIT_UNBINNED_NLL) {
+        g.fusedKernel(true);
+        g.fusedKernel(false);
+    }
     plan.source = g.os.str();
     return plan;
 }

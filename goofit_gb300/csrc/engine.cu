@@ -133,6 +133,12 @@ void dropGraphs(gf_engine *e) {
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
+    for(int i = 0; i < 2; ++i) {
+        if(e->graph_src[i])
+            cudaGraphDestroy(e->graph_src[i]);
+        e->graph_src[i]  = nullptr;
+        e->fused_node[i] = nullptr;
+    }
 }
 
 void freeLayout(gf_engine *e) {
@@ -148,6 +154,10 @@ void freeLayout(gf_engine *e) {
     dfree(e->d_gcounter);
     dfree(e->d_partial);
     dfree(e->d_counter);
+    dfree(e->d_gbar);
+    hfree(e->h_fpart);
+    e->d_fpart   = nullptr;
+    e->chunk_cap = 0;
     e->d_out = nullptr; // inside h_out
     dfree(e->d_chunks);
     e->chunk_cap = 0;
@@ -235,9 +245,20 @@ int setChunks(gf_engine *e, int chunk) {
     if(n > e->chunk_cap) {
         dfree(e->d_chunks);
         dfree(e->d_partial);
+        hfree(e->h_fpart);
+        e->d_fpart   = nullptr;
         e->chunk_cap = 0;
         if((rc = dalloc(e, e->d_chunks, (size_t)3 * n, false)) || (rc = dalloc(e, e->d_partial, (size_t)n * (NGp + 1), false)))
             return rc;
+        // rows of the one-launch kernel: [value, gradient..., count, status] per chunk, written by the kernel
+        // into mapped page-locked memory and added up on the host
+        e->fused_row = NGp + 2;
+        if(cudaHostAlloc((void **)&e->h_fpart, sizeof(double) * (size_t)n * e->fused_row, cudaHostAllocMapped) !=
+               cudaSuccess ||
+           cudaHostGetDevicePointer((void **)&e->d_fpart, e->h_fpart, 0) != cudaSuccess) {
+            cudaGetLastError();
+            return gf_fail(e, GF_ERR_OOM, "cudaHostAlloc chunk rows");
+        }
         e->chunk_cap = n;
     }
     cudaError_t r = cudaMemcpy(e->d_chunks, chunks.data(), sizeof(long long) * chunks.size(), cudaMemcpyHostToDevice);
@@ -321,6 +342,7 @@ int buildLayout(gf_engine *e) {
     chk(dalloc(e, e->d_gpartial, (size_t)NT * std::max(1, NQ) * std::max(1, e->plan.max_grid_blocks) * NGp));
     chk(dalloc(e, e->d_gcounter, (size_t)NT * std::max(1, NQ)));
     chk(dalloc(e, e->d_counter, NT));
+    chk(dalloc(e, e->d_gbar, 4));
     chk(dalloc(e, e->d_toy_chunk0, NT));
     chk(dalloc(e, e->d_toy_nchunks, NT));
     chk(dalloc(e, e->d_toy_nevents, NT));
@@ -464,6 +486,8 @@ GfArgs makeArgs(gf_engine *e) {
     a.n_chunks    = e->n_chunks;
     a.n_toys      = e->n_toys;
     a.metric      = 1;
+    a.gbar        = e->d_gbar;
+    a.bar_ns      = e->bar_ns;
     return a;
 }
 
@@ -539,7 +563,60 @@ cudaError_t recordEvent(gf_engine *e, cudaEvent_t ev) {
     return cudaEventRecord(ev, e->stream);
 }
 
+// One toy with the one-launch kernels loaded and enabled: the evaluation is a single cooperative launch.
+bool fusedPath(const gf_engine *e) {
+    return e->use_fused && e->n_toys == 1 && !e->batch_kernels && e->mod.fcn_g && e->mod.fcn_n && e->fcn_grid > 0 &&
+           e->h_fpart;
+}
+
+// Arguments of the one-launch kernel: the toy's record (parameters as R, analytic factors) by value when it
+// fits, so that no CTA reads it from host memory; the page-locked block in place otherwise; no activity flag
+// (the one toy is evaluated whatever its flag says); the chunk rows in mapped host memory.
+GfArgs fusedArgs(gf_engine *e, bool grad) {
+    GfArgs a    = makeArgs(e);
+    a.stage_off = (int)e->plan.fused_stage_off[grad ? 1 : 0];
+    a.stage_cap = e->use_stage ? (unsigned)e->plan.fused_stage_cap[grad ? 1 : 0] : 0u;
+    const size_t poff = sizeof(double) * (size_t)e->n_toys * std::max(1, e->tree.n_params);
+    char *hp          = nullptr;
+    if(cudaHostGetDevicePointer((void **)&hp, e->h_P, 0) == cudaSuccess) {
+        a.P  = (const double *)hp;
+        a.Pr = hp + poff;
+    } else
+        cudaGetLastError();
+    a.active        = nullptr;
+    a.hpart         = e->d_fpart;
+    const size_t rb = rsize(e) * (size_t)e->plan.nl.npr;
+    a.rec_n         = 0;
+    if(rb > 0 && rb <= sizeof(a.rec)) {
+        std::memcpy(a.rec, reinterpret_cast<const char *>(e->h_P) + poff, rb);
+        a.rec_n = e->plan.nl.npr;
+    }
+    return a;
+}
+
 cudaError_t enqueueEval(gf_engine *e, bool grad) {
+    if(fusedPath(e)) {
+        // tables, grids and the event pass in one cooperative launch (all CTAs resident, grid barrier)
+        GfArgs a      = fusedArgs(e, grad);
+        cudaError_t r = recordEvent(e, e->ev[0]);
+        if(r == cudaSuccess) {
+            void *args[] = {&a};
+            cudaLaunchAttribute attr[1];
+            attr[0].id              = cudaLaunchAttributeCooperative;
+            attr[0].val.cooperative = 1;
+            cudaLaunchConfig_t cfg{};
+            cfg.gridDim          = dim3(e->fcn_grid);
+            cfg.blockDim         = dim3(e->block);
+            cfg.dynamicSmemBytes = e->plan.fused_smem[grad ? 1 : 0];
+            cfg.stream           = e->stream;
+            cfg.attrs            = attr;
+            cfg.numAttrs         = 1;
+            r = cudaLaunchKernelExC(&cfg, (const void *)(grad ? e->mod.fcn_g : e->mod.fcn_n), args);
+        }
+        if(r == cudaSuccess)
+            r = recordEvent(e, e->ev[3]);
+        return r;
+    }
     GfArgs a = makeArgs(e);
     // qflag is zero between evaluations: the event kernel's finisher clears it after reading it
     cudaError_t r = recordEvent(e, e->ev[0]);
@@ -578,6 +655,8 @@ int statusOf(double st) {
         return GF_ERR_NONPOS_NORM;
     if(s & 4)
         return GF_ERR_ZERO_NLL;
+    if(s & 8)
+        return GF_ERR_TIMEOUT;
     return GF_OK;
 }
 
@@ -614,6 +693,8 @@ int loadModule(gf_engine *e) {
     if((rc = get(e->mod.amp, "gf_amp", hasAmp)) || (rc = get(e->mod.ampn, "gf_ampn", hasAmp)) ||
        (rc = get(e->mod.gram, "gf_gram", hasAmp)))
         return rc;
+    if((rc = get(e->mod.fcn_g, "gf_fcn_g", e->plan.fused)) || (rc = get(e->mod.fcn_n, "gf_fcn_n", e->plan.fused)))
+        return rc;
     auto smem = [&](cudaKernel_t k, size_t bytes) -> int {
         if(!k || bytes <= 48 * 1024)
             return GF_OK;
@@ -624,7 +705,8 @@ int loadModule(gf_engine *e) {
     };
     if((rc = smem(e->mod.conv_g, e->plan.conv_smem_grad)) || (rc = smem(e->mod.conv_n, e->plan.conv_smem_nograd)) ||
        (rc = smem(e->mod.evt_g, e->plan.evt_smem_grad)) || (rc = smem(e->mod.evt_n, e->plan.evt_smem_nograd)) ||
-       (rc = smem(e->mod.val_n, e->plan.evt_smem_nograd)))
+       (rc = smem(e->mod.val_n, e->plan.evt_smem_nograd)) || (rc = smem(e->mod.fcn_g, e->plan.fused_smem[1])) ||
+       (rc = smem(e->mod.fcn_n, e->plan.fused_smem[0])))
         return rc;
     const size_t maxSmem = 227 * 1024;
     if(e->plan.conv_smem_grad > maxSmem || e->plan.evt_smem_grad > maxSmem)
@@ -1227,8 +1309,15 @@ int gf_run(gf_engine *e, bool grad, int, int) {
         if((rc = autotune(e)))
             return rc;
     }
+    // one-launch evaluation: every chunk row's status starts negative and only the CTA that evaluated the
+    // chunk overwrites it, so an evaluation that a barrier wait stopped cannot pass for a result
+    const bool fused = fusedPath(e);
+    const int frow   = fused ? e->plan.fused_row[grad ? 1 : 0] : 0;
+    if(fused)
+        for(int c = 0; c < e->n_chunks; ++c)
+            e->h_fpart[(size_t)c * frow + frow - 1] = -1.0;
     cudaError_t r;
-    if(e->use_graph) {
+    if(e->use_graph && !(fused && !e->fused_graph_ok)) {
         cudaGraphExec_t &ge = e->graph[grad ? 1 : 0];
         if(!ge) {
             cudaGraph_t g = nullptr;
@@ -1237,24 +1326,74 @@ int gf_run(gf_engine *e, bool grad, int, int) {
                 return gf_cuda_check(e, r, "cudaStreamBeginCapture");
             cudaError_t r1 = enqueueEval(e, grad);
             r              = cudaStreamEndCapture(e->stream, &g);
-            if(r1 != cudaSuccess) {
-                if(g)
-                    cudaGraphDestroy(g);
+            if(r1 == cudaSuccess && r == cudaSuccess) {
+                r = cudaGraphInstantiate(&ge, g, 0);
+                if(r != cudaSuccess)
+                    ge = nullptr;
+            }
+            if(fused && ge) {
+                // the graph's one kernel node: its arguments carry the record, replaced before every launch
+                size_t nn = 0;
+                cudaGraphGetNodes(g, nullptr, &nn);
+                std::vector<cudaGraphNode_t> nodes(nn);
+                cudaGraphGetNodes(g, nodes.data(), &nn);
+                cudaGraphNode_t kn = nullptr;
+                for(auto nd : nodes) {
+                    cudaGraphNodeType ty;
+                    if(cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel)
+                        kn = nd;
+                }
+                if(kn) {
+                    cudaKernelNodeParams &kp = e->fused_kp[grad ? 1 : 0];
+                    kp                       = cudaKernelNodeParams{};
+                    kp.func                  = (void *)(grad ? e->mod.fcn_g : e->mod.fcn_n);
+                    kp.gridDim               = dim3(e->fcn_grid);
+                    kp.blockDim              = dim3(e->block);
+                    kp.sharedMemBytes        = (unsigned)e->plan.fused_smem[grad ? 1 : 0];
+                    e->graph_src[grad ? 1 : 0]  = g;
+                    e->fused_node[grad ? 1 : 0] = kn;
+                    g                           = nullptr;
+                } else {
+                    cudaGetLastError();
+                    cudaGraphExecDestroy(ge);
+                    ge = nullptr;
+                    r  = cudaErrorNotSupported;
+                }
+            }
+            if(g)
+                cudaGraphDestroy(g);
+            if(fused && (r1 != cudaSuccess || r != cudaSuccess)) {
+                // a cooperative launch this runtime does not capture: launch it directly from now on
+                cudaGetLastError();
+                e->fused_graph_ok = false;
+                ge                = nullptr;
+            } else if(r1 != cudaSuccess)
                 return gf_cuda_check(e, r1, "capturing the evaluation graph");
-            }
-            if(r != cudaSuccess)
-                return gf_cuda_check(e, r, "cudaStreamEndCapture");
-            r = cudaGraphInstantiate(&ge, g, 0);
-            cudaGraphDestroy(g);
-            if(r != cudaSuccess) {
-                ge = nullptr;
-                return gf_cuda_check(e, r, "cudaGraphInstantiate");
-            }
+            else if(r != cudaSuccess)
+                return gf_cuda_check(e, r, "cudaStreamEndCapture / cudaGraphInstantiate");
         }
-        NvtxScope s("gf_graph_launch");
-        r = cudaGraphLaunch(ge, e->stream);
+        if(ge) {
+            NvtxScope s("gf_graph_launch");
+            if(fused) {
+                GfArgs a                = fusedArgs(e, grad);
+                void *args[]            = {&a};
+                cudaKernelNodeParams kp = e->fused_kp[grad ? 1 : 0];
+                kp.kernelParams         = args;
+                kp.extra                = nullptr;
+                r                       = cudaGraphExecKernelNodeSetParams(ge, e->fused_node[grad ? 1 : 0], &kp);
+                if(r != cudaSuccess) {
+                    // this runtime does not update the captured cooperative node: launch directly from now on
+                    cudaGetLastError();
+                    e->fused_graph_ok = false;
+                    r                 = enqueueEval(e, grad);
+                } else
+                    r = cudaGraphLaunch(ge, e->stream);
+            } else
+                r = cudaGraphLaunch(ge, e->stream);
+        } else
+            r = enqueueEval(e, grad);
         if(r != cudaSuccess)
-            return gf_cuda_check(e, r, "cudaGraphLaunch");
+            return gf_cuda_check(e, r, "evaluation launch");
     } else {
         r = enqueueEval(e, grad);
         if(r != cudaSuccess)
@@ -1266,6 +1405,53 @@ int gf_run(gf_engine *e, bool grad, int, int) {
     float ms = 0;
     if(cudaEventElapsedTime(&ms, e->ev[0], e->ev[3]) == cudaSuccess)
         e->last_ms_total = ms;
+    bool stopped = false;
+    if(fused) {
+        // the chunk rows in chunk order: sums of the components, the OR of the status words; a row still
+        // holding its -1 was never written (its CTA stopped at a barrier or on its bulk copy)
+        const int nc = frow - 1, NGp = 1 + (grad ? e->tree.NG : 0);
+        std::vector<double> sum(std::max(1, nc), 0.0);
+        int st = 0;
+        for(int c = 0; c < e->n_chunks; ++c) {
+            const double *row = e->h_fpart + (size_t)c * frow;
+            if(row[nc] < 0) {
+                stopped = true;
+                continue;
+            }
+            st |= (int)row[nc];
+            for(int k = 0; k < nc; ++k)
+                sum[k] += row[k];
+        }
+        double *o = e->h_out;
+        o[0]      = sum[0];
+        for(int k = 1; k < NGp; ++k)
+            o[1 + k] = sum[k];
+        if(e->plan.factor_root)
+            o[2 + e->tree.NG] = sum[NGp];
+        else if(o[0] == 0.0)
+            st |= 4;
+        o[1]    = (double)st;
+        stopped = stopped || (st & 8);
+        if(!stopped && (st & 3)) {
+            // a numeric normalisation was NaN or not positive: clear the flag word for the next evaluation
+            cudaMemsetAsync(e->d_qflag, 0, sizeof(int) * e->n_toys, e->stream);
+            cudaStreamSynchronize(e->stream);
+        }
+    }
+    if(stopped) {
+        // a grid barrier wait ran out: clear the barrier words and the completion counters and flags that
+        // the stopped CTAs left behind, so that the next evaluation starts clean
+        const gf::Tree &T = e->tree;
+        cudaMemsetAsync(e->d_gbar, 0, 4 * sizeof(unsigned), e->stream);
+        cudaMemsetAsync(e->d_counter, 0, sizeof(unsigned) * e->n_toys, e->stream);
+        cudaMemsetAsync(e->d_gcounter, 0, sizeof(unsigned) * e->n_toys * std::max<size_t>(1, T.nums.size()), e->stream);
+        cudaMemsetAsync(e->d_qflag, 0, sizeof(int) * e->n_toys, e->stream);
+        r = cudaStreamSynchronize(e->stream);
+        if(r != cudaSuccess)
+            return gf_cuda_check(e, r, "clearing the grid barrier");
+        e->h_out[1] = 8.0;
+        return gf_fail(e, GF_ERR_TIMEOUT, "a grid barrier wait of the one-launch evaluation ran out");
+    }
     return GF_OK;
 }
 
@@ -1316,6 +1502,10 @@ int gf_engine_create(gf_engine **out, int device, int precision) {
     e->use_pdl = precision == GF_MIXED;
     if(const char *p = std::getenv("GF_NO_PDL"))
         e->use_pdl = e->use_pdl && !(p[0] == '1');
+    if(const char *f = std::getenv("GF_FUSED"))
+        e->use_fused = !(f[0] == '0');
+    if(const char *st = std::getenv("GF_STAGE"))
+        e->use_stage = !(st[0] == '0');
     if(const char *c = std::getenv("GF_EVT_CTAS_PER_SM")) {
         e->evt_ctas_per_sm   = std::max(1, atoi(c));
         e->evt_ctas_fixed    = true;
@@ -1410,6 +1600,21 @@ static int compileTree(gf_engine *e) {
             occ = 0;
         }
         e->evt_ctas_per_sm = std::min(8, std::max(1, occ));
+    }
+    // the one-launch kernel's grid: every CTA resident (a cooperative launch), at most as many per SM as the
+    // event kernel's chunk layout assumes
+    e->fcn_grid = 0;
+    if(e->plan.fused && e->mod.fcn_g && e->mod.fcn_n) {
+        int o1 = 0, o0 = 0;
+        if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, (const void *)e->mod.fcn_g, e->block,
+                                                         e->plan.fused_smem[1]) != cudaSuccess ||
+           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o0, (const void *)e->mod.fcn_n, e->block,
+                                                         e->plan.fused_smem[0]) != cudaSuccess) {
+            cudaGetLastError();
+            o1 = o0 = 0;
+        }
+        const int per = std::min(std::min(o1, o0), e->evt_ctas_per_sm);
+        e->fcn_grid   = per > 0 ? per * e->sm_count : 0;
     }
     return GF_OK;
 }
@@ -1903,9 +2108,18 @@ int gf_time_kernels(gf_engine *e, int toy, int with_grad, double *ms_conv, doubl
 
 int64_t gf_event_chunk(const gf_engine *e) { return e && e->layout_ready ? e->chunk : 0; }
 
+int gf_set_wait_limit(gf_engine *e, uint64_t ns) {
+    if(!e)
+        return gf_fail(nullptr, GF_ERR_INVALID, "null engine");
+    e->bar_ns = ns ? ns : 1000000000ull;
+    return GF_OK;
+}
+
 int gf_launches_per_eval(const gf_engine *e, int) {
     if(!e || !e->has_tree)
         return 0;
+    if(fusedPath(e))
+        return 1;
     return 1 + (e->tree.convs.empty() ? 0 : 1) + (e->tree.nums.empty() || !gridWork(e) ? 0 : 1);
 }
 

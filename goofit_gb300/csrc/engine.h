@@ -44,6 +44,14 @@ struct GfArgs {
     int gtoy;
     long long chunk;      // events per chunk
     long long nevt0;      // events of toy 0
+    unsigned *gbar;       // grid barrier words of the one-launch evaluation [arrivals, generation, error]
+    unsigned long long bar_ns; // longest barrier wait (ns) before the one-launch kernel gives up
+    int rec_n;            // one-launch evaluation: the toy's record (rec_n R values) passed by value in rec
+    int stage_off;        // one-launch evaluation: shared-memory offset and room (bytes) of the staged events
+    unsigned stage_cap;
+    int stage_pad;
+    double *hpart;        // one-launch evaluation: per-chunk [components..., status] rows in page-locked memory
+    alignas(16) unsigned char rec[512];
     const void *p0[192];  // toy 0: observable columns, bin-offset columns, amplitude columns (one toy only)
 };
 
@@ -69,6 +77,7 @@ struct GfModule {
     cudaKernel_t conv_g = nullptr, conv_n = nullptr, grid_g = nullptr, grid_n = nullptr;
     cudaKernel_t evt_g = nullptr, evt_n = nullptr, val_n = nullptr;
     cudaKernel_t amp = nullptr, ampn = nullptr, gram = nullptr;
+    cudaKernel_t fcn_g = nullptr, fcn_n = nullptr; // one toy: the whole evaluation in one cooperative launch
 };
 
 struct gf_engine {
@@ -157,6 +166,22 @@ struct gf_engine {
     double last_ms_total = 0, last_ms_evt = 0;
     bool use_graph = true;
     bool use_pdl   = true;
+    // one-launch evaluation (one toy, unbinned NLL): resident CTAs of the cooperative launch, the barrier
+    // words it synchronises on and the longest barrier wait before it gives up (GF_FUSED=0: three launches)
+    bool use_fused        = true;
+    bool use_stage        = true; // GF_STAGE=0: the one-launch kernel reads events from global memory
+    int fcn_grid          = 0;
+    unsigned *d_gbar      = nullptr;
+    unsigned long long bar_ns = 1000000000ull;
+    bool fused_graph_ok   = true; // false: the cooperative launch is not captured into a graph here
+    // captured one-launch graphs [nograd, grad]: the source graph, its kernel node and that node's launch
+    // parameters, whose arguments (the toy's record by value) are replaced before every graph launch
+    cudaGraph_t graph_src[2]         = {nullptr, nullptr};
+    cudaGraphNode_t fused_node[2]    = {nullptr, nullptr};
+    cudaKernelNodeParams fused_kp[2] = {};
+    // the one-launch kernel's per-chunk rows (mapped page-locked memory), chunk_cap rows of fused_row doubles
+    double *h_fpart = nullptr, *d_fpart = nullptr;
+    int fused_row   = 0;
 };
 
 // helpers shared between translation units

@@ -213,6 +213,13 @@ struct KernelPlan {
     // the root's normalisation is applied on the host: the event pass returns sum -log P, sum -dP/P and the
     // count of events with P > 0 (out[2 + NG]); the host adds count * (-log N) and count * (-dN/N)
     bool factor_root = false;
+    // one toy: the whole evaluation as one cooperative launch (gf_fcn_g / gf_fcn_n), [nograd, grad]
+    bool fused = false;
+    bool fused_tab = false;             // its event pass gathers per-k tabulated terms (event function of k alone)
+    size_t fused_smem[2] = {0, 0};      // dynamic shared memory, staged events included
+    size_t fused_stage_off[2] = {0, 0}; // where the staged events start (after the tables' working space)
+    size_t fused_stage_cap[2] = {0, 0}; // and the bytes of them that fit
+    int fused_row[2] = {0, 0};          // doubles per chunk row it writes to host memory (components, status)
     NormLayout nl;
 };
 

@@ -229,6 +229,10 @@ class Engine:
     def launches_per_eval(self, grad: bool = True) -> int:
         return self._L.gf_launches_per_eval(self._h, 1 if grad else 0)
 
+    def set_wait_limit(self, ns: int) -> None:
+        """Longest device-side wait at the one-launch evaluation's grid barrier (ns; 0: the default 1 s)."""
+        self._check(self._L.gf_set_wait_limit(self._h, int(ns)))
+
     def event_chunk(self) -> int:
         """Events per chunk of the event pass (after the autotuner, once an evaluation has run)."""
         return int(self._L.gf_event_chunk(self._h))

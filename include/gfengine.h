@@ -200,6 +200,11 @@ int gf_launches_per_eval(const gf_engine *eng, int with_grad);
 /* Events per chunk of the event pass (chosen from the occupancy, then by the autotuner at the first
    evaluation of a layout unless GF_AUTOTUNE=0 or GF_CHUNK is set); 0 before the first evaluation. */
 int64_t gf_event_chunk(const gf_engine *eng);
+/* Longest wait, in nanoseconds of the GPU's global timer, at the grid barrier of the one-launch evaluation
+ * (one toy: tables, grids and event pass in one cooperative launch); ns = 0 restores the default of 1 s.
+ * A wait that runs out stops the launch, the call returns GF_ERR_TIMEOUT and the engine stays usable.
+ * No counterpart in the reference (its Thrust reductions have no device-side waits). */
+int gf_set_wait_limit(gf_engine *eng, uint64_t ns);
 
 /* ---- minimiser (Minuit2 MnMigrad surface, src/goofit/FitManagerMinuit2.cpp:31-119) ---- */
 typedef struct gf_minimizer gf_minimizer;

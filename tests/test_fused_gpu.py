@@ -1,0 +1,97 @@
+"""The one-launch evaluation (one toy): convolution tables, numeric grids and the event pass of an FCN in
+one cooperative launch with a bounded grid barrier, against the FP64 oracle and against the three-launch
+chain of the same engine, in both event-pass forms (per-k tabulated terms, per-event arithmetic) and with
+the events bulk-copied to shared memory or read from global memory; and the barrier's bounded wait made
+to run out on purpose (a limit of 1 ns, which the waiting CTAs exceed while the table CTAs still work),
+after which the same engine must return the oracle's values again.
+
+Tolerances as in the other parity tests: NLL 1e-6 relative (mixed) / 1e-10 (FP64); gradient against the
+oracle's central differences within 2e-4 relative + 2e-3 sqrt(n).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import goofit_gb300 as gf
+from goofit_gb300 import _abi as A
+from goofit_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+NLL_RTOL = {"mixed": 1e-6, "fp64": 1e-10}
+
+
+def c2_engine(n, seed, prec, monkeypatch, fused="1", tab="1", stage="1"):
+    wl = W.make_c2(n, seed=seed)
+    nodes, params, obs = wl.pdf._flatten()
+    olist = [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs]
+    mask = [0 if v.fixed else 1 for v in params]
+    pv = np.array([v.value for v in params])
+    monkeypatch.setenv("GF_FUSED", fused)
+    monkeypatch.setenv("GF_EVT_TAB", tab)
+    monkeypatch.setenv("GF_STAGE", stage)
+    eng = gf.Engine(prec)
+    eng.set_tree(nodes, olist, len(params), mask)
+    eng.upload(wl.data.to_numpy())
+    return eng, wl, nodes, olist, params, mask, pv
+
+
+@pytest.mark.parametrize("form", [("1", "1"), ("0", "1"), ("1", "0")], ids=["tab-staged", "perevent-staged",
+                                                                        "tab-global"])
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+@pytest.mark.parametrize("n", [5_000, 2_000_000])
+def test_one_launch_matches_oracle_and_three_launches(n, prec, form, monkeypatch):
+    tab, stage = form
+    eng, wl, nodes, olist, params, mask, pv = c2_engine(n, 31, prec, monkeypatch, "1", tab, stage)
+    eng3 = c2_engine(n, 31, prec, monkeypatch, "0")[0]
+    data = wl.data.to_numpy()
+    names = [v.name for v in params]
+    free = [i for i, m in enumerate(mask) if m]
+    for shift in (0.0, 0.04, -0.03):
+        p = pv.copy()
+        p[names.index("alpha")] += shift
+        p[names.index("mu")] += shift / 3
+        got, g = eng.nll_grad(p)
+        assert eng.launches_per_eval(True) == 1
+        ref = O.nll(nodes, olist, p, data)
+        assert got == pytest.approx(ref, rel=NLL_RTOL[prec]), (shift, got, ref)
+        assert eng.nll(p) == pytest.approx(ref, rel=NLL_RTOL[prec])
+        got3, g3 = eng3.nll_grad(p)
+        assert eng3.launches_per_eval(True) > 1
+        assert got == pytest.approx(got3, rel=NLL_RTOL[prec])
+        np.testing.assert_allclose(g, g3, rtol=1e-5, atol=1e-4 * math.sqrt(n))
+        if n <= 5_000:
+            fd = O.fd_grad(nodes, olist, p, data, free, h=1e-6)
+            np.testing.assert_allclose(g, fd, rtol=2e-4, atol=2e-3 * math.sqrt(n))
+    eng.close()
+    eng3.close()
+
+
+def test_invalid_normalisation_in_one_launch(monkeypatch):
+    eng, wl, nodes, olist, params, mask, pv = c2_engine(3000, 33, "mixed", monkeypatch)
+    p = pv.copy()
+    p[[v.name for v in params].index("sigma")] = float("nan")
+    with pytest.raises(A.EngineError) as ei:
+        eng.nll_grad(p)
+    assert ei.value.code == A.GF_ERR_NAN_NORM
+    assert eng.nll_grad(pv)[0] == pytest.approx(O.nll(nodes, olist, pv, wl.data.to_numpy()), rel=1e-6)
+    eng.close()
+
+
+def test_barrier_wait_that_runs_out_is_reported_and_recovered(monkeypatch):
+    eng, wl, nodes, olist, params, mask, pv = c2_engine(200_000, 32, "mixed", monkeypatch)
+    data = wl.data.to_numpy()
+    ref = O.nll(nodes, olist, pv, data)
+    assert eng.nll_grad(pv)[0] == pytest.approx(ref, rel=1e-6)
+    for _ in range(2):
+        eng.set_wait_limit(1)
+        with pytest.raises(A.EngineError) as ei:
+            eng.nll_grad(pv)
+        assert ei.value.code == A.GF_ERR_TIMEOUT
+        eng.set_wait_limit(0)
+        got, g = eng.nll_grad(pv)
+        assert got == pytest.approx(ref, rel=1e-6)
+        assert eng.nll(pv) == pytest.approx(ref, rel=1e-6)
+    eng.close()
