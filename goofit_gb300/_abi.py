@@ -117,6 +117,7 @@ class gf_fit_options(C.Structure):
         ("use_grad", C.c_int32),
         ("reserved", C.c_int32),
         ("fnoise_rel", C.c_double),
+        ("cov", _f64p),
     ]
 
 

@@ -1456,6 +1456,8 @@ class FitManager:
             v.value = res.values[i] + blind[i]
             v.error = res.errors[i]
         self.result = res
+        # external covariance of the final Hesse over all parameters (fixed ones have zero rows)
+        self.covariance = res.covariance
         self.retval = FitManager.Valid if res.valid else FitManager.InValid
         self.minos_errors = {}
         if self.minos and res.valid:

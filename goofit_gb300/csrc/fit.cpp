@@ -235,6 +235,8 @@ int gf_fit_batch_impl(gf_engine *eng, int toy, int n_toys, const gf_fit_options 
             std::memcpy(X + (size_t)t * np, r.x.data(), sizeof(double) * np);
         if(ERR)
             std::memcpy(ERR + (size_t)t * np, r.err.data(), sizeof(double) * np);
+        if(o->cov && r.cov.size() == (size_t)np * np)
+            std::memcpy(o->cov + (size_t)t * np * np, r.cov.data(), sizeof(double) * np * np);
         fillResult(r, res ? res + t : nullptr);
     }
     return rc;

@@ -34,12 +34,13 @@ class FitResult:
     hesse_failed: bool
     made_posdef: bool
     n_iter: int
+    covariance: np.ndarray | None = None  # external covariance of the final Hesse (n x n), when requested
 
     @staticmethod
-    def from_c(r: A.gf_fit_result, x, e) -> "FitResult":
+    def from_c(r: A.gf_fit_result, x, e, cov=None) -> "FitResult":
         return FitResult(np.array(x, dtype=float), np.array(e, dtype=float), r.fmin, r.edm, r.nfcn, r.ngrad,
                          bool(r.valid), bool(r.above_max_edm), bool(r.call_limit), bool(r.has_covariance),
-                         bool(r.hesse_failed), bool(r.made_posdef), r.n_iter)
+                         bool(r.hesse_failed), bool(r.made_posdef), r.n_iter, cov)
 
     # Minuit2::FunctionMinimum spellings used by GooFit users
     def IsValid(self) -> bool:
@@ -255,10 +256,12 @@ class Engine:
         xa, xp = A.f64(x0)
         x = np.zeros(n)
         e = np.zeros(n)
+        cov = np.zeros((n, n))
+        o.cov = cov.ctypes.data_as(A._f64p)
         r = A.gf_fit_result()
         self._check(self._L.gf_fit(self._h, toy, C.byref(o), xp, x.ctypes.data_as(A._f64p),
                                    e.ctypes.data_as(A._f64p), C.byref(r)))
-        return FitResult.from_c(r, x, e)
+        return FitResult.from_c(r, x, e, cov)
 
     def fit_batch(self, X0, err, lo, hi, limited, fixed, *, up=0.5, tolerance=0.1, strategy=1, maxfcn=0,
                   use_grad=True, fnoise_rel=None) -> list[FitResult]:
@@ -270,10 +273,12 @@ class Engine:
         X0 = np.ascontiguousarray(X0, dtype=np.float64).reshape(T, n)
         X = np.zeros((T, n))
         E = np.zeros((T, n))
+        COV = np.zeros((T, n, n))
+        o.cov = COV.ctypes.data_as(A._f64p)
         R = (A.gf_fit_result * T)()
         self._check(self._L.gf_fit_batch(self._h, T, C.byref(o), X0.ctypes.data_as(A._f64p),
                                          X.ctypes.data_as(A._f64p), E.ctypes.data_as(A._f64p), R))
-        return [FitResult.from_c(R[t], X[t], E[t]) for t in range(T)]
+        return [FitResult.from_c(R[t], X[t], E[t], COV[t]) for t in range(T)]
 
 
 class Minimizer:

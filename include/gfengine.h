@@ -266,6 +266,8 @@ typedef struct gf_fit_options {
     int32_t reserved;
     double fnoise_rel;       /* relative rounding noise of the NLL (0: exact FP64 sums); the line search
                                 treats value changes below fnoise_rel * |NLL| as ties and follows the gradient */
+    double *cov;             /* optional out: [n_toys][n_params][n_params] external covariance of the final
+                                Hesse (Minuit2's FunctionMinimum::UserCovariance); NULL: not returned */
 } gf_fit_options;
 
 /* Fits toy `toy` starting from x0[n_params]; x/err receive the result. */

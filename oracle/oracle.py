@@ -118,6 +118,18 @@ def fd_grad(nodes, observables, params, soa, indices, h: float = 1e-5) -> np.nda
     return g
 
 
+def minimum_offset_sigma(nodes, observables, params, soa, cov, free, h: float = 1e-5) -> np.ndarray:
+    """Distance, per free parameter and in units of its error, from `params` to the oracle's own NLL
+    minimum: one Newton step -V g with g the oracle's central-difference gradient at `params` and V the
+    fit's covariance (for an NLL with up = 0.5, V is the inverse Hessian).  Exact for a quadratic NLL, so a
+    fitted point within 0.01 sigma of the oracle's minimum gives values below 0.01 here."""
+    free = list(free)
+    g = fd_grad(nodes, observables, params, soa, free, h=h)
+    V = np.asarray(cov, dtype=np.float64)[np.ix_(free, free)]
+    step = V @ g
+    return np.abs(step) / np.sqrt(np.diag(V))
+
+
 def mt19937_exponential(seed: int, lam: float, n: int) -> np.ndarray:
     """std::mt19937(seed) + std::exponential_distribution<>(lam) draws."""
     out = np.zeros(n)
