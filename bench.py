@@ -1,8 +1,9 @@
-"""Benchmark of the fit path on the composite 1-D workload (2,000,000 events).
+"""Benchmark of the fit path on the composite 1-D workload (2,000,000 events), with --config c1/c3/c4/c5
+legs for the other configurations.
 
-Workload: AddPdf(fsig; ConvolutionPdf(ExpPdf(alpha), GaussianPdf(mu, sigma)), flat PolynomialPdf) on
-x in [-5, 10], tau = 1.5, mu = 0, sigma = 0.3, background fraction 0.3, 10,000-bin numeric
-normalisation, 2e6 seeded synthetic events (accept-reject on the model density).
+Workload (default, C2): AddPdf(fsig; ConvolutionPdf(ExpPdf(alpha), GaussianPdf(mu, sigma)), flat
+PolynomialPdf) on x in [-5, 10], tau = 1.5, mu = 0, sigma = 0.3, background fraction 0.3, 10,000-bin
+numeric normalisation, 2e6 seeded synthetic events (accept-reject on the model density).
 
 A step is one FCN call of MIGRAD on the whole dataset: the NLL and its analytic gradient with
 respect to the four floated parameters, i.e. 2e6 event-NLL evaluations.  `value` is event-NLL
@@ -10,6 +11,11 @@ evaluations per second with the events resident in HBM; the L2 cache (129 MB) is
 256 MB write before every timed step because the event columns (16 MB) would otherwise stay in L2.
 `e2e` repeats the step through the C ABI with host buffers: the FP64 events are copied from pinned
 host memory and converted on the device every step, and the NLL/gradient are read back.
+
+`fit` runs MIGRAD at tolerance 0.01 three ways on the same data: mixed precision + analytic gradient,
+FP64 + analytic gradient (the precision change alone) and FP64 + numerical gradient (the reference's
+plain path); `parity` compares the mixed fit with the FP64 fit and, outside any timed region, with the
+FP64 oracle (NLL at the minimum, and the distance to the oracle's own minimum in units of sigma).
 
 --impl reference times the reference algorithm on the host cores instead: the FP64 restatement of
 GooFit's OMP path (brute-force convolution per event, numeric normalisation), on a bounded sample.
@@ -39,6 +45,10 @@ EVT_DRAM_EVENTS = 2_000_000
 # DRAM bytes of one gf_evt_g launch of the amplitude workloads (profiles/gf_evt_g_amp3_amp4_c3_c5.md):
 # C3 over 5e5 events, C5 over 3e5 events
 EVT_DRAM_BYTES_AMP = {"c3": (32_034_048, 500_000), "c5": (14_432_256, 300_000)}
+# DRAM bytes of one gf_fcn_g launch (the one-launch FCN) over 2e6 events, from one ncu capture
+# (profiles/gf_fcn_g_c2_composite_2e6.md)
+FCN_DRAM_BYTES = 8_081_920
+FCN_DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/gf_fcn_g_c2_composite_2e6.md"
 N_EVENTS = 2_000_000
 WORKLOAD = "c2: AddPdf(0.7 Conv(Exp tau=1.5, Gauss mu=0 sigma=0.3) + 0.3 flat Poly), x in [-5,10], 2e6 events"
 
@@ -177,6 +187,68 @@ def cpu_baseline(sample: int, reps: int = 2) -> dict:
                       "brute-force convolution per event)"}
 
 
+def fit_report(wl, nodes, olist, params, free, norm=None, tolerance: float = 0.01) -> dict:
+    """MIGRAD on the workload three ways (mixed + analytic, FP64 + analytic, FP64 + numerical gradient) at
+    the given tolerance, then the parity of the mixed fit against the FP64 fit and the FP64 oracle (the
+    oracle as checker, after the timed fits)."""
+    import numpy as np
+
+    import goofit_gb300 as gf
+    from oracle import oracle as O
+
+    fits, cov = {}, None
+    for label, prec, grad in (("mixed_analytic", "mixed", "analytic"), ("fp64_analytic", "fp64", "analytic"),
+                              ("fp64_numerical", "fp64", "numerical")):
+        # the engine of this precision evaluates once before the timed fit (layout, event-chunk autotuner,
+        # captured graphs, amplitude caches: one-time costs of a data set, not of the fit)
+        wl.reset()
+        eng, _ = wl.pdf._engine_for(wl.data, prec)
+        p0 = np.array([v.value for v in params])
+        eng.nll(p0)
+        eng.nll_grad(p0)
+        wl.reset()
+        fm = gf.FitManager(wl.pdf, precision=prec, gradient=grad, tolerance=tolerance)
+        fm.verbosity = 0
+        r = fm.fit()
+        fits[label] = {"wall_s": fm.wall_seconds, "nfcn": r.nfcn, "valid": r.valid, "fmin": r.fmin, "edm": r.edm,
+                       "values": {params[i].name: params[i].value for i in free},
+                       "errors": {params[i].name: params[i].error for i in free}}
+        if label == "mixed_analytic":
+            cov = fm.covariance
+            xm = np.array([v.value for v in params])
+    m, a, n = fits["mixed_analytic"], fits["fp64_analytic"], fits["fp64_numerical"]
+    fits["tolerance"] = tolerance
+    fits["speedup_wall"] = n["wall_s"] / m["wall_s"]
+    fits["speedup_wall_precision_only"] = a["wall_s"] / m["wall_s"]
+    data = wl.data.to_numpy()
+    if norm is not None:
+        O.set_amp4_norm_events(norm)
+    ref = O.nll(nodes, olist, xm, data)
+    off = O.minimum_offset_sigma(nodes, olist, xm, data, cov, free)
+    parity = {
+        "mixed_vs_fp64_rel_dnll": abs(m["fmin"] - a["fmin"]) / abs(a["fmin"]),
+        "mixed_vs_fp64_max_dsigma": max(abs(m["values"][k] - a["values"][k]) / a["errors"][k] for k in m["values"]),
+        "oracle_rel_nll": abs(m["fmin"] - ref) / abs(ref),
+        "oracle_max_dsigma": float(np.max(off)),
+        "oracle": "FP64 CPU restatement of the reference algorithm; distance to its minimum = one Newton step "
+                  "with its central-difference gradient and the mixed fit's covariance",
+    }
+    return {"fit": fits, "parity": parity}
+
+
+def fcn_wall_us(call, n: int = 50) -> float:
+    """Median host wall time of one FCN call (warm, no L2 flush, no clock sampler running)."""
+    import numpy as np
+    for _ in range(3):
+        call()
+    t = []
+    for _ in range(n):
+        t0 = time.perf_counter()
+        call()
+        t.append(time.perf_counter() - t0)
+    return float(np.median(t) * 1e6)
+
+
 def run_engine(args) -> dict | None:
     import ctypes as C
 
@@ -215,27 +287,41 @@ def run_engine(args) -> dict | None:
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    dev_ms, evt_ms = [], []
-    with ClockSampler(local) as clk:
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            flush.zero_()
+
+    def timed(sampler: bool):
+        dev_ms = []
+        clk = ClockSampler(local) if sampler else None
+        if clk:
+            clk.__enter__()
+        try:
+            if world > 1:
+                import torch.distributed as dist
+                dist.barrier()
             torch.cuda.synchronize()
-            step()
-            a, b = eng.last_timing()
-            dev_ms.append(a)
-            evt_ms.append(b)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                step()
+                dev_ms.append(eng.last_timing()[0])
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        finally:
+            if clk:
+                clk.__exit__(None, None, None)
+        return dev_ms, wall, clk
+
+    dev_ms, wall, clk = timed(True)
     ms = float(np.mean(dev_ms))
     ms = barrier_max(ms, world, dev)
     value = world * N_EVENTS / (ms / 1e3)
+    # the same loop without the nvidia-smi sampler, and the FCN call alone (host wall, warm)
+    _, wall_nosampler, _ = timed(False)
+    fcn_us = fcn_wall_us(step)
 
-    # each kernel of the evaluation launched alone (CUDA events on the engine's stream), L2 flushed first
+    launches = eng.launches_per_eval(True)
+    one_launch = launches == 1
+    # the three-launch chain's kernels, each launched alone (CUDA events on the engine's stream, L2 flushed)
     kt = []
     for _ in range(max(args.steps, 5)):
         flush.zero_()
@@ -255,32 +341,26 @@ def run_engine(args) -> dict | None:
             e2e_ms.append(1e3 * dt)
     e2e = barrier_max(float(np.mean(e2e_ms)), world, dev)
 
-    # roofline of the event kernel: algorithmic bytes = the int32 bin offset of every event
-    # (the flat polynomial needs no x; the convolution needs x only through its bin offset)
+    # roofline of the dominant kernel.  One launch per FCN (gf_fcn_g): the whole step is that kernel, timed
+    # by the CUDA events around it; three launches: the event kernel launched alone.  Algorithmic bytes = the
+    # int32 bin offset of every event (the flat polynomial needs no x; the convolution needs x only through
+    # its bin offset); the tables stay on chip.
     bytes_per_event = 4
-    evt = float(kt[2])
+    kern_ms = ms if one_launch else float(kt[2])
     peaks = load_peaks()
-    achieved = N_EVENTS * bytes_per_event / (evt / 1e3) / 1e9
+    achieved = N_EVENTS * bytes_per_event / (kern_ms / 1e3) / 1e9
+    traffic = FCN_DRAM_BYTES if one_launch else EVT_DRAM_BYTES_PER_LAUNCH * N_EVENTS / EVT_DRAM_EVENTS
+    traffic_src = (FCN_DRAM_SOURCE if one_launch else
+                   "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/gf_evt_g_c2_composite_2e6.md")
 
-    # MIGRAD fits on the same data: mixed + analytic gradient vs FP64 + numerical gradient
-    fits = {}
+    rep = {}
     if rank == 0 and not args.no_fit:
-        for label, prec, grad in (("mixed_analytic", "mixed", "analytic"), ("fp64_numerical", "fp64", "numerical")):
-            wl.reset()
-            fm = gf.FitManager(wl.pdf, precision=prec, gradient=grad, tolerance=0.1)
-            fm.verbosity = 0
-            r = fm.fit()
-            fits[label] = {"wall_s": fm.wall_seconds, "nfcn": r.nfcn, "valid": r.valid, "fmin": r.fmin,
-                           "values": {v.name: v.value for v in params if not v.fixed},
-                           "errors": {v.name: v.error for v in params if not v.fixed}}
-        fits["speedup_wall"] = fits["fp64_numerical"]["wall_s"] / fits["mixed_analytic"]["wall_s"]
-        dn = fits["mixed_analytic"]["fmin"] - fits["fp64_numerical"]["fmin"]
-        fits["rel_dnll"] = abs(dn) / abs(fits["fp64_numerical"]["fmin"])
+        free = [i for i, m in enumerate(mask) if m]
+        rep = fit_report(wl, nodes, olist, params, free, tolerance=args.fit_tolerance)
 
     if rank != 0:
         return None
     cpu = cpu_baseline(args.cpu_sample) if not args.no_cpu else None
-    launches = eng.launches_per_eval(True)
     line = {
         "metric": METRIC, "value": value, "unit": "event-NLL evals/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -288,6 +368,7 @@ def run_engine(args) -> dict | None:
         "data": "synthetic (seeded accept-reject on the model density)",
         "config": {"workload": WORKLOAD, "events": N_EVENTS, "precision": args.precision,
                    "step": "one FCN call: NLL + analytic gradient (4 floated parameters)",
+                   "kernels_per_step": launches,
                    "l2": "flushed (256 MB write) before every timed step",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "event_chunk": eng.event_chunk(), "event_chunk_autotuned": os.environ.get("GF_AUTOTUNE", "1") != "0"},
@@ -295,27 +376,36 @@ def run_engine(args) -> dict | None:
                 "h2d_bytes_per_step": N_EVENTS * 8 + len(params) * 8, "d2h_bytes_per_step": (2 + eng.n_grad) * 8,
                 "ms_per_step": e2e},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "traffic": EVT_DRAM_BYTES_PER_LAUNCH * N_EVENTS / EVT_DRAM_EVENTS,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/gf_evt_g_c2_composite_2e6.md",
-                     "kernel": "gf_evt_g",
-                     "kernel_ms": evt, "bytes_per_event": bytes_per_event, "peak_source": peaks["src"],
-                     "kernels_alone_ms": {"gf_conv_g": float(kt[0]), "gf_grid_g": float(kt[1]), "gf_evt_g": float(kt[2])}},
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "traffic_source": traffic_src,
+                     "kernel": "gf_fcn_g" if one_launch else "gf_evt_g",
+                     "kernel_ms": kern_ms, "bytes_per_event": bytes_per_event, "peak_source": peaks["src"],
+                     "three_launch_kernels_alone_ms": {"gf_conv_g": float(kt[0]), "gf_grid_g": float(kt[1]),
+                                                       "gf_evt_g": float(kt[2])}},
         "cpu_baseline": cpu,
         "gpu_launches": launches * args.steps,
         "clocks": clk.summary(),
         "wall_ms_per_step": 1e3 * wall / args.steps,
-        "fit": fits,
+        "wall_ms_per_step_without_clock_sampler": 1e3 * wall_nosampler / args.steps,
+        "fcn_wall_us": fcn_us,
+        "wall_note": "wall_ms_per_step is the host time of the timed loop per step: the 256 MB L2 flush, two "
+                     "device synchronisations and the FCN call, with nvidia-smi sampling clocks alongside; "
+                     "fcn_wall_us is one FCN call alone (host wall, warm)",
     }
+    line.update(rep)
     return line
 
 
 def run_toys(args) -> dict:
     """C4: lockstep MIGRAD fits of n toys of the composite model, one batched graph launch per round."""
+    import ctypes as C
+
     import numpy as np
     import torch
 
     import goofit_gb300 as gf
+    from goofit_gb300 import _abi as A
     from goofit_gb300 import workloads as W
+    from oracle import oracle as O
 
     torch.cuda.set_device(0)
     study = W.make_c4(n_toys=args.toys, seed=4)
@@ -329,37 +419,76 @@ def run_toys(args) -> dict:
     hi = np.array([v.upperlimit for v in params])
     fixed = np.array([1 if v.fixed else 0 for v in params], np.int32)
     limited = np.array([0 if v.fixed else 1 for v in params], np.int32)
-    n_events = int(sum(d.shape[1] for d in study.datas))
+    free = [i for i in range(len(params)) if not fixed[i]]
+    counts = [int(d.shape[1]) for d in study.datas]
+    n_events = int(sum(counts))
+    tol = args.fit_tolerance
+    # the toys' FP64 events in one page-locked host block (the e2e leg uploads them from there every step)
+    host = torch.empty(n_events, dtype=torch.float64, pin_memory=True)
+    off = np.cumsum([0] + counts)
+    for t, d in enumerate(study.datas):
+        host.numpy()[off[t]:off[t + 1]] = d[0]
+    base = host.data_ptr()
+    L = A.lib()
     out = {"metric": METRIC, "config": {"workload": f"c4: {args.toys} toys of the composite model, Poisson(20000) "
                                                     "events clipped to [5000, 60000], +-10% jittered truths",
                                         "events_total": n_events}}
-    for label, prec, grad in (("mixed_analytic", "mixed", True), ("fp64_numerical", "fp64", False)):
+    res_by = {}
+    clk = None
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
+    for label, prec, grad in (("mixed_analytic", "mixed", True), ("fp64_analytic", "fp64", True),
+                              ("fp64_numerical", "fp64", False)):
         eng = gf.Engine(prec)
         eng.set_tree(nodes, olist, len(params), mask)
         eng.set_num_toys(args.toys)
-        for t, d in enumerate(study.datas):
-            eng.upload(d, toy=t)
+        for t in range(args.toys):
+            A.check(L.gf_upload_events(eng._h, t, C.cast(base + 8 * int(off[t]), C.POINTER(C.c_double)), counts[t]),
+                    eng._h)
+            eng._n_events[t] = counts[t]
         P = np.tile(x0, (args.toys, 1))
         for _ in range(3):
             eng.nll_batch(P, grad=True)
         torch.cuda.synchronize()
         rt = []
         for _ in range(10):
+            flush.zero_()
+            torch.cuda.synchronize()
             eng.nll_batch(P, grad=True)
             rt.append(eng.last_timing()[0])
         X0 = np.tile(x0, (args.toys, 1))
+        if label == "mixed_analytic":
+            clk = ClockSampler(0)
+            clk.__enter__()
         t0 = time.perf_counter()
-        res = eng.fit_batch(X0, err, lo, hi, limited, fixed, tolerance=0.1, use_grad=grad)
+        res = eng.fit_batch(X0, err, lo, hi, limited, fixed, tolerance=tol, use_grad=grad)
         wall = time.perf_counter() - t0
+        if label == "mixed_analytic":
+            clk.__exit__(None, None, None)
+            kt = []
+            for _ in range(5):
+                flush.zero_()
+                torch.cuda.synchronize()
+                kt.append(eng.time_kernels(True, -1))
+            kt = np.mean(np.array(kt), axis=0)
+            launches_round = eng.launches_per_eval(True)
+            # end to end through the C ABI: every toy's events uploaded from page-locked host memory, then the
+            # whole lockstep fit; the fitted values and errors are read back
+            e2e_s = []
+            for _ in range(2):
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                for t in range(args.toys):
+                    A.check(L.gf_upload_events(eng._h, t, C.cast(base + 8 * int(off[t]), C.POINTER(C.c_double)),
+                                               counts[t]), eng._h)
+                eng.fit_batch(X0, err, lo, hi, limited, fixed, tolerance=tol, use_grad=grad)
+                e2e_s.append(time.perf_counter() - t1)
         vals = np.array([r.values for r in res])
         errs = np.array([r.errors for r in res])
         pulls = {}
-        for i, nm in enumerate(names):
-            if fixed[i]:
-                continue
-            truth = np.array([tr[nm] for tr in study.truths])
+        for i in free:
+            truth = np.array([tr[names[i]] for tr in study.truths])
             pl = (vals[:, i] - truth) / np.where(errs[:, i] > 0, errs[:, i], np.nan)
-            pulls[nm] = {"mean": float(np.nanmean(pl)), "std": float(np.nanstd(pl))}
+            pulls[names[i]] = {"mean": float(np.nanmean(pl)), "std": float(np.nanstd(pl))}
         out[label] = {"fit_wall_s": wall, "fits_per_s": args.toys / wall,
                       "valid": int(sum(r.valid for r in res)), "mean_nfcn": float(np.mean([r.nfcn for r in res])),
                       "max_nfcn": int(max(r.nfcn for r in res)),
@@ -368,25 +497,63 @@ def run_toys(args) -> dict:
                                           "no_covariance": int(sum(not r.has_covariance for r in res))},
                       "round_ms_with_grad": float(np.mean(rt)),
                       "event_nll_evals_per_s": n_events / (np.mean(rt) / 1e3), "pulls": pulls}
-        out.setdefault("_vals", {})[label] = (vals, errs)
+        res_by[label] = res
         eng.close()
-    vm, em = out["_vals"].pop("mixed_analytic")
-    vf, ef = out["_vals"].pop("fp64_numerical")
-    del out["_vals"]
-    free = [i for i in range(len(params)) if not fixed[i]]
-    dsig = np.abs(vm[:, free] - vf[:, free]) / ef[:, free]
-    out["mixed_vs_fp64_max_dsigma"] = float(np.nanmax(dsig))
-    out["speedup_wall"] = out["fp64_numerical"]["fit_wall_s"] / out["mixed_analytic"]["fit_wall_s"]
-    # the contract's keys: the headline of this workload is fits/s of the mixed-precision lockstep batch
     m = out["mixed_analytic"]
+    rm, ra = res_by["mixed_analytic"], res_by["fp64_analytic"]
+    dsig = max(abs(a.values[i] - b.values[i]) / b.errors[i] for a, b in zip(rm, ra) for i in free)
+    # the oracle as checker (after the timed fits): NLL at the fitted minima and distance to the oracle's own
+    # minima for a sample of toys
+    sample = list(range(0, args.toys, max(1, args.toys // 16)))
+    orel, ooff = 0.0, 0.0
+    for t in sample:
+        ref = O.nll(nodes, olist, rm[t].values, study.datas[t])
+        orel = max(orel, abs(rm[t].fmin - ref) / abs(ref))
+        ooff = max(ooff, float(np.max(O.minimum_offset_sigma(nodes, olist, rm[t].values, study.datas[t],
+                                                              rm[t].covariance, free, h=1e-6))))
+    out["parity"] = {"mixed_vs_fp64_max_dsigma": dsig, "toys_compared": args.toys,
+                     "oracle_rel_nll": orel, "oracle_max_dsigma": ooff, "oracle_toys": len(sample)}
+    out["speedup_wall"] = out["fp64_numerical"]["fit_wall_s"] / m["fit_wall_s"]
+    out["speedup_wall_precision_only"] = out["fp64_analytic"]["fit_wall_s"] / m["fit_wall_s"]
+    # CPU baseline: MIGRAD fits of a few toys with the oracle NLL (numerical gradient) on the host cores
+    cpu = None
+    if not args.no_cpu:
+        t0 = time.perf_counter()
+        nfit = 4
+        for t in range(nfit):
+            mz = gf.Minimizer(x0, err, lo, hi, limited, fixed, tolerance=tol)
+            mz.minimize(lambda p, d=study.datas[t]: O.nll(nodes, olist, p, d))
+        dt = time.perf_counter() - t0
+        cpu = {"value": nfit / dt, "unit": "fits/s", "cores": O.num_threads(), "kind": "port",
+               "sample": f"{nfit} toys fitted with MIGRAD (numerical gradient) on the FP64 restatement"}
+    # roofline of the event kernel (batch shape) over all toys: 4 bytes (bin offset) per event; the table
+    # kernel, issue-bound on FP32 arithmetic, is reported beside it as a share of the round
+    peaks = load_peaks()
+    evt_ms = float(kt[2])
+    achieved = n_events * 4 / (evt_ms / 1e3) / 1e9
+    rounds = int(max(r.nfcn for r in rm))
     out.update({"value": m["fits_per_s"], "unit": "fits/s", "n_gpus": 1, "steps": args.toys, "warmup": 3,
                 "ms_per_step": 1e3 * m["fit_wall_s"] / args.toys, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32-events/f64-reductions",
                 "data": "synthetic (seeded accept-reject per toy)",
-                "e2e": None, "roofline": None, "cpu_baseline": None,
-                "gpu_launches": None})
+                "e2e": {"value": args.toys / float(np.mean(e2e_s)), "unit": "fits/s",
+                        "h2d_bytes_per_step": n_events * 8 // args.toys,
+                        "d2h_bytes_per_step": 2 * len(params) * 8,
+                        "note": "a step is one toy's fit; every toy's FP64 events are uploaded from page-locked "
+                                "host memory before the lockstep fit, inside the timed region"},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                             "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": "gf_evt_g (batch)",
+                             "kernel_ms": evt_ms, "bytes_per_event": 4, "peak_source": peaks["src"],
+                             "round_kernels_alone_ms": {"gf_conv_g": float(kt[0]), "gf_grid_g": float(kt[1]),
+                                                        "gf_evt_g": evt_ms},
+                             "note": "the convolution-table kernel dominates the round; it is bound by the issue "
+                                     "rate of its FP32 products and two-sum corrections, not by HBM"},
+                "cpu_baseline": cpu,
+                "gpu_launches": rounds * launches_round,
+                "clocks": clk.summary() if clk else None})
     out["config"].update({"toys": args.toys, "precision": "mixed", "step": "one toy's MIGRAD fit (lockstep)",
-                          "parallelism": "single GPU"})
+                          "fit_tolerance": tol, "parallelism": "single GPU",
+                          "l2": "flushed before each timed round of round_ms_with_grad; the fits run back to back"})
     return out
 
 
@@ -479,25 +646,16 @@ def run_dalitz(args) -> dict:
     n_amp = 6 if c5 else 8
     bytes_per_event = n_amp * 2 * rbytes
     peaks = load_peaks()
-    achieved = n * bytes_per_event / (evt / 1e3) / 1e9
+    # one launch per FCN (gf_fcn_g): the step is that kernel; else the event kernel launched alone
+    one_launch = eng.launches_per_eval(True) == 1
+    kern = "gf_fcn_g" if one_launch else "gf_evt_g"
+    kern_ms = ms if one_launch else evt
+    achieved = n * bytes_per_event / (kern_ms / 1e3) / 1e9
 
-    fits = {}
+    rep = {}
     if not args.no_fit:
-        for label, prec, grad in (("mixed_analytic", "mixed", "analytic"), ("fp64_numerical", "fp64", "numerical")):
-            wl.reset()
-            fm = gf.FitManager(wl.pdf, precision=prec, gradient=grad, tolerance=0.1)
-            fm.verbosity = 0
-            r = fm.fit()
-            free = [v for v in params if not v.fixed and id(v) not in nd]
-            fits[label] = {"wall_s": fm.wall_seconds, "nfcn": r.nfcn, "valid": r.valid, "fmin": r.fmin, "edm": r.edm,
-                           "call_limit": r.call_limit, "above_max_edm": r.above_max_edm,
-                           "has_covariance": r.has_covariance, "hesse_failed": r.hesse_failed,
-                           "values": {v.name: v.value for v in free}, "errors": {v.name: v.error for v in free}}
-        fits["speedup_wall"] = fits["fp64_numerical"]["wall_s"] / fits["mixed_analytic"]["wall_s"]
-        fits["rel_dnll"] = abs(fits["mixed_analytic"]["fmin"] - fits["fp64_numerical"]["fmin"]) / \
-            abs(fits["fp64_numerical"]["fmin"])
-        fits["max_dsigma"] = max(abs(fits["mixed_analytic"]["values"][k] - fits["fp64_numerical"]["values"][k]) /
-                                 fits["fp64_numerical"]["errors"][k] for k in fits["mixed_analytic"]["values"])
+        free = [i for i, m in enumerate(mask) if m]
+        rep = fit_report(wl, nodes, olist, params, free, wl.pdf.norm_events if c5 else None, args.fit_tolerance)
     cpu = None
     if not args.no_cpu:
         from oracle import oracle as O
@@ -508,10 +666,20 @@ def run_dalitz(args) -> dict:
         t1 = time.perf_counter()
         O.nll(nodes, olist, pv, cols[:, :sample])
         dt = time.perf_counter() - t1
-        integ = "the 2e6-event normalisation sum" if c5 else "the 1500 x 1500 integrals"
-        cpu = {"value": sample / dt, "unit": "event-NLL evals/s", "cores": O.num_threads(), "kind": "port",
-               "sample": f"{sample} events, one NLL (FP64 restatement: amplitudes per event and {integ} "
-                         "recomputed every call, no cache)"}
+        # the restatement recomputes the normalisation integrals on every call; the reference caches them
+        # while the resonance parameters stay put (Amp3Body.cu:263-330, Amp4Body.cu:405-418), so their time
+        # is taken out of the per-FCN cost
+        t1 = time.perf_counter()
+        if c5:
+            O.amp4_gram(nodes, olist, pv, 0, 6)
+        else:
+            O.amp3_integrals(nodes, olist, pv, 0, 8)
+        dti = time.perf_counter() - t1
+        integ = "the 2e6-event normalisation sums" if c5 else "the 1500 x 1500 integrals"
+        cpu = {"value": sample / max(dt - dti, 1e-9), "unit": "event-NLL evals/s", "cores": O.num_threads(),
+               "kind": "port",
+               "sample": f"{sample} events, one NLL (FP64 restatement: amplitudes per event), minus the time of "
+                         f"{integ} ({dti:.3f} s of {dt:.3f} s), which the reference caches between FCNs"}
     return {
         "metric": METRIC, "value": n / (ms / 1e3), "unit": "event-NLL evals/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -534,14 +702,125 @@ def run_dalitz(args) -> dict:
                      "frac": achieved / peaks["hbm_gbs"],
                      "traffic": EVT_DRAM_BYTES_AMP[args.config][0] * n / EVT_DRAM_BYTES_AMP[args.config][1],
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
-                                       "profiles/gf_evt_g_amp3_amp4_c3_c5.md", "kernel": "gf_evt_g", "kernel_ms": evt,
+                                       "profiles/gf_evt_g_amp3_amp4_c3_c5.md (event pass of the same bytes)",
+                     "kernel": kern, "kernel_ms": kern_ms, "event_kernel_alone_ms": evt,
                      "bytes_per_event": bytes_per_event, "peak_source": peaks["src"]},
         "cpu_baseline": cpu,
         "gpu_launches": eng.launches_per_eval(True) * args.steps,
         "clocks": clk.summary(),
         "wall_ms_per_step": 1e3 * wall / args.steps,
-        "fit": fits,
+        **rep,
     }
+
+
+def run_c1(args) -> dict:
+    """C1: ExpPdf(x; alpha) on x in [0, 10], 1e5 events drawn from exp(-0.7 x), analytic normalisation, MIGRAD
+    from alpha = -0.3.  A step is one FCN (NLL + dNLL/dalpha); the fits are compared with an FP64 oracle fit
+    (MIGRAD on the restatement's NLL, numerical gradient), as the reference's test_exp.py compares alpha and
+    its error."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import goofit_gb300 as gf
+    from goofit_gb300 import _abi as A
+    from goofit_gb300 import workloads as W
+    from oracle import oracle as O
+
+    torch.cuda.set_device(0)
+    n = args.events or 100_000
+    wl = W.make_c1(n, seed=1)
+    nodes, params, obs = wl.pdf._flatten()
+    olist = [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs]
+    pv = np.array([v.value for v in params])
+    eng = gf.Engine(args.precision)
+    eng.set_tree(nodes, olist, len(params), [1])
+    host = torch.empty((1, n), dtype=torch.float64, pin_memory=True)
+    host.numpy()[:] = wl.data.to_numpy()
+    hp = C.cast(host.data_ptr(), C.POINTER(C.c_double))
+    L = A.lib()
+    A.check(L.gf_upload_events(eng._h, 0, hp, n), eng._h)
+    eng._n_events[0] = n
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
+    for _ in range(args.warmup):
+        eng.nll_grad(pv)
+    torch.cuda.synchronize()
+    dev_ms = []
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            eng.nll_grad(pv)
+            dev_ms.append(eng.last_timing()[0])
+        torch.cuda.synchronize()
+    ms = float(np.mean(dev_ms))
+    fcn_us = fcn_wall_us(lambda: eng.nll_grad(pv))
+    kt = []
+    for _ in range(max(args.steps, 5)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        kt.append(eng.time_kernels(True))
+    evt = float(np.mean(np.array(kt), axis=0)[2])
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        A.check(L.gf_upload_events(eng._h, 0, hp, n), eng._h)
+        eng.nll_grad(pv)
+        if i >= args.warmup:
+            e2e_ms.append(1e3 * (time.perf_counter() - t1))
+    e2e = float(np.mean(e2e_ms))
+    bpe = 4 if args.precision == "mixed" else 8
+    peaks = load_peaks()
+    achieved = n * bpe / (evt / 1e3) / 1e9
+    rep = {}
+    if not args.no_fit:
+        rep = fit_report(wl, nodes, olist, params, [0], tolerance=args.fit_tolerance)
+        # the reference scenario's FP64 fit on the host: MIGRAD over the restatement's NLL
+        data = wl.data.to_numpy()
+        t1 = time.perf_counter()
+        mz = gf.Minimizer([-0.3], [0.1], [-10.0], [10.0], np.array([1], np.int32), np.array([0], np.int32),
+                          tolerance=args.fit_tolerance)
+        ro = mz.minimize(lambda p: O.nll(nodes, olist, p, data))
+        wall_o = time.perf_counter() - t1
+        m = rep["fit"]["mixed_analytic"]
+        rep["oracle_fit"] = {"alpha": float(ro.values[0]), "error": float(ro.errors[0]), "nfcn": ro.nfcn,
+                             "wall_s": wall_o, "valid": ro.valid,
+                             "mixed_dsigma": abs(m["values"]["alpha"] - ro.values[0]) / ro.errors[0],
+                             "mixed_rel_error_diff": abs(m["errors"]["alpha"] - ro.errors[0]) / ro.errors[0]}
+    cpu = None
+    if not args.no_cpu:
+        data = wl.data.to_numpy()
+        O.nll(nodes, olist, pv, data)
+        t1 = time.perf_counter()
+        reps = 20
+        for _ in range(reps):
+            O.nll(nodes, olist, pv, data)
+        dt = (time.perf_counter() - t1) / reps
+        cpu = {"value": n / dt, "unit": "event-NLL evals/s", "cores": O.num_threads(), "kind": "port",
+               "sample": f"all {n} events, {reps} NLL evaluations (FP64 restatement)"}
+    line = {
+        "metric": METRIC, "value": n / (ms / 1e3), "unit": "event-NLL evals/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-events/f64-reductions" if args.precision == "mixed" else "f64",
+        "data": "synthetic (inverse-CDF draws from exp(-0.7 x) on [0, 10])",
+        "config": {"workload": f"c1: ExpPdf(x; alpha), x in [0, 10], {n} events, analytic normalisation",
+                   "events": n, "precision": args.precision, "step": "one FCN: NLL + dNLL/dalpha",
+                   "l2": "flushed (256 MB write) before every timed step", "parallelism": "single GPU"},
+        "e2e": {"value": n / (e2e / 1e3), "unit": "event-NLL evals/s", "h2d_bytes_per_step": n * 8 + 8,
+                "d2h_bytes_per_step": 4 * 8, "ms_per_step": e2e},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "kernel": "gf_evt_g", "kernel_ms": evt,
+                     "bytes_per_event": bpe, "peak_source": peaks["src"]},
+        "cpu_baseline": cpu,
+        "gpu_launches": eng.launches_per_eval(True) * args.steps,
+        "clocks": clk.summary(),
+        "fcn_wall_us": fcn_us,
+    }
+    line.update(rep)
+    return line
 
 
 def main():
@@ -555,7 +834,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=100_000)
     ap.add_argument("--no-fit", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="c2", choices=["c2", "c3", "c4", "c5"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--fit-tolerance", type=float, default=0.01)
     ap.add_argument("--toys", type=int, default=1024)
     ap.add_argument("--events", type=int, default=0)
     args = ap.parse_args()
@@ -563,6 +843,9 @@ def main():
     world, rank, local = dist_setup()
     if args.config == "c4":
         print(json.dumps(run_toys(args)))
+        return
+    if args.config == "c1":
+        print(json.dumps(run_c1(args)))
         return
     if args.config in ("c3", "c5"):
         print(json.dumps(run_dalitz(args)))

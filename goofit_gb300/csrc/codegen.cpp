@@ -3239,8 +3239,6 @@ struct Gen {
         bool hasGrid = false;
         for(int q = 0; q < NQ; ++q)
             hasGrid = hasGrid || !plan.num_folded[q];
-        if(NC == 0 && !hasGrid)
-            return;
         // the per-event terms depend on the event only through one convolution's bin offset: tabulate them
         // (at most 16 table rows per thread, held in registers)
         const bool tab = NC == 1 && T.n_amp_cols == 0 && !evtReadsObs[grad ? 1 : 0] && !tabDisabled() &&
@@ -3340,7 +3338,9 @@ struct Gen {
             if(hasGrid)
                 gridLoop(false);
         }
-        barrier();
+        // no tables and no grids (analytic or amplitude normalisations): the event pass needs no barrier
+        if(NC > 0 || hasGrid)
+            barrier();
         os << "  gf_evt_" << sfx << "_body(a, blockIdx, gridDim, sPr, s_staged ? gf_dyn + a.stage_off : nullptr, s_soff, sb0, "
               "&s_mbar);\n";
         os << "}\n\n";
