@@ -74,6 +74,33 @@ def _c2_nll(x, xlo, xhi, bins, conv, P):
     return out
 
 
+def _prod_nll(xs, ys, P):
+    L = _lib()
+    xs, ys, P = _d(xs), _d(ys), _d(P).reshape(-1, 3)
+    out = np.zeros(len(P))
+    _check(L, L.ref_prod_nll(xs.ctypes.data_as(_f64p), ys.ctypes.data_as(_f64p), C.c_long(len(xs)),
+                             P.ctypes.data_as(_f64p), len(P), out.ctypes.data_as(_f64p)))
+    return out
+
+
+def _prod_overlap_nll(xs, bins, P):
+    L = _lib()
+    xs, P = _d(xs), _d(P).reshape(-1, 3)
+    out = np.zeros(len(P))
+    _check(L, L.ref_prod_overlap_nll(xs.ctypes.data_as(_f64p), C.c_long(len(xs)), int(bins), P.ctypes.data_as(_f64p),
+                                     len(P), out.ctypes.data_as(_f64p)))
+    return out
+
+
+def _extadd_nll(xs, P):
+    L = _lib()
+    xs, P = _d(xs), _d(P).reshape(-1, 5)
+    out = np.zeros(len(P))
+    _check(L, L.ref_extadd_nll(xs.ctypes.data_as(_f64p), C.c_long(len(xs)), P.ctypes.data_as(_f64p), len(P),
+                               out.ctypes.data_as(_f64p)))
+    return out
+
+
 def _amp3_nll(m12, m13, bins, dec, spin, cyc, P):
     L = _lib()
     m12, m13, dec = _d(m12), _d(m13), _d(dec)
@@ -116,7 +143,8 @@ def _run(q, fn, args):
 
 
 def isolated(fn: str, *args, timeout: float = 600.0):
-    """Runs one of the entry points above (by name: exp_nll, c2_nll, amp3_nll, amp4_nll, dim5) in a fresh
+    """Runs one of the entry points above (by name: exp_nll, c2_nll, prod_nll, prod_overlap_nll, extadd_nll,
+    amp3_nll, amp4_nll, dim5) in a fresh
     spawned process and returns its result."""
     ctx = mp.get_context("spawn")
     q = ctx.Queue()

@@ -13,6 +13,7 @@
 #include <goofit/PDFs/basic/PolynomialPdf.h>
 #include <goofit/PDFs/combine/AddPdf.h>
 #include <goofit/PDFs/combine/ConvolutionPdf.h>
+#include <goofit/PDFs/combine/ProdPdf.h>
 #include <goofit/PDFs/physics/Amp3Body.h>
 #include <goofit/PDFs/physics/Amp4Body.h>
 #include <goofit/PDFs/physics/Amplitude.h>
@@ -111,6 +112,66 @@ int ref_c2_nll(const double *xs, long n, double xlo, double xhi, int bins, const
         fill(data, x, xs, n);
         pdf.setData(&data);
         std::vector<GooFit::Variable> vars{fsig, alpha, mu, sigma, c0};
+        for(int k = 0; k < npts; ++k)
+            out[k] = evaluate(pdf, vars, P + 5 * k);
+    });
+}
+
+// ProdPdf(GaussianPdf(x; mx, sx), ExpPdf(y; ay)) on x in [-5, 5], y in [0, 10]: separate observables, each
+// factor normalised analytically.  P[3 k ..] = (mx, sx, ay).
+int ref_prod_nll(const double *xs, const double *ys, long n, const double *P, int npts, double *out) {
+    return guarded([&] {
+        GooFit::Observable x("x", -5.0, 5.0), y("y", 0.0, 10.0);
+        GooFit::Variable mx("mx", P[0], 0.01, -1, 1), sx("sx", P[1], 0.01, 0.1, 3), ay("ay", P[2], 0.01, -2, -0.01);
+        GooFit::GaussianPdf g("gx", x, mx, sx);
+        GooFit::ExpPdf e("ey", y, ay);
+        GooFit::ProdPdf pdf("prod", {&g, &e});
+        GooFit::UnbinnedDataSet data({x, y});
+        for(long i = 0; i < n; ++i) {
+            x.setValue(xs[i]);
+            y.setValue(ys[i]);
+            data.addEvent();
+        }
+        pdf.setData(&data);
+        std::vector<GooFit::Variable> vars{mx, sx, ay};
+        for(int k = 0; k < npts; ++k)
+            out[k] = evaluate(pdf, vars, P + 3 * k);
+    });
+}
+
+// ProdPdf(GaussianPdf(x; mx, sx), ExpPdf(x; ax)) on x in [-5, 5] with `bins` bins: the factors share x, so
+// the product is normalised numerically.  P[3 k ..] = (mx, sx, ax).
+int ref_prod_overlap_nll(const double *xs, long n, int bins, const double *P, int npts, double *out) {
+    return guarded([&] {
+        GooFit::Observable x("x", -5.0, 5.0);
+        x.setNumBins(bins);
+        GooFit::Variable mx("mx", P[0], 0.01, -1, 1), sx("sx", P[1], 0.01, 0.1, 3), ax("ax", P[2], 0.01, -2, 2);
+        GooFit::GaussianPdf g("gx", x, mx, sx);
+        GooFit::ExpPdf e("ex", x, ax);
+        GooFit::ProdPdf pdf("prod", {&g, &e});
+        GooFit::UnbinnedDataSet data(x);
+        fill(data, x, xs, n);
+        pdf.setData(&data);
+        std::vector<GooFit::Variable> vars{mx, sx, ax};
+        for(int k = 0; k < npts; ++k)
+            out[k] = evaluate(pdf, vars, P + 3 * k);
+    });
+}
+
+// Extended AddPdf({n_e, n_g}; ExpPdf(x; a), GaussianPdf(x; m, s)) on x in [0, 10].
+// P[5 k ..] = (a, m, s, n_e, n_g).
+int ref_extadd_nll(const double *xs, long n, const double *P, int npts, double *out) {
+    return guarded([&] {
+        GooFit::Observable x("x", 0.0, 10.0);
+        GooFit::Variable a("a", P[0], 0.01, -3, -0.01), m("m", P[1], 0.01, 1, 8), sg("s", P[2], 0.01, 0.1, 3);
+        GooFit::Variable ne("n_e", P[3], 10, 0, 1e6), ng("n_g", P[4], 10, 0, 1e6);
+        GooFit::ExpPdf e("e", x, a);
+        GooFit::GaussianPdf g("g", x, m, sg);
+        GooFit::AddPdf pdf("ext", {ne, ng}, {&e, &g});
+        GooFit::UnbinnedDataSet data(x);
+        fill(data, x, xs, n);
+        pdf.setData(&data);
+        std::vector<GooFit::Variable> vars{a, m, sg, ne, ng};
         for(int k = 0; k < npts; ++k)
             out[k] = evaluate(pdf, vars, P + 5 * k);
     });

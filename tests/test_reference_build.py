@@ -6,6 +6,8 @@ the same events and parameter points.
 * C1 ExpPdf (analytic normalisation).
 * C2 Add(Convolution(Exp, Gauss), flat Poly) on a 10,000-bin numeric normalisation, at the truth and at
   shifted alpha, mu and sigma (the convolution table values and its grid sum).
+* ProdPdf of factors on separate observables (analytic norms) and on a shared one (numeric norm), and
+  an extended AddPdf (the yields' term of AddPdf::calculateNLL).
 * C3 Amp3Body with the eight relativistic Breit-Wigner resonances, at the coefficients of the workload and
   with every coefficient, mass and width shifted (cached waves and the 64 integrals rebuilt by the
   reference).
@@ -23,6 +25,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+import combine_trees as CT
 from goofit_gb300 import phasespace as PS
 from goofit_gb300 import workloads as W
 from oracle import oracle as O
@@ -66,6 +69,37 @@ def test_c2_composite_matches_reference():
         pv = np.array([pt[order.index(n)] for n in names])
         assert O.nll(nodes, olist, pv, x) == pytest.approx(r, rel=RTOL)
         assert O.nll(nodes, olist, pv, x, brute_force=True) == pytest.approx(r, rel=RTOL)
+
+
+def _pv(pdf, values):
+    return np.array([values[v.name] for v in pdf._flatten()[1]])
+
+
+def test_prodpdf_and_extended_addpdf_match_reference():
+    # separate observables
+    pdf, cols = CT.prod_separate()
+    nodes, olist, params = tree(pdf)
+    pts = np.array([[0.2, 1.1, -0.4], [0.25, 1.0, -0.45]])
+    ref = R.isolated("prod_nll", cols[0], cols[1], pts)
+    for pt, r in zip(pts, ref):
+        pv = _pv(pdf, dict(zip(["mx", "sx", "ay"], pt)))
+        assert O.nll(nodes, olist, pv, cols) == pytest.approx(r, rel=RTOL)
+    # shared observable: numeric normalisation of the product
+    pdf, cols = CT.prod_overlap()
+    nodes, olist, params = tree(pdf)
+    pts = np.array([[0.2, 1.4, -0.15], [0.1, 1.3, -0.2]])
+    ref = R.isolated("prod_overlap_nll", cols[0], 2000, pts)
+    for pt, r in zip(pts, ref):
+        pv = _pv(pdf, dict(zip(["mx", "sx", "ax"], pt)))
+        assert O.nll(nodes, olist, pv, cols) == pytest.approx(r, rel=RTOL)
+    # extended AddPdf
+    pdf, cols, _ = CT.extended_add()
+    nodes, olist, params = tree(pdf)
+    pts = np.array([[-0.5, 4.0, 0.7, 30_000.0, 20_000.0], [-0.45, 4.1, 0.75, 31_000.0, 18_500.0]])
+    ref = R.isolated("extadd_nll", cols[0], pts)
+    for pt, r in zip(pts, ref):
+        pv = _pv(pdf, dict(zip(["a", "m", "s", "n_e", "n_g"], pt)))
+        assert O.nll(nodes, olist, pv, cols) == pytest.approx(r, rel=RTOL)
 
 
 def _dalitz_points(n, seed):
