@@ -446,8 +446,14 @@ def run_toys(args) -> dict:
                     eng._h)
             eng._n_events[t] = counts[t]
         P = np.tile(x0, (args.toys, 1))
+        eng.nll_batch(P, grad=True)
+        # launch shapes (table k-tiles; the event chunk is tuned at the first evaluation), once per process
+        t_tune = time.perf_counter()
+        shapes = eng.tune_shapes()
+        tune_s = time.perf_counter() - t_tune
         for _ in range(3):
             eng.nll_batch(P, grad=True)
+        shapes["event_chunk"] = eng.event_chunk()
         torch.cuda.synchronize()
         rt = []
         for _ in range(10):
@@ -455,6 +461,10 @@ def run_toys(args) -> dict:
             torch.cuda.synchronize()
             eng.nll_batch(P, grad=True)
             rt.append(eng.last_timing()[0])
+        rtw = []
+        for _ in range(10):
+            eng.nll_batch(P, grad=True)
+            rtw.append(eng.last_timing()[0])
         X0 = np.tile(x0, (args.toys, 1))
         if label == "mixed_analytic":
             clk = ClockSampler(0)
@@ -496,7 +506,16 @@ def run_toys(args) -> dict:
                                           "above_max_edm": int(sum(r.above_max_edm for r in res)),
                                           "no_covariance": int(sum(not r.has_covariance for r in res))},
                       "round_ms_with_grad": float(np.mean(rt)),
-                      "event_nll_evals_per_s": n_events / (np.mean(rt) / 1e3), "pulls": pulls}
+                      "event_nll_evals_per_s": n_events / (np.mean(rt) / 1e3), "pulls": pulls,
+                      "shapes": shapes, "shape_tuning_s": tune_s,
+                      # per lockstep round of the fit: wall time, and the part of it that is not the batched
+                      # evaluation (host MIGRAD steps, launch, synchronisation) - what keeping the whole fit in
+                      # one persistent launch could at most remove
+                      "rounds": int(max(r.nfcn for r in res)),
+                      "round_wall_ms": 1e3 * wall / max(1, int(max(r.nfcn for r in res))),
+                      "round_ms_with_grad_warm_l2": float(np.mean(rtw)),
+                      "round_host_and_launch_ms": 1e3 * wall / max(1, int(max(r.nfcn for r in res))) -
+                      float(np.mean(rtw))}
         res_by[label] = res
         eng.close()
     m = out["mixed_analytic"]
@@ -552,6 +571,7 @@ def run_toys(args) -> dict:
                 "gpu_launches": rounds * launches_round,
                 "clocks": clk.summary() if clk else None})
     out["config"].update({"toys": args.toys, "precision": "mixed", "step": "one toy's MIGRAD fit (lockstep)",
+                          "tuned_shapes": m["shapes"],
                           "fit_tolerance": tol, "parallelism": "single GPU",
                           "l2": "flushed before each timed round of round_ms_with_grad; the fits run back to back"})
     return out
@@ -656,6 +676,8 @@ def run_dalitz(args) -> dict:
     if not args.no_fit:
         free = [i for i, m in enumerate(mask) if m]
         rep = fit_report(wl, nodes, olist, params, free, wl.pdf.norm_events if c5 else None, args.fit_tolerance)
+    if c5 and not args.no_modes:
+        rep["lineshapes_floated"] = c5_lineshape_modes(args, cols, max(args.steps, 5))
     cpu = None
     if not args.no_cpu:
         from oracle import oracle as O
@@ -711,6 +733,61 @@ def run_dalitz(args) -> dict:
         "wall_ms_per_step": 1e3 * wall / args.steps,
         **rep,
     }
+
+
+def c5_lineshape_modes(args, cols, steps: int) -> dict:
+    """C5 with the ten line-shape masses and widths floated (20 free parameters), in the two amplitude modes:
+    'store' keeps dA/dt per event and per normalisation point, 'recompute' recomputes them in the gradient
+    pass and in the integrals.  Per mode: one FCN (NLL + gradient) with the caches valid (device time, L2
+    flushed), one FCN after a line-shape change (wall time: value columns and integrals rebuilt, then the
+    FCN), and the device bytes the store mode keeps; and the largest gradient difference between the modes."""
+    import numpy as np
+    import torch
+
+    import goofit_gb300 as gf
+    from goofit_gb300 import workloads as W
+
+    pdf = W.c5_model(2_000_000, float_lineshapes=True)[0]
+    nodes, params, obs = pdf._flatten()
+    olist = [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs]
+    nd = pdf._nondiff_all()
+    mask = [0 if (v.fixed or id(v) in nd) else 1 for v in params]
+    names = [v.name for v in params]
+    pv = np.array([v.value for v in params])
+    im = names.index("rho_mass")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
+    out, grads = {}, {}
+    for mode in ("store", "recompute"):
+        eng = gf.Engine(args.precision)
+        eng.set_amp_mode(mode)
+        eng.set_tree(nodes, olist, len(params), mask)
+        eng.set_norm_events(0, pdf.norm_events)
+        eng.upload(cols)
+        for _ in range(max(3, args.warmup)):
+            eng.nll_grad(pv)
+        dev = []
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            eng.nll_grad(pv)
+            dev.append(eng.last_timing()[0])
+        reb = []
+        for k in range(steps):
+            p = pv.copy()
+            p[im] *= 1 + 1e-6 * (k + 1)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            eng.nll_grad(p)
+            reb.append(1e3 * (time.perf_counter() - t1))
+        grads[mode] = eng.nll_grad(pv)[1]
+        out[mode] = {"fcn_ms": float(np.mean(dev)), "fcn_after_lineshape_change_ms": float(np.median(reb)),
+                     "recomputing": eng.amp_recomputing(),
+                     "store_mode_bytes": eng.amp_store_bytes() if mode == "store" else 0}
+        eng.close()
+    gs, gr = grads["store"], grads["recompute"]
+    out["grad_max_rel_diff"] = float(np.abs(gs - gr).max() / np.abs(gs).max())
+    out["free_parameters"] = int(sum(mask))
+    return out
 
 
 def run_c1(args) -> dict:
@@ -835,6 +912,8 @@ def main():
     ap.add_argument("--no-fit", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--no-modes", action="store_true",
+                    help="c5: skip the floated-line-shape FCNs in the store and recompute amplitude modes")
     ap.add_argument("--fit-tolerance", type=float, default=0.01)
     ap.add_argument("--toys", type=int, default=1024)
     ap.add_argument("--events", type=int, default=0)

@@ -56,6 +56,9 @@ GF_FLAG_SEPARATE_NORM = 2
 GF_METRIC_EVAL = 0
 GF_METRIC_NLL = 1
 GF_METRIC_PROB = 2
+GF_AMP_AUTO = 0
+GF_AMP_STORE = 1
+GF_AMP_RECOMPUTE = 2
 GF_FIT_UNBINNED_NLL = 0
 GF_FIT_BINNED_NLL = 1
 GF_FIT_BINNED_ERROR = 2
@@ -149,6 +152,11 @@ SIGNATURES = [
     ("gf_launches_per_eval", C.c_int, [_vp, C.c_int]),
     ("gf_event_chunk", C.c_int64, [_vp]),
     ("gf_set_wait_limit", C.c_int, [_vp, C.c_uint64]),
+    ("gf_set_amp_mode", C.c_int, [_vp, C.c_int, C.c_int64]),
+    ("gf_amp_recomputing", C.c_int, [_vp]),
+    ("gf_amp_store_bytes", C.c_int64, [_vp]),
+    ("gf_tune_shapes", C.c_int, [_vp]),
+    ("gf_get_shapes", C.c_int, [_vp, _i32p, _i32p, _i32p]),
     ("gf_time_kernels", C.c_int, [_vp, C.c_int, C.c_int, _f64p, _f64p, _f64p]),
     ("gf_minimizer_create", C.c_int, [C.POINTER(_vp), C.c_int, _f64p, _f64p, _f64p, _f64p, _i32p, _i32p,
                                       C.c_double, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double]),

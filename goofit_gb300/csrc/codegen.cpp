@@ -1501,6 +1501,11 @@ struct Gen {
     KernelPlan &plan;
     std::ostringstream os;
     const bool ctabL1 = ctabThroughL1();
+    // amplitude trees with floated line-shape / resonance parameters: also emit the recompute-mode kernels
+    // (gf_evt_gr, gf_gramr); `recompute` is set while the event pass of that mode is generated
+    bool recomputeKernels = false;
+    bool recompute        = false;
+    Shapes shapes;
 
     // per-toy column pointer i of table `tab` (n per toy); one toy: from the kernel arguments at p0[off + i]
     static std::string p0ptr(const char *tab, int n, int i, int off) {
@@ -1553,8 +1558,9 @@ struct Gen {
         sh.KP = 1;
         if(batch) {
             const char *v = std::getenv("GF_CONV_KP");
-            sh.KP         = v ? std::max(1, std::min(8, std::atoi(v))) : 4;
+            sh.KP = shapes.conv_kp > 0 ? std::min(8, shapes.conv_kp) : v ? std::max(1, std::min(8, std::atoi(v))) : 4;
         }
+        plan.conv_kp = sh.KP;
         for(size_t ci = 0; ci < T.convs.size(); ++ci) {
             const int comps = convComps((int)ci, grad);
             if(comps > sh.items)
@@ -2333,6 +2339,53 @@ struct Gen {
         return e;
     }
 
+    // Declarations before the loop over the normalisation points of amplitude node k: npts (and the points'
+    // stride nst), the Amp3Body bin list or the Amp4Body events.
+    void normPointsHead(int k, std::ostream &o) {
+        const int n3 = (int)T.amp3s.size();
+        if(k < n3) {
+            o << "    const i64 npts = " << (int64_t)T.amp3s[k].grid.size() << "LL, nst = (npts + 3) & ~3LL; (void)nst;\n";
+            o << "    const unsigned *pts = a.dgrid + " << plan.dgrid_off.at(k) << "LL;\n";
+        } else {
+            o << "    const double *ne = a.nevt[" << k - n3 << "];\n";
+            o << "    const i64 npts = a.nnorm[" << k - n3 << "], nst = (npts + 3) & ~3LL; (void)nst;\n";
+        }
+    }
+    // Point p of node k's normalisation set: A and dA (declared by the caller) and its weight `const R e`, the
+    // efficiency at an Amp3Body bin centre (the reference's fake event holds 2 in slot 0), 1 for Amp4Body.
+    // Reads P (FP64 parameters) and the R parameter locals p<j>.
+    void normPoint(int k, std::ostream &o) {
+        const int n3 = (int)T.amp3s.size();
+        if(k >= n3) {
+            o << "      gf_ampv_" << k << "(ne[p], ne[npts + p], ne[2 * npts + p], ne[3 * npts + p], ne[4 * npts + p], P, A, dA);\n";
+            o << "      const R e = R(1); (void)e;\n";
+            return;
+        }
+        const Amp3Info &A = T.amp3s[k];
+        const gf_observable &g12 = T.obs[A.o12], &g13 = T.obs[A.o13];
+        double w12 = g12.hi - g12.lo;
+        w12 /= A.nb12;
+        double w13 = g13.hi - g13.lo;
+        w13 /= A.nb13q;
+        o << "      const unsigned q = pts[p];\n";
+        o << "      const double c12 = gf_centre(" << lit(g12.lo) << ", " << lit(w12) << ", (int)(q & 0xffffu));\n";
+        o << "      const double c13 = gf_centre(" << lit(g13.lo) << ", " << lit(w13) << ", (int)(q >> 16));\n";
+        o << "      gf_ampv_" << k << "(c12, c13, P, A, dA);\n";
+        std::ostringstream body;
+        Ctx c{body, T, false, false, nullptr, nullptr, nullptr, nullptr};
+        c.x = [&](int ob) -> std::string {
+            if(ob == A.o12)
+                return "((R)c12)";
+            if(ob == A.o13)
+                return "((R)c13)";
+            return "R(2)";
+        };
+        c.k   = [&](int) -> std::string { throw std::runtime_error("codegen: convolution in an efficiency"); };
+        c.tab = [&](int, int) -> std::string { throw std::runtime_error("codegen: convolution in an efficiency"); };
+        Val ev = emit(c, A.eff);
+        o << "      R e;\n      {\n" << body.str() << "      e = " << ev.v << ";\n      }\n";
+    }
+
     void ampKernels() {
         const int NK = T.n_amp_nodes();
         if(NK == 0)
@@ -2372,7 +2425,8 @@ struct Gen {
                 os << "      ac[" << T.amp_col0(k) + q << "][i] = A[" << q << "];\n";
             for(int t = 0, d = 0; t < (int)theta.size(); ++t)
                 for(size_t j = 0; j < theta[t].amps.size(); ++j, ++d)
-                    os << "      ac[" << theta[t].col0 + (int)j << "][i] = dA[" << d << "];\n";
+                    os << "      if(ac[" << theta[t].col0 + (int)j << "]) ac[" << theta[t].col0 + (int)j << "][i] = dA[" << d
+                       << "];\n";
             os << "    }\n    break; }\n";
         }
         os << "  default: break;\n  }\n}\n\n";
@@ -2394,44 +2448,15 @@ struct Gen {
             os << "    R2 *sc = reinterpret_cast<R2 *>(a.nscr[" << k << "]);\n";
             os << "    R2 A[" << nAmp << "], dA[" << ND << "];\n";
             if(k < n3) {
-                const Amp3Info &A = T.amp3s[k];
                 plan.dgrid_off.push_back(goff);
-                const gf_observable &g12 = T.obs[A.o12], &g13 = T.obs[A.o13];
-                double w12 = g12.hi - g12.lo;
-                w12 /= A.nb12;
-                double w13 = g13.hi - g13.lo;
-                w13 /= A.nb13q;
-                const int64_t npts = (int64_t)A.grid.size();
-                os << "    const i64 npts = " << npts << "LL, nst = (npts + 3) & ~3LL;\n";
-                os << "    R *se = reinterpret_cast<R *>(sc + " << NC << " * nst);\n";
-                os << "    const unsigned *pts = a.dgrid + " << goff << "LL;\n";
-                goff += npts;
-                os << "    for(i64 p = (i64)blockIdx.x * 256 + tid; p < npts; p += (i64)gridDim.x * 256) {\n";
-                os << "      const unsigned q = pts[p];\n";
-                os << "      const double c12 = gf_centre(" << lit(g12.lo) << ", " << lit(w12) << ", (int)(q & 0xffffu));\n";
-                os << "      const double c13 = gf_centre(" << lit(g13.lo) << ", " << lit(w13) << ", (int)(q >> 16));\n";
-                os << "      gf_ampv_" << k << "(c12, c13, P, A, dA);\n";
-                // the efficiency at the bin centre; the reference's fake event holds 2 in slot 0
-                std::ostringstream body;
-                Ctx c{body, T, false, false, nullptr, nullptr, nullptr, nullptr};
-                c.x = [&](int o) -> std::string {
-                    if(o == A.o12)
-                        return "((R)c12)";
-                    if(o == A.o13)
-                        return "((R)c13)";
-                    return "R(2)";
-                };
-                c.k   = [&](int) -> std::string { throw std::runtime_error("codegen: convolution in an efficiency"); };
-                c.tab = [&](int, int) -> std::string { throw std::runtime_error("codegen: convolution in an efficiency"); };
-                Val ev = emit(c, A.eff);
-                os << "      {\n" << body.str() << "      se[p] = " << ev.v << ";\n      }\n";
-            } else {
-                const int k4 = k - n3;
-                os << "    const double *ne = a.nevt[" << k4 << "];\n";
-                os << "    const i64 npts = a.nnorm[" << k4 << "], nst = (npts + 3) & ~3LL;\n";
-                os << "    for(i64 p = (i64)blockIdx.x * 256 + tid; p < npts; p += (i64)gridDim.x * 256) {\n";
-                os << "      gf_ampv_" << k << "(ne[p], ne[npts + p], ne[2 * npts + p], ne[3 * npts + p], ne[4 * npts + p], P, A, dA);\n";
+                goff += (int64_t)T.amp3s[k].grid.size();
             }
+            normPointsHead(k, os);
+            os << "    R *se = reinterpret_cast<R *>(sc + " << NC << " * nst); (void)se;\n";
+            os << "    for(i64 p = (i64)blockIdx.x * 256 + tid; p < npts; p += (i64)gridDim.x * 256) {\n";
+            normPoint(k, os);
+            if(k < n3)
+                os << "      se[p] = e;\n";
             for(int q = 0; q < nAmp; ++q)
                 os << "      sc[" << q << " * nst + p] = A[" << q << "];\n";
             for(int d = 0; d < nDeriv(k); ++d)
@@ -2451,11 +2476,22 @@ struct Gen {
                 plan.gram_pairs_max = std::max(plan.gram_pairs_max, t.p1 - t.p0);
             }
         }
+        // gf_gramr (recompute mode): the same reduction with the amplitudes and their derivatives recomputed at
+        // every point instead of read from scratch columns (no per-point storage; each tile of a node evaluates
+        // the node's amplitudes again)
         const int PM = plan.gram_pairs_max, NW = 256 / 32;
-        os << "extern \"C\" __global__ void __launch_bounds__(256) gf_gram(const GfArgs a) {\n";
+        for(int rv = 0; rv < (recomputeKernels ? 2 : 1); ++rv) {
+        os << "extern \"C\" __global__ void __launch_bounds__(256) " << (rv ? "gf_gramr" : "gf_gram") << "(const GfArgs a) {\n";
         os << "  const int z = blockIdx.z, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;\n";
         os << "  __shared__ double red[" << NW << "][" << 2 * PM << "];\n";
         os << "  double *out = a.gram + ((i64)z * gridDim.x + blockIdx.x) * " << 2 * PM << ";\n";
+        if(rv) {
+            os << "  const int toy = a.gtoy;\n";
+            os << "  const double *P = a.P + (i64)toy * " << np << "; (void)P;\n";
+            os << "  const R *Pr = reinterpret_cast<const R *>(a.Pr) + (i64)toy * " << plan.nl.npr << "; (void)Pr;\n";
+            for(int j = 0; j < T.n_params; ++j)
+                os << "  const R p" << j << " = Pr[" << j << "]; (void)p" << j << ";\n";
+        }
         os << "  switch(z) {\n";
         for(size_t ti = 0; ti < plan.gram_tiles.size(); ++ti) {
             const auto &tile = plan.gram_tiles[ti];
@@ -2474,6 +2510,18 @@ struct Gen {
             os << "  case " << ti << ": {\n";
             for(int q = 0; q < npr; ++q)
                 os << "    R sr" << q << " = R(0), si" << q << " = R(0);\n";
+            if(rv) {
+                normPointsHead(k, os);
+                os << "    for(i64 p = (i64)blockIdx.x * 256 + tid; p < npts; p += (i64)gridDim.x * 256) {\n";
+                os << "      R2 A[" << nAmp << "], dA[" << std::max(1, nDeriv(k)) << "];\n";
+                normPoint(k, os);
+                for(int v = 0; v < nAmp; ++v)
+                    if(needV[v])
+                        os << "      const R2 b" << v << " = A[" << v << "];\n";
+                for(int d = 0; d < nDeriv(k); ++d)
+                    if(needD[d])
+                        os << "      const R2 g" << d << " = dA[" << d << "];\n";
+            } else {
             os << "    const R2 *sc = reinterpret_cast<const R2 *>(a.nscr[" << k << "]);\n";
             if(k < n3)
                 os << "    const i64 npts = " << (int64_t)T.amp3s[k].grid.size() << "LL, nst = (npts + 3) & ~3LL;\n"
@@ -2488,6 +2536,7 @@ struct Gen {
             for(int d = 0; d < nDeriv(k); ++d)
                 if(needD[d])
                     os << "      const R2 g" << d << " = sc[" << nAmp + d << " * nst + p];\n";
+            }
             for(int q = 0; q < npr; ++q) {
                 const std::string x = es[q].h ? "g" + std::to_string(es[q].i) : "b" + std::to_string(es[q].i);
                 const std::string y = "b" + std::to_string(es[q].j);
@@ -2507,6 +2556,7 @@ struct Gen {
             os << "    break; }\n";
         }
         os << "  default: break;\n  }\n}\n\n";
+        }
     }
 
     // ---------------- event pass ----------------
@@ -2517,8 +2567,12 @@ struct Gen {
     // function that depends on the event only through one convolution's bin offset k): each CTA first
     // tabulates the per-event terms -log P and -dP/P over the table's k range in shared memory, and the
     // event loop gathers and adds them
+    // recompute (amplitude trees, gradient pass): dA/dt of the amplitude nodes is recomputed per event from the
+    // FP64 event columns by the nodes' amplitude functions instead of read from stored derivative columns; the
+    // amplitudes themselves are still read from their cached value columns
     void eventKernel(bool grad, bool values, bool asBody = false, bool tab = false) {
-        const std::string name = values ? "gf_val_n" : (grad ? "gf_evt_g" : "gf_evt_n");
+        const bool rc = recompute && grad && !values && !asBody && !tab;
+        const std::string name = values ? "gf_val_n" : (grad ? (rc ? "gf_evt_gr" : "gf_evt_g") : "gf_evt_n");
         const int NGp = 1 + (grad ? T.NG : 0);
         const int NGs = 1 + T.NG;
         const int NC  = (int)T.convs.size();
@@ -2564,11 +2618,28 @@ struct Gen {
             aused[T.amp_col0(ai) + r] = 1;
             return "am" + std::to_string(T.amp_col0(ai) + r);
         };
+        // derivative column -> (amplitude node, index in its dA array), and which of them the event function reads
+        std::map<int, std::pair<int, int>> dcolOf;
+        for(int k = 0; k < T.n_amp_nodes(); ++k) {
+            int d = 0;
+            for(auto &th : T.amp_theta(k))
+                for(size_t j = 0; j < th.amps.size(); ++j, ++d)
+                    dcolOf[th.col0 + (int)j] = {k, d};
+        }
+        std::vector<int> rused(std::max(1, NA), 0);
         c.ampcol = [&](int col) {
+            if(rc && dcolOf.count(col)) {
+                rused[col] = 1;
+                return "rd" + std::to_string(col);
+            }
             aused[col] = 1;
             return "am" + std::to_string(col);
         };
         Val root = emit(c, 0);
+        std::vector<int> rnode(std::max(1, T.n_amp_nodes()), 0);
+        for(auto &kv : dcolOf)
+            if(rused[kv.first])
+                rnode[kv.second.first] = 1;
         if(!values && !grad) {
             plan.obs_used_evt.clear();
             for(int o = 0; o < NO; ++o)
@@ -2614,6 +2685,8 @@ struct Gen {
         os << "  extern __shared__ __align__(16) unsigned char smraw[];\n";
         os << "  R *stab = reinterpret_cast<R *>(smraw); (void)stab;\n";
         os << "  __shared__ int s_toy, last;\n";
+        if(rc)
+            os << "  __shared__ double sPd[" << std::max(1, T.n_params) << "];\n";
         if(!values)
             os << "  __shared__ ACC red[" << NW << "][" << NGp + 1 << "];\n";
         os << "  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5; (void)lane; (void)wid;\n";
@@ -2809,6 +2882,24 @@ struct Gen {
         } else
             os << "  for(int ch = cb; ch < ce; ++ch) {\n";
         os << "    int toy; i64 b0, e0; gf_chunk(a, ch, toy, b0, e0);\n";
+        if(rc) {
+            // the toy's FP64 parameters for the amplitude functions, and the FP64 event columns they read
+            const int np = std::max(1, T.n_params), n3 = (int)T.amp3s.size();
+            os << "    __syncthreads();\n";
+            os << "    for(int q = tid; q < " << np << "; q += " << block << ") sPd[q] = a.P[(i64)toy * " << np << " + q];\n";
+            os << "    __syncthreads();\n";
+            for(int k = 0; k < T.n_amp_nodes(); ++k) {
+                if(!rnode[k])
+                    continue;
+                std::vector<int> ob;
+                if(k < n3)
+                    ob = {T.amp3s[k].o12, T.amp3s[k].o13};
+                else
+                    ob.assign(T.amp4s[k - n3].obs, T.amp4s[k - n3].obs + 5);
+                for(size_t v = 0; v < ob.size(); ++v)
+                    os << "    const double *xd" << k << "_" << v << " = a.dcol[(i64)toy * " << NO << " + " << ob[v] << "];\n";
+            }
+        }
         // the activity flag is read beside the parameters (independent loads), the branch comes after them
         if(batch)
             os << "    const bool toy_on = !a.active || a.active[toy];\n";
@@ -3020,6 +3111,20 @@ struct Gen {
                            << "reinterpret_cast<const float4 *>(tp" << ci << " + " << 4 * g4 << "));\n";
             }
         }
+        for(int k = 0; k < T.n_amp_nodes() && rc; ++k) {
+            if(!rnode[k])
+                continue;
+            // this event's amplitudes and derivatives (a duplicate of the iteration's first event past its end)
+            const int nv = k < (int)T.amp3s.size() ? 2 : 5;
+            os << "        R2 rA" << k << "[" << T.amp_count(k) << "], rD" << k << "[" << std::max(1, nDeriv(k)) << "];\n";
+            os << "        {\n          const i64 ij = i0 + (j < jn ? j : 0);\n          gf_ampv_" << k << "(";
+            for(int v = 0; v < nv; ++v)
+                os << "xd" << k << "_" << v << "[ij], ";
+            os << "sPd, rA" << k << ", rD" << k << ");\n        }\n";
+        }
+        for(auto &kv : dcolOf)
+            if(rused[kv.first])
+                os << "        const R2 rd" << kv.first << " = rD" << kv.second.first << "[" << kv.second.second << "];\n";
         os << "        {\n" << body.str();
         os << "        const R pv = " << normMul(c, 0, root.v) << ";\n";
         if(values) {
@@ -3362,13 +3467,14 @@ struct Gen {
 
 NormLayout norm_layout(const Tree &t) { return computeNormLayout(t); }
 
-KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, bool batch) {
+KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, bool batch, const Shapes &shapes) {
     KernelPlan plan;
     plan.nl                  = norm_layout(t);
     // one toy: 256 bins per CTA (C2's 10,000-bin grids: FCN 36.7 us; 1024 / 2048 / 4096 / 16384 bins per
     // CTA: 36.2 / 38.1 / 43.6 / 46.7 us, fewer CTAs leaving more of the per-bin load latency exposed)
-    plan.grid_bins_per_block = batch ? 1024 : 256;
+    plan.grid_bins_per_block = shapes.grid_bpb > 0 ? shapes.grid_bpb : batch ? 1024 : 256;
     Gen g{t, mixed, evt_block, batch, plan, {}};
+    g.shapes = shapes;
     g.os << "// generated likelihood kernels\n";
     if(mixed)
         g.os << "typedef float R;\ntypedef float2 R2;\n#define GF_EXP(x) expf(x)\n#define GF_LOG(x) logf(x)\n";
@@ -3393,6 +3499,9 @@ KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, bool batch
         g.os << kPreludeF32;
     else
         g.os << kPreludeF64;
+    for(int k = 0; k < t.n_amp_nodes(); ++k)
+        if(g.nDeriv(k) > 0)
+            g.recomputeKernels = true;
     g.tableLayout(true);
     g.tableLayout(false);
     g.planNumerics();
@@ -3404,6 +3513,21 @@ KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, bool batch
     g.eventKernel(true, false);
     g.eventKernel(false, false);
     g.eventKernel(false, true);
+    if(g.recomputeKernels) {
+        // the recompute-mode gradient pass; the plan keeps the store-mode kernels' figures
+        const KernelPlan saved = plan;
+        const size_t bs        = g.bodySmem;
+        const bool ro          = g.evtReadsObs[1];
+        g.recompute            = true;
+        g.eventKernel(true, false);
+        g.recompute            = false;
+        g.evtReadsObs[1]       = ro;
+        const size_t smem      = plan.evt_smem_grad;
+        plan                   = saved;
+        plan.evt_smem_gr       = smem;
+        plan.recompute_kernels = true;
+        g.bodySmem             = bs;
+    }
     if(!batch && t.fit_metric == GF_FIT_UNBINNED_NLL) {
         g.fusedKernel(true);
         g.fusedKernel(false);

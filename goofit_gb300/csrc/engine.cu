@@ -17,6 +17,7 @@
 #include <map>
 #include <mutex>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -563,10 +564,15 @@ cudaError_t recordEvent(gf_engine *e, cudaEvent_t ev) {
     return cudaEventRecord(ev, e->stream);
 }
 
-// One toy with the one-launch kernels loaded and enabled: the evaluation is a single cooperative launch.
+// The gradient event kernel of the engine's amplitude mode, and its dynamic shared memory.
+cudaKernel_t evtGradKernel(const gf_engine *e) { return e->amp_recompute ? e->mod.evt_gr : e->mod.evt_g; }
+size_t evtGradSmem(const gf_engine *e) { return e->amp_recompute ? e->plan.evt_smem_gr : e->plan.evt_smem_grad; }
+
+// One toy with the one-launch kernels loaded and enabled: the evaluation is a single cooperative launch
+// (the store mode's kernels only: recomputed amplitude derivatives use the separate gradient event kernel).
 bool fusedPath(const gf_engine *e) {
     return e->use_fused && e->n_toys == 1 && !e->batch_kernels && e->mod.fcn_g && e->mod.fcn_n && e->fcn_grid > 0 &&
-           e->h_fpart;
+           e->h_fpart && !e->amp_recompute;
 }
 
 // Arguments of the one-launch kernel: the toy's record (parameters as R, analytic factors) by value when it
@@ -640,8 +646,8 @@ cudaError_t enqueueEval(gf_engine *e, bool grad) {
     if(r == cudaSuccess)
         r = enqueuePrep(e, grad, a, &kernelLast);
     if(r == cudaSuccess)
-        r = launch(grad ? e->mod.evt_g : e->mod.evt_n, dim3(evtGrid(e)), dim3(e->block),
-                   grad ? e->plan.evt_smem_grad : e->plan.evt_smem_nograd, e->stream, a, kernelLast && e->use_pdl);
+        r = launch(grad ? evtGradKernel(e) : e->mod.evt_n, dim3(evtGrid(e)), dim3(e->block),
+                   grad ? evtGradSmem(e) : e->plan.evt_smem_nograd, e->stream, a, kernelLast && e->use_pdl);
     if(r == cudaSuccess)
         r = recordEvent(e, e->ev[3]);
     return r;
@@ -695,6 +701,9 @@ int loadModule(gf_engine *e) {
         return rc;
     if((rc = get(e->mod.fcn_g, "gf_fcn_g", e->plan.fused)) || (rc = get(e->mod.fcn_n, "gf_fcn_n", e->plan.fused)))
         return rc;
+    if((rc = get(e->mod.evt_gr, "gf_evt_gr", e->plan.recompute_kernels)) ||
+       (rc = get(e->mod.gramr, "gf_gramr", e->plan.recompute_kernels)))
+        return rc;
     auto smem = [&](cudaKernel_t k, size_t bytes) -> int {
         if(!k || bytes <= 48 * 1024)
             return GF_OK;
@@ -705,6 +714,7 @@ int loadModule(gf_engine *e) {
     };
     if((rc = smem(e->mod.conv_g, e->plan.conv_smem_grad)) || (rc = smem(e->mod.conv_n, e->plan.conv_smem_nograd)) ||
        (rc = smem(e->mod.evt_g, e->plan.evt_smem_grad)) || (rc = smem(e->mod.evt_n, e->plan.evt_smem_nograd)) ||
+       (rc = smem(e->mod.evt_gr, e->plan.evt_smem_gr)) ||
        (rc = smem(e->mod.val_n, e->plan.evt_smem_nograd)) || (rc = smem(e->mod.fcn_g, e->plan.fused_smem[1])) ||
        (rc = smem(e->mod.fcn_n, e->plan.fused_smem[0])))
         return rc;
@@ -910,6 +920,47 @@ int64_t ampPoints(const gf_engine *e, int k) {
 // column stride of the scratch columns: the points rounded up to a multiple of 4
 int64_t ampStride(const gf_engine *e, int k) { return (std::max<int64_t>(1, ampPoints(e, k)) + 3) / 4 * 4; }
 
+// Bytes the store mode keeps for amplitude derivatives and normalisation points: the derivative columns of every
+// toy's events (npad events each) and the normalisation scratch columns.
+size_t ampStoreBytes(const gf_engine *e, int64_t npad) {
+    const gf::Tree &T = e->tree;
+    const size_t rs   = rsize(e);
+    size_t nd = 0, scr = 0;
+    for(int k = 0; k < T.n_amp_nodes(); ++k) {
+        int ndk = 0;
+        for(auto &th : T.amp_theta(k))
+            ndk += (int)th.amps.size();
+        nd += (size_t)ndk;
+        scr += (size_t)ampStride(e, k) * ((T.amp_count(k) + ndk) * 2 * rs + rs);
+    }
+    return (size_t)e->n_toys * (size_t)npad * nd * 2 * rs + scr;
+}
+
+// Fixes the amplitude mode of the engine's events (once per tree and toy count, at the first upload).
+void decideAmpMode(gf_engine *e, int64_t npad) {
+    if(e->amp_decided)
+        return;
+    bool rc = false;
+    if(e->plan.recompute_kernels && e->mod.evt_gr && e->mod.gramr) {
+        if(e->amp_mode == GF_AMP_RECOMPUTE)
+            rc = true;
+        else if(e->amp_mode == GF_AMP_AUTO) {
+            size_t budget = (size_t)std::max<int64_t>(0, e->amp_budget);
+            if(budget == 0) {
+                size_t fr = 0, tot = 0;
+                if(cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+                    cudaGetLastError();
+                    fr = 0;
+                }
+                budget = fr / 4;
+            }
+            rc = ampStoreBytes(e, npad) > budget;
+        }
+    }
+    e->amp_recompute = rc;
+    e->amp_decided   = true;
+}
+
 // Scratch columns of the normalisation pass: per amplitude node, (values + derivatives) R2 columns and an R
 // efficiency column over its points.
 int ensureScratch(gf_engine *e) {
@@ -1004,7 +1055,7 @@ int updateAmpCaches(gf_engine *e) {
     if(!anyData && !anyNorm)
         return GF_OK;
     fillRecords(e); // R copies of the parameters for the efficiency in the integral kernel
-    int rc = ensureScratch(e);
+    int rc = e->amp_recompute ? GF_OK : ensureScratch(e);
     if(rc)
         return rc;
     GfArgs a      = makeArgs(e);
@@ -1031,13 +1082,15 @@ int updateAmpCaches(gf_engine *e) {
     for(int t = 0; t < NT && r == cudaSuccess; ++t) {
         if(!normDirty[t])
             continue;
-        // the normalisation points of this toy: amplitudes (and derivatives), then their reduction
+        // the normalisation points of this toy: amplitudes (and derivatives), then their reduction (recompute
+        // mode: one kernel that evaluates the amplitudes at every point and reduces them in place)
         a.gtoy = t;
-        r      = launch(e->mod.ampn, dim3((unsigned)bn, 1, (unsigned)NAN_), dim3(256), 0, e->stream, a);
+        if(!e->amp_recompute)
+            r = launch(e->mod.ampn, dim3((unsigned)bn, 1, (unsigned)NAN_), dim3(256), 0, e->stream, a);
         GfToy &ty = e->toys[t];
         ty.amp_I.assign(NAN_, {});
         ty.amp_H.assign(NAN_, {});
-        if(e->gram_tc) {
+        if(e->gram_tc && !e->amp_recompute) {
             // tensor cores: the real Gram matrix G of each node's columns, then I and H from its blocks
             for(int k = 0; k < NAN_ && r == cudaSuccess; ++k) {
                 const int n = T.amp_count(k), nc = ampColumns(T, k), m = 2 * nc;
@@ -1048,7 +1101,8 @@ int updateAmpCaches(gf_engine *e) {
                 r = cudaMemsetAsync(e->d_gtc_err, 0, sizeof(int), e->stream);
                 if(r == cudaSuccess)
                     r = gf_gram_tc_launch(sc, npts, nst, nc, eff, std::max(1, e->sm_count), e->d_gtc_part,
-                                          e->d_gtc_out, e->d_gtc_err, e->stream);
+                                          e->d_gtc_out, e->d_gtc_err, e->stream,
+                                          e->gram_w >= gf_gram_tc_width(nc) ? e->gram_w : 0);
                 if(r == cudaSuccess)
                     r = cudaMemcpyAsync(e->h_gtc.data(), e->d_gtc_out, sizeof(double) * (size_t)m * m,
                                         cudaMemcpyDeviceToHost, e->stream);
@@ -1091,7 +1145,8 @@ int updateAmpCaches(gf_engine *e) {
             continue;
         }
         if(r == cudaSuccess)
-            r = launch(e->mod.gram, dim3(e->gram_blocks, 1, NTILE), dim3(256), 0, e->stream, a);
+            r = launch(e->amp_recompute ? e->mod.gramr : e->mod.gram, dim3(e->gram_blocks, 1, NTILE), dim3(256), 0,
+                       e->stream, a);
         if(r == cudaSuccess)
             r = cudaMemcpyAsync(e->h_gram, e->d_gram, gbytes, cudaMemcpyDeviceToHost, e->stream);
         if(r == cudaSuccess)
@@ -1219,7 +1274,7 @@ int autotune(gf_engine *e) {
         if(r0 == cudaSuccess)
             r0 = enqueuePrep(e, true, a0);
         if(r0 == cudaSuccess)
-            r0 = launch(e->mod.evt_g, dim3(evtGrid(e)), dim3(e->block), e->plan.evt_smem_grad, e->stream, a0);
+            r0 = launch(evtGradKernel(e), dim3(evtGrid(e)), dim3(e->block), evtGradSmem(e), e->stream, a0);
         if(r0 == cudaSuccess)
             r0 = cudaStreamSynchronize(e->stream);
         if(r0 != cudaSuccess)
@@ -1257,7 +1312,7 @@ int autotune(gf_engine *e) {
             if(r == cudaSuccess)
                 r = cudaEventRecord(e->ev[1], e->stream);
             if(r == cudaSuccess)
-                r = launch(e->mod.evt_g, dim3(evtGrid(e)), dim3(e->block), e->plan.evt_smem_grad, e->stream, a);
+                r = launch(evtGradKernel(e), dim3(evtGrid(e)), dim3(e->block), evtGradSmem(e), e->stream, a);
             if(r == cudaSuccess)
                 r = cudaEventRecord(e->ev[2], e->stream);
             if(r == cudaSuccess)
@@ -1559,8 +1614,9 @@ int gf_set_tree(gf_engine *e, const gf_node *nodes, int n_nodes, const gf_observ
     for(auto &ty : e->toys)
         freeToy(ty);
     freeNormEvents(e);
-    e->tree     = t;
-    e->has_tree = false;
+    e->tree        = t;
+    e->has_tree    = false;
+    e->amp_decided = false;
     if(!t.amp4s.empty()) {
         const size_t k = t.amp4s.size();
         e->norm_buf.assign(k, nullptr);
@@ -1584,7 +1640,7 @@ int gf_set_tree(gf_engine *e, const gf_node *nodes, int n_nodes, const gf_observ
 static int compileTree(gf_engine *e) {
     e->batch_kernels = e->n_toys > 1;
     try {
-        e->plan = gf::generate_kernels(e->tree, e->precision == GF_MIXED, e->block, e->batch_kernels);
+        e->plan = gf::generate_kernels(e->tree, e->precision == GF_MIXED, e->block, e->batch_kernels, e->shapes);
     } catch(std::exception &ex) {
         return gf_fail(e, GF_ERR_BAD_TREE, ex.what());
     }
@@ -1639,6 +1695,7 @@ int gf_set_num_toys(gf_engine *e, int n) {
         freeToy(t);
     e->n_toys = n;
     e->toys.assign(n, GfToy());
+    e->amp_decided = false;
     // one toy and batches of toys use differently shaped table and grid kernels
     if(e->has_tree && (n > 1) != e->batch_kernels)
         return compileTree(e);
@@ -1680,6 +1737,17 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
         // the Dalitz variables for the amplitude kernel
         const int NA = T.n_amp_cols;
         if(NA > 0) {
+            decideAmpMode(e, npad);
+            // recompute mode: no derivative columns (their pointers stay null)
+            std::vector<char> keep(NA, 1);
+            if(e->amp_recompute)
+                for(int k = 0; k < T.n_amp_nodes(); ++k)
+                    for(auto &th : T.amp_theta(k))
+                        for(size_t j = 0; j < th.amps.size(); ++j)
+                            keep[th.col0 + (int)j] = 0;
+            int nkeep = 0;
+            for(int c = 0; c < NA; ++c)
+                nkeep += keep[c];
             std::vector<int> dob;
             for(auto &A : T.amp3s)
                 for(int o : {A.o12, A.o13})
@@ -1691,16 +1759,16 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
                         dob.push_back(o);
             const bool mixed = e->precision == GF_MIXED;
             size_t aBytes    = (size_t)npad * 2 * rs;
-            size_t bytes     = aBytes * NA + (mixed ? (size_t)npad * 8 * dob.size() : 0) + 256;
+            size_t bytes     = aBytes * nkeep + (mixed ? (size_t)npad * 8 * dob.size() : 0) + 256;
             r                = cudaMalloc(&ty.abase, bytes);
             if(r != cudaSuccess) {
                 freeToy(ty);
                 return gf_cuda_check(e, r, "cudaMalloc amplitude cache");
             }
-            for(int c = 0; c < NA; ++c)
-                ty.acols[c] = (char *)ty.abase + aBytes * c;
+            for(int c = 0, q = 0; c < NA; ++c)
+                ty.acols[c] = keep[c] ? (char *)ty.abase + aBytes * q++ : nullptr;
             for(size_t k = 0; k < dob.size(); ++k)
-                ty.dcols[dob[k]] = mixed ? (double *)((char *)ty.abase + aBytes * NA + (size_t)npad * 8 * k)
+                ty.dcols[dob[k]] = mixed ? (double *)((char *)ty.abase + aBytes * nkeep + (size_t)npad * 8 * k)
                                          : (double *)ty.cols[dob[k]];
         }
     }
@@ -2088,8 +2156,8 @@ int gf_time_kernels(gf_engine *e, int toy, int with_grad, double *ms_conv, doubl
     if(r == cudaSuccess)
         r = cudaEventRecord(t2, e->stream);
     if(r == cudaSuccess)
-        r = launch(grad ? e->mod.evt_g : e->mod.evt_n, dim3(evtGrid(e)), dim3(e->block),
-                   grad ? e->plan.evt_smem_grad : e->plan.evt_smem_nograd, e->stream, a);
+        r = launch(grad ? evtGradKernel(e) : e->mod.evt_n, dim3(evtGrid(e)), dim3(e->block),
+                   grad ? evtGradSmem(e) : e->plan.evt_smem_nograd, e->stream, a);
     if(r == cudaSuccess)
         r = cudaEventRecord(t3, e->stream);
     if(r == cudaSuccess)
@@ -2113,6 +2181,217 @@ int gf_set_wait_limit(gf_engine *e, uint64_t ns) {
         return gf_fail(nullptr, GF_ERR_INVALID, "null engine");
     e->bar_ns = ns ? ns : 1000000000ull;
     return GF_OK;
+}
+
+// ---- launch-shape autotuner ----
+namespace {
+
+// Device time of one gradient evaluation of every toy (the engine's CUDA events around it), after a write of
+// twice the L2 size; the best of `reps` after one untimed evaluation.
+int timeEval(gf_engine *e, void *flush, size_t flushBytes, int reps, double *best) {
+    *best = 1e30;
+    for(int it = 0; it <= reps; ++it) {
+        if(flush && cudaMemsetAsync(flush, it & 0xff, flushBytes, e->stream) != cudaSuccess)
+            return gf_cuda_check(e, cudaGetLastError(), "autotune flush");
+        for(int t = 0; t < e->n_toys; ++t)
+            e->h_active[t] = 1;
+        if(int rc = gf_run(e, true, -1, 1))
+            return rc;
+        if(it > 0)
+            *best = std::min(*best, e->last_ms_total);
+    }
+    return GF_OK;
+}
+
+// Recompiles the tree with the given shapes and rebuilds the layout, keeping the parameters, the active flags
+// and the event chunk.
+int applyShapes(gf_engine *e, const gf::Shapes &sh, const std::vector<double> &P, const std::vector<int> &act) {
+    const int chunk = e->chunk;
+    const bool fixed = e->chunk_fixed;
+    e->shapes = sh;
+    if(int rc = compileTree(e))
+        return rc;
+    e->layout_ready = false;
+    e->chunk_fixed  = true;
+    e->chunk        = chunk;
+    int rc          = buildLayout(e);
+    e->chunk_fixed  = fixed;
+    if(rc)
+        return rc;
+    std::memcpy(e->h_P, P.data(), sizeof(double) * P.size());
+    for(int t = 0; t < e->n_toys; ++t)
+        e->h_active[t] = act[t];
+    return GF_OK;
+}
+
+struct TunedShapes {
+    gf::Shapes sh;
+    int gram_w = 0;
+};
+
+} // namespace
+
+int gf_tune_shapes(gf_engine *e) {
+    if(!e || !e->has_tree)
+        return gf_fail(e, GF_ERR_STATE, "no tree");
+    cudaSetDevice(e->device);
+    int rc = buildLayout(e);
+    if(rc)
+        return rc;
+    static std::mutex mu;
+    static std::map<std::string, TunedShapes> cache;
+    int64_t total = 0;
+    for(auto &t : e->toys)
+        total += t.n;
+    const gf::Tree &T = e->tree;
+    const int np      = std::max(1, T.n_params);
+    std::vector<double> P(e->h_P, e->h_P + (size_t)e->n_toys * np);
+    std::vector<int> act(e->h_active, e->h_active + e->n_toys);
+    const std::string key = std::to_string(std::hash<std::string>{}(
+                                gf::generate_kernels(T, e->precision == GF_MIXED, e->block, e->batch_kernels).source)) +
+                            ":" + std::to_string(e->precision) + ":" + std::to_string(e->n_toys) + ":" +
+                            std::to_string(total) + ":" + std::to_string(e->amp_recompute ? 1 : 0);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if(it != cache.end()) {
+            e->gram_w = it->second.gram_w;
+            if(it->second.sh.conv_kp == e->plan.conv_kp && it->second.sh.grid_bpb == e->plan.grid_bins_per_block)
+                return GF_OK;
+            return applyShapes(e, it->second.sh, P, act);
+        }
+    }
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, e->device);
+    const size_t flushBytes = (size_t)std::max(l2, 1 << 20) * 2;
+    void *flush             = nullptr;
+    if(cudaMalloc(&flush, flushBytes) != cudaSuccess) {
+        cudaGetLastError();
+        flush = nullptr;
+    }
+    struct Free {
+        void *p;
+        ~Free() {
+            if(p)
+                cudaFree(p);
+        }
+    } guard{flush};
+    // candidates: table k-tiles (batches with convolutions), then grid bins per CTA (grids not folded into a
+    // table), each with the best of the other; the chunk stays as it is while they are compared
+    gf::Shapes best{e->plan.conv_kp, e->plan.grid_bins_per_block};
+    double bestMs = 1e30;
+    if((rc = timeEval(e, flush, flushBytes, 5, &bestMs)))
+        return rc;
+    auto tryShape = [&](gf::Shapes sh) -> int {
+        if(sh.conv_kp == best.conv_kp && sh.grid_bpb == best.grid_bpb)
+            return GF_OK;
+        if(int r2 = applyShapes(e, sh, P, act))
+            return r2;
+        double ms = 0;
+        if(int r2 = timeEval(e, flush, flushBytes, 5, &ms))
+            return r2;
+        if(ms < bestMs) {
+            bestMs = ms;
+            best   = sh;
+        }
+        return GF_OK;
+    };
+    if(e->batch_kernels && !T.convs.empty())
+        for(int kp : {1, 2, 4, 8})
+            if((rc = tryShape(gf::Shapes{kp, best.grid_bpb})))
+                return rc;
+    bool unfolded = false;
+    for(size_t q = 0; q < T.nums.size(); ++q)
+        unfolded = unfolded || !e->plan.num_folded[q];
+    if(unfolded)
+        for(int bpb : {128, 256, 512, 1024, 2048})
+            if((rc = tryShape(gf::Shapes{best.conv_kp, bpb})))
+                return rc;
+    if(e->shapes.conv_kp != best.conv_kp || e->shapes.grid_bpb != best.grid_bpb ||
+       e->plan.conv_kp != best.conv_kp || e->plan.grid_bins_per_block != best.grid_bpb)
+        if((rc = applyShapes(e, best, P, act)))
+            return rc;
+    // tensor-core Gram slice width: the integral rebuild timed at every width the widest node allows
+    int bestW = 0;
+    if(e->gram_tc && !e->amp_recompute && T.n_amp_nodes() > 0) {
+        int wmin = 16;
+        for(int k = 0; k < T.n_amp_nodes(); ++k)
+            wmin = std::max(wmin, gf_gram_tc_width(ampColumns(T, k)));
+        double bestG = 1e30;
+        for(int w : {16, 32, 64}) {
+            if(w < wmin)
+                continue;
+            e->gram_w = w;
+            double mn = 1e30;
+            for(int it = 0; it < 4; ++it) {
+                for(auto &ty : e->toys)
+                    ty.norm_valid = false;
+                if(flush)
+                    cudaMemsetAsync(flush, it & 0xff, flushBytes, e->stream);
+                cudaStreamSynchronize(e->stream);
+                const auto t0 = std::chrono::steady_clock::now();
+                if((rc = updateAmpCaches(e)))
+                    return rc;
+                const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+                if(it > 0)
+                    mn = std::min(mn, ms);
+            }
+            if(mn < bestG) {
+                bestG = mn;
+                bestW = w;
+            }
+        }
+        e->gram_w = bestW;
+        for(auto &ty : e->toys)
+            ty.norm_valid = false;
+    }
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        cache[key] = TunedShapes{best, bestW};
+    }
+    return GF_OK;
+}
+
+int gf_get_shapes(const gf_engine *e, int32_t *conv_kp, int32_t *grid_bpb, int32_t *gram_w) {
+    if(!e || !e->has_tree)
+        return gf_fail(nullptr, GF_ERR_STATE, "no tree");
+    if(conv_kp)
+        *conv_kp = e->plan.conv_kp;
+    if(grid_bpb)
+        *grid_bpb = e->plan.grid_bins_per_block;
+    if(gram_w) {
+        int w = 0;
+        for(int k = 0; k < e->tree.n_amp_nodes(); ++k)
+            w = std::max(w, gf_gram_tc_width(ampColumns(e->tree, k)));
+        *gram_w = e->gram_tc ? std::max(e->gram_w, w) : 0;
+    }
+    return GF_OK;
+}
+
+int gf_set_amp_mode(gf_engine *e, int mode, int64_t budget_bytes) {
+    if(!e)
+        return gf_fail(nullptr, GF_ERR_INVALID, "null engine");
+    if(mode < GF_AMP_AUTO || mode > GF_AMP_RECOMPUTE || budget_bytes < 0)
+        return gf_fail(e, GF_ERR_INVALID, "amplitude mode: GF_AMP_AUTO, GF_AMP_STORE or GF_AMP_RECOMPUTE, budget >= 0");
+    for(auto &t : e->toys)
+        if(t.loaded)
+            return gf_fail(e, GF_ERR_STATE, "gf_set_amp_mode must come before gf_upload_events");
+    e->amp_mode    = mode;
+    e->amp_budget  = budget_bytes;
+    e->amp_decided = false;
+    return GF_OK;
+}
+
+int64_t gf_amp_store_bytes(const gf_engine *e) {
+    if(!e || !e->has_tree || e->tree.n_amp_nodes() == 0 || e->toys.empty() || !e->toys[0].loaded)
+        return 0;
+    return (int64_t)ampStoreBytes(e, e->toys[0].npad);
+}
+
+int gf_amp_recomputing(const gf_engine *e) {
+    if(!e)
+        return -1;
+    return e->amp_decided ? (e->amp_recompute ? 1 : 0) : -1;
 }
 
 int gf_launches_per_eval(const gf_engine *e, int) {

@@ -77,6 +77,7 @@ struct GfModule {
     cudaKernel_t conv_g = nullptr, conv_n = nullptr, grid_g = nullptr, grid_n = nullptr;
     cudaKernel_t evt_g = nullptr, evt_n = nullptr, val_n = nullptr;
     cudaKernel_t amp = nullptr, ampn = nullptr, gram = nullptr;
+    cudaKernel_t evt_gr = nullptr, gramr = nullptr; // amplitude recompute mode (gradient pass, integrals)
     cudaKernel_t fcn_g = nullptr, fcn_n = nullptr; // one toy: the whole evaluation in one cooperative launch
 };
 
@@ -100,6 +101,19 @@ struct gf_engine {
     bool tune_pending   = false;  // the next evaluation runs the event-chunking autotuner
     int tuned_chunk     = 0;      // chunk size the autotuner chose (0: not tuned)
     int chunk_cap       = 0;      // chunks the chunk list and partials have room for
+
+    // amplitude derivatives (enum gf_amp_mode): stored per event and per normalisation point, or recomputed
+    // where they are used; auto recomputes when storing them would take more than amp_budget bytes (0: a
+    // quarter of the free device memory).  Decided at the first event upload after gf_set_tree.
+    int amp_mode         = GF_AMP_AUTO;
+    int64_t amp_budget   = 0;
+    bool amp_recompute   = false;
+    bool amp_decided     = false;
+
+    // launch shapes (gf_tune_shapes): the generator's table k-tiles and grid bins per CTA, and the tensor-core
+    // Gram kernel's slice width (0: the defaults)
+    gf::Shapes shapes;
+    int gram_w = 0;
 
     int fit_metric = GF_FIT_UNBINNED_NLL;
     int n_toys = 1;
@@ -193,8 +207,9 @@ int gf_gram_tc_width(int ncol);
 size_t gf_gram_tc_part_doubles(int ncol, int grid);
 // G (2 ncol x 2 ncol, FP64) = sum_{p < npts} x_r(p) eff(p) x_s(p) of the columns sc[c * nst + p] (nst a
 // multiple of 4, sc and eff 16-byte aligned) into out; part holds gf_gram_tc_part_doubles(ncol, sm_count)
-// doubles; *err gets bit 0 when a bounded wait ran out
+// doubles; *err gets bit 0 when a bounded wait ran out; width: real columns per slice (16, 32 or 64, at least
+// gf_gram_tc_width(ncol)), 0 for the narrowest
 cudaError_t gf_gram_tc_launch(const float2 *sc, long long npts, long long nst, int ncol, const float *eff,
-                              int sm_count, double *part, double *out, int *err, cudaStream_t s);
+                              int sm_count, double *part, double *out, int *err, cudaStream_t s, int width = 0);
 int gf_cuda_check(gf_engine *e, cudaError_t r, const char *what);
 int gf_run(gf_engine *e, bool grad, int metric_values_toy, int metric);

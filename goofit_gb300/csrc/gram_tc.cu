@@ -432,9 +432,11 @@ int gf_gram_tc_width(int ncol) {
 size_t gf_gram_tc_part_doubles(int ncol, int grid) { return (size_t)grid * 4 * ncol * ncol; }
 
 cudaError_t gf_gram_tc_launch(const float2 *sc, long long npts, long long nst, int ncol, const float *eff,
-                              int sm_count, double *part, double *out, int *err, cudaStream_t s) {
-    const int W = gf_gram_tc_width(ncol);
-    if(W == 0 || ncol < 1 || npts <= 0 || nst < npts || nst % 4 != 0 || ((uintptr_t)sc & 15) != 0 ||
+                              int sm_count, double *part, double *out, int *err, cudaStream_t s, int width) {
+    const int Wmin = gf_gram_tc_width(ncol);
+    const int W    = width == 0 ? Wmin : width;
+    if(Wmin == 0 || W < Wmin || (W != 16 && W != 32 && W != 64) || ncol < 1 || npts <= 0 || nst < npts ||
+       nst % 4 != 0 || ((uintptr_t)sc & 15) != 0 ||
        (eff && ((uintptr_t)eff & 15) != 0))
         return cudaErrorInvalidValue;
     const long long unit = (long long)(kRows / W) * kKS; // points per stage

@@ -187,10 +187,13 @@ NormLayout norm_layout(const Tree &t);
 struct KernelPlan {
     std::string source;
     size_t evt_smem_grad = 0, evt_smem_nograd = 0; // dynamic shared memory of the event kernels
+    bool recompute_kernels = false; // gf_evt_gr and gf_gramr were generated (amplitude recompute mode)
+    size_t evt_smem_gr     = 0;     // dynamic shared memory of gf_evt_gr
     size_t conv_smem_grad = 0, conv_smem_nograd = 0;
     int conv_tk = 64;      // table entries per conv CTA
     int conv_blocks = 0;   // CTAs per (toy, conv) of the table kernel
     int grid_bins_per_block = 256; // 1024 for batches of toys
+    int conv_kp             = 1;   // table k-tiles per staged model and resolution (batches of toys)
     std::vector<int> grid_blocks; // per numeric node
     int max_grid_blocks = 0;      // also covers the conv kernel's folded grid sums
     // A numeric node that is a ConvolutionPdf on a 1-D grid has the grid sum sum_b T[k(b)] = sum_k n_k T[k]
@@ -224,6 +227,12 @@ struct KernelPlan {
 };
 
 // batch: kernels shaped for many toys per launch (fewer, larger table and grid CTAs)
-KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, bool batch);
+// Launch shapes the autotuner varies (0: the generator's default): table k-tiles per staged model and resolution
+// (batches of toys), numeric-grid bins per CTA.
+struct Shapes {
+    int conv_kp  = 0;
+    int grid_bpb = 0;
+};
+KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, bool batch, const Shapes &shapes = Shapes());
 
 } // namespace gf

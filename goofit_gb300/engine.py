@@ -234,6 +234,34 @@ class Engine:
         """Longest device-side wait at the one-launch evaluation's grid barrier (ns; 0: the default 1 s)."""
         self._check(self._L.gf_set_wait_limit(self._h, int(ns)))
 
+    def set_amp_mode(self, mode: str, budget_bytes: int = 0) -> None:
+        """Amplitude derivatives 'store'd per event and normalisation point, 'recompute'd where they are used,
+        or 'auto' (recompute when storing would take more than budget_bytes; 0: a quarter of the free device
+        memory).  Before the first upload."""
+        m = {"auto": A.GF_AMP_AUTO, "store": A.GF_AMP_STORE, "recompute": A.GF_AMP_RECOMPUTE}[mode]
+        self._check(self._L.gf_set_amp_mode(self._h, m, int(budget_bytes)))
+
+    def amp_recomputing(self) -> int | None:
+        """True / False once decided (the first upload after set_tree), None before."""
+        r = int(self._L.gf_amp_recomputing(self._h))
+        return None if r < 0 else bool(r)
+
+    def amp_store_bytes(self) -> int:
+        """Device bytes the store mode keeps for amplitude derivatives and normalisation points."""
+        return int(self._L.gf_amp_store_bytes(self._h))
+
+    def tune_shapes(self) -> dict:
+        """Runs the launch-shape autotuner (table k-tiles, grid bins per CTA, Gram slice width) on the uploaded
+        events and returns the shapes in use."""
+        self._check(self._L.gf_tune_shapes(self._h))
+        return self.shapes()
+
+    def shapes(self) -> dict:
+        kp, bpb, w = C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(self._L.gf_get_shapes(self._h, C.byref(kp), C.byref(bpb), C.byref(w)))
+        return {"conv_kp": kp.value, "grid_bins_per_cta": bpb.value, "gram_slice_width": w.value,
+                "event_chunk": self.event_chunk()}
+
     def event_chunk(self) -> int:
         """Events per chunk of the event pass (after the autotuner, once an evaluation has run)."""
         return int(self._L.gf_event_chunk(self._h))

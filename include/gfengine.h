@@ -206,6 +206,34 @@ int64_t gf_event_chunk(const gf_engine *eng);
  * No counterpart in the reference (its Thrust reductions have no device-side waits). */
 int gf_set_wait_limit(gf_engine *eng, uint64_t ns);
 
+/* Where the derivatives of the amplitudes by floated resonance / line-shape parameters live (Amp3Body, Amp4Body).
+   GF_AMP_STORE: per-event columns and per-normalisation-point scratch columns, as the reference caches its
+   line shapes, spin factors and amplitudes (src/PDFs/physics/Amp4Body.cu:348-395).  GF_AMP_RECOMPUTE: only the
+   amplitude values are cached per event; the gradient pass recomputes dA/dt per event, and the integrals are
+   reduced from amplitudes recomputed at every normalisation point (no per-point storage).  GF_AMP_AUTO (the
+   default) recomputes when storing would take more than budget_bytes (0: a quarter of the free device memory).
+   Takes effect at the next gf_set_tree, or at the first gf_upload_events after it; GF_ERR_STATE once events
+   are uploaded. */
+enum gf_amp_mode { GF_AMP_AUTO = 0, GF_AMP_STORE = 1, GF_AMP_RECOMPUTE = 2 };
+int gf_set_amp_mode(gf_engine *eng, int mode, int64_t budget_bytes);
+/* 1: the engine recomputes amplitude derivatives, 0: it stores them (or the tree has none), -1: not decided yet
+   (no events uploaded since gf_set_tree). */
+int gf_amp_recomputing(const gf_engine *eng);
+/* Device bytes the store mode keeps for the derivative columns of the uploaded events and the normalisation
+   scratch columns (what the recompute mode does without); 0 without amplitude nodes or events. */
+int64_t gf_amp_store_bytes(const gf_engine *eng);
+
+/* Launch-shape autotuner (the counterpart of the reference's grain-size sweep, scripts/find_optimal.py): times
+   one gradient evaluation of every toy (device time, L2 flushed) for each candidate and keeps the fastest.
+   Candidates: the table kernel's k-tiles per staged model and resolution (1, 2, 4, 8; batches of toys with a
+   convolution), the numeric-grid bins per CTA (128 ... 2048; grids not folded into a table), then the
+   tensor-core Gram kernel's slice width (16, 32, 64 real columns; the integral rebuild timed).  Each table or
+   grid candidate recompiles the tree.  Needs uploaded events; results are remembered for the process, keyed by
+   tree, precision, toy count and events. */
+int gf_tune_shapes(gf_engine *eng);
+/* The shapes in use: table k-tiles, grid bins per CTA, Gram slice width (0: no tensor-core Gram). */
+int gf_get_shapes(const gf_engine *eng, int32_t *conv_kp, int32_t *grid_bpb, int32_t *gram_w);
+
 /* ---- minimiser (Minuit2 MnMigrad surface, src/goofit/FitManagerMinuit2.cpp:31-119) ---- */
 typedef struct gf_minimizer gf_minimizer;
 

@@ -90,3 +90,51 @@ def test_amp4body_lineshape_parameters_get_derivative_columns():
     marr, mp = A.i32(full)
     rc = L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, A.GF_MIXED, None, 0, C.byref(n))
     assert rc == A.GF_ERR_BAD_TREE and b"efficiency" in L.gf_last_error(None)
+
+
+def _source(nodes, olist, params, mask, prec):
+    L = A.lib()
+    nl = A.NodeList(nodes)
+    obs = A.observables_array(olist)
+    marr, mp = A.i32(mask)
+    n = C.c_int64()
+    assert L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, prec, None, 0, C.byref(n)) == 0
+    buf = C.create_string_buffer(n.value + 1)
+    L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, prec, buf, n.value + 1, C.byref(n))
+    return buf.value.decode()
+
+
+def c3_floated(bins):
+    """The C3 Amp3Body with the masses and widths of its first two resonances floated."""
+    pdf = W.c3_model(bins)[0]
+    names = [nm for nm, *_ in W.C3_RESONANCES[:2]]
+    for v in pdf.getParameters():
+        if any(v.name in (f"{nm}_mass", f"{nm}_width") for nm in names):
+            v.fixed = False
+            v.error = 0.01 * v.value
+            v.lowerlimit, v.upperlimit = 0.5 * v.value, 1.5 * v.value
+    return pdf
+
+
+@pytest.mark.parametrize("prec", [A.GF_MIXED, A.GF_FP64])
+@pytest.mark.parametrize("model", ["c5", "c3"])
+def test_recompute_mode_kernels_compile_for_sm103a(prec, model):
+    """With floated line-shape (C5) or resonance (C3) parameters the tree also gets the recompute-mode kernels:
+    a gradient event kernel that calls the amplitude functions per event and an integral kernel that
+    evaluates them per normalisation point; both compile for sm_103a."""
+    pdf = W.c5_model(1000, float_lineshapes=True)[0] if model == "c5" else c3_floated(300)
+    nodes, olist, params, mask = _tree(pdf)
+    src = _source(nodes, olist, params, mask, prec)
+    assert "gf_evt_gr(" in src and "gf_gramr(" in src
+    body = src[src.index("gf_evt_gr("):]
+    assert "gf_ampv_0(xd0_0[ij]" in body[:body.index("extern \"C\"") if "extern \"C\"" in body else len(body)]
+    L = A.lib()
+    nl = A.NodeList(nodes)
+    obs = A.observables_array(olist)
+    marr, mp = A.i32(mask)
+    n = C.c_int64()
+    assert L.gf_compile_tree(nl.arr, nl.n, obs, len(olist), len(params), mp, prec, C.byref(n)) == 0, \
+        L.gf_last_error(None)
+    # without floated amplitude-shape parameters there is nothing to recompute
+    fixed = [0 if (v.fixed or v.name.endswith(("_mass", "_width"))) else m for v, m in zip(params, mask)]
+    assert "gf_evt_gr(" not in _source(nodes, olist, params, fixed, prec)
