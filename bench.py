@@ -508,14 +508,15 @@ def run_toys(args) -> dict:
                       "round_ms_with_grad": float(np.mean(rt)),
                       "event_nll_evals_per_s": n_events / (np.mean(rt) / 1e3), "pulls": pulls,
                       "shapes": shapes, "shape_tuning_s": tune_s,
-                      # per lockstep round of the fit: wall time, and the part of it that is not the batched
-                      # evaluation (host MIGRAD steps, launch, synchronisation) - what keeping the whole fit in
-                      # one persistent launch could at most remove
-                      "rounds": int(max(r.nfcn for r in res)),
-                      "round_wall_ms": 1e3 * wall / max(1, int(max(r.nfcn for r in res))),
-                      "round_ms_with_grad_warm_l2": float(np.mean(rtw)),
-                      "round_host_and_launch_ms": 1e3 * wall / max(1, int(max(r.nfcn for r in res))) -
-                      float(np.mean(rtw))}
+                      "round_ms_with_grad_warm_l2": float(np.mean(rtw))}
+        if label == "mixed_analytic":
+            # per lockstep round of the fit (one batched evaluation; rounds = the most FCNs of any toy): wall
+            # time, and the part of it beyond a gradient round's device time (host MIGRAD steps, launch,
+            # synchronisation; a lower bound, value-only rounds being shorter) - what keeping the whole fit in
+            # one persistent launch could remove
+            rounds = int(max(r.nfcn for r in res))
+            out[label].update({"rounds": rounds, "round_wall_ms": 1e3 * wall / rounds,
+                               "round_host_and_launch_ms": 1e3 * wall / rounds - float(np.mean(rtw))})
         res_by[label] = res
         eng.close()
     m = out["mixed_analytic"]
