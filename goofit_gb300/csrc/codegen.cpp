@@ -501,18 +501,23 @@ struct GfArgs {
     int gtoy;                  /* toy of the normalisation pass */
     i64 chunk;                 /* events per chunk */
     i64 nevt0;                 /* events of toy 0 */
-    unsigned *gbar;            /* grid barrier of the one-launch evaluation: [arrivals, generation, error] */
+    unsigned *gbar;            /* grid barrier of the one-launch evaluation: [arrivals, unused, error] */
     unsigned long long bar_ns; /* longest wait at that barrier (%globaltimer ns) before the kernel gives up */
     int rec_n;                 /* one-launch evaluation: the toy's record passed by value in rec (R values) */
     int stage_off;             /* one-launch evaluation: shared-memory offset of the CTA's staged events */
     unsigned stage_cap;        /* and the bytes available there (0: events are read from global memory) */
-    int stage_pad;
+    unsigned bar_target;       /* the arrival count at which this launch's grid barrier opens */
     double *hpart;             /* one-launch evaluation: per chunk [components..., status] in page-locked host memory */
+    const int *ksort;          /* one-launch tabulated path: toy 0's bin offsets sorted by bin (null: read kcol) */
     alignas(16) unsigned char rec[512];
     const void *p0[192];       /* one toy: its observable, bin-offset and amplitude columns, no table lookup */
 };
 
 // chunk ch of the event list: with one toy its bounds follow from the chunk size, else from the table
+// pairwise sum of 8 values: exact when they are equal, three roundings on any path otherwise
+__device__ __forceinline__ R gf_tree8(const R *v) {
+    return ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+}
 __device__ __forceinline__ void gf_chunk(const GfArgs &a, int ch, int &toy, i64 &b0, i64 &e0) {
     if(a.n_toys == 1) {
         toy = 0;
@@ -552,34 +557,28 @@ __device__ __forceinline__ unsigned long long gf_globaltimer() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-__device__ __noinline__ bool gf_grid_sync(unsigned *bar, unsigned long long limit) {
+__device__ __noinline__ bool gf_grid_sync(unsigned *bar, unsigned target, unsigned long long limit) {
     __shared__ int ok;
     __syncthreads();
     if(threadIdx.x == 0) {
         int good = 1;
-        unsigned gen;
-        asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(gen) : "l"(bar + 1) : "memory");
-        // the arrival releases the CTA's writes (ordered before it by the __syncthreads above) and acquires
-        // the earlier arrivals' ones; the generation is released by the last arrival and acquired by the
-        // waiters, so every CTA sees every CTA's writes from before the barrier
-        unsigned prev;
-        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(prev) : "l"(bar) : "memory");
-        if(prev == gridDim.x * gridDim.y * gridDim.z - 1) {
-            asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" :: "l"(bar) : "memory");
-            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" :: "l"(bar + 1) : "memory");
-        } else {
-            const unsigned long long t0 = gf_globaltimer();
-            for(;;) {
-                unsigned g;
-                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(bar + 1) : "memory");
-                if(g != gen)
-                    break;
-                if(gf_globaltimer() - t0 > limit) {
-                    atomicOr(bar + 2, 1u);
-                    good = 0;
-                    break;
-                }
-                __nanosleep(20);
+        // The arrival counter only grows: launch e of the engine opens at e x (CTAs) arrivals (modulo 2^32),
+        // so an arriving CTA adds without reading and every CTA waits for the count itself (one trip to the
+        // counter, no second word written by a last arrival).  The arrival releases the CTA's writes (ordered
+        // before it by the __syncthreads above); the waiter's acquire of a count that includes every
+        // arrival synchronises with all of them (each later addition extends the earlier ones' release
+        // sequences), so every CTA sees every CTA's writes from before the barrier.
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" :: "l"(bar) : "memory");
+        const unsigned long long t0 = gf_globaltimer();
+        for(;;) {
+            unsigned c;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(bar) : "memory");
+            if((int)(c - target) >= 0)
+                break;
+            if(gf_globaltimer() - t0 > limit) {
+                atomicOr(bar + 2, 1u);
+                good = 0;
+                break;
             }
         }
         ok = good;
@@ -698,6 +697,9 @@ __device__ __forceinline__ ACC warp_acc2(ACC a) {
 __device__ __forceinline__ ACC acc_shfl_xor(ACC a, int o) {
     return make_float2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
 }
+__device__ __forceinline__ ACC acc_shfl(ACC a, int src) {
+    return make_float2(__shfl_sync(0xffffffffu, a.x, src), __shfl_sync(0xffffffffu, a.y, src));
+}
 __device__ __forceinline__ double acc_value(ACC a) { return (double)a.x + (double)a.y; }
 __device__ __forceinline__ float acc_r(ACC a) { return a.x + a.y; }
 // x * (h + l) for a normalisation factor kept as an FP32 pair: one rounding, no bias from rounding the factor
@@ -722,6 +724,7 @@ __device__ __forceinline__ ACC acc_add(ACC a, ACC b) { return a + b; }
 __device__ __forceinline__ ACC warp_acc(double v) { return gf_warp_sum(v); }
 __device__ __forceinline__ ACC warp_acc2(ACC a) { return gf_warp_sum(a); }
 __device__ __forceinline__ ACC acc_shfl_xor(ACC a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
+__device__ __forceinline__ ACC acc_shfl(ACC a, int src) { return __shfl_sync(0xffffffffu, a, src); }
 __device__ __forceinline__ double acc_value(ACC a) { return a; }
 __device__ __forceinline__ double acc_r(ACC a) { return a; }
 __device__ __forceinline__ double gf_nm(double x, double h, double l) { return x * h; }
@@ -1732,6 +1735,15 @@ struct Gen {
             os << "    if(k0 > " << cv.kmax << ") { gf_pdl_wait(); return; }\n";
             os << "    R *sM = sm; R *sR = sm + " << mcomp * nMp << ";\n";
             os << "    const int rbase = " << cv.offset << " - (k0 + " << KB - 1 << ");\n";
+            const bool kcPre = plan.conv_fold_q[ci] >= 0 && KB <= block;
+            if(kcPre) {
+                // the grid-bin count of one of this CTA's table entries per thread, loaded into a register now
+                // and stored after the staging below, so that the load's latency overlaps the staging
+                os << "    __shared__ R s_kc[" << KB << "];\n";
+                os << "    R kcv = R(0);\n";
+                os << "    if(tid < " << KB << " && k0 + tid <= " << cv.kmax << ") kcv = (R)gf_kcount_" << ci << "[k0 + tid - "
+                   << cv.kmin << "];\n";
+            }
             const double wM = (cv.ic[1] - cv.ic[0]) / cv.nM, wR = (cv.ic[4] - cv.ic[3]) / cv.nR;
             // support of every staged array: the first and last index holding a nonzero value (products with
             // an exact zero factor add nothing, so each item sums only the m range where both factors can
@@ -1780,6 +1792,8 @@ struct Gen {
                     }
                 os << "      }\n    }\n";
             }
+            if(kcPre)
+                os << "    if(tid < " << KB << ") s_kc[tid] = kcv;\n";
             os << "    __syncthreads();\n";
             os << "#pragma unroll\n    for(int c = 0; c < " << NA << "; ++c) {\n";
             os << "      const int lo = __reduce_min_sync(0xffffffffu, slo[c]), hi = __reduce_max_sync(0xffffffffu, "
@@ -1893,7 +1907,10 @@ struct Gen {
             else {
                 os << "      if(live && ms == 0 && k <= " << cv.kmax << ") {\n";
                 os << "        ctab[" << off[ci] << " + (k - " << cv.kmin << ") * " << cp << " + comp] = t;\n";
-                os << "        fs = acc_add(fs, gf_two_prod((R)gf_kcount_" << ci << "[k - " << cv.kmin << "], t));\n";
+                if(kcPre)
+                    os << "        fs = acc_add(fs, gf_two_prod(s_kc[k - k0], t));\n";
+                else
+                    os << "        fs = acc_add(fs, gf_two_prod((R)gf_kcount_" << ci << "[k - " << cv.kmin << "], t));\n";
                 os << "      }\n";
             }
             os << "    }\n";
@@ -2567,6 +2584,13 @@ struct Gen {
     // function that depends on the event only through one convolution's bin offset k): each CTA first
     // tabulates the per-event terms -log P and -dP/P over the table's k range in shared memory, and the
     // event loop gathers and adds them
+    // Bin offsets of convolution ci as the event pass reads them; in tab mode the sorted copy of toy 0's offsets
+    // when the engine provides one (the order of an event pass whose terms depend on the offset alone is free)
+    std::string kcolExpr(int ci, bool tab) const {
+        const std::string k = p0ptr("a.kcol", (int)T.convs.size(), ci, (int)T.obs.size());
+        return tab && ci == 0 ? "(a.ksort ? (const void *)a.ksort : " + k + ")" : k;
+    }
+
     // recompute (amplitude trees, gradient pass): dA/dt of the amplitude nodes is recomputed per event from the
     // FP64 event columns by the nodes' amplitude functions instead of read from stored derivative columns; the
     // amplitudes themselves are still read from their cached value columns
@@ -2719,7 +2743,7 @@ struct Gen {
             if(xused[o])
                 evtStreams.push_back({p0ptr("a.col", NO, o, 0), mixed ? 4 : 8});
         for(int ci = 0; ci < NC; ++ci)
-            evtStreams.push_back({p0ptr("a.kcol", NC, ci, NO), 4});
+            evtStreams.push_back({kcolExpr(ci, tab), 4});
         for(int ac = 0; ac < NA; ++ac)
             if(aused[ac])
                 evtStreams.push_back({p0ptr("a.acol", NA, ac, NO + NC), mixed ? 8 : 16});
@@ -2750,10 +2774,24 @@ struct Gen {
                 const int fq = plan.conv_fold_q[0];
                 const int comps = convComps(0, grad);
                 os << "  R *ltab = stab;\n";
+                // rows [kr_lo, kr_hi] of the table: with the events sorted by bin, those between this CTA's first
+                // and last event (read from its staged copy once that has arrived), else all of them
+                os << "  int kr_lo = 0, kr_hi = " << cv.nK - 1 << ";\n";
+                if(asBody) {
+                    os << "  if(a.ksort) {\n    kr_hi = -1;\n";
+                    os << "    const i64 le = ((i64)ce * a.chunk < a.nevt0 ? (i64)ce * a.chunk : a.nevt0) - 1;\n";
+                    os << "    if(cb < ce && le >= gf_ib) {\n";
+                    os << "      if(gf_st && gf_mbar_wait(gf_mbar, 0u, 1000000000ull)) {\n";
+                    os << "        const int *ks = reinterpret_cast<const int *>(gf_st + gf_soff[0]);\n";
+                    os << "        kr_lo = ks[0] - " << cv.kmin << "; kr_hi = ks[le - gf_ib] - " << cv.kmin << ";\n";
+                    os << "      } else { kr_lo = a.ksort[gf_ib] - " << cv.kmin << "; kr_hi = a.ksort[le] - " << cv.kmin << "; }\n";
+                    os << "      kr_lo = max(kr_lo, 0); kr_hi = min(kr_hi, " << cv.nK - 1 << ");\n";
+                    os << "    }\n  }\n";
+                }
                 os << "  " << vt << " tv[" << NR << "][" << nvr << "];\n";
                 os << "  {\n    const R *gt = reinterpret_cast<const R *>(a.ctab) + " << off[0] << ";\n";
-                os << "#pragma unroll\n    for(int r = 0; r < " << NR << "; ++r) {\n      const int kk = tid + r * " << block
-                   << ";\n      if(kk < " << cv.nK << ") {\n";
+                os << "#pragma unroll\n    for(int r = 0; r < " << NR << "; ++r) {\n      const int kk = kr_lo + tid + r * " << block
+                   << ";\n      if(kk <= kr_hi) {\n";
                 os << "#pragma unroll\n        for(int v = 0; v < " << nvr << "; ++v) tv[r][v] = *reinterpret_cast<const " << vt
                    << " *>(gt + kk * " << cp << " + " << per << " * v);\n";
                 os << "      }\n    }\n  }\n";
@@ -2801,10 +2839,13 @@ struct Gen {
                         vals.push_back("fs" + std::to_string(c));
                     emitCtaReduce(os, vals, "    ");
                     // GooPdf::normalize's numeric branch (src/PDFs/GooPdf.cu:366-395) on the CTA's sums
-                    os << "    if(tid == 0) {\n";
+                    // lane c of warp 0 sums component c over the warps; lane 0 gathers them
+                    os << "    if(tid < 32) {\n";
+                    os << "      ACC tc = acc_zero();\n";
+                    os << "      if(lane < " << comps << ") for(int w = 0; w < " << NW << "; ++w) tc = acc_add(tc, red[w][lane]);\n";
                     os << "      ACC tt[" << comps << "];\n";
-                    os << "      for(int c = 0; c < " << comps << "; ++c) { tt[c] = acc_zero(); for(int w = 0; w < " << NW
-                       << "; ++w) tt[c] = acc_add(tt[c], red[w][c]); }\n";
+                    os << "#pragma unroll\n      for(int c = 0; c < " << comps << "; ++c) tt[c] = acc_shfl(tc, c);\n";
+                    os << "      if(lane == 0) {\n";
                     os << "      const double S = acc_value(tt[0]);\n";
                     os << "      s_fbits = isnan(S) ? 1 : !(S > 0.0) ? 2 : 0;\n";
                     os << "      const double I = " << lit(cc) << " * S;\n";
@@ -2814,7 +2855,7 @@ struct Gen {
                     if(grad)
                         for(int j = 1; j < comps; ++j)
                             os << "      s_fn[" << 1 + j << "] = -N * N * (R)" << lit(cc) << " * (R)acc_r(tt[" << j << "]);\n";
-                    os << "    }\n    __syncthreads();\n  }\n";
+                    os << "      }\n    }\n    __syncthreads();\n  }\n";
                     os << "  const R N" << node << " = s_fn[0], NL" << node << " = s_fn[1]; (void)NL" << node << ";\n";
                     if(grad)
                         for(auto &d : plan.nl.qdN[fq]) {
@@ -2824,8 +2865,8 @@ struct Gen {
                         }
                 }
                 // per-k terms
-                os << "#pragma unroll\n  for(int r = 0; r < " << NR << "; ++r) {\n    const int kk = tid + r * " << block
-                   << ";\n    if(kk < " << cv.nK << ") {\n";
+                os << "#pragma unroll\n  for(int r = 0; r < " << NR << "; ++r) {\n    const int kk = kr_lo + tid + r * " << block
+                   << ";\n    if(kk <= kr_hi) {\n";
                 os << "      const int ek0 = " << cv.kmin << " + kk; (void)ek0;\n";
                 if(mixed) {
                     if(cp == 1)
@@ -2955,7 +2996,7 @@ struct Gen {
             if(xused[o])
                 os << "    const R *col" << o << " = " << colPtr("R", mixed ? 4 : 8, p0ptr("a.col", NO, o, 0)) << ";\n";
         for(int ci = 0; ci < NC; ++ci)
-            os << "    const int *kc" << ci << " = " << colPtr("int", 4, p0ptr("a.kcol", NC, ci, NO)) << ";\n";
+            os << "    const int *kc" << ci << " = " << colPtr("int", 4, kcolExpr(ci, tab)) << ";\n";
         for(int ac = 0; ac < NA; ++ac)
             if(aused[ac])
                 os << "    const R2 *acp" << ac << " = " << colPtr("R2", mixed ? 8 : 16, p0ptr("a.acol", NA, ac, NO + NC))
@@ -3065,6 +3106,12 @@ struct Gen {
             os << "      const int ka" << ci << "[8] = {kv" << ci << "a.x, kv" << ci << "a.y, kv" << ci << "a.z, kv" << ci
                << "a.w, kv" << ci << "b.x, kv" << ci << "b.y, kv" << ci << "b.z, kv" << ci << "b.w};\n";
         }
+        // tab: the iteration's events' terms are kept per component and summed pairwise after the loop
+        // (exact for equal terms, as neighbouring events in bin order mostly are; three roundings otherwise)
+        const int tabAcc = NGp + (factorRoot ? 1 : 0);
+        if(tab)
+            for(int q = 0; q < tabAcc; ++q)
+                os << "      R tsum" << q << "[" << VEC << "];\n";
         os << "#pragma unroll\n      for(int j = 0; j < " << VEC << "; ++j) {\n";
         if(tab) {
             // gather the event's tabulated terms (16-byte and narrower shared loads) and add them
@@ -3078,12 +3125,13 @@ struct Gen {
                 const int b = q / vw;
                 return "lq" + std::to_string(b) + (bw[b] == 1 ? std::string("") : std::string(fld[q % vw]));
             };
-            os << "        {\n        if(j < jn) {\n";
-            os << "          av += " << comp(0) << ";\n";
+            os << "        {\n        {\n";
+            os << "          const bool in = j < jn;\n";
+            os << "          tsum0[j] = in ? " << comp(0) << " : R(0);\n";
             for(int sl = 0; sl < NGp - 1; ++sl)
-                os << "          ag" << sl << " += " << comp(1 + sl) << ";\n";
+                os << "          tsum" << 1 + sl << "[j] = in ? " << comp(1 + sl) << " : R(0);\n";
             if(factorRoot)
-                os << "          nv += " << comp(tabComps - 1) << ";\n";
+                os << "          tsum" << NGp << "[j] = in ? " << comp(tabComps - 1) << " : R(0);\n";
             os << "        }\n";
         } else {
         for(int o = 0; o < NO; ++o)
@@ -3246,6 +3294,13 @@ struct Gen {
             if(logProd) {
                 os << "      av -= logf(lm) + (float)le * GF_LN2_LO;\n";
                 os << "      gf_comp_add(avh, avl, (float)(-le) * GF_LN2_HI);\n";
+            }
+            if(tab) {
+                os << "      av = gf_tree8(tsum0);\n";
+                for(int sl = 0; sl < NGp - 1; ++sl)
+                    os << "      ag" << sl << " = gf_tree8(tsum" << 1 + sl << ");\n";
+                if(factorRoot)
+                    os << "      nv += gf_tree8(tsum" << NGp << ");\n";
             }
             os << "      gf_comp_add(avh, avl, av);\n";
             // gradient sums are compensated where it is cheap (8 events per iteration) or many events per
@@ -3410,7 +3465,7 @@ struct Gen {
         // a CTA that leaves early still waits (bounded) for its own bulk copy, so that no copy writes the shared
         // memory of a finished CTA
         auto barrier = [&]() {
-            os << "  if(!gf_grid_sync(a.gbar, a.bar_ns)) {\n";
+            os << "  if(!gf_grid_sync(a.gbar, a.bar_target, a.bar_ns)) {\n";
             os << "    if(s_staged) gf_mbar_wait(&s_mbar, 0u, 1000000000ull);\n";
             os << "    return;\n  }\n";
         };

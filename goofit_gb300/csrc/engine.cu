@@ -92,6 +92,103 @@ __global__ void gf_convert_events(const ConvertArgs a) {
 
 size_t rsize(const gf_engine *e) { return e->precision == GF_MIXED ? 4 : 8; }
 
+// Counting sort of one toy's convolution bin offsets (the one-launch tabulated path, where an event's terms
+// depend on the event only through its bin offset, so the order in which the events are summed is free):
+// the histogram of the offsets, then every sorted position takes the bin whose prefix range holds it.  With the
+// events in bin order every warp's gathers from the per-bin term table hit one or two rows (shared-memory
+// broadcasts instead of bank conflicts), and each CTA's events span a few bins only.
+__global__ void gf_khist(const int *__restrict__ k, long long n, int kmin, int nK, unsigned *__restrict__ hist) {
+    extern __shared__ unsigned sh[];
+    const bool local = nK <= 8192;
+    if(local)
+        for(int i = threadIdx.x; i < nK; i += blockDim.x)
+            sh[i] = 0;
+    __syncthreads();
+    for(long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int b = k[e] - kmin;
+        if(b >= 0 && b < nK)
+            atomicAdd(local ? &sh[b] : &hist[b], 1u);
+    }
+    __syncthreads();
+    if(local)
+        for(int i = threadIdx.x; i < nK; i += blockDim.x)
+            if(sh[i])
+                atomicAdd(&hist[i], sh[i]);
+}
+
+// offs[0..nK]: prefix sums of the histogram; positions past n (padding) take the first bin
+__global__ void gf_kfill(const long long *__restrict__ offs, int nK, int kmin, long long n, long long npad,
+                         int *__restrict__ out) {
+    for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < npad; i += (long long)gridDim.x * blockDim.x) {
+        int b = 0;
+        if(i < n) {
+            int lo = 0, hi = nK - 1; // the last b with offs[b] <= i
+            while(lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if(offs[mid] <= i)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            b = lo;
+        }
+        out[i] = kmin + b;
+    }
+}
+
+// Sorted copy of toy 0's offsets of convolution 0 (allocated on first use, rebuilt after every upload).
+int buildKSort(gf_engine *e) {
+    GfToy &ty = e->toys[0];
+    if(!ty.loaded || e->tree.convs.empty())
+        return GF_OK;
+    const gf::ConvInfo &cv = e->tree.convs[0];
+    const int nK           = cv.nK;
+    cudaError_t r          = cudaSuccess;
+    if(!ty.ksort)
+        r = cudaMalloc((void **)&ty.ksort, sizeof(int) * (size_t)std::max<int64_t>(8, ty.npad));
+    unsigned *hist = nullptr;
+    long long *offs = nullptr;
+    if(r == cudaSuccess)
+        r = cudaMalloc((void **)&hist, sizeof(unsigned) * nK);
+    if(r == cudaSuccess)
+        r = cudaMalloc((void **)&offs, sizeof(long long) * (nK + 1));
+    std::vector<unsigned> h(nK);
+    std::vector<long long> o(nK + 1, 0);
+    const int grid = std::max(1, e->sm_count) * 2;
+    if(r == cudaSuccess)
+        r = cudaMemsetAsync(hist, 0, sizeof(unsigned) * nK, e->stream);
+    if(r == cudaSuccess) {
+        gf_khist<<<grid, 256, nK <= 8192 ? sizeof(unsigned) * nK : 0, e->stream>>>(ty.kcols[0], ty.n, cv.kmin, nK, hist);
+        r = cudaGetLastError();
+    }
+    if(r == cudaSuccess)
+        r = cudaMemcpyAsync(h.data(), hist, sizeof(unsigned) * nK, cudaMemcpyDeviceToHost, e->stream);
+    if(r == cudaSuccess)
+        r = cudaStreamSynchronize(e->stream);
+    if(r == cudaSuccess) {
+        for(int b = 0; b < nK; ++b)
+            o[b + 1] = o[b] + h[b];
+        if(o[nK] != ty.n)
+            r = cudaErrorInvalidValue; // an offset outside the table (rejected at upload already)
+    }
+    if(r == cudaSuccess)
+        r = cudaMemcpyAsync(offs, o.data(), sizeof(long long) * (nK + 1), cudaMemcpyHostToDevice, e->stream);
+    if(r == cudaSuccess) {
+        gf_kfill<<<grid, 256, 0, e->stream>>>(offs, nK, cv.kmin, ty.n, ty.npad, ty.ksort);
+        r = cudaGetLastError();
+    }
+    if(r == cudaSuccess)
+        r = cudaStreamSynchronize(e->stream);
+    if(hist)
+        cudaFree(hist);
+    if(offs)
+        cudaFree(offs);
+    if(r != cudaSuccess)
+        return gf_cuda_check(e, r, "sorting the bin offsets");
+    ty.ksort_valid = true;
+    return GF_OK;
+}
+
 void freeToy(GfToy &t) {
     for(int o = 0; o < 16; ++o)
         if(t.cols[o]) {
@@ -101,6 +198,10 @@ void freeToy(GfToy &t) {
         }
     for(int c = 0; c < 8; ++c)
         t.kcols[c] = nullptr;
+    if(t.ksort)
+        cudaFree(t.ksort);
+    t.ksort       = nullptr;
+    t.ksort_valid = false;
     if(t.abase)
         cudaFree(t.abase);
     t.abase = nullptr;
@@ -344,6 +445,7 @@ int buildLayout(gf_engine *e) {
     chk(dalloc(e, e->d_gcounter, (size_t)NT * std::max(1, NQ)));
     chk(dalloc(e, e->d_counter, NT));
     chk(dalloc(e, e->d_gbar, 4));
+    e->bar_epoch = 0;
     chk(dalloc(e, e->d_toy_chunk0, NT));
     chk(dalloc(e, e->d_toy_nchunks, NT));
     chk(dalloc(e, e->d_toy_nevents, NT));
@@ -435,6 +537,9 @@ int buildLayout(gf_engine *e) {
     cudaError_t r = cudaDeviceSynchronize();
     if(r != cudaSuccess)
         return gf_cuda_check(e, r, "layout upload");
+    if(e->plan.fused_tab && e->n_toys == 1 && e->use_ksort && !e->toys[0].ksort_valid)
+        if(int rk = buildKSort(e))
+            return rk;
     e->layout_ready = true;
     return GF_OK;
 }
@@ -591,6 +696,8 @@ GfArgs fusedArgs(gf_engine *e, bool grad) {
         cudaGetLastError();
     a.active        = nullptr;
     a.hpart         = e->d_fpart;
+    a.bar_target    = (e->bar_epoch + 1u) * (unsigned)e->fcn_grid;
+    a.ksort         = e->plan.fused_tab && e->toys[0].ksort_valid ? e->toys[0].ksort : nullptr;
     const size_t rb = rsize(e) * (size_t)e->plan.nl.npr;
     a.rec_n         = 0;
     if(rb > 0 && rb <= sizeof(a.rec)) {
@@ -618,6 +725,10 @@ cudaError_t enqueueEval(gf_engine *e, bool grad) {
             cfg.attrs            = attr;
             cfg.numAttrs         = 1;
             r = cudaLaunchKernelExC(&cfg, (const void *)(grad ? e->mod.fcn_g : e->mod.fcn_n), args);
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            if(r == cudaSuccess && cudaStreamIsCapturing(e->stream, &cs) == cudaSuccess &&
+               cs == cudaStreamCaptureStatusNone)
+                ++e->bar_epoch;
         }
         if(r == cudaSuccess)
             r = recordEvent(e, e->ev[3]);
@@ -1441,8 +1552,11 @@ int gf_run(gf_engine *e, bool grad, int, int) {
                     cudaGetLastError();
                     e->fused_graph_ok = false;
                     r                 = enqueueEval(e, grad);
-                } else
+                } else {
                     r = cudaGraphLaunch(ge, e->stream);
+                    if(r == cudaSuccess)
+                        ++e->bar_epoch;
+                }
             } else
                 r = cudaGraphLaunch(ge, e->stream);
         } else
@@ -1498,6 +1612,7 @@ int gf_run(gf_engine *e, bool grad, int, int) {
         // the stopped CTAs left behind, so that the next evaluation starts clean
         const gf::Tree &T = e->tree;
         cudaMemsetAsync(e->d_gbar, 0, 4 * sizeof(unsigned), e->stream);
+        e->bar_epoch = 0;
         cudaMemsetAsync(e->d_counter, 0, sizeof(unsigned) * e->n_toys, e->stream);
         cudaMemsetAsync(e->d_gcounter, 0, sizeof(unsigned) * e->n_toys * std::max<size_t>(1, T.nums.size()), e->stream);
         cudaMemsetAsync(e->d_qflag, 0, sizeof(int) * e->n_toys, e->stream);
@@ -1559,6 +1674,8 @@ int gf_engine_create(gf_engine **out, int device, int precision) {
         e->use_pdl = e->use_pdl && !(p[0] == '1');
     if(const char *f = std::getenv("GF_FUSED"))
         e->use_fused = !(f[0] == '0');
+    if(const char *ks = std::getenv("GF_KSORT"))
+        e->use_ksort = ks[0] != '0';
     if(const char *st = std::getenv("GF_STAGE"))
         e->use_stage = !(st[0] == '0');
     if(const char *c = std::getenv("GF_EVT_CTAS_PER_SM")) {
@@ -1860,6 +1977,9 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
     }
     if(herr)
         return gf_fail(e, GF_ERR_INVALID, "event outside the observable range of a ConvolutionPdf");
+    ty.ksort_valid = false;
+    if(toy == 0 && e->n_toys == 1 && e->plan.fused_tab && e->use_ksort)
+        return buildKSort(e);
     return GF_OK;
 }
 

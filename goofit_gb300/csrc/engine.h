@@ -44,13 +44,14 @@ struct GfArgs {
     int gtoy;
     long long chunk;      // events per chunk
     long long nevt0;      // events of toy 0
-    unsigned *gbar;       // grid barrier words of the one-launch evaluation [arrivals, generation, error]
+    unsigned *gbar;       // grid barrier words of the one-launch evaluation [arrivals, unused, error]
     unsigned long long bar_ns; // longest barrier wait (ns) before the one-launch kernel gives up
     int rec_n;            // one-launch evaluation: the toy's record (rec_n R values) passed by value in rec
     int stage_off;        // one-launch evaluation: shared-memory offset and room (bytes) of the staged events
     unsigned stage_cap;
-    int stage_pad;
+    unsigned bar_target;  // the arrival count at which this launch's grid barrier opens
     double *hpart;        // one-launch evaluation: per-chunk [components..., status] rows in page-locked memory
+    const int *ksort;     // one-launch tabulated path: toy 0's bin offsets sorted by bin (null: read kcol)
     alignas(16) unsigned char rec[512];
     const void *p0[192];  // toy 0: observable columns, bin-offset columns, amplitude columns (one toy only)
 };
@@ -61,6 +62,8 @@ struct GfToy {
     double total = 0; // number of events: n, or the summed bin contents of binned data
     void *cols[16] = {nullptr};
     int *kcols[8]  = {nullptr};
+    int *ksort     = nullptr;           // one-launch tabulated path: the bin offsets of conv 0 sorted by bin
+    bool ksort_valid = false;
     void *abase    = nullptr;           // cached resonance amplitudes and FP64 Dalitz columns (one allocation)
     void *acols[128] = {nullptr};       // R2 per event: amplitude columns, then derivative columns
     double *dcols[16] = {nullptr};      // FP64 event columns of the Dalitz variables
@@ -184,9 +187,11 @@ struct gf_engine {
     // words it synchronises on and the longest barrier wait before it gives up (GF_FUSED=0: three launches)
     bool use_fused        = true;
     bool use_stage        = true; // GF_STAGE=0: the one-launch kernel reads events from global memory
+    bool use_ksort        = true; // GF_KSORT=0: its tabulated event pass reads the offsets in upload order
     int fcn_grid          = 0;
     unsigned *d_gbar      = nullptr;
     unsigned long long bar_ns = 1000000000ull;
+    unsigned bar_epoch        = 0; // one-launch evaluations run since the barrier words were cleared
     bool fused_graph_ok   = true; // false: the cooperative launch is not captured into a graph here
     // captured one-launch graphs [nograd, grad]: the source graph, its kernel node and that node's launch
     // parameters, whose arguments (the toy's record by value) are replaced before every graph launch
