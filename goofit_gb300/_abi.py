@@ -152,6 +152,7 @@ SIGNATURES = [
     ("gf_launches_per_eval", C.c_int, [_vp, C.c_int]),
     ("gf_event_chunk", C.c_int64, [_vp]),
     ("gf_set_wait_limit", C.c_int, [_vp, C.c_uint64]),
+    ("gf_set_gram_wait_limit", C.c_int, [_vp, C.c_uint64]),
     ("gf_set_amp_mode", C.c_int, [_vp, C.c_int, C.c_int64]),
     ("gf_amp_recomputing", C.c_int, [_vp]),
     ("gf_amp_store_bytes", C.c_int64, [_vp]),

@@ -22,6 +22,7 @@
 #include "tree.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstdio>
 #include <functional>
@@ -628,6 +629,20 @@ __device__ __forceinline__ float gf_group_sum(float v, int width) {
     }
     return hi + lo;
 }
+// The width lanes' pairs v + c summed as pairs: the total as a normalised pair (hi, lo) in every lane
+__device__ __forceinline__ float2 gf_group_sum2(float v, float c, int width) {
+    float hi = v, lo = c;
+    for(int o = width >> 1; o > 0; o >>= 1) {
+        const float h2 = __shfl_xor_sync(0xffffffffu, hi, o, width);
+        const float l2 = __shfl_xor_sync(0xffffffffu, lo, o, width);
+        float s, e;
+        gf_two_sum(hi, h2, s, e);
+        hi = s;
+        lo += l2 + e;
+    }
+    const float h = hi + lo;
+    return make_float2(h, lo - (h - hi));
+}
 // s + c += v with a two-sum correction term c.
 __device__ __forceinline__ void gf_comp_add(float &s, float &c, float v) {
     float t, e;
@@ -706,6 +721,99 @@ __device__ __forceinline__ float acc_r(ACC a) { return a.x + a.y; }
 __device__ __forceinline__ float gf_nm(float x, float h, float l) { return fmaf(x, h, x * l); }
 #define GF_CENTRE(lo, w, b) ((float)(lo) + (float)(w) * ((float)(b) + 0.5f))
 )CUDA";
+
+// Unevaluated FP32 pairs h + l (about 44 significant bits) for the per-bin terms of the tabulated event pass.
+// There the event function and -log P of each bin offset are evaluated once and then added once per event,
+// so a rounding of a bin's term in single precision would be repeated by every event of that bin and would
+// move the NLL in steps as the parameters change.  The arithmetic is the classic double-single one (Dekker's
+// exact products through fma, Knuth's two-sum); the logarithm reduces x = (m + ml) 2^e with
+// m in [1/sqrt 2, sqrt 2) around c = 1 + j/32 and sums ln 2^e + ln c + 2 atanh(s), s = (m + ml - c) / (m + ml + c),
+// |s| < 0.011, with the series 2 s + 2 s^3 / 3 + 2 s^5 / 5 + 2 s^7 / 7 (the first term as a pair).
+const char *kPreludeDF = R"CUDA(
+struct gf_df {
+    float h, l;
+    __device__ __forceinline__ gf_df() : h(0.f), l(0.f) {}
+    __device__ __forceinline__ gf_df(float x) : h(x), l(0.f) {}
+    __device__ __forceinline__ gf_df(int x) : h((float)x), l(0.f) {}
+    __device__ __forceinline__ gf_df(float hi, float lo) : h(hi), l(lo) {}
+};
+__device__ __forceinline__ gf_df gf_df_fast(float a, float b) { const float s = a + b; return gf_df(s, b - (s - a)); }
+__device__ __forceinline__ gf_df operator+(gf_df a, gf_df b) {
+    float s, e;
+    gf_two_sum(a.h, b.h, s, e);
+    e += a.l + b.l;
+    return gf_df_fast(s, e);
+}
+__device__ __forceinline__ gf_df operator-(gf_df a) { return gf_df(-a.h, -a.l); }
+__device__ __forceinline__ gf_df operator-(gf_df a, gf_df b) { return a + (-b); }
+__device__ __forceinline__ gf_df operator*(gf_df a, gf_df b) {
+    const float p = a.h * b.h;
+    const float e = fmaf(a.h, b.l, fmaf(a.l, b.h, fmaf(a.h, b.h, -p)));
+    return gf_df_fast(p, e);
+}
+// a / b: a first quotient, the exact residual a - q1 b, and its quotient (each quotient to a few ulps suffices:
+// the second corrects the first, and its own error is 2^-23 of a term 2^-22 smaller than the first)
+__device__ __forceinline__ gf_df operator/(gf_df a, gf_df b) {
+    const float q1 = __fdividef(a.h, b.h);
+    const float p = q1 * b.h, pe = fmaf(q1, b.h, -p);
+    float s, e;
+    gf_two_sum(a.h, -p, s, e);
+    e += a.l - pe - q1 * b.l;
+    return gf_df_fast(q1, __fdividef(s + e, b.h));
+}
+__device__ __forceinline__ gf_df &operator+=(gf_df &a, gf_df b) { a = a + b; return a; }
+__device__ __forceinline__ gf_df &operator-=(gf_df &a, gf_df b) { a = a - b; return a; }
+__device__ __forceinline__ gf_df &operator*=(gf_df &a, gf_df b) { a = a * b; return a; }
+__device__ __forceinline__ gf_df &operator/=(gf_df &a, gf_df b) { a = a / b; return a; }
+__device__ __forceinline__ bool operator>(gf_df a, gf_df b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
+__device__ __forceinline__ bool operator<(gf_df a, gf_df b) { return b > a; }
+// x * (h + l) for a normalisation factor kept as an FP32 pair
+__device__ __forceinline__ gf_df gf_nm(gf_df x, float h, float l) { return x * gf_df(h, l); }
+#define GF_LN2_DH 0.693147182f
+#define GF_LN2_DL -1.90465421e-09f
+// ln x; single precision for x <= 0, NaN and infinity
+__device__ __forceinline__ gf_df gf_df_log(gf_df x) {
+    if(!(x.h > 0.f) || isinf(x.h))
+        return gf_df(logf(x.h));
+    int e;
+    float m = frexpf(x.h, &e);
+    if(m < 0.707106769f) {
+        m *= 2.f;
+        e -= 1;
+    }
+    const float ml = ldexpf(x.l, -e);
+    const int j    = __float2int_rn((m - 1.f) * 32.f);
+    const float c  = fmaf((float)j, 0.03125f, 1.f);
+    float uh, ul;
+    gf_two_sum(m - c, ml, uh, ul);
+    const gf_df u(uh, ul);
+    const gf_df s = u / (gf_df(2.f * c) + u);
+    const float s2   = s.h * s.h;
+    const float tail = s.h * s2 * fmaf(s2, fmaf(s2, 0.285714298f, 0.4f), 0.666666687f);
+    gf_df r = gf_df(2.f * s.h, 2.f * s.l) + gf_df(tail);
+    r += gf_df(gf_lnc_h[j + 9], gf_lnc_l[j + 9]);
+    const float fe = (float)e;
+    const float p  = fe * GF_LN2_DH;
+    r += gf_df_fast(p, fmaf(fe, GF_LN2_DL, fmaf(fe, GF_LN2_DH, -p)));
+    return r;
+}
+)CUDA";
+
+// ln(1 + j/32), j = -9 .. 13, as FP32 pairs for gf_df_log (from the host's FP64 logarithm)
+std::string dfLogTable() {
+    std::string h = "__device__ const float gf_lnc_h[23] = {", l = "__device__ const float gf_lnc_l[23] = {";
+    char buf[64];
+    for(int j = -9; j <= 13; ++j) {
+        const double v  = std::log1p(j / 32.0);
+        const float vh  = (float)v;
+        const float vl  = (float)(v - (double)vh);
+        std::snprintf(buf, sizeof buf, "%s%.9ef", j > -9 ? ", " : "", (double)vh);
+        h += buf;
+        std::snprintf(buf, sizeof buf, "%s%.9ef", j > -9 ? ", " : "", (double)vl);
+        l += buf;
+    }
+    return h + "};\n" + l + "};\n";
+}
 
 const char *kPreludeF64 = R"CUDA(
 __device__ __forceinline__ double gf_group_sum(double v, int width) {
@@ -1522,6 +1630,29 @@ struct Gen {
     static int convStride(int n) { return n + (((8 - n) % 32) + 32) % 32; }
 
     // Table layout per toy: for each conv, AoS [k][cp] with cp = padded component count (16-byte rows).
+    // The event function of the tabulated pass can be evaluated with gf_df: only sums, products and quotients
+    // (AddPdf, ProdPdf, constant polynomials) above the convolution, whose model and resolution the table kernel
+    // evaluates.
+    bool dfEligible() const {
+        std::vector<int> st{0};
+        while(!st.empty()) {
+            const TNode &n = T.nodes[st.back()];
+            st.pop_back();
+            switch(n.op) {
+            case GF_OP_CONVOLUTION:
+            case GF_OP_POLYNOMIAL:
+            case GF_OP_POLYNOMIAL_OFFSET: break;
+            case GF_OP_ADD:
+            case GF_OP_ADD_EXT:
+            case GF_OP_PROD:
+                for(int ch : n.children)
+                    st.push_back(ch);
+                break;
+            default: return false;
+            }
+        }
+        return true;
+    }
     void tableLayout(bool grad) {
         auto &off = grad ? plan.ctab_off_grad : plan.ctab_off_nograd;
         auto &cps = grad ? plan.ctab_cp_grad : plan.ctab_cp_nograd;
@@ -1536,6 +1667,12 @@ struct Gen {
             total += (int64_t)cp * T.convs[ci].nK;
         }
         total = (total + 3) / 4 * 4;
+        int64_t &lo = grad ? plan.ctab_lo_off_grad : plan.ctab_lo_off_nograd;
+        lo          = -1;
+        if(mixed && !batch && !T.convs.empty()) {
+            lo = total;
+            total += (T.convs[0].nK + 3) / 4 * 4;
+        }
         (grad ? plan.ctab_per_toy_grad : plan.ctab_per_toy_nograd) = total;
     }
 
@@ -1553,6 +1690,9 @@ struct Gen {
         for(size_t ci = 0; ci < T.convs.size(); ++ci)
             maxComps = std::max(maxComps, convComps((int)ci, grad));
         sh.MS    = (!batch && maxComps <= block / 32) ? 32 : 8;
+        // one toy: 4 entries per item tile, so that the table spreads over twice as many CTAs (its sums and lane
+        // reductions halve per CTA; the launch has CTAs to spare, every one of which waits at the grid barrier)
+        sh.KT = batch ? 8 : 4;
         sh.items = block / sh.MS;
         // batches: each item covers KP k-tiles in turn, so that one CTA's staged model and resolution
         // arrays (whose evaluation is a third of the work at KP = 1) serve KP times the table entries;
@@ -1735,7 +1875,19 @@ struct Gen {
             os << "    if(k0 > " << cv.kmax << ") { gf_pdl_wait(); return; }\n";
             os << "    R *sM = sm; R *sR = sm + " << mcomp * nMp << ";\n";
             os << "    const int rbase = " << cv.offset << " - (k0 + " << KB - 1 << ");\n";
-            const bool kcPre = plan.conv_fold_q[ci] >= 0 && KB <= block;
+            // one pass of k-tiles per item: the lane that adds an item's entries to the folded grid sum (ms == 0)
+            // loads their grid-bin counts into registers first, so that nothing waits for these loads before
+            // the fold at the end
+            const bool kcReg = plan.conv_fold_q[ci] >= 0 && sh.KP == 1;
+            const bool kcPre = plan.conv_fold_q[ci] >= 0 && KB <= block && !kcReg;
+            if(kcReg) {
+                os << "    R kcr[" << KT << "];\n    {\n";
+                os << "      const int kb_ = (tid / " << MS << ") / " << comps << ", kt0_ = k0 + kb_ * " << KT << ";\n";
+                os << "      const bool kl_ = tid % " << MS << " == 0 && kb_ < " << ktiles << ";\n";
+                os << "#pragma unroll\n      for(int j = 0; j < " << KT << "; ++j)\n";
+                os << "        kcr[j] = kl_ && kt0_ + j <= " << cv.kmax << " ? (R)gf_kcount_" << ci << "[kt0_ + j - " << cv.kmin
+                   << "] : R(0);\n    }\n";
+            }
             if(kcPre) {
                 // the grid-bin count of one of this CTA's table entries per thread, loaded into a register now
                 // and stored after the staging below, so that the load's latency overlaps the staging
@@ -1897,20 +2049,36 @@ struct Gen {
             os << "          }\n";
             os << "#pragma unroll\n          for(int j = 0; j < " << KT << "; ++j) gf_comp_add(acc[j], cmp[j], bs[j]);\n";
             os << "        }\n      }\n    }\n";
-            os << "#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) acc[j] += cmp[j];\n";
-            os << "#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) {\n";
-            os << "      const R t = gf_group_sum(acc[j], " << MS << ");\n";
+            // mixed precision: the lanes' compensated sums reduced as pairs; conv 0's values keep the pair's low
+            // part (one toy), so that a value enters the per-bin terms and the folded grid sum unrounded
+            const int64_t loOff = ci == 0 ? (grad ? plan.ctab_lo_off_grad : plan.ctab_lo_off_nograd) : -1;
+            if(mixed) {
+                os << "#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) {\n";
+                os << "      const ACC tp = gf_group_sum2(acc[j], cmp[j], " << MS << ");\n";
+                os << "      const R t = tp.x;\n";
+            } else {
+                os << "#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) acc[j] += cmp[j];\n";
+                os << "#pragma unroll\n    for(int j = 0; j < " << KT << "; ++j) {\n";
+                os << "      const R t = gf_group_sum(acc[j], " << MS << ");\n";
+            }
             os << "      const int k = kt0 + j;\n";
-            if(fq < 0)
-                os << "      if(live && ms == 0 && k <= " << cv.kmax << ") ctab[" << off[ci] << " + (k - " << cv.kmin
-                   << ") * " << cp << " + comp] = t;\n";
-            else {
+            const std::string loStore = loOff >= 0 ? "        if(comp == 0) ctab[" + std::to_string(loOff) + " + (k - " +
+                                                         std::to_string(cv.kmin) + ")] = tp.y;\n"
+                                                   : "";
+            if(fq < 0) {
                 os << "      if(live && ms == 0 && k <= " << cv.kmax << ") {\n";
-                os << "        ctab[" << off[ci] << " + (k - " << cv.kmin << ") * " << cp << " + comp] = t;\n";
-                if(kcPre)
-                    os << "        fs = acc_add(fs, gf_two_prod(s_kc[k - k0], t));\n";
+                os << "        ctab[" << off[ci] << " + (k - " << cv.kmin << ") * " << cp << " + comp] = t;\n" << loStore;
+                os << "      }\n";
+            } else {
+                os << "      if(live && ms == 0 && k <= " << cv.kmax << ") {\n";
+                os << "        ctab[" << off[ci] << " + (k - " << cv.kmin << ") * " << cp << " + comp] = t;\n" << loStore;
+                const std::string kc = kcReg   ? "kcr[j]"
+                                       : kcPre ? "s_kc[k - k0]"
+                                               : "(R)gf_kcount_" + std::to_string(ci) + "[k - " + std::to_string(cv.kmin) + "]";
+                if(mixed)
+                    os << "        { ACC pr = gf_two_prod(" << kc << ", t); pr.y = fmaf(" << kc << ", tp.y, pr.y); fs = acc_add(fs, pr); }\n";
                 else
-                    os << "        fs = acc_add(fs, gf_two_prod((R)gf_kcount_" << ci << "[k - " << cv.kmin << "], t));\n";
+                    os << "        fs = acc_add(fs, gf_two_prod(" << kc << ", t));\n";
                 os << "      }\n";
             }
             os << "    }\n";
@@ -2680,11 +2848,30 @@ struct Gen {
         // blocks of 16 bytes (4 FP32 / 2 FP64 terms), each block its own array over k, the remainder in a
         // narrower array, so that an event's gather reads no padding (C2: 16 + 4 bytes)
         const int tabComps = NGp + (factorRoot ? 1 : 0);
+        // mixed precision: each bin's event function and -log P as FP32 pairs (gf_df), the low part of -log P as
+        // one more term after the others (an event adds it to the low part of its value sum)
+        const int64_t loOff = grad ? plan.ctab_lo_off_grad : plan.ctab_lo_off_nograd;
+        const bool dfTab    = tab && mixed && loOff >= 0 && dfEligible();
+        const int tabAll    = tabComps + (dfTab ? 1 : 0);
+        // the event function's value once more with R = gf_df: conv 0's value read as (high, low) pair
+        std::ostringstream bodyDF;
+        std::string pvDF;
+        if(dfTab) {
+            Ctx cd{bodyDF, T, false, true, nullptr, nullptr, nullptr, nullptr};
+            cd.lohi = true;
+            cd.x    = [&](int) -> std::string {
+                throw std::runtime_error("codegen: the tabulated event function reads an observable");
+            };
+            cd.k   = c.k;
+            cd.tab = [&](int ci, int comp) { return "gf_df(" + c.tab(ci, comp) + ", tlo0)"; };
+            const Val rd = emit(cd, 0);
+            pvDF         = factorRoot ? rd.v : normMul(cd, 0, rd.v);
+        }
         const int vw = mixed ? 4 : 2;
         std::vector<int> bw, boff; // per block: width (terms) and offset (elements) in ltab
         int LP = 0;
-        for(int q0 = 0; q0 < tabComps; q0 += vw) {
-            int w = std::min(vw, tabComps - q0);
+        for(int q0 = 0; q0 < tabAll; q0 += vw) {
+            int w = std::min(vw, tabAll - q0);
             if(w == 3)
                 w = 4;
             bw.push_back(w);
@@ -2760,6 +2947,10 @@ struct Gen {
         os << "  __syncthreads();\n";
         if(!batch) {
             os << "  const int toy = toy1;\n  const R *Pr = Pr1; (void)Pr;\n";
+            // one-launch evaluation: the status words, read before the tables (written before the grid barrier;
+            // a CTA stopped later leaves its rows unwritten, which the host detects)
+            if(asBody)
+                os << "  const int gf_st0 = tid == 0 ? (a.qflag[0] | (a.gbar[2] ? 8 : 0)) : 0;\n";
             if(!tab)
                 emitNormReads(os, T, grad, plan.nl, "  ");
             else {
@@ -2795,6 +2986,12 @@ struct Gen {
                 os << "#pragma unroll\n        for(int v = 0; v < " << nvr << "; ++v) tv[r][v] = *reinterpret_cast<const " << vt
                    << " *>(gt + kk * " << cp << " + " << per << " * v);\n";
                 os << "      }\n    }\n  }\n";
+                if(dfTab) {
+                    os << "  float tlo[" << NR << "];\n";
+                    os << "  {\n    const float *gl = reinterpret_cast<const float *>(a.ctab) + " << loOff << ";\n";
+                    os << "#pragma unroll\n    for(int r = 0; r < " << NR << "; ++r) {\n      const int kk = kr_lo + tid + r * "
+                       << block << ";\n      tlo[r] = kk <= kr_hi ? gl[kk] : 0.f;\n    }\n  }\n";
+                }
                 // the other normalisation factors as usual
                 {
                     std::ostringstream nr;
@@ -2846,12 +3043,24 @@ struct Gen {
                     os << "      ACC tt[" << comps << "];\n";
                     os << "#pragma unroll\n      for(int c = 0; c < " << comps << "; ++c) tt[c] = acc_shfl(tc, c);\n";
                     os << "      if(lane == 0) {\n";
-                    os << "      const double S = acc_value(tt[0]);\n";
-                    os << "      s_fbits = isnan(S) ? 1 : !(S > 0.0) ? 2 : 0;\n";
-                    os << "      const double I = " << lit(cc) << " * S;\n";
-                    os << "      const double Nd = 1.0 / I;\n";
-                    os << "      const R N = (R)Nd;\n";
-                    os << "      s_fn[0] = N;\n      s_fn[1] = (R)(Nd - (double)N);\n";
+                    if(mixed) {
+                        // N = 1 / (cc S) as an FP32 pair, from the pair S (no FP64 division on the critical path)
+                        const float cch = (float)cc, ccl = (float)(cc - (double)cch);
+                        char cb[96];
+                        std::snprintf(cb, sizeof cb, "gf_df(%.9ef, %.9ef)", (double)cch, (double)ccl);
+                        os << "      const gf_df Sd(tt[0].x, tt[0].y);\n";
+                        os << "      s_fbits = isnan(Sd.h) ? 1 : !(Sd.h > 0.f) ? 2 : 0;\n";
+                        os << "      const gf_df Nd = gf_df(1) / (Sd * " << cb << ");\n";
+                        os << "      const R N = Nd.h;\n";
+                        os << "      s_fn[0] = N;\n      s_fn[1] = Nd.l;\n";
+                    } else {
+                        os << "      const double S = acc_value(tt[0]);\n";
+                        os << "      s_fbits = isnan(S) ? 1 : !(S > 0.0) ? 2 : 0;\n";
+                        os << "      const double I = " << lit(cc) << " * S;\n";
+                        os << "      const double Nd = 1.0 / I;\n";
+                        os << "      const R N = (R)Nd;\n";
+                        os << "      s_fn[0] = N;\n      s_fn[1] = (R)(Nd - (double)N);\n";
+                    }
                     if(grad)
                         for(int j = 1; j < comps; ++j)
                             os << "      s_fn[" << 1 + j << "] = -N * N * (R)" << lit(cc) << " * (R)acc_r(tt[" << j << "]);\n";
@@ -2881,9 +3090,18 @@ struct Gen {
                 os << "      {\n" << body.str();
                 const std::string pvE = factorRoot ? root.v : normMul(c, 0, root.v);
                 os << "      const R pv = " << pvE << ";\n";
+                if(dfTab) {
+                    os << "      gf_df pvd;\n      {\n        typedef gf_df R;\n        const float tlo0 = tlo[r];\n";
+                    os << bodyDF.str();
+                    os << "        pvd = " << pvDF << ";\n      }\n";
+                }
                 os << "      R lt[" << LP << "];\n#pragma unroll\n      for(int q = 0; q < " << LP << "; ++q) lt[q] = R(0);\n";
                 os << "      if(pv > R(0)) {\n";
-                os << "        lt[0] = -GF_LOG(pv);\n";
+                if(dfTab)
+                    os << "        const gf_df ld = gf_df_log(pvd);\n        lt[0] = -ld.h;\n        lt[" << tabComps
+                       << "] = -ld.l;\n";
+                else
+                    os << "        lt[0] = -GF_LOG(pv);\n";
                 if(grad && T.NG > 0) {
                     os << "        const R inv = gf_rcp(pv);\n";
                     for(int sl = 0; sl < T.NG; ++sl) {
@@ -3109,9 +3327,36 @@ struct Gen {
         // tab: the iteration's events' terms are kept per component and summed pairwise after the loop
         // (exact for equal terms, as neighbouring events in bin order mostly are; three roundings otherwise)
         const int tabAcc = NGp + (factorRoot ? 1 : 0);
-        if(tab)
+        if(tab) {
+            // all events of the iteration in one bin (with the events sorted by bin, most iterations): one
+            // gather, and each sum is 8 x the term, which is what the pairwise sum of 8 equal terms gives
+            const ConvInfo &cv = T.convs[0];
+            const char *fld[] = {".x", ".y", ".z", ".w"};
+            auto compS = [&](int q) {
+                const int b = q / vw;
+                return "lq" + std::to_string(b) + (bw[b] == 1 ? std::string("") : std::string(fld[q % vw]));
+            };
+            os << "      const bool gsame = jn == " << VEC;
+            for(int j = 1; j < VEC; ++j)
+                os << " && ka0[" << j << "] == ka0[0]";
+            os << ";\n      if(gsame) {\n";
+            os << "        const int lk = ka0[0] - " << cv.kmin << ";\n";
+            for(size_t b = 0; b < bw.size(); ++b)
+                os << "        const " << vtype(bw[b]) << " lq" << b << " = *reinterpret_cast<const " << vtype(bw[b])
+                   << " *>(ltab + " << boff[b] << " + lk * " << bw[b] << ");\n";
+            os << "        av = R(" << VEC << ") * " << compS(0) << ";\n";
+            for(int sl = 0; sl < NGp - 1; ++sl)
+                os << "        ag" << sl << " = R(" << VEC << ") * " << compS(1 + sl) << ";\n";
+            if(factorRoot)
+                os << "        nv += R(" << VEC << ") * " << compS(tabComps - 1) << ";\n";
+            if(dfTab)
+                os << "        avl += R(" << VEC << ") * " << compS(tabComps) << ";\n";
+            os << "      } else {\n";
             for(int q = 0; q < tabAcc; ++q)
                 os << "      R tsum" << q << "[" << VEC << "];\n";
+        }
+        if(dfTab)
+            os << "      R tsumL[" << VEC << "];\n";
         os << "#pragma unroll\n      for(int j = 0; j < " << VEC << "; ++j) {\n";
         if(tab) {
             // gather the event's tabulated terms (16-byte and narrower shared loads) and add them
@@ -3132,6 +3377,8 @@ struct Gen {
                 os << "          tsum" << 1 + sl << "[j] = in ? " << comp(1 + sl) << " : R(0);\n";
             if(factorRoot)
                 os << "          tsum" << NGp << "[j] = in ? " << comp(tabComps - 1) << " : R(0);\n";
+            if(dfTab)
+                os << "          tsumL[j] = in ? " << comp(tabComps) << " : R(0);\n";
             os << "        }\n";
         } else {
         for(int o = 0; o < NO; ++o)
@@ -3297,10 +3544,13 @@ struct Gen {
             }
             if(tab) {
                 os << "      av = gf_tree8(tsum0);\n";
+                if(dfTab)
+                    os << "      avl += gf_tree8(tsumL);\n";
                 for(int sl = 0; sl < NGp - 1; ++sl)
                     os << "      ag" << sl << " = gf_tree8(tsum" << 1 + sl << ");\n";
                 if(factorRoot)
                     os << "      nv += gf_tree8(tsum" << NGp << ");\n";
+                os << "      }\n"; // the iteration's events in several bins
             }
             os << "      gf_comp_add(avh, avl, av);\n";
             // gradient sums are compensated where it is cheap (8 events per iteration) or many events per
@@ -3337,8 +3587,8 @@ struct Gen {
             const bool foldTab = tab && plan.conv_fold_q[0] >= 0;
             os << "    if(tid < " << NGc << ") { ACC t = acc_zero(); for(int w = 0; w < " << NW
                << "; ++w) t = acc_add(t, red[w][tid]); a.hpart[(i64)ch * " << NGc + 1 << " + tid] = acc_value(t); }\n";
-            os << "    if(tid == 0) a.hpart[(i64)ch * " << NGc + 1 << " + " << NGc << "] = (double)(a.qflag[toy]"
-               << (foldTab ? " | s_fbits" : "") << " | (a.gbar[2] ? 8 : 0));\n";
+            os << "    if(tid == 0) a.hpart[(i64)ch * " << NGc + 1 << " + " << NGc << "] = (double)(gf_st0"
+               << (foldTab ? " | s_fbits" : "") << ");\n";
             os << "    __syncthreads();\n";
             os << "  }\n}\n\n";
             endBody(asBody);
@@ -3412,7 +3662,16 @@ struct Gen {
         eventKernel(grad, false, true, tab);
         const size_t evtSmem = bodySmem;
         const int CB = plan.conv_blocks, MGB = plan.max_grid_blocks;
-        const int nConvV = NC > 0 ? CB * NC : 0, nGridV = hasGrid ? MGB * NQ : 0;
+        // grid virtual blocks: only the unfolded numeric nodes' blocks, one node after another (a folded node's
+        // block slots would only return, and could push a grid block onto a CTA that also builds a table)
+        std::vector<std::pair<int, int>> gridNodes; // (numeric node, blocks)
+        int nGridV = 0;
+        for(int q = 0; q < NQ && hasGrid; ++q)
+            if(!plan.num_folded[q] && plan.grid_blocks[q] > 0) {
+                gridNodes.push_back({q, plan.grid_blocks[q]});
+                nGridV += plan.grid_blocks[q];
+            }
+        const int nConvV = NC > 0 ? CB * NC : 0;
         os << "extern \"C\" __global__ void __launch_bounds__(" << block << ", 2) gf_fcn_" << sfx
            << "(const GfArgs a) {\n";
         os << "  const int toy = 0; (void)toy;\n";
@@ -3484,8 +3743,15 @@ struct Gen {
                    << "      const unsigned g = vb - " << nConvV << "u;\n";
             else
                 os << "    {\n      const unsigned g = vb;\n";
-            os << "      gf_grid_" << sfx << "_body(a, make_uint3(g % " << MGB << "u, 0u, g / " << MGB << "u), make_uint3("
-               << MGB << "u, 1u, " << NQ << "u), sPr);\n    }\n";
+            os << "      unsigned gb = g, gq = " << (gridNodes.empty() ? 0 : gridNodes[0].first) << "u;\n";
+            for(size_t i = 1; i < gridNodes.size(); ++i) {
+                int before = 0;
+                for(size_t j = 0; j < i; ++j)
+                    before += gridNodes[j].second;
+                os << "      if(g >= " << before << "u) { gb = g - " << before << "u; gq = " << gridNodes[i].first << "u; }\n";
+            }
+            os << "      gf_grid_" << sfx << "_body(a, make_uint3(gb, 0u, gq), make_uint3(" << MGB << "u, 1u, " << NQ
+               << "u), sPr);\n    }\n";
             os << "    __syncthreads();\n  }\n";
         };
         if(NC > 0 && hasGrid && !plan.grid_needs_conv)
@@ -3551,7 +3817,7 @@ KernelPlan generate_kernels(const Tree &t, bool mixed, int evt_block, bool batch
             g.os << kPreludeAmp4F;
     }
     if(mixed)
-        g.os << kPreludeF32;
+        g.os << kPreludeF32 << dfLogTable() << kPreludeDF;
     else
         g.os << kPreludeF64;
     for(int k = 0; k < t.n_amp_nodes(); ++k)

@@ -1210,10 +1210,13 @@ int updateAmpCaches(gf_engine *e) {
                 const float *eff   = k < (int)T.amp3s.size() ? reinterpret_cast<const float *>(sc + (size_t)nc * nst) : nullptr;
                 int herr           = 0;
                 r = cudaMemsetAsync(e->d_gtc_err, 0, sizeof(int), e->stream);
+                // GF_GRAM_TEST_STALL_STAGE (tests of the failure path): the wait for that stage runs out
+                const char *stall = std::getenv("GF_GRAM_TEST_STALL_STAGE");
                 if(r == cudaSuccess)
                     r = gf_gram_tc_launch(sc, npts, nst, nc, eff, std::max(1, e->sm_count), e->d_gtc_part,
                                           e->d_gtc_out, e->d_gtc_err, e->stream,
-                                          e->gram_w >= gf_gram_tc_width(nc) ? e->gram_w : 0);
+                                          e->gram_w >= gf_gram_tc_width(nc) ? e->gram_w : 0, e->gram_ns,
+                                          stall && *stall ? std::atoi(stall) : -1);
                 if(r == cudaSuccess)
                     r = cudaMemcpyAsync(e->h_gtc.data(), e->d_gtc_out, sizeof(double) * (size_t)m * m,
                                         cudaMemcpyDeviceToHost, e->stream);
@@ -2300,6 +2303,13 @@ int gf_set_wait_limit(gf_engine *e, uint64_t ns) {
     if(!e)
         return gf_fail(nullptr, GF_ERR_INVALID, "null engine");
     e->bar_ns = ns ? ns : 1000000000ull;
+    return GF_OK;
+}
+
+int gf_set_gram_wait_limit(gf_engine *e, uint64_t ns) {
+    if(!e)
+        return gf_fail(nullptr, GF_ERR_INVALID, "null engine");
+    e->gram_ns = ns;
     return GF_OK;
 }
 

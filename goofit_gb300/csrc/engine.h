@@ -191,6 +191,7 @@ struct gf_engine {
     int fcn_grid          = 0;
     unsigned *d_gbar      = nullptr;
     unsigned long long bar_ns = 1000000000ull;
+    unsigned long long gram_ns = 0; // per-stage wait limit of the tensor-core Gram kernel (0: its 2 s default)
     unsigned bar_epoch        = 0; // one-launch evaluations run since the barrier words were cleared
     bool fused_graph_ok   = true; // false: the cooperative launch is not captured into a graph here
     // captured one-launch graphs [nograd, grad]: the source graph, its kernel node and that node's launch
@@ -213,8 +214,11 @@ size_t gf_gram_tc_part_doubles(int ncol, int grid);
 // G (2 ncol x 2 ncol, FP64) = sum_{p < npts} x_r(p) eff(p) x_s(p) of the columns sc[c * nst + p] (nst a
 // multiple of 4, sc and eff 16-byte aligned) into out; part holds gf_gram_tc_part_doubles(ncol, sm_count)
 // doubles; *err gets bit 0 when a bounded wait ran out; width: real columns per slice (16, 32 or 64, at least
-// gf_gram_tc_width(ncol)), 0 for the narrowest
+// gf_gram_tc_width(ncol)), 0 for the narrowest; wait_ns: the limit of each per-stage mbarrier wait (0: 2 s; the
+// wait for the last committed MMAs before the tensor memory is freed is always 2 s); stall >= 0: a test of the
+// failure path, in which the wait for stage `stall` also waits on a barrier that never completes
 cudaError_t gf_gram_tc_launch(const float2 *sc, long long npts, long long nst, int ncol, const float *eff,
-                              int sm_count, double *part, double *out, int *err, cudaStream_t s, int width = 0);
+                              int sm_count, double *part, double *out, int *err, cudaStream_t s, int width = 0,
+                              unsigned long long wait_ns = 0, int stall = -1);
 int gf_cuda_check(gf_engine *e, cudaError_t r, const char *what);
 int gf_run(gf_engine *e, bool grad, int metric_values_toy, int metric);

@@ -21,11 +21,10 @@
 // cross terms hi.lo + lo.hi, 2^-11 smaller, accumulate in a third accumulator over the CTA's points.  The
 // CTAs' partials are summed in FP64 by gf_gram_tc_sum.
 //
-// Pipeline per CTA (256 threads, one elected thread issues the MMAs): cp.async 16-byte copies fill a
-// three-slot ring of raw (unsplit) stages two stages ahead; the threads split the oldest raw stage and
-// store it into one of two operand stages in the canonical no-swizzle K-major layout while the tensor
-// core works on the other; tcgen05.commit arrives on the operand stage's mbarrier when its MMAs have
-// read it.  Every wait is bounded: a wait that runs out sets *err and the CTA stops issuing work,
+// Pipeline per CTA (512 threads for 16-column slices, else 256; one elected thread issues the MMAs): cp.async
+// 16-byte copies fill a three-slot ring of raw (unsplit) stages two stages ahead; the threads split the oldest raw
+// stage and store it into one of two operand stages in the canonical no-swizzle K-major layout while the tensor
+// core works on the other; tcgen05.commit arrives on the operand stage's mbarrier when its MMAs have read it.  Every wait is bounded: a wait that runs out sets *err and the CTA stops issuing work,
 // waits (bounded) for what it issued, frees its tensor memory and returns.
 #include <cuda_runtime.h>
 
@@ -35,7 +34,12 @@
 
 namespace {
 
-constexpr int kThreads = 256; // eight warps; warps 0-3 read tensor-memory lanes 32w .. 32w + 31 (D rows)
+// Threads per CTA: warps 0-3 read tensor-memory lanes 32w .. 32w + 31 (the D rows); all warps copy and split the
+// stages.  W = 16 (2 W compensated registers per drain thread) takes 16 warps, which halves each stage's copy and
+// split work per warp and gives the single CTA per SM more warps to cover latencies; wider slices keep 8 warps
+// (their drain registers do not fit the 128 per thread of a 512-thread CTA).
+template <int W>
+__host__ __device__ constexpr int threadsFor() { return W == 16 ? 512 : 256; }
 constexpr int kRows    = 128; // MMA M = N = 128 rows: S slices x W real columns
 constexpr int kKS      = 32;  // points of one slice per stage: four MMA K-steps of 8 (kind::tf32)
 constexpr int kOpBytes = kRows * kKS * 4;   // one operand split of one stage: 16 KB
@@ -50,7 +54,9 @@ constexpr int kRawRow        = kKS * 8 + 16;      // one (slice, column) row of 
 constexpr int kRawCplx       = 64 * kRawRow;      // at most S x C = 64 rows
 constexpr int kRawSlot       = kRawCplx + 8 * kKS * 4; // + the efficiency of S <= 8 slices
 constexpr int kSmemBytes     = kOperandBytes + kRawSlots * kRawSlot;
-constexpr unsigned long long kWaitNs = 2000000000ull; // 2 s: an mbarrier wait that takes longer fails
+// 2 s: the default limit of a per-stage mbarrier wait, and always the limit of the wait for the last committed
+// MMAs before the tensor memory is freed (that wait must not give up while MMAs may still write it)
+constexpr unsigned long long kWaitNs = 2000000000ull;
 
 // Instruction descriptor of tcgen05.mma kind::tf32: D F32 (bits 4-5 = 1), A and B TF32 (bits 7-9 and
 // 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22, M >> 4 in bits 24-28.
@@ -92,20 +98,23 @@ __device__ __forceinline__ void mbar_init(uint32_t addr, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
 }
 
-// Waits until phase `parity` of the mbarrier has completed; false after kWaitNs.
-__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+// Waits until phase `parity` of the mbarrier has completed; false after `limit` ns of the global timer.  Each
+// try_wait suspends the thread for at most min(limit, 1 ms) (its suspend-time hint), so that a short limit is
+// checked within about that time instead of the hardware's own suspension limit.
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity, unsigned long long limit) {
     const unsigned long long t0 = globaltimer();
+    const uint32_t hint         = limit < 1000000ull ? (uint32_t)limit : 1000000u;
     while(true) {
         uint32_t done;
         asm volatile("{\n\t.reg .pred p;\n\t"
-                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
                      "selp.u32 %0, 1, 0, p;\n\t}\n"
                      : "=r"(done)
-                     : "r"(addr), "r"(parity)
+                     : "r"(addr), "r"(parity), "r"(hint)
                      : "memory");
         if(done)
             return true;
-        if(globaltimer() - t0 > kWaitNs)
+        if(globaltimer() - t0 > limit)
             return false;
     }
 }
@@ -161,13 +170,16 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
 // W real columns per slice (2C <= W), S = 128 / W slices.  eff != nullptr: the efficiency multiplies B.
 // Columns sc[c * nst + p], nst a multiple of 4; sc and eff 16-byte aligned.
 template <int W>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(threadsFor<W>(), 1)
     gf_gram_tc(const float2 *__restrict__ sc, long long npts, long long nst, int ncol, const float *__restrict__ eff,
-               long long per_cta, double *__restrict__ part, int *__restrict__ err) {
+               long long per_cta, double *__restrict__ part, int *__restrict__ err, unsigned long long wait_ns,
+               int stall) {
     constexpr int S  = kRows / W;
+    constexpr int kThreads = threadsFor<W>();
     constexpr int KC = kKS / 4; // 16-byte chunks of 4 points per row and stage
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) unsigned long long mbar[2];
+    __shared__ __align__(8) unsigned long long mbar_never; // no thread or copy ever arrives on it
     __shared__ uint32_t tmem_slot;
     __shared__ int s_fail;
 
@@ -184,6 +196,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if(tid == 0) {
         mbar_init(smem_u32(&mbar[0]), 1);
         mbar_init(smem_u32(&mbar[1]), 1);
+        mbar_init(smem_u32(&mbar_never), 1);
         s_fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -232,8 +245,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
     };
     // waits for stage u's MMAs (and so for every earlier one); false on every thread if any wait ran out
+    // stall = u (a test of the failure path, -1 otherwise): stage u's wait also waits for a barrier that never
+    // completes, so that it runs out after wait_ns while the stage's MMAs complete normally
     auto stage_done = [&](int u) -> bool {
-        const bool ok = mbar_wait(smem_u32(&mbar[u & 1]), (uint32_t)((u >> 1) & 1));
+        bool ok = mbar_wait(smem_u32(&mbar[u & 1]), (uint32_t)((u >> 1) & 1), wait_ns);
+        if(u == stall)
+            ok = ok && mbar_wait(smem_u32(&mbar_never), 0u, wait_ns);
         return !__syncthreads_or(!ok);
     };
 
@@ -280,7 +297,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             cp_async_commit();
         cp_async_wait<kRawSlots - 1>();
         // the MMAs of stage t - 2 have read this operand buffer (waited for already by the drain of t - 1)
-        if(t >= 2 && !mbar_wait(smem_u32(&mbar[buf]), (uint32_t)(((t - 2) >> 1) & 1)))
+        if(t >= 2 && !mbar_wait(smem_u32(&mbar[buf]), (uint32_t)(((t - 2) >> 1) & 1), wait_ns))
             s_fail = 1;
         __syncthreads();
         // one task = one real row x 4 points: 8 consecutive lanes write the 8 rows of one core matrix
@@ -363,7 +380,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             atomicOr(err, 1);
         // wait (bounded) for the last committed stage before the tensor memory goes away
         if(issued_last >= 0)
-            mbar_wait(smem_u32(&mbar[issued_last & 1]), (uint32_t)((issued_last >> 1) & 1));
+            mbar_wait(smem_u32(&mbar[issued_last & 1]), (uint32_t)((issued_last >> 1) & 1), kWaitNs);
     }
     tc_fence_before();
     __syncthreads();
@@ -412,13 +429,13 @@ __global__ void __launch_bounds__(128) gf_gram_tc_sum(const double *__restrict__
 
 template <int W>
 cudaError_t launchW(const float2 *sc, long long npts, long long nst, int ncol, const float *eff, int grid,
-                    long long per_cta, double *part, int *err, cudaStream_t s) {
+                    long long per_cta, double *part, int *err, unsigned long long wait_ns, int stall, cudaStream_t s) {
     // per launch: the attribute belongs to the current device, and the kernel runs once per cache rebuild
     cudaError_t r = cudaFuncSetAttribute(gf_gram_tc<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
     if(r != cudaSuccess)
         return r;
     // every launch requests the full size: one CTA per SM, so the 512-column allocation never waits
-    gf_gram_tc<W><<<grid, kThreads, kSmemBytes, s>>>(sc, npts, nst, ncol, eff, per_cta, part, err);
+    gf_gram_tc<W><<<grid, threadsFor<W>(), kSmemBytes, s>>>(sc, npts, nst, ncol, eff, per_cta, part, err, wait_ns, stall);
     return cudaGetLastError();
 }
 
@@ -432,7 +449,10 @@ int gf_gram_tc_width(int ncol) {
 size_t gf_gram_tc_part_doubles(int ncol, int grid) { return (size_t)grid * 4 * ncol * ncol; }
 
 cudaError_t gf_gram_tc_launch(const float2 *sc, long long npts, long long nst, int ncol, const float *eff,
-                              int sm_count, double *part, double *out, int *err, cudaStream_t s, int width) {
+                              int sm_count, double *part, double *out, int *err, cudaStream_t s, int width,
+                              unsigned long long wait_ns, int stall) {
+    if(wait_ns == 0)
+        wait_ns = kWaitNs;
     const int Wmin = gf_gram_tc_width(ncol);
     const int W    = width == 0 ? Wmin : width;
     if(Wmin == 0 || W < Wmin || (W != 16 && W != 32 && W != 64) || ncol < 1 || npts <= 0 || nst < npts ||
@@ -445,9 +465,9 @@ cudaError_t gf_gram_tc_launch(const float2 *sc, long long npts, long long nst, i
     const int grid       = (int)((npts + per_cta - 1) / per_cta);
     static_assert((size_t)kRows * 64 * 8 <= (size_t)kOperandBytes, "slice reduction does not fit");
     static_assert(kSmemBytes <= 227 * 1024, "shared memory");
-    cudaError_t r = W == 16   ? launchW<16>(sc, npts, nst, ncol, eff, grid, per_cta, part, err, s)
-                    : W == 32 ? launchW<32>(sc, npts, nst, ncol, eff, grid, per_cta, part, err, s)
-                              : launchW<64>(sc, npts, nst, ncol, eff, grid, per_cta, part, err, s);
+    cudaError_t r = W == 16   ? launchW<16>(sc, npts, nst, ncol, eff, grid, per_cta, part, err, wait_ns, stall, s)
+                    : W == 32 ? launchW<32>(sc, npts, nst, ncol, eff, grid, per_cta, part, err, wait_ns, stall, s)
+                              : launchW<64>(sc, npts, nst, ncol, eff, grid, per_cta, part, err, wait_ns, stall, s);
     if(r != cudaSuccess)
         return r;
     const int nent = 4 * ncol * ncol;

@@ -204,6 +204,9 @@ struct KernelPlan {
     bool grid_needs_conv = false; // an unfolded numeric node reads a convolution table
     int64_t ctab_per_toy_grad = 0, ctab_per_toy_nograd = 0; // table elements per toy
     std::vector<int64_t> ctab_off_grad, ctab_off_nograd;    // per conv
+    // mixed precision, one toy: the low parts of conv 0's values (the table's value column holds the high parts
+    // of unevaluated FP32 pairs), at this element offset of the toy's table block; -1 when not kept
+    int64_t ctab_lo_off_grad = -1, ctab_lo_off_nograd = -1;
     std::vector<int> ctab_cp_grad, ctab_cp_nograd;          // per conv: padded components per table row
     std::vector<int> obs_used_evt;                          // observables the event kernel loads
     // Amp3Body integrals: pairs (i <= j) of each node split into tiles; one CTA row per tile

@@ -234,6 +234,10 @@ class Engine:
         """Longest device-side wait at the one-launch evaluation's grid barrier (ns; 0: the default 1 s)."""
         self._check(self._L.gf_set_wait_limit(self._h, int(ns)))
 
+    def set_gram_wait_limit(self, ns: int) -> None:
+        """Longest wait of each pipeline stage of the tensor-core Gram kernel (ns; 0: the default 2 s)."""
+        self._check(self._L.gf_set_gram_wait_limit(self._h, int(ns)))
+
     def set_amp_mode(self, mode: str, budget_bytes: int = 0) -> None:
         """Amplitude derivatives 'store'd per event and normalisation point, 'recompute'd where they are used,
         or 'auto' (recompute when storing would take more than budget_bytes; 0: a quarter of the free device

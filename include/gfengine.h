@@ -205,6 +205,13 @@ int64_t gf_event_chunk(const gf_engine *eng);
  * A wait that runs out stops the launch, the call returns GF_ERR_TIMEOUT and the engine stays usable.
  * No counterpart in the reference (its Thrust reductions have no device-side waits). */
 int gf_set_wait_limit(gf_engine *eng, uint64_t ns);
+/* Longest wait, in nanoseconds of the GPU's global timer, of each pipeline-stage mbarrier wait of the mixed
+ * engine's tensor-core Gram kernel (the normalisation integrals of Amp3Body / Amp4Body); ns = 0 restores the
+ * default of 2 s.  The kernel's wait for its last committed MMAs before it frees its tensor memory always keeps
+ * the 2 s limit.  A wait that runs out makes the integral rebuild return GF_ERR_CUDA; the engine stays usable
+ * and rebuilds the integrals at the next evaluation.  No counterpart in the reference (its integrals are
+ * Thrust reductions, src/PDFs/physics/detail/SpecialResonanceIntegrator.cu:52-121, without device-side waits). */
+int gf_set_gram_wait_limit(gf_engine *eng, uint64_t ns);
 
 /* Where the derivatives of the amplitudes by floated resonance / line-shape parameters live (Amp3Body, Amp4Body).
    GF_AMP_STORE: per-event columns and per-normalisation-point scratch columns, as the reference caches its

@@ -197,3 +197,31 @@ def test_tensor_core_gram_matches_cuda_core_gram(c3_events, bins, monkeypatch):
     scale = np.abs(np.diag(out["cuda"])).max()
     assert np.abs(out["tc"] - out["cuda"]).max() / scale < 2e-6
     np.testing.assert_array_equal(out["tc"], out["tc"].conj().T)
+
+
+def test_gram_stage_wait_that_runs_out_is_reported_and_recovered(c3_events, monkeypatch):
+    """A per-stage mbarrier wait of the tensor-core Gram kernel that runs out ends the integral rebuild with
+    GF_ERR_CUDA and leaves the engine usable.  The wait is made to run out without any fault: the test hook
+    GF_GRAM_TEST_STALL_STAGE=0 makes stage 0's wait also wait for a barrier on which nothing ever arrives, under
+    a 1 ms limit, while the stage's MMAs complete normally.  The kernel then waits, with its fixed 2 s limit, for
+    its last committed MMAs before it frees its tensor memory.  Without the hook and at the default limit, the
+    next evaluation's integrals (within 2e-5 of the largest diagonal entry) and NLL (1e-6 relative) match the
+    oracle."""
+    pdf, _, _ = W.c3_model(300)
+    nodes, olist, params, mask, pv = tree(pdf)
+    eng = gf.Engine("mixed")
+    eng.set_tree(nodes, olist, len(params), mask)
+    eng.upload(c3_events)
+    monkeypatch.setenv("GF_GRAM_TEST_STALL_STAGE", "0")
+    eng.set_gram_wait_limit(1_000_000)
+    for _ in range(2):
+        with pytest.raises(A.EngineError) as ei:
+            eng.nll(pv)
+        assert ei.value.code == A.GF_ERR_CUDA
+    monkeypatch.delenv("GF_GRAM_TEST_STALL_STAGE")
+    eng.set_gram_wait_limit(0)
+    nll = eng.nll(pv)
+    assert nll == pytest.approx(O.nll(nodes, olist, pv, c3_events), rel=NLL_RTOL["mixed"])
+    got = eng.amp3_integrals(0, 8)
+    ref = O.amp3_integrals(nodes, olist, pv, 0, 8)
+    assert np.abs(got - ref).max() / np.abs(np.diag(ref)).max() < AMP_RTOL["mixed"]

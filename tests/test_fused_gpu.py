@@ -95,3 +95,44 @@ def test_barrier_wait_that_runs_out_is_reported_and_recovered(monkeypatch):
         assert got == pytest.approx(ref, rel=1e-6)
         assert eng.nll(pv) == pytest.approx(ref, rel=1e-6)
     eng.close()
+
+
+def test_tabulated_terms_in_pairs_track_the_oracle(monkeypatch):
+    """Mixed precision, tabulated event pass: every bin's event function and -log P are FP32 pairs, so that a
+    bin's rounding is not repeated by each of its events.  At 2e6 events the NLL then matches the oracle,
+    evaluated at the FP32-rounded parameters the kernels see, within 2e-10 relative over a scan of alpha and
+    mu (a single-precision term per bin left it 5e-9 away, in steps as the parameters moved)."""
+    eng, wl, nodes, olist, params, mask, pv = c2_engine(2_000_000, 34, "mixed", monkeypatch)
+    data = wl.data.to_numpy()
+    names = [v.name for v in params]
+    for shift in np.linspace(-0.02, 0.02, 5):
+        p = pv.copy()
+        p[names.index("alpha")] += shift
+        p[names.index("mu")] -= shift / 2
+        p32 = p.astype(np.float32).astype(np.float64)
+        got = eng.nll(p)
+        assert got == pytest.approx(O.nll(nodes, olist, p32, data), rel=2e-10), shift
+    eng.close()
+
+
+@pytest.mark.parametrize("seed", [3, 5, 6])
+def test_mixed_fit_converges_as_the_fp64_fit(seed, monkeypatch):
+    """MIGRAD with the analytic gradient on the 2e6-event composite model: the mixed-precision fit takes at
+    most two more FCN calls than the FP64 fit and reaches its minimum within 1e-9 relative and 0.01 sigma
+    (datasets on which single-precision per-bin terms made the mixed fit take 300-700 calls)."""
+    monkeypatch.setenv("GF_FUSED", "1")
+    wl = W.make_c2(2_000_000, seed=seed)
+    nodes, params, obs = wl.pdf._flatten()
+    free = [i for i, v in enumerate(params) if not v.fixed]
+    out = {}
+    for prec in ("mixed", "fp64"):
+        wl.reset()
+        fm = gf.FitManager(wl.pdf, precision=prec, gradient="analytic", tolerance=0.01)
+        fm.verbosity = 0
+        r = fm.fit()
+        assert r.valid
+        out[prec] = (r.nfcn, r.fmin, [params[i].value for i in free], [params[i].error for i in free])
+    (nm, fm_, vm, _), (nf, ff, vf, ef) = out["mixed"], out["fp64"]
+    assert nm <= nf + 2, (nm, nf)
+    assert fm_ == pytest.approx(ff, rel=1e-9)
+    assert max(abs(a - b) / e for a, b, e in zip(vm, vf, ef)) < 0.01
