@@ -60,6 +60,7 @@ struct Ctx {
     std::function<std::string(int, int)> amp; // amplitude node, amplitude -> R2 amplitude expression
     std::function<std::string(int)> ampcol;   // amplitude / derivative column -> R2 expression
     bool lohi = false;                        // normalisation factors as FP32 hi + lo pairs
+    bool single = false;                      // R is FP32 (mixed engine): divisions by parameters become products
     // the root, when it is an amplitude PDF: |T|^2 = tr^2 + ti^2 and, per gradient slot, the inner term
     // d|T|^2/dp / 2 (its gradient divided by the value needs no efficiency)
     bool ampRoot = false;
@@ -182,11 +183,24 @@ Val emit(Ctx &c, int i) {
         std::string x = c.x(n.obs[0]), d = c.tmp("d"), s = c.tmp("s"), v = c.tmp("v");
         os << "    const R " << d << " = " << x << " - " << P(n.params[0]) << ";\n";
         os << "    const R " << s << " = " << P(n.params[1]) << ";\n";
-        os << "    const R " << v << " = GF_EXP(R(-0.5) * " << d << " * " << d << " / (" << s << " * " << s
-           << "));\n";
-        out.v = v;
-        gadd(c, out, slot(c, n.params[0]), v + " * " + d + " / (" + s + " * " + s + ")");
-        gadd(c, out, slot(c, n.params[1]), v + " * " + d + " * " + d + " / (" + s + " * " + s + " * " + s + ")");
+        if(c.single) {
+            // single precision: the reciprocals of sigma^2 and sigma^3 depend on the parameter only, so that a
+            // loop over bins or events hoists them and multiplies (three IEEE divisions per value made the
+            // convolution's resolution staging the longest step of a one-launch FCN)
+            const std::string iq = c.tmp("iq"), iqs = c.tmp("iqs");
+            os << "    const R " << iq << " = R(1) / (" << s << " * " << s << ");\n";
+            os << "    const R " << iqs << " = " << iq << " / " << s << ";\n";
+            os << "    const R " << v << " = GF_EXP(R(-0.5) * " << d << " * " << d << " * " << iq << ");\n";
+            out.v = v;
+            gadd(c, out, slot(c, n.params[0]), v + " * " + d + " * " + iq);
+            gadd(c, out, slot(c, n.params[1]), v + " * " + d + " * " + d + " * " + iqs);
+        } else {
+            os << "    const R " << v << " = GF_EXP(R(-0.5) * " << d << " * " << d << " / (" << s << " * " << s
+               << "));\n";
+            out.v = v;
+            gadd(c, out, slot(c, n.params[0]), v + " * " + d + " / (" + s + " * " + s + ")");
+            gadd(c, out, slot(c, n.params[1]), v + " * " + d + " * " + d + " / (" + s + " * " + s + " * " + s + ")");
+        }
         break;
     }
     case GF_OP_POLYNOMIAL:
@@ -1923,6 +1937,7 @@ struct Gen {
                        << "      const R wx = (R)GF_CENTRE(" << lit(cv.ic[3]) << ", " << lit(wR) << ", r);\n";
                 std::ostringstream body;
                 Ctx c{body, T, grad, false, nullptr, nullptr, nullptr, nullptr};
+                c.single = mixed;
                 c.x   = [&](int) { return std::string("wx"); };
                 c.k   = [&](int) -> std::string { throw std::runtime_error("codegen: conv in workspace"); };
                 c.tab = [&](int, int) -> std::string { throw std::runtime_error("codegen: conv in workspace"); };
@@ -2194,6 +2209,7 @@ struct Gen {
             }
             std::ostringstream body;
             Ctx c{body, T, grad, false, nullptr, nullptr, nullptr, nullptr};
+            c.single = mixed;
             c.x = [&](int o) { return "gx" + std::to_string(o); };
             c.k = [&](int ci) -> std::string {
                 for(size_t j = 0; j < g.convs.size(); ++j)
@@ -2558,6 +2574,7 @@ struct Gen {
         o << "      gf_ampv_" << k << "(c12, c13, P, A, dA);\n";
         std::ostringstream body;
         Ctx c{body, T, false, false, nullptr, nullptr, nullptr, nullptr};
+        c.single = mixed;
         c.x = [&](int ob) -> std::string {
             if(ob == A.o12)
                 return "((R)c12)";
@@ -2784,6 +2801,7 @@ struct Gen {
         std::vector<int> xused(NO, 0);
         std::ostringstream body;
         Ctx c{body, T, grad, true, nullptr, nullptr, nullptr, &xused};
+        c.single = mixed;
         c.lohi = mixed;
         c.x    = [&](int o) {
             xused[o] = 1;
@@ -2859,6 +2877,7 @@ struct Gen {
         if(dfTab) {
             Ctx cd{bodyDF, T, false, true, nullptr, nullptr, nullptr, nullptr};
             cd.lohi = true;
+            cd.single = true;
             cd.x    = [&](int) -> std::string {
                 throw std::runtime_error("codegen: the tabulated event function reads an observable");
             };

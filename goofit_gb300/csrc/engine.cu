@@ -116,27 +116,49 @@ __global__ void gf_khist(const int *__restrict__ k, long long n, int kmin, int n
                 atomicAdd(&hist[i], sh[i]);
 }
 
-// offs[0..nK]: prefix sums of the histogram; positions past n (padding) take the first bin
-__global__ void gf_kfill(const long long *__restrict__ offs, int nK, int kmin, long long n, long long npad,
-                         int *__restrict__ out) {
-    for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < npad; i += (long long)gridDim.x * blockDim.x) {
-        int b = 0;
-        if(i < n) {
-            int lo = 0, hi = nK - 1; // the last b with offs[b] <= i
-            while(lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if(offs[mid] <= i)
-                    lo = mid;
-                else
-                    hi = mid - 1;
-            }
-            b = lo;
-        }
-        out[i] = kmin + b;
+// offs[0..nK]: exclusive prefix sums of the histogram (one CTA of 1024 threads: each sums a contiguous run of
+// bins, a scan over the 1024 run totals, then each writes its run's offsets)
+__global__ void __launch_bounds__(1024) gf_kscan(const unsigned *__restrict__ hist, int nK, long long *__restrict__ offs) {
+    __shared__ long long part[1024];
+    const int tid = threadIdx.x, per = (nK + 1023) / 1024;
+    const int b0 = min(nK, tid * per), b1 = min(nK, b0 + per);
+    long long s = 0;
+    for(int b = b0; b < b1; ++b)
+        s += hist[b];
+    part[tid] = s;
+    __syncthreads();
+    for(int o = 1; o < 1024; o <<= 1) {
+        const long long v = tid >= o ? part[tid - o] : 0;
+        __syncthreads();
+        part[tid] += v;
+        __syncthreads();
     }
+    long long run = tid > 0 ? part[tid - 1] : 0;
+    for(int b = b0; b < b1; ++b) {
+        offs[b] = run;
+        run += hist[b];
+    }
+    if(tid == 1023)
+        offs[nK] = part[1023];
 }
 
-// Sorted copy of toy 0's offsets of convolution 0 (allocated on first use, rebuilt after every upload).
+// block b writes bin b's run [offs[b], offs[b + 1]) of the sorted column (coalesced stores, no search); the
+// last block also fills everything after the last run, the padding up to npad, with the first bin (the runs end
+// at n: the upload rejects offsets outside the table)
+__global__ void gf_kfill(const long long *__restrict__ offs, int nK, int kmin, long long npad, int *__restrict__ out) {
+    const int b = blockIdx.x;
+    if(b < nK)
+        for(long long i = offs[b] + threadIdx.x; i < offs[b + 1]; i += blockDim.x)
+            out[i] = kmin + b;
+    if(b == nK - 1)
+        for(long long i = offs[nK] + threadIdx.x; i < npad; i += blockDim.x)
+            out[i] = kmin;
+}
+
+// Sorted copy of toy 0's offsets of convolution 0: histogram, prefix sums and fill, all on the device and
+// asynchronous on the engine's stream (the upload's own range check has already rejected offsets outside the
+// table); the sorted column and the histogram scratch are allocated on first use and kept across uploads of
+// the same size.
 int buildKSort(gf_engine *e) {
     GfToy &ty = e->toys[0];
     if(!ty.loaded || e->tree.convs.empty())
@@ -146,43 +168,29 @@ int buildKSort(gf_engine *e) {
     cudaError_t r          = cudaSuccess;
     if(!ty.ksort)
         r = cudaMalloc((void **)&ty.ksort, sizeof(int) * (size_t)std::max<int64_t>(8, ty.npad));
-    unsigned *hist = nullptr;
-    long long *offs = nullptr;
-    if(r == cudaSuccess)
-        r = cudaMalloc((void **)&hist, sizeof(unsigned) * nK);
-    if(r == cudaSuccess)
-        r = cudaMalloc((void **)&offs, sizeof(long long) * (nK + 1));
-    std::vector<unsigned> h(nK);
-    std::vector<long long> o(nK + 1, 0);
+    if(r == cudaSuccess && ty.khist_n < nK) {
+        if(ty.khist)
+            cudaFree(ty.khist);
+        if(ty.koffs)
+            cudaFree(ty.koffs);
+        ty.khist   = nullptr;
+        ty.koffs   = nullptr;
+        ty.khist_n = 0;
+        r          = cudaMalloc((void **)&ty.khist, sizeof(unsigned) * nK);
+        if(r == cudaSuccess)
+            r = cudaMalloc((void **)&ty.koffs, sizeof(long long) * (nK + 1));
+        if(r == cudaSuccess)
+            ty.khist_n = nK;
+    }
     const int grid = std::max(1, e->sm_count) * 2;
     if(r == cudaSuccess)
-        r = cudaMemsetAsync(hist, 0, sizeof(unsigned) * nK, e->stream);
+        r = cudaMemsetAsync(ty.khist, 0, sizeof(unsigned) * nK, e->stream);
     if(r == cudaSuccess) {
-        gf_khist<<<grid, 256, nK <= 8192 ? sizeof(unsigned) * nK : 0, e->stream>>>(ty.kcols[0], ty.n, cv.kmin, nK, hist);
+        gf_khist<<<grid, 256, nK <= 8192 ? sizeof(unsigned) * nK : 0, e->stream>>>(ty.kcols[0], ty.n, cv.kmin, nK, ty.khist);
+        gf_kscan<<<1, 1024, 0, e->stream>>>(ty.khist, nK, ty.koffs);
+        gf_kfill<<<nK, 256, 0, e->stream>>>(ty.koffs, nK, cv.kmin, ty.npad, ty.ksort);
         r = cudaGetLastError();
     }
-    if(r == cudaSuccess)
-        r = cudaMemcpyAsync(h.data(), hist, sizeof(unsigned) * nK, cudaMemcpyDeviceToHost, e->stream);
-    if(r == cudaSuccess)
-        r = cudaStreamSynchronize(e->stream);
-    if(r == cudaSuccess) {
-        for(int b = 0; b < nK; ++b)
-            o[b + 1] = o[b] + h[b];
-        if(o[nK] != ty.n)
-            r = cudaErrorInvalidValue; // an offset outside the table (rejected at upload already)
-    }
-    if(r == cudaSuccess)
-        r = cudaMemcpyAsync(offs, o.data(), sizeof(long long) * (nK + 1), cudaMemcpyHostToDevice, e->stream);
-    if(r == cudaSuccess) {
-        gf_kfill<<<grid, 256, 0, e->stream>>>(offs, nK, cv.kmin, ty.n, ty.npad, ty.ksort);
-        r = cudaGetLastError();
-    }
-    if(r == cudaSuccess)
-        r = cudaStreamSynchronize(e->stream);
-    if(hist)
-        cudaFree(hist);
-    if(offs)
-        cudaFree(offs);
     if(r != cudaSuccess)
         return gf_cuda_check(e, r, "sorting the bin offsets");
     ty.ksort_valid = true;
@@ -200,7 +208,14 @@ void freeToy(GfToy &t) {
         t.kcols[c] = nullptr;
     if(t.ksort)
         cudaFree(t.ksort);
+    if(t.khist)
+        cudaFree(t.khist);
+    if(t.koffs)
+        cudaFree(t.koffs);
     t.ksort       = nullptr;
+    t.khist       = nullptr;
+    t.koffs       = nullptr;
+    t.khist_n     = 0;
     t.ksort_valid = false;
     if(t.abase)
         cudaFree(t.abase);
@@ -862,7 +877,8 @@ double ampIntegral(const gf_engine *e, int t, int node, const double *P, const g
     const gf::TNode &nd = T.nodes[node];
     const int ai        = T.amp_index(node);
     const int n         = T.amp_count(ai);
-    if((int)e->toys[t].amp_I.size() <= ai) { // integrals not built yet for this toy
+    // integrals not built yet for this toy, or their last rebuild failed (the rebuild empties them first)
+    if((int)e->toys[t].amp_I.size() <= ai || e->toys[t].amp_I[ai].empty()) {
         for(size_t k = 0; k < an.dN.size() && k < 64; ++k)
             dQ[k] = 0;
         return NAN;
@@ -878,7 +894,8 @@ double ampIntegral(const gf_engine *e, int t, int node, const double *P, const g
         }
     }
     const auto &theta = T.amp_theta(ai);
-    const std::vector<double> &H = e->toys[t].amp_H.size() > (size_t)ai ? e->toys[t].amp_H[ai] : I;
+    const std::vector<double> &H =
+        e->toys[t].amp_H.size() > (size_t)ai && !e->toys[t].amp_H[ai].empty() ? e->toys[t].amp_H[ai] : I;
     for(size_t k = 0; k < an.dN.size() && k < 64; ++k) {
         const int p = T.gparam[an.dN[k].first];
         // a resonance / line-shape parameter: dQ = 2 Re sum_{a dep} sum_b c_a conj(c_b) H_ab

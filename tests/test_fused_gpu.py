@@ -99,9 +99,11 @@ def test_barrier_wait_that_runs_out_is_reported_and_recovered(monkeypatch):
 
 def test_tabulated_terms_in_pairs_track_the_oracle(monkeypatch):
     """Mixed precision, tabulated event pass: every bin's event function and -log P are FP32 pairs, so that a
-    bin's rounding is not repeated by each of its events.  At 2e6 events the NLL then matches the oracle,
-    evaluated at the FP32-rounded parameters the kernels see, within 2e-10 relative over a scan of alpha and
-    mu (a single-precision term per bin left it 5e-9 away, in steps as the parameters moved)."""
+    bin's rounding is not repeated by each of its events.  At 2e6 events the NLL then follows the oracle,
+    evaluated at the FP32-rounded parameters the kernels see, up to a smooth offset (the single-precision bin
+    centres and exponentials of the table inputs: below 1e-8 relative over a scan of alpha and mu), and its
+    changes over steps of 2e-5 in alpha (0.02 sigma) match the oracle's within 1e-3 absolute.  With a
+    single-precision term per bin the NLL jumped by 0.02-0.04 between such neighbouring points."""
     eng, wl, nodes, olist, params, mask, pv = c2_engine(2_000_000, 34, "mixed", monkeypatch)
     data = wl.data.to_numpy()
     names = [v.name for v in params]
@@ -110,8 +112,16 @@ def test_tabulated_terms_in_pairs_track_the_oracle(monkeypatch):
         p[names.index("alpha")] += shift
         p[names.index("mu")] -= shift / 2
         p32 = p.astype(np.float32).astype(np.float64)
-        got = eng.nll(p)
-        assert got == pytest.approx(O.nll(nodes, olist, p32, data), rel=2e-10), shift
+        assert eng.nll(p) == pytest.approx(O.nll(nodes, olist, p32, data), rel=1e-8), shift
+    prev = None
+    for j in range(6):
+        p = pv.copy()
+        p[names.index("alpha")] += 2e-5 * j
+        p32 = p.astype(np.float32).astype(np.float64)
+        cur = (eng.nll(p), O.nll(nodes, olist, p32, data))
+        if prev is not None:
+            assert abs((cur[0] - prev[0]) - (cur[1] - prev[1])) < 1e-3, (j, cur, prev)
+        prev = cur
     eng.close()
 
 
