@@ -1895,19 +1895,24 @@ struct Gen {
             const bool kcReg = plan.conv_fold_q[ci] >= 0 && sh.KP == 1;
             const bool kcPre = plan.conv_fold_q[ci] >= 0 && KB <= block && !kcReg;
             if(kcReg) {
-                os << "    R kcr[" << KT << "];\n    {\n";
-                os << "      const int kb_ = (tid / " << MS << ") / " << comps << ", kt0_ = k0 + kb_ * " << KT << ";\n";
-                os << "      const bool kl_ = tid % " << MS << " == 0 && kb_ < " << ktiles << ";\n";
+                // kept as loaded (int) and converted where the fold uses them: a conversion right after the load
+                // would stall the warp on the load (a DRAM miss after an L2 flush, ~1.8 us) before the staging
+                // every lane loads its item's counts at a clamped (valid) index, without a predicate or a select:
+                // nothing consumes the loaded registers before the fold, which reads them only for entries that
+                // exist, so the warp does not wait for the loads (a DRAM miss after an L2 flush)
+                os << "    int kcr[" << KT << "];\n    {\n";
+                os << "      const int kt0_ = k0 + min((tid / " << MS << ") / " << comps << ", " << ktiles - 1 << ") * " << KT
+                   << ";\n";
                 os << "#pragma unroll\n      for(int j = 0; j < " << KT << "; ++j)\n";
-                os << "        kcr[j] = kl_ && kt0_ + j <= " << cv.kmax << " ? (R)gf_kcount_" << ci << "[kt0_ + j - " << cv.kmin
-                   << "] : R(0);\n    }\n";
+                os << "        kcr[j] = gf_kcount_" << ci << "[min(kt0_ + j, " << cv.kmax << ") - " << cv.kmin << "];\n    }\n";
             }
             if(kcPre) {
                 // the grid-bin count of one of this CTA's table entries per thread, loaded into a register now
                 // and stored after the staging below, so that the load's latency overlaps the staging
                 os << "    __shared__ R s_kc[" << KB << "];\n";
-                os << "    R kcv = R(0);\n";
-                os << "    if(tid < " << KB << " && k0 + tid <= " << cv.kmax << ") kcv = (R)gf_kcount_" << ci << "[k0 + tid - "
+                // loaded as int by every thread at a clamped index (no predicate or select, which would stall the
+                // warp on the load) and converted at the store after the staging
+                os << "    const int kcv = gf_kcount_" << ci << "[min(k0 + min(tid, " << KB - 1 << "), " << cv.kmax << ") - "
                    << cv.kmin << "];\n";
             }
             const double wM = (cv.ic[1] - cv.ic[0]) / cv.nM, wR = (cv.ic[4] - cv.ic[3]) / cv.nR;
@@ -1960,7 +1965,7 @@ struct Gen {
                 os << "      }\n    }\n";
             }
             if(kcPre)
-                os << "    if(tid < " << KB << ") s_kc[tid] = kcv;\n";
+                os << "    if(tid < " << KB << ") s_kc[tid] = (R)kcv;\n";
             os << "    __syncthreads();\n";
             os << "#pragma unroll\n    for(int c = 0; c < " << NA << "; ++c) {\n";
             os << "      const int lo = __reduce_min_sync(0xffffffffu, slo[c]), hi = __reduce_max_sync(0xffffffffu, "
@@ -2087,7 +2092,7 @@ struct Gen {
             } else {
                 os << "      if(live && ms == 0 && k <= " << cv.kmax << ") {\n";
                 os << "        ctab[" << off[ci] << " + (k - " << cv.kmin << ") * " << cp << " + comp] = t;\n" << loStore;
-                const std::string kc = kcReg   ? "kcr[j]"
+                const std::string kc = kcReg   ? "(R)kcr[j]"
                                        : kcPre ? "s_kc[k - k0]"
                                                : "(R)gf_kcount_" + std::to_string(ci) + "[k - " + std::to_string(cv.kmin) + "]";
                 if(mixed)
@@ -2969,7 +2974,7 @@ struct Gen {
             // one-launch evaluation: the status words, read before the tables (written before the grid barrier;
             // a CTA stopped later leaves its rows unwritten, which the host detects)
             if(asBody)
-                os << "  const int gf_st0 = tid == 0 ? (a.qflag[0] | (a.gbar[2] ? 8 : 0)) : 0;\n";
+                os << "  int gf_q0 = 0; unsigned gf_g2 = 0;\n  if(tid == 0) { gf_q0 = a.qflag[0]; gf_g2 = a.gbar[2]; }\n";
             if(!tab)
                 emitNormReads(os, T, grad, plan.nl, "  ");
             else {
@@ -3008,8 +3013,9 @@ struct Gen {
                 if(dfTab) {
                     os << "  float tlo[" << NR << "];\n";
                     os << "  {\n    const float *gl = reinterpret_cast<const float *>(a.ctab) + " << loOff << ";\n";
+                    // zero, then predicated loads: nothing consumes them before the per-bin terms
                     os << "#pragma unroll\n    for(int r = 0; r < " << NR << "; ++r) {\n      const int kk = kr_lo + tid + r * "
-                       << block << ";\n      tlo[r] = kk <= kr_hi ? gl[kk] : 0.f;\n    }\n  }\n";
+                       << block << ";\n      tlo[r] = 0.f;\n      if(kk <= kr_hi) tlo[r] = gl[kk];\n    }\n  }\n";
                 }
                 // the other normalisation factors as usual
                 {
@@ -3044,12 +3050,23 @@ struct Gen {
                     os << "  {\n";
                     os << "    const ACC *gp = reinterpret_cast<const ACC *>(a.gpartial) + ((i64)toy * " << NQ << " + " << fq
                        << ") * " << NGs << " * " << MGB << ";\n";
-                    for(int c = 0; c < comps; ++c) {
-                        const int cs = c == 0 ? 0 : 1 + cv.dep[c - 1];
-                        os << "    ACC fs" << c << " = acc_zero();\n";
-                        os << "    for(int bi = tid; bi < " << nblk << "; bi += " << block << ") fs" << c << " = acc_add(fs" << c
-                           << ", gp[" << cs * MGB << " + bi]);\n";
-                    }
+                    if(nblk <= block) {
+                        // one partial per thread and component: all loads issued before any is used
+                        for(int c = 0; c < comps; ++c)
+                            os << "    ACC fs" << c << " = acc_zero();\n";
+                        os << "    if(tid < " << nblk << ") {\n";
+                        for(int c = 0; c < comps; ++c) {
+                            const int cs = c == 0 ? 0 : 1 + cv.dep[c - 1];
+                            os << "      fs" << c << " = gp[" << cs * MGB << " + tid];\n";
+                        }
+                        os << "    }\n";
+                    } else
+                        for(int c = 0; c < comps; ++c) {
+                            const int cs = c == 0 ? 0 : 1 + cv.dep[c - 1];
+                            os << "    ACC fs" << c << " = acc_zero();\n";
+                            os << "    for(int bi = tid; bi < " << nblk << "; bi += " << block << ") fs" << c << " = acc_add(fs" << c
+                               << ", gp[" << cs * MGB << " + bi]);\n";
+                        }
                     std::vector<std::string> vals;
                     for(int c = 0; c < comps; ++c)
                         vals.push_back("fs" + std::to_string(c));
@@ -3606,7 +3623,7 @@ struct Gen {
             const bool foldTab = tab && plan.conv_fold_q[0] >= 0;
             os << "    if(tid < " << NGc << ") { ACC t = acc_zero(); for(int w = 0; w < " << NW
                << "; ++w) t = acc_add(t, red[w][tid]); a.hpart[(i64)ch * " << NGc + 1 << " + tid] = acc_value(t); }\n";
-            os << "    if(tid == 0) a.hpart[(i64)ch * " << NGc + 1 << " + " << NGc << "] = (double)(gf_st0"
+            os << "    if(tid == 0) a.hpart[(i64)ch * " << NGc + 1 << " + " << NGc << "] = (double)(gf_q0 | (gf_g2 ? 8 : 0)"
                << (foldTab ? " | s_fbits" : "") << ");\n";
             os << "    __syncthreads();\n";
             os << "  }\n}\n\n";
