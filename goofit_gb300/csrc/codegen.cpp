@@ -1894,18 +1894,9 @@ struct Gen {
             // the fold at the end
             const bool kcReg = plan.conv_fold_q[ci] >= 0 && sh.KP == 1;
             const bool kcPre = plan.conv_fold_q[ci] >= 0 && KB <= block && !kcReg;
-            if(kcReg) {
-                // kept as loaded (int) and converted where the fold uses them: a conversion right after the load
-                // would stall the warp on the load (a DRAM miss after an L2 flush, ~1.8 us) before the staging
-                // every lane loads its item's counts at a clamped (valid) index, without a predicate or a select:
-                // nothing consumes the loaded registers before the fold, which reads them only for entries that
-                // exist, so the warp does not wait for the loads (a DRAM miss after an L2 flush)
-                os << "    int kcr[" << KT << "];\n    {\n";
-                os << "      const int kt0_ = k0 + min((tid / " << MS << ") / " << comps << ", " << ktiles - 1 << ") * " << KT
-                   << ";\n";
-                os << "#pragma unroll\n      for(int j = 0; j < " << KT << "; ++j)\n";
-                os << "        kcr[j] = gf_kcount_" << ci << "[min(kt0_ + j, " << cv.kmax << ") - " << cv.kmin << "];\n    }\n";
-            }
+            // kcReg: the counts are loaded after the support's barrier (below), because a barrier waits for the
+            // warp's loads in flight (a DRAM miss after an L2 flush, ~1.3 us); the sums that follow have no
+            // barrier and cover the load
             if(kcPre) {
                 // the grid-bin count of one of this CTA's table entries per thread, loaded into a register now
                 // and stored after the staging below, so that the load's latency overlaps the staging
@@ -1974,6 +1965,16 @@ struct Gen {
             os << "    }\n";
             os << "    __syncthreads();\n";
             const int fq = plan.conv_fold_q[ci];
+            if(kcReg) {
+                // every lane loads its item's counts at a clamped (valid) index, without a predicate or a select,
+                // and keeps them as ints: nothing consumes them before the fold, which reads them only for
+                // entries that exist
+                os << "    int kcr[" << KT << "];\n    {\n";
+                os << "      const int kt0_ = k0 + min((tid / " << MS << ") / " << comps << ", " << ktiles - 1 << ") * " << KT
+                   << ";\n";
+                os << "#pragma unroll\n      for(int j = 0; j < " << KT << "; ++j)\n";
+                os << "        kcr[j] = gf_kcount_" << ci << "[min(kt0_ + j, " << cv.kmax << ") - " << cv.kmin << "];\n    }\n";
+            }
             os << "    const int ms = tid % " << MS << ", item = tid / " << MS << ", comp = item % " << comps
                << ", ktb = item / " << comps << ";\n";
             os << "    const bool live = ktb < " << ktiles << ";\n";
