@@ -1631,6 +1631,9 @@ struct Gen {
     bool recomputeKernels = false;
     bool recompute        = false;
     Shapes shapes;
+    bool countDecl = false; // the counting pass's shared variables have been declared
+    // rows (bins) a CTA's events may span for the counting pass of the tabulated event pass
+    static constexpr int kCountRows = 256;
 
     // per-toy column pointer i of table `tab` (n per toy); one toy: from the kernel arguments at p0[off + i]
     static std::string p0ptr(const char *tab, int n, int i, int off) {
@@ -1644,6 +1647,30 @@ struct Gen {
     static int convStride(int n) { return n + (((8 - n) % 32) + 32) % 32; }
 
     // Table layout per toy: for each conv, AoS [k][cp] with cp = padded component count (16-byte rows).
+    // Counting pass of the tabulated event pass (events sorted by bin, staged in shared memory): every event's
+    // bin offset is read once, 8 per thread and step, and each run of equal offsets records its start in
+    // gf_rstart[bin - kr_lo]; the events of a bin are then the distance to the next run's start.  Emitted after
+    // the table loads were issued and before their first use, so that it runs while they are in flight (it
+    // holds no barrier, which would wait for them).  cnt_ok = 0 (the per-event loop instead) for unsorted or
+    // unstaged events, and for a range over more than kCountRows bins.
+    void emitCountPass(const ConvInfo &cv) {
+        os << "  {\n";
+        os << "    const i64 ee = (i64)ce * a.chunk < a.nevt0 ? (i64)ce * a.chunk : a.nevt0;\n";
+        os << "    cnt_ok = a.ksort != nullptr && gf_st != nullptr && cb < ce && ee > gf_ib && cnt_nrows > 0 && cnt_nrows <= "
+           << kCountRows << ";\n";
+        os << "    if(cnt_ok) {\n";
+        os << "      cnt_nev = (int)(ee - gf_ib);\n";
+        os << "      const int *ks = reinterpret_cast<const int *>(gf_st + gf_soff[0]);\n";
+        os << "      for(int i0 = 8 * tid; i0 < cnt_nev; i0 += " << 8 * block << ") {\n";
+        os << "        const int4 u = *reinterpret_cast<const int4 *>(ks + i0), w = *reinterpret_cast<const int4 *>(ks + i0 + 4);\n";
+        os << "        const int kv[8] = {u.x, u.y, u.z, u.w, w.x, w.y, w.z, w.w};\n";
+        os << "        int prev = i0 > 0 ? ks[i0 - 1] : " << cv.kmin - 1 << ";\n";
+        os << "#pragma unroll\n        for(int j = 0; j < 8; ++j) {\n";
+        os << "          const int r = kv[j] - " << cv.kmin << " - kr_lo;\n";
+        os << "          if(i0 + j < cnt_nev && kv[j] != prev && r >= 0 && r < cnt_nrows) gf_rstart[r] = i0 + j;\n";
+        os << "          prev = kv[j];\n        }\n      }\n    }\n  }\n";
+    }
+
     // The event function of the tabulated pass can be evaluated with gf_df: only sums, products and quotients
     // (AddPdf, ProdPdf, constant polynomials) above the convolution, whose model and resolution the table kernel
     // evaluates.
@@ -3004,6 +3031,8 @@ struct Gen {
                     os << "      kr_lo = max(kr_lo, 0); kr_hi = min(kr_hi, " << cv.nK - 1 << ");\n";
                     os << "    }\n  }\n";
                 }
+                if(asBody)
+                    os << "  int cnt_ok = 0, cnt_nrows = kr_hi - kr_lo + 1, cnt_nev = 0; (void)cnt_nev;\n";
                 os << "  " << vt << " tv[" << NR << "][" << nvr << "];\n";
                 os << "  {\n    const R *gt = reinterpret_cast<const R *>(a.ctab) + " << off[0] << ";\n";
                 os << "#pragma unroll\n    for(int r = 0; r < " << NR << "; ++r) {\n      const int kk = kr_lo + tid + r * " << block
@@ -3037,6 +3066,8 @@ struct Gen {
                     }
                     os << txt;
                 }
+                if(fq < 0 && asBody)
+                    emitCountPass(cv);
                 if(fq >= 0) {
                     const NumInfo &g = T.nums[fq];
                     const int node   = g.node;
@@ -3071,6 +3102,8 @@ struct Gen {
                     std::vector<std::string> vals;
                     for(int c = 0; c < comps; ++c)
                         vals.push_back("fs" + std::to_string(c));
+                    if(asBody)
+                        emitCountPass(cv);
                     emitCtaReduce(os, vals, "    ");
                     // GooPdf::normalize's numeric branch (src/PDFs/GooPdf.cu:366-395) on the CTA's sums
                     // lane c of warp 0 sums component c over the warps; lane 0 gathers them
@@ -3167,6 +3200,57 @@ struct Gen {
                            << "];\n";
                 os << "      }\n    }\n  }\n  __syncthreads();\n";
             }
+        }
+        const bool countMode = asBody && tab;
+        if(countMode) {
+            // counted events (cnt_ok, from the counting pass below the table loads): each bin's terms
+            // times its events' count (the value as an exact product pair), in place of the per-event loop; the
+            // CTA's sums go to its first chunk's row, its other chunks' rows get zeros
+            const int NGc0 = NGp + (factorRoot ? 1 : 0);
+            const char *fld[] = {".x", ".y", ".z", ".w"};
+            auto compC = [&](int q) {
+                const int b = q / vw;
+                return "lq" + std::to_string(b) + (bw[b] == 1 ? std::string("") : std::string(fld[q % vw]));
+            };
+            const bool foldTab = plan.conv_fold_q[0] >= 0;
+            const std::string st = std::string("(double)(gf_q0 | (gf_g2 ? 8 : 0)") + (foldTab ? " | s_fbits" : "") + ")";
+            os << "  if(cnt_ok) {\n";
+            os << "    ACC cs0 = acc_zero();\n";
+            for(int sl = 0; sl < NGp - 1; ++sl)
+                os << "    ACC cs" << 1 + sl << " = acc_zero();\n";
+            if(factorRoot)
+                os << "    ACC csn = acc_zero();\n";
+            os << "    for(int r = tid; r < cnt_nrows; r += " << block << ") {\n";
+            os << "      const int st = gf_rstart[r];\n      if(st < 0) continue;\n";
+            os << "      int en = cnt_nev;\n";
+            os << "      for(int q = r + 1; q < cnt_nrows; ++q) { const int sq = gf_rstart[q]; if(sq >= 0) { en = sq; break; } }\n";
+            os << "      const R c = (R)(en - st);\n";
+            os << "      const int lk = kr_lo + r;\n";
+            for(size_t b = 0; b < bw.size(); ++b)
+                os << "      const " << vtype(bw[b]) << " lq" << b << " = *reinterpret_cast<const " << vtype(bw[b])
+                   << " *>(ltab + " << boff[b] << " + lk * " << bw[b] << ");\n";
+            os << "      cs0 = acc_add(cs0, gf_two_prod(c, " << compC(0) << "));\n";
+            if(dfTab)
+                os << "      cs0 = acc_add(cs0, acc_of(c * " << compC(tabComps) << "));\n";
+            for(int sl = 0; sl < NGp - 1; ++sl)
+                os << "      cs" << 1 + sl << " = acc_add(cs" << 1 + sl << ", gf_two_prod(c, " << compC(1 + sl) << "));\n";
+            if(factorRoot)
+                os << "      csn = acc_add(csn, acc_of(c * " << compC(tabComps - 1) << "));\n";
+            os << "    }\n";
+            std::vector<std::string> vals{"cs0"};
+            for(int sl = 0; sl < NGp - 1; ++sl)
+                vals.push_back("cs" + std::to_string(1 + sl));
+            if(factorRoot)
+                vals.push_back("csn");
+            emitCtaReduce(os, vals, "    ");
+            os << "    if(tid < " << NGc0 << ") { ACC t = acc_zero(); for(int w = 0; w < " << NW
+               << "; ++w) t = acc_add(t, red[w][tid]); a.hpart[(i64)cb * " << NGc0 + 1 << " + tid] = acc_value(t); }\n";
+            os << "    if(tid == 0) a.hpart[(i64)cb * " << NGc0 + 1 << " + " << NGc0 << "] = " << st << ";\n";
+            os << "    for(int ch = cb + 1; ch < ce; ++ch) {\n";
+            os << "      if(tid < " << NGc0 << ") a.hpart[(i64)ch * " << NGc0 + 1 << " + tid] = 0.0;\n";
+            os << "      if(tid == 0) a.hpart[(i64)ch * " << NGc0 + 1 << " + " << NGc0 << "] = " << st << ";\n";
+            os << "    }\n";
+            os << "  } else {\n";
         }
         if(asBody) {
             // staged events: every thread waits for the bulk copy (bounded); a copy that does not arrive leaves
@@ -3627,7 +3711,7 @@ struct Gen {
             os << "    if(tid == 0) a.hpart[(i64)ch * " << NGc + 1 << " + " << NGc << "] = (double)(gf_q0 | (gf_g2 ? 8 : 0)"
                << (foldTab ? " | s_fbits" : "") << ");\n";
             os << "    __syncthreads();\n";
-            os << "  }\n}\n\n";
+            os << "  }\n" << (countMode ? "  }\n" : "") << "}\n\n";
             endBody(asBody);
             return;
         }
@@ -3696,6 +3780,12 @@ struct Gen {
             convKernel(grad, true, tab);
         if(hasGrid)
             gridKernel(grad, true);
+        if(tab && !countDecl) {
+            // the counting pass's results, shared by the fused kernel (which counts before the grid barrier) and
+            // its event body (which multiplies the per-bin terms by the counts after it)
+            os << "__shared__ int gf_rstart[" << kCountRows << "];\n";
+            countDecl = true;
+        }
         eventKernel(grad, false, true, tab);
         const size_t evtSmem = bodySmem;
         const int CB = plan.conv_blocks, MGB = plan.max_grid_blocks;
@@ -3758,6 +3848,9 @@ struct Gen {
         os << "    s_staged = staged;\n";
         os << "  }\n";
         os << "  __syncthreads();\n";
+        if(tab)
+            // the counting pass's run starts (written after the grid barrier, whose own barrier orders this)
+            os << "  for(int r = threadIdx.x; r < " << kCountRows << "; r += blockDim.x) gf_rstart[r] = -1;\n";
         // a CTA that leaves early still waits (bounded) for its own bulk copy, so that no copy writes the shared
         // memory of a finished CTA
         auto barrier = [&]() {
