@@ -1501,6 +1501,48 @@ __device__ __forceinline__ GfDual sqrt(GfDual x) {
     return GfDual(r, x.a / (2 * r), x.b / (2 * r));
 }
 __device__ __forceinline__ GfDual fabs(GfDual x) { return x.v < 0 ? -x : x; }
+// Single precision (the mixed engine's floated line shapes): sums and differences with an FP64 operand are
+// formed in FP64 and rounded once (the pole difference mass^2 - m^2 cancels near the pole), every other
+// operation is FP32.
+struct GfDualF {
+    float v, a, b;
+    __device__ __forceinline__ GfDualF(float v_ = 0.f, float a_ = 0.f, float b_ = 0.f) : v(v_), a(a_), b(b_) {}
+    __device__ __forceinline__ GfDualF(double v_) : v((float)v_), a(0.f), b(0.f) {}
+    __device__ __forceinline__ GfDualF(int v_) : v((float)v_), a(0.f), b(0.f) {}
+};
+__device__ __forceinline__ float dval(const GfDualF &x) { return x.v; }
+__device__ __forceinline__ GfDualF operator+(GfDualF x, GfDualF y) { return GfDualF(x.v + y.v, x.a + y.a, x.b + y.b); }
+__device__ __forceinline__ GfDualF operator-(GfDualF x, GfDualF y) { return GfDualF(x.v - y.v, x.a - y.a, x.b - y.b); }
+__device__ __forceinline__ GfDualF operator-(GfDualF x) { return GfDualF(-x.v, -x.a, -x.b); }
+__device__ __forceinline__ GfDualF operator*(GfDualF x, GfDualF y) {
+    return GfDualF(x.v * y.v, x.a * y.v + x.v * y.a, x.b * y.v + x.v * y.b);
+}
+__device__ __forceinline__ GfDualF operator/(GfDualF x, GfDualF y) {
+    const float q = x.v / y.v;
+    return GfDualF(q, (x.a - q * y.a) / y.v, (x.b - q * y.b) / y.v);
+}
+__device__ __forceinline__ GfDualF operator+(GfDualF x, double y) { return GfDualF((float)((double)x.v + y), x.a, x.b); }
+__device__ __forceinline__ GfDualF operator+(double y, GfDualF x) { return GfDualF((float)((double)x.v + y), x.a, x.b); }
+__device__ __forceinline__ GfDualF operator-(GfDualF x, double y) { return GfDualF((float)((double)x.v - y), x.a, x.b); }
+__device__ __forceinline__ GfDualF operator-(double y, GfDualF x) { return GfDualF((float)(y - (double)x.v), -x.a, -x.b); }
+__device__ __forceinline__ GfDualF operator*(GfDualF x, double y) {
+    const float f = (float)y;
+    return GfDualF(x.v * f, x.a * f, x.b * f);
+}
+__device__ __forceinline__ GfDualF operator*(double y, GfDualF x) { return x * y; }
+__device__ __forceinline__ GfDualF operator/(GfDualF x, double y) {
+    const float f = (float)y;
+    return GfDualF(x.v / f, x.a / f, x.b / f);
+}
+__device__ __forceinline__ GfDualF operator/(double y, GfDualF x) {
+    const float q = (float)y / x.v;
+    return GfDualF(q, -q * x.a / x.v, -q * x.b / x.v);
+}
+__device__ __forceinline__ GfDualF sqrt(GfDualF x) {
+    const float r = sqrtf(x.v);
+    return GfDualF(r, x.a / (2.f * r), x.b / (2.f * r));
+}
+__device__ __forceinline__ GfDualF fabs(GfDualF x) { return x.v < 0 ? -x : x; }
 )CUDA";
 
 // Where every normalisation factor is kept (see NormLayout in tree.h).
@@ -2443,7 +2485,8 @@ struct Gen {
             const TNode &L = T.nodes[A.ls[u]];
             anyDep |= thetaParam(k, L.params[0]) || thetaParam(k, L.params[1]);
         }
-        const bool kin32 = mixed && !anyDep;
+        (void)anyDep;
+        const bool kin32 = mixed; // floated line shapes: single-precision duals over the FP32 pair masses
         if(kin32) {
             os << "  GfLVf W[4];\n";
             os << "  gf_get4vecs_f(W, (float)m12, (float)m34, (float)c12, (float)c34, (float)phi, (float)" << lit(A.M)
@@ -2484,12 +2527,15 @@ struct Gen {
                        << "], P[" << L.params[1] << "], " << (int)L.consts[1] << ", " << (int)L.consts[2] << ", "
                        << lit(L.consts[3]) << ");\n";
             } else {
-                // value and derivatives from the FP64 dual-number line shape
+                // value and derivatives from the dual-number line shape (single precision in the mixed engine)
+                const char *DT = mixed ? "GfDualF" : "GfDual";
+                const std::string one = mixed ? "1.f, 0.f" : "1.0, 0.0", two = mixed ? "0.f, 1.f" : "0.0, 1.0";
+                const std::string cv0 = mixed ? "(float)" : "";
                 os << "  " << C2 << " L" << u << ", Lm" << u << ", Lw" << u << ";\n";
-                os << "  { GfDual re, im;\n";
-                os << "    gf_lineshape_t<GfDual>(" << sbw << ", mp, d1, d2, GfDual(P[" << L.params[0]
-                   << "], 1.0, 0.0), GfDual(P[" << L.params[1] << "], 0.0, 1.0), " << (int)L.consts[1] << ", "
-                   << (int)L.consts[2] << ", " << lit(L.consts[3]) << ", re, im);\n";
+                os << "  { " << DT << " re, im;\n";
+                os << "    gf_lineshape_t<" << DT << ">(" << sbw << ", mp, d1, d2, " << DT << "(" << cv0 << "P[" << L.params[0]
+                   << "], " << one << "), " << DT << "(" << cv0 << "P[" << L.params[1] << "], " << two << "), "
+                   << (int)L.consts[1] << ", " << (int)L.consts[2] << ", " << lit(L.consts[3]) << ", re, im);\n";
                 os << "    L" << u << " = " << MK << "(re.v, im.v); Lm" << u << " = " << MK << "(re.a, im.a); Lw" << u
                    << " = " << MK << "(re.b, im.b); }\n";
             }

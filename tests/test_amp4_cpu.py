@@ -68,8 +68,8 @@ def test_amp4body_kernels_compile_for_sm103a(prec):
 
 
 def test_amp4body_lineshape_parameters_get_derivative_columns():
-    """Floated line-shape masses and widths have analytic derivatives (dual numbers through the line shapes);
-    the efficiency's parameters do not."""
+    """Floated line-shape masses and widths have analytic derivatives (dual numbers through the line shapes,
+    single precision in the mixed engine); the efficiency's parameters do not."""
     pdf, _, _, ls = W.c5_model(1000, float_lineshapes=True)
     nodes, olist, params, mask = _tree(pdf)
     assert sum(mask) == 20
@@ -82,7 +82,7 @@ def test_amp4body_lineshape_parameters_get_derivative_columns():
     buf = C.create_string_buffer(n.value + 1)
     L.gf_generated_source(nl.arr, nl.n, obs, len(olist), len(params), mp, A.GF_MIXED, buf, n.value + 1, C.byref(n))
     src = buf.value.decode()
-    assert "gf_lineshape_t<GfDual>" in src and "gf_ampn" in src
+    assert "gf_lineshape_t<GfDualF>" in src and "gf_ampn" in src
     full = [0 if v.fixed else 1 for v in params]
     for i, v in enumerate(params):
         if v.name == "constantOne":
