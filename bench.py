@@ -47,7 +47,7 @@ EVT_DRAM_EVENTS = 2_000_000
 EVT_DRAM_BYTES_AMP = {"c3": (32_034_048, 500_000), "c5": (14_432_256, 300_000)}
 # DRAM bytes of one gf_fcn_g launch (the one-launch FCN) over 2e6 events, from one ncu capture
 # (profiles/gf_fcn_g_c2_composite_2e6.md)
-FCN_DRAM_BYTES = 8_088_320
+FCN_DRAM_BYTES = 8_084_736
 FCN_DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/gf_fcn_g_c2_composite_2e6.md"
 N_EVENTS = 2_000_000
 WORKLOAD = "c2: AddPdf(0.7 Conv(Exp tau=1.5, Gauss mu=0 sigma=0.3) + 0.3 flat Poly), x in [-5,10], 2e6 events"
