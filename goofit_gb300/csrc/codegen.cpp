@@ -3749,8 +3749,8 @@ struct Gen {
         if(asBody) {
             plan.fused_row[grad ? 1 : 0] = NGc + 1;
             // one-launch evaluation: each chunk's sums and status go straight to page-locked host memory (row
-            // ch: [components..., status]); the host adds the rows in chunk order after the launch, so no CTA
-            // waits on a completion counter and no finishing CTA runs
+            // ch: [components..., status], each word one aligned 8-byte store); the host adds the rows in chunk
+            // order as their words arrive, so no CTA waits on a completion counter and no finishing CTA runs
             const bool foldTab = tab && plan.conv_fold_q[0] >= 0;
             os << "    if(tid < " << NGc << ") { ACC t = acc_zero(); for(int w = 0; w < " << NW
                << "; ++w) t = acc_add(t, red[w][tid]); a.hpart[(i64)ch * " << NGc + 1 << " + tid] = acc_value(t); }\n";

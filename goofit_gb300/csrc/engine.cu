@@ -1478,6 +1478,31 @@ struct NvtxScope {
     ~NvtxScope() { nvtxRangePop(); }
 };
 
+// The host's mark of a one-launch row word not yet written: a signalling-NaN bit pattern, which no arithmetic
+// result (quiet NaNs only) and no status or zero the kernel stores can equal.
+static constexpr uint64_t kRowUnset = 0x7ff40000dead0001ull;
+
+// A row word written by the device into mapped host memory (one aligned 8-byte store), read as a double.
+static inline double wordValue(const uint64_t *p) {
+    const uint64_t u = __atomic_load_n(p, __ATOMIC_RELAXED);
+    double d;
+    std::memcpy(&d, &u, sizeof d);
+    return d;
+}
+
+// Device time of the last evaluation (its CUDA events), read when first asked for after the evaluation.
+double lastMsTotal(const gf_engine *e) {
+    if(e->timing_pending) {
+        e->timing_pending = false;
+        float ms = 0;
+        if(cudaEventSynchronize(e->ev[3]) == cudaSuccess && cudaEventElapsedTime(&ms, e->ev[0], e->ev[3]) == cudaSuccess)
+            e->last_ms_total = ms;
+        else
+            cudaGetLastError();
+    }
+    return e->last_ms_total;
+}
+
 int gf_run(gf_engine *e, bool grad, int, int) {
     NvtxScope fcn(grad ? "gf_fcn_grad" : "gf_fcn");
     int rc = buildLayout(e);
@@ -1495,15 +1520,18 @@ int gf_run(gf_engine *e, bool grad, int, int) {
         if((rc = autotune(e)))
             return rc;
     }
-    // one-launch evaluation: every chunk row's status starts negative and only the CTA that evaluated the
-    // chunk overwrites it, so an evaluation that a barrier wait stopped cannot pass for a result
+    // one-launch evaluation: every word of every chunk row starts as kRowUnset and only the CTA that evaluated
+    // the chunk overwrites it, so the host can read each word as soon as it changes, and an evaluation that a
+    // barrier wait stopped cannot pass for a result
     const bool fused = fusedPath(e);
     const int frow   = fused ? e->plan.fused_row[grad ? 1 : 0] : 0;
-    if(fused)
-        for(int c = 0; c < e->n_chunks; ++c)
-            e->h_fpart[(size_t)c * frow + frow - 1] = -1.0;
+    if(fused) {
+        uint64_t *w = reinterpret_cast<uint64_t *>(e->h_fpart);
+        for(size_t i = 0, n = (size_t)e->n_chunks * frow; i < n; ++i)
+            w[i] = kRowUnset;
+    }
     cudaError_t r;
-    if(e->use_graph && !(fused && !e->fused_graph_ok)) {
+    if(e->use_graph && !(fused && (!e->fused_graph_ok || e->fused_direct))) {
         cudaGraphExec_t &ge = e->graph[grad ? 1 : 0];
         if(!ge) {
             cudaGraph_t g = nullptr;
@@ -1588,29 +1616,44 @@ int gf_run(gf_engine *e, bool grad, int, int) {
         if(r != cudaSuccess)
             return gf_cuda_check(e, r, "launch");
     }
-    r = cudaStreamSynchronize(e->stream);
-    if(r != cudaSuccess)
-        return gf_cuda_check(e, r, "evaluation");
-    float ms = 0;
-    if(cudaEventElapsedTime(&ms, e->ev[0], e->ev[3]) == cudaSuccess)
-        e->last_ms_total = ms;
     bool stopped = false;
     if(fused) {
-        // the chunk rows in chunk order: sums of the components, the OR of the status words; a row still
-        // holding its -1 was never written (its CTA stopped at a barrier or on its bulk copy)
+        // the chunk rows in chunk order: sums of the components, the OR of the status words. Each word of a row
+        // is written once per launch by one aligned 8-byte store, so a word that no longer holds kRowUnset is
+        // final: the host adds the rows as they arrive instead of waiting for the launch to end and its stream
+        // to report it (5-6 us per FCN), and the kernel needs no fence. A row still holding kRowUnset once the
+        // stream reports the launch's end was never written (its CTA stopped at a barrier or on its bulk copy).
         const int nc = frow - 1, NGp = 1 + (grad ? e->tree.NG : 0);
-        std::vector<double> sum(std::max(1, nc), 0.0);
+        std::vector<double> &sum = e->fsum;
+        sum.assign(std::max(1, nc), 0.0);
         int st = 0;
-        for(int c = 0; c < e->n_chunks; ++c) {
-            const double *row = e->h_fpart + (size_t)c * frow;
-            if(row[nc] < 0) {
-                stopped = true;
+        bool ended = false;
+        unsigned spins = 0;
+        for(int c = 0; c < e->n_chunks;) {
+            const uint64_t *row = reinterpret_cast<const uint64_t *>(e->h_fpart + (size_t)c * frow);
+            bool ready = true;
+            for(int k = 0; k < frow && ready; ++k)
+                ready = __atomic_load_n(row + k, __ATOMIC_RELAXED) != kRowUnset;
+            if(!ready && !ended) {
+                if((++spins & 127u) == 0) {
+                    r = cudaStreamQuery(e->stream);
+                    if(r == cudaSuccess)
+                        ended = true; // the launch's writes are all visible: read this row once more
+                    else if(r != cudaErrorNotReady)
+                        return gf_cuda_check(e, r, "evaluation");
+                }
                 continue;
             }
-            st |= (int)row[nc];
-            for(int k = 0; k < nc; ++k)
-                sum[k] += row[k];
+            if(!ready)
+                stopped = true;
+            else {
+                st |= (int)wordValue(row + nc);
+                for(int k = 0; k < nc; ++k)
+                    sum[k] += wordValue(row + k);
+            }
+            ++c;
         }
+        e->timing_pending = true;
         double *o = e->h_out;
         o[0]      = sum[0];
         for(int k = 1; k < NGp; ++k)
@@ -1626,6 +1669,12 @@ int gf_run(gf_engine *e, bool grad, int, int) {
             cudaMemsetAsync(e->d_qflag, 0, sizeof(int) * e->n_toys, e->stream);
             cudaStreamSynchronize(e->stream);
         }
+    } else {
+        r = cudaStreamSynchronize(e->stream);
+        if(r != cudaSuccess)
+            return gf_cuda_check(e, r, "evaluation");
+        e->timing_pending = true;
+        lastMsTotal(e);
     }
     if(stopped) {
         // a grid barrier wait ran out: clear the barrier words and the completion counters and flags that
@@ -1683,6 +1732,8 @@ int gf_engine_create(gf_engine **out, int device, int precision) {
     cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device);
     if(const char *g = std::getenv("GF_NO_GRAPH"))
         e->use_graph = !(g[0] == '1');
+    if(const char *d = std::getenv("GF_FUSED_DIRECT"))
+        e->fused_direct = d[0] == '1';
     if(const char *c = std::getenv("GF_CHUNK")) {
         e->chunk       = std::max(256, (atoi(c) / 256) * 256);
         e->chunk_fixed = true;
@@ -2256,7 +2307,7 @@ int gf_last_timing(const gf_engine *e, double *ms_total, double *ms_evt) {
     if(!e)
         return GF_ERR_INVALID;
     if(ms_total)
-        *ms_total = e->last_ms_total;
+        *ms_total = lastMsTotal(e);
     if(ms_evt)
         *ms_evt = e->last_ms_evt;
     return GF_OK;
@@ -2345,7 +2396,7 @@ int timeEval(gf_engine *e, void *flush, size_t flushBytes, int reps, double *bes
         if(int rc = gf_run(e, true, -1, 1))
             return rc;
         if(it > 0)
-            *best = std::min(*best, e->last_ms_total);
+            *best = std::min(*best, lastMsTotal(e));
     }
     return GF_OK;
 }

@@ -183,8 +183,14 @@ struct gf_engine {
     bool layout_ready = false;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    double last_ms_total = 0, last_ms_evt = 0;
+    // device time of the last evaluation (CUDA events around it); after a one-launch evaluation whose rows the
+    // host read before the launch ended, it is read from the events when first asked for
+    mutable double last_ms_total = 0;
+    double last_ms_evt = 0;
+    mutable bool timing_pending = false;
     bool use_graph = true;
+    bool fused_direct = false; // GF_FUSED_DIRECT=1: the one-launch kernel is launched directly, not replayed from a graph
+    std::vector<double> fsum; // the host's sums of the one-launch rows
     bool use_pdl   = true;
     // one-launch evaluation (one toy, unbinned NLL): resident CTAs of the cooperative launch, the barrier
     // words it synchronises on and the longest barrier wait before it gives up (GF_FUSED=0: three launches)
