@@ -3488,8 +3488,13 @@ struct Gen {
             if(!pipe)
                 os << "      const int4 kv" << ci << "a = *reinterpret_cast<const int4 *>(kc" << ci << " + i0), kv" << ci
                    << "b = *reinterpret_cast<const int4 *>(kc" << ci << " + i0 + 4);\n";
-            os << "      const int ka" << ci << "[8] = {kv" << ci << "a.x, kv" << ci << "a.y, kv" << ci << "a.z, kv" << ci
+            os << "      int ka" << ci << "[8] = {kv" << ci << "a.x, kv" << ci << "a.y, kv" << ci << "a.z, kv" << ci
                << "a.w, kv" << ci << "b.x, kv" << ci << "b.y, kv" << ci << "b.z, kv" << ci << "b.w};\n";
+            // an iteration that runs past the chunk's end reads offsets beyond its events: from a staged copy,
+            // shared memory past the copied bytes (any value), so they take the table's first row before any
+            // gather uses them as an index (their terms are masked out)
+            os << "      if(jn < 8) {\n#pragma unroll\n        for(int j = 0; j < 8; ++j) if(j >= jn) ka" << ci
+               << "[j] = " << T.convs[ci].kmin << ";\n      }\n";
         }
         // tab: the iteration's events' terms are kept per component and summed pairwise after the loop
         // (exact for equal terms, as neighbouring events in bin order mostly are; three roundings otherwise)
@@ -3951,12 +3956,14 @@ struct Gen {
         const size_t work = std::max(grad ? plan.conv_smem_grad : plan.conv_smem_nograd, evtSmem);
         const size_t soff = (work + 127) / 128 * 128;
         // two resident CTAs per SM (228 KB of shared memory per SM, 1 KB of it reserved per CTA, a few KB of
-        // static arrays): the staged events get what is left of 109 KB, at most 64 KB
-        const size_t budget = 109 * 1024;
-        const size_t cap    = soff < budget ? std::min<size_t>(64 * 1024, (budget - soff) / 16 * 16) : 0;
+        // static arrays): the staged events get what is left of 109 KB, at most 64 KB. 64 bytes of slack follow
+        // the staging area: the event loop's last iteration reads whole 8-event (2-event) groups, up to 56 bytes
+        // past a stream's last staged event, and those reads must stay inside the CTA's shared memory
+        const size_t budget = 109 * 1024, slack = 64;
+        const size_t cap    = soff + slack < budget ? std::min<size_t>(64 * 1024, (budget - soff - slack) / 16 * 16) : 0;
         plan.fused_stage_off[grad ? 1 : 0] = soff;
         plan.fused_stage_cap[grad ? 1 : 0] = cap;
-        plan.fused_smem[grad ? 1 : 0]      = soff + cap;
+        plan.fused_smem[grad ? 1 : 0]      = soff + cap + slack;
     }
 };
 

@@ -41,16 +41,46 @@ struct ConvertArgs {
     int conv_kmin[8], conv_kmax[8];
     double pad_val[16];
     int *err;
+    // histogram of convolution 0's offsets for the sorted copy (null: none), its bins and the offsets of the
+    // sorted runs; khist[k_nK] counts the CTAs that finished
+    unsigned *khist;
+    long long *koffs;
+    int k_nK;
 };
+
+// offs[0..nK]: exclusive prefix sums of hist[0..nK) by one CTA (a power-of-two block of at most 1024 threads):
+// each thread sums a contiguous run of bins, a scan over the run totals, then each thread writes its run's
+// offsets
+__device__ void gf_scan_runs(const unsigned *hist, int nK, long long *offs) {
+    __shared__ long long part[1024];
+    const int tid = threadIdx.x, nt = blockDim.x, per = (nK + nt - 1) / nt;
+    const int b0 = min(nK, tid * per), b1 = min(nK, b0 + per);
+    long long s = 0;
+    for(int b = b0; b < b1; ++b)
+        s += __ldcg(hist + b);
+    part[tid] = s;
+    __syncthreads();
+    for(int o = 1; o < nt; o <<= 1) {
+        const long long v = tid >= o ? part[tid - o] : 0;
+        __syncthreads();
+        part[tid] += v;
+        __syncthreads();
+    }
+    long long run = tid > 0 ? part[tid - 1] : 0;
+    for(int b = b0; b < b1; ++b) {
+        offs[b] = run;
+        run += __ldcg(hist + b);
+    }
+    if(tid == nt - 1)
+        offs[nK] = part[nt - 1];
+}
 
 // FP64 SoA -> engine columns (FP32 or FP64) plus the ConvolutionPdf bin
 // offset of every event (src/PDFs/combine/ConvolutionPdf.cu:40-43, FP64),
-// which is all the convolution needs of x.
+// which is all the convolution needs of x: one event (or padding slot) i, returning convolution 0's offset.
 template <typename R>
-__global__ void gf_convert_events(const ConvertArgs a) {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if(i >= a.npad)
-        return;
+__device__ __forceinline__ int gf_convert_one(const ConvertArgs &a, long long i) {
+    int k0 = 0;
     // every value is read once (the source may be page-locked host memory read over the interconnect),
     // all loads issued before the first store
     double xs[16];
@@ -87,6 +117,38 @@ __global__ void gf_convert_events(const ConvertArgs a) {
         } else
             k = a.conv_kmin[c];
         a.kcols[c][i] = k;
+        if(c == 0)
+            k0 = k;
+    }
+    return k0;
+}
+
+// One thread per event or padding slot. With a.khist set it also builds the histogram of convolution 0's offsets
+// (events only, not the padding) for the sorted copy of the one-launch tabulated path, hidden under the
+// interconnect-bound reads: one atomic per distinct offset in a warp, and the last CTA to finish turns the
+// histogram into the offsets of the sorted runs.
+template <typename R>
+__global__ void gf_convert_events(const ConvertArgs a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int k0 = i < a.npad ? gf_convert_one<R>(a, i) : 0;
+    if(a.khist) {
+        const bool counted  = i < a.n;
+        const unsigned part = __ballot_sync(0xffffffffu, counted);
+        if(counted) {
+            const unsigned same = __match_any_sync(part, k0);
+            if((int)(threadIdx.x & 31) == __ffs(same) - 1)
+                atomicAdd(a.khist + (k0 - a.conv_kmin[0]), (unsigned)__popc(same));
+        }
+        __shared__ bool last;
+        __threadfence();
+        __syncthreads();
+        if(threadIdx.x == 0)
+            last = atomicAdd(a.khist + a.k_nK, 1u) == gridDim.x - 1;
+        __syncthreads();
+        if(last) {
+            __threadfence();
+            gf_scan_runs(a.khist, a.k_nK, a.koffs);
+        }
     }
 }
 
@@ -116,30 +178,9 @@ __global__ void gf_khist(const int *__restrict__ k, long long n, int kmin, int n
                 atomicAdd(&hist[i], sh[i]);
 }
 
-// offs[0..nK]: exclusive prefix sums of the histogram (one CTA of 1024 threads: each sums a contiguous run of
-// bins, a scan over the 1024 run totals, then each writes its run's offsets)
+// offs[0..nK]: exclusive prefix sums of the histogram (one CTA of 1024 threads)
 __global__ void __launch_bounds__(1024) gf_kscan(const unsigned *__restrict__ hist, int nK, long long *__restrict__ offs) {
-    __shared__ long long part[1024];
-    const int tid = threadIdx.x, per = (nK + 1023) / 1024;
-    const int b0 = min(nK, tid * per), b1 = min(nK, b0 + per);
-    long long s = 0;
-    for(int b = b0; b < b1; ++b)
-        s += hist[b];
-    part[tid] = s;
-    __syncthreads();
-    for(int o = 1; o < 1024; o <<= 1) {
-        const long long v = tid >= o ? part[tid - o] : 0;
-        __syncthreads();
-        part[tid] += v;
-        __syncthreads();
-    }
-    long long run = tid > 0 ? part[tid - 1] : 0;
-    for(int b = b0; b < b1; ++b) {
-        offs[b] = run;
-        run += hist[b];
-    }
-    if(tid == 1023)
-        offs[nK] = part[1023];
+    gf_scan_runs(hist, nK, offs);
 }
 
 // block b writes bin b's run [offs[b], offs[b + 1]) of the sorted column (coalesced stores, no search); the
@@ -155,11 +196,31 @@ __global__ void gf_kfill(const long long *__restrict__ offs, int nK, int kmin, l
             out[i] = kmin;
 }
 
+// The sort's histogram (nK bins and a finished-CTA counter) and run offsets of toy 0, allocated on first use and
+// kept across uploads.
+cudaError_t ensureKHist(GfToy &ty, int nK) {
+    if(ty.khist_n >= nK)
+        return cudaSuccess;
+    if(ty.khist)
+        cudaFree(ty.khist);
+    if(ty.koffs)
+        cudaFree(ty.koffs);
+    ty.khist      = nullptr;
+    ty.koffs      = nullptr;
+    ty.khist_n    = 0;
+    cudaError_t r = cudaMalloc((void **)&ty.khist, sizeof(unsigned) * (nK + 1));
+    if(r == cudaSuccess)
+        r = cudaMalloc((void **)&ty.koffs, sizeof(long long) * (nK + 1));
+    if(r == cudaSuccess)
+        ty.khist_n = nK;
+    return r;
+}
+
 // Sorted copy of toy 0's offsets of convolution 0: histogram, prefix sums and fill, all on the device and
 // asynchronous on the engine's stream (the upload's own range check has already rejected offsets outside the
-// table); the sorted column and the histogram scratch are allocated on first use and kept across uploads of
-// the same size.
-int buildKSort(gf_engine *e) {
+// table). histReady: the upload's conversion kernel has already built the histogram and the run offsets. The
+// sorted column is allocated on first use and kept across uploads of the same size.
+int buildKSort(gf_engine *e, bool histReady) {
     GfToy &ty = e->toys[0];
     if(!ty.loaded || e->tree.convs.empty())
         return GF_OK;
@@ -168,26 +229,19 @@ int buildKSort(gf_engine *e) {
     cudaError_t r          = cudaSuccess;
     if(!ty.ksort)
         r = cudaMalloc((void **)&ty.ksort, sizeof(int) * (size_t)std::max<int64_t>(8, ty.npad));
-    if(r == cudaSuccess && ty.khist_n < nK) {
-        if(ty.khist)
-            cudaFree(ty.khist);
-        if(ty.koffs)
-            cudaFree(ty.koffs);
-        ty.khist   = nullptr;
-        ty.koffs   = nullptr;
-        ty.khist_n = 0;
-        r          = cudaMalloc((void **)&ty.khist, sizeof(unsigned) * nK);
+    if(!histReady) {
         if(r == cudaSuccess)
-            r = cudaMalloc((void **)&ty.koffs, sizeof(long long) * (nK + 1));
+            r = ensureKHist(ty, nK);
+        const int grid = std::max(1, e->sm_count) * 2;
         if(r == cudaSuccess)
-            ty.khist_n = nK;
+            r = cudaMemsetAsync(ty.khist, 0, sizeof(unsigned) * nK, e->stream);
+        if(r == cudaSuccess) {
+            gf_khist<<<grid, 256, nK <= 8192 ? sizeof(unsigned) * nK : 0, e->stream>>>(ty.kcols[0], ty.n, cv.kmin, nK, ty.khist);
+            gf_kscan<<<1, 1024, 0, e->stream>>>(ty.khist, nK, ty.koffs);
+            r = cudaGetLastError();
+        }
     }
-    const int grid = std::max(1, e->sm_count) * 2;
-    if(r == cudaSuccess)
-        r = cudaMemsetAsync(ty.khist, 0, sizeof(unsigned) * nK, e->stream);
     if(r == cudaSuccess) {
-        gf_khist<<<grid, 256, nK <= 8192 ? sizeof(unsigned) * nK : 0, e->stream>>>(ty.kcols[0], ty.n, cv.kmin, nK, ty.khist);
-        gf_kscan<<<1, 1024, 0, e->stream>>>(ty.khist, nK, ty.koffs);
         gf_kfill<<<nK, 256, 0, e->stream>>>(ty.koffs, nK, cv.kmin, ty.npad, ty.ksort);
         r = cudaGetLastError();
     }
@@ -553,7 +607,7 @@ int buildLayout(gf_engine *e) {
     if(r != cudaSuccess)
         return gf_cuda_check(e, r, "layout upload");
     if(e->plan.fused_tab && e->n_toys == 1 && e->use_ksort && !e->toys[0].ksort_valid)
-        if(int rk = buildKSort(e))
+        if(int rk = buildKSort(e, false))
             return rk;
     e->layout_ready = true;
     return GF_OK;
@@ -2025,6 +2079,19 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
     }
     a.err = derr;
     unsigned blocks = (unsigned)((npad + 255) / 256);
+    // the one-launch tabulated path sorts toy 0's events by bin offset: the conversion kernel builds the sort's
+    // histogram and run offsets on the way
+    const bool sorted = toy == 0 && e->n_toys == 1 && e->plan.fused_tab && e->use_ksort && NC > 0;
+    const bool histInConvert = sorted && blocks > 0 && n > 0;
+    if(histInConvert) {
+        const int nK = T.convs[0].nK;
+        if((r = ensureKHist(ty, nK)) != cudaSuccess ||
+           (r = cudaMemsetAsync(ty.khist, 0, sizeof(unsigned) * (nK + 1), e->stream)) != cudaSuccess)
+            return gf_cuda_check(e, r, "sort histogram");
+        a.khist = ty.khist;
+        a.koffs = ty.koffs;
+        a.k_nK  = nK;
+    }
     if(e->precision == GF_MIXED)
         gf_convert_events<float><<<blocks, 256, 0, e->stream>>>(a);
     else
@@ -2049,8 +2116,8 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
     if(herr)
         return gf_fail(e, GF_ERR_INVALID, "event outside the observable range of a ConvolutionPdf");
     ty.ksort_valid = false;
-    if(toy == 0 && e->n_toys == 1 && e->plan.fused_tab && e->use_ksort)
-        return buildKSort(e);
+    if(sorted)
+        return buildKSort(e, histInConvert);
     return GF_OK;
 }
 

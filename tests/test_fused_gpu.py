@@ -146,3 +146,33 @@ def test_mixed_fit_converges_as_the_fp64_fit(seed, monkeypatch):
     assert nm <= nf + 2, (nm, nf)
     assert fm_ == pytest.approx(ff, rel=1e-9)
     assert max(abs(a - b) / e for a, b, e in zip(vm, vf, ef)) < 0.01
+
+
+def test_sorted_events_match_upload_order_and_survive_reuploads(monkeypatch):
+    """The tabulated path's events sorted by bin offset (histogram and run offsets built by the upload's
+    conversion kernel, then the fill) against the same engine reading them in upload order, at sizes that leave
+    padding slots, and across uploads of other sizes into the same engine (the histogram scratch is reused)."""
+    eng = c2_engine(20_001, 41, "mixed", monkeypatch)[0]
+    monkeypatch.setenv("GF_KSORT", "0")
+    eng_u = c2_engine(20_001, 41, "mixed", monkeypatch)[0]
+    monkeypatch.delenv("GF_KSORT")
+    for n, seed in ((20_001, 41), (1_000_003, 42), (7_777, 43)):
+        wl = W.make_c2(n, seed=seed)
+        nodes, params, obs = wl.pdf._flatten()
+        olist = [(o.lowerlimit, o.upperlimit, o.numbins, int(o.is_event_number)) for o in obs]
+        pv = np.array([v.value for v in params])
+        data = wl.data.to_numpy()
+        eng.upload(data)
+        eng_u.upload(data)
+        for shift in (0.0, 0.05):
+            p = pv.copy()
+            p[[v.name for v in params].index("alpha")] += shift
+            got, g = eng.nll_grad(p)
+            got_u, g_u = eng_u.nll_grad(p)
+            # the counted sums are exact products of a bin's terms; the per-event loop adds 8 events' FP32 terms
+            # pairwise first (a rounding of 2^-24 of the group sum each), about 1e-9 relative over the data set
+            assert got == pytest.approx(got_u, rel=1e-8), (n, shift)
+            np.testing.assert_allclose(g, g_u, rtol=1e-6, atol=1e-5 * math.sqrt(n))
+            assert got == pytest.approx(O.nll(nodes, olist, p, data), rel=1e-6), (n, shift)
+    eng.close()
+    eng_u.close()
