@@ -41,11 +41,6 @@ struct ConvertArgs {
     int conv_kmin[8], conv_kmax[8];
     double pad_val[16];
     int *err;
-    // histogram of convolution 0's offsets for the sorted copy (null: none), its bins and the offsets of the
-    // sorted runs; khist[k_nK] counts the CTAs that finished
-    unsigned *khist;
-    long long *koffs;
-    int k_nK;
 };
 
 // offs[0..nK]: exclusive prefix sums of hist[0..nK) by one CTA (a power-of-two block of at most 1024 threads):
@@ -77,10 +72,9 @@ __device__ void gf_scan_runs(const unsigned *hist, int nK, long long *offs) {
 
 // FP64 SoA -> engine columns (FP32 or FP64) plus the ConvolutionPdf bin
 // offset of every event (src/PDFs/combine/ConvolutionPdf.cu:40-43, FP64),
-// which is all the convolution needs of x: one event (or padding slot) i, returning convolution 0's offset.
+// which is all the convolution needs of x: one event (or padding slot) i.
 template <typename R>
-__device__ __forceinline__ int gf_convert_one(const ConvertArgs &a, long long i) {
-    int k0 = 0;
+__device__ __forceinline__ void gf_convert_one(const ConvertArgs &a, long long i) {
     // every value is read once (the source may be page-locked host memory read over the interconnect),
     // all loads issued before the first store
     double xs[16];
@@ -117,39 +111,15 @@ __device__ __forceinline__ int gf_convert_one(const ConvertArgs &a, long long i)
         } else
             k = a.conv_kmin[c];
         a.kcols[c][i] = k;
-        if(c == 0)
-            k0 = k;
     }
-    return k0;
 }
 
-// One thread per event or padding slot. With a.khist set it also builds the histogram of convolution 0's offsets
-// (events only, not the padding) for the sorted copy of the one-launch tabulated path, hidden under the
-// interconnect-bound reads: one atomic per distinct offset in a warp, and the last CTA to finish turns the
-// histogram into the offsets of the sorted runs.
+// One thread per event or padding slot.
 template <typename R>
 __global__ void gf_convert_events(const ConvertArgs a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int k0 = i < a.npad ? gf_convert_one<R>(a, i) : 0;
-    if(a.khist) {
-        const bool counted  = i < a.n;
-        const unsigned part = __ballot_sync(0xffffffffu, counted);
-        if(counted) {
-            const unsigned same = __match_any_sync(part, k0);
-            if((int)(threadIdx.x & 31) == __ffs(same) - 1)
-                atomicAdd(a.khist + (k0 - a.conv_kmin[0]), (unsigned)__popc(same));
-        }
-        __shared__ bool last;
-        __threadfence();
-        __syncthreads();
-        if(threadIdx.x == 0)
-            last = atomicAdd(a.khist + a.k_nK, 1u) == gridDim.x - 1;
-        __syncthreads();
-        if(last) {
-            __threadfence();
-            gf_scan_runs(a.khist, a.k_nK, a.koffs);
-        }
-    }
+    if(i < a.npad)
+        gf_convert_one<R>(a, i);
 }
 
 size_t rsize(const gf_engine *e) { return e->precision == GF_MIXED ? 4 : 8; }
@@ -196,8 +166,7 @@ __global__ void gf_kfill(const long long *__restrict__ offs, int nK, int kmin, l
             out[i] = kmin;
 }
 
-// The sort's histogram (nK bins and a finished-CTA counter) and run offsets of toy 0, allocated on first use and
-// kept across uploads.
+// The sort's histogram and run offsets of toy 0, allocated on first use and kept across uploads.
 cudaError_t ensureKHist(GfToy &ty, int nK) {
     if(ty.khist_n >= nK)
         return cudaSuccess;
@@ -208,7 +177,7 @@ cudaError_t ensureKHist(GfToy &ty, int nK) {
     ty.khist      = nullptr;
     ty.koffs      = nullptr;
     ty.khist_n    = 0;
-    cudaError_t r = cudaMalloc((void **)&ty.khist, sizeof(unsigned) * (nK + 1));
+    cudaError_t r = cudaMalloc((void **)&ty.khist, sizeof(unsigned) * nK);
     if(r == cudaSuccess)
         r = cudaMalloc((void **)&ty.koffs, sizeof(long long) * (nK + 1));
     if(r == cudaSuccess)
@@ -218,9 +187,10 @@ cudaError_t ensureKHist(GfToy &ty, int nK) {
 
 // Sorted copy of toy 0's offsets of convolution 0: histogram, prefix sums and fill, all on the device and
 // asynchronous on the engine's stream (the upload's own range check has already rejected offsets outside the
-// table). histReady: the upload's conversion kernel has already built the histogram and the run offsets. The
-// sorted column is allocated on first use and kept across uploads of the same size.
-int buildKSort(gf_engine *e, bool histReady) {
+// table); the sorted column is allocated on first use and kept across uploads of the same size. (The histogram
+// built inside the conversion kernel instead, with warp-aggregated atomics and a last-CTA scan, made the 2e6-event
+// upload 2.5x slower.)
+int buildKSort(gf_engine *e) {
     GfToy &ty = e->toys[0];
     if(!ty.loaded || e->tree.convs.empty())
         return GF_OK;
@@ -229,19 +199,14 @@ int buildKSort(gf_engine *e, bool histReady) {
     cudaError_t r          = cudaSuccess;
     if(!ty.ksort)
         r = cudaMalloc((void **)&ty.ksort, sizeof(int) * (size_t)std::max<int64_t>(8, ty.npad));
-    if(!histReady) {
-        if(r == cudaSuccess)
-            r = ensureKHist(ty, nK);
-        const int grid = std::max(1, e->sm_count) * 2;
-        if(r == cudaSuccess)
-            r = cudaMemsetAsync(ty.khist, 0, sizeof(unsigned) * nK, e->stream);
-        if(r == cudaSuccess) {
-            gf_khist<<<grid, 256, nK <= 8192 ? sizeof(unsigned) * nK : 0, e->stream>>>(ty.kcols[0], ty.n, cv.kmin, nK, ty.khist);
-            gf_kscan<<<1, 1024, 0, e->stream>>>(ty.khist, nK, ty.koffs);
-            r = cudaGetLastError();
-        }
-    }
+    if(r == cudaSuccess)
+        r = ensureKHist(ty, nK);
+    const int grid = std::max(1, e->sm_count) * 2;
+    if(r == cudaSuccess)
+        r = cudaMemsetAsync(ty.khist, 0, sizeof(unsigned) * nK, e->stream);
     if(r == cudaSuccess) {
+        gf_khist<<<grid, 256, nK <= 8192 ? sizeof(unsigned) * nK : 0, e->stream>>>(ty.kcols[0], ty.n, cv.kmin, nK, ty.khist);
+        gf_kscan<<<1, 1024, 0, e->stream>>>(ty.khist, nK, ty.koffs);
         gf_kfill<<<nK, 256, 0, e->stream>>>(ty.koffs, nK, cv.kmin, ty.npad, ty.ksort);
         r = cudaGetLastError();
     }
@@ -607,7 +572,7 @@ int buildLayout(gf_engine *e) {
     if(r != cudaSuccess)
         return gf_cuda_check(e, r, "layout upload");
     if(e->plan.fused_tab && e->n_toys == 1 && e->use_ksort && !e->toys[0].ksort_valid)
-        if(int rk = buildKSort(e, false))
+        if(int rk = buildKSort(e))
             return rk;
     e->layout_ready = true;
     return GF_OK;
@@ -1682,6 +1647,12 @@ int gf_run(gf_engine *e, bool grad, int, int) {
         sum.assign(std::max(1, nc), 0.0);
         int st = 0;
         bool ended = false;
+        if(e->wait_sync) {
+            // GF_WAIT_SYNC=1: wait for the launch's end first (the rows are then all final or never written)
+            if((r = cudaStreamSynchronize(e->stream)) != cudaSuccess)
+                return gf_cuda_check(e, r, "evaluation");
+            ended = true;
+        }
         unsigned spins = 0;
         for(int c = 0; c < e->n_chunks;) {
             const uint64_t *row = reinterpret_cast<const uint64_t *>(e->h_fpart + (size_t)c * frow);
@@ -1788,6 +1759,8 @@ int gf_engine_create(gf_engine **out, int device, int precision) {
         e->use_graph = !(g[0] == '1');
     if(const char *d = std::getenv("GF_FUSED_DIRECT"))
         e->fused_direct = d[0] == '1';
+    if(const char *w = std::getenv("GF_WAIT_SYNC"))
+        e->wait_sync = w[0] == '1';
     if(const char *c = std::getenv("GF_CHUNK")) {
         e->chunk       = std::max(256, (atoi(c) / 256) * 256);
         e->chunk_fixed = true;
@@ -2079,19 +2052,8 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
     }
     a.err = derr;
     unsigned blocks = (unsigned)((npad + 255) / 256);
-    // the one-launch tabulated path sorts toy 0's events by bin offset: the conversion kernel builds the sort's
-    // histogram and run offsets on the way
+    // the one-launch tabulated path sorts toy 0's events by bin offset
     const bool sorted = toy == 0 && e->n_toys == 1 && e->plan.fused_tab && e->use_ksort && NC > 0;
-    const bool histInConvert = sorted && blocks > 0 && n > 0;
-    if(histInConvert) {
-        const int nK = T.convs[0].nK;
-        if((r = ensureKHist(ty, nK)) != cudaSuccess ||
-           (r = cudaMemsetAsync(ty.khist, 0, sizeof(unsigned) * (nK + 1), e->stream)) != cudaSuccess)
-            return gf_cuda_check(e, r, "sort histogram");
-        a.khist = ty.khist;
-        a.koffs = ty.koffs;
-        a.k_nK  = nK;
-    }
     if(e->precision == GF_MIXED)
         gf_convert_events<float><<<blocks, 256, 0, e->stream>>>(a);
     else
@@ -2117,7 +2079,7 @@ int gf_upload_events(gf_engine *e, int toy, const double *soa, int64_t n) {
         return gf_fail(e, GF_ERR_INVALID, "event outside the observable range of a ConvolutionPdf");
     ty.ksort_valid = false;
     if(sorted)
-        return buildKSort(e, histInConvert);
+        return buildKSort(e);
     return GF_OK;
 }
 

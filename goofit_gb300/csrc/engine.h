@@ -191,6 +191,7 @@ struct gf_engine {
     bool use_graph = true;
     bool fused_direct = false; // GF_FUSED_DIRECT=1: the one-launch kernel is launched directly, not replayed from a graph
     std::vector<double> fsum; // the host's sums of the one-launch rows
+    bool wait_sync = false;   // GF_WAIT_SYNC=1: the host synchronises the stream before it reads the one-launch rows
     bool use_pdl   = true;
     // one-launch evaluation (one toy, unbinned NLL): resident CTAs of the cooperative launch, the barrier
     // words it synchronises on and the longest barrier wait before it gives up (GF_FUSED=0: three launches)
