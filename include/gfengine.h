@@ -169,6 +169,9 @@ int gf_upload_events(gf_engine *eng, int toy, const double *soa, int64_t n_event
 
 /* ---- evaluation: FCN::operator() + GooPdf::calculateNLL ---- */
 int gf_set_params(gf_engine *eng, int toy, const double *params, int n_params);
+/* Returns once the result is on the host. In the one-launch form the engine's kernel may still be ending on
+ * the engine's stream at that point (its result rows are read as they arrive); later engine calls are ordered
+ * after it, and gf_last_timing waits for it. */
 int gf_nll(gf_engine *eng, int toy, double *nll);
 /* grad has one entry per parameter whose grad_mask is set, in parameter order */
 int gf_nll_grad(gf_engine *eng, int toy, double *nll, double *grad);
