@@ -1775,6 +1775,8 @@ struct Gen {
         sh.MS    = (!batch && maxComps <= block / 32) ? 32 : 8;
         // one toy: 4 entries per item tile, so that the table spreads over twice as many CTAs (its sums and lane
         // reductions halve per CTA; the launch has CTAs to spare, every one of which waits at the grid barrier)
+        // (3 entries per item tile, 251 table CTAs for C2's 1501 entries, so that fewer SMs run two table CTAs:
+        // the FCN took 19.1-19.3 us against 17.6-18.0 us at 4)
         sh.KT = batch ? 8 : 4;
         sh.items = block / sh.MS;
         // batches: each item covers KP k-tiles in turn, so that one CTA's staged model and resolution
