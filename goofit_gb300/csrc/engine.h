@@ -64,8 +64,7 @@ struct GfToy {
     int *kcols[8]  = {nullptr};
     int *ksort     = nullptr;           // one-launch tabulated path: the bin offsets of conv 0 sorted by bin
     bool ksort_valid = false;
-    unsigned *khist = nullptr;          // the sort's histogram (khist_n bins) and prefix sums (khist_n + 1)
-    long long *koffs = nullptr;
+    unsigned *khist = nullptr;          // the sort's histogram (khist_n bins)
     int khist_n      = 0;
     void *abase    = nullptr;           // cached resonance amplitudes and FP64 Dalitz columns (one allocation)
     void *acols[128] = {nullptr};       // R2 per event: amplitude columns, then derivative columns
