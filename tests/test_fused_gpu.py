@@ -176,3 +176,28 @@ def test_sorted_events_match_upload_order_and_survive_reuploads(monkeypatch):
             assert got == pytest.approx(O.nll(nodes, olist, p, data), rel=1e-6), (n, shift)
     eng.close()
     eng_u.close()
+
+
+def test_rows_read_as_they_arrive_equal_rows_read_after_the_launch(monkeypatch):
+    """The host adds the one-launch rows while the launch is still ending (each word checked against the unset
+    mark); with GF_WAIT_SYNC=1 it synchronises the stream first. Both read the same rows in the same order, so
+    the results are bit-identical, FCN after FCN (a fixed event chunk, so that both engines cut the events the
+    same way)."""
+    monkeypatch.setenv("GF_CHUNK", "2048")
+    eng, wl, nodes, olist, params, mask, pv = c2_engine(300_001, 51, "mixed", monkeypatch)
+    monkeypatch.setenv("GF_WAIT_SYNC", "1")
+    eng_s = c2_engine(300_001, 51, "mixed", monkeypatch)[0]
+    monkeypatch.delenv("GF_WAIT_SYNC")
+    names = [v.name for v in params]
+    for it in range(40):
+        p = pv.copy()
+        p[names.index("alpha")] += 0.002 * (it % 7)
+        p[names.index("sigma")] += 0.001 * (it % 5)
+        got, g = eng.nll_grad(p)
+        got_s, g_s = eng_s.nll_grad(p)
+        assert got == got_s, it
+        np.testing.assert_array_equal(g, g_s)
+        assert eng.nll(p) == eng_s.nll(p)
+    assert eng.last_timing()[0] > 0
+    eng.close()
+    eng_s.close()
